@@ -1,0 +1,300 @@
+"""CPU oracle for the lattice-Boltzmann hot path (test infrastructure only).
+
+This package is the checker: a plain-C restatement (``ludwig_oracle.c``) of
+the reference's algorithm, loaded through ctypes.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs import it; the
+product library never does.
+
+Array layout everywhere: interior sites only, periodic, component-major,
+z fastest, i.e. numpy shape ``(ncomp, Lx, Ly, Lz)``, C order, float64.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SHIM = os.path.join(REF_DIR, "ref_shim")
+
+NVEL = 19
+
+_lib = None
+
+
+def build(quiet=True):
+    """Compile the oracle shared library (gcc, -ffp-contract=off)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def build_reference(ref_root="/root/reference", jobs=8):
+    """Build the reference itself (serial+OpenMP) into oracle/_ref.
+
+    Only possible where the reference sources are present; used to pin the
+    oracle and to regenerate golden fixtures.
+    """
+    if not os.path.isdir(ref_root):
+        return False
+    out = subprocess.run(["make", "-f", os.path.join(HERE, "ref.mk"),
+                          "REF=" + ref_root, "-j%d" % jobs],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + out.stderr[-4000:])
+    return True
+
+
+class SymmParam(ctypes.Structure):
+    _fields_ = [("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("kappa", ctypes.c_double)]
+
+
+class CollideParam(ctypes.Structure):
+    _fields_ = [("rtau_shear", ctypes.c_double),
+                ("rtau_bulk", ctypes.c_double),
+                ("rtau_ghost", ctypes.c_double * NVEL),
+                ("force_global", ctypes.c_double * 3)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+_P = ctypes.POINTER(ctypes.c_double)
+_U8 = ctypes.POINTER(ctypes.c_uint8)
+_I3 = ctypes.c_int * 3
+
+
+def _declare(L):
+    L.orc_collide_param_m10.argtypes = [ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double,
+                                        ctypes.POINTER(CollideParam)]
+    L.orc_spinodal_init.argtypes = [_I3, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, _P]
+    L.orc_lb_init_rest.argtypes = [_I3, ctypes.c_double, _P]
+    L.orc_grad_7pt.argtypes = [_I3, ctypes.c_int, _P, _P, _P]
+    L.orc_symm_mu.argtypes = [_I3, ctypes.POINTER(SymmParam), _P, _P, _P]
+    L.orc_symm_stress.argtypes = [_I3, ctypes.POINTER(SymmParam), _P, _P, _P,
+                                  _P]
+    L.orc_force_divergence.argtypes = [_I3, _P, _P]
+    L.orc_advect_upwind.argtypes = [_I3, ctypes.c_int, _P, _P, _P, _P, _P, _P]
+    L.orc_ch_flux_mu.argtypes = [_I3, ctypes.POINTER(SymmParam),
+                                 ctypes.c_double, _P, _P, _P, _P, _P, _P]
+    L.orc_flux_no_normal.argtypes = [_I3, ctypes.c_int, _U8, _P, _P, _P, _P]
+    L.orc_ch_update.argtypes = [_I3, _P, _P, _P, _P, _P]
+    L.orc_collide_mrt.argtypes = [_I3, ctypes.POINTER(CollideParam), _U8, _P,
+                                  _P, _P, _P]
+    L.orc_propagate.argtypes = [_I3, _P, _P]
+    L.orc_binary_step.argtypes = [_I3, ctypes.POINTER(SymmParam),
+                                  ctypes.c_double,
+                                  ctypes.POINTER(CollideParam), _U8,
+                                  _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
+    L.orc_field_stats.argtypes = [_I3, _P, _P]
+    L.orc_symm_fed_total.argtypes = [_I3, ctypes.POINTER(SymmParam), _P, _P]
+    L.orc_symm_fed_total.restype = ctypes.c_double
+    for name in ("orc_ma", "orc_mi", "orc_wv"):
+        getattr(L, name).restype = _P
+    L.orc_cv.restype = ctypes.POINTER(ctypes.c_int8)
+
+
+def _p(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def _u8(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint8 and a.flags.c_contiguous
+    return a.ctypes.data_as(_U8)
+
+
+def _dims(L):
+    return _I3(*[int(v) for v in L])
+
+
+def tables():
+    """(cv[19,3], wv[19], ma[19,19], mi[19,19]) as used by the oracle."""
+    L = lib()
+    cv = np.ctypeslib.as_array(L.orc_cv(), shape=(NVEL * 3,)).reshape(NVEL, 3)
+    wv = np.ctypeslib.as_array(L.orc_wv(), shape=(NVEL,))
+    ma = np.ctypeslib.as_array(L.orc_ma(), shape=(NVEL * NVEL,))
+    mi = np.ctypeslib.as_array(L.orc_mi(), shape=(NVEL * NVEL,))
+    return (cv.copy(), wv.copy(), ma.reshape(NVEL, NVEL).copy(),
+            mi.reshape(NVEL, NVEL).copy())
+
+
+def collide_param_m10(eta, eta_bulk=None, rho0=1.0, force_global=(0, 0, 0)):
+    p = CollideParam()
+    lib().orc_collide_param_m10(float(eta), float(eta if eta_bulk is None
+                                                  else eta_bulk),
+                                float(rho0), ctypes.byref(p))
+    for i in range(3):
+        p.force_global[i] = float(force_global[i])
+    return p
+
+
+def symm_param(a, b, kappa):
+    return SymmParam(float(a), float(b), float(kappa))
+
+
+def spinodal_init(L, seed, phi0=0.0, amp=0.02):
+    phi = np.zeros((1,) + tuple(L))
+    lib().orc_spinodal_init(_dims(L), int(seed), float(phi0), float(amp),
+                            _p(phi))
+    return phi
+
+
+def lb_init_rest(L, rho0=1.0):
+    f = np.zeros((NVEL,) + tuple(L))
+    lib().orc_lb_init_rest(_dims(L), float(rho0), _p(f))
+    return f
+
+
+def grad_7pt(L, field):
+    field = np.ascontiguousarray(field, dtype=np.float64)
+    nf = field.shape[0]
+    grad = np.zeros((3 * nf,) + tuple(L))
+    delsq = np.zeros((nf,) + tuple(L))
+    lib().orc_grad_7pt(_dims(L), nf, _p(field), _p(grad), _p(delsq))
+    return grad, delsq
+
+
+def symm_stress(L, fe, phi, grad, delsq):
+    pth = np.zeros((9,) + tuple(L))
+    lib().orc_symm_stress(_dims(L), ctypes.byref(fe), _p(phi), _p(grad),
+                          _p(delsq), _p(pth))
+    return pth
+
+
+def symm_mu(L, fe, phi, delsq):
+    mu = np.zeros((1,) + tuple(L))
+    lib().orc_symm_mu(_dims(L), ctypes.byref(fe), _p(phi), _p(delsq), _p(mu))
+    return mu
+
+
+def force_divergence(L, pth, force=None):
+    if force is None:
+        force = np.zeros((3,) + tuple(L))
+    lib().orc_force_divergence(_dims(L), _p(pth), _p(force))
+    return force
+
+
+def phi_force(L, fe, phi):
+    """phi_force_calculation (stress divergence) on a zeroed force."""
+    grad, delsq = grad_7pt(L, phi)
+    pth = symm_stress(L, fe, phi, grad, delsq)
+    return force_divergence(L, pth)
+
+
+def cahn_hilliard(L, fe, mobility, phi, u, status=None):
+    """phi_cahn_hilliard: returns the updated phi (a copy)."""
+    phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    grad, delsq = grad_7pt(L, phi)
+    fw, fe_, fy, fz = (np.zeros((1,) + tuple(L)) for _ in range(4))
+    lib().orc_advect_upwind(_dims(L), 1, _p(phi), _p(u), _p(fw), _p(fe_),
+                            _p(fy), _p(fz))
+    lib().orc_ch_flux_mu(_dims(L), ctypes.byref(fe), float(mobility), _p(phi),
+                         _p(delsq), _p(fw), _p(fe_), _p(fy), _p(fz))
+    lib().orc_flux_no_normal(_dims(L), 1, _u8(status), _p(fw), _p(fe_),
+                             _p(fy), _p(fz))
+    lib().orc_ch_update(_dims(L), _p(fw), _p(fe_), _p(fy), _p(fz), _p(phi))
+    return phi
+
+
+def collide(L, cp, f, force, status=None):
+    """lb_collide (M10): returns (f, rho, u); f is a copy."""
+    f = np.ascontiguousarray(f, dtype=np.float64).copy()
+    force = np.ascontiguousarray(force, dtype=np.float64)
+    rho = np.zeros((1,) + tuple(L))
+    u = np.zeros((3,) + tuple(L))
+    lib().orc_collide_mrt(_dims(L), ctypes.byref(cp), _u8(status), _p(f),
+                          _p(force), _p(rho), _p(u))
+    return f, rho, u
+
+
+def propagate(L, f):
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    out = np.zeros_like(f)
+    lib().orc_propagate(_dims(L), _p(f), _p(out))
+    return out
+
+
+class BinaryState:
+    """Host state of the binary fluid: f, phi, u, rho, force."""
+
+    def __init__(self, L, f, phi, u=None):
+        self.L = tuple(int(v) for v in L)
+        n = self.L
+        self.f = np.ascontiguousarray(f, dtype=np.float64).copy()
+        self.phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
+        self.u = (np.zeros((3,) + n) if u is None else
+                  np.ascontiguousarray(u, dtype=np.float64).copy())
+        self.rho = np.zeros((1,) + n)
+        self.force = np.zeros((3,) + n)
+        self._fs = np.zeros_like(self.f)
+        self._work = np.zeros((13,) + n)
+
+
+def binary_steps(state, fe, mobility, cp, nsteps, status=None):
+    """Advance a BinaryState by nsteps of the reference main loop."""
+    s = state
+    lib().orc_binary_step(_dims(s.L), ctypes.byref(fe), float(mobility),
+                          ctypes.byref(cp), _u8(status), _p(s.f), _p(s._fs),
+                          _p(s.phi), _p(s.u), _p(s.rho), _p(s.force),
+                          _p(s._work), int(nsteps))
+    return s
+
+
+def field_stats(L, q):
+    out = np.zeros(5)
+    lib().orc_field_stats(_dims(L), _p(np.ascontiguousarray(q[0] if q.ndim == 4
+                                                           else q)), _p(out))
+    return out
+
+
+def symm_fed_total(L, fe, phi):
+    grad, _ = grad_7pt(L, phi)
+    return lib().orc_symm_fed_total(_dims(L), ctypes.byref(fe), _p(phi),
+                                    _p(grad))
+
+
+# ---------------------------------------------------------------------------
+# The reference itself (only where oracle/_ref was built from its sources)
+# ---------------------------------------------------------------------------
+
+def have_reference():
+    return os.path.exists(REF_SHIM)
+
+
+def write_arrays(prefix, **arrays):
+    for name, a in arrays.items():
+        np.ascontiguousarray(a, dtype=np.float64).tofile(
+            "%s_%s.bin" % (prefix, name))
+
+
+def read_array(prefix, name, shape):
+    return np.fromfile("%s_%s.bin" % (prefix, name)).reshape(shape)
+
+
+def run_reference(args, threads=1):
+    """Run oracle/_ref/ref_shim with key=value arguments."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    out = subprocess.run([REF_SHIM] + ["%s=%s" % kv for kv in args.items()],
+                         capture_output=True, text=True, env=env)
+    if out.returncode != 0:
+        raise RuntimeError("ref_shim failed: " + out.stderr[-2000:])
+    return out.stdout

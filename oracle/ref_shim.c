@@ -1,0 +1,346 @@
+/*****************************************************************************
+ *
+ *  ref_shim.c
+ *
+ *  Test infrastructure only.  A small driver linked against the
+ *  reference (Ludwig v0.23, built from its own sources by oracle/ref.mk)
+ *  that runs the reference's own hot-path functions on given inputs and
+ *  writes the results as raw little-endian doubles.  It pins the oracle
+ *  restatement (oracle/ludwig_oracle.c) and generates the golden fixtures
+ *  under tests/golden/.  Nothing in the product links against it.
+ *
+ *  File layout of every array: interior sites only, component-major,
+ *  z fastest:  a[(n*Lx + x)*Ly + y)*Lz + z]  with x,y,z 0-based.
+ *
+ *  Usage (key=value arguments):
+ *    ref_shim mode=run    size=X,Y,Z steps=N A= B= K= M= eta= seed= noise=
+ *                         phi0= out=PREFIX
+ *    ref_shim mode=collide  size=.. eta= in=PREFIX out=PREFIX
+ *    ref_shim mode=propagate size=.. in=PREFIX out=PREFIX
+ *    ref_shim mode=grad     size=.. in=PREFIX out=PREFIX       (nf from file)
+ *    ref_shim mode=force    size=.. A= B= K= in=PREFIX out=PREFIX
+ *    ref_shim mode=ch       size=.. A= B= K= M= in=PREFIX out=PREFIX
+ *    ref_shim mode=step     size=.. A= B= K= M= eta= steps= in=PREFIX out=PREFIX
+ *
+ *  The call sequence of mode=run/step follows src/ludwig.c:528-860 for
+ *  the symmetric free energy with finite-difference Cahn-Hilliard.
+ *
+ *****************************************************************************/
+
+#include <assert.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "pe.h"
+#include "coords.h"
+#include "physics.h"
+#include "leesedwards.h"
+#include "field.h"
+#include "field_grad.h"
+#include "gradient_3d_7pt_fluid.h"
+#include "symmetric.h"
+#include "phi_force.h"
+#include "phi_force_stress.h"
+#include "phi_cahn_hilliard.h"
+#include "hydro.h"
+#include "map.h"
+#include "lb_data.h"
+#include "collision.h"
+#include "propagation.h"
+#include "field_phi_init.h"
+#include "util_sum.h"
+#include "wall.h"
+
+static const char * arg(int argc, char ** argv, const char * key,
+			const char * def) {
+  size_t n = strlen(key);
+  for (int i = 1; i < argc; i++) {
+    if (strncmp(argv[i], key, n) == 0 && argv[i][n] == '=') return argv[i]+n+1;
+  }
+  return def;
+}
+
+static double argd(int argc, char ** argv, const char * key, double def) {
+  const char * s = arg(argc, argv, key, NULL);
+  return s ? atof(s) : def;
+}
+
+static int L[3];
+
+static size_t nint(void) { return (size_t) L[0]*L[1]*L[2]; }
+static size_t canon(int n, int x, int y, int z) {
+  return (((size_t) n*L[0] + x)*L[1] + y)*L[2] + z;
+}
+
+static double * readf(const char * prefix, const char * name, size_t n) {
+  char path[1024];
+  snprintf(path, sizeof(path), "%s_%s.bin", prefix, name);
+  FILE * fp = fopen(path, "rb");
+  if (fp == NULL) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+  double * a = malloc(n*sizeof(double));
+  if (fread(a, sizeof(double), n, fp) != n) {
+    fprintf(stderr, "short read %s\n", path); exit(2);
+  }
+  fclose(fp);
+  return a;
+}
+
+static void writef(const char * prefix, const char * name, const double * a,
+		   size_t n) {
+  char path[1024];
+  snprintf(path, sizeof(path), "%s_%s.bin", prefix, name);
+  FILE * fp = fopen(path, "wb");
+  if (fp == NULL) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+  fwrite(a, sizeof(double), n, fp);
+  fclose(fp);
+}
+
+/* Field <-> canonical copies (interior only) */
+
+static void field_get(cs_t * cs, field_t * f, double * out) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int n = 0; n < f->nf; n++)
+	out[canon(n,x,y,z)] = f->data[addr_rank1(f->nsites, f->nf, index, n)];
+    }
+}
+
+static void field_put(cs_t * cs, field_t * f, const double * in) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int n = 0; n < f->nf; n++)
+	f->data[addr_rank1(f->nsites, f->nf, index, n)] = in[canon(n,x,y,z)];
+    }
+}
+
+static void lb_get(cs_t * cs, lb_t * lb, double * out) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int p = 0; p < NVEL; p++)
+	out[canon(p,x,y,z)] = lb->f[LB_ADDR(lb->nsite, lb->ndist, NVEL,
+					     index, 0, p)];
+    }
+}
+
+static void lb_put(cs_t * cs, lb_t * lb, const double * in) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int p = 0; p < NVEL; p++)
+	lb->f[LB_ADDR(lb->nsite, lb->ndist, NVEL, index, 0, p)]
+	  = in[canon(p,x,y,z)];
+    }
+}
+
+typedef struct sys_s {
+  pe_t * pe;
+  cs_t * cs;
+  physics_t * phys;
+  lees_edw_t * le;
+  field_t * phi;
+  field_grad_t * dphi;
+  fe_symm_t * fe;
+  phi_ch_t * pch;
+  pth_t * pth;
+  hydro_t * hydro;
+  map_t * map;
+  lb_t * lb;
+  wall_t * wall;
+} sys_t;
+
+static void sys_create(int argc, char ** argv, sys_t * s) {
+
+  memset(s, 0, sizeof(*s));
+  pe_create(MPI_COMM_WORLD, PE_QUIET, &s->pe);
+  cs_create(s->pe, &s->cs);
+  cs_nhalo_set(s->cs, 2);
+  cs_ntotal_set(s->cs, L);
+  cs_init(s->cs);
+
+  physics_create(s->pe, &s->phys);
+  {
+    double eta = argd(argc, argv, "eta", 0.1);
+    physics_eta_shear_set(s->phys, eta);
+    physics_eta_bulk_set(s->phys, argd(argc, argv, "eta_bulk", eta));
+    physics_mobility_set(s->phys, argd(argc, argv, "M", 0.3));
+  }
+
+  {
+    lees_edw_options_t opts = {0};
+    lees_edw_create(s->pe, s->cs, &opts, &s->le);
+  }
+  {
+    field_options_t opts = field_options_ndata_nhalo(1, 2);
+    field_create(s->pe, s->cs, s->le, "phi", &opts, &s->phi);
+    field_grad_create(s->pe, s->phi, 2, &s->dphi);
+    field_grad_set(s->dphi, grad_3d_7pt_fluid_d2, NULL);
+  }
+  {
+    fe_symm_param_t p = {0};
+    p.a     = argd(argc, argv, "A", -0.0625);
+    p.b     = argd(argc, argv, "B", +0.0625);
+    p.kappa = argd(argc, argv, "K", 0.04);
+    fe_symm_create(s->pe, s->cs, s->phi, s->dphi, &s->fe);
+    fe_symm_param_set(s->fe, p);
+  }
+  {
+    phi_ch_info_t info = {.conserve = 0, .noise = 0};
+    phi_ch_create(s->pe, s->cs, s->le, &info, &s->pch);
+  }
+  pth_create(s->pe, s->cs, FE_FORCE_METHOD_STRESS_DIVERGENCE, &s->pth);
+  {
+    hydro_options_t opts = hydro_options_default();
+    hydro_create(s->pe, s->cs, s->le, &opts, &s->hydro);
+  }
+  {
+    map_options_t opts = map_options_default();
+    map_create(s->pe, s->cs, &opts, &s->map);
+  }
+  {
+    lb_data_options_t opts = lb_data_options_default();
+    lb_data_create(s->pe, s->cs, &opts, &s->lb);
+    lb_init_rest_f(s->lb, 1.0);
+  }
+  wall_create(s->pe, s->cs, s->map, s->lb, &s->wall);
+}
+
+/* One time step as src/ludwig.c:528-860 (symmetric, FD CH, no colloids). */
+
+static void sys_step(sys_t * s) {
+  double zero[3] = {0.0, 0.0, 0.0};
+  physics_control_next_step(s->phys);
+  hydro_f_zero(s->hydro, zero);
+  field_halo(s->phi);
+  field_grad_compute(s->dphi);
+  phi_force_calculation(s->pe, s->cs, s->le, s->wall, s->pth,
+			(fe_t *) s->fe, s->map, s->phi, s->hydro);
+  phi_cahn_hilliard(s->pch, (fe_t *) s->fe, s->phi, s->hydro, s->map, NULL);
+  hydro_u_zero(s->hydro, zero);
+  lb_collide(s->lb, s->hydro, s->map, NULL, (fe_t *) s->fe, NULL);
+  lb_halo(s->lb);
+  lb_propagation(s->lb);
+}
+
+static void sys_dump(sys_t * s, const char * out) {
+  size_t n = nint();
+  double * a = malloc(NVEL*n*sizeof(double));
+  field_get(s->cs, s->phi, a);           writef(out, "phi", a, n);
+  field_get(s->cs, s->hydro->u, a);      writef(out, "u", a, 3*n);
+  field_get(s->cs, s->hydro->rho, a);    writef(out, "rho", a, n);
+  field_get(s->cs, s->hydro->force, a);  writef(out, "force", a, 3*n);
+  lb_get(s->cs, s->lb, a);               writef(out, "f", a, NVEL*n);
+  free(a);
+}
+
+int main(int argc, char ** argv) {
+
+  const char * mode = arg(argc, argv, "mode", "run");
+  const char * in   = arg(argc, argv, "in", NULL);
+  const char * out  = arg(argc, argv, "out", "ref");
+  sys_t s;
+
+  MPI_Init(&argc, &argv);
+
+  if (sscanf(arg(argc, argv, "size", "8,8,8"), "%d,%d,%d",
+	     L, L+1, L+2) != 3) return 2;
+
+  sys_create(argc, argv, &s);
+
+  if (strcmp(mode, "run") == 0) {
+    int seed = atoi(arg(argc, argv, "seed", "13"));
+    double amp = argd(argc, argv, "noise", 0.02);
+    double phi0 = argd(argc, argv, "phi0", 0.0);
+    int steps = atoi(arg(argc, argv, "steps", "1"));
+    field_phi_init_spinodal(s.phi, seed, phi0, amp);
+    if (atoi(arg(argc, argv, "dump0", "0"))) {
+      char p0[1024];
+      snprintf(p0, sizeof(p0), "%s0", out);
+      sys_dump(&s, p0);
+    }
+    for (int n = 0; n < steps; n++) sys_step(&s);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "step") == 0) {
+    size_t n = nint();
+    double * phi = readf(in, "phi", n);
+    double * u   = readf(in, "u", 3*n);
+    double * f   = readf(in, "f", NVEL*n);
+    int steps = atoi(arg(argc, argv, "steps", "1"));
+    field_put(s.cs, s.phi, phi);
+    field_put(s.cs, s.hydro->u, u);
+    lb_put(s.cs, s.lb, f);
+    for (int k = 0; k < steps; k++) sys_step(&s);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "collide") == 0) {
+    size_t n = nint();
+    double * f = readf(in, "f", NVEL*n);
+    double * force = readf(in, "force", 3*n);
+    lb_put(s.cs, s.lb, f);
+    field_put(s.cs, s.hydro->force, force);
+    lb_collide(s.lb, s.hydro, s.map, NULL, (fe_t *) s.fe, NULL);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "propagate") == 0) {
+    size_t n = nint();
+    double * f = readf(in, "f", NVEL*n);
+    lb_put(s.cs, s.lb, f);
+    lb_halo(s.lb);
+    lb_propagation(s.lb);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "grad") == 0) {
+    size_t n = nint();
+    double * phi = readf(in, "phi", n);
+    double * g = malloc(3*n*sizeof(double));
+    double * d = malloc(n*sizeof(double));
+    field_put(s.cs, s.phi, phi);
+    field_halo(s.phi);
+    field_grad_compute(s.dphi);
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(s.cs, x+1, y+1, z+1);
+	for (int ia = 0; ia < 3; ia++)
+	  g[canon(ia,x,y,z)] = s.dphi->grad[addr_rank2(s.dphi->nsite, 1, 3,
+						       index, 0, ia)];
+	d[canon(0,x,y,z)] = s.dphi->delsq[addr_rank1(s.dphi->nsite, 1,
+						    index, 0)];
+      }
+    writef(out, "grad", g, 3*n);
+    writef(out, "delsq", d, n);
+  }
+  else if (strcmp(mode, "force") == 0) {
+    size_t n = nint();
+    double zero[3] = {0.0, 0.0, 0.0};
+    double * phi = readf(in, "phi", n);
+    field_put(s.cs, s.phi, phi);
+    hydro_f_zero(s.hydro, zero);
+    field_halo(s.phi);
+    field_grad_compute(s.dphi);
+    phi_force_calculation(s.pe, s.cs, s.le, s.wall, s.pth, (fe_t *) s.fe,
+			  s.map, s.phi, s.hydro);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "ch") == 0) {
+    size_t n = nint();
+    double * phi = readf(in, "phi", n);
+    double * u   = readf(in, "u", 3*n);
+    field_put(s.cs, s.phi, phi);
+    field_put(s.cs, s.hydro->u, u);
+    field_halo(s.phi);
+    field_grad_compute(s.dphi);
+    phi_cahn_hilliard(s.pch, (fe_t *) s.fe, s.phi, s.hydro, s.map, NULL);
+    sys_dump(&s, out);
+  }
+  else {
+    fprintf(stderr, "unknown mode %s\n", mode);
+    return 2;
+  }
+
+  MPI_Finalize();
+  return 0;
+}

@@ -1,0 +1,302 @@
+/*****************************************************************************
+ *
+ *  ludwig_gb.h
+ *
+ *  C ABI of libludwig_gb.so: the lattice-Boltzmann time step of Ludwig
+ *  (symmetric binary fluid and cholesteric liquid crystal) on one GB300.
+ *
+ *  The hot-path entry points keep the names, argument lists and meaning of
+ *  the reference functions they replace (cited per declaration as
+ *  path:line within the reference tree).  Objects are opaque handles that
+ *  own device memory; data stay resident on the device between calls.
+ *  Host arrays passed to the *_to_host / *_from_host functions use one
+ *  layout: interior sites only, component-major, z fastest,
+ *      a[((n*Lx + x)*Ly + y)*Lz + z],   x, y, z = 0 .. L-1.
+ *  Every function returns 0 on success or a LUDWIG_GB_E* code, with a
+ *  message from ludwig_gb_last_error().  Nothing traps on the device.
+ *  Calls are synchronous: results are complete when a call returns.
+ *
+ *  Types not supported on this path (noise with kT > 0, viscosity models,
+ *  walls, Lees-Edwards planes, colloids) are accepted as NULL only.
+ *
+ *****************************************************************************/
+
+#ifndef LUDWIG_GB_H
+#define LUDWIG_GB_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes */
+enum {
+  LUDWIG_GB_OK       = 0,
+  LUDWIG_GB_EINVAL   = 1,    /* invalid argument or unsupported option */
+  LUDWIG_GB_ENOMEM   = 2,    /* device or host allocation failed */
+  LUDWIG_GB_ECUDA    = 3,    /* CUDA runtime error */
+  LUDWIG_GB_ESTATE   = 4,    /* object in the wrong state for this call */
+  LUDWIG_GB_ETIMEOUT = 5,    /* a bounded device wait ran out */
+  LUDWIG_GB_ENOTFINITE = 6   /* NaN or Inf detected in a reduction */
+};
+
+const char * ludwig_gb_last_error(void);
+const char * ludwig_gb_version(void);
+
+/* Arithmetic and storage of a state */
+typedef enum ludwig_gb_prec_e {
+  LUDWIG_GB_FP64 = 0,        /* double; the drop-in, reference-exact */
+  LUDWIG_GB_FP32 = 1,        /* float; f stored as f - w_p rho0 */
+  LUDWIG_GB_FP16 = 2         /* float arithmetic; (f - w_p rho0)*scale as half */
+} ludwig_gb_prec_t;
+
+/* Opaque objects (names as in the reference) */
+typedef struct pe_s pe_t;
+typedef struct cs_s cs_t;
+typedef struct physics_s physics_t;
+typedef struct lb_data_s lb_t;
+typedef struct field_s field_t;
+typedef struct field_grad_s field_grad_t;
+typedef struct hydro_s hydro_t;
+typedef struct map_s map_t;
+typedef struct fe_s fe_t;
+typedef struct fe_symm_s fe_symm_t;
+typedef struct fe_lc_s fe_lc_t;
+typedef struct pth_s pth_t;
+typedef struct phi_ch_s phi_ch_t;
+typedef struct beris_edw_s beris_edw_t;
+typedef struct noise_s noise_t;              /* NULL only */
+typedef struct visc_s visc_t;                /* NULL only */
+typedef struct wall_s wall_t;                /* NULL only */
+typedef struct lees_edw_s lees_edw_t;        /* NULL only */
+typedef struct colloids_info_s colloids_info_t;  /* NULL only */
+
+/*---------------------------------------------------------------------------
+ * Parallel environment (one process, one GPU): src/pe.h:26-27
+ *-------------------------------------------------------------------------*/
+int pe_create(int device, pe_t ** ppe);
+int pe_free(pe_t * pe);
+
+/*---------------------------------------------------------------------------
+ * Coordinate system: src/coords.h:73-84.  Periodic in all directions.
+ * nhalo is recorded for layout conversions; device arrays hold no halo.
+ *-------------------------------------------------------------------------*/
+int cs_create(pe_t * pe, cs_t ** pcs);
+int cs_free(cs_t * cs);
+int cs_ntotal_set(cs_t * cs, const int ntotal[3]);
+int cs_nhalo_set(cs_t * cs, int nhalo);
+int cs_init(cs_t * cs);
+int cs_nlocal(cs_t * cs, int nlocal[3]);
+
+/*---------------------------------------------------------------------------
+ * Physical parameters: src/physics.h:20-37.  As in the reference, the most
+ * recently created object is the one the collision and Cahn-Hilliard
+ * stages read (physics_ref, src/physics.c:76).
+ *-------------------------------------------------------------------------*/
+int physics_create(pe_t * pe, physics_t ** phys);
+int physics_free(physics_t * phys);
+int physics_rho0_set(physics_t * phys, double rho0);
+int physics_eta_shear_set(physics_t * phys, double eta);
+int physics_eta_bulk_set(physics_t * phys, double zeta);
+int physics_mobility_set(physics_t * phys, double mobility);
+int physics_fbody_set(physics_t * phys, const double f[3]);
+int physics_ref(physics_t ** ref);
+
+/*---------------------------------------------------------------------------
+ * Distributions: src/lb_data.h:30-47,162-171 (D3Q19, ndist = 1)
+ *-------------------------------------------------------------------------*/
+typedef enum {LB_RELAXATION_M10, LB_RELAXATION_BGK, LB_RELAXATION_TRT}
+  lb_relaxation_enum_t;
+
+typedef struct lb_data_options_s {
+  int ndim;                      /* 3 */
+  int nvel;                      /* 19 */
+  int ndist;                     /* 1 */
+  lb_relaxation_enum_t nrelax;   /* default M10 */
+  int precision;                 /* ludwig_gb_prec_t; default FP64 */
+  double fp16_scale;             /* FP16 storage scale; 0 = default 1024 */
+} lb_data_options_t;
+
+lb_data_options_t lb_data_options_default(void);
+int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
+		   lb_t ** lb);
+int lb_free(lb_t * lb);
+int lb_init_rest_f(lb_t * lb, double rho0);                /* lb_data.c:659 */
+int lb_halo(lb_t * lb);                                     /* lb_data.c:754 */
+int lb_f_to_host(lb_t * lb, double * f);       /* 19 x nsites, reference f */
+int lb_f_from_host(lb_t * lb, const double * f);
+
+/* src/collision.h:27, src/collision.c:143 */
+int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
+	       fe_t * fe, visc_t * visc);
+/* src/propagation.h:21, src/propagation.c:43 */
+int lb_propagation(lb_t * lb);
+
+/*---------------------------------------------------------------------------
+ * Fields: src/field.h:97-119, src/field_options.h
+ *-------------------------------------------------------------------------*/
+typedef struct field_options_s {
+  int ndata;                     /* components: 1 (phi) or 5 (Q) */
+  int nhcomm;                    /* halo width requested (recorded) */
+  int precision;                 /* ludwig_gb_prec_t */
+} field_options_t;
+
+field_options_t field_options_ndata_nhalo(int ndata, int nhalo);
+int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
+		 const field_options_t * opts, field_t ** pobj);
+int field_free(field_t * obj);
+int field_nf(field_t * obj, int * nf);
+int field_halo(field_t * obj);                              /* field.c:371 */
+int field_to_host(field_t * obj, double * data);
+int field_from_host(field_t * obj, const double * data);
+int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp);
+                                                    /* field_phi_init.c:484 */
+
+/*---------------------------------------------------------------------------
+ * Gradients: src/field_grad.h:44-50 (3d_7pt_fluid stencil)
+ *-------------------------------------------------------------------------*/
+int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p);
+int field_grad_free(field_grad_t * obj);
+/* src/field_grad.c:319 -> src/gradient_3d_7pt_fluid.c:231 */
+int field_grad_compute(field_grad_t * obj);
+/* grad: 3*nf x nsites ([n][ia]), delsq: nf x nsites */
+int field_grad_to_host(field_grad_t * obj, double * grad, double * delsq);
+
+/*---------------------------------------------------------------------------
+ * Hydrodynamic fields: src/hydro.h:28-61
+ *-------------------------------------------------------------------------*/
+typedef struct hydro_options_s {
+  int nhcomm;
+  int precision;
+} hydro_options_t;
+
+hydro_options_t hydro_options_default(void);
+int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		 const hydro_options_t * opts, hydro_t ** pobj);
+int hydro_free(hydro_t * obj);
+int hydro_f_zero(hydro_t * obj, const double fzero[3]);    /* hydro.c:244 */
+int hydro_u_zero(hydro_t * obj, const double uzero[3]);    /* hydro.c:217 */
+int hydro_u_halo(hydro_t * obj);                            /* hydro.c:185 */
+int hydro_to_host(hydro_t * obj, double * rho, double * u, double * force);
+int hydro_from_host(hydro_t * obj, const double * rho, const double * u,
+		    const double * force);
+
+/*---------------------------------------------------------------------------
+ * Site status map: src/map.h:26-63 (MAP_FLUID = 0)
+ *-------------------------------------------------------------------------*/
+enum map_status {MAP_FLUID, MAP_BOUNDARY, MAP_COLLOID, MAP_STATUS_MAX};
+int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj);
+int map_free(map_t * obj);
+int map_status_from_host(map_t * obj, const uint8_t * status);
+
+/*---------------------------------------------------------------------------
+ * Free energy: the fe_t interface of src/free_energy.h:54-80
+ *-------------------------------------------------------------------------*/
+typedef enum fe_id_enum {FE_SYMMETRIC = 1, FE_LC = 2} fe_id_enum_t;
+
+typedef int  (* fe_free_ft)(fe_t * fe);
+typedef int  (* fe_target_ft)(fe_t * fe, fe_t ** target);
+typedef int  (* fe_fed_ft)(fe_t * fe, int index, double * fed);
+typedef int  (* fe_mu_ft)(fe_t * fe, int index, double * mu);
+typedef int  (* fe_str_ft)(fe_t * fe, int index, double s[3][3]);
+typedef int  (* fe_htensor_ft)(fe_t * fe, int index, double h[3][3]);
+
+typedef struct fe_vt_s {
+  fe_free_ft    free;
+  fe_target_ft  target;
+  fe_fed_ft     fed;          /* free energy density at site index */
+  fe_mu_ft      mu;           /* chemical potential (symmetric) */
+  fe_str_ft     stress;       /* full chemical stress */
+  fe_str_ft     str_symm;     /* symmetric part */
+  fe_str_ft     str_anti;     /* antisymmetric part (NULL if none) */
+  fe_htensor_ft htensor;      /* molecular field (LC), else NULL */
+} fe_vt_t;
+
+struct fe_s {
+  fe_id_enum_t id;
+  int use_stress_relaxation;
+  const fe_vt_t * func;
+};
+
+/* index = ((x*Ly + y)*Lz + z) of an interior site (0-based) */
+
+/* src/symmetric.h:38-51 */
+typedef struct fe_symm_param_s {
+  double a;
+  double b;
+  double kappa;
+  double c;
+  double h;
+} fe_symm_param_t;
+
+int fe_symm_create(pe_t * pe, cs_t * cs, field_t * phi, field_grad_t * dphi,
+		   fe_symm_t ** p);
+int fe_symm_free(fe_symm_t * fe);
+int fe_symm_param_set(fe_symm_t * fe, fe_symm_param_t values);
+int fe_symm_param(fe_symm_t * fe, fe_symm_param_t * values);
+
+/*---------------------------------------------------------------------------
+ * Force from the free energy: src/phi_force_stress.h:36-39,
+ * src/phi_force.h:24 (stress divergence, fluid only)
+ *-------------------------------------------------------------------------*/
+enum {FE_FORCE_METHOD_NO_FORCE = 0, FE_FORCE_METHOD_STRESS_DIVERGENCE = 1};
+int pth_create(pe_t * pe, cs_t * cs, int method, pth_t ** pth);
+int pth_free(pth_t * pth);
+int pth_stress_compute(pth_t * pth, fe_t * fe);   /* phi_force_stress.c:171 */
+int pth_to_host(pth_t * pth, double * str);        /* 9 x nsites */
+int phi_force_calculation(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			  wall_t * wall, pth_t * pth, fe_t * fe, map_t * map,
+			  field_t * phi, hydro_t * hydro);
+
+/*---------------------------------------------------------------------------
+ * Cahn-Hilliard finite-difference update: src/phi_cahn_hilliard.h:35-56
+ *-------------------------------------------------------------------------*/
+typedef struct phi_ch_info_s {
+  int conserve;                  /* 0 only */
+  int noise;                     /* 0 only */
+} phi_ch_info_t;
+
+int phi_ch_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		  const phi_ch_info_t * info, phi_ch_t ** pch);
+int phi_ch_free(phi_ch_t * pch);
+int phi_cahn_hilliard(phi_ch_t * pch, fe_t * fe, field_t * phi,
+		      hydro_t * hydro, map_t * map, noise_t * noise);
+
+/*---------------------------------------------------------------------------
+ * Fused GB300 step.  One call performs nsteps iterations of the main loop
+ * of src/ludwig.c:528-860 for the symmetric binary fluid (field gradients,
+ * stress-divergence force, Cahn-Hilliard update, collision, streaming),
+ * one kernel launch per step, replayed from a CUDA graph.  For FP64
+ * objects the results equal those of calling the functions above one by
+ * one.  hydro's force is not stored by the fused step.
+ *-------------------------------------------------------------------------*/
+int ludwig_gb_binary_step(lb_t * lb, field_t * phi, hydro_t * hydro,
+			  map_t * map, fe_t * fe, int nsteps);
+/* As above without synchronising: the steps are queued on the library's
+ * stream; ludwig_gb_sync() waits for them. */
+int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				map_t * map, fe_t * fe, int nsteps);
+int ludwig_gb_sync(void);
+/* The CUDA stream (cudaStream_t) every launch of the library uses. */
+void * ludwig_gb_stream(void);
+/* Tuning of the fused kernel: planes per x chunk and tile height. */
+int ludwig_gb_tune_set(int xchunk, int tile_y);
+
+/*---------------------------------------------------------------------------
+ * Statistics (FP64 accumulation, compensated), src/phi_stats.c:91-140,
+ * src/stats_distribution.c:55-120, src/stats_free_energy.c:38
+ *-------------------------------------------------------------------------*/
+/* out = {total, mean, variance, min, max} of component n */
+int stats_field_q(field_t * field, int n, double out[5]);
+/* out = {total mass, momentum x, y, z} from the distributions */
+int stats_distribution(lb_t * lb, double out[4]);
+/* total symmetric free energy (bulk + gradient) */
+int stats_free_energy_symm(fe_symm_t * fe, double * total);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

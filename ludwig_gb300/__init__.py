@@ -1,0 +1,531 @@
+"""ludwig_gb300: the Ludwig lattice-Boltzmann time step on one GB300.
+
+Python mirror of the C ABI in ``include/ludwig_gb.h`` (ctypes over the
+in-tree ``libludwig_gb.so``).  Objects carry the reference's names
+(``cs_t`` -> :class:`Coords`, ``lb_t`` -> :class:`LB`, ``field_t`` ->
+:class:`Field`, ...) and their methods call the C entry points of the same
+name.  There is no CPU fallback: if the CUDA library is missing or no GPU is
+visible, loading fails with an error.
+
+Host arrays use the layout of the C ABI: numpy float64, shape
+``(ncomp, Lx, Ly, Lz)``, C order.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libludwig_gb.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "ludwig_gb.h")
+
+FP64, FP32, FP16 = 0, 1, 2
+NVEL = 19
+
+_lib = None
+
+
+class LudwigGBError(RuntimeError):
+    pass
+
+
+def build(verbose=False, force=False):
+    from . import buildlib
+    return buildlib.build(verbose=verbose, force=force)
+
+
+def load_library(path=LIB_PATH):
+    """Load libludwig_gb.so (no GPU needed to load)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise LudwigGBError(
+                "libludwig_gb.so is not built (run ludwig_gb300.build())")
+        _lib = ctypes.CDLL(path)
+        _declare(_lib)
+    return _lib
+
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I3 = ctypes.c_int * 3
+_D3 = ctypes.c_double * 3
+
+
+class LbDataOptions(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int), ("nvel", ctypes.c_int),
+                ("ndist", ctypes.c_int), ("nrelax", ctypes.c_int),
+                ("precision", ctypes.c_int), ("fp16_scale", ctypes.c_double)]
+
+
+class FieldOptions(ctypes.Structure):
+    _fields_ = [("ndata", ctypes.c_int), ("nhcomm", ctypes.c_int),
+                ("precision", ctypes.c_int)]
+
+
+class HydroOptions(ctypes.Structure):
+    _fields_ = [("nhcomm", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+class FeSymmParam(ctypes.Structure):
+    _fields_ = [("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("kappa", ctypes.c_double), ("c", ctypes.c_double),
+                ("h", ctypes.c_double)]
+
+
+class PhiChInfo(ctypes.Structure):
+    _fields_ = [("conserve", ctypes.c_int), ("noise", ctypes.c_int)]
+
+
+def _declare(L):
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "ludwig_gb_last_error": ([], ctypes.c_char_p),
+        "ludwig_gb_version": ([], ctypes.c_char_p),
+        "ludwig_gb_stream": ([], _P),
+        "ludwig_gb_sync": ([], ctypes.c_int),
+        "ludwig_gb_tune_set": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "pe_create": ([ctypes.c_int, pp], ctypes.c_int),
+        "pe_free": ([_P], ctypes.c_int),
+        "cs_create": ([_P, pp], ctypes.c_int),
+        "cs_free": ([_P], ctypes.c_int),
+        "cs_ntotal_set": ([_P, _I3], ctypes.c_int),
+        "cs_nhalo_set": ([_P, ctypes.c_int], ctypes.c_int),
+        "cs_init": ([_P], ctypes.c_int),
+        "physics_create": ([_P, pp], ctypes.c_int),
+        "physics_free": ([_P], ctypes.c_int),
+        "physics_rho0_set": ([_P, ctypes.c_double], ctypes.c_int),
+        "physics_eta_shear_set": ([_P, ctypes.c_double], ctypes.c_int),
+        "physics_eta_bulk_set": ([_P, ctypes.c_double], ctypes.c_int),
+        "physics_mobility_set": ([_P, ctypes.c_double], ctypes.c_int),
+        "physics_fbody_set": ([_P, _D3], ctypes.c_int),
+        "lb_data_create": ([_P, _P, ctypes.POINTER(LbDataOptions), pp],
+                           ctypes.c_int),
+        "lb_free": ([_P], ctypes.c_int),
+        "lb_init_rest_f": ([_P, ctypes.c_double], ctypes.c_int),
+        "lb_halo": ([_P], ctypes.c_int),
+        "lb_f_to_host": ([_P, _D], ctypes.c_int),
+        "lb_f_from_host": ([_P, _D], ctypes.c_int),
+        "lb_collide": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+        "lb_propagation": ([_P], ctypes.c_int),
+        "field_create": ([_P, _P, _P, ctypes.c_char_p,
+                          ctypes.POINTER(FieldOptions), pp], ctypes.c_int),
+        "field_free": ([_P], ctypes.c_int),
+        "field_halo": ([_P], ctypes.c_int),
+        "field_to_host": ([_P, _D], ctypes.c_int),
+        "field_from_host": ([_P, _D], ctypes.c_int),
+        "field_phi_init_spinodal": ([_P, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double], ctypes.c_int),
+        "field_grad_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
+        "field_grad_free": ([_P], ctypes.c_int),
+        "field_grad_compute": ([_P], ctypes.c_int),
+        "field_grad_to_host": ([_P, _D, _D], ctypes.c_int),
+        "hydro_create": ([_P, _P, _P, ctypes.POINTER(HydroOptions), pp],
+                         ctypes.c_int),
+        "hydro_free": ([_P], ctypes.c_int),
+        "hydro_f_zero": ([_P, _D3], ctypes.c_int),
+        "hydro_u_zero": ([_P, _D3], ctypes.c_int),
+        "hydro_u_halo": ([_P], ctypes.c_int),
+        "hydro_to_host": ([_P, _D, _D, _D], ctypes.c_int),
+        "hydro_from_host": ([_P, _D, _D, _D], ctypes.c_int),
+        "map_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
+        "map_free": ([_P], ctypes.c_int),
+        "map_status_from_host": ([_P, ctypes.POINTER(ctypes.c_uint8)],
+                                 ctypes.c_int),
+        "fe_symm_create": ([_P, _P, _P, _P, pp], ctypes.c_int),
+        "fe_symm_free": ([_P], ctypes.c_int),
+        "fe_symm_param_set": ([_P, FeSymmParam], ctypes.c_int),
+        "pth_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
+        "pth_free": ([_P], ctypes.c_int),
+        "pth_stress_compute": ([_P, _P], ctypes.c_int),
+        "pth_to_host": ([_P, _D], ctypes.c_int),
+        "phi_force_calculation": ([_P] * 9, ctypes.c_int),
+        "phi_ch_create": ([_P, _P, _P, ctypes.POINTER(PhiChInfo), pp],
+                          ctypes.c_int),
+        "phi_ch_free": ([_P], ctypes.c_int),
+        "phi_cahn_hilliard": ([_P] * 6, ctypes.c_int),
+        "ludwig_gb_binary_step": ([_P] * 5 + [ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_binary_step_async": ([_P] * 5 + [ctypes.c_int],
+                                        ctypes.c_int),
+        "stats_field_q": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "stats_distribution": ([_P, _D], ctypes.c_int),
+        "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+
+
+def lib():
+    return load_library()
+
+
+def _check(rc, what=""):
+    if rc != 0:
+        msg = lib().ludwig_gb_last_error().decode()
+        raise LudwigGBError("%s failed (code %d): %s" % (what, rc, msg))
+
+
+def _new(fn, *args):
+    out = ctypes.c_void_p()
+    _check(getattr(lib(), fn)(*args, ctypes.byref(out)), fn)
+    return out
+
+
+def _dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_D)
+
+
+# ---------------------------------------------------------------------------
+# Objects
+# ---------------------------------------------------------------------------
+
+class _Obj:
+    _free = None
+
+    def __init__(self):
+        self.ptr = None
+
+    def close(self):
+        if self.ptr is not None and self._free is not None:
+            getattr(lib(), self._free)(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PE(_Obj):
+    _free = "pe_free"
+
+    def __init__(self, device=0):
+        super().__init__()
+        self.ptr = _new("pe_create", int(device))
+
+
+class Coords(_Obj):
+    """cs_t: periodic lattice of ntotal sites (src/coords.c)."""
+    _free = "cs_free"
+
+    def __init__(self, pe, ntotal, nhalo=2):
+        super().__init__()
+        self.pe = pe
+        self.ntotal = tuple(int(v) for v in ntotal)
+        self.ptr = _new("cs_create", pe.ptr)
+        _check(lib().cs_ntotal_set(self.ptr, _I3(*self.ntotal)),
+               "cs_ntotal_set")
+        _check(lib().cs_nhalo_set(self.ptr, int(nhalo)), "cs_nhalo_set")
+        _check(lib().cs_init(self.ptr), "cs_init")
+
+    @property
+    def nsites(self):
+        return int(np.prod(self.ntotal))
+
+
+class Physics(_Obj):
+    _free = "physics_free"
+
+    def __init__(self, pe, rho0=1.0, eta=1.0 / 6.0, eta_bulk=None,
+                 mobility=0.0, fbody=(0.0, 0.0, 0.0)):
+        super().__init__()
+        self.ptr = _new("physics_create", pe.ptr)
+        L = lib()
+        _check(L.physics_rho0_set(self.ptr, float(rho0)), "rho0")
+        _check(L.physics_eta_shear_set(self.ptr, float(eta)), "eta")
+        _check(L.physics_eta_bulk_set(self.ptr, float(eta if eta_bulk is None
+                                                      else eta_bulk)), "zeta")
+        _check(L.physics_mobility_set(self.ptr, float(mobility)), "mobility")
+        _check(L.physics_fbody_set(self.ptr, _D3(*fbody)), "fbody")
+
+
+class LB(_Obj):
+    """lb_t: D3Q19 distributions (src/lb_data.c)."""
+    _free = "lb_free"
+
+    def __init__(self, cs, precision=FP64, nrelax=0, fp16_scale=0.0):
+        super().__init__()
+        self.cs = cs
+        self.precision = precision
+        o = LbDataOptions(3, 19, 1, int(nrelax), int(precision),
+                          float(fp16_scale))
+        self.ptr = _new("lb_data_create", cs.pe.ptr, cs.ptr, ctypes.byref(o))
+
+    def init_rest(self, rho0=1.0):
+        _check(lib().lb_init_rest_f(self.ptr, float(rho0)), "lb_init_rest_f")
+
+    def get(self):
+        f = np.zeros((NVEL,) + self.cs.ntotal)
+        _check(lib().lb_f_to_host(self.ptr, _dp(f)), "lb_f_to_host")
+        return f
+
+    def set(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        assert f.shape == (NVEL,) + self.cs.ntotal
+        _check(lib().lb_f_from_host(self.ptr, _dp(f)), "lb_f_from_host")
+
+    def collide(self, hydro, map_=None, fe=None):
+        _check(lib().lb_collide(self.ptr, hydro.ptr,
+                                map_.ptr if map_ else None, None,
+                                fe.ptr if fe else None, None), "lb_collide")
+
+    def halo(self):
+        _check(lib().lb_halo(self.ptr), "lb_halo")
+
+    def propagation(self):
+        _check(lib().lb_propagation(self.ptr), "lb_propagation")
+
+    def moments(self):
+        out = np.zeros(4)
+        _check(lib().stats_distribution(self.ptr, _dp(out)),
+               "stats_distribution")
+        return out
+
+
+class Field(_Obj):
+    """field_t: nf-component site field (src/field.c)."""
+    _free = "field_free"
+
+    def __init__(self, cs, nf=1, nhalo=2, precision=FP64, name="phi"):
+        super().__init__()
+        self.cs = cs
+        self.nf = nf
+        o = FieldOptions(int(nf), int(nhalo), int(precision))
+        self.ptr = _new("field_create", cs.pe.ptr, cs.ptr, None,
+                        name.encode(), ctypes.byref(o))
+
+    def get(self):
+        a = np.zeros((self.nf,) + self.cs.ntotal)
+        _check(lib().field_to_host(self.ptr, _dp(a)), "field_to_host")
+        return a
+
+    def set(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.shape == (self.nf,) + self.cs.ntotal
+        _check(lib().field_from_host(self.ptr, _dp(a)), "field_from_host")
+
+    def halo(self):
+        _check(lib().field_halo(self.ptr), "field_halo")
+
+    def init_spinodal(self, seed, phi0=0.0, amp=0.02):
+        _check(lib().field_phi_init_spinodal(self.ptr, int(seed), float(phi0),
+                                             float(amp)), "spinodal")
+
+    def stats(self, n=0):
+        out = np.zeros(5)
+        _check(lib().stats_field_q(self.ptr, int(n), _dp(out)),
+               "stats_field_q")
+        return out
+
+
+class FieldGrad(_Obj):
+    _free = "field_grad_free"
+
+    def __init__(self, field, level=2):
+        super().__init__()
+        self.field = field
+        self.ptr = _new("field_grad_create", field.cs.pe.ptr, field.ptr,
+                        int(level))
+
+    def compute(self):
+        _check(lib().field_grad_compute(self.ptr), "field_grad_compute")
+
+    def get(self):
+        nf = self.field.nf
+        g = np.zeros((3 * nf,) + self.field.cs.ntotal)
+        d = np.zeros((nf,) + self.field.cs.ntotal)
+        _check(lib().field_grad_to_host(self.ptr, _dp(g), _dp(d)),
+               "field_grad_to_host")
+        return g, d
+
+
+class Hydro(_Obj):
+    _free = "hydro_free"
+
+    def __init__(self, cs, precision=FP64):
+        super().__init__()
+        self.cs = cs
+        o = HydroOptions(1, int(precision))
+        self.ptr = _new("hydro_create", cs.pe.ptr, cs.ptr, None,
+                        ctypes.byref(o))
+
+    def get(self):
+        n = self.cs.ntotal
+        rho, u, force = (np.zeros((1,) + n), np.zeros((3,) + n),
+                         np.zeros((3,) + n))
+        _check(lib().hydro_to_host(self.ptr, _dp(rho), _dp(u), _dp(force)),
+               "hydro_to_host")
+        return rho, u, force
+
+    def set(self, rho=None, u=None, force=None):
+        args = []
+        for a in (rho, u, force):
+            if a is None:
+                args.append(None)
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                args.append(a)
+        _check(lib().hydro_from_host(self.ptr, *[None if a is None else _dp(a)
+                                                 for a in args]),
+               "hydro_from_host")
+
+    def f_zero(self):
+        _check(lib().hydro_f_zero(self.ptr, _D3(0.0, 0.0, 0.0)),
+               "hydro_f_zero")
+
+    def u_zero(self):
+        _check(lib().hydro_u_zero(self.ptr, _D3(0.0, 0.0, 0.0)),
+               "hydro_u_zero")
+
+    def u_halo(self):
+        _check(lib().hydro_u_halo(self.ptr), "hydro_u_halo")
+
+
+class Map(_Obj):
+    _free = "map_free"
+
+    def __init__(self, cs):
+        super().__init__()
+        self.cs = cs
+        self.ptr = _new("map_create", cs.pe.ptr, cs.ptr, 0)
+
+    def set_status(self, status):
+        s = np.ascontiguousarray(status, dtype=np.uint8)
+        assert s.size == self.cs.nsites
+        _check(lib().map_status_from_host(
+            self.ptr, s.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+            "map_status_from_host")
+
+
+class FeSymm(_Obj):
+    _free = "fe_symm_free"
+
+    def __init__(self, cs, phi, dphi, a=-0.0625, b=0.0625, kappa=0.04):
+        super().__init__()
+        self.ptr = _new("fe_symm_create", cs.pe.ptr, cs.ptr, phi.ptr,
+                        dphi.ptr)
+        _check(lib().fe_symm_param_set(self.ptr, FeSymmParam(a, b, kappa,
+                                                             0.0, 0.0)),
+               "fe_symm_param_set")
+
+    def fed_total(self):
+        out = ctypes.c_double()
+        _check(lib().stats_free_energy_symm(self.ptr, ctypes.byref(out)),
+               "stats_free_energy_symm")
+        return out.value
+
+
+class Pth(_Obj):
+    _free = "pth_free"
+
+    def __init__(self, cs, method=1):
+        super().__init__()
+        self.cs = cs
+        self.ptr = _new("pth_create", cs.pe.ptr, cs.ptr, int(method))
+
+    def stress_compute(self, fe):
+        _check(lib().pth_stress_compute(self.ptr, fe.ptr),
+               "pth_stress_compute")
+
+    def get(self):
+        s = np.zeros((9,) + self.cs.ntotal)
+        _check(lib().pth_to_host(self.ptr, _dp(s)), "pth_to_host")
+        return s
+
+
+class PhiCH(_Obj):
+    _free = "phi_ch_free"
+
+    def __init__(self, cs):
+        super().__init__()
+        info = PhiChInfo(0, 0)
+        self.ptr = _new("phi_ch_create", cs.pe.ptr, cs.ptr, None,
+                        ctypes.byref(info))
+
+
+# ---------------------------------------------------------------------------
+# The reference's main loop (src/ludwig.c:528-860) for the binary fluid
+# ---------------------------------------------------------------------------
+
+def phi_force_calculation(pe, cs, pth, fe, map_, phi, hydro):
+    _check(lib().phi_force_calculation(pe.ptr, cs.ptr, None, None, pth.ptr,
+                                       fe.ptr, map_.ptr if map_ else None,
+                                       phi.ptr, hydro.ptr),
+           "phi_force_calculation")
+
+
+def phi_cahn_hilliard(pch, fe, phi, hydro, map_=None):
+    _check(lib().phi_cahn_hilliard(pch.ptr, fe.ptr, phi.ptr,
+                                   hydro.ptr if hydro else None,
+                                   map_.ptr if map_ else None, None),
+           "phi_cahn_hilliard")
+
+
+class BinaryFluid:
+    """All objects of a symmetric binary fluid (the configs' model)."""
+
+    def __init__(self, ntotal, precision=FP64, a=-0.0625, b=0.0625,
+                 kappa=0.04, mobility=0.3, eta=0.1, eta_bulk=None, rho0=1.0,
+                 fbody=(0.0, 0.0, 0.0), device=0, fp16_scale=0.0,
+                 nrelax=0):
+        self.pe = PE(device)
+        self.cs = Coords(self.pe, ntotal)
+        self.phys = Physics(self.pe, rho0=rho0, eta=eta, eta_bulk=eta_bulk,
+                            mobility=mobility, fbody=fbody)
+        self.lb = LB(self.cs, precision, nrelax=nrelax,
+                     fp16_scale=fp16_scale)
+        self.phi = Field(self.cs, 1, 2, precision, "phi")
+        self.dphi = FieldGrad(self.phi, 2)
+        self.hydro = Hydro(self.cs, precision)
+        self.map = Map(self.cs)
+        self.fe = FeSymm(self.cs, self.phi, self.dphi, a, b, kappa)
+        self.pth = Pth(self.cs)
+        self.pch = PhiCH(self.cs)
+        self.lb.init_rest(rho0)
+
+    def step_reference_order(self, nsteps=1):
+        """One call per reference function, in the main-loop order."""
+        for _ in range(nsteps):
+            self.hydro.f_zero()
+            self.phi.halo()
+            self.dphi.compute()
+            phi_force_calculation(self.pe, self.cs, self.pth, self.fe,
+                                  self.map, self.phi, self.hydro)
+            self.hydro.u_halo()
+            phi_cahn_hilliard(self.pch, self.fe, self.phi, self.hydro,
+                              self.map)
+            self.hydro.u_zero()
+            self.lb.collide(self.hydro, self.map, self.fe)
+            self.lb.halo()
+            self.lb.propagation()
+
+    def step(self, nsteps=1):
+        """The fused GB300 step (one kernel per step, graph replay)."""
+        _check(lib().ludwig_gb_binary_step(self.lb.ptr, self.phi.ptr,
+                                           self.hydro.ptr, self.map.ptr,
+                                           self.fe.ptr, int(nsteps)),
+               "ludwig_gb_binary_step")
+
+    def step_async(self, nsteps=1):
+        _check(lib().ludwig_gb_binary_step_async(self.lb.ptr, self.phi.ptr,
+                                                 self.hydro.ptr, self.map.ptr,
+                                                 self.fe.ptr, int(nsteps)),
+               "ludwig_gb_binary_step_async")
+
+    def state(self):
+        rho, u, force = self.hydro.get()
+        return {"f": self.lb.get(), "phi": self.phi.get(), "u": u,
+                "rho": rho, "force": force}
+
+
+def sync():
+    _check(lib().ludwig_gb_sync(), "ludwig_gb_sync")
+
+
+def tune(xchunk, tile_y):
+    _check(lib().ludwig_gb_tune_set(int(xchunk), int(tile_y)), "tune")

@@ -1,0 +1,193 @@
+/*****************************************************************************
+ *
+ *  lgb_fused32.cu
+ *
+ *  Reduced-precision forms of the fused binary-fluid step:
+ *    FP32: float arithmetic; distributions stored as f - w_p rho0 (float)
+ *    FP16: float arithmetic; (f - w_p rho0)*scale stored as half
+ *  phi, u and rho are float in both.  Also the conversions between the
+ *  FP64 canonical arrays and these storage forms, and streaming of stored
+ *  distributions.
+ *
+ *****************************************************************************/
+
+#include "lgb_fused.cuh"
+
+extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
+				    const lgbk_binary_args_t * a, int xchunk,
+				    int ty, void * stream);
+
+template <typename S, bool HAS_MAP, int TY, int MINB>
+static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
+		    int xchunk, cudaStream_t stream) {
+  auto kern = k_binary_fused<float, S, false, true, true, HAS_MAP, TY, MINB>;
+  size_t smem = FusedSmem<float, TY>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TY, smem);
+  if (occ < 1) occ = 1;
+
+  int ntz = (d->nz + 31)/32, nty = (d->ny + TY - 1)/TY;
+  int ncx = (d->nx + xchunk - 1)/xchunk;
+  long long items = (long long) ntz*nty*ncx;
+  long long grid = (long long) nsm*occ;
+  if (grid > items) grid = items;
+
+  kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(*d, *a, xchunk);
+  return (int) cudaGetLastError();
+}
+
+template <typename S>
+static int dispatch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
+		      int xchunk, int ty, cudaStream_t s) {
+  if (ty == 4) {
+    return a->status ? launch32<S, true, 4, 4>(d, a, xchunk, s)
+                     : launch32<S, false, 4, 4>(d, a, xchunk, s);
+  }
+  if (ty == 16) {
+    return a->status ? launch32<S, true, 16, 1>(d, a, xchunk, s)
+                     : launch32<S, false, 16, 1>(d, a, xchunk, s);
+  }
+  return a->status ? launch32<S, true, 8, 2>(d, a, xchunk, s)
+                   : launch32<S, false, 8, 2>(d, a, xchunk, s);
+}
+
+extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
+				const lgbk_binary_args_t * a, int xchunk,
+				int ty, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  if (xchunk <= 0) xchunk = 32;
+  if (ty <= 0) ty = 8;
+  switch (prec) {
+  case LGBK_PREC_FP64:
+    return lgbk_binary_step_f64(d, a, xchunk, ty, stream);
+  case LGBK_PREC_FP32:
+    if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
+    return dispatch32<float>(d, a, xchunk, ty, s);
+  case LGBK_PREC_FP16:
+    if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
+    return dispatch32<__half>(d, a, xchunk, ty, s);
+  default:
+    return (int) cudaErrorInvalidValue;
+  }
+}
+
+/*****************************************************************************
+ *
+ *  Conversions.  For distributions (ncomp == 19) the shift w_p rho0 is
+ *  removed on the way in and restored on the way out; other fields are
+ *  converted as they are (shift_rho0 ignored).
+ *
+ *****************************************************************************/
+
+template <typename S>
+__global__ void k_to_store(long long nsites, int ncomp, double rho0,
+			   double scale, const double * __restrict__ src,
+			   S * __restrict__ dst) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  long long n = nsites*ncomp;
+  if (i >= n) return;
+  int p = (int) (i / nsites);
+  double v = src[i];
+  if (ncomp == LGB_NVEL) v -= lgb_w(p)*rho0;
+  FStore<S, double>::st(dst + i, v, scale);
+}
+
+template <typename S>
+__global__ void k_from_store(long long nsites, int ncomp, double rho0,
+			     double scale, const S * __restrict__ src,
+			     double * __restrict__ dst) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  long long n = nsites*ncomp;
+  if (i >= n) return;
+  int p = (int) (i / nsites);
+  double v = FStore<S, double>::ld(src + i, 1.0/scale);
+  if (ncomp == LGB_NVEL) v += lgb_w(p)*rho0;
+  dst[i] = v;
+}
+
+template <typename S>
+__global__ void k_propagate_store(lgbk_dims_t d, int dir,
+				  const S * __restrict__ f,
+				  S * __restrict__ fp) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i >= d.nsites) return;
+  int z = (int) (i % d.nz);
+  long long r = i / d.nz;
+  int y = (int) (r % d.ny);
+  int x = (int) (r / d.ny);
+  const long long N = d.nsites;
+  #pragma unroll
+  for (int p = 0; p < LGB_NVEL; p++) {
+    long long j = lgb_site_w(d, x - dir*lgb_cv_c[p][0], y - dir*lgb_cv_c[p][1],
+			     z - dir*lgb_cv_c[p][2]);
+    fp[p*N + i] = f[p*N + j];
+  }
+}
+
+static dim3 g256(long long n) { return dim3((unsigned int) ((n + 255)/256)); }
+
+extern "C" int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,
+				 double shift_rho0, double scale,
+				 const double * src, void * dst, void * stream) {
+  long long n = d->nsites*ncomp;
+  cudaStream_t s = (cudaStream_t) stream;
+  if (prec == LGBK_PREC_FP64) {
+    return (int) cudaMemcpyAsync(dst, src, n*sizeof(double),
+				 cudaMemcpyDeviceToDevice, s);
+  }
+  if (prec == LGBK_PREC_FP16 && ncomp == LGB_NVEL) {
+    k_to_store<__half><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+					       scale, src, (__half *) dst);
+  }
+  else {
+    k_to_store<float><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+					      1.0, src, (float *) dst);
+  }
+  return (int) cudaGetLastError();
+}
+
+extern "C" int lgbk_store_to_f64(const lgbk_dims_t * d, int prec, int ncomp,
+				 double shift_rho0, double scale,
+				 const void * src, double * dst, void * stream) {
+  long long n = d->nsites*ncomp;
+  cudaStream_t s = (cudaStream_t) stream;
+  if (prec == LGBK_PREC_FP64) {
+    return (int) cudaMemcpyAsync(dst, src, n*sizeof(double),
+				 cudaMemcpyDeviceToDevice, s);
+  }
+  if (prec == LGBK_PREC_FP16 && ncomp == LGB_NVEL) {
+    k_from_store<__half><<<g256(n), 256, 0, s>>>(d->nsites, ncomp,
+						 shift_rho0, scale,
+						 (const __half *) src, dst);
+  }
+  else {
+    k_from_store<float><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+						1.0, (const float *) src, dst);
+  }
+  return (int) cudaGetLastError();
+}
+
+extern "C" int lgbk_propagate_store(const lgbk_dims_t * d, int prec, int dir,
+				    const void * f, void * fprime,
+				    void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  switch (prec) {
+  case LGBK_PREC_FP64:
+    return lgbk_propagate_f64(d, dir, (const double *) f, (double *) fprime,
+			      stream);
+  case LGBK_PREC_FP32:
+    k_propagate_store<float><<<g256(d->nsites), 256, 0, s>>>(
+      *d, dir, (const float *) f, (float *) fprime);
+    break;
+  default:
+    k_propagate_store<__half><<<g256(d->nsites), 256, 0, s>>>(
+      *d, dir, (const __half *) f, (__half *) fprime);
+  }
+  return (int) cudaGetLastError();
+}

@@ -1,0 +1,122 @@
+/*****************************************************************************
+ *
+ *  lgb_kernels.h
+ *
+ *  Thin C ABI between the host-side C library (ludwig_gb.c) and the CUDA
+ *  kernels (lgb_*.cu).  Plain pointers to device memory, sizes, parameter
+ *  structs and a cudaStream_t passed as void *.  Every launcher returns 0
+ *  or a cudaError_t value from the launch.
+ *
+ *  Device layout of every lattice array: interior sites only (periodic
+ *  boundaries are applied by index wrap inside the kernels), one
+ *  contiguous plane per component, z fastest:
+ *      a[((n*nx + x)*ny + y)*nz + z]
+ *
+ *****************************************************************************/
+
+#ifndef LGB_KERNELS_H
+#define LGB_KERNELS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LGB_NVEL 19
+
+typedef struct lgbk_dims_s {
+  int nx, ny, nz;
+  long long nsites;
+} lgbk_dims_t;
+
+typedef struct lgbk_symm_s {
+  double a, b, kappa;
+} lgbk_symm_t;
+
+typedef struct lgbk_collide_s {
+  double rtau_shear;
+  double rtau_bulk;
+  double rtau_ghost[LGB_NVEL];
+  double force_global[3];
+  int ghosts_zero;               /* 1 if every ghost rtau is exactly 1 */
+} lgbk_collide_t;
+
+/* Precision / storage of the fused step */
+enum lgbk_prec {
+  LGBK_PREC_FP64 = 0,            /* double, reference-exact */
+  LGBK_PREC_FP32 = 1,            /* float arithmetic, f stored as f - w rho0 */
+  LGBK_PREC_FP16 = 2             /* as FP32, f - w rho0 stored as scaled half */
+};
+
+/* Reference-semantics FP64 kernels (one per reference kernel) */
+int lgbk_grad7_f64(const lgbk_dims_t * d, int nf, const double * field,
+		   double * grad, double * delsq, void * stream);
+int lgbk_symm_stress_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
+			 const double * phi, const double * grad,
+			 const double * delsq, double * pth, void * stream);
+int lgbk_symm_mu_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
+		     const double * phi, const double * delsq, double * mu,
+		     void * stream);
+int lgbk_force_div_f64(const lgbk_dims_t * d, const double * pth,
+		       double * force, void * stream);
+int lgbk_advect_upwind_f64(const lgbk_dims_t * d, int nf,
+			   const double * field, const double * u,
+			   double * fw, double * fe, double * fy, double * fz,
+			   void * stream);
+int lgbk_ch_flux_mu_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
+			double mobility, const double * phi,
+			const double * delsq, double * fw, double * fe_,
+			double * fy, double * fz, void * stream);
+int lgbk_flux_no_normal_f64(const lgbk_dims_t * d, int nf,
+			    const uint8_t * status, double * fw, double * fe,
+			    double * fy, double * fz, void * stream);
+int lgbk_ch_update_f64(const lgbk_dims_t * d, const double * fw,
+		       const double * fe, const double * fy, const double * fz,
+		       double * phi, void * stream);
+int lgbk_collide_f64(const lgbk_dims_t * d, const lgbk_collide_t * cp,
+		     const uint8_t * status, double * f, const double * force,
+		     double * rho, double * u, void * stream);
+/* dir = +1: fprime_p(x) = f_p(x - c_p) (propagation); dir = -1: inverse */
+int lgbk_propagate_f64(const lgbk_dims_t * d, int dir, const double * f,
+		       double * fprime, void * stream);
+int lgbk_fill_f64(double * a, long long n, double v, void * stream);
+
+/* Fused binary-fluid step (one kernel per step).
+ * Input f is the post-collision state of the previous step (its streamed
+ * image is the reference's f); output likewise.  force_out may be NULL. */
+typedef struct lgbk_binary_args_s {
+  const void * f_in;   void * f_out;
+  const void * phi_in; void * phi_out;
+  const void * u_in;   void * u_out;
+  void * rho_out;
+  void * force_out;
+  const uint8_t * status;
+  double mobility;
+  double rho0;
+  double fscale;       /* FP16 storage: stored = (f - w rho0)*fscale */
+  lgbk_symm_t fe;
+  lgbk_collide_t cp;
+} lgbk_binary_args_t;
+
+int lgbk_binary_step(const lgbk_dims_t * d, int prec,
+		     const lgbk_binary_args_t * a, int xchunk, int ty,
+		     void * stream);
+
+/* Conversions between FP64 canonical state and reduced storage */
+int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,
+		      double shift_rho0, double scale, const double * src,
+		      void * dst, void * stream);
+int lgbk_store_to_f64(const lgbk_dims_t * d, int prec, int ncomp,
+		      double shift_rho0, double scale, const void * src,
+		      double * dst, void * stream);
+/* Streaming of reduced-precision distributions (dir as above) */
+int lgbk_propagate_store(const lgbk_dims_t * d, int prec, int dir,
+			 const void * f, void * fprime, void * stream);
+
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

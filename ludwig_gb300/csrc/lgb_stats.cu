@@ -1,0 +1,275 @@
+/*****************************************************************************
+ *
+ *  lgb_stats.cu
+ *
+ *  Global sums on the device in FP64 with doubly compensated (Klein)
+ *  accumulation: field totals/variance/min/max (src/phi_stats.c:211-270),
+ *  distribution mass and momentum (src/stats_distribution.c:125-260) and
+ *  the symmetric free-energy total (src/stats_free_energy.c:38).
+ *
+ *  Two passes, both deterministic: a fixed grid of LGBK_RED_BLOCKS blocks
+ *  writes per-block partials to a scratch array, then one block combines
+ *  them in block order.  Within a block, partials are combined through
+ *  warp shuffles and shared memory in a fixed tree order.
+ *
+ *****************************************************************************/
+
+#include "lgb_fused.cuh"
+#include "lgb_stats.h"
+
+/* Klein doubly compensated sum, src/util_sum.c:91-120 */
+struct Klein {
+  double sum, cs, ccs;
+  __device__ __forceinline__ void zero() { sum = cs = ccs = 0.0; }
+  __device__ __forceinline__ void add(double v) {
+    double t = sum + v;
+    double c = (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+    sum = t;
+    t = cs + c;
+    double cc = (fabs(cs) >= fabs(c)) ? (cs - t) + c : (c - t) + cs;
+    cs = t;
+    ccs = ccs + cc;
+  }
+  __device__ __forceinline__ void add(const Klein & o) {
+    add(o.sum); add(o.cs); add(o.ccs);
+  }
+  __device__ __forceinline__ double total() const { return sum + cs + ccs; }
+};
+
+__device__ __forceinline__ Klein shfl_down(const Klein & k, int off) {
+  Klein r;
+  r.sum = __shfl_down_sync(0xffffffffu, k.sum, off);
+  r.cs  = __shfl_down_sync(0xffffffffu, k.cs, off);
+  r.ccs = __shfl_down_sync(0xffffffffu, k.ccs, off);
+  return r;
+}
+
+/* Reduce NK Klein sums + min/max over a block; thread 0 gets the result */
+template <int NK>
+__device__ void block_reduce(Klein k[NK], double & vmin, double & vmax) {
+  __shared__ Klein sk[32][NK];
+  __shared__ double smin[32], smax[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  #pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) {
+      Klein o = shfl_down(k[j], off);
+      if (lane < off) k[j].add(o);
+    }
+    double omin = __shfl_down_sync(0xffffffffu, vmin, off);
+    double omax = __shfl_down_sync(0xffffffffu, vmax, off);
+    if (lane < off) { vmin = fmin(vmin, omin); vmax = fmax(vmax, omax); }
+  }
+  if (lane == 0) {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) sk[warp][j] = k[j];
+    smin[warp] = vmin; smax[warp] = vmax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int w = 1; w < nw; w++) {
+      #pragma unroll
+      for (int j = 0; j < NK; j++) k[j].add(sk[w][j]);
+      vmin = fmin(vmin, smin[w]);
+      vmax = fmax(vmax, smax[w]);
+    }
+  }
+}
+
+/* Partial record per block: NK*3 Klein words, then min, max */
+
+template <int NK>
+__device__ void write_partial(double * part, const Klein k[NK], double vmin,
+			      double vmax) {
+  double * p = part + (size_t) blockIdx.x*(3*NK + 2);
+  #pragma unroll
+  for (int j = 0; j < NK; j++) {
+    p[3*j] = k[j].sum; p[3*j + 1] = k[j].cs; p[3*j + 2] = k[j].ccs;
+  }
+  p[3*NK] = vmin;
+  p[3*NK + 1] = vmax;
+}
+
+template <int NK>
+__global__ void k_final(const double * __restrict__ part, int nblocks,
+			double * __restrict__ out) {
+  /* one warp; lane j < NK combines word j in block order */
+  Klein k;
+  k.zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  for (int b = 0; b < nblocks; b++) {
+    const double * p = part + (size_t) b*(3*NK + 2);
+    if ((int) threadIdx.x < NK) {
+      Klein o;
+      o.sum = p[3*threadIdx.x]; o.cs = p[3*threadIdx.x + 1];
+      o.ccs = p[3*threadIdx.x + 2];
+      k.add(o);
+    }
+    vmin = fmin(vmin, p[3*NK]);
+    vmax = fmax(vmax, p[3*NK + 1]);
+  }
+  if ((int) threadIdx.x < NK) out[threadIdx.x] = k.total();
+  if (threadIdx.x == 0) { out[NK] = vmin; out[NK + 1] = vmax; }
+}
+
+template <typename T>
+__device__ __forceinline__ double ldv(const T * p) { return (double) *p; }
+
+/* Field component: sum, sum of squares, min, max */
+template <typename T>
+__global__ void k_field_stats(long long n, const T * __restrict__ a,
+			      double * __restrict__ part) {
+  Klein k[2];
+  k[0].zero(); k[1].zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
+       i += (long long) gridDim.x*blockDim.x) {
+    double v = ldv(a + i);
+    k[0].add(v);
+    k[1].add(v*v);
+    vmin = fmin(vmin, v);
+    vmax = fmax(vmax, v);
+  }
+  block_reduce<2>(k, vmin, vmax);
+  if (threadIdx.x == 0) write_partial<2>(part, k, vmin, vmax);
+}
+
+/* Distribution moments: mass and momentum of stored (possibly shifted) f */
+template <typename S>
+__global__ void k_dist_moments(long long n, const S * __restrict__ f,
+			       double rscale, double * __restrict__ part) {
+  Klein k[4];
+  #pragma unroll
+  for (int j = 0; j < 4; j++) k[j].zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
+       i += (long long) gridDim.x*blockDim.x) {
+    double fp[LGB_NVEL];
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) {
+      fp[p] = FStore<S, double>::ld(f + p*n + i, rscale);
+    }
+    double m = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) {
+      m += fp[p];
+      jx += lgb_cv_c[p][0]*fp[p];
+      jy += lgb_cv_c[p][1]*fp[p];
+      jz += lgb_cv_c[p][2]*fp[p];
+    }
+    k[0].add(m); k[1].add(jx); k[2].add(jy); k[3].add(jz);
+    vmin = fmin(vmin, m);
+    vmax = fmax(vmax, m);
+  }
+  block_reduce<4>(k, vmin, vmax);
+  if (threadIdx.x == 0) write_partial<4>(part, k, vmin, vmax);
+}
+
+/* Symmetric free energy density (src/symmetric.c:285-300) */
+template <typename T>
+__global__ void k_symm_fed(lgbk_dims_t d, lgbk_symm_t fe,
+			   const T * __restrict__ phi,
+			   double * __restrict__ part) {
+  Klein k[1];
+  k[0].zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+       i < d.nsites; i += (long long) gridDim.x*blockDim.x) {
+    int z = (int) (i % d.nz);
+    long long r = i / d.nz;
+    int y = (int) (r % d.ny);
+    int x = (int) (r / d.ny);
+    double g[3];
+    g[0] = 0.5*(ldv(phi + lgb_site_w(d, x+1, y, z))
+		- ldv(phi + lgb_site_w(d, x-1, y, z)));
+    g[1] = 0.5*(ldv(phi + lgb_site_w(d, x, y+1, z))
+		- ldv(phi + lgb_site_w(d, x, y-1, z)));
+    g[2] = 0.5*(ldv(phi + lgb_site_w(d, x, y, z+1))
+		- ldv(phi + lgb_site_w(d, x, y, z-1)));
+    double p = ldv(phi + i);
+    double fed = (0.5*fe.a + 0.25*fe.b*p*p)*p*p
+      + 0.5*fe.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
+    k[0].add(fed);
+    vmin = fmin(vmin, fed);
+    vmax = fmax(vmax, fed);
+  }
+  block_reduce<1>(k, vmin, vmax);
+  if (threadIdx.x == 0) write_partial<1>(part, k, vmin, vmax);
+}
+
+#define RED_TPB 256
+
+static int finish(int nk, double * scratch, double * out_host,
+		  cudaStream_t s) {
+  double * out = scratch + (size_t) LGBK_RED_BLOCKS*LGBK_RED_REC;
+  switch (nk) {
+  case 1: k_final<1><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  case 2: k_final<2><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  default: k_final<4><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  err = cudaMemcpyAsync(out_host, out, (nk + 2)*sizeof(double),
+			cudaMemcpyDeviceToHost, s);
+  if (err != cudaSuccess) return (int) err;
+  return (int) cudaStreamSynchronize(s);
+}
+
+extern "C" int lgbk_field_stats(const lgbk_dims_t * d, int prec,
+				const void * a, double * scratch,
+				double out_host[4], void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  if (prec == LGBK_PREC_FP64) {
+    k_field_stats<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      d->nsites, (const double *) a, scratch);
+  }
+  else {
+    k_field_stats<float><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      d->nsites, (const float *) a, scratch);
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return finish(2, scratch, out_host, s);
+}
+
+extern "C" int lgbk_dist_moments(const lgbk_dims_t * d, int prec,
+				 const void * f, double scale, double * scratch,
+				 double out_host[6], void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  if (prec == LGBK_PREC_FP64) {
+    k_dist_moments<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      d->nsites, (const double *) f, 1.0, scratch);
+  }
+  else if (prec == LGBK_PREC_FP32) {
+    k_dist_moments<float><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      d->nsites, (const float *) f, 1.0, scratch);
+  }
+  else {
+    k_dist_moments<__half><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      d->nsites, (const __half *) f, 1.0/scale, scratch);
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return finish(4, scratch, out_host, s);
+}
+
+extern "C" int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,
+				   const lgbk_symm_t * fe, const void * phi,
+				   double * scratch, double out_host[3],
+				   void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  if (prec == LGBK_PREC_FP64) {
+    k_symm_fed<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      *d, *fe, (const double *) phi, scratch);
+  }
+  else {
+    k_symm_fed<float><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      *d, *fe, (const float *) phi, scratch);
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return finish(1, scratch, out_host, s);
+}

@@ -1,0 +1,1357 @@
+/*****************************************************************************
+ *
+ *  ludwig_gb.c
+ *
+ *  Host side of libludwig_gb.so, in C: the objects and entry points of
+ *  include/ludwig_gb.h on top of the kernel launchers of lgb_kernels.h.
+ *
+ *  State of the distributions.  The reference keeps f and, after
+ *  lb_collide, overwrites it with post-collision values which
+ *  lb_propagation then streams.  Here an lb_t carries a flag "pending":
+ *  when set, the stored array holds post-collision values and the
+ *  reference's f is their streamed image.  lb_propagation only sets the
+ *  flag (streaming is folded into the next pull); the fused step keeps it
+ *  set; any call that needs the reference's f materialises the stream
+ *  first.  All of this is exact: streaming is a permutation.
+ *
+ *****************************************************************************/
+
+#include <assert.h>
+#include <limits.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "ludwig_gb.h"
+#include "lgb_kernels.h"
+#include "lgb_stats.h"
+
+#define NVEL LGB_NVEL
+
+/*****************************************************************************
+ *  Errors
+ *****************************************************************************/
+
+static __thread char last_error_[512] = "";
+
+static int err_set(int code, const char * fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(last_error_, sizeof(last_error_), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+static int cuda_check(int rc, const char * where) {
+  if (rc != 0) {
+    return err_set(LUDWIG_GB_ECUDA, "%s: %s", where,
+		   cudaGetErrorString((cudaError_t) rc));
+  }
+  return LUDWIG_GB_OK;
+}
+
+#define CK(call, where) do { int rc_ = (int) (call); \
+    if (rc_) return cuda_check(rc_, where); } while (0)
+
+const char * ludwig_gb_last_error(void) { return last_error_; }
+const char * ludwig_gb_version(void) { return "ludwig-gb300 0.1"; }
+
+/*****************************************************************************
+ *  Library stream and scratch
+ *****************************************************************************/
+
+static cudaStream_t stream_ = NULL;
+static double * red_scratch_ = NULL;
+static int tune_xchunk_ = 32;
+static int tune_ty_ = 8;
+
+static int lib_init(void) {
+  if (stream_ == NULL) {
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking),
+       "cudaStreamCreate");
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int red_scratch(double ** p) {
+  if (red_scratch_ == NULL) {
+    CK(cudaMalloc((void **) &red_scratch_, LGBK_RED_SCRATCH*sizeof(double)),
+       "cudaMalloc(scratch)");
+  }
+  *p = red_scratch_;
+  return LUDWIG_GB_OK;
+}
+
+void * ludwig_gb_stream(void) {
+  if (lib_init()) return NULL;
+  return (void *) stream_;
+}
+
+int ludwig_gb_sync(void) {
+  if (lib_init()) return LUDWIG_GB_ECUDA;
+  CK(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_tune_set(int xchunk, int tile_y) {
+  if (xchunk < 1 || (tile_y != 4 && tile_y != 8 && tile_y != 16)) {
+    return err_set(LUDWIG_GB_EINVAL, "tune: xchunk >= 1, tile_y in {4,8,16}");
+  }
+  tune_xchunk_ = xchunk;
+  tune_ty_ = tile_y;
+  return LUDWIG_GB_OK;
+}
+
+static size_t prec_size(int prec) {
+  return (prec == LUDWIG_GB_FP64) ? 8 : ((prec == LUDWIG_GB_FP32) ? 4 : 2);
+}
+
+/* phi, u and rho are float in both reduced-precision forms */
+static size_t field_size(int prec) { return (prec == LUDWIG_GB_FP64) ? 8 : 4; }
+static int field_kprec(int prec) {
+  return (prec == LUDWIG_GB_FP64) ? LGBK_PREC_FP64 : LGBK_PREC_FP32;
+}
+
+static int dev_alloc(void ** p, size_t bytes, const char * what) {
+  *p = NULL;
+  if (bytes == 0) return LUDWIG_GB_OK;
+  if (cudaMalloc(p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *p = NULL;
+    return err_set(LUDWIG_GB_ENOMEM, "cudaMalloc(%s, %zu bytes) failed",
+		   what, bytes);
+  }
+  return LUDWIG_GB_OK;
+}
+
+static void dev_free(void * p) { if (p) cudaFree(p); }
+
+/*****************************************************************************
+ *  pe_t, cs_t, physics_t
+ *****************************************************************************/
+
+struct pe_s { int device; };
+
+int pe_create(int device, pe_t ** ppe) {
+  if (ppe == NULL) return err_set(LUDWIG_GB_EINVAL, "pe_create: NULL");
+  CK(cudaSetDevice(device), "cudaSetDevice");
+  pe_t * pe = (pe_t *) calloc(1, sizeof(pe_t));
+  if (pe == NULL) return err_set(LUDWIG_GB_ENOMEM, "pe_create");
+  pe->device = device;
+  *ppe = pe;
+  return lib_init();
+}
+
+int pe_free(pe_t * pe) { free(pe); return LUDWIG_GB_OK; }
+
+struct cs_s {
+  int ntotal[3];
+  int nhalo;
+  int initialised;
+  lgbk_dims_t d;
+};
+
+int cs_create(pe_t * pe, cs_t ** pcs) {
+  (void) pe;
+  if (pcs == NULL) return err_set(LUDWIG_GB_EINVAL, "cs_create: NULL");
+  cs_t * cs = (cs_t *) calloc(1, sizeof(cs_t));
+  if (cs == NULL) return err_set(LUDWIG_GB_ENOMEM, "cs_create");
+  cs->ntotal[0] = cs->ntotal[1] = cs->ntotal[2] = 64;   /* src/coords.c */
+  cs->nhalo = 1;
+  *pcs = cs;
+  return LUDWIG_GB_OK;
+}
+
+int cs_free(cs_t * cs) { free(cs); return LUDWIG_GB_OK; }
+
+int cs_ntotal_set(cs_t * cs, const int ntotal[3]) {
+  if (cs == NULL || ntotal == NULL) return err_set(LUDWIG_GB_EINVAL, "cs");
+  if (cs->initialised) return err_set(LUDWIG_GB_ESTATE, "cs initialised");
+  for (int i = 0; i < 3; i++) {
+    if (ntotal[i] < 2) {
+      return err_set(LUDWIG_GB_EINVAL, "cs_ntotal_set: every extent >= 2");
+    }
+    cs->ntotal[i] = ntotal[i];
+  }
+  return LUDWIG_GB_OK;
+}
+
+int cs_nhalo_set(cs_t * cs, int nhalo) {
+  if (cs == NULL || nhalo < 0) return err_set(LUDWIG_GB_EINVAL, "nhalo");
+  if (cs->initialised) return err_set(LUDWIG_GB_ESTATE, "cs initialised");
+  cs->nhalo = nhalo;
+  return LUDWIG_GB_OK;
+}
+
+int cs_init(cs_t * cs) {
+  if (cs == NULL) return err_set(LUDWIG_GB_EINVAL, "cs_init: NULL");
+  cs->d.nx = cs->ntotal[0];
+  cs->d.ny = cs->ntotal[1];
+  cs->d.nz = cs->ntotal[2];
+  cs->d.nsites = (long long) cs->d.nx*cs->d.ny*cs->d.nz;
+  cs->initialised = 1;
+  return LUDWIG_GB_OK;
+}
+
+int cs_nlocal(cs_t * cs, int nlocal[3]) {
+  if (cs == NULL || !cs->initialised) {
+    return err_set(LUDWIG_GB_ESTATE, "cs not initialised");
+  }
+  nlocal[0] = cs->d.nx; nlocal[1] = cs->d.ny; nlocal[2] = cs->d.nz;
+  return LUDWIG_GB_OK;
+}
+
+struct physics_s {
+  double rho0;
+  double eta_shear;
+  double eta_bulk;
+  double mobility;
+  double fbody[3];
+};
+
+static physics_t * phys_ref_ = NULL;
+
+int physics_create(pe_t * pe, physics_t ** phys) {
+  (void) pe;
+  if (phys == NULL) return err_set(LUDWIG_GB_EINVAL, "physics_create");
+  physics_t * p = (physics_t *) calloc(1, sizeof(physics_t));
+  if (p == NULL) return err_set(LUDWIG_GB_ENOMEM, "physics_create");
+  /* Defaults of src/physics.c:108-111 */
+  p->eta_shear = 1.0/6.0;
+  p->eta_bulk = 1.0/6.0;
+  p->rho0 = 1.0;
+  phys_ref_ = p;
+  *phys = p;
+  return LUDWIG_GB_OK;
+}
+
+int physics_free(physics_t * phys) {
+  if (phys == phys_ref_) phys_ref_ = NULL;
+  free(phys);
+  return LUDWIG_GB_OK;
+}
+
+int physics_ref(physics_t ** ref) { *ref = phys_ref_; return LUDWIG_GB_OK; }
+int physics_rho0_set(physics_t * p, double v) { p->rho0 = v; return 0; }
+int physics_eta_shear_set(physics_t * p, double v) { p->eta_shear = v; return 0; }
+int physics_eta_bulk_set(physics_t * p, double v) { p->eta_bulk = v; return 0; }
+int physics_mobility_set(physics_t * p, double v) { p->mobility = v; return 0; }
+int physics_fbody_set(physics_t * p, const double f[3]) {
+  for (int i = 0; i < 3; i++) p->fbody[i] = f[i];
+  return 0;
+}
+
+static int phys_get(physics_t ** p) {
+  if (phys_ref_ == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "no physics_t: call physics_create()");
+  }
+  *p = phys_ref_;
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  lb_t
+ *****************************************************************************/
+
+struct lb_data_s {
+  cs_t * cs;
+  int prec;
+  lb_relaxation_enum_t nrelax;
+  double fscale;
+  double rho0;                 /* shift of the reduced-precision storage */
+  void * f;
+  void * fprime;
+  int pending;                 /* stored values await streaming */
+};
+
+lb_data_options_t lb_data_options_default(void) {
+  lb_data_options_t o = {3, 19, 1, LB_RELAXATION_M10, LUDWIG_GB_FP64, 0.0};
+  return o;
+}
+
+int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
+		   lb_t ** plb) {
+  (void) pe;
+  lb_data_options_t o = opts ? *opts : lb_data_options_default();
+  if (cs == NULL || !cs->initialised || plb == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: cs not initialised");
+  }
+  if (o.ndim != 3 || o.nvel != 19 || o.ndist != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: D3Q19, ndist 1 only");
+  }
+  if (o.precision < LUDWIG_GB_FP64 || o.precision > LUDWIG_GB_FP16) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: precision");
+  }
+  int rc = lib_init();
+  if (rc) return rc;
+
+  lb_t * lb = (lb_t *) calloc(1, sizeof(lb_t));
+  if (lb == NULL) return err_set(LUDWIG_GB_ENOMEM, "lb_data_create");
+  lb->cs = cs;
+  lb->prec = o.precision;
+  lb->nrelax = o.nrelax;
+  lb->fscale = (o.fp16_scale > 0.0) ? o.fp16_scale : 1024.0;
+  lb->rho0 = phys_ref_ ? phys_ref_->rho0 : 1.0;
+
+  size_t bytes = NVEL*(size_t) cs->d.nsites*prec_size(lb->prec);
+  if ((rc = dev_alloc(&lb->f, bytes, "f")) ||
+      (rc = dev_alloc(&lb->fprime, bytes, "fprime"))) {
+    lb_free(lb);
+    return rc;
+  }
+  *plb = lb;
+  return lb_init_rest_f(lb, lb->rho0);
+}
+
+int lb_free(lb_t * lb) {
+  if (lb) {
+    dev_free(lb->f);
+    dev_free(lb->fprime);
+    free(lb);
+  }
+  return LUDWIG_GB_OK;
+}
+
+static void lb_swap(lb_t * lb) {
+  void * t = lb->f; lb->f = lb->fprime; lb->fprime = t;
+}
+
+/* Make the stored array hold the reference's f (apply pending streaming) */
+static int lb_materialise(lb_t * lb) {
+  if (!lb->pending) return LUDWIG_GB_OK;
+  CK(lgbk_propagate_store(&lb->cs->d, lb->prec, +1, lb->f, lb->fprime,
+			  stream_), "propagate");
+  lb_swap(lb);
+  lb->pending = 0;
+  return LUDWIG_GB_OK;
+}
+
+/* Make the stored array hold post-collision values (pending = 1) */
+static int lb_unstream(lb_t * lb) {
+  if (lb->pending) return LUDWIG_GB_OK;
+  CK(lgbk_propagate_store(&lb->cs->d, lb->prec, -1, lb->f, lb->fprime,
+			  stream_), "unstream");
+  lb_swap(lb);
+  lb->pending = 1;
+  return LUDWIG_GB_OK;
+}
+
+/* src/lb_data.c:659-680 and :809-834 with u = 0: f_p = rho0 w_p */
+int lb_init_rest_f(lb_t * lb, double rho0) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_init_rest_f");
+  const lgbk_dims_t * d = &lb->cs->d;
+  double * tmp = NULL;
+  int rc = dev_alloc((void **) &tmp, NVEL*(size_t) d->nsites*sizeof(double),
+		     "init");
+  if (rc) return rc;
+  for (int p = 0; p < NVEL; p++) {
+    static const int w36[NVEL] = {12, 1, 1, 2, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1,
+				  1, 1, 2, 1, 1};
+    double w = (double) w36[p]/36.0;
+    rc = lgbk_fill_f64(tmp + p*d->nsites, d->nsites, rho0*w*1.0, stream_);
+    if (rc) break;
+  }
+  if (rc == 0) {
+    rc = lgbk_f64_to_store(d, lb->prec, NVEL, lb->rho0, lb->fscale, tmp,
+			   lb->f, stream_);
+  }
+  if (rc == 0) rc = cudaStreamSynchronize(stream_);
+  dev_free(tmp);
+  lb->pending = 0;
+  return cuda_check(rc, "lb_init_rest_f");
+}
+
+int lb_halo(lb_t * lb) {
+  /* Periodic images are read in place by every kernel. */
+  return (lb == NULL) ? err_set(LUDWIG_GB_EINVAL, "lb_halo") : LUDWIG_GB_OK;
+}
+
+int lb_f_to_host(lb_t * lb, double * fh) {
+  if (lb == NULL || fh == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_f");
+  const lgbk_dims_t * d = &lb->cs->d;
+  const void * src = lb->f;
+  size_t n = NVEL*(size_t) d->nsites;
+  if (lb->pending) {
+    CK(lgbk_propagate_store(d, lb->prec, +1, lb->f, lb->fprime, stream_),
+       "propagate");
+    src = lb->fprime;
+  }
+  if (lb->prec == LUDWIG_GB_FP64) {
+    CK(cudaMemcpyAsync(fh, src, n*sizeof(double), cudaMemcpyDeviceToHost,
+		       stream_), "lb_f_to_host");
+  }
+  else {
+    double * tmp = NULL;
+    int rc = dev_alloc((void **) &tmp, n*sizeof(double), "convert");
+    if (rc) return rc;
+    rc = lgbk_store_to_f64(d, lb->prec, NVEL, lb->rho0, lb->fscale, src, tmp,
+			   stream_);
+    if (rc == 0) rc = cudaMemcpyAsync(fh, tmp, n*sizeof(double),
+				      cudaMemcpyDeviceToHost, stream_);
+    if (rc == 0) rc = cudaStreamSynchronize(stream_);
+    dev_free(tmp);
+    return cuda_check(rc, "lb_f_to_host");
+  }
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int lb_f_from_host(lb_t * lb, const double * fh) {
+  if (lb == NULL || fh == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_f");
+  const lgbk_dims_t * d = &lb->cs->d;
+  size_t n = NVEL*(size_t) d->nsites;
+  if (lb->prec == LUDWIG_GB_FP64) {
+    CK(cudaMemcpyAsync(lb->f, fh, n*sizeof(double), cudaMemcpyHostToDevice,
+		       stream_), "lb_f_from_host");
+  }
+  else {
+    double * tmp = NULL;
+    int rc = dev_alloc((void **) &tmp, n*sizeof(double), "convert");
+    if (rc) return rc;
+    rc = cudaMemcpyAsync(tmp, fh, n*sizeof(double), cudaMemcpyHostToDevice,
+			 stream_);
+    if (rc == 0) rc = lgbk_f64_to_store(d, lb->prec, NVEL, lb->rho0,
+					lb->fscale, tmp, lb->f, stream_);
+    if (rc == 0) rc = cudaStreamSynchronize(stream_);
+    dev_free(tmp);
+    if (rc) return cuda_check(rc, "lb_f_from_host");
+  }
+  CK(cudaStreamSynchronize(stream_), "sync");
+  lb->pending = 0;
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  field_t, field_grad_t
+ *****************************************************************************/
+
+struct field_s {
+  cs_t * cs;
+  int nf;
+  int nhcomm;
+  int prec;
+  char name[32];
+  void * data;
+  void * data2;                /* second buffer for the fused step */
+};
+
+field_options_t field_options_ndata_nhalo(int ndata, int nhalo) {
+  field_options_t o = {ndata, nhalo, LUDWIG_GB_FP64};
+  return o;
+}
+
+int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
+		 const field_options_t * opts, field_t ** pobj) {
+  (void) pe;
+  if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
+  if (cs == NULL || !cs->initialised || opts == NULL || pobj == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "field_create");
+  }
+  if (opts->ndata < 1 || opts->ndata > 5) {
+    return err_set(LUDWIG_GB_EINVAL, "field_create: ndata in 1..5");
+  }
+  int rc = lib_init();
+  if (rc) return rc;
+  field_t * f = (field_t *) calloc(1, sizeof(field_t));
+  if (f == NULL) return err_set(LUDWIG_GB_ENOMEM, "field_create");
+  f->cs = cs;
+  f->nf = opts->ndata;
+  f->nhcomm = opts->nhcomm;
+  f->prec = opts->precision;
+  snprintf(f->name, sizeof(f->name), "%s", name ? name : "field");
+  size_t bytes = (size_t) f->nf*cs->d.nsites*field_size(f->prec);
+  if ((rc = dev_alloc(&f->data, bytes, "field")) ||
+      (rc = dev_alloc(&f->data2, bytes, "field2"))) {
+    field_free(f);
+    return rc;
+  }
+  CK(cudaMemsetAsync(f->data, 0, bytes, stream_), "memset");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  *pobj = f;
+  return LUDWIG_GB_OK;
+}
+
+int field_free(field_t * f) {
+  if (f) { dev_free(f->data); dev_free(f->data2); free(f); }
+  return LUDWIG_GB_OK;
+}
+
+int field_nf(field_t * f, int * nf) { *nf = f->nf; return LUDWIG_GB_OK; }
+
+int field_halo(field_t * f) {
+  return (f == NULL) ? err_set(LUDWIG_GB_EINVAL, "field_halo") : LUDWIG_GB_OK;
+}
+
+static int copy_to_host(int prec, long long n, const void * src, double * dst) {
+  if (prec == LUDWIG_GB_FP64) {
+    CK(cudaMemcpyAsync(dst, src, n*sizeof(double), cudaMemcpyDeviceToHost,
+		       stream_), "to_host");
+    CK(cudaStreamSynchronize(stream_), "sync");
+    return LUDWIG_GB_OK;
+  }
+  float * tmp = (float *) malloc(n*sizeof(float));
+  if (tmp == NULL) return err_set(LUDWIG_GB_ENOMEM, "to_host");
+  int rc = cudaMemcpyAsync(tmp, src, n*sizeof(float), cudaMemcpyDeviceToHost,
+			   stream_);
+  if (rc == 0) rc = cudaStreamSynchronize(stream_);
+  for (long long i = 0; rc == 0 && i < n; i++) dst[i] = tmp[i];
+  free(tmp);
+  return cuda_check(rc, "to_host");
+}
+
+static int copy_from_host(int prec, long long n, const double * src,
+			  void * dst) {
+  if (prec == LUDWIG_GB_FP64) {
+    CK(cudaMemcpyAsync(dst, src, n*sizeof(double), cudaMemcpyHostToDevice,
+		       stream_), "from_host");
+    CK(cudaStreamSynchronize(stream_), "sync");
+    return LUDWIG_GB_OK;
+  }
+  float * tmp = (float *) malloc(n*sizeof(float));
+  if (tmp == NULL) return err_set(LUDWIG_GB_ENOMEM, "from_host");
+  for (long long i = 0; i < n; i++) tmp[i] = (float) src[i];
+  int rc = cudaMemcpyAsync(dst, tmp, n*sizeof(float), cudaMemcpyHostToDevice,
+			   stream_);
+  if (rc == 0) rc = cudaStreamSynchronize(stream_);
+  free(tmp);
+  return cuda_check(rc, "from_host");
+}
+
+int field_to_host(field_t * f, double * data) {
+  if (f == NULL || data == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  return copy_to_host(f->prec, f->nf*f->cs->d.nsites, f->data, data);
+}
+
+int field_from_host(field_t * f, const double * data) {
+  if (f == NULL || data == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  return copy_from_host(f->prec, f->nf*f->cs->d.nsites, data, f->data);
+}
+
+/* KISS99-type generator of src/noise.h:96-112 and the per-site seeding of
+ * src/noise.c:278-340; spinodal phi = phi0 + amp (r - 1/2),
+ * src/field_phi_init.c:484-518.  Global coordinates are 1-based. */
+
+static unsigned int kiss(unsigned int s[4]) {
+  unsigned int b;
+  s[0] = 69069u*s[0] + 1234567u;
+  b = s[1] ^ (s[1] << 17);
+  b ^= (b >> 13);
+  s[1] = b ^ (b << 5);
+  s[2] = 36969u*(s[2] & 0xffffu) + (s[2] >> 16);
+  s[3] = 18000u*(s[3] & 0xffffu) + (s[3] >> 16);
+  b = (s[2] << 16) + s[3];
+  return (s[1] + (s[0] ^ b));
+}
+
+int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
+  if (phi == NULL || phi->nf != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "field_phi_init_spinodal: scalar field");
+  }
+  const lgbk_dims_t * d = &phi->cs->d;
+  double * h = (double *) malloc(d->nsites*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "spinodal");
+  unsigned int seed0 = (seed > 1) ? (unsigned int) seed : 13u;
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	unsigned int sl[4], st[4];
+	sl[0] = seed0 + (unsigned int) (x + 1);
+	sl[1] = 12953u + (unsigned int) (y + 1);
+	sl[2] = 712357u + (unsigned int) (z + 1);
+	sl[3] = 22383979u;
+	for (int k = 0; k < 4; k++) st[k] = kiss(sl);
+	double ran = (1.0/UINT_MAX)*kiss(st);
+	h[((long long) x*d->ny + y)*d->nz + z] = phi0 + amp*(ran - 0.5);
+      }
+    }
+  }
+  int rc = field_from_host(phi, h);
+  free(h);
+  return rc;
+}
+
+struct field_grad_s {
+  field_t * field;
+  int level;
+  double * grad;
+  double * delsq;
+};
+
+int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p) {
+  (void) pe;
+  if (f == NULL || p == NULL || level < 1) {
+    return err_set(LUDWIG_GB_EINVAL, "field_grad_create");
+  }
+  field_grad_t * g = (field_grad_t *) calloc(1, sizeof(field_grad_t));
+  if (g == NULL) return err_set(LUDWIG_GB_ENOMEM, "field_grad_create");
+  g->field = f;
+  g->level = level;
+  *p = g;
+  return LUDWIG_GB_OK;
+}
+
+int field_grad_free(field_grad_t * g) {
+  if (g) { dev_free(g->grad); dev_free(g->delsq); free(g); }
+  return LUDWIG_GB_OK;
+}
+
+static int grad_alloc(field_grad_t * g) {
+  if (g->grad) return LUDWIG_GB_OK;
+  size_t n = (size_t) g->field->nf*g->field->cs->d.nsites;
+  int rc = dev_alloc((void **) &g->grad, 3*n*sizeof(double), "grad");
+  if (rc == 0) rc = dev_alloc((void **) &g->delsq, n*sizeof(double), "delsq");
+  return rc;
+}
+
+int field_grad_compute(field_grad_t * g) {
+  if (g == NULL) return err_set(LUDWIG_GB_EINVAL, "field_grad_compute");
+  if (g->field->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "field_grad_compute: FP64 fields only");
+  }
+  int rc = grad_alloc(g);
+  if (rc) return rc;
+  CK(lgbk_grad7_f64(&g->field->cs->d, g->field->nf,
+		    (const double *) g->field->data, g->grad, g->delsq,
+		    stream_), "grad7");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int field_grad_to_host(field_grad_t * g, double * grad, double * delsq) {
+  if (g == NULL || g->grad == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "field_grad_to_host: not computed");
+  }
+  long long n = (long long) g->field->nf*g->field->cs->d.nsites;
+  int rc = LUDWIG_GB_OK;
+  if (grad) rc = copy_to_host(LUDWIG_GB_FP64, 3*n, g->grad, grad);
+  if (rc == 0 && delsq) rc = copy_to_host(LUDWIG_GB_FP64, n, g->delsq, delsq);
+  return rc;
+}
+
+/*****************************************************************************
+ *  hydro_t, map_t
+ *****************************************************************************/
+
+struct hydro_s {
+  cs_t * cs;
+  int prec;
+  void * rho;
+  void * u;
+  void * u2;
+  void * force;
+};
+
+hydro_options_t hydro_options_default(void) {
+  hydro_options_t o = {1, LUDWIG_GB_FP64};
+  return o;
+}
+
+int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		 const hydro_options_t * opts, hydro_t ** pobj) {
+  (void) pe;
+  if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
+  if (cs == NULL || !cs->initialised || pobj == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "hydro_create");
+  }
+  hydro_options_t o = opts ? *opts : hydro_options_default();
+  int rc = lib_init();
+  if (rc) return rc;
+  hydro_t * h = (hydro_t *) calloc(1, sizeof(hydro_t));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "hydro_create");
+  h->cs = cs;
+  h->prec = o.precision;
+  size_t n = (size_t) cs->d.nsites, es = field_size(h->prec);
+  if ((rc = dev_alloc(&h->rho, n*es, "rho")) ||
+      (rc = dev_alloc(&h->u, 3*n*es, "u")) ||
+      (rc = dev_alloc(&h->u2, 3*n*es, "u2")) ||
+      (rc = dev_alloc(&h->force, 3*n*es, "force"))) {
+    hydro_free(h);
+    return rc;
+  }
+  CK(cudaMemsetAsync(h->u, 0, 3*n*es, stream_), "memset");
+  CK(cudaMemsetAsync(h->force, 0, 3*n*es, stream_), "memset");
+  CK(cudaMemsetAsync(h->rho, 0, n*es, stream_), "memset");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  *pobj = h;
+  return LUDWIG_GB_OK;
+}
+
+int hydro_free(hydro_t * h) {
+  if (h) {
+    dev_free(h->rho); dev_free(h->u); dev_free(h->u2); dev_free(h->force);
+    free(h);
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int fill3(hydro_t * h, void * a, const double v[3]) {
+  long long n = h->cs->d.nsites;
+  if (h->prec != LUDWIG_GB_FP64) {
+    if (v[0] == 0.0 && v[1] == 0.0 && v[2] == 0.0) {
+      CK(cudaMemsetAsync(a, 0, 3*n*sizeof(float), stream_), "memset");
+      CK(cudaStreamSynchronize(stream_), "sync");
+      return LUDWIG_GB_OK;
+    }
+    return err_set(LUDWIG_GB_EINVAL, "non-zero fill of a float field");
+  }
+  for (int i = 0; i < 3; i++) {
+    CK(lgbk_fill_f64((double *) a + i*n, n, v[i], stream_), "fill");
+  }
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int hydro_f_zero(hydro_t * h, const double fzero[3]) {
+  if (h == NULL || fzero == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro");
+  return fill3(h, h->force, fzero);
+}
+
+int hydro_u_zero(hydro_t * h, const double uzero[3]) {
+  if (h == NULL || uzero == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro");
+  return fill3(h, h->u, uzero);
+}
+
+int hydro_u_halo(hydro_t * h) {
+  return (h == NULL) ? err_set(LUDWIG_GB_EINVAL, "hydro") : LUDWIG_GB_OK;
+}
+
+int hydro_to_host(hydro_t * h, double * rho, double * u, double * force) {
+  if (h == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro_to_host");
+  long long n = h->cs->d.nsites;
+  int rc = LUDWIG_GB_OK;
+  if (rho) rc = copy_to_host(h->prec, n, h->rho, rho);
+  if (rc == 0 && u) rc = copy_to_host(h->prec, 3*n, h->u, u);
+  if (rc == 0 && force) rc = copy_to_host(h->prec, 3*n, h->force, force);
+  return rc;
+}
+
+int hydro_from_host(hydro_t * h, const double * rho, const double * u,
+		    const double * force) {
+  if (h == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro_from_host");
+  long long n = h->cs->d.nsites;
+  int rc = LUDWIG_GB_OK;
+  if (rho) rc = copy_from_host(h->prec, n, rho, h->rho);
+  if (rc == 0 && u) rc = copy_from_host(h->prec, 3*n, u, h->u);
+  if (rc == 0 && force) rc = copy_from_host(h->prec, 3*n, force, h->force);
+  return rc;
+}
+
+struct map_s {
+  cs_t * cs;
+  uint8_t * status;
+  int all_fluid;
+};
+
+int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj) {
+  (void) pe;
+  if (cs == NULL || !cs->initialised || pobj == NULL || ndata != 0) {
+    return err_set(LUDWIG_GB_EINVAL, "map_create: ndata 0 only");
+  }
+  int rc = lib_init();
+  if (rc) return rc;
+  map_t * m = (map_t *) calloc(1, sizeof(map_t));
+  if (m == NULL) return err_set(LUDWIG_GB_ENOMEM, "map_create");
+  m->cs = cs;
+  m->all_fluid = 1;
+  if ((rc = dev_alloc((void **) &m->status, (size_t) cs->d.nsites, "map"))) {
+    free(m);
+    return rc;
+  }
+  CK(cudaMemsetAsync(m->status, 0, (size_t) cs->d.nsites, stream_), "memset");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  *pobj = m;
+  return LUDWIG_GB_OK;
+}
+
+int map_free(map_t * m) {
+  if (m) { dev_free(m->status); free(m); }
+  return LUDWIG_GB_OK;
+}
+
+int map_status_from_host(map_t * m, const uint8_t * status) {
+  if (m == NULL || status == NULL) return err_set(LUDWIG_GB_EINVAL, "map");
+  long long n = m->cs->d.nsites;
+  m->all_fluid = 1;
+  for (long long i = 0; i < n; i++) {
+    if (status[i] >= MAP_STATUS_MAX) {
+      return err_set(LUDWIG_GB_EINVAL, "map status value out of range");
+    }
+    if (status[i] != MAP_FLUID) m->all_fluid = 0;
+  }
+  CK(cudaMemcpyAsync(m->status, status, (size_t) n, cudaMemcpyHostToDevice,
+		     stream_), "map");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* Device status pointer, or NULL when every site is fluid */
+static const uint8_t * map_dev(map_t * m) {
+  return (m == NULL || m->all_fluid) ? NULL : m->status;
+}
+
+/*****************************************************************************
+ *  Symmetric free energy (fe_t interface)
+ *****************************************************************************/
+
+struct fe_symm_s {
+  fe_t super;
+  fe_symm_param_t param;
+  field_t * phi;
+  field_grad_t * dphi;
+};
+
+static int site_get(field_t * f, int n, int index, double * v) {
+  if (index < 0 || index >= f->cs->d.nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "site index out of range");
+  }
+  const char * base = (const char *) f->data
+    + ((size_t) n*f->cs->d.nsites + index)*field_size(f->prec);
+  if (f->prec == LUDWIG_GB_FP64) {
+    CK(cudaMemcpy(v, base, sizeof(double), cudaMemcpyDeviceToHost), "site");
+  }
+  else {
+    float t;
+    CK(cudaMemcpy(&t, base, sizeof(float), cudaMemcpyDeviceToHost), "site");
+    *v = t;
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int grad_site(field_grad_t * g, int index, double gr[3], double * dsq) {
+  if (g->grad == NULL) return err_set(LUDWIG_GB_ESTATE, "gradients not computed");
+  size_t N = (size_t) g->field->cs->d.nsites;
+  for (int ia = 0; ia < 3; ia++) {
+    CK(cudaMemcpy(gr + ia, g->grad + ia*N + index, sizeof(double),
+		  cudaMemcpyDeviceToHost), "grad");
+  }
+  if (dsq) {
+    CK(cudaMemcpy(dsq, g->delsq + index, sizeof(double),
+		  cudaMemcpyDeviceToHost), "delsq");
+  }
+  return LUDWIG_GB_OK;
+}
+
+/* src/symmetric.c:285-300 */
+static int symm_fed(fe_t * base, int index, double * fed) {
+  fe_symm_t * fe = (fe_symm_t *) base;
+  double phi, g[3];
+  int rc = site_get(fe->phi, 0, index, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, index, g, NULL);
+  if (rc) return rc;
+  *fed = (0.5*fe->param.a + 0.25*fe->param.b*phi*phi)*phi*phi
+    + 0.5*fe->param.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
+  return LUDWIG_GB_OK;
+}
+
+/* src/symmetric.c:308-320 */
+static int symm_mu(fe_t * base, int index, double * mu) {
+  fe_symm_t * fe = (fe_symm_t *) base;
+  double phi, g[3], dsq;
+  int rc = site_get(fe->phi, 0, index, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, index, g, &dsq);
+  if (rc) return rc;
+  *mu = fe->param.a*phi + fe->param.b*phi*phi*phi - fe->param.kappa*dsq;
+  return LUDWIG_GB_OK;
+}
+
+/* src/symmetric.c:334-365 */
+static int symm_str(fe_t * base, int index, double s[3][3]) {
+  fe_symm_t * fe = (fe_symm_t *) base;
+  double phi, g[3], dsq;
+  int rc = site_get(fe->phi, 0, index, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, index, g, &dsq);
+  if (rc) return rc;
+  double kappa = fe->param.kappa;
+  double p0 = 0.5*fe->param.a*phi*phi + 0.75*fe->param.b*phi*phi*phi*phi
+    - kappa*phi*dsq - 0.5*kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      double dab = (ia == ib);
+      s[ia][ib] = p0*dab + kappa*g[ia]*g[ib];
+    }
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int symm_free(fe_t * base) { return fe_symm_free((fe_symm_t *) base); }
+static int symm_target(fe_t * base, fe_t ** t) { *t = base; return 0; }
+
+static const fe_vt_t fe_symm_vt_ = {
+  symm_free, symm_target, symm_fed, symm_mu, symm_str, symm_str, NULL, NULL
+};
+
+int fe_symm_create(pe_t * pe, cs_t * cs, field_t * phi, field_grad_t * dphi,
+		   fe_symm_t ** p) {
+  (void) pe; (void) cs;
+  if (phi == NULL || dphi == NULL || p == NULL || phi->nf != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_symm_create");
+  }
+  fe_symm_t * fe = (fe_symm_t *) calloc(1, sizeof(fe_symm_t));
+  if (fe == NULL) return err_set(LUDWIG_GB_ENOMEM, "fe_symm_create");
+  fe->super.id = FE_SYMMETRIC;
+  fe->super.func = &fe_symm_vt_;
+  /* Defaults of src/symmetric.c:40-42 */
+  fe->param.a = -0.003125;
+  fe->param.b = +0.003125;
+  fe->param.kappa = +0.002;
+  fe->phi = phi;
+  fe->dphi = dphi;
+  *p = fe;
+  return LUDWIG_GB_OK;
+}
+
+int fe_symm_free(fe_symm_t * fe) { free(fe); return LUDWIG_GB_OK; }
+
+int fe_symm_param_set(fe_symm_t * fe, fe_symm_param_t values) {
+  if (fe == NULL) return err_set(LUDWIG_GB_EINVAL, "fe_symm_param_set");
+  fe->param = values;
+  return LUDWIG_GB_OK;
+}
+
+int fe_symm_param(fe_symm_t * fe, fe_symm_param_t * values) {
+  *values = fe->param;
+  return LUDWIG_GB_OK;
+}
+
+static int fe_symm_get(fe_t * fe, fe_symm_t ** s) {
+  if (fe == NULL || fe->id != FE_SYMMETRIC) {
+    return err_set(LUDWIG_GB_EINVAL, "symmetric free energy required");
+  }
+  *s = (fe_symm_t *) fe;
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Force: pth_t and phi_force_calculation
+ *****************************************************************************/
+
+struct pth_s {
+  cs_t * cs;
+  int method;
+  double * str;
+};
+
+int pth_create(pe_t * pe, cs_t * cs, int method, pth_t ** p) {
+  (void) pe;
+  if (cs == NULL || p == NULL ||
+      (method != FE_FORCE_METHOD_NO_FORCE &&
+       method != FE_FORCE_METHOD_STRESS_DIVERGENCE)) {
+    return err_set(LUDWIG_GB_EINVAL, "pth_create: no_force or "
+		   "stress_divergence");
+  }
+  pth_t * pth = (pth_t *) calloc(1, sizeof(pth_t));
+  if (pth == NULL) return err_set(LUDWIG_GB_ENOMEM, "pth_create");
+  pth->cs = cs;
+  pth->method = method;
+  *p = pth;
+  return LUDWIG_GB_OK;
+}
+
+int pth_free(pth_t * pth) {
+  if (pth) { dev_free(pth->str); free(pth); }
+  return LUDWIG_GB_OK;
+}
+
+int pth_stress_compute(pth_t * pth, fe_t * fe) {
+  fe_symm_t * s = NULL;
+  int rc = fe_symm_get(fe, &s);
+  if (rc) return rc;
+  if (s->phi->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "pth_stress_compute: FP64 only");
+  }
+  if (pth->str == NULL) {
+    rc = dev_alloc((void **) &pth->str, 9*(size_t) pth->cs->d.nsites
+		   *sizeof(double), "pth");
+    if (rc) return rc;
+  }
+  rc = grad_alloc(s->dphi);
+  if (rc) return rc;
+  lgbk_symm_t sp = {s->param.a, s->param.b, s->param.kappa};
+  CK(lgbk_symm_stress_f64(&pth->cs->d, &sp, (const double *) s->phi->data,
+			  s->dphi->grad, s->dphi->delsq, pth->str, stream_),
+     "stress");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int pth_to_host(pth_t * pth, double * str) {
+  if (pth == NULL || pth->str == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "pth_to_host: stress not computed");
+  }
+  return copy_to_host(LUDWIG_GB_FP64, 9*pth->cs->d.nsites, pth->str, str);
+}
+
+/* src/phi_force.c:74-140, stress divergence, fluid only */
+int phi_force_calculation(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			  wall_t * wall, pth_t * pth, fe_t * fe, map_t * map,
+			  field_t * phi, hydro_t * hydro) {
+  (void) pe; (void) cs; (void) map; (void) phi;
+  if (pth == NULL) return err_set(LUDWIG_GB_EINVAL, "pth NULL");
+  if (le != NULL || wall != NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "walls and Lees-Edwards not supported");
+  }
+  if (hydro == NULL) return LUDWIG_GB_OK;
+  if (pth->method == FE_FORCE_METHOD_NO_FORCE) return LUDWIG_GB_OK;
+  if (hydro->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_force_calculation: FP64 only");
+  }
+  int rc = pth_stress_compute(pth, fe);
+  if (rc) return rc;
+  CK(lgbk_force_div_f64(&pth->cs->d, pth->str, (double *) hydro->force,
+			stream_), "force");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Cahn-Hilliard
+ *****************************************************************************/
+
+struct phi_ch_s {
+  cs_t * cs;
+  phi_ch_info_t info;
+  double * flux;               /* fw, fe, fy, fz */
+};
+
+int phi_ch_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		  const phi_ch_info_t * info, phi_ch_t ** pch) {
+  (void) pe;
+  if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
+  if (cs == NULL || pch == NULL) return err_set(LUDWIG_GB_EINVAL, "phi_ch");
+  if (info && (info->conserve != 0 || info->noise != 0)) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_ch: conserve 0, noise 0 only");
+  }
+  phi_ch_t * p = (phi_ch_t *) calloc(1, sizeof(phi_ch_t));
+  if (p == NULL) return err_set(LUDWIG_GB_ENOMEM, "phi_ch_create");
+  p->cs = cs;
+  if (info) p->info = *info;
+  *pch = p;
+  return LUDWIG_GB_OK;
+}
+
+int phi_ch_free(phi_ch_t * p) {
+  if (p) { dev_free(p->flux); free(p); }
+  return LUDWIG_GB_OK;
+}
+
+/* src/phi_cahn_hilliard.c:213-288 */
+int phi_cahn_hilliard(phi_ch_t * pch, fe_t * fe, field_t * phi,
+		      hydro_t * hydro, map_t * map, noise_t * noise) {
+  fe_symm_t * s = NULL;
+  int rc = fe_symm_get(fe, &s);
+  if (rc) return rc;
+  if (pch == NULL || phi == NULL || phi->nf != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_cahn_hilliard");
+  }
+  if (noise != NULL) return err_set(LUDWIG_GB_EINVAL, "noise not supported");
+  if (phi->prec != LUDWIG_GB_FP64 || (hydro && hydro->prec != LUDWIG_GB_FP64)) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_cahn_hilliard: FP64 only");
+  }
+  physics_t * ph = NULL;
+  if ((rc = phys_get(&ph))) return rc;
+
+  const lgbk_dims_t * d = &phi->cs->d;
+  size_t N = (size_t) d->nsites;
+  if (pch->flux == NULL) {
+    rc = dev_alloc((void **) &pch->flux, 4*N*sizeof(double), "flux");
+    if (rc) return rc;
+  }
+  /* mu uses the gradients last computed by field_grad_compute(), as the
+   * reference's fe_symm_mu reads fe->dphi (src/symmetric.c:308-320) */
+  if (s->dphi->delsq == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "phi_cahn_hilliard: call "
+		   "field_grad_compute() first");
+  }
+
+  double * fw = pch->flux, * fe_ = fw + N, * fy = fw + 2*N, * fz = fw + 3*N;
+  if (hydro) {
+    CK(lgbk_advect_upwind_f64(d, 1, (const double *) phi->data,
+			      (const double *) hydro->u, fw, fe_, fy, fz,
+			      stream_), "advect");
+  }
+  else {
+    CK(cudaMemsetAsync(pch->flux, 0, 4*N*sizeof(double), stream_), "zero");
+  }
+  lgbk_symm_t sp = {s->param.a, s->param.b, s->param.kappa};
+  CK(lgbk_ch_flux_mu_f64(d, &sp, ph->mobility, (const double *) phi->data,
+			 s->dphi->delsq, fw, fe_, fy, fz, stream_), "flux_mu");
+  CK(lgbk_flux_no_normal_f64(d, 1, map_dev(map), fw, fe_, fy, fz, stream_),
+     "no_flux");
+  CK(lgbk_ch_update_f64(d, fw, fe_, fy, fz, (double *) phi->data, stream_),
+     "update");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Collision and propagation
+ *****************************************************************************/
+
+/* src/collision.c:1163-1246, src/collision.c:1906-1958 */
+static int collide_param(lb_t * lb, lgbk_collide_t * cp) {
+  physics_t * ph = NULL;
+  int rc = phys_get(&ph);
+  if (rc) return rc;
+  const double cs2 = (1.0/3.0);
+  double rho0 = ph->rho0;
+  double rtau_shear = 1.0/(0.5 + ph->eta_shear / (rho0*cs2));
+  double rtau_bulk = 1.0/(0.5 + ph->eta_bulk / (rho0*cs2));
+  memset(cp, 0, sizeof(*cp));
+  cp->rtau_shear = rtau_shear;
+  cp->rtau_bulk = rtau_bulk;
+  for (int p = 0; p < NVEL; p++) cp->rtau_ghost[p] = 1.0;
+  if (lb->nrelax == LB_RELAXATION_BGK) {
+    cp->rtau_bulk = rtau_shear;
+    for (int p = 0; p < NVEL; p++) cp->rtau_ghost[p] = rtau_shear;
+  }
+  if (lb->nrelax == LB_RELAXATION_TRT) {
+    double tau = ph->eta_shear / (rho0*cs2);
+    double rtau = 0.5 + 2.0*tau/(tau + 3.0/8.0);
+    if (rtau > 2.0) rtau = 2.0;
+    cp->rtau_ghost[10] = rtau_shear;
+    cp->rtau_ghost[14] = rtau_shear;
+    cp->rtau_ghost[18] = rtau_shear;
+    cp->rtau_ghost[11] = cp->rtau_ghost[12] = cp->rtau_ghost[13] = rtau;
+    cp->rtau_ghost[15] = cp->rtau_ghost[16] = cp->rtau_ghost[17] = rtau;
+  }
+  cp->ghosts_zero = 1;
+  for (int p = 10; p < NVEL; p++) {
+    if (cp->rtau_ghost[p] != 1.0) cp->ghosts_zero = 0;
+  }
+  for (int i = 0; i < 3; i++) cp->force_global[i] = ph->fbody[i];
+  return LUDWIG_GB_OK;
+}
+
+int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
+	       fe_t * fe, visc_t * visc) {
+  (void) fe;
+  if (hydro == NULL) return LUDWIG_GB_OK;
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_collide: lb NULL");
+  if (noise != NULL || visc != NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_collide: noise/visc not supported");
+  }
+  if (lb->prec != LUDWIG_GB_FP64 || hydro->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_collide: FP64 objects only");
+  }
+  lgbk_collide_t cp;
+  int rc = collide_param(lb, &cp);
+  if (rc) return rc;
+  if ((rc = lb_materialise(lb))) return rc;
+  CK(lgbk_collide_f64(&lb->cs->d, &cp, map_dev(map), (double *) lb->f,
+		      (const double *) hydro->force, (double *) hydro->rho,
+		      (double *) hydro->u, stream_), "collide");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int lb_propagation(lb_t * lb) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_propagation");
+  int rc = lb_materialise(lb);
+  if (rc) return rc;
+  lb->pending = 1;
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Fused step with CUDA-graph replay
+ *****************************************************************************/
+
+typedef struct graph_cache_s {
+  lgbk_binary_args_t args;     /* arguments of the first step of the pair */
+  int prec;
+  int xchunk, ty;
+  lgbk_dims_t d;
+  cudaGraphExec_t exec;
+  int valid;
+} graph_cache_t;
+
+static graph_cache_t gcache_[2];
+
+static int binary_args(lb_t * lb, field_t * phi, hydro_t * hydro,
+		       map_t * map, fe_t * fe, lgbk_binary_args_t * a) {
+  fe_symm_t * s = NULL;
+  physics_t * ph = NULL;
+  int rc = fe_symm_get(fe, &s);
+  if (rc == 0) rc = phys_get(&ph);
+  if (rc) return rc;
+  if (lb == NULL || phi == NULL || hydro == NULL || phi->nf != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "binary_step: lb, phi, hydro required");
+  }
+  int fp = (lb->prec == LUDWIG_GB_FP64);
+  if (fp != (phi->prec == LUDWIG_GB_FP64) ||
+      fp != (hydro->prec == LUDWIG_GB_FP64)) {
+    return err_set(LUDWIG_GB_EINVAL, "binary_step: lb, phi and hydro must "
+		   "be all FP64 or all reduced precision");
+  }
+  if (lb->cs->d.nsites != phi->cs->d.nsites ||
+      lb->cs->d.nsites != hydro->cs->d.nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "binary_step: lattice mismatch");
+  }
+  memset(a, 0, sizeof(*a));
+  if ((rc = collide_param(lb, &a->cp))) return rc;
+  if (lb->prec != LUDWIG_GB_FP64 && !a->cp.ghosts_zero) {
+    return err_set(LUDWIG_GB_EINVAL, "reduced precision: M10 only");
+  }
+  a->f_in = lb->f;       a->f_out = lb->fprime;
+  a->phi_in = phi->data; a->phi_out = phi->data2;
+  a->u_in = hydro->u;    a->u_out = hydro->u2;
+  a->rho_out = hydro->rho;
+  a->force_out = NULL;
+  a->status = map_dev(map);
+  a->mobility = ph->mobility;
+  a->rho0 = lb->rho0;
+  a->fscale = lb->fscale;
+  a->fe.a = s->param.a; a->fe.b = s->param.b; a->fe.kappa = s->param.kappa;
+  return LUDWIG_GB_OK;
+}
+
+static void binary_swap(lb_t * lb, field_t * phi, hydro_t * hydro) {
+  void * t;
+  lb_swap(lb);
+  t = phi->data; phi->data = phi->data2; phi->data2 = t;
+  t = hydro->u; hydro->u = hydro->u2; hydro->u2 = t;
+}
+
+static int pair_graph(const lgbk_binary_args_t * a, int prec,
+		      const lgbk_dims_t * d, cudaGraphExec_t * exec) {
+  graph_cache_t * slot = NULL;
+  for (int i = 0; i < 2; i++) {
+    graph_cache_t * g = gcache_ + i;
+    if (g->valid && g->prec == prec && g->xchunk == tune_xchunk_ &&
+	g->ty == tune_ty_ && memcmp(&g->d, d, sizeof(*d)) == 0 &&
+	memcmp(&g->args, a, sizeof(*a)) == 0) {
+      *exec = g->exec;
+      return LUDWIG_GB_OK;
+    }
+  }
+  /* replace the older slot */
+  slot = gcache_[0].valid ? (gcache_[1].valid ? gcache_ : gcache_ + 1)
+                          : gcache_;
+  if (slot->valid) {
+    cudaGraphExecDestroy(slot->exec);
+    slot->valid = 0;
+  }
+  lgbk_binary_args_t b = *a;
+  b.f_in = a->f_out;     b.f_out = (void *) a->f_in;
+  b.phi_in = a->phi_out; b.phi_out = (void *) a->phi_in;
+  b.u_in = a->u_out;     b.u_out = (void *) a->u_in;
+
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed),
+     "BeginCapture");
+  int rc1 = lgbk_binary_step(d, prec, a, tune_xchunk_, tune_ty_, stream_);
+  int rc2 = lgbk_binary_step(d, prec, &b, tune_xchunk_, tune_ty_, stream_);
+  int rc3 = cudaStreamEndCapture(stream_, &graph);
+  if (rc1 || rc2 || rc3) {
+    return cuda_check(rc1 ? rc1 : (rc2 ? rc2 : rc3), "graph capture");
+  }
+  int rc = cudaGraphInstantiate(&slot->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (rc) return cuda_check(rc, "cudaGraphInstantiate");
+  slot->args = *a;
+  slot->prec = prec;
+  slot->d = *d;
+  slot->xchunk = tune_xchunk_;
+  slot->ty = tune_ty_;
+  slot->valid = 1;
+  *exec = slot->exec;
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				map_t * map, fe_t * fe, int nsteps) {
+  lgbk_binary_args_t a;
+  int rc;
+  if (nsteps < 0) return err_set(LUDWIG_GB_EINVAL, "nsteps < 0");
+  if ((rc = binary_args(lb, phi, hydro, map, fe, &a))) return rc;
+  if ((rc = lb_unstream(lb))) return rc;
+  a.f_in = lb->f;
+  a.f_out = lb->fprime;
+
+  const lgbk_dims_t * d = &lb->cs->d;
+  int npair = nsteps/2;
+  if (npair > 0) {
+    cudaGraphExec_t exec = NULL;
+    if ((rc = pair_graph(&a, lb->prec, d, &exec))) return rc;
+    for (int k = 0; k < npair; k++) {
+      CK(cudaGraphLaunch(exec, stream_), "cudaGraphLaunch");
+    }
+  }
+  if (nsteps % 2) {
+    CK(lgbk_binary_step(d, lb->prec, &a, tune_xchunk_, tune_ty_, stream_),
+       "binary_step");
+    binary_swap(lb, phi, hydro);
+  }
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_binary_step(lb_t * lb, field_t * phi, hydro_t * hydro,
+			  map_t * map, fe_t * fe, int nsteps) {
+  int rc = ludwig_gb_binary_step_async(lb, phi, hydro, map, fe, nsteps);
+  if (rc) return rc;
+  return ludwig_gb_sync();
+}
+
+/*****************************************************************************
+ *  Statistics
+ *****************************************************************************/
+
+int stats_field_q(field_t * field, int n, double out[5]) {
+  if (field == NULL || n < 0 || n >= field->nf || out == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "stats_field_q");
+  }
+  double * scr = NULL, r[4];
+  int rc = red_scratch(&scr);
+  if (rc) return rc;
+  const lgbk_dims_t * d = &field->cs->d;
+  const char * a = (const char *) field->data
+    + (size_t) n*d->nsites*field_size(field->prec);
+  CK(lgbk_field_stats(d, field_kprec(field->prec), a, scr, r, stream_),
+     "field_stats");
+  double vol = (double) d->nsites;
+  double rvol = 1.0/vol;
+  out[0] = r[0];
+  out[1] = rvol*r[0];
+  out[2] = rvol*r[1] - out[1]*out[1];
+  out[3] = r[2];
+  out[4] = r[3];
+  if (!isfinite(r[0]) || !isfinite(r[1])) {
+    return err_set(LUDWIG_GB_ENOTFINITE, "stats_field_q: NaN or Inf");
+  }
+  return LUDWIG_GB_OK;
+}
+
+int stats_distribution(lb_t * lb, double out[4]) {
+  if (lb == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
+  double * scr = NULL, r[6];
+  int rc = red_scratch(&scr);
+  if (rc) return rc;
+  const lgbk_dims_t * d = &lb->cs->d;
+  /* Streaming only permutes values: the sums are the same either way. */
+  CK(lgbk_dist_moments(d, lb->prec, lb->f, lb->fscale, scr, r, stream_),
+     "dist_moments");
+  out[0] = r[0];
+  if (lb->prec != LUDWIG_GB_FP64) out[0] += lb->rho0*(double) d->nsites;
+  out[1] = r[1]; out[2] = r[2]; out[3] = r[3];
+  if (!isfinite(out[0])) {
+    return err_set(LUDWIG_GB_ENOTFINITE, "stats_distribution: NaN or Inf");
+  }
+  return LUDWIG_GB_OK;
+}
+
+int stats_free_energy_symm(fe_symm_t * fe, double * total) {
+  if (fe == NULL || total == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
+  double * scr = NULL, r[3];
+  int rc = red_scratch(&scr);
+  if (rc) return rc;
+  lgbk_symm_t sp = {fe->param.a, fe->param.b, fe->param.kappa};
+  CK(lgbk_symm_fed_total(&fe->phi->cs->d, field_kprec(fe->phi->prec), &sp,
+			 fe->phi->data, scr, r, stream_), "fed");
+  *total = r[0];
+  return LUDWIG_GB_OK;
+}

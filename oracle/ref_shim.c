@@ -21,6 +21,7 @@
  *    ref_shim mode=force    size=.. A= B= K= in=PREFIX out=PREFIX
  *    ref_shim mode=ch       size=.. A= B= K= M= in=PREFIX out=PREFIX
  *    ref_shim mode=step     size=.. A= B= K= M= eta= steps= in=PREFIX out=PREFIX
+ *  Any mode accepts status=FILE (uint8 per site, canonical order; 0 fluid).
  *
  *  The call sequence of mode=run/step follows src/ludwig.c:528-860 for
  *  the symmetric free energy with finite-difference Cahn-Hilliard.
@@ -206,6 +207,26 @@ static void sys_create(int argc, char ** argv, sys_t * s) {
     lb_init_rest_f(s->lb, 1.0);
   }
   wall_create(s->pe, s->cs, s->map, s->lb, &s->wall);
+
+  /* Optional site status (uint8, canonical order), e.g. solid sites */
+  {
+    const char * sp = arg(argc, argv, "status", NULL);
+    if (sp) {
+      FILE * fp = fopen(sp, "rb");
+      unsigned char * st = malloc(nint());
+      if (fp == NULL || fread(st, 1, nint(), fp) != nint()) {
+	fprintf(stderr, "cannot read status %s\n", sp); exit(2);
+      }
+      fclose(fp);
+      for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+	for (int z = 0; z < L[2]; z++) {
+	  map_status_set(s->map, cs_index(s->cs, x+1, y+1, z+1),
+			 st[canon(0,x,y,z)]);
+	}
+      map_halo(s->map);
+      free(st);
+    }
+  }
 }
 
 /* One time step as src/ludwig.c:528-860 (symmetric, FD CH, no colloids). */

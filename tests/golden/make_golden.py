@@ -1,0 +1,101 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+The reference (Ludwig v0.23) is built from its own sources into
+oracle/_ref by oracle/ref.mk, and oracle/ref_shim.c drives its hot-path
+functions (lb_collide, lb_propagation, field_grad_compute,
+phi_force_calculation, phi_cahn_hilliard and the main-loop step of
+src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
+
+Needs the reference sources (only where they are present):
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+SYMM = dict(A=-0.0625, B=0.0625, K=0.04, M=0.3, eta=0.1)
+
+
+def kv(L, **extra):
+    d = dict(size="%d,%d,%d" % L)
+    d.update({k: repr(v) if isinstance(v, float) else str(v)
+              for k, v in extra.items()})
+    return d
+
+
+def run_case(name, L, steps, seed, status=None, keep=("phi", "u", "rho",
+                                                       "force", "f")):
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "out")
+        args = kv(L, mode="run", steps=steps, seed=seed, noise=0.02,
+                  phi0=0.0, out=out, dump0=1, **SYMM)
+        if status is not None:
+            sp = os.path.join(tmp, "status.bin")
+            status.astype(np.uint8).tofile(sp)
+            args["status"] = sp
+        oracle.run_reference(args)
+        res = {"L": np.array(L), "steps": steps, "seed": seed}
+        if status is not None:
+            res["status"] = status.astype(np.uint8)
+        res["phi0"] = oracle.read_array(out + "0", "phi", (1,) + L)
+        ncomp = dict(phi=1, u=3, rho=1, force=3, f=19)
+        for k in keep:
+            res[k] = oracle.read_array(out, k, (ncomp[k],) + L)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print("wrote", name)
+
+
+def op_case(name, mode, L, inputs, outputs, **extra):
+    with tempfile.TemporaryDirectory() as tmp:
+        pin, pout = os.path.join(tmp, "in"), os.path.join(tmp, "out")
+        oracle.write_arrays(pin, **inputs)
+        oracle.run_reference(kv(L, mode=mode, **{"in": pin}, out=pout,
+                                **SYMM, **extra))
+        res = {"L": np.array(L)}
+        res.update({"in_" + k: v for k, v in inputs.items()})
+        for k, nc in outputs.items():
+            res[k] = oracle.read_array(pout, k, (nc,) + L)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print("wrote", name)
+
+
+def main(ref_root):
+    if not oracle.build_reference(ref_root):
+        raise SystemExit("reference sources not found at " + ref_root)
+    rng = np.random.default_rng(20261203)
+
+    run_case("run_8x6x4_s10", (8, 6, 4), 10, 8361235)
+    run_case("run_12x10x8_s50", (12, 10, 8), 50, 77,
+             keep=("phi", "u", "rho", "f"))
+    st = (rng.uniform(size=(10, 8, 6)) < 0.1).astype(np.uint8)
+    run_case("run_map_10x8x6_s12", (10, 8, 6), 12, 4242, status=st,
+             keep=("phi", "u", "f"))
+    run_case("run_32cube_s1000", (32, 32, 32), 1000, 8361235, keep=("phi",))
+
+    L = (6, 5, 4)
+    f = oracle.lb_init_rest(L) * (1.0 + 1e-3 * rng.standard_normal((19,) + L))
+    force = 1e-4 * rng.standard_normal((3,) + L)
+    op_case("collide_6x5x4", "collide", L, dict(f=f, force=force),
+            dict(f=19, rho=1, u=3))
+    L = (5, 4, 3)
+    op_case("propagate_5x4x3", "propagate", L,
+            dict(f=rng.standard_normal((19,) + L)), dict(f=19))
+    L = (6, 5, 4)
+    phi = rng.uniform(-1, 1, (1,) + L)
+    op_case("grad_6x5x4", "grad", L, dict(phi=phi), dict(grad=3, delsq=1))
+    op_case("force_6x5x4", "force", L, dict(phi=phi), dict(force=3))
+    u = 0.01 * rng.standard_normal((3,) + L)
+    op_case("ch_6x5x4", "ch", L, dict(phi=phi, u=u), dict(phi=1))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

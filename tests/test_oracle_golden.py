@@ -1,0 +1,94 @@
+"""The oracle against golden fixtures made by the reference itself.
+
+tests/golden/make_golden.py ran the reference (built from its own sources)
+on these inputs; the oracle must reproduce every value exactly.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+A, B, KAPPA, MOB, ETA = -0.0625, 0.0625, 0.04, 0.3, 0.1
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def L_of(g):
+    return tuple(int(v) for v in g["L"])
+
+
+@pytest.mark.parametrize("name", ["run_8x6x4_s10", "run_12x10x8_s50",
+                                  "run_map_10x8x6_s12"])
+def test_oracle_run_matches_reference(orc, name):
+    g = load(name)
+    L = L_of(g)
+    phi0 = orc.spinodal_init(L, int(g["seed"]), 0.0, 0.02)
+    assert np.array_equal(phi0, g["phi0"])
+    status = g["status"].reshape(-1).copy() if "status" in g else None
+    st = orc.BinaryState(L, orc.lb_init_rest(L), phi0)
+    orc.binary_steps(st, orc.symm_param(A, B, KAPPA), MOB,
+                     orc.collide_param_m10(ETA), int(g["steps"]), status)
+    for k in ("phi", "u", "rho", "force", "f"):
+        if k in g:
+            assert np.array_equal(getattr(st, k), g[k]), k
+
+
+def test_oracle_1000_steps_matches_reference(orc):
+    g = load("run_32cube_s1000")
+    L = L_of(g)
+    st = orc.BinaryState(L, orc.lb_init_rest(L), g["phi0"])
+    orc.binary_steps(st, orc.symm_param(A, B, KAPPA), MOB,
+                     orc.collide_param_m10(ETA), 1000)
+    assert np.array_equal(st.phi, g["phi"])
+
+
+def test_oracle_collide(orc):
+    g = load("collide_6x5x4")
+    L = L_of(g)
+    f, rho, u = orc.collide(L, orc.collide_param_m10(ETA), g["in_f"],
+                            g["in_force"])
+    assert np.array_equal(f, g["f"])
+    assert np.array_equal(rho, g["rho"])
+    assert np.array_equal(u, g["u"])
+
+
+def test_oracle_propagate(orc):
+    g = load("propagate_5x4x3")
+    assert np.array_equal(orc.propagate(L_of(g), g["in_f"]), g["f"])
+
+
+def test_oracle_grad(orc):
+    g = load("grad_6x5x4")
+    grad, delsq = orc.grad_7pt(L_of(g), g["in_phi"])
+    assert np.array_equal(grad, g["grad"])
+    assert np.array_equal(delsq, g["delsq"])
+
+
+def test_oracle_force(orc):
+    g = load("force_6x5x4")
+    force = orc.phi_force(L_of(g), orc.symm_param(A, B, KAPPA), g["in_phi"])
+    assert np.array_equal(force, g["force"])
+
+
+def test_oracle_cahn_hilliard(orc):
+    g = load("ch_6x5x4")
+    phi = orc.cahn_hilliard(L_of(g), orc.symm_param(A, B, KAPPA), MOB,
+                            g["in_phi"], g["in_u"])
+    assert np.array_equal(phi, g["phi"])
+
+
+def test_model_tables(orc):
+    """Mode matrix properties (tests/unit/test_lb_model.c:272-377)."""
+    cv, wv, ma, mi = orc.tables()
+    assert np.allclose(ma @ mi, np.eye(19), atol=1e-14)
+    assert abs(wv.sum() - 1.0) < 1e-15
+    # orthogonality of modes under the weights
+    gram = ma @ np.diag(wv) @ ma.T
+    assert np.allclose(gram - np.diag(np.diag(gram)), 0, atol=1e-14)
+    # opposite velocity exists for each p
+    for p in range(19):
+        assert any((cv[q] == -cv[p]).all() for q in range(19))

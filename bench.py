@@ -1,0 +1,380 @@
+"""Benchmark: D3Q19 symmetric binary fluid at 256^3 on one GB300.
+
+Workload (one "step" = one time step of the main loop of the reference,
+src/ludwig.c:528-860, for the symmetric free energy: 7-point gradients,
+stress-divergence force, upwind + chemical-potential Cahn-Hilliard fluxes,
+forward-Euler phi update, M10 collision with the force, streaming):
+  256^3 periodic, rho0 = 1, eta = 0.1, A = -0.0625, B = 0.0625,
+  kappa = 0.04, M = 0.3, phi0 uniform in [-0.01, 0.01] from the reference's
+  KISS99 per-site seeding (seed 8361235), f at rest equilibrium.
+
+Headline ``value``: MLUPS of the FP32-shifted fused step (float arithmetic,
+f stored as f - w_p rho0), inputs resident in HBM; the state (3.1 GB) is
+larger than L2, so no flush is needed between steps.  Beside it: the FP64
+fused step (bit-identical to the reference's arithmetic) and the FP16-storage
+form, the end-to-end rate through the C ABI with the state in pinned host
+memory, and the CPU oracle on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the box on
+its own GPU ("replicas only": the single-box path has no exchange step);
+``value`` is the total over ranks divided by the slowest rank's time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZE = (256, 256, 256)
+PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
+SEED = 8361235
+METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
+
+# Algorithmic bytes per site update (compulsory traffic of the fused step):
+#   FP64: f 2*19*8 + phi 2*8 + u 2*3*8 = 368;  FP32: 184;  FP16: f 2*19*2 +
+#   phi 2*4 + u 2*12 = 108.  rho (written for output) is not counted.
+ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108}
+
+# DRAM bytes per site of the fused FP32 kernel from ncu
+# (profiles/binary_fused_fp32_ncu.md); None until captured.
+NCU_BYTES_PER_SITE = {"fp32": None, "fp64": None, "fp16": None}
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fp:
+            d = json.load(fp)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU legs: the oracle (a C restatement of the reference), host cores
+# ---------------------------------------------------------------------------
+
+def cpu_run(size, steps, threads):
+    """MLUPS of the oracle on the host cores (test infrastructure)."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle
+    oracle.build()
+    fe = oracle.symm_param(PARAMS["a"], PARAMS["b"], PARAMS["kappa"])
+    cp = oracle.collide_param_m10(PARAMS["eta"])
+    st = oracle.BinaryState(size, oracle.lb_init_rest(size),
+                            oracle.spinodal_init(size, SEED, 0.0, 0.02))
+    oracle.binary_steps(st, fe, PARAMS["mobility"], cp, 1)   # warm-up
+    t0 = time.perf_counter()
+    oracle.binary_steps(st, fe, PARAMS["mobility"], cp, steps)
+    dt = time.perf_counter() - t0
+    n = size[0] * size[1] * size[2]
+    return n * steps / dt / 1e6, dt
+
+
+def reference_arm(args):
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    # Each step: one oracle step on a 256 x 256 x 16 periodic slab, 1/16 of
+    # the 256^3 workload with the same per-site work and a working set
+    # (~0.5 GB) far beyond the caches.
+    sample = (SIZE[0], SIZE[1], 16)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle
+    oracle.build()
+    fe = oracle.symm_param(PARAMS["a"], PARAMS["b"], PARAMS["kappa"])
+    cp = oracle.collide_param_m10(PARAMS["eta"])
+    st = oracle.BinaryState(sample, oracle.lb_init_rest(sample),
+                            oracle.spinodal_init(sample, SEED, 0.0, 0.02))
+    oracle.binary_steps(st, fe, PARAMS["mobility"], cp, args.warmup)
+    t0 = time.perf_counter()
+    oracle.binary_steps(st, fe, PARAMS["mobility"], cp, args.steps)
+    dt = time.perf_counter() - t0
+    n = sample[0] * sample[1] * sample[2]
+    mlups = n * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": mlups,
+        "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (spinodal phi0, seed %d)" % SEED,
+        "config": {"workload": "symmetric binary fluid 256^3, M10, 7pt, "
+                   "FD Cahn-Hilliard", "size": list(SIZE),
+                   "precision": "fp64"},
+        "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d steps of a 256x256x16 periodic slab "
+                                   "(1/16 of 256^3), oracle C restatement, "
+                                   "OpenMP" % args.steps},
+        "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def make_system(lg, prec):
+    s = lg.BinaryFluid(SIZE, precision=prec, a=PARAMS["a"], b=PARAMS["b"],
+                       kappa=PARAMS["kappa"], mobility=PARAMS["mobility"],
+                       eta=PARAMS["eta"])
+    s.phi.init_spinodal(SEED, 0.0, 0.02)
+    return s
+
+
+def roofline(kind, ms_per_step, nsites, peak, peak_kind):
+    algo = ALGO_BYTES[kind] * nsites
+    achieved = algo / (ms_per_step * 1e-3) / 1e9
+    ncu = NCU_BYTES_PER_SITE.get(kind)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None if ncu is None else ncu * nsites,
+            "algorithmic_bytes": algo,
+            "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+            if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+
+def gpu_arm(args):
+    world, rank, local, pg = dist_setup()
+    import ludwig_gb300 as lg
+    lg.load_library()
+    lg.PE(local)                      # select the device for this rank
+    nsites = SIZE[0] * SIZE[1] * SIZE[2]
+    peak, peak_kind = measured_peaks()
+
+    # --- headline: FP32-shifted -------------------------------------------
+    s32 = make_system(lg, lg.FP32)
+    s32.step(args.warmup)
+    lg.sync()
+    m0 = s32.lb.moments()[0]
+    clocks = Clocks(local)
+    clocks.start()
+    barrier(pg)
+    lg.sync()
+    ms32 = lg.time_binary(s32, args.steps)
+    lg.sync()
+    barrier(pg)
+    clk = clocks.stop()
+    ms32 = max_over_ranks(pg, ms32)
+    m1 = s32.lb.moments()[0]
+    drift32 = abs(m1 - m0) / m0 / args.steps
+    phi_stats32 = s32.phi.stats()
+
+    # --- end to end through the C ABI with host buffers --------------------
+    e2e_steps = max(3, min(args.steps, 20))
+    pinned = lg.PinnedState(s32)
+    lg.time_binary_e2e(s32, pinned, 1)                 # warm-up
+    barrier(pg)
+    ms_e2e = lg.time_binary_e2e(s32, pinned, e2e_steps)
+    barrier(pg)
+    ms_e2e = max_over_ranks(pg, ms_e2e)
+    h2d, d2h = pinned.bytes_in, pinned.bytes_out
+    pinned.close()
+    s32 = None
+
+    # --- FP16 storage -------------------------------------------------------
+    s16 = make_system(lg, lg.FP16)
+    s16.step(args.warmup)
+    lg.sync()
+    ms16 = lg.time_binary(s16, args.steps)
+    s16 = None
+
+    # --- FP64 (reference-exact arithmetic) ---------------------------------
+    k64 = max(2, min(args.steps, 40))
+    s64 = make_system(lg, lg.FP64)
+    s64.step(min(args.warmup, 3))
+    lg.sync()
+    barrier(pg)
+    ms64 = lg.time_binary(s64, k64)
+    barrier(pg)
+    ms64 = max_over_ranks(pg, ms64)
+    s64 = None
+
+    total_sites = sum_over_ranks(pg, nsites)
+    per32 = ms32 / args.steps
+    value = total_sites * args.steps / (ms32 * 1e-3) / 1e6
+    fp64_mlups = total_sites * k64 / (ms64 * 1e-3) / 1e6
+    fp16_mlups = nsites * args.steps / (ms16 * 1e-3) / 1e6 * world
+    e2e = total_sites * e2e_steps / (ms_e2e * 1e-3) / 1e6
+
+    if rank != 0:
+        return 0
+
+    cpu = None
+    try:
+        threads = os.cpu_count() or 1
+        cpu_mlups, cpu_dt = cpu_run(SIZE, 2, threads)
+        cpu = {"value": cpu_mlups, "unit": "MLUPS", "cores": threads,
+               "kind": "port",
+               "sample": "2 steps at 256^3 after 1 warm-up step (%.1f s), "
+                         "oracle C restatement of the reference, OpenMP"
+                         % cpu_dt}
+    except Exception as exc:                          # pragma: no cover
+        cpu = {"value": None, "unit": "MLUPS", "cores": 0, "kind": "port",
+               "sample": "failed: %s" % exc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per32,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: spinodal phi0 in [-0.01,0.01] (KISS99 seed %d), "
+                "f at rest" % SEED,
+        "config": {"workload": "symmetric binary fluid 256^3 periodic, D3Q19 "
+                   "M10, 7-point gradients, stress divergence, FD "
+                   "Cahn-Hilliard (A=-0.0625 B=0.0625 kappa=0.04 M=0.3 "
+                   "eta=0.1)", "size": list(SIZE),
+                   "precision": "fp32-shifted",
+                   "l2": "state larger than L2 (3.1 GB), no flush",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "roofline": roofline("fp32", per32, nsites, peak, peak_kind),
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "how": "per step: f, phi, u H2D from pinned host memory, one "
+                       "fused step, f, phi, u, rho D2H (C ABI)"},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "fp64": {"value": fp64_mlups, "unit": "MLUPS", "steps": k64,
+                 "ms_per_step": ms64 / k64,
+                 "roofline": roofline("fp64", ms64 / k64, nsites, peak,
+                                      peak_kind)},
+        "fp16": {"value": fp16_mlups, "unit": "MLUPS",
+                 "ms_per_step": ms16 / args.steps,
+                 "roofline": roofline("fp16", ms16 / args.steps, nsites, peak,
+                                      peak_kind)},
+        "fp32_over_fp64": value / fp64_mlups,
+        "mass_drift_rel_per_step_fp32": drift32,
+        "phi_stats_fp32": [float(v) for v in phi_stats32],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

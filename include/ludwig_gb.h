@@ -285,6 +285,35 @@ void * ludwig_gb_stream(void);
 int ludwig_gb_tune_set(int xchunk, int tile_y);
 
 /*---------------------------------------------------------------------------
+ * State transfer in the storage format of the objects' precision, for
+ * callers that keep the state in host memory between steps.  Elements:
+ * f 19*nsites (FP64: double; FP32: float f - w_p rho0; FP16: half
+ * (f - w_p rho0)*scale), phi nsites and u 3*nsites (double or float).
+ * f is the carried post-collision state of the fused step.  The copies are
+ * queued on the library's stream (use pinned host memory for speed).
+ *-------------------------------------------------------------------------*/
+int ludwig_gb_state_bytes(lb_t * lb, size_t * f_bytes, size_t * phi_bytes,
+			  size_t * u_bytes);
+int ludwig_gb_state_to_host_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				  void * f, void * phi_h, void * u);
+int ludwig_gb_state_from_host_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				    const void * f, const void * phi_h,
+				    const void * u);
+/* Page-locked host memory */
+int ludwig_gb_host_alloc(size_t bytes, void ** p);
+int ludwig_gb_host_free(void * p);
+
+/* Device time (CUDA events on the library's stream) of nsteps fused steps,
+ * and of nsteps end-to-end steps: state in from host buffers, one fused
+ * step, state (and rho) back to host buffers. */
+int ludwig_gb_time_binary(lb_t * lb, field_t * phi, hydro_t * hydro,
+			  map_t * map, fe_t * fe, int nsteps, double * ms);
+int ludwig_gb_time_binary_e2e(lb_t * lb, field_t * phi, hydro_t * hydro,
+			      map_t * map, fe_t * fe, int nsteps, void * f_h,
+			      void * phi_h, void * u_h, void * rho_h,
+			      double * ms);
+
+/*---------------------------------------------------------------------------
  * Statistics (FP64 accumulation, compensated), src/phi_stats.c:91-140,
  * src/stats_distribution.c:55-120, src/stats_free_energy.c:38
  *-------------------------------------------------------------------------*/

@@ -148,6 +148,16 @@ def _declare(L):
         "ludwig_gb_binary_step": ([_P] * 5 + [ctypes.c_int], ctypes.c_int),
         "ludwig_gb_binary_step_async": ([_P] * 5 + [ctypes.c_int],
                                         ctypes.c_int),
+        "ludwig_gb_state_bytes": ([_P] + [ctypes.POINTER(ctypes.c_size_t)]
+                                  * 3, ctypes.c_int),
+        "ludwig_gb_state_to_host_async": ([_P] * 6, ctypes.c_int),
+        "ludwig_gb_state_from_host_async": ([_P] * 6, ctypes.c_int),
+        "ludwig_gb_host_alloc": ([ctypes.c_size_t, pp], ctypes.c_int),
+        "ludwig_gb_host_free": ([_P], ctypes.c_int),
+        "ludwig_gb_time_binary": ([_P] * 5 + [ctypes.c_int, _D],
+                                  ctypes.c_int),
+        "ludwig_gb_time_binary_e2e": ([_P] * 5 + [ctypes.c_int] + [_P] * 4
+                                      + [_D], ctypes.c_int),
         "stats_field_q": ([_P, ctypes.c_int, _D], ctypes.c_int),
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
@@ -529,3 +539,53 @@ def sync():
 
 def tune(xchunk, tile_y):
     _check(lib().ludwig_gb_tune_set(int(xchunk), int(tile_y)), "tune")
+
+
+class PinnedState:
+    """Page-locked host buffers for the raw state of a BinaryFluid."""
+
+    def __init__(self, system):
+        L = lib()
+        fb, pb, ub = (ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t())
+        _check(L.ludwig_gb_state_bytes(system.lb.ptr, ctypes.byref(fb),
+                                       ctypes.byref(pb), ctypes.byref(ub)),
+               "state_bytes")
+        self.sizes = (fb.value, pb.value, ub.value, pb.value)
+        self.bufs = [_new("ludwig_gb_host_alloc", ctypes.c_size_t(b))
+                     for b in self.sizes]
+        self.bytes_in = fb.value + pb.value + ub.value
+        self.bytes_out = fb.value + pb.value + ub.value + pb.value
+
+    def close(self):
+        for b in self.bufs:
+            lib().ludwig_gb_host_free(b)
+        self.bufs = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def time_binary(system, nsteps):
+    ms = ctypes.c_double()
+    s = system
+    _check(lib().ludwig_gb_time_binary(s.lb.ptr, s.phi.ptr, s.hydro.ptr,
+                                       s.map.ptr, s.fe.ptr, int(nsteps),
+                                       ctypes.byref(ms)), "time_binary")
+    return ms.value
+
+
+def time_binary_e2e(system, pinned, nsteps):
+    ms = ctypes.c_double()
+    s = system
+    L = lib()
+    _check(L.ludwig_gb_state_to_host_async(s.lb.ptr, s.phi.ptr, s.hydro.ptr,
+                                           *pinned.bufs[:3]), "state_to_host")
+    sync()
+    _check(L.ludwig_gb_time_binary_e2e(s.lb.ptr, s.phi.ptr, s.hydro.ptr,
+                                       s.map.ptr, s.fe.ptr, int(nsteps),
+                                       *pinned.bufs, ctypes.byref(ms)),
+           "time_binary_e2e")
+    return ms.value

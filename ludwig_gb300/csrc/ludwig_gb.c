@@ -1355,3 +1355,123 @@ int stats_free_energy_symm(fe_symm_t * fe, double * total) {
   *total = r[0];
   return LUDWIG_GB_OK;
 }
+
+/*****************************************************************************
+ *  Raw state transfer, pinned memory, timing
+ *****************************************************************************/
+
+int ludwig_gb_state_bytes(lb_t * lb, size_t * fb, size_t * pb, size_t * ub) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "state_bytes");
+  size_t n = (size_t) lb->cs->d.nsites;
+  if (fb) *fb = NVEL*n*prec_size(lb->prec);
+  if (pb) *pb = n*field_size(lb->prec);
+  if (ub) *ub = 3*n*field_size(lb->prec);
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_state_to_host_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				  void * f, void * ph, void * u) {
+  size_t fb, pb, ub;
+  if (lb == NULL || phi == NULL || hydro == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "state_to_host");
+  }
+  ludwig_gb_state_bytes(lb, &fb, &pb, &ub);
+  int rc = lb_unstream(lb);
+  if (rc) return rc;
+  if (f)  CK(cudaMemcpyAsync(f, lb->f, fb, cudaMemcpyDeviceToHost, stream_),
+	     "f");
+  if (ph) CK(cudaMemcpyAsync(ph, phi->data, pb, cudaMemcpyDeviceToHost,
+			     stream_), "phi");
+  if (u)  CK(cudaMemcpyAsync(u, hydro->u, ub, cudaMemcpyDeviceToHost,
+			     stream_), "u");
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_state_from_host_async(lb_t * lb, field_t * phi, hydro_t * hydro,
+				    const void * f, const void * ph,
+				    const void * u) {
+  size_t fb, pb, ub;
+  if (lb == NULL || phi == NULL || hydro == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "state_from_host");
+  }
+  ludwig_gb_state_bytes(lb, &fb, &pb, &ub);
+  if (f) {
+    CK(cudaMemcpyAsync(lb->f, f, fb, cudaMemcpyHostToDevice, stream_), "f");
+    lb->pending = 1;
+  }
+  if (ph) CK(cudaMemcpyAsync(phi->data, ph, pb, cudaMemcpyHostToDevice,
+			     stream_), "phi");
+  if (u)  CK(cudaMemcpyAsync(hydro->u, u, ub, cudaMemcpyHostToDevice,
+			     stream_), "u");
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_host_alloc(size_t bytes, void ** p) {
+  if (p == NULL) return err_set(LUDWIG_GB_EINVAL, "host_alloc");
+  if (cudaMallocHost(p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return err_set(LUDWIG_GB_ENOMEM, "cudaMallocHost(%zu)", bytes);
+  }
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_host_free(void * p) {
+  if (p) cudaFreeHost(p);
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_time_binary(lb_t * lb, field_t * phi, hydro_t * hydro,
+			  map_t * map, fe_t * fe, int nsteps, double * ms) {
+  cudaEvent_t e0, e1;
+  int rc;
+  /* settle the state and the graph outside the timed region */
+  if ((rc = lb_unstream(lb))) return rc;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  CK(cudaEventRecord(e0, stream_), "record");
+  rc = ludwig_gb_binary_step_async(lb, phi, hydro, map, fe, nsteps);
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e1, stream_), "record");
+  if (rc == 0) rc = cuda_check(cudaEventSynchronize(e1), "sync");
+  if (rc == 0) {
+    float t = 0.0f;
+    rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int ludwig_gb_time_binary_e2e(lb_t * lb, field_t * phi, hydro_t * hydro,
+			      map_t * map, fe_t * fe, int nsteps, void * f_h,
+			      void * phi_h, void * u_h, void * rho_h,
+			      double * ms) {
+  cudaEvent_t e0, e1;
+  int rc = 0;
+  size_t pb = 0;
+  ludwig_gb_state_bytes(lb, NULL, &pb, NULL);
+  if ((rc = lb_unstream(lb))) return rc;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  CK(cudaEventRecord(e0, stream_), "record");
+  for (int k = 0; rc == 0 && k < nsteps; k++) {
+    rc = ludwig_gb_state_from_host_async(lb, phi, hydro, f_h, phi_h, u_h);
+    if (rc == 0) rc = ludwig_gb_binary_step_async(lb, phi, hydro, map, fe, 1);
+    if (rc == 0) rc = ludwig_gb_state_to_host_async(lb, phi, hydro, f_h,
+						     phi_h, u_h);
+    if (rc == 0 && rho_h) {
+      rc = cuda_check(cudaMemcpyAsync(rho_h, hydro->rho, pb,
+				      cudaMemcpyDeviceToHost, stream_), "rho");
+    }
+  }
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e1, stream_), "record");
+  if (rc == 0) rc = cuda_check(cudaEventSynchronize(e1), "sync");
+  if (rc == 0) {
+    float t = 0.0f;
+    rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}

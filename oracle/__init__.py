@@ -298,3 +298,111 @@ def run_reference(args, threads=1):
     if out.returncode != 0:
         raise RuntimeError("ref_shim failed: " + out.stderr[-2000:])
     return out.stdout
+
+
+# ---------------------------------------------------------------------------
+# Cholesteric liquid crystal
+# ---------------------------------------------------------------------------
+
+NQAB = 5
+
+
+class LcParam(ctypes.Structure):
+    _fields_ = [("a0", ctypes.c_double), ("q0", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("kappa0", ctypes.c_double),
+                ("kappa1", ctypes.c_double), ("xi", ctypes.c_double),
+                ("redshift", ctypes.c_double), ("rredshift", ctypes.c_double),
+                ("epsilon", ctypes.c_double), ("e0", ctypes.c_double * 3),
+                ("coswt", ctypes.c_double), ("amplitude0", ctypes.c_double)]
+
+
+def lc_param(a0=0.01, gamma=3.0, kappa0=0.01, kappa1=0.01, pitch=32.0,
+             xi=0.7, redshift=1.0, amplitude=-0.2):
+    """As fe_lc_param_set (src/blue_phase.c:241-260); no electric field."""
+    p = LcParam()
+    p.a0, p.gamma, p.kappa0, p.kappa1 = a0, gamma, kappa0, kappa1
+    p.q0 = 2.0 * 3.1415926535897932385 / pitch
+    p.xi = xi
+    p.redshift = redshift
+    p.rredshift = 1.0 / redshift
+    p.epsilon = 0.0
+    p.coswt = 1.0
+    p.amplitude0 = amplitude
+    return p
+
+
+def _declare_lc(L):
+    LP = ctypes.POINTER(LcParam)
+    L.orc_lc_mol_field.argtypes = [_I3, LP, _P, _P, _P, _P]
+    L.orc_lc_stress.argtypes = [_I3, LP, _P, _P, _P, _P]
+    L.orc_lc_fed.argtypes = [_I3, LP, _P, _P, _P]
+    L.orc_beris_edw_update.argtypes = [_I3, LP, ctypes.c_double, _U8, _P, _P,
+                                       _P, _P, _P]
+    L.orc_lc_step.argtypes = [_I3, LP, ctypes.c_double,
+                              ctypes.POINTER(CollideParam), _U8, _P, _P, _P,
+                              _P, _P, _P, _P, ctypes.c_int]
+    L.orc_lc_init_o8m.argtypes = [_I3, LP, _P]
+
+
+def lc_lib():
+    L = lib()
+    if not getattr(L, "_lc_declared", False):
+        _declare_lc(L)
+        L._lc_declared = True
+    return L
+
+
+def lc_init_o8m(L, p):
+    q = np.zeros((NQAB,) + tuple(L))
+    lc_lib().orc_lc_init_o8m(_dims(L), ctypes.byref(p), _p(q))
+    return q
+
+
+def lc_fields(L, p, q):
+    """(h[5], stress[9], fed[1]) of a given q."""
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    grad, delsq = grad_7pt(L, q)
+    h = np.zeros((NQAB,) + tuple(L))
+    s = np.zeros((9,) + tuple(L))
+    fed = np.zeros((1,) + tuple(L))
+    Lb = lc_lib()
+    Lb.orc_lc_mol_field(_dims(L), ctypes.byref(p), _p(q), _p(grad), _p(delsq),
+                        _p(h))
+    Lb.orc_lc_stress(_dims(L), ctypes.byref(p), _p(q), _p(grad), _p(delsq),
+                     _p(s))
+    Lb.orc_lc_fed(_dims(L), ctypes.byref(p), _p(q), _p(grad), _p(fed))
+    return h, s, fed
+
+
+def lc_be_update(L, p, gamma_rot, q, u, status=None):
+    q = np.ascontiguousarray(q, dtype=np.float64).copy()
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    grad, delsq = grad_7pt(L, q)
+    work = np.zeros((30,) + tuple(L))
+    lc_lib().orc_beris_edw_update(_dims(L), ctypes.byref(p), float(gamma_rot),
+                                  _u8(status), _p(u), _p(grad), _p(delsq),
+                                  _p(q), _p(work))
+    return q
+
+
+class LcState:
+    def __init__(self, L, f, q, u=None):
+        self.L = tuple(int(v) for v in L)
+        n = self.L
+        self.f = np.ascontiguousarray(f, dtype=np.float64).copy()
+        self.q = np.ascontiguousarray(q, dtype=np.float64).copy()
+        self.u = (np.zeros((3,) + n) if u is None else
+                  np.ascontiguousarray(u, dtype=np.float64).copy())
+        self.rho = np.zeros((1,) + n)
+        self.force = np.zeros((3,) + n)
+        self._fs = np.zeros_like(self.f)
+        self._work = np.zeros((50,) + n)
+
+
+def lc_steps(state, p, gamma_rot, cp, nsteps, status=None):
+    s = state
+    lc_lib().orc_lc_step(_dims(s.L), ctypes.byref(p), float(gamma_rot),
+                         ctypes.byref(cp), _u8(status), _p(s.f), _p(s._fs),
+                         _p(s.q), _p(s.u), _p(s.rho), _p(s.force),
+                         _p(s._work), int(nsteps))
+    return s

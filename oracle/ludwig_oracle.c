@@ -788,3 +788,419 @@ double orc_symm_fed_total(const int L[3], const orc_symm_param_t * fe,
   }
   return orc_klein_total(&k);
 }
+
+/*****************************************************************************
+ *
+ *  Cholesteric liquid crystal (Landau-de Gennes free energy).
+ *
+ *  The per-site formulas follow the loop forms of the reference:
+ *  molecular field src/blue_phase.c:1016-1110 (fe_lc_compute_h),
+ *  free-energy density :309-400 (fe_lc_compute_fed), chiral stress
+ *  :827-930 (fe_lc_compute_stress, with its final minus sign).  The
+ *  reference's device build evaluates the same expressions through
+ *  unrolled forms (:2094-2450), so the two agree to rounding.
+ *
+ *****************************************************************************/
+
+enum {NQAB = 5};
+
+static const int lc_e_[3][3][3] = {
+  {{0, 0, 0}, {0, 0, 1}, {0, -1, 0}},
+  {{0, 0, -1}, {0, 0, 0}, {1, 0, 0}},
+  {{0, 1, 0}, {-1, 0, 0}, {0, 0, 0}}};
+
+static void lc_expand(const double * a, size_t N, size_t i, double t[3][3]) {
+  t[0][0] = a[0*N + i];
+  t[0][1] = a[1*N + i];
+  t[0][2] = a[2*N + i];
+  t[1][0] = t[0][1];
+  t[1][1] = a[3*N + i];
+  t[1][2] = a[4*N + i];
+  t[2][0] = t[0][2];
+  t[2][1] = t[1][2];
+  t[2][2] = 0.0 - t[0][0] - t[1][1];
+}
+
+/* dq[ia][b][c] = d_ia Q_bc from grad[(3*n + ia)] of the 5 components */
+static void lc_expand_grad(const double * g, size_t N, size_t i,
+			   double dq[3][3][3]) {
+  for (int ia = 0; ia < 3; ia++) {
+    dq[ia][0][0] = g[(3*0 + ia)*N + i];
+    dq[ia][0][1] = g[(3*1 + ia)*N + i];
+    dq[ia][0][2] = g[(3*2 + ia)*N + i];
+    dq[ia][1][0] = dq[ia][0][1];
+    dq[ia][1][1] = g[(3*3 + ia)*N + i];
+    dq[ia][1][2] = g[(3*4 + ia)*N + i];
+    dq[ia][2][0] = dq[ia][0][2];
+    dq[ia][2][1] = dq[ia][1][2];
+    dq[ia][2][2] = 0.0 - dq[ia][0][0] - dq[ia][1][1];
+  }
+}
+
+static void lc_h_site(const orc_lc_param_t * p, double q[3][3],
+		      double dq[3][3][3], double dsq[3][3], double h[3][3]) {
+  const double r3 = (1.0/3.0);
+  const double gamma = p->gamma;
+  double q0 = p->q0*p->rredshift;
+  double kappa0 = p->kappa0*p->redshift*p->redshift;
+  double kappa1 = p->kappa1*p->redshift*p->redshift;
+  double q2 = 0.0, eq = 0.0, e2 = 0.0;
+
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) q2 += q[ia][ib]*q[ia][ib];
+
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      double sum = 0.0;
+      double dab = (ia == ib);
+      for (int ic = 0; ic < 3; ic++) sum += q[ia][ic]*q[ib][ic];
+      h[ia][ib] = -p->a0*(1.0 - r3*gamma)*q[ia][ib]
+	+ p->a0*gamma*(sum - r3*q2*dab)
+	- p->a0*gamma*q2*q[ia][ib];
+    }
+  }
+
+  for (int ib = 0; ib < 3; ib++)
+    for (int ic = 0; ic < 3; ic++)
+      for (int ia = 0; ia < 3; ia++) eq += lc_e_[ib][ic][ia]*dq[ib][ic][ia];
+
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      double sum = 0.0;
+      double dab = (ia == ib);
+      for (int ic = 0; ic < 3; ic++) {
+	for (int id = 0; id < 3; id++) {
+	  sum += (lc_e_[ia][ic][id]*dq[ic][ib][id]
+		  + lc_e_[ib][ic][id]*dq[ic][ia][id]);
+	}
+      }
+      h[ia][ib] += kappa0*dsq[ia][ib]
+	- 2.0*kappa1*q0*sum + 4.0*r3*kappa1*q0*eq*dab
+	- 4.0*kappa1*q0*q0*q[ia][ib];
+    }
+  }
+
+  for (int ia = 0; ia < 3; ia++) {
+    double ea = p->e0[ia]*p->coswt;
+    e2 += ea*ea;
+  }
+  for (int ia = 0; ia < 3; ia++) {
+    double ea = p->e0[ia]*p->coswt;
+    for (int ib = 0; ib < 3; ib++) {
+      double eb = p->e0[ib]*p->coswt;
+      double dab = (ia == ib);
+      h[ia][ib] += p->epsilon*(ea*eb - r3*dab*e2);
+    }
+  }
+}
+
+static double lc_fed_site(const orc_lc_param_t * p, double q[3][3],
+			  double dq[3][3][3]) {
+  const double r3 = 1.0/3.0;
+  const double gamma = p->gamma;
+  double q0 = p->q0*p->rredshift;
+  double kappa0 = p->kappa0*p->redshift*p->redshift;
+  double kappa1 = p->kappa1*p->redshift*p->redshift;
+  double q2 = 0.0, q3 = 0.0, dq0 = 0.0, dq1 = 0.0, efield = 0.0;
+
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) q2 += q[ia][ib]*q[ia][ib];
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++)
+      for (int ic = 0; ic < 3; ic++) q3 += q[ia][ib]*q[ib][ic]*q[ia][ic];
+  for (int ia = 0; ia < 3; ia++) {
+    double sum = 0.0;
+    for (int ib = 0; ib < 3; ib++) sum += dq[ib][ia][ib];
+    dq0 += sum*sum;
+  }
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      double sum = 0.0;
+      for (int ic = 0; ic < 3; ic++)
+	for (int id = 0; id < 3; id++) sum += lc_e_[ia][ic][id]*dq[ic][ib][id];
+      sum += 2.0*q0*q[ia][ib];
+      dq1 += sum*sum;
+    }
+  }
+  for (int ia = 0; ia < 3; ia++) {
+    double ea = p->e0[ia]*p->coswt;
+    for (int ib = 0; ib < 3; ib++) {
+      double eb = p->e0[ib]*p->coswt;
+      efield += ea*q[ia][ib]*eb;
+    }
+  }
+  return 0.5*p->a0*(1.0 - r3*gamma)*q2 - r3*p->a0*gamma*q3
+    + 0.25*p->a0*gamma*q2*q2 + 0.5*kappa0*dq0 + 0.5*kappa1*dq1
+    - p->epsilon*efield;
+}
+
+static void lc_stress_site(const orc_lc_param_t * p, double q[3][3],
+			   double dq[3][3][3], double h[3][3],
+			   double sth[3][3]) {
+  const double r3 = (1.0/3.0);
+  double q0 = p->q0*p->rredshift;
+  double kappa0 = p->kappa0*p->redshift*p->redshift;
+  double kappa1 = p->kappa1*p->redshift*p->redshift;
+  double p0 = 0.0 - lc_fed_site(p, q, dq);
+  double qh = 0.0;
+
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) qh += q[ia][ib]*h[ia][ib];
+
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      double dab = (ia == ib);
+      sth[ia][ib] = -p0*dab + 2.0*p->xi*(q[ia][ib] + r3*dab)*qh;
+    }
+  }
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      for (int ic = 0; ic < 3; ic++) {
+	double dbc = (ib == ic), dac = (ia == ic);
+	sth[ia][ib] += -p->xi*h[ia][ic]*(q[ib][ic] + r3*dbc)
+	  -p->xi*(q[ia][ic] + r3*dac)*h[ib][ic];
+      }
+    }
+  }
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      for (int ic = 0; ic < 3; ic++) {
+	for (int id = 0; id < 3; id++) {
+	  sth[ia][ib] += - kappa0*dq[ia][ib][ic]*dq[id][ic][id]
+	    - kappa1*dq[ia][ic][id]*dq[ib][ic][id]
+	    + kappa1*dq[ia][ic][id]*dq[ic][ib][id];
+	  for (int ie = 0; ie < 3; ie++) {
+	    sth[ia][ib] += -2.0*kappa1*q0*dq[ia][ic][id]*lc_e_[ib][ic][ie]
+	      *q[id][ie];
+	  }
+	}
+      }
+    }
+  }
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++)
+      for (int ic = 0; ic < 3; ic++)
+	sth[ia][ib] += q[ia][ic]*h[ib][ic] - h[ia][ic]*q[ib][ic];
+
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) sth[ia][ib] = -sth[ia][ib];
+}
+
+void orc_lc_mol_field(const int L[3], const orc_lc_param_t * p,
+		      const double * q, const double * grad,
+		      const double * delsq, double * h) {
+  size_t N = nsites(L);
+  #pragma omp parallel for
+  for (size_t i = 0; i < N; i++) {
+    double qs[3][3], dq[3][3][3], dsq[3][3], hs[3][3];
+    lc_expand(q, N, i, qs);
+    lc_expand_grad(grad, N, i, dq);
+    lc_expand(delsq, N, i, dsq);
+    lc_h_site(p, qs, dq, dsq, hs);
+    h[0*N + i] = hs[0][0]; h[1*N + i] = hs[0][1]; h[2*N + i] = hs[0][2];
+    h[3*N + i] = hs[1][1]; h[4*N + i] = hs[1][2];
+  }
+}
+
+void orc_lc_stress(const int L[3], const orc_lc_param_t * p,
+		   const double * q, const double * grad,
+		   const double * delsq, double * pth) {
+  size_t N = nsites(L);
+  #pragma omp parallel for
+  for (size_t i = 0; i < N; i++) {
+    double qs[3][3], dq[3][3][3], dsq[3][3], hs[3][3], s[3][3];
+    lc_expand(q, N, i, qs);
+    lc_expand_grad(grad, N, i, dq);
+    lc_expand(delsq, N, i, dsq);
+    lc_h_site(p, qs, dq, dsq, hs);
+    lc_stress_site(p, qs, dq, hs, s);
+    for (int ia = 0; ia < 3; ia++)
+      for (int ib = 0; ib < 3; ib++) pth[(3*ia + ib)*N + i] = s[ia][ib];
+  }
+}
+
+void orc_lc_fed(const int L[3], const orc_lc_param_t * p, const double * q,
+		const double * grad, double * fed) {
+  size_t N = nsites(L);
+  #pragma omp parallel for
+  for (size_t i = 0; i < N; i++) {
+    double qs[3][3], dq[3][3][3];
+    lc_expand(q, N, i, qs);
+    lc_expand_grad(grad, N, i, dq);
+    fed[i] = lc_fed_site(p, qs, dq);
+  }
+}
+
+/*****************************************************************************
+ *
+ *  orc_beris_edw_update
+ *
+ *  src/blue_phase_beris_edwards.c:266-289 (driver): upwind advective
+ *  fluxes of the 5 components (src/advection.c:538-629), no-normal-flux
+ *  mask, molecular field, then the site update of :538-840:
+ *    W_ab = d_b u_a (centred), made traceless; D, Omega its symmetric and
+ *    antisymmetric parts;
+ *    S = -2 xi (Q + I/3) tr(QW) + (xi D + Omega)(Q + I/3)
+ *        + (Q + I/3)(xi D - Omega);
+ *    Q += S + Gamma H - div(flux)   (dt = 1, no noise)
+ *  at fluid sites.  u may be NULL (no hydrodynamics).
+ *
+ *****************************************************************************/
+
+void orc_beris_edw_update(const int L[3], const orc_lc_param_t * p,
+			  double gamma_rot, const uint8_t * status,
+			  const double * u, const double * grad,
+			  const double * delsq, double * q, double * work) {
+  size_t N = nsites(L);
+  double * fw = work, * fe = work + 5*N, * fy = work + 10*N;
+  double * fz = work + 15*N;
+  double * h = work + 20*N;                     /* 5 N */
+
+  if (u) {
+    orc_advect_upwind(L, NQAB, q, u, fw, fe, fy, fz);
+    orc_flux_no_normal(L, NQAB, status, fw, fe, fy, fz);
+  }
+  orc_lc_mol_field(L, p, q, grad, delsq, h);
+
+  {
+    double * qn = work + 25*N;                   /* 5 N */
+    const double r3 = (1.0/3.0);
+    const double dt = 1.0;
+
+    #pragma omp parallel for
+    for (int x = 0; x < L[0]; x++) {
+      for (int y = 0; y < L[1]; y++) {
+	for (int z = 0; z < L[2]; z++) {
+	  size_t i = site(L, x, y, z);
+	  double qs[3][3], w[3][3] = {{0}}, d[3][3], om[3][3], s[3][3] = {{0}};
+	  lc_expand(q, N, i, qs);
+	  int fluid = (status == NULL || status[i] == 0);
+
+	  if (u) {
+	    size_t im = site(L, x-1, y, z), ip = site(L, x+1, y, z);
+	    double tr, trace_qw = 0.0;
+	    if (fluid) {
+	      for (int ia = 0; ia < 3; ia++)
+		w[ia][0] = 0.5*(u[ia*N + ip] - u[ia*N + im]);
+	    }
+	    im = site(L, x, y-1, z); ip = site(L, x, y+1, z);
+	    for (int ia = 0; ia < 3; ia++)
+	      w[ia][1] = 0.5*(u[ia*N + ip] - u[ia*N + im]);
+	    im = site(L, x, y, z-1); ip = site(L, x, y, z+1);
+	    for (int ia = 0; ia < 3; ia++)
+	      w[ia][2] = 0.5*(u[ia*N + ip] - u[ia*N + im]);
+
+	    tr = r3*(w[0][0] + w[1][1] + w[2][2]);
+	    w[0][0] -= tr; w[1][1] -= tr; w[2][2] -= tr;
+
+	    for (int ia = 0; ia < 3; ia++) {
+	      for (int ib = 0; ib < 3; ib++) {
+		trace_qw += qs[ia][ib]*w[ib][ia];
+		d[ia][ib]  = 0.5*(w[ia][ib] + w[ib][ia]);
+		om[ia][ib] = 0.5*(w[ia][ib] - w[ib][ia]);
+	      }
+	    }
+	    for (int ia = 0; ia < 3; ia++) {
+	      for (int ib = 0; ib < 3; ib++) {
+		double dab = (ia == ib);
+		s[ia][ib] = -2.0*p->xi*(qs[ia][ib] + r3*dab)*trace_qw;
+		for (int id = 0; id < 3; id++) {
+		  double ddb = (id == ib), dad = (ia == id);
+		  s[ia][ib] += (p->xi*d[ia][id] + om[ia][id])
+		    *(qs[id][ib] + r3*ddb)
+		    + (qs[ia][id] + r3*dad)*(p->xi*d[id][ib] - om[id][ib]);
+		}
+	      }
+	    }
+	  }
+
+	  {
+	    static const int ca[NQAB] = {0, 0, 0, 1, 1};
+	    static const int cb[NQAB] = {0, 1, 2, 1, 2};
+	    size_t ij = site(L, x, y-1, z), ik = site(L, x, y, z-1);
+	    for (int n = 0; n < NQAB; n++) {
+	      double v = qs[ca[n]][cb[n]];
+	      if (fluid) {
+		double fl = 0.0;
+		if (u) {
+		  fl = - fe[n*N + i] + fw[n*N + i]
+		    - fy[n*N + i] + fy[n*N + ij]
+		    - fz[n*N + i] + fz[n*N + ik];
+		}
+		v += dt*(s[ca[n]][cb[n]] + 0.0 + gamma_rot*h[n*N + i] + fl);
+	      }
+	      qn[n*N + i] = v;
+	    }
+	  }
+	}
+      }
+    }
+    memcpy(q, qn, 5*N*sizeof(double));
+  }
+}
+
+/*****************************************************************************
+ *
+ *  orc_lc_step
+ *
+ *  src/ludwig.c:528-860 for the cholesteric (no colloids, walls or
+ *  planes): q halo, q gradients, stress divergence force, u halo,
+ *  Beris-Edwards update, u zero, collision, halo, propagation.
+ *  work >= 45 N doubles.
+ *
+ *****************************************************************************/
+
+void orc_lc_step(const int L[3], const orc_lc_param_t * p, double gamma_rot,
+		 const orc_collide_param_t * cp, const uint8_t * status,
+		 double * f, double * fscratch, double * q, double * u,
+		 double * rho, double * force, double * work, int nsteps) {
+  size_t N = nsites(L);
+  double * grad = work;                 /* 15 N */
+  double * delsq = work + 15*N;         /*  5 N */
+  double * pth = work + 20*N;           /*  9 N; reused by the update */
+  double * bew = work + 20*N;           /* 30 N for the update */
+
+  tables_init();
+
+  for (int step = 0; step < nsteps; step++) {
+    memset(force, 0, 3*N*sizeof(double));
+    orc_grad_7pt(L, NQAB, q, grad, delsq);
+    orc_lc_stress(L, p, q, grad, delsq, pth);
+    orc_force_divergence(L, pth, force);
+    orc_beris_edw_update(L, p, gamma_rot, status, u, grad, delsq, q, bew);
+    memset(u, 0, 3*N*sizeof(double));
+    orc_collide_mrt(L, cp, status, f, force, rho, u);
+    orc_propagate(L, f, fscratch);
+    memcpy(f, fscratch, NVEL*N*sizeof(double));
+  }
+}
+
+/* src/blue_phase_init.c:59-132 without rotation; global coordinates are
+ * 1-based */
+
+void orc_lc_init_o8m(const int L[3], const orc_lc_param_t * p, double * q) {
+  size_t N = nsites(L);
+  const double root2 = sqrt(2.0);
+  const double q0 = p->q0, a = p->amplitude0;
+
+  for (int x = 0; x < L[0]; x++) {
+    for (int y = 0; y < L[1]; y++) {
+      for (int z = 0; z < L[2]; z++) {
+	size_t i = site(L, x, y, z);
+	double r[3];
+	r[0] = (double) (x + 1) - 0.5*L[0];
+	r[1] = (double) (y + 1) - 0.5*L[1];
+	r[2] = (double) (z + 1) - 0.5*L[2];
+	r[0] += 0.5*L[0]; r[1] += 0.5*L[1]; r[2] += 0.5*L[2];
+	double cosx = cos(root2*q0*r[0]), sinx = sin(root2*q0*r[0]);
+	double cosy = cos(root2*q0*r[1]), siny = sin(root2*q0*r[1]);
+	double cosz = cos(root2*q0*r[2]), sinz = sin(root2*q0*r[2]);
+	q[0*N + i] = a*(-2.0*cosy*sinz + sinx*cosz + cosx*siny);
+	q[1*N + i] = a*(root2*cosy*cosz + root2*sinx*sinz - sinx*cosy);
+	q[2*N + i] = a*(root2*cosx*cosy + root2*sinz*siny - cosx*sinz);
+	q[3*N + i] = a*(-2.0*sinx*cosz + siny*cosx + cosy*sinz);
+	q[4*N + i] = a*(root2*cosz*cosx + root2*siny*sinx - siny*cosz);
+      }
+    }
+  }
+}

@@ -96,6 +96,47 @@ void orc_field_stats(const int L[3], const double * q, double out[5]);
 double orc_symm_fed_total(const int L[3], const orc_symm_param_t * fe,
 			  const double * phi, const double * grad);
 
+/* Cholesteric liquid crystal (Landau-de Gennes), src/blue_phase.h:50-75.
+ * Q is stored as its 5 independent components XX, XY, XZ, YY, YZ;
+ * gradients as grad[(3*n + ia)*N + i], delsq[n*N + i]. */
+typedef struct orc_lc_param_s {
+  double a0;
+  double q0;
+  double gamma;
+  double kappa0;
+  double kappa1;
+  double xi;
+  double redshift;
+  double rredshift;
+  double epsilon;            /* already divided by 12 pi */
+  double e0[3];
+  double coswt;
+  double amplitude0;
+} orc_lc_param_t;
+
+void orc_lc_mol_field(const int L[3], const orc_lc_param_t * p,
+		      const double * q, const double * grad,
+		      const double * delsq, double * h);
+void orc_lc_stress(const int L[3], const orc_lc_param_t * p,
+		   const double * q, const double * grad,
+		   const double * delsq, double * pth);
+void orc_lc_fed(const int L[3], const orc_lc_param_t * p, const double * q,
+		const double * grad, double * fed);
+/* Beris-Edwards update of q (src/blue_phase_beris_edwards.c:266-289,
+ * :538-840) given u and upwind fluxes computed here; work >= 20 N. */
+void orc_beris_edw_update(const int L[3], const orc_lc_param_t * p,
+			  double gamma_rot, const uint8_t * status,
+			  const double * u, const double * grad,
+			  const double * delsq, double * q, double * work);
+/* Full LC step as src/ludwig.c:528-860; work >= 40 N doubles. */
+void orc_lc_step(const int L[3], const orc_lc_param_t * p, double gamma_rot,
+		 const orc_collide_param_t * cp, const uint8_t * status,
+		 double * f, double * fscratch, double * q, double * u,
+		 double * rho, double * force, double * work, int nsteps);
+/* Blue phase I (O8M) initial condition, src/blue_phase_init.c:59-132,
+ * no rotation */
+void orc_lc_init_o8m(const int L[3], const orc_lc_param_t * p, double * q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,11 @@
  *    ref_shim mode=force    size=.. A= B= K= in=PREFIX out=PREFIX
  *    ref_shim mode=ch       size=.. A= B= K= M= in=PREFIX out=PREFIX
  *    ref_shim mode=step     size=.. A= B= K= M= eta= steps= in=PREFIX out=PREFIX
+ *    ref_shim mode=lc       size=.. steps= a0= gamma= kappa0= kappa1= pitch= xi=
+ *                           Gamma= redshift= amplitude= eta= out=PREFIX
+ *    ref_shim mode=lc_fields size=.. (lc parameters) in=PREFIX out=PREFIX
+ *    ref_shim mode=lc_be    size=.. (lc parameters) in=PREFIX out=PREFIX
+ *    ref_shim mode=lc_step  size=.. (lc parameters) steps= in=PREFIX out=PREFIX
  *  Any mode accepts status=FILE (uint8 per site, canonical order; 0 fluid).
  *
  *  The call sequence of mode=run/step follows src/ludwig.c:528-860 for
@@ -32,6 +37,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 
 #include "pe.h"
 #include "coords.h"
@@ -52,6 +58,10 @@
 #include "field_phi_init.h"
 #include "util_sum.h"
 #include "wall.h"
+#include "blue_phase.h"
+#include "blue_phase_init.h"
+#include "blue_phase_beris_edwards.h"
+#include "colloids.h"
 
 static const char * arg(int argc, char ** argv, const char * key,
 			const char * def) {
@@ -257,6 +267,156 @@ static void sys_dump(sys_t * s, const char * out) {
   free(a);
 }
 
+
+/*****************************************************************************
+ *
+ *  Cholesteric liquid crystal: src/ludwig.c:1598-1660 set-up and the main
+ *  loop order of src/ludwig.c:528-860 (no colloids, walls or planes).
+ *
+ *****************************************************************************/
+
+typedef struct lcsys_s {
+  sys_t b;                    /* pe, cs, physics, le, hydro, map, lb, wall */
+  field_t * q;
+  field_grad_t * dq;
+  fe_lc_t * fe;
+  beris_edw_t * be;
+  pth_t * pth;
+  colloids_info_t * cinfo;
+} lcsys_t;
+
+static void lcsys_create(int argc, char ** argv, lcsys_t * s) {
+  sys_create(argc, argv, &s->b);
+  {
+    field_options_t opts = field_options_ndata_nhalo(NQAB, 2);
+    field_create(s->b.pe, s->b.cs, s->b.le, "q", &opts, &s->q);
+    field_grad_create(s->b.pe, s->q, 2, &s->dq);
+    field_grad_set(s->dq, grad_3d_7pt_fluid_d2, NULL);
+  }
+  fe_lc_create(s->b.pe, s->b.cs, s->b.le, s->q, s->dq, &s->fe);
+  {
+    fe_lc_param_t p = {0};
+    const double pi = 4.0*atan(1.0);
+    p.a0 = argd(argc, argv, "a0", 0.01);
+    p.gamma = argd(argc, argv, "gamma", 3.0);
+    p.kappa0 = argd(argc, argv, "kappa0", 0.01);
+    p.kappa1 = argd(argc, argv, "kappa1", 0.01);
+    p.q0 = 2.0*pi/argd(argc, argv, "pitch", 32.0);
+    p.xi = argd(argc, argv, "xi", 0.7);
+    p.redshift = argd(argc, argv, "redshift", 1.0);
+    p.amplitude0 = argd(argc, argv, "amplitude", -0.2);
+    fe_lc_param_set(s->fe, &p);
+  }
+  beris_edw_create(s->b.pe, s->b.cs, s->b.le, &s->be);
+  {
+    beris_edw_param_t bp = {0};
+    bp.xi = argd(argc, argv, "xi", 0.7);
+    bp.gamma = argd(argc, argv, "Gamma", 0.5);
+    beris_edw_param_set(s->be, &bp);
+  }
+  pth_create(s->b.pe, s->b.cs, FE_FORCE_METHOD_STRESS_DIVERGENCE, &s->pth);
+  {
+    int ncell[3] = {2, 2, 2};
+    colloids_info_create(s->b.pe, s->b.cs, ncell, &s->cinfo);
+    colloids_info_map_init(s->cinfo);
+  }
+}
+
+static void lcsys_step(lcsys_t * s) {
+  double zero[3] = {0.0, 0.0, 0.0};
+  physics_control_next_step(s->b.phys);
+  hydro_f_zero(s->b.hydro, zero);
+  field_halo(s->q);
+  field_grad_compute(s->dq);
+  fe_lc_redshift_compute(s->b.cs, s->fe);
+  phi_force_calculation(s->b.pe, s->b.cs, s->b.le, s->b.wall, s->pth,
+			(fe_t *) s->fe, s->b.map, s->q, s->b.hydro);
+  hydro_u_halo(s->b.hydro);
+  beris_edw_update(s->be, (fe_t *) s->fe, s->q, s->dq, s->b.hydro, s->cinfo,
+		   s->b.map, NULL);
+  hydro_u_zero(s->b.hydro, zero);
+  lb_collide(s->b.lb, s->b.hydro, s->b.map, NULL, (fe_t *) s->fe, NULL);
+  lb_halo(s->b.lb);
+  lb_propagation(s->b.lb);
+}
+
+static int lc_main(int argc, char ** argv, const char * mode) {
+  lcsys_t s;
+  const char * in   = arg(argc, argv, "in", NULL);
+  const char * out  = arg(argc, argv, "out", "ref");
+  size_t n = nint();
+  double * a = malloc(NVEL*n*sizeof(double));
+
+  lcsys_create(argc, argv, &s);
+
+  if (strcmp(mode, "lc") == 0) {
+    double angles[3] = {0.0, 0.0, 0.0};
+    fe_lc_param_t p;
+    int steps = atoi(arg(argc, argv, "steps", "1"));
+    fe_lc_param(s.fe, &p);
+    blue_phase_O8M_init(s.b.cs, &p, s.q, angles);
+    field_get(s.b.cs, s.q, a);
+    writef(out, "q0", a, NQAB*n);
+    for (int k = 0; k < steps; k++) lcsys_step(&s);
+    sys_dump(&s.b, out);
+    field_get(s.b.cs, s.q, a);
+    writef(out, "q", a, NQAB*n);
+  }
+  else if (strcmp(mode, "lc_fields") == 0) {
+    /* molecular field, stress and free energy density of a given q */
+    double * q = readf(in, "q", NQAB*n);
+    field_put(s.b.cs, s.q, q);
+    field_halo(s.q);
+    field_grad_compute(s.dq);
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(s.b.cs, x+1, y+1, z+1);
+	double h[3][3], st[3][3], fed;
+	fe_lc_mol_field(s.fe, index, h);
+	fe_lc_stress(s.fe, index, st);
+	fe_lc_fed(s.fe, index, &fed);
+	a[canon(0,x,y,z)] = h[0][0]; a[canon(1,x,y,z)] = h[0][1];
+	a[canon(2,x,y,z)] = h[0][2]; a[canon(3,x,y,z)] = h[1][1];
+	a[canon(4,x,y,z)] = h[1][2];
+	for (int ia = 0; ia < 3; ia++) for (int ib = 0; ib < 3; ib++)
+	  a[canon(5 + 3*ia + ib,x,y,z)] = st[ia][ib];
+	a[canon(14,x,y,z)] = fed;
+      }
+    writef(out, "h", a, 5*n);
+    writef(out, "stress", a + 5*n, 9*n);
+    writef(out, "fed", a + 14*n, n);
+  }
+  else if (strcmp(mode, "lc_be") == 0) {
+    double * q = readf(in, "q", NQAB*n);
+    double * u = readf(in, "u", 3*n);
+    field_put(s.b.cs, s.q, q);
+    field_put(s.b.cs, s.b.hydro->u, u);
+    field_halo(s.q);
+    field_grad_compute(s.dq);
+    hydro_u_halo(s.b.hydro);
+    beris_edw_update(s.be, (fe_t *) s.fe, s.q, s.dq, s.b.hydro, s.cinfo,
+		     s.b.map, NULL);
+    field_get(s.b.cs, s.q, a);
+    writef(out, "q", a, NQAB*n);
+  }
+  else if (strcmp(mode, "lc_step") == 0) {
+    double * q = readf(in, "q", NQAB*n);
+    double * u = readf(in, "u", 3*n);
+    double * f = readf(in, "f", NVEL*n);
+    int steps = atoi(arg(argc, argv, "steps", "1"));
+    field_put(s.b.cs, s.q, q);
+    field_put(s.b.cs, s.b.hydro->u, u);
+    lb_put(s.b.cs, s.b.lb, f);
+    for (int k = 0; k < steps; k++) lcsys_step(&s);
+    sys_dump(&s.b, out);
+    field_get(s.b.cs, s.q, a);
+    writef(out, "q", a, NQAB*n);
+  }
+  free(a);
+  MPI_Finalize();
+  return 0;
+}
+
 int main(int argc, char ** argv) {
 
   const char * mode = arg(argc, argv, "mode", "run");
@@ -268,6 +428,8 @@ int main(int argc, char ** argv) {
 
   if (sscanf(arg(argc, argv, "size", "8,8,8"), "%d,%d,%d",
 	     L, L+1, L+2) != 3) return 2;
+
+  if (strncmp(mode, "lc", 2) == 0) return lc_main(argc, argv, mode);
 
   sys_create(argc, argv, &s);
 

@@ -324,6 +324,23 @@ int stats_distribution(lb_t * lb, double out[4]);
 /* total symmetric free energy (bulk + gradient) */
 int stats_free_energy_symm(fe_symm_t * fe, double * total);
 
+/* Field statistics that allocate nothing.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory themselves
+ * (their device memory belongs to another allocator or runtime, or the call
+ * sits in a loop that must not pay the implicit synchronisation of
+ * cudaMalloc): d_data is the caller's device array of ncomp x nsites
+ * doubles (component-major), out the caller's host array of 5*ncomp
+ * doubles, per component {total, mean, variance, min, max} as
+ * stats_field_q.  stream is a cudaStream_t (NULL: the default stream).
+ * Partial sums go to a static device array sized for at most
+ * LUDWIG_GB_NOALLOC_MAX_NCOMP components; larger ncomp is rejected with
+ * LUDWIG_GB_EINVAL.  The first call on each device looks up that array's
+ * device address, so make it before any stream capture.  Calls that overlap
+ * on the GPU share the array and race: order them (e.g. one stream). */
+#define LUDWIG_GB_NOALLOC_MAX_NCOMP 5
+int ludwig_gb_field_stats_noalloc(const double * d_data, long long nsites,
+				  int ncomp, double * out, void * stream);
+
 #ifdef __cplusplus
 }
 #endif

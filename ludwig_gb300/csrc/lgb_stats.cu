@@ -16,6 +16,7 @@
 
 #include "lgb_fused.cuh"
 #include "lgb_stats.h"
+#include "ludwig_gb.h"
 
 /* Klein doubly compensated sum, src/util_sum.c:91-120 */
 struct Klein {
@@ -272,4 +273,95 @@ extern "C" int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
   return finish(1, scratch, out_host, s);
+}
+
+/*****************************************************************************
+ *
+ *  Field statistics without allocation.
+ *
+ *  For callers that cannot allocate device memory themselves: code that
+ *  runs where cudaMalloc is not allowed or not wanted, for example a host
+ *  application whose device memory is owned by another allocator or
+ *  runtime, or a time-critical loop that must not pay the implicit device
+ *  synchronisation of cudaMalloc/cudaFree.  They pass a device pointer to
+ *  their own data and a host array for the result; the per-block partial
+ *  sums go to the static array below instead of a buffer the library
+ *  allocates.
+ *
+ *  The array is a file-scope __device__ variable: every GPU that loads the
+ *  library holds it (LUDWIG_GB_NOALLOC_SCRATCH_DOUBLES doubles, 328 KB)
+ *  until the process exits.  Host code cannot use the name of a __device__
+ *  variable as a device address (on the host it names a stand-in object),
+ *  so the device address is looked up with cudaGetSymbolAddress once per
+ *  device, with that device current, on the first call made on it.  That
+ *  first call should therefore come before any stream capture.
+ *
+ *  All calls share the one array and it keeps whatever the last call left
+ *  there: each call writes every partial record it later reads, so nothing
+ *  has to be cleared first.  Calls whose work overlaps on the GPU (several
+ *  host threads, or several streams) race on the array; the caller must
+ *  order them, for instance by using one stream.
+ *
+ *****************************************************************************/
+
+#define NOALLOC_REC (3*2 + 2)                       /* k_field_stats NK = 2 */
+#define NOALLOC_SLOT (LGBK_RED_BLOCKS*NOALLOC_REC + 16)
+#define NOALLOC_MAX_NCOMP 5
+#define NOALLOC_DEVICES 64
+
+static __device__ __align__(256) double
+  lgb_noalloc_scratch[NOALLOC_MAX_NCOMP*NOALLOC_SLOT];
+
+static double * noalloc_addr_[NOALLOC_DEVICES];
+
+extern "C" int ludwig_gb_field_stats_noalloc(const double * d_data,
+					     long long nsites, int ncomp,
+					     double * out, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  int dev = 0;
+  double raw[NOALLOC_MAX_NCOMP][4];
+
+  static_assert(NOALLOC_MAX_NCOMP == LUDWIG_GB_NOALLOC_MAX_NCOMP,
+		"static scratch sized for the documented maximum");
+
+  /* More components than the static array holds partials for */
+  if (ncomp < 1 || ncomp > NOALLOC_MAX_NCOMP) return LUDWIG_GB_EINVAL;
+  if (d_data == NULL || out == NULL || nsites <= 0) return LUDWIG_GB_EINVAL;
+
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+  if (dev < 0 || dev >= NOALLOC_DEVICES) return LUDWIG_GB_EINVAL;
+  if (noalloc_addr_[dev] == NULL) {
+    /* once per device, with that device current */
+    void * p = NULL;
+    err = cudaGetSymbolAddress(&p, lgb_noalloc_scratch);
+    if (err != cudaSuccess || p == NULL) return LUDWIG_GB_ECUDA;
+    noalloc_addr_[dev] = (double *) p;
+  }
+
+  for (int n = 0; n < ncomp; n++) {
+    double * part = noalloc_addr_[dev] + (size_t) n*NOALLOC_SLOT;
+    double * fin = part + (size_t) LGBK_RED_BLOCKS*NOALLOC_REC;
+    k_field_stats<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      nsites, d_data + (size_t) n*nsites, part);
+    k_final<2><<<1, 32, 0, s>>>(part, LGBK_RED_BLOCKS, fin);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+    err = cudaMemcpyAsync(raw[n], fin, 4*sizeof(double),
+			  cudaMemcpyDeviceToHost, s);
+    if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+  }
+  err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+
+  for (int n = 0; n < ncomp; n++) {
+    double rvol = 1.0/(double) nsites;
+    double mean = rvol*raw[n][0];
+    out[5*n + 0] = raw[n][0];
+    out[5*n + 1] = mean;
+    out[5*n + 2] = rvol*raw[n][1] - mean*mean;
+    out[5*n + 3] = raw[n][2];
+    out[5*n + 4] = raw[n][3];
+  }
+  return LUDWIG_GB_OK;
 }

@@ -237,6 +237,65 @@ int fe_symm_free(fe_symm_t * fe);
 int fe_symm_param_set(fe_symm_t * fe, fe_symm_param_t values);
 int fe_symm_param(fe_symm_t * fe, fe_symm_param_t * values);
 
+/* Cholesteric liquid crystal: src/blue_phase.h:37-75 (Q as 5 components
+ * XX, XY, XZ, YY, YZ of a field with ndata = 5) */
+typedef struct fe_lc_param_s {
+  double a0;
+  double q0;
+  double gamma;
+  double kappa0;
+  double kappa1;
+  double xi;                  /* flow aligning parameter */
+  double zeta0, zeta1, zeta2; /* active stress: 0 only */
+  double redshift;
+  double rredshift;           /* set by fe_lc_param_set */
+  double epsilon;             /* dielectric anisotropy (scaled by 1/12pi) */
+  double amplitude0;          /* initial amplitude */
+  double e0[3];               /* external electric field */
+  double coswt;               /* field phase (1 for a static field) */
+  int is_redshift_updated;    /* 0 only */
+  int is_active;              /* 0 only */
+} fe_lc_param_t;
+
+int fe_lc_create(pe_t * pe, cs_t * cs, lees_edw_t * le, field_t * q,
+		 field_grad_t * dq, fe_lc_t ** p);      /* blue_phase.c:78 */
+int fe_lc_free(fe_lc_t * fe);
+/* blue_phase.c:241: epsilon is divided by 12 pi, rredshift = 1/redshift */
+int fe_lc_param_set(fe_lc_t * fe, const fe_lc_param_t * values);
+int fe_lc_param(fe_lc_t * fe, fe_lc_param_t * values);
+/* Blue phase I initial condition, src/blue_phase_init.c:59 (no rotation:
+ * euler_angles must be zero) */
+int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
+			const double euler_angles[3]);
+
+/* Beris-Edwards: src/blue_phase_beris_edwards.h:28-49 */
+typedef struct beris_edw_param_s {
+  double xi;                  /* effective aspect ratio */
+  double gamma;               /* rotational diffusion constant Gamma */
+  int noise;                  /* 0 only */
+  double var;
+} beris_edw_param_t;
+
+int beris_edw_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		     beris_edw_t ** pobj);
+int beris_edw_free(beris_edw_t * be);
+int beris_edw_param_set(beris_edw_t * be, beris_edw_param_t * values);
+/* src/blue_phase_beris_edwards.c:266 */
+int beris_edw_update(beris_edw_t * be, fe_t * fe, field_t * fq,
+		     field_grad_t * fq_grad, hydro_t * hydro,
+		     colloids_info_t * cinfo, map_t * map, noise_t * noise);
+/* molecular field of the last update: 5 x nsites */
+int beris_edw_h_to_host(beris_edw_t * be, double * h);
+
+/* Fused GB300 step of the cholesteric: nsteps iterations of the main loop
+ * of src/ludwig.c:528-860 (q gradients, molecular field and chiral stress,
+ * stress-divergence force, Beris-Edwards update with upwind fluxes,
+ * collision, streaming) in two kernel launches per step.  FP64 objects
+ * give the results of the functions above called one by one; FP32 objects
+ * (lb, q, hydro) run the same step in float arithmetic. */
+int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
+		      fe_t * fe, beris_edw_t * be, int nsteps);
+
 /*---------------------------------------------------------------------------
  * Force from the free energy: src/phi_force_stress.h:36-39,
  * src/phi_force.h:24 (stress divergence, fluid only)
@@ -281,8 +340,9 @@ int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
 int ludwig_gb_sync(void);
 /* The CUDA stream (cudaStream_t) every launch of the library uses. */
 void * ludwig_gb_stream(void);
-/* Tuning of the fused kernel: planes per x chunk and tile height. */
-int ludwig_gb_tune_set(int xchunk, int tile_y);
+/* Tuning of the fused kernel: planes per x chunk, tile height (4, 8, 16)
+ * and resident CTAs per SM for tile height 8 (2..4; 0 = default). */
+int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks);
 
 /*---------------------------------------------------------------------------
  * State transfer in the storage format of the objects' precision, for
@@ -323,6 +383,61 @@ int stats_field_q(field_t * field, int n, double out[5]);
 int stats_distribution(lb_t * lb, double out[4]);
 /* total symmetric free energy (bulk + gradient) */
 int stats_free_energy_symm(fe_symm_t * fe, double * total);
+
+/*---------------------------------------------------------------------------
+ * Ensembles: many independent periodic binary-fluid boxes of any sizes and
+ * parameters advanced together, one kernel launch per step for all boxes
+ * (replayed from a CUDA graph).  No counterpart in the reference, which
+ * runs one system per job; each box follows the same step as
+ * ludwig_gb_binary_step.
+ *-------------------------------------------------------------------------*/
+typedef struct ludwig_gb_ensemble_s ludwig_gb_ensemble_t;
+
+typedef struct ludwig_gb_box_param_s {
+  int ntotal[3];
+  double rho0;
+  double eta;                 /* shear viscosity */
+  double eta_bulk;            /* bulk viscosity (<= 0: eta) */
+  double a, b, kappa;         /* symmetric free energy */
+  double mobility;
+  int seed;                   /* spinodal initial condition */
+  double phi0, noise;
+} ludwig_gb_box_param_t;
+
+int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
+			      int precision, ludwig_gb_ensemble_t ** pens);
+int ludwig_gb_ensemble_free(ludwig_gb_ensemble_t * ens);
+int ludwig_gb_ensemble_step(ludwig_gb_ensemble_t * ens, int nsteps);
+/* device time of nsteps (CUDA events on the library stream) */
+int ludwig_gb_ensemble_time(ludwig_gb_ensemble_t * ens, int nsteps,
+			    double * ms);
+int ludwig_gb_ensemble_tune_set(ludwig_gb_ensemble_t * ens, int xchunk,
+				int tile_y, int min_blocks);
+/* Time each candidate tiling for trial_steps on a copy of the state and
+ * keep the fastest; the state itself is left unchanged. */
+int ludwig_gb_ensemble_autotune(ludwig_gb_ensemble_t * ens, int trial_steps,
+				int best[3], double * ms_best);
+/* reference f (19 x n), phi (n), u (3 x n), rho (n) of one box; any NULL */
+int ludwig_gb_ensemble_box_get(ludwig_gb_ensemble_t * ens, int box,
+			       double * f, double * phi, double * u,
+			       double * rho);
+int ludwig_gb_ensemble_box_set_phi(ludwig_gb_ensemble_t * ens, int box,
+				   const double * phi);
+/* Boxes whose mass or total phi is no longer finite are quarantined: they
+ * are not stepped any more; the others continue unchanged. */
+int ludwig_gb_ensemble_check(ludwig_gb_ensemble_t * ens, int * nactive);
+int ludwig_gb_ensemble_box_active(ludwig_gb_ensemble_t * ens, int box,
+				  int * active);
+/* lattice sites of the active boxes */
+int ludwig_gb_ensemble_sites(ludwig_gb_ensemble_t * ens, long long * n);
+
+/* Domain length from the spherically averaged structure factor of a
+ * scalar field (util/length_from_sk.c:88-190): L = 2 pi sum S dk /
+ * sum k S dk over 128 bins.  faithful = 1 keeps the reference's
+ * wavevector for i > N/2 (dk*i - pi); faithful = 0 uses dk*i - 2 pi.
+ * sk and nk (128 doubles each, may be NULL) receive the binned sums. */
+int ludwig_gb_length_from_sk(field_t * phi, int faithful, double * length,
+			     double * sk, double * nk);
 
 /* Field statistics that allocate nothing.  No counterpart in the
  * reference.  For callers that cannot allocate device memory themselves

@@ -78,6 +78,33 @@ class PhiChInfo(ctypes.Structure):
     _fields_ = [("conserve", ctypes.c_int), ("noise", ctypes.c_int)]
 
 
+class BoxParam(ctypes.Structure):
+    _fields_ = [("ntotal", ctypes.c_int * 3), ("rho0", ctypes.c_double),
+                ("eta", ctypes.c_double), ("eta_bulk", ctypes.c_double),
+                ("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("kappa", ctypes.c_double), ("mobility", ctypes.c_double),
+                ("seed", ctypes.c_int), ("phi0", ctypes.c_double),
+                ("noise", ctypes.c_double)]
+
+
+class FeLcParam(ctypes.Structure):
+    _fields_ = [("a0", ctypes.c_double), ("q0", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("kappa0", ctypes.c_double),
+                ("kappa1", ctypes.c_double), ("xi", ctypes.c_double),
+                ("zeta0", ctypes.c_double), ("zeta1", ctypes.c_double),
+                ("zeta2", ctypes.c_double), ("redshift", ctypes.c_double),
+                ("rredshift", ctypes.c_double), ("epsilon", ctypes.c_double),
+                ("amplitude0", ctypes.c_double), ("e0", ctypes.c_double * 3),
+                ("coswt", ctypes.c_double),
+                ("is_redshift_updated", ctypes.c_int),
+                ("is_active", ctypes.c_int)]
+
+
+class BerisEdwParam(ctypes.Structure):
+    _fields_ = [("xi", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("noise", ctypes.c_int), ("var", ctypes.c_double)]
+
+
 def _declare(L):
     pp = ctypes.POINTER(ctypes.c_void_p)
     sig = {
@@ -85,7 +112,7 @@ def _declare(L):
         "ludwig_gb_version": ([], ctypes.c_char_p),
         "ludwig_gb_stream": ([], _P),
         "ludwig_gb_sync": ([], ctypes.c_int),
-        "ludwig_gb_tune_set": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_tune_set": ([ctypes.c_int] * 3, ctypes.c_int),
         "pe_create": ([ctypes.c_int, pp], ctypes.c_int),
         "pe_free": ([_P], ctypes.c_int),
         "cs_create": ([_P, pp], ctypes.c_int),
@@ -158,6 +185,41 @@ def _declare(L):
                                   ctypes.c_int),
         "ludwig_gb_time_binary_e2e": ([_P] * 5 + [ctypes.c_int] + [_P] * 4
                                       + [_D], ctypes.c_int),
+        "fe_lc_create": ([_P, _P, _P, _P, _P, pp], ctypes.c_int),
+        "fe_lc_free": ([_P], ctypes.c_int),
+        "fe_lc_param_set": ([_P, ctypes.POINTER(FeLcParam)], ctypes.c_int),
+        "blue_phase_O8M_init": ([_P, ctypes.POINTER(FeLcParam), _P, _D],
+                                ctypes.c_int),
+        "beris_edw_create": ([_P, _P, _P, pp], ctypes.c_int),
+        "beris_edw_free": ([_P], ctypes.c_int),
+        "beris_edw_param_set": ([_P, ctypes.POINTER(BerisEdwParam)],
+                                ctypes.c_int),
+        "beris_edw_update": ([_P] * 8, ctypes.c_int),
+        "beris_edw_h_to_host": ([_P, _D], ctypes.c_int),
+        "ludwig_gb_lc_step": ([_P] * 6 + [ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_length_from_sk": ([_P, ctypes.c_int, _D, _D, _D],
+                                     ctypes.c_int),
+        "ludwig_gb_ensemble_create": ([ctypes.c_int, ctypes.POINTER(BoxParam),
+                                       ctypes.c_int, pp], ctypes.c_int),
+        "ludwig_gb_ensemble_free": ([_P], ctypes.c_int),
+        "ludwig_gb_ensemble_step": ([_P, ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_ensemble_time": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "ludwig_gb_ensemble_tune_set": ([_P] + [ctypes.c_int] * 3,
+                                        ctypes.c_int),
+        "ludwig_gb_ensemble_autotune": ([_P, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int), _D],
+                                        ctypes.c_int),
+        "ludwig_gb_ensemble_box_get": ([_P, ctypes.c_int, _D, _D, _D, _D],
+                                       ctypes.c_int),
+        "ludwig_gb_ensemble_box_set_phi": ([_P, ctypes.c_int, _D],
+                                           ctypes.c_int),
+        "ludwig_gb_ensemble_check": ([_P, ctypes.POINTER(ctypes.c_int)],
+                                     ctypes.c_int),
+        "ludwig_gb_ensemble_box_active": ([_P, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int)],
+                                          ctypes.c_int),
+        "ludwig_gb_ensemble_sites": ([_P, ctypes.POINTER(ctypes.c_longlong)],
+                                     ctypes.c_int),
         "stats_field_q": ([_P, ctypes.c_int, _D], ctypes.c_int),
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
@@ -325,6 +387,15 @@ class Field(_Obj):
     def init_spinodal(self, seed, phi0=0.0, amp=0.02):
         _check(lib().field_phi_init_spinodal(self.ptr, int(seed), float(phi0),
                                              float(amp)), "spinodal")
+
+    def length_from_sk(self, faithful=True):
+        """Domain length L from the structure factor (and S, counts)."""
+        L = ctypes.c_double()
+        sk, nk = np.zeros(128), np.zeros(128)
+        _check(lib().ludwig_gb_length_from_sk(self.ptr, int(bool(faithful)),
+                                              ctypes.byref(L), _dp(sk),
+                                              _dp(nk)), "length_from_sk")
+        return L.value, sk, nk
 
     def stats(self, n=0):
         out = np.zeros(5)
@@ -537,8 +608,9 @@ def sync():
     _check(lib().ludwig_gb_sync(), "ludwig_gb_sync")
 
 
-def tune(xchunk, tile_y):
-    _check(lib().ludwig_gb_tune_set(int(xchunk), int(tile_y)), "tune")
+def tune(xchunk, tile_y, min_blocks=0):
+    _check(lib().ludwig_gb_tune_set(int(xchunk), int(tile_y),
+                                    int(min_blocks)), "tune")
 
 
 class PinnedState:
@@ -589,3 +661,213 @@ def time_binary_e2e(system, pinned, nsteps):
                                        *pinned.bufs, ctypes.byref(ms)),
            "time_binary_e2e")
     return ms.value
+
+
+# ---------------------------------------------------------------------------
+# Cholesteric liquid crystal
+# ---------------------------------------------------------------------------
+
+class FeLC(_Obj):
+    """fe_lc_t: Landau-de Gennes free energy (src/blue_phase.c)."""
+    _free = "fe_lc_free"
+
+    def __init__(self, cs, q, dq, a0=0.01, gamma=3.0, kappa0=0.01,
+                 kappa1=0.01, pitch=32.0, xi=0.7, redshift=1.0,
+                 amplitude=-0.2):
+        super().__init__()
+        self.ptr = _new("fe_lc_create", cs.pe.ptr, cs.ptr, None, q.ptr,
+                        dq.ptr)
+        p = FeLcParam()
+        p.a0, p.gamma, p.kappa0, p.kappa1 = a0, gamma, kappa0, kappa1
+        p.q0 = 2.0 * 3.1415926535897932385 / pitch
+        p.xi, p.redshift, p.amplitude0, p.coswt = xi, redshift, amplitude, 1.0
+        self.param = p
+        _check(lib().fe_lc_param_set(self.ptr, ctypes.byref(p)),
+               "fe_lc_param_set")
+
+
+class BerisEdw(_Obj):
+    _free = "beris_edw_free"
+
+    def __init__(self, cs, xi=0.7, gamma=0.5):
+        super().__init__()
+        self.cs = cs
+        self.ptr = _new("beris_edw_create", cs.pe.ptr, cs.ptr, None)
+        p = BerisEdwParam(xi, gamma, 0, 0.0)
+        _check(lib().beris_edw_param_set(self.ptr, ctypes.byref(p)),
+               "beris_edw_param_set")
+
+    def update(self, fe, q, dq, hydro, map_=None):
+        _check(lib().beris_edw_update(self.ptr, fe.ptr, q.ptr, dq.ptr,
+                                      hydro.ptr if hydro else None, None,
+                                      map_.ptr if map_ else None, None),
+               "beris_edw_update")
+
+    def h(self):
+        a = np.zeros((5,) + self.cs.ntotal)
+        _check(lib().beris_edw_h_to_host(self.ptr, _dp(a)), "be_h")
+        return a
+
+
+class LiquidCrystal:
+    """All objects of the cholesteric LC with hydrodynamics (config 4)."""
+
+    def __init__(self, ntotal, eta=0.5, gamma_rot=0.5, device=0,
+                 precision=FP64, **lc):
+        self.pe = PE(device)
+        self.cs = Coords(self.pe, ntotal)
+        self.phys = Physics(self.pe, rho0=1.0, eta=eta)
+        self.lb = LB(self.cs, precision)
+        self.q = Field(self.cs, 5, 2, precision, "q")
+        self.dq = FieldGrad(self.q, 2)
+        self.hydro = Hydro(self.cs, precision)
+        self.map = Map(self.cs)
+        self.fe = FeLC(self.cs, self.q, self.dq, **lc)
+        self.be = BerisEdw(self.cs, xi=self.fe.param.xi, gamma=gamma_rot)
+        self.pth = Pth(self.cs)
+        self.lb.init_rest(1.0)
+
+    def init_o8m(self):
+        zero = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+        _check(lib().blue_phase_O8M_init(self.cs.ptr,
+                                         ctypes.byref(self.fe.param),
+                                         self.q.ptr, zero), "o8m")
+
+    def step_reference_order(self, nsteps=1):
+        for _ in range(nsteps):
+            self.hydro.f_zero()
+            self.q.halo()
+            self.dq.compute()
+            phi_force_calculation(self.pe, self.cs, self.pth, self.fe,
+                                  self.map, self.q, self.hydro)
+            self.hydro.u_halo()
+            self.be.update(self.fe, self.q, self.dq, self.hydro, self.map)
+            self.hydro.u_zero()
+            self.lb.collide(self.hydro, self.map, self.fe)
+            self.lb.halo()
+            self.lb.propagation()
+
+    def step(self, nsteps=1):
+        """The fused GB300 LC step (two kernels per step)."""
+        _check(lib().ludwig_gb_lc_step(self.lb.ptr, self.q.ptr,
+                                       self.hydro.ptr, self.map.ptr,
+                                       self.fe.ptr, self.be.ptr,
+                                       int(nsteps)), "ludwig_gb_lc_step")
+
+    def state(self):
+        rho, u, force = self.hydro.get()
+        return {"f": self.lb.get(), "q": self.q.get(), "u": u, "rho": rho,
+                "force": force}
+
+
+# ---------------------------------------------------------------------------
+# Ensembles of independent boxes
+# ---------------------------------------------------------------------------
+
+def box_param(ntotal, eta=0.1, a=-0.0625, b=0.0625, kappa=0.04,
+              mobility=0.3, seed=8361235, rho0=1.0, phi0=0.0, noise=0.02):
+    p = BoxParam()
+    for i in range(3):
+        p.ntotal[i] = int(ntotal[i])
+    p.rho0, p.eta, p.eta_bulk = rho0, eta, 0.0
+    p.a, p.b, p.kappa, p.mobility = a, b, kappa, mobility
+    p.seed, p.phi0, p.noise = int(seed), phi0, noise
+    return p
+
+
+class Ensemble:
+    """ludwig_gb_ensemble_t: boxes advanced together, one launch a step."""
+
+    def __init__(self, params, precision=FP32, device=0):
+        self.pe = PE(device)
+        self.params = list(params)
+        arr = (BoxParam * len(self.params))(*self.params)
+        self.ptr = _new("ludwig_gb_ensemble_create", len(self.params), arr,
+                        int(precision))
+
+    def close(self):
+        if self.ptr is not None:
+            lib().ludwig_gb_ensemble_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        _check(lib().ludwig_gb_ensemble_step(self.ptr, int(n)), "ens_step")
+
+    def time(self, n):
+        ms = ctypes.c_double()
+        _check(lib().ludwig_gb_ensemble_time(self.ptr, int(n),
+                                             ctypes.byref(ms)), "ens_time")
+        return ms.value
+
+    def tune(self, xchunk, tile_y, min_blocks=0):
+        _check(lib().ludwig_gb_ensemble_tune_set(self.ptr, int(xchunk),
+                                                 int(tile_y),
+                                                 int(min_blocks)), "tune")
+
+    def autotune(self, trial_steps=10):
+        best = (ctypes.c_int * 3)()
+        ms = ctypes.c_double()
+        _check(lib().ludwig_gb_ensemble_autotune(self.ptr, int(trial_steps),
+                                                 best, ctypes.byref(ms)),
+               "autotune")
+        return tuple(best), ms.value
+
+    def box(self, b, f=False):
+        L = tuple(self.params[b].ntotal)
+        phi, u, rho = (np.zeros((1,) + L), np.zeros((3,) + L),
+                       np.zeros((1,) + L))
+        ff = np.zeros((NVEL,) + L) if f else None
+        _check(lib().ludwig_gb_ensemble_box_get(
+            self.ptr, int(b), _dp(ff) if f else None, _dp(phi), _dp(u),
+            _dp(rho)), "box_get")
+        out = {"phi": phi, "u": u, "rho": rho}
+        if f:
+            out["f"] = ff
+        return out
+
+    def set_phi(self, b, phi):
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        _check(lib().ludwig_gb_ensemble_box_set_phi(self.ptr, int(b), _dp(a)),
+               "set_phi")
+
+    def check(self):
+        n = ctypes.c_int()
+        _check(lib().ludwig_gb_ensemble_check(self.ptr, ctypes.byref(n)),
+               "check")
+        return n.value
+
+    def active(self, b):
+        a = ctypes.c_int()
+        _check(lib().ludwig_gb_ensemble_box_active(self.ptr, int(b),
+                                                   ctypes.byref(a)), "active")
+        return bool(a.value)
+
+    def sites(self):
+        n = ctypes.c_longlong()
+        _check(lib().ludwig_gb_ensemble_sites(self.ptr, ctypes.byref(n)),
+               "sites")
+        return n.value
+
+
+def ensemble_config3(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
+    """Config 3: boxes with edges drawn per axis from `edges`, viscosity
+    U[0.02, 0.2], kappa U[0.02, 0.08], A = -B with |A| U[0.03, 0.1],
+    mobility min(0.45, 1/(12 (12 kappa - |A|))) (half the 7-point
+    stability bound), phi0 +-0.01 from per-box seeds."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nbox):
+        n = [int(rng.choice(edges)) for _ in range(3)]
+        eta = float(rng.uniform(0.02, 0.2))
+        kappa = float(rng.uniform(0.02, 0.08))
+        amag = float(rng.uniform(0.03, 0.1))
+        mob = min(0.45, 1.0 / (12.0 * (12.0 * kappa - amag)))
+        out.append(box_param(n, eta=eta, a=-amag, b=amag, kappa=kappa,
+                             mobility=mob, seed=1000 + 17 * k))
+    return out

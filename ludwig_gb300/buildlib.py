@@ -25,6 +25,9 @@ CU_SOURCES = [
     ("lgb_ref64.cu", ["--fmad=false"]),
     ("lgb_fused64.cu", ["--fmad=false"]),
     ("lgb_stats.cu", ["--fmad=false"]),
+    ("lgb_lc64.cu", ["--fmad=false"]),
+    ("lgb_sk.cu", []),
+    ("lgb_lc32.cu", []),
     ("lgb_fused32.cu", []),
 ]
 C_SOURCES = ["ludwig_gb.c"]

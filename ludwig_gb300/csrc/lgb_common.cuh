@@ -88,19 +88,28 @@ template <> struct Unroll<0> {
  *****************************************************************************/
 
 template <typename T>
+__device__ __forceinline__ T lgb_symm_mu(T a, T b, T kappa, T phi, T delsq) {
+  return a*phi + b*phi*phi*phi - kappa*delsq;
+}
+
+template <typename T>
 __device__ __forceinline__ T lgb_symm_mu(const lgbk_symm_t & fe, T phi,
 					 T delsq) {
-  const T a = (T) fe.a, b = (T) fe.b, kappa = (T) fe.kappa;
-  return a*phi + b*phi*phi*phi - kappa*delsq;
+  return lgb_symm_mu<T>((T) fe.a, (T) fe.b, (T) fe.kappa, phi, delsq);
 }
 
 /* p0 of P_ab = p0 delta_ab + kappa g_a g_b (src/symmetric.c:386-391) */
 template <typename T>
-__device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
-					 T delsq, const T g[3]) {
-  const T a = (T) fe.a, b = (T) fe.b, kappa = (T) fe.kappa;
+__device__ __forceinline__ T lgb_symm_p0(T a, T b, T kappa, T phi, T delsq,
+					 const T g[3]) {
   return T(0.5)*a*phi*phi + T(0.75)*b*phi*phi*phi*phi - kappa*phi*delsq
     - T(0.5)*kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
+}
+
+template <typename T>
+__device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
+					 T delsq, const T g[3]) {
+  return lgb_symm_p0<T>((T) fe.a, (T) fe.b, (T) fe.kappa, phi, delsq, g);
 }
 
 /*****************************************************************************
@@ -118,7 +127,8 @@ __device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
  *****************************************************************************/
 
 template <typename T, bool SEQ, bool SHIFT, bool GZERO>
-__device__ __forceinline__ void lgb_collide_site(const lgbk_collide_t & cp,
+__device__ __forceinline__ void lgb_collide_site(T rtau, T rtau_bulk,
+						 const double * rtau_ghost,
 						 T rho0, T fs[LGB_NVEL],
 						 const T force[3], T & rho_out,
 						 T u[3]) {
@@ -129,8 +139,6 @@ __device__ __forceinline__ void lgb_collide_site(const lgbk_collide_t & cp,
   else     d3q19_f2mode_fast<T, NM>(fs, mode);
 
   const T rdim = T(1.0/3.0);
-  const T rtau = (T) cp.rtau_shear;
-  const T rtau_bulk = (T) cp.rtau_bulk;
 
   /* density: mode 0 is rho (or rho - rho0 for shifted populations) */
   const T rho = SHIFT ? (rho0 + mode[0]) : mode[0];
@@ -181,7 +189,7 @@ __device__ __forceinline__ void lgb_collide_site(const lgbk_collide_t & cp,
   if (!GZERO) {
     #pragma unroll
     for (int m = 10; m < LGB_NVEL; m++) {
-      mode[m] = mode[m] - ((T) cp.rtau_ghost[m])*(mode[m] - T(0.0));
+      mode[m] = mode[m] - ((T) rtau_ghost[m])*(mode[m] - T(0.0));
     }
   }
 
@@ -189,6 +197,17 @@ __device__ __forceinline__ void lgb_collide_site(const lgbk_collide_t & cp,
   else     d3q19_mode2f_fast<T, NM>(mode, fs);
 
   rho_out = rho;
+}
+
+/* As above with the relaxation times of a parameter block */
+template <typename T, bool SEQ, bool SHIFT, bool GZERO>
+__device__ __forceinline__ void lgb_collide_site(const lgbk_collide_t & cp,
+						 T rho0, T fs[LGB_NVEL],
+						 const T force[3], T & rho_out,
+						 T u[3]) {
+  lgb_collide_site<T, SEQ, SHIFT, GZERO>((T) cp.rtau_shear,
+					 (T) cp.rtau_bulk, cp.rtau_ghost,
+					 rho0, fs, force, rho_out, u);
 }
 
 #endif

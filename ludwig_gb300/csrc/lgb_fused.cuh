@@ -34,6 +34,7 @@
 #define LGB_FUSED_CUH
 
 #include "lgb_common.cuh"
+#include <cuda_pipeline.h>
 
 /* Storage of distributions */
 
@@ -56,6 +57,17 @@ __device__ __forceinline__ int lgb_mod(int i, int n) {
   return (r < 0) ? r + n : r;
 }
 
+/* Typed access to the parameter block */
+template <typename T> struct KP;
+template <> struct KP<float> {
+  static __device__ __forceinline__ float get(const lgbk_binary_args_t & a,
+					      int i) { return a.pf[i]; }
+};
+template <> struct KP<double> {
+  static __device__ __forceinline__ double get(const lgbk_binary_args_t & a,
+					       int i) { return a.pd[i]; }
+};
+
 template <typename T, int TY>
 struct FusedSmem {
   static constexpr int TZ = 32;
@@ -65,35 +77,42 @@ struct FusedSmem {
   static constexpr int ND = DY*DZ;
   static constexpr int NDC = 10;                     /* P (9) + mu */
   static constexpr size_t bytes() {
-    return sizeof(T)*(3*NPHI + 2*NDC*ND + 3*ND);
+    return sizeof(T)*(4*NPHI + 2*NDC*ND + 2*3*ND);
   }
 };
 
+/* Wrap a coordinate that may lie up to one tile outside [0, n) */
+__device__ __forceinline__ int lgb_wrap_far(int i, int n) {
+  if (i < 0) i += n;
+  while (i >= n) i -= n;
+  return i;
+}
+
+/* One work item: the TY x 32 tile (ity, itz) of box d, planes
+ * [icx*xchunk, icx*xchunk + xchunk).  Called by every thread of the CTA;
+ * smem_raw holds FusedSmem<T, TY>::bytes(). */
 template <typename T, typename S, bool SEQ, bool SHIFT, bool GZERO,
-	  bool HAS_MAP, int TY, int MINB>
-__global__ void __launch_bounds__(32*TY, MINB)
-k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
+	  bool HAS_MAP, int TY>
+__device__ __forceinline__ void
+binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int xchunk,
+	    int itz, int ity, int icx, unsigned char * smem_raw) {
 
   using SM = FusedSmem<T, TY>;
   constexpr int TZ = SM::TZ;
   constexpr int PZ = SM::PZ, DZ = SM::DZ;
   constexpr int NPHI = SM::NPHI, ND = SM::ND;
+  constexpr int NTHR = TY*TZ;
+  constexpr int KPHI = (NPHI + NTHR - 1)/NTHR;      /* phi halo loads/thread */
+  constexpr int KD = (ND + NTHR - 1)/NTHR;          /* D sites / u loads */
 
-  extern __shared__ unsigned char smem_raw[];
-  T * sphi = reinterpret_cast<T *>(smem_raw);          /* [3][NPHI] */
-  T * sD = sphi + 3*NPHI;                              /* [2][10][ND] */
-  T * su = sD + 2*SM::NDC*ND;                          /* [3][ND] */
+  T * sphi = reinterpret_cast<T *>(smem_raw);          /* [4][NPHI] */
+  T * sD = sphi + 4*NPHI;                              /* [2][10][ND] */
+  T * su0 = sD + 2*SM::NDC*ND;                         /* [2][3][ND] */
 
   const int tz = threadIdx.x, ty = threadIdx.y;
   const int tid = ty*TZ + tz;
-  const int nthr = TY*TZ;
   const long long N = d.nsites;
-  const long long NP = (long long) d.ny*d.nz;          /* sites per x plane */
-
-  const int ntz = (d.nz + TZ - 1)/TZ;
-  const int nty = (d.ny + TY - 1)/TY;
-  const int ncx = (d.nx + xchunk - 1)/xchunk;
-  const int nitems = ntz*nty*ncx;
+  const int NP = d.ny*d.nz;                            /* sites per x plane */
 
   const T * __restrict__ phi_in = (const T *) a.phi_in;
   T * __restrict__ phi_out = (T *) a.phi_out;
@@ -105,43 +124,70 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
   S * __restrict__ f_out = (S *) a.f_out;
   const uint8_t * __restrict__ st = a.status;
 
-  const T mobility = (T) a.mobility;
-  const T rho0 = (T) a.rho0;
-  const T fscale = (T) a.fscale;
-  const T rfscale = T(1.0)/fscale;
-  const T kappa = (T) a.fe.kappa;
+  const T mobility = KP<T>::get(a, LGBK_P_MOBILITY);
+  const T rho0 = KP<T>::get(a, LGBK_P_RHO0);
+  const T fscale = KP<T>::get(a, LGBK_P_FSCALE);
+  const T rfscale = KP<T>::get(a, LGBK_P_RFSCALE);
+  const T pa = KP<T>::get(a, LGBK_P_A);
+  const T pb = KP<T>::get(a, LGBK_P_B);
+  const T kappa = KP<T>::get(a, LGBK_P_KAPPA);
 
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+  const int cidx = (ty + 1)*DZ + (tz + 1);       /* own site in D/u */
+  const int pidx = (ty + 2)*PZ + (tz + 2);       /* own site in phi */
 
-    const int itz = item % ntz;
-    const int ity = (item / ntz) % nty;
-    const int icx = item / (ntz*nty);
+  {
     const int z0 = itz*TZ, y0 = ity*TY, x0 = icx*xchunk;
     const int xe = min(x0 + xchunk, d.nx);
 
-    /* Ring slot of plane x: phi ring of 3, D ring of 2 (x >= x0 - 2) */
-    auto pslot = [&](int x) { return (x - x0 + 3) % 3; };
+    /* In-plane offsets (wrapped) of the halo elements this thread loads;
+     * fixed for the whole item, so no index arithmetic per plane. */
+    int phoff[KPHI], uoff[KD];
+    #pragma unroll
+    for (int j = 0; j < KPHI; j++) {
+      int k = tid + j*NTHR;
+      int ly = k / PZ - 2, lz = k % PZ - 2;
+      phoff[j] = (k < NPHI) ? lgb_wrap_far(y0 + ly, d.ny)*d.nz
+	+ lgb_wrap_far(z0 + lz, d.nz) : -1;
+    }
+    #pragma unroll
+    for (int j = 0; j < KD; j++) {
+      int k = tid + j*NTHR;
+      int ly = k / DZ - 1, lz = k % DZ - 1;
+      uoff[j] = (k < ND) ? lgb_wrap_far(y0 + ly, d.ny)*d.nz
+	+ lgb_wrap_far(z0 + lz, d.nz) : -1;
+    }
+
+    /* Ring slots (x >= x0 - 2): phi 4 planes, D 2 planes, u 2 planes.
+     * Halo planes are copied asynchronously one plane ahead (cp.async):
+     * phi(x+3) and u(x+1) stream in while plane x is processed. */
+    auto pslot = [&](int x) { return (x - x0 + 4) & 3; };
     auto dslot = [&](int x) { return (x - x0 + 2) & 1; };
+    auto uslot = [&](int x) { return su0 + ((x - x0 + 2) & 1)*3*ND; };
 
     auto load_phi = [&](int x) {
-      const int xw = lgb_mod(x, d.nx);
+      const T * src = phi_in + (long long) lgb_wrap_far(x, d.nx)*NP;
       T * dst = sphi + pslot(x)*NPHI;
-      for (int k = tid; k < NPHI; k += nthr) {
-	int ly = k / PZ - 2, lz = k % PZ - 2;
-	int yw = lgb_mod(y0 + ly, d.ny), zw = lgb_mod(z0 + lz, d.nz);
-	dst[k] = phi_in[(long long) xw*NP + (long long) yw*d.nz + zw];
+      #pragma unroll
+      for (int j = 0; j < KPHI; j++) {
+	if (phoff[j] >= 0) {
+	  __pipeline_memcpy_async(dst + tid + j*NTHR, src + phoff[j],
+				  sizeof(T));
+	}
       }
     };
 
     auto load_u = [&](int x) {
-      const int xw = lgb_mod(x, d.nx);
-      for (int k = tid; k < ND; k += nthr) {
-	int ly = k / DZ - 1, lz = k % DZ - 1;
-	int yw = lgb_mod(y0 + ly, d.ny), zw = lgb_mod(z0 + lz, d.nz);
-	long long s = (long long) xw*NP + (long long) yw*d.nz + zw;
-	su[k]        = u_in[s];
-	su[ND + k]   = u_in[N + s];
-	su[2*ND + k] = u_in[2*N + s];
+      const T * src = u_in + (long long) lgb_wrap_far(x, d.nx)*NP;
+      T * dst = uslot(x);
+      #pragma unroll
+      for (int j = 0; j < KD; j++) {
+	if (uoff[j] >= 0) {
+	  const int k = tid + j*NTHR;
+	  __pipeline_memcpy_async(dst + k, src + uoff[j], sizeof(T));
+	  __pipeline_memcpy_async(dst + ND + k, src + N + uoff[j], sizeof(T));
+	  __pipeline_memcpy_async(dst + 2*ND + k, src + 2*N + uoff[j],
+				  sizeof(T));
+	}
       }
     };
 
@@ -151,9 +197,12 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
       const T * pp = sphi + pslot(x + 1)*NPHI;
       const T * pm = sphi + pslot(x - 1)*NPHI;
       T * D = sD + dslot(x)*SM::NDC*ND;
-      for (int k = tid; k < ND; k += nthr) {
-	int ly = k / DZ, lz = k % DZ;          /* halo-1 coordinates + 1 */
-	int q = (ly + 1)*PZ + (lz + 1);        /* same site in phi plane */
+      #pragma unroll
+      for (int j = 0; j < KD; j++) {
+	const int k = tid + j*NTHR;
+	if (k >= ND) break;
+	const int ly = k / DZ, lz = k % DZ;    /* halo-1 coordinates + 1 */
+	const int q = (ly + 1)*PZ + (lz + 1);  /* same site in phi plane */
 	T c = pc[q];
 	T xp = pp[q], xm = pm[q];
 	T yp = pc[q + PZ], ym = pc[q - PZ];
@@ -163,7 +212,7 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 	g[1] = T(0.5)*(yp - ym);
 	g[2] = T(0.5)*(zp - zm);
 	T delsq = xp + xm + yp + ym + zp + zm - T(6.0)*c;
-	T p0 = lgb_symm_p0<T>(a.fe, c, delsq, g);
+	T p0 = lgb_symm_p0<T>(pa, pb, kappa, c, delsq, g);
 	T p0z = p0*T(0.0);
 	#pragma unroll
 	for (int ia = 0; ia < 3; ia++) {
@@ -172,24 +221,33 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 	    D[(3*ia + ib)*ND + k] = ((ia == ib) ? p0 : p0z) + kappa*g[ia]*g[ib];
 	  }
 	}
-	D[9*ND + k] = lgb_symm_mu<T>(a.fe, c, delsq);
+	D[9*ND + k] = lgb_symm_mu<T>(pa, pb, kappa, c, delsq);
       }
     };
+
+    const int yg = y0 + ty, zg = z0 + tz;
+    const bool active = (yg < d.ny) && (zg < d.nz);
+    const int ygw = active ? yg : 0, zgw = active ? zg : 0;
+
+    /* Wrapped offsets of the pull sources in y and z (fixed per item):
+     * a population with c_y = +1 comes from y - 1, etc. */
+    const int oyp = (ygw == 0) ? (d.ny - 1)*d.nz : -d.nz;
+    const int oym = (ygw == d.ny - 1) ? -(d.ny - 1)*d.nz : d.nz;
+    const int ozp = (zgw == 0) ? d.nz - 1 : -1;
+    const int ozm = (zgw == d.nz - 1) ? -(d.nz - 1) : 1;
+    const int syz = ygw*d.nz + zgw;
 
     /* ---- prologue: D(x0-1), D(x0) and the x0-1 column registers ---- */
 
     load_phi(x0 - 2);
     load_phi(x0 - 1);
     load_phi(x0);
+    load_phi(x0 + 1);
+    __pipeline_commit();
+    __pipeline_wait_prior(0);
     __syncthreads();
     compute_D(x0 - 1);
     __syncthreads();
-
-    const int cidx = (ty + 1)*DZ + (tz + 1);       /* own site in D/u */
-    const int pidx = (ty + 2)*PZ + (tz + 2);       /* own site in phi */
-    const int yg = y0 + ty, zg = z0 + tz;
-    const bool active = (yg < d.ny) && (zg < d.nz);
-    const int ygw = active ? yg : 0, zgw = active ? zg : 0;
 
     T prevP[3], prev_mu, prev_phi, prev_ux;
     {
@@ -198,44 +256,57 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
       for (int ia = 0; ia < 3; ia++) prevP[ia] = D[(3*ia)*ND + cidx];
       prev_mu = D[9*ND + cidx];
       prev_phi = sphi[pslot(x0 - 1)*NPHI + pidx];
-      prev_ux = u_in[(long long) lgb_mod(x0 - 1, d.nx)*NP
-		     + (long long) ygw*d.nz + zgw];
+      prev_ux = u_in[(long long) lgb_wrap_far(x0 - 1, d.nx)*NP + syz];
     }
-    __syncthreads();
-    load_phi(x0 + 1);
-    __syncthreads();
     compute_D(x0);
-    __syncthreads();
+    load_phi(x0 + 2);
+    load_u(x0);
+    __pipeline_commit();
 
     /* ---- march along x ---- */
 
     for (int x = x0; x < xe; x++) {
 
-      load_phi(x + 2);
-      load_u(x);
+      const long long s0 = (long long) x*NP + syz;
+      const int oxp = (x == 0) ? (d.nx - 1)*NP : -NP;
+      const int oxm = (x == d.nx - 1) ? -(d.nx - 1)*NP : NP;
+
+      /* Pulled populations f_p(x - c_p): issued first, consumed after the
+       * stencil phase, so their latency overlaps it. */
+      T fs[LGB_NVEL];
+      if (active) {
+	const S * fb = f_in + s0;
+	Unroll<LGB_NVEL>::run([&](auto P) {
+	  constexpr int p = decltype(P)::value;
+	  int off = 0;
+	  if (Cv<p>::X == +1) off += oxp;
+	  if (Cv<p>::X == -1) off += oxm;
+	  if (Cv<p>::Y == +1) off += oyp;
+	  if (Cv<p>::Y == -1) off += oym;
+	  if (Cv<p>::Z == +1) off += ozp;
+	  if (Cv<p>::Z == -1) off += ozm;
+	  fs[p] = FStore<S, T>::ld(fb + p*N + off, rfscale);
+	});
+      }
+
+      /* phi(x+2) and u(x) have landed; stream phi(x+3) and u(x+1) into
+       * the slots of phi(x-1) and u(x-1), free since the last barrier */
+      __pipeline_wait_prior(0);
       __syncthreads();
+      if (x + 1 < xe) {
+	load_phi(x + 3);
+	load_u(x + 1);
+      }
+      __pipeline_commit();
       compute_D(x + 1);
       __syncthreads();
 
       if (active) {
-	const long long s0 = (long long) x*NP + (long long) yg*d.nz + zg;
-
-	/* Pulled populations f_p(x - c_p): issue the loads first */
-	T fs[LGB_NVEL];
-	Unroll<LGB_NVEL>::run([&](auto P) {
-	  constexpr int p = decltype(P)::value;
-	  int xs = x - Cv<p>::X, ys = yg - Cv<p>::Y, zs = zg - Cv<p>::Z;
-	  if (Cv<p>::X != 0) xs = lgb_wrap(xs, d.nx);
-	  if (Cv<p>::Y != 0) ys = lgb_wrap(ys, d.ny);
-	  if (Cv<p>::Z != 0) zs = lgb_wrap(zs, d.nz);
-	  long long j = (long long) xs*NP + (long long) ys*d.nz + zs;
-	  fs[p] = FStore<S, T>::ld(f_in + p*N + j, rfscale);
-	});
-
 	const T * Dc = sD + dslot(x)*SM::NDC*ND;
 	const T * Dn = sD + dslot(x + 1)*SM::NDC*ND;
 	const T * pc = sphi + pslot(x)*NPHI;
 	const T * pn = sphi + pslot(x + 1)*NPHI;
+	const T * su = uslot(x);
 
 	/* Force: src/phi_force_colloid.c:352-455 */
 	T force[3];
@@ -268,8 +339,7 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 	  fw -= mobility*(muc - prev_mu);
 	}
 	{
-	  const T uxp = u_in[(long long) lgb_wrap(x + 1, d.nx)*NP
-			     + (long long) yg*d.nz + zg];
+	  const T uxp = u_in[s0 + oxm];
 	  const T phip = pn[pidx];
 	  const T mup = Dn[9*ND + cidx];
 	  T uf = T(0.5)*(uxc + uxp);
@@ -299,17 +369,13 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 
 	bool fluid = true;
 	if (HAS_MAP) {
-	  auto fl = [&](int xx, int yy, int zz) -> T {
-	    long long j = (long long) lgb_wrap(xx, d.nx)*NP
-	      + (long long) lgb_wrap(yy, d.ny)*d.nz + lgb_wrap(zz, d.nz);
-	    return (T) (st[j] == 0);
-	  };
-	  T m0 = fl(x, yg, zg);
-	  T mym = fl(x, yg - 1, zg), mzm = fl(x, yg, zg - 1);
-	  fw  *= m0*fl(x - 1, yg, zg);
-	  fe  *= m0*fl(x + 1, yg, zg);
-	  fy  *= m0*fl(x, yg + 1, zg);
-	  fz  *= m0*fl(x, yg, zg + 1);
+	  /* pull offsets double as neighbour offsets: x-1 is s0 + oxp, etc. */
+	  const T m0 = (T) (st[s0] == 0);
+	  const T mym = (T) (st[s0 + oyp] == 0), mzm = (T) (st[s0 + ozp] == 0);
+	  fw  *= m0*((T) (st[s0 + oxp] == 0));
+	  fe  *= m0*((T) (st[s0 + oxm] == 0));
+	  fy  *= m0*((T) (st[s0 + oym] == 0));
+	  fz  *= m0*((T) (st[s0 + ozm] == 0));
 	  fym *= mym*m0;
 	  fzm *= mzm*m0;
 	  fluid = (st[s0] == 0);
@@ -326,7 +392,8 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 	T ftot[3];
 	#pragma unroll
 	for (int ia = 0; ia < 3; ia++) {
-	  ftot[ia] = ((T) a.cp.force_global[ia]) + (T(0.0) + force[ia]*T(1.0));
+	  ftot[ia] = KP<T>::get(a, LGBK_P_FX + ia)
+	    + (T(0.0) + force[ia]*T(1.0));
 	}
 	if (force_out) {
 	  #pragma unroll
@@ -335,22 +402,69 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 
 	T rho, uu[3];
 	if (fluid) {
-	  lgb_collide_site<T, SEQ, SHIFT, GZERO>(a.cp, rho0, fs, ftot, rho, uu);
+	  lgb_collide_site<T, SEQ, SHIFT, GZERO>(
+	    KP<T>::get(a, LGBK_P_RTAU_SHEAR), KP<T>::get(a, LGBK_P_RTAU_BULK),
+	    a.cp.rtau_ghost, rho0, fs, ftot, rho, uu);
 	  rho_out[s0] = rho;
 	}
 	else {
 	  uu[0] = uu[1] = uu[2] = T(0.0);
 	}
+	S * ob = f_out + s0;
 	#pragma unroll
 	for (int p = 0; p < LGB_NVEL; p++) {
-	  FStore<S, T>::st(f_out + p*N + s0, fs[p], fscale);
+	  FStore<S, T>::st(ob + p*N, fs[p], fscale);
 	}
 	#pragma unroll
 	for (int ia = 0; ia < 3; ia++) u_out[ia*N + s0] = uu[ia];
       }
-      __syncthreads();
     }
+    __pipeline_wait_prior(0);
     __syncthreads();
+  }
+}
+
+template <typename T, typename S, bool SEQ, bool SHIFT, bool GZERO,
+	  bool HAS_MAP, int TY, int MINB>
+__global__ void __launch_bounds__(32*TY, MINB)
+k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
+  extern __shared__ unsigned char smem_raw[];
+  const int ntz = (d.nz + 31)/32;
+  const int nty = (d.ny + TY - 1)/TY;
+  const int ncx = (d.nx + xchunk - 1)/xchunk;
+  const int nitems = ntz*nty*ncx;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int itz = item % ntz;
+    const int ity = (item / ntz) % nty;
+    const int icx = item / (ntz*nty);
+    binary_item<T, S, SEQ, SHIFT, GZERO, HAS_MAP, TY>(d, a, xchunk, itz, ity,
+						      icx, smem_raw);
+  }
+}
+
+/* Ensemble of independent boxes: box descriptors and a flat list of
+ * (box, local item) pairs; one launch covers every box.  Boxes marked
+ * inactive (quarantined) are skipped. */
+template <typename T, typename S, bool SEQ, bool SHIFT, bool GZERO,
+	  bool HAS_MAP, int TY, int MINB>
+__global__ void __launch_bounds__(32*TY, MINB)
+k_binary_ensemble(const lgbk_box_t * __restrict__ boxes,
+		  const int2 * __restrict__ items, int nitems, int xchunk) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ lgbk_box_t sb;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int2 it = items[item];
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) sb = boxes[it.x];
+    __syncthreads();
+    if (!sb.active) continue;
+    const int ntz = (sb.d.nz + 31)/32;
+    const int nty = (sb.d.ny + TY - 1)/TY;
+    const int itz = it.y % ntz;
+    const int ity = (it.y / ntz) % nty;
+    const int icx = it.y / (ntz*nty);
+    binary_item<T, S, SEQ, SHIFT, GZERO, HAS_MAP, TY>(sb.d, sb.a, xchunk, itz,
+						      ity, icx, smem_raw);
   }
 }
 

@@ -16,6 +16,9 @@
 extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
 				    const lgbk_binary_args_t * a, int xchunk,
 				    int ty, void * stream);
+extern "C" int lgbk_ensemble_step_f64(const lgbk_box_t * boxes,
+				      const void * items, int nitems,
+				      int xchunk, int has_map, void * stream);
 
 template <typename S, bool HAS_MAP, int TY, int MINB>
 static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
@@ -42,24 +45,36 @@ static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
   return (int) cudaGetLastError();
 }
 
+/* Tile height and resident CTAs per SM (register cap 65536/(32*TY*MINB)):
+ * (8,4) and (16,2) and (4,8) cap at 64 registers, (8,3) at 85, (8,2) at 128.
+ * minb = 0 picks the default for the tile height. */
 template <typename S>
 static int dispatch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
-		      int xchunk, int ty, cudaStream_t s) {
+		      int xchunk, int ty, int minb, cudaStream_t s) {
+  const bool m = (a->status != NULL);
   if (ty == 4) {
-    return a->status ? launch32<S, true, 4, 4>(d, a, xchunk, s)
-                     : launch32<S, false, 4, 4>(d, a, xchunk, s);
+    return m ? launch32<S, true, 4, 8>(d, a, xchunk, s)
+             : launch32<S, false, 4, 8>(d, a, xchunk, s);
   }
   if (ty == 16) {
-    return a->status ? launch32<S, true, 16, 1>(d, a, xchunk, s)
-                     : launch32<S, false, 16, 1>(d, a, xchunk, s);
+    return m ? launch32<S, true, 16, 2>(d, a, xchunk, s)
+             : launch32<S, false, 16, 2>(d, a, xchunk, s);
   }
-  return a->status ? launch32<S, true, 8, 2>(d, a, xchunk, s)
-                   : launch32<S, false, 8, 2>(d, a, xchunk, s);
+  if (minb == 2) {
+    return m ? launch32<S, true, 8, 2>(d, a, xchunk, s)
+             : launch32<S, false, 8, 2>(d, a, xchunk, s);
+  }
+  if (minb == 3) {
+    return m ? launch32<S, true, 8, 3>(d, a, xchunk, s)
+             : launch32<S, false, 8, 3>(d, a, xchunk, s);
+  }
+  return m ? launch32<S, true, 8, 4>(d, a, xchunk, s)
+           : launch32<S, false, 8, 4>(d, a, xchunk, s);
 }
 
 extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 				const lgbk_binary_args_t * a, int xchunk,
-				int ty, void * stream) {
+				int ty, int minb, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
   if (xchunk <= 0) xchunk = 32;
   if (ty <= 0) ty = 8;
@@ -68,13 +83,92 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
     return lgbk_binary_step_f64(d, a, xchunk, ty, stream);
   case LGBK_PREC_FP32:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<float>(d, a, xchunk, ty, s);
+    return dispatch32<float>(d, a, xchunk, ty, minb, s);
   case LGBK_PREC_FP16:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<__half>(d, a, xchunk, ty, s);
+    return dispatch32<__half>(d, a, xchunk, ty, minb, s);
   default:
     return (int) cudaErrorInvalidValue;
   }
+}
+
+/*****************************************************************************
+ *
+ *  Ensembles of boxes (one launch for all boxes)
+ *
+ *****************************************************************************/
+
+template <typename S, bool HAS_MAP, int TY, int MINB>
+static int launch_ens32(const lgbk_box_t * boxes, const void * items,
+			int nitems, int xchunk, cudaStream_t stream) {
+  auto kern = k_binary_ensemble<float, S, false, true, true, HAS_MAP, TY,
+				MINB>;
+  size_t smem = FusedSmem<float, TY>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TY, smem);
+  if (occ < 1) occ = 1;
+  long long grid = (long long) nsm*occ;
+  if (grid > nitems) grid = nitems;
+  if (grid < 1) return 0;
+  kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(
+    boxes, (const int2 *) items, nitems, xchunk);
+  return (int) cudaGetLastError();
+}
+
+template <typename S>
+static int dispatch_ens32(const lgbk_box_t * b, const void * it, int n,
+			  int xchunk, int ty, int minb, int m,
+			  cudaStream_t s) {
+  if (ty == 4) {
+    return m ? launch_ens32<S, true, 4, 8>(b, it, n, xchunk, s)
+             : launch_ens32<S, false, 4, 8>(b, it, n, xchunk, s);
+  }
+  if (ty == 16) {
+    return m ? launch_ens32<S, true, 16, 2>(b, it, n, xchunk, s)
+             : launch_ens32<S, false, 16, 2>(b, it, n, xchunk, s);
+  }
+  if (minb == 3) {
+    return m ? launch_ens32<S, true, 8, 3>(b, it, n, xchunk, s)
+             : launch_ens32<S, false, 8, 3>(b, it, n, xchunk, s);
+  }
+  return m ? launch_ens32<S, true, 8, 4>(b, it, n, xchunk, s)
+           : launch_ens32<S, false, 8, 4>(b, it, n, xchunk, s);
+}
+
+extern "C" int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes,
+				  const void * items, int nitems, int xchunk,
+				  int ty, int minb, int has_map,
+				  void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  switch (prec) {
+  case LGBK_PREC_FP64:
+    return lgbk_ensemble_step_f64(boxes, items, nitems, xchunk, has_map,
+				  stream);
+  case LGBK_PREC_FP32:
+    return dispatch_ens32<float>(boxes, items, nitems, xchunk, ty, minb,
+				 has_map, s);
+  case LGBK_PREC_FP16:
+    return dispatch_ens32<__half>(boxes, items, nitems, xchunk, ty, minb,
+				  has_map, s);
+  default:
+    return (int) cudaErrorInvalidValue;
+  }
+}
+
+extern "C" int lgbk_ensemble_items(const lgbk_dims_t * d, int box,
+				   int xchunk, int ty, int * items) {
+  int ntz = (d->nz + 31)/32, nty = (d->ny + ty - 1)/ty;
+  int ncx = (d->nx + xchunk - 1)/xchunk;
+  int n = ntz*nty*ncx;
+  if (items) {
+    for (int k = 0; k < n; k++) { items[2*k] = box; items[2*k + 1] = k; }
+  }
+  return n;
 }
 
 /*****************************************************************************

@@ -49,3 +49,36 @@ extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
   return a->status ? launch64<false, true>(d, a, xchunk, ty, s)
                    : launch64<false, false>(d, a, xchunk, ty, s);
 }
+
+/* Ensembles in FP64 (tile 8 x 32, 2 CTAs per SM) */
+template <bool HAS_MAP>
+static int launch_ens64(const lgbk_box_t * boxes, const void * items,
+			int nitems, int xchunk, cudaStream_t stream) {
+  constexpr int TY = 8;
+  auto kern = k_binary_ensemble<double, double, true, false, true, HAS_MAP,
+				TY, 2>;
+  size_t smem = FusedSmem<double, TY>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TY, smem);
+  if (occ < 1) occ = 1;
+  long long grid = (long long) nsm*occ;
+  if (grid > nitems) grid = nitems;
+  if (grid < 1) return 0;
+  kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(
+    boxes, (const int2 *) items, nitems, xchunk);
+  return (int) cudaGetLastError();
+}
+
+/* Requires every box to relax its ghost modes with rtau = 1 (M10). */
+extern "C" int lgbk_ensemble_step_f64(const lgbk_box_t * boxes,
+				      const void * items, int nitems,
+				      int xchunk, int has_map, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  return has_map ? launch_ens64<true>(boxes, items, nitems, xchunk, s)
+                 : launch_ens64<false>(boxes, items, nitems, xchunk, s);
+}

@@ -85,6 +85,14 @@ int lgbk_fill_f64(double * a, long long n, double v, void * stream);
 /* Fused binary-fluid step (one kernel per step).
  * Input f is the post-collision state of the previous step (its streamed
  * image is the reference's f); output likewise.  force_out may be NULL. */
+/* Scalar parameters of the fused step, as doubles (pd) and as floats (pf)
+ * so that reduced-precision kernels use them without conversions */
+enum lgbk_param_index {
+  LGBK_P_RTAU_SHEAR, LGBK_P_RTAU_BULK, LGBK_P_FX, LGBK_P_FY, LGBK_P_FZ,
+  LGBK_P_MOBILITY, LGBK_P_RHO0, LGBK_P_FSCALE, LGBK_P_RFSCALE,
+  LGBK_P_A, LGBK_P_B, LGBK_P_KAPPA, LGBK_NPARAM
+};
+
 typedef struct lgbk_binary_args_s {
   const void * f_in;   void * f_out;
   const void * phi_in; void * phi_out;
@@ -97,10 +105,46 @@ typedef struct lgbk_binary_args_s {
   double fscale;       /* FP16 storage: stored = (f - w rho0)*fscale */
   lgbk_symm_t fe;
   lgbk_collide_t cp;
+  double pd[LGBK_NPARAM];
+  float pf[LGBK_NPARAM];
 } lgbk_binary_args_t;
 
+/* Fill pd/pf from the other members */
+static inline void lgbk_binary_args_pack(lgbk_binary_args_t * a) {
+  a->pd[LGBK_P_RTAU_SHEAR] = a->cp.rtau_shear;
+  a->pd[LGBK_P_RTAU_BULK] = a->cp.rtau_bulk;
+  a->pd[LGBK_P_FX] = a->cp.force_global[0];
+  a->pd[LGBK_P_FY] = a->cp.force_global[1];
+  a->pd[LGBK_P_FZ] = a->cp.force_global[2];
+  a->pd[LGBK_P_MOBILITY] = a->mobility;
+  a->pd[LGBK_P_RHO0] = a->rho0;
+  a->pd[LGBK_P_FSCALE] = a->fscale;
+  a->pd[LGBK_P_RFSCALE] = 1.0/a->fscale;
+  a->pd[LGBK_P_A] = a->fe.a;
+  a->pd[LGBK_P_B] = a->fe.b;
+  a->pd[LGBK_P_KAPPA] = a->fe.kappa;
+  for (int i = 0; i < LGBK_NPARAM; i++) a->pf[i] = (float) a->pd[i];
+}
+
+/* A box of an ensemble: its lattice, its step arguments, and whether it
+ * is still stepped (0 once quarantined). */
+typedef struct lgbk_box_s {
+  lgbk_dims_t d;
+  lgbk_binary_args_t a;
+  int active;
+} lgbk_box_t;
+
+/* One step of every active box: items[k] = (box, item within the box),
+ * built for tile height ty and xchunk by lgbk_ensemble_items(). */
+int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes_dev,
+		       const void * items_dev, int nitems, int xchunk, int ty,
+		       int minb, int has_map, void * stream);
+/* Number of work items of one box (and fill items if non-NULL, host) */
+int lgbk_ensemble_items(const lgbk_dims_t * d, int box, int xchunk, int ty,
+			int * items);
+
 int lgbk_binary_step(const lgbk_dims_t * d, int prec,
-		     const lgbk_binary_args_t * a, int xchunk, int ty,
+		     const lgbk_binary_args_t * a, int xchunk, int ty, int minb,
 		     void * stream);
 
 /* Conversions between FP64 canonical state and reduced storage */

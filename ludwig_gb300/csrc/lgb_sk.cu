@@ -1,0 +1,157 @@
+/*****************************************************************************
+ *
+ *  lgb_sk.cu
+ *
+ *  Spherically averaged structure factor S(|k|) of a scalar field and the
+ *  domain length L = 2 pi sum S dk / sum k S dk (util/length_from_sk.c:
+ *  88-190).  The 3-d transform is three passes of direct 1-d DFTs (one
+ *  line per CTA, twiddles from a table), accurate in FP64 accumulation;
+ *  this is a diagnostic computed between steps, not part of the step.
+ *
+ *  Binning follows the reference: half space k_z in [0, N/2], 128 bins of
+ *  width sqrt(3) pi / 128.  With faithful = 1 the reference's wavevector
+ *  for i > N/2 is dk*i - pi (its util/length_from_sk.c:138, which
+ *  subtracts pi rather than 2 pi); faithful = 0 uses dk*i - 2 pi.  The
+ *  corner |k| = sqrt(3) pi falls in the last bin (the reference would
+ *  index one past the end there).
+ *
+ *****************************************************************************/
+
+#include "lgb_common.cuh"
+#include "lgb_sk.h"
+
+/* One 1-d DFT along axis `axis` for every line: out[k] = sum_n in[n] w^kn,
+ * w = exp(-2 pi i / n).  in/out: complex double2 arrays in the canonical
+ * site order.  One CTA per line; the line is staged in shared memory. */
+__global__ void k_dft_axis(lgbk_dims_t d, int axis,
+			   const double2 * __restrict__ in,
+			   double2 * __restrict__ out,
+			   const double2 * __restrict__ tw) {
+  extern __shared__ double2 line[];
+  const int n = (axis == 0) ? d.nx : ((axis == 1) ? d.ny : d.nz);
+  const long long stride = (axis == 0) ? (long long) d.ny*d.nz
+    : ((axis == 1) ? d.nz : 1);
+  /* line index -> base site */
+  long long li = blockIdx.x;
+  long long base;
+  if (axis == 2) base = li*d.nz;
+  else if (axis == 1) {
+    long long x = li / d.nz, z = li % d.nz;
+    base = x*(long long) d.ny*d.nz + z;
+  }
+  else base = li;                        /* x-lines: li = y*nz + z */
+
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    line[i] = in[base + i*stride];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    double re = 0.0, im = 0.0;
+    int idx = 0;
+    for (int j = 0; j < n; j++) {
+      const double2 w = tw[idx];
+      const double2 v = line[j];
+      re += v.x*w.x - v.y*w.y;
+      im += v.x*w.y + v.y*w.x;
+      idx += k;
+      if (idx >= n) idx -= n;
+    }
+    out[base + k*stride] = make_double2(re, im);
+  }
+}
+
+template <typename T>
+__global__ void k_to_complex(long long n, const T * __restrict__ a,
+			     double2 * __restrict__ c) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i < n) c[i] = make_double2((double) a[i], 0.0);
+}
+
+__global__ void k_bin_sk(lgbk_dims_t d, int faithful,
+			 const double2 * __restrict__ c,
+			 double * __restrict__ sk, double * __restrict__ nk) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  const int nzh = d.nz/2 + 1;
+  long long nh = (long long) d.nx*d.ny*nzh;
+  if (i >= nh) return;
+  int k = (int) (i % nzh);
+  long long r = i / nzh;
+  int j = (int) (r % d.ny);
+  int ii = (int) (r / d.ny);
+  const double pi = 3.14159265358979323846;
+  const double shift = faithful ? pi : 2.0*pi;
+  double kx = 2.0*pi*ii/d.nx; if (ii > d.nx/2) kx -= shift;
+  double ky = 2.0*pi*j/d.ny;  if (j > d.ny/2) ky -= shift;
+  double kz = 2.0*pi*k/d.nz;
+  double kmod = sqrt(kx*kx + ky*ky + kz*kz);
+  int n = (int) floor(kmod*LGBK_SK_NBIN/(sqrt(3.0)*pi));
+  if (n >= LGBK_SK_NBIN) n = LGBK_SK_NBIN - 1;
+  const double2 v = c[((long long) ii*d.ny + j)*d.nz + k];
+  atomicAdd(sk + n, v.x*v.x + v.y*v.y);
+  atomicAdd(nk + n, 1.0);
+}
+
+extern "C" int lgbk_structure_factor(const lgbk_dims_t * d, int prec,
+				     const void * phi, int faithful,
+				     void * work, double * sk_host,
+				     double * nk_host, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  const long long N = d->nsites;
+  double2 * a = (double2 *) work;
+  double2 * b = a + N;
+  double2 * tw = b + N;                  /* up to 3 tables of n entries */
+  double * bins = (double *) (tw + (d->nx + d->ny + d->nz));
+  const int nmax = (d->nx > d->ny) ? ((d->nx > d->nz) ? d->nx : d->nz)
+    : ((d->ny > d->nz) ? d->ny : d->nz);
+  if (nmax > LGBK_SK_NMAX) return (int) cudaErrorInvalidValue;
+
+  /* twiddle tables exp(-2 pi i m / n), computed on the host in double */
+  double2 twh[3*LGBK_SK_NMAX];
+  const int ns[3] = {d->nx, d->ny, d->nz};
+  int off[3] = {0, d->nx, d->nx + d->ny};
+  for (int ax = 0; ax < 3; ax++) {
+    for (int m = 0; m < ns[ax]; m++) {
+      double ang = -2.0*3.14159265358979323846*(double) m/ns[ax];
+      twh[off[ax] + m] = make_double2(cos(ang), sin(ang));
+    }
+  }
+  cudaError_t err = cudaMemcpyAsync(tw, twh, (d->nx + d->ny + d->nz)
+				    *sizeof(double2), cudaMemcpyHostToDevice, s);
+  if (err != cudaSuccess) return (int) err;
+
+  dim3 g((unsigned int) ((N + 255)/256));
+  if (prec == LGBK_PREC_FP64) {
+    k_to_complex<double><<<g, 256, 0, s>>>(N, (const double *) phi, a);
+  }
+  else {
+    k_to_complex<float><<<g, 256, 0, s>>>(N, (const float *) phi, a);
+  }
+  /* z lines, then y lines, then x lines */
+  k_dft_axis<<<(unsigned int) (N/d->nz), 128, d->nz*sizeof(double2), s>>>(
+    *d, 2, a, b, tw + off[2]);
+  k_dft_axis<<<(unsigned int) (N/d->ny), 128, d->ny*sizeof(double2), s>>>(
+    *d, 1, b, a, tw + off[1]);
+  k_dft_axis<<<(unsigned int) (N/d->nx), 128, d->nx*sizeof(double2), s>>>(
+    *d, 0, a, b, tw + off[0]);
+  err = cudaMemsetAsync(bins, 0, 2*LGBK_SK_NBIN*sizeof(double), s);
+  if (err != cudaSuccess) return (int) err;
+  long long nh = (long long) d->nx*d->ny*(d->nz/2 + 1);
+  k_bin_sk<<<(unsigned int) ((nh + 255)/256), 256, 0, s>>>(
+    *d, faithful, b, bins, bins + LGBK_SK_NBIN);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  err = cudaMemcpyAsync(sk_host, bins, LGBK_SK_NBIN*sizeof(double),
+			cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) {
+    err = cudaMemcpyAsync(nk_host, bins + LGBK_SK_NBIN,
+			  LGBK_SK_NBIN*sizeof(double), cudaMemcpyDeviceToHost,
+			  s);
+  }
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  return (int) err;
+}
+
+extern "C" size_t lgbk_structure_factor_work_bytes(const lgbk_dims_t * d) {
+  return (size_t) (2*d->nsites + d->nx + d->ny + d->nz)*sizeof(double2)
+    + 2*LGBK_SK_NBIN*sizeof(double);
+}

@@ -29,6 +29,8 @@
 #include "ludwig_gb.h"
 #include "lgb_kernels.h"
 #include "lgb_stats.h"
+#include "lgb_lc.h"
+#include "lgb_sk.h"
 
 #define NVEL LGB_NVEL
 
@@ -66,8 +68,9 @@ const char * ludwig_gb_version(void) { return "ludwig-gb300 0.1"; }
 
 static cudaStream_t stream_ = NULL;
 static double * red_scratch_ = NULL;
-static int tune_xchunk_ = 32;
+static int tune_xchunk_ = 16;
 static int tune_ty_ = 8;
+static int tune_minb_ = 3;
 
 static int lib_init(void) {
   if (stream_ == NULL) {
@@ -97,12 +100,15 @@ int ludwig_gb_sync(void) {
   return LUDWIG_GB_OK;
 }
 
-int ludwig_gb_tune_set(int xchunk, int tile_y) {
-  if (xchunk < 1 || (tile_y != 4 && tile_y != 8 && tile_y != 16)) {
-    return err_set(LUDWIG_GB_EINVAL, "tune: xchunk >= 1, tile_y in {4,8,16}");
+int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks) {
+  if (xchunk < 1 || (tile_y != 4 && tile_y != 8 && tile_y != 16) ||
+      min_blocks < 0 || min_blocks > 4) {
+    return err_set(LUDWIG_GB_EINVAL, "tune: xchunk >= 1, tile_y in {4,8,16},"
+		   " min_blocks in 0..4");
   }
   tune_xchunk_ = xchunk;
   tune_ty_ = tile_y;
+  tune_minb_ = min_blocks;
   return LUDWIG_GB_OK;
 }
 
@@ -925,6 +931,7 @@ static int fe_symm_get(fe_t * fe, fe_symm_t ** s) {
   return LUDWIG_GB_OK;
 }
 
+
 /*****************************************************************************
  *  Force: pth_t and phi_force_calculation
  *****************************************************************************/
@@ -956,17 +963,23 @@ int pth_free(pth_t * pth) {
   return LUDWIG_GB_OK;
 }
 
+static int lc_stress_compute(pth_t * pth, fe_lc_t * fe);
+static int collide_param(lb_t * lb, lgbk_collide_t * cp);
+
 int pth_stress_compute(pth_t * pth, fe_t * fe) {
+  if (pth == NULL || fe == NULL) return err_set(LUDWIG_GB_EINVAL, "pth");
+  if (pth->str == NULL) {
+    int rc = dev_alloc((void **) &pth->str, 9*(size_t) pth->cs->d.nsites
+		       *sizeof(double), "pth");
+    if (rc) return rc;
+  }
+  if (fe->id == FE_LC) return lc_stress_compute(pth, (fe_lc_t *) fe);
+
   fe_symm_t * s = NULL;
   int rc = fe_symm_get(fe, &s);
   if (rc) return rc;
   if (s->phi->prec != LUDWIG_GB_FP64) {
     return err_set(LUDWIG_GB_EINVAL, "pth_stress_compute: FP64 only");
-  }
-  if (pth->str == NULL) {
-    rc = dev_alloc((void **) &pth->str, 9*(size_t) pth->cs->d.nsites
-		   *sizeof(double), "pth");
-    if (rc) return rc;
   }
   rc = grad_alloc(s->dphi);
   if (rc) return rc;
@@ -1005,6 +1018,353 @@ int phi_force_calculation(pe_t * pe, cs_t * cs, lees_edw_t * le,
 			stream_), "force");
   CK(cudaStreamSynchronize(stream_), "sync");
   return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Cholesteric liquid crystal: fe_lc_t, Beris-Edwards
+ *****************************************************************************/
+
+struct fe_lc_s {
+  fe_t super;
+  fe_lc_param_t param;
+  field_t * q;
+  field_grad_t * dq;
+};
+
+static void lc_kparam(const fe_lc_t * fe, lgbk_lc_t * k) {
+  memset(k, 0, sizeof(*k));
+  k->a0 = fe->param.a0;
+  k->q0 = fe->param.q0;
+  k->gamma = fe->param.gamma;
+  k->kappa0 = fe->param.kappa0;
+  k->kappa1 = fe->param.kappa1;
+  k->xi = fe->param.xi;
+  k->redshift = fe->param.redshift;
+  k->rredshift = fe->param.rredshift;
+  k->epsilon = fe->param.epsilon;
+  for (int i = 0; i < 3; i++) k->e0[i] = fe->param.e0[i];
+  k->coswt = fe->param.coswt;
+}
+
+static int lc_ready(fe_lc_t * fe) {
+  if (fe->q->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "liquid crystal: FP64 fields only");
+  }
+  if (fe->dq->grad == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "liquid crystal: call "
+		   "field_grad_compute() on the q gradients first");
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int lc_stress_compute(pth_t * pth, fe_lc_t * fe) {
+  int rc = lc_ready(fe);
+  if (rc) return rc;
+  lgbk_lc_t k;
+  lc_kparam(fe, &k);
+  CK(lgbk_lc_stress_f64(&pth->cs->d, &k, (const double *) fe->q->data,
+			fe->dq->grad, fe->dq->delsq, pth->str, stream_),
+     "lc_stress");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* Per-site vtable entries: evaluate on the lattice, return one site. */
+static int lc_site_eval(fe_lc_t * fe, int index, int what, double * out) {
+  const lgbk_dims_t * d = &fe->q->cs->d;
+  double * tmp = NULL;
+  int ncomp = (what == 0) ? 1 : ((what == 1) ? 9 : 5);
+  int rc = lc_ready(fe);
+  if (rc) return rc;
+  if (index < 0 || index >= d->nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "site index out of range");
+  }
+  rc = dev_alloc((void **) &tmp, (size_t) ncomp*d->nsites*sizeof(double),
+		 "lc_site");
+  if (rc) return rc;
+  lgbk_lc_t k;
+  lc_kparam(fe, &k);
+  const double * q = (const double *) fe->q->data;
+  if (what == 0) rc = lgbk_lc_fed_f64(d, &k, q, fe->dq->grad, tmp, stream_);
+  if (what == 1) rc = lgbk_lc_stress_f64(d, &k, q, fe->dq->grad,
+					 fe->dq->delsq, tmp, stream_);
+  if (what == 2) rc = lgbk_lc_h_f64(d, &k, q, fe->dq->grad, fe->dq->delsq,
+				    tmp, stream_);
+  if (rc == 0) rc = cudaStreamSynchronize(stream_);
+  for (int n = 0; rc == 0 && n < ncomp; n++) {
+    rc = cudaMemcpy(out + n, tmp + (size_t) n*d->nsites + index,
+		    sizeof(double), cudaMemcpyDeviceToHost);
+  }
+  dev_free(tmp);
+  return cuda_check(rc, "lc_site_eval");
+}
+
+static int lc_fed(fe_t * base, int index, double * fed) {
+  return lc_site_eval((fe_lc_t *) base, index, 0, fed);
+}
+
+static int lc_stress(fe_t * base, int index, double s[3][3]) {
+  return lc_site_eval((fe_lc_t *) base, index, 1, &s[0][0]);
+}
+
+static int lc_str_symm(fe_t * base, int index, double s[3][3]) {
+  double t[3][3];
+  int rc = lc_stress(base, index, t);
+  if (rc) return rc;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib] = 0.5*(t[ia][ib] + t[ib][ia]);
+  return LUDWIG_GB_OK;
+}
+
+static int lc_str_anti(fe_t * base, int index, double s[3][3]) {
+  double t[3][3];
+  int rc = lc_stress(base, index, t);
+  if (rc) return rc;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib] = 0.5*(t[ia][ib] - t[ib][ia]);
+  return LUDWIG_GB_OK;
+}
+
+static int lc_htensor(fe_t * base, int index, double h[3][3]) {
+  double h5[5];
+  int rc = lc_site_eval((fe_lc_t *) base, index, 2, h5);
+  if (rc) return rc;
+  h[0][0] = h5[0]; h[0][1] = h5[1]; h[0][2] = h5[2];
+  h[1][0] = h5[1]; h[1][1] = h5[3]; h[1][2] = h5[4];
+  h[2][0] = h5[2]; h[2][1] = h5[4]; h[2][2] = 0.0 - h5[0] - h5[3];
+  return LUDWIG_GB_OK;
+}
+
+static int lc_free(fe_t * base) { return fe_lc_free((fe_lc_t *) base); }
+static int lc_target(fe_t * base, fe_t ** t) { *t = base; return 0; }
+
+static const fe_vt_t fe_lc_vt_ = {
+  lc_free, lc_target, lc_fed, NULL, lc_stress, lc_str_symm, lc_str_anti,
+  lc_htensor
+};
+
+int fe_lc_create(pe_t * pe, cs_t * cs, lees_edw_t * le, field_t * q,
+		 field_grad_t * dq, fe_lc_t ** p) {
+  (void) pe; (void) cs;
+  if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
+  if (q == NULL || dq == NULL || p == NULL || q->nf != 5) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_lc_create: q must have 5 components");
+  }
+  fe_lc_t * fe = (fe_lc_t *) calloc(1, sizeof(fe_lc_t));
+  if (fe == NULL) return err_set(LUDWIG_GB_ENOMEM, "fe_lc_create");
+  fe->super.id = FE_LC;
+  fe->super.func = &fe_lc_vt_;
+  fe->q = q;
+  fe->dq = dq;
+  fe->param.redshift = 1.0;
+  fe->param.rredshift = 1.0;
+  fe->param.coswt = 1.0;
+  *p = fe;
+  return LUDWIG_GB_OK;
+}
+
+int fe_lc_free(fe_lc_t * fe) { free(fe); return LUDWIG_GB_OK; }
+
+int fe_lc_param_set(fe_lc_t * fe, const fe_lc_param_t * values) {
+  const double pi = 3.1415926535897932385;
+  if (fe == NULL || values == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_lc_param_set");
+  }
+  if (values->is_active || values->is_redshift_updated ||
+      values->zeta0 != 0.0 || values->zeta1 != 0.0 || values->zeta2 != 0.0) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_lc: active stress and dynamic "
+		   "redshift are not supported");
+  }
+  if (values->redshift == 0.0) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_lc: redshift must be non-zero");
+  }
+  fe->param = *values;
+  fe->param.epsilon *= (1.0/(12.0*pi));
+  fe->param.rredshift = 1.0/fe->param.redshift;
+  return LUDWIG_GB_OK;
+}
+
+int fe_lc_param(fe_lc_t * fe, fe_lc_param_t * values) {
+  if (fe == NULL || values == NULL) return err_set(LUDWIG_GB_EINVAL, "fe_lc");
+  *values = fe->param;
+  return LUDWIG_GB_OK;
+}
+
+/* src/blue_phase_init.c:59-132 without rotation; global coordinates are
+ * 1-based */
+int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
+			const double euler_angles[3]) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O8M_init");
+  }
+  if (euler_angles && (euler_angles[0] != 0.0 || euler_angles[1] != 0.0 ||
+		       euler_angles[2] != 0.0)) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O8M_init: rotation not "
+		   "supported");
+  }
+  const lgbk_dims_t * d = &cs->d;
+  const long long N = d->nsites;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "o8m");
+  const double root2 = sqrt(2.0);
+  const double q0 = param->q0, a = param->amplitude0;
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	long long i = ((long long) x*d->ny + y)*d->nz + z;
+	double r[3];
+	r[0] = (double) (x + 1) - 0.5*d->nx;
+	r[1] = (double) (y + 1) - 0.5*d->ny;
+	r[2] = (double) (z + 1) - 0.5*d->nz;
+	r[0] += 0.5*d->nx; r[1] += 0.5*d->ny; r[2] += 0.5*d->nz;
+	double cosx = cos(root2*q0*r[0]), sinx = sin(root2*q0*r[0]);
+	double cosy = cos(root2*q0*r[1]), siny = sin(root2*q0*r[1]);
+	double cosz = cos(root2*q0*r[2]), sinz = sin(root2*q0*r[2]);
+	h[0*N + i] = a*(-2.0*cosy*sinz + sinx*cosz + cosx*siny);
+	h[1*N + i] = a*(root2*cosy*cosz + root2*sinx*sinz - sinx*cosy);
+	h[2*N + i] = a*(root2*cosx*cosy + root2*sinz*siny - cosx*sinz);
+	h[3*N + i] = a*(-2.0*sinx*cosz + siny*cosx + cosy*sinz);
+	h[4*N + i] = a*(root2*cosz*cosx + root2*siny*sinx - siny*cosz);
+      }
+    }
+  }
+  int rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
+struct beris_edw_s {
+  cs_t * cs;
+  beris_edw_param_t param;
+  double * flux;               /* fw, fe, fy, fz: 4 x 5 x nsites */
+  double * h;                  /* 5 x nsites */
+};
+
+int beris_edw_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+		     beris_edw_t ** pobj) {
+  (void) pe;
+  if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
+  if (cs == NULL || !cs->initialised || pobj == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "beris_edw_create");
+  }
+  beris_edw_t * be = (beris_edw_t *) calloc(1, sizeof(beris_edw_t));
+  if (be == NULL) return err_set(LUDWIG_GB_ENOMEM, "beris_edw_create");
+  be->cs = cs;
+  size_t N = (size_t) cs->d.nsites;
+  int rc;
+  if ((rc = dev_alloc((void **) &be->flux, 20*N*sizeof(double), "flux")) ||
+      (rc = dev_alloc((void **) &be->h, 5*N*sizeof(double), "h"))) {
+    beris_edw_free(be);
+    return rc;
+  }
+  *pobj = be;
+  return LUDWIG_GB_OK;
+}
+
+int beris_edw_free(beris_edw_t * be) {
+  if (be) { dev_free(be->flux); dev_free(be->h); free(be); }
+  return LUDWIG_GB_OK;
+}
+
+int beris_edw_param_set(beris_edw_t * be, beris_edw_param_t * values) {
+  if (be == NULL || values == NULL) return err_set(LUDWIG_GB_EINVAL, "be");
+  if (values->noise) {
+    return err_set(LUDWIG_GB_EINVAL, "beris_edw: noise not supported");
+  }
+  be->param = *values;
+  return LUDWIG_GB_OK;
+}
+
+/* src/blue_phase_beris_edwards.c:266-289 */
+int beris_edw_update(beris_edw_t * be, fe_t * fe, field_t * fq,
+		     field_grad_t * fq_grad, hydro_t * hydro,
+		     colloids_info_t * cinfo, map_t * map, noise_t * noise) {
+  if (be == NULL || fe == NULL || fq == NULL || fq_grad == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "beris_edw_update");
+  }
+  if (fe->id != FE_LC) return err_set(LUDWIG_GB_EINVAL, "fe_lc required");
+  if (cinfo != NULL || noise != NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "colloids/noise not supported");
+  }
+  fe_lc_t * lc = (fe_lc_t *) fe;
+  int rc = lc_ready(lc);
+  if (rc) return rc;
+  if (hydro && hydro->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "beris_edw_update: FP64 hydro only");
+  }
+  const lgbk_dims_t * d = &be->cs->d;
+  const long long N5 = 5*d->nsites;
+  if (hydro) {
+    double * fw = be->flux, * fe_ = fw + N5, * fy = fw + 2*N5;
+    double * fz = fw + 3*N5;
+    CK(lgbk_advect_upwind_f64(d, 5, (const double *) fq->data,
+			      (const double *) hydro->u, fw, fe_, fy, fz,
+			      stream_), "advect");
+    CK(lgbk_flux_no_normal_f64(d, 5, map_dev(map), fw, fe_, fy, fz, stream_),
+       "no_flux");
+  }
+  lgbk_lc_t k;
+  lc_kparam(lc, &k);
+  CK(lgbk_lc_h_f64(d, &k, (const double *) fq->data, fq_grad->grad,
+		   fq_grad->delsq, be->h, stream_), "h");
+  CK(lgbk_be_update_f64(d, be->param.xi, be->param.gamma, map_dev(map),
+			hydro ? (const double *) hydro->u : NULL,
+			hydro ? be->flux : NULL, be->h, (double *) fq->data,
+			stream_), "be_update");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
+		      fe_t * fe, beris_edw_t * be, int nsteps) {
+  if (lb == NULL || q == NULL || hydro == NULL || fe == NULL || be == NULL ||
+      nsteps < 0 || q->nf != 5) {
+    return err_set(LUDWIG_GB_EINVAL, "ludwig_gb_lc_step");
+  }
+  if (fe->id != FE_LC) return err_set(LUDWIG_GB_EINVAL, "fe_lc required");
+  int fp = (lb->prec == LUDWIG_GB_FP64);
+  if (fp != (q->prec == LUDWIG_GB_FP64) ||
+      fp != (hydro->prec == LUDWIG_GB_FP64)) {
+    return err_set(LUDWIG_GB_EINVAL, "lc_step: lb, q and hydro must be all "
+		   "FP64 or all reduced precision");
+  }
+  fe_lc_t * lc = (fe_lc_t *) fe;
+  lgbk_lc_t k;
+  lc_kparam(lc, &k);
+  lgbk_lc_step_args_t a;
+  memset(&a, 0, sizeof(a));
+  int rc = collide_param(lb, &a.cp);
+  if (rc) return rc;
+  if (!a.cp.ghosts_zero) {
+    return err_set(LUDWIG_GB_EINVAL, "lc_step: M10 relaxation only");
+  }
+  if ((rc = lb_unstream(lb))) return rc;
+  const size_t N = (size_t) lb->cs->d.nsites;
+  const size_t es = field_size(q->prec);
+  a.status = map_dev(map);
+  a.xi = be->param.xi;
+  a.gamma_rot = be->param.gamma;
+  a.rho0 = lb->rho0;
+  a.fscale = lb->fscale;
+  a.rho_out = hydro->rho;
+  a.pth = be->flux;                                /* 9 N elements */
+  a.h = (const char *) be->flux + 9*N*es;          /* 5 N elements */
+  for (int n = 0; n < nsteps; n++) {
+    a.f_in = lb->f;   a.f_out = lb->fprime;
+    a.q_in = q->data; a.q_out = q->data2;
+    a.u_in = hydro->u; a.u_out = hydro->u2;
+    CK(lgbk_lc_step(&lb->cs->d, lb->prec, &k, &a, stream_), "lc_step");
+    lb_swap(lb);
+    void * t = q->data; q->data = q->data2; q->data2 = t;
+    t = hydro->u; hydro->u = hydro->u2; hydro->u2 = t;
+  }
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int beris_edw_h_to_host(beris_edw_t * be, double * h) {
+  if (be == NULL || h == NULL) return err_set(LUDWIG_GB_EINVAL, "be_h");
+  return copy_to_host(LUDWIG_GB_FP64, 5*be->cs->d.nsites, be->h, h);
 }
 
 /*****************************************************************************
@@ -1164,7 +1524,7 @@ int lb_propagation(lb_t * lb) {
 typedef struct graph_cache_s {
   lgbk_binary_args_t args;     /* arguments of the first step of the pair */
   int prec;
-  int xchunk, ty;
+  int xchunk, ty, minb;
   lgbk_dims_t d;
   cudaGraphExec_t exec;
   int valid;
@@ -1207,6 +1567,7 @@ static int binary_args(lb_t * lb, field_t * phi, hydro_t * hydro,
   a->rho0 = lb->rho0;
   a->fscale = lb->fscale;
   a->fe.a = s->param.a; a->fe.b = s->param.b; a->fe.kappa = s->param.kappa;
+  lgbk_binary_args_pack(a);
   return LUDWIG_GB_OK;
 }
 
@@ -1223,7 +1584,8 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
   for (int i = 0; i < 2; i++) {
     graph_cache_t * g = gcache_ + i;
     if (g->valid && g->prec == prec && g->xchunk == tune_xchunk_ &&
-	g->ty == tune_ty_ && memcmp(&g->d, d, sizeof(*d)) == 0 &&
+	g->ty == tune_ty_ && g->minb == tune_minb_ &&
+	memcmp(&g->d, d, sizeof(*d)) == 0 &&
 	memcmp(&g->args, a, sizeof(*a)) == 0) {
       *exec = g->exec;
       return LUDWIG_GB_OK;
@@ -1244,8 +1606,8 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed),
      "BeginCapture");
-  int rc1 = lgbk_binary_step(d, prec, a, tune_xchunk_, tune_ty_, stream_);
-  int rc2 = lgbk_binary_step(d, prec, &b, tune_xchunk_, tune_ty_, stream_);
+  int rc1 = lgbk_binary_step(d, prec, a, tune_xchunk_, tune_ty_, tune_minb_, stream_);
+  int rc2 = lgbk_binary_step(d, prec, &b, tune_xchunk_, tune_ty_, tune_minb_, stream_);
   int rc3 = cudaStreamEndCapture(stream_, &graph);
   if (rc1 || rc2 || rc3) {
     return cuda_check(rc1 ? rc1 : (rc2 ? rc2 : rc3), "graph capture");
@@ -1258,6 +1620,7 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
   slot->d = *d;
   slot->xchunk = tune_xchunk_;
   slot->ty = tune_ty_;
+  slot->minb = tune_minb_;
   slot->valid = 1;
   *exec = slot->exec;
   return LUDWIG_GB_OK;
@@ -1283,7 +1646,8 @@ int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
     }
   }
   if (nsteps % 2) {
-    CK(lgbk_binary_step(d, lb->prec, &a, tune_xchunk_, tune_ty_, stream_),
+    CK(lgbk_binary_step(d, lb->prec, &a, tune_xchunk_, tune_ty_, tune_minb_,
+			 stream_),
        "binary_step");
     binary_swap(lb, phi, hydro);
   }
@@ -1474,4 +1838,508 @@ int ludwig_gb_time_binary_e2e(lb_t * lb, field_t * phi, hydro_t * hydro,
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;
+}
+
+/*****************************************************************************
+ *  Domain length from the structure factor
+ *****************************************************************************/
+
+int ludwig_gb_length_from_sk(field_t * phi, int faithful, double * length,
+			     double * sk, double * nk) {
+  if (phi == NULL || phi->nf != 1 || length == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "length_from_sk: scalar field");
+  }
+  const lgbk_dims_t * d = &phi->cs->d;
+  if (d->nx > LGBK_SK_NMAX || d->ny > LGBK_SK_NMAX || d->nz > LGBK_SK_NMAX) {
+    return err_set(LUDWIG_GB_EINVAL, "length_from_sk: extent > %d",
+		   LGBK_SK_NMAX);
+  }
+  void * work = NULL;
+  double skh[LGBK_SK_NBIN], nkh[LGBK_SK_NBIN];
+  int rc = dev_alloc(&work, lgbk_structure_factor_work_bytes(d), "sk");
+  if (rc) return rc;
+  rc = lgbk_structure_factor(d, field_kprec(phi->prec), phi->data, faithful,
+			     work, skh, nkh, stream_);
+  dev_free(work);
+  if (rc) return cuda_check(rc, "structure_factor");
+
+  /* quadrature of the binned S(k), util/length_from_sk.c:170-185 */
+  const double pi = 3.14159265358979323846;
+  const double dk = sqrt(3.0)*pi/LGBK_SK_NBIN;
+  double sum1 = 0.0, sum2 = 0.0;
+  for (int k = 0; k < LGBK_SK_NBIN; k++) {
+    double sbar = (nkh[k] != 0.0) ? skh[k]/nkh[k] : 0.0;
+    double kk = (k + 0.5)*dk;
+    sum1 += dk*sbar;
+    sum2 += kk*dk*sbar;
+  }
+  *length = 2.0*pi*sum1/sum2;
+  if (sk) memcpy(sk, skh, sizeof(skh));
+  if (nk) memcpy(nk, nkh, sizeof(nkh));
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Ensembles of independent boxes
+ *****************************************************************************/
+
+struct ludwig_gb_ensemble_s {
+  int nbox;
+  int prec;
+  ludwig_gb_box_param_t * param;
+  long long * off;             /* first site of each box */
+  long long ntot;
+  int * active;
+  void * f[2];                 /* 19 x ntot each (storage type) */
+  void * phi[2];               /* ntot */
+  void * u[2];                 /* 3 x ntot */
+  void * rho;                  /* ntot */
+  lgbk_box_t * boxes_h[2];     /* arrangement k: reads buffer k */
+  lgbk_box_t * boxes_d[2];
+  int * items_d;
+  int nitems;
+  int xchunk, ty, minb;
+  int parity;                  /* buffers read by the next step */
+  cudaGraphExec_t pair[2];
+  int pair_valid[2];
+};
+
+static void ens_graph_reset(ludwig_gb_ensemble_t * e) {
+  for (int k = 0; k < 2; k++) {
+    if (e->pair_valid[k]) cudaGraphExecDestroy(e->pair[k]);
+    e->pair_valid[k] = 0;
+  }
+}
+
+static int ens_items(ludwig_gb_ensemble_t * e) {
+  int n = 0;
+  for (int b = 0; b < e->nbox; b++) {
+    lgbk_dims_t d = e->boxes_h[0][b].d;
+    n += lgbk_ensemble_items(&d, b, e->xchunk, e->ty, NULL);
+  }
+  int * h = (int *) malloc(2*(size_t) n*sizeof(int));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "ensemble items");
+  int k = 0;
+  for (int b = 0; b < e->nbox; b++) {
+    lgbk_dims_t d = e->boxes_h[0][b].d;
+    k += lgbk_ensemble_items(&d, b, e->xchunk, e->ty, h + 2*k);
+  }
+  dev_free(e->items_d);
+  e->items_d = NULL;
+  int rc = dev_alloc((void **) &e->items_d, 2*(size_t) n*sizeof(int),
+		     "items");
+  if (rc == 0) {
+    rc = cuda_check(cudaMemcpy(e->items_d, h, 2*(size_t) n*sizeof(int),
+			       cudaMemcpyHostToDevice), "items");
+  }
+  free(h);
+  e->nitems = n;
+  ens_graph_reset(e);
+  return rc;
+}
+
+static int ens_upload_boxes(ludwig_gb_ensemble_t * e) {
+  for (int k = 0; k < 2; k++) {
+    for (int b = 0; b < e->nbox; b++) e->boxes_h[k][b].active = e->active[b];
+    CK(cudaMemcpy(e->boxes_d[k], e->boxes_h[k], e->nbox*sizeof(lgbk_box_t),
+		  cudaMemcpyHostToDevice), "boxes");
+  }
+  ens_graph_reset(e);
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_free(ludwig_gb_ensemble_t * e) {
+  if (e == NULL) return LUDWIG_GB_OK;
+  ens_graph_reset(e);
+  for (int k = 0; k < 2; k++) {
+    dev_free(e->f[k]); dev_free(e->phi[k]); dev_free(e->u[k]);
+    dev_free(e->boxes_d[k]);
+    free(e->boxes_h[k]);
+  }
+  dev_free(e->rho);
+  dev_free(e->items_d);
+  free(e->param); free(e->off); free(e->active);
+  free(e);
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
+			      int precision, ludwig_gb_ensemble_t ** pens) {
+  if (nbox < 1 || p == NULL || pens == NULL ||
+      precision < LUDWIG_GB_FP64 || precision > LUDWIG_GB_FP16) {
+    return err_set(LUDWIG_GB_EINVAL, "ensemble_create");
+  }
+  int rc = lib_init();
+  if (rc) return rc;
+  ludwig_gb_ensemble_t * e =
+    (ludwig_gb_ensemble_t *) calloc(1, sizeof(ludwig_gb_ensemble_t));
+  if (e == NULL) return err_set(LUDWIG_GB_ENOMEM, "ensemble");
+  e->nbox = nbox;
+  e->prec = precision;
+  e->xchunk = 16; e->ty = 8; e->minb = (precision == LUDWIG_GB_FP64) ? 0 : 3;
+  e->param = (ludwig_gb_box_param_t *) malloc(nbox*sizeof(*p));
+  e->off = (long long *) calloc(nbox + 1, sizeof(long long));
+  e->active = (int *) malloc(nbox*sizeof(int));
+  for (int k = 0; k < 2; k++) {
+    e->boxes_h[k] = (lgbk_box_t *) calloc(nbox, sizeof(lgbk_box_t));
+  }
+  if (!e->param || !e->off || !e->active || !e->boxes_h[0] ||
+      !e->boxes_h[1]) {
+    ludwig_gb_ensemble_free(e);
+    return err_set(LUDWIG_GB_ENOMEM, "ensemble");
+  }
+  memcpy(e->param, p, nbox*sizeof(*p));
+  for (int b = 0; b < nbox; b++) {
+    for (int i = 0; i < 3; i++) {
+      if (p[b].ntotal[i] < 2) {
+	ludwig_gb_ensemble_free(e);
+	return err_set(LUDWIG_GB_EINVAL, "ensemble: box %d extent < 2", b);
+      }
+    }
+    e->off[b + 1] = e->off[b]
+      + (long long) p[b].ntotal[0]*p[b].ntotal[1]*p[b].ntotal[2];
+    e->active[b] = 1;
+  }
+  e->ntot = e->off[nbox];
+
+  const size_t es = prec_size(precision), fs = field_size(precision);
+  const size_t n = (size_t) e->ntot;
+  for (int k = 0; k < 2 && rc == 0; k++) {
+    if ((rc = dev_alloc(&e->f[k], NVEL*n*es, "ens f")) == 0 &&
+	(rc = dev_alloc(&e->phi[k], n*fs, "ens phi")) == 0 &&
+	(rc = dev_alloc(&e->u[k], 3*n*fs, "ens u")) == 0) {
+      rc = dev_alloc((void **) &e->boxes_d[k], nbox*sizeof(lgbk_box_t),
+		     "boxes");
+    }
+  }
+  if (rc == 0) rc = dev_alloc(&e->rho, n*fs, "ens rho");
+  if (rc) { ludwig_gb_ensemble_free(e); return rc; }
+
+  /* Box descriptors (arrangement 0 reads buffer 0, writes buffer 1) */
+  for (int b = 0; b < nbox && rc == 0; b++) {
+    const ludwig_gb_box_param_t * q = p + b;
+    lgbk_dims_t d = {q->ntotal[0], q->ntotal[1], q->ntotal[2],
+		     (long long) q->ntotal[0]*q->ntotal[1]*q->ntotal[2]};
+    const double cs2 = (1.0/3.0);
+    double eta_bulk = (q->eta_bulk > 0.0) ? q->eta_bulk : q->eta;
+    lgbk_binary_args_t a;
+    memset(&a, 0, sizeof(a));
+    a.cp.rtau_shear = 1.0/(0.5 + q->eta / (q->rho0*cs2));
+    a.cp.rtau_bulk = 1.0/(0.5 + eta_bulk / (q->rho0*cs2));
+    for (int m = 0; m < NVEL; m++) a.cp.rtau_ghost[m] = 1.0;
+    a.cp.ghosts_zero = 1;
+    a.mobility = q->mobility;
+    a.rho0 = q->rho0;
+    a.fscale = 1024.0;
+    a.fe.a = q->a; a.fe.b = q->b; a.fe.kappa = q->kappa;
+    lgbk_binary_args_pack(&a);
+    a.status = NULL;
+    a.force_out = NULL;
+    a.rho_out = (char *) e->rho + e->off[b]*fs;
+    for (int k = 0; k < 2; k++) {
+      lgbk_binary_args_t ak = a;
+      int in = k, out = 1 - k;
+      ak.f_in = (char *) e->f[in] + NVEL*e->off[b]*es;
+      ak.f_out = (char *) e->f[out] + NVEL*e->off[b]*es;
+      ak.phi_in = (char *) e->phi[in] + e->off[b]*fs;
+      ak.phi_out = (char *) e->phi[out] + e->off[b]*fs;
+      ak.u_in = (char *) e->u[in] + 3*e->off[b]*fs;
+      ak.u_out = (char *) e->u[out] + 3*e->off[b]*fs;
+      e->boxes_h[k][b].d = d;
+      e->boxes_h[k][b].a = ak;
+      e->boxes_h[k][b].active = 1;
+    }
+  }
+
+  /* Initial state: rest distributions (shift removed), spinodal phi, u = 0
+   * (the f buffers are post-collision values; a uniform state streams to
+   * itself) */
+  for (int b = 0; b < nbox && rc == 0; b++) {
+    const ludwig_gb_box_param_t * q = p + b;
+    lgbk_dims_t d = e->boxes_h[0][b].d;
+    double * tmp = NULL;
+    rc = dev_alloc((void **) &tmp, NVEL*(size_t) d.nsites*sizeof(double),
+		   "init");
+    for (int m = 0; rc == 0 && m < NVEL; m++) {
+      static const int w36[NVEL] = {12, 1, 1, 2, 1, 1, 1, 2, 1, 2, 2, 1, 2,
+				    1, 1, 1, 2, 1, 1};
+      rc = lgbk_fill_f64(tmp + m*d.nsites, d.nsites,
+			 q->rho0*((double) w36[m]/36.0)*1.0, stream_);
+    }
+    if (rc == 0) {
+      rc = lgbk_f64_to_store(&d, precision, NVEL, q->rho0, 1024.0, tmp,
+			     (char *) e->f[0] + NVEL*e->off[b]*es, stream_);
+    }
+    if (rc == 0) rc = cudaStreamSynchronize(stream_);
+    dev_free(tmp);
+    if (rc) { rc = cuda_check(rc, "ensemble init"); break; }
+  }
+  if (rc == 0) {
+    rc = cuda_check(cudaMemset(e->u[0], 0, 3*n*fs), "u");
+    if (rc == 0) rc = cuda_check(cudaMemset(e->rho, 0, n*fs), "rho");
+  }
+  for (int b = 0; b < nbox && rc == 0; b++) {
+    const ludwig_gb_box_param_t * q = p + b;
+    lgbk_dims_t d = e->boxes_h[0][b].d;
+    double * h = (double *) malloc(d.nsites*sizeof(double));
+    if (h == NULL) { rc = err_set(LUDWIG_GB_ENOMEM, "init"); break; }
+    unsigned int seed0 = (q->seed > 1) ? (unsigned int) q->seed : 13u;
+    for (int x = 0; x < d.nx; x++) {
+      for (int y = 0; y < d.ny; y++) {
+	for (int z = 0; z < d.nz; z++) {
+	  unsigned int sl[4], st[4];
+	  sl[0] = seed0 + (unsigned int) (x + 1);
+	  sl[1] = 12953u + (unsigned int) (y + 1);
+	  sl[2] = 712357u + (unsigned int) (z + 1);
+	  sl[3] = 22383979u;
+	  for (int k = 0; k < 4; k++) st[k] = kiss(sl);
+	  double ran = (1.0/UINT_MAX)*kiss(st);
+	  h[((long long) x*d.ny + y)*d.nz + z] = q->phi0 + q->noise*(ran - 0.5);
+	}
+      }
+    }
+    rc = copy_from_host(precision, d.nsites, h,
+			(char *) e->phi[0] + e->off[b]*fs);
+    free(h);
+  }
+  if (rc == 0) rc = ens_items(e);
+  if (rc == 0) rc = ens_upload_boxes(e);
+  if (rc) { ludwig_gb_ensemble_free(e); return rc; }
+  e->parity = 0;
+  *pens = e;
+  return LUDWIG_GB_OK;
+}
+
+static int ens_launch(ludwig_gb_ensemble_t * e, int k) {
+  return lgbk_ensemble_step(e->prec, e->boxes_d[k], e->items_d, e->nitems,
+			    e->xchunk, e->ty, e->minb, 0, stream_);
+}
+
+static int ens_step_async(ludwig_gb_ensemble_t * e, int nsteps) {
+  int npair = nsteps/2;
+  if (npair > 0) {
+    int k = e->parity;
+    if (!e->pair_valid[k]) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed),
+	 "capture");
+      int rc1 = ens_launch(e, k);
+      int rc2 = ens_launch(e, 1 - k);
+      int rc3 = cudaStreamEndCapture(stream_, &g);
+      if (rc1 || rc2 || rc3) {
+	return cuda_check(rc1 ? rc1 : (rc2 ? rc2 : rc3), "ensemble capture");
+      }
+      int rc = cudaGraphInstantiate(&e->pair[k], g, 0);
+      cudaGraphDestroy(g);
+      if (rc) return cuda_check(rc, "instantiate");
+      e->pair_valid[k] = 1;
+    }
+    for (int i = 0; i < npair; i++) {
+      CK(cudaGraphLaunch(e->pair[k], stream_), "graph launch");
+    }
+  }
+  if (nsteps % 2) {
+    CK(ens_launch(e, e->parity), "ensemble step");
+    e->parity = 1 - e->parity;
+  }
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_step(ludwig_gb_ensemble_t * e, int nsteps) {
+  if (e == NULL || nsteps < 0) return err_set(LUDWIG_GB_EINVAL, "ens step");
+  int rc = ens_step_async(e, nsteps);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_time(ludwig_gb_ensemble_t * e, int nsteps,
+			    double * ms) {
+  cudaEvent_t e0, e1;
+  if (e == NULL || ms == NULL) return err_set(LUDWIG_GB_EINVAL, "ens time");
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  CK(cudaEventRecord(e0, stream_), "record");
+  int rc = ens_step_async(e, nsteps);
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e1, stream_), "record");
+  if (rc == 0) rc = cuda_check(cudaEventSynchronize(e1), "sync");
+  if (rc == 0) {
+    float t = 0.0f;
+    rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int ludwig_gb_ensemble_tune_set(ludwig_gb_ensemble_t * e, int xchunk,
+				int tile_y, int min_blocks) {
+  if (e == NULL || xchunk < 1 || (tile_y != 4 && tile_y != 8 &&
+				   tile_y != 16)) {
+    return err_set(LUDWIG_GB_EINVAL, "ensemble tune");
+  }
+  if (e->prec == LUDWIG_GB_FP64) tile_y = 8;     /* one FP64 form */
+  e->xchunk = xchunk;
+  e->ty = tile_y;
+  e->minb = min_blocks;
+  return ens_items(e);
+}
+
+int ludwig_gb_ensemble_autotune(ludwig_gb_ensemble_t * e, int trial_steps,
+				int best[3], double * ms_best) {
+  static const int cand[][3] = {{16, 4, 0}, {32, 4, 0}, {8, 4, 0},
+				{16, 8, 4}, {32, 8, 4}, {16, 8, 3},
+				{32, 16, 2}};
+  const int ncand = (int) (sizeof(cand)/sizeof(cand[0]));
+  if (e == NULL || trial_steps < 2) {
+    return err_set(LUDWIG_GB_EINVAL, "autotune: trial_steps >= 2");
+  }
+  /* save the state: the trials advance a copy of it */
+  const size_t es = prec_size(e->prec), fs = field_size(e->prec);
+  const size_t n = (size_t) e->ntot;
+  const int k = e->parity;
+  void * sf = NULL, * sp = NULL, * su = NULL;
+  int rc = dev_alloc(&sf, NVEL*n*es, "save f");
+  if (rc == 0) rc = dev_alloc(&sp, n*fs, "save phi");
+  if (rc == 0) rc = dev_alloc(&su, 3*n*fs, "save u");
+  if (rc == 0) rc = cuda_check(cudaMemcpy(sf, e->f[k], NVEL*n*es,
+					  cudaMemcpyDeviceToDevice), "save");
+  if (rc == 0) rc = cuda_check(cudaMemcpy(sp, e->phi[k], n*fs,
+					  cudaMemcpyDeviceToDevice), "save");
+  if (rc == 0) rc = cuda_check(cudaMemcpy(su, e->u[k], 3*n*fs,
+					  cudaMemcpyDeviceToDevice), "save");
+  int bi = -1;
+  double bt = 1.0e300;
+  for (int c = 0; rc == 0 && c < ncand; c++) {
+    if (e->prec == LUDWIG_GB_FP64 && cand[c][1] != 8) continue;
+    rc = ludwig_gb_ensemble_tune_set(e, cand[c][0], cand[c][1], cand[c][2]);
+    double ms = 0.0;
+    if (rc == 0) rc = ludwig_gb_ensemble_step(e, 2);        /* warm-up */
+    if (rc == 0) rc = ludwig_gb_ensemble_time(e, trial_steps, &ms);
+    if (rc == 0 && ms < bt) { bt = ms; bi = c; }
+  }
+  /* restore */
+  if (e->parity != k) e->parity = k;
+  if (rc == 0) rc = cuda_check(cudaMemcpy(e->f[k], sf, NVEL*n*es,
+					  cudaMemcpyDeviceToDevice), "restore");
+  if (rc == 0) rc = cuda_check(cudaMemcpy(e->phi[k], sp, n*fs,
+					  cudaMemcpyDeviceToDevice), "restore");
+  if (rc == 0) rc = cuda_check(cudaMemcpy(e->u[k], su, 3*n*fs,
+					  cudaMemcpyDeviceToDevice), "restore");
+  dev_free(sf); dev_free(sp); dev_free(su);
+  if (rc == 0 && bi >= 0) {
+    rc = ludwig_gb_ensemble_tune_set(e, cand[bi][0], cand[bi][1],
+				     cand[bi][2]);
+    if (best) { best[0] = cand[bi][0]; best[1] = cand[bi][1];
+      best[2] = cand[bi][2]; }
+    if (ms_best) *ms_best = bt/trial_steps;
+  }
+  return rc;
+}
+
+int ludwig_gb_ensemble_box_get(ludwig_gb_ensemble_t * e, int box, double * f,
+			       double * phi, double * u, double * rho) {
+  if (e == NULL || box < 0 || box >= e->nbox) {
+    return err_set(LUDWIG_GB_EINVAL, "ensemble box");
+  }
+  const size_t es = prec_size(e->prec), fs = field_size(e->prec);
+  const int k = e->parity;
+  lgbk_dims_t d = e->boxes_h[0][box].d;
+  int rc = LUDWIG_GB_OK;
+  if (f) {
+    /* stored values are post-collision: stream them (into the spare
+     * buffer, free between steps), then convert */
+    void * src = (char *) e->f[k] + NVEL*e->off[box]*es;
+    void * dst = (char *) e->f[1 - k] + NVEL*e->off[box]*es;
+    double * tmp = NULL;
+    rc = cuda_check(lgbk_propagate_store(&d, e->prec, +1, src, dst, stream_),
+		    "propagate");
+    if (rc == 0) rc = dev_alloc((void **) &tmp,
+				NVEL*(size_t) d.nsites*sizeof(double), "tmp");
+    if (rc == 0) {
+      rc = cuda_check(lgbk_store_to_f64(&d, e->prec, NVEL,
+					e->param[box].rho0, 1024.0, dst, tmp,
+					stream_), "convert");
+    }
+    if (rc == 0) rc = cuda_check(cudaMemcpyAsync(f, tmp, NVEL*d.nsites
+						 *sizeof(double),
+						 cudaMemcpyDeviceToHost,
+						 stream_), "f");
+    if (rc == 0) rc = cuda_check(cudaStreamSynchronize(stream_), "sync");
+    dev_free(tmp);
+  }
+  if (rc == 0 && phi) {
+    rc = copy_to_host(e->prec, d.nsites,
+		      (char *) e->phi[k] + e->off[box]*fs, phi);
+  }
+  if (rc == 0 && u) {
+    rc = copy_to_host(e->prec, 3*d.nsites,
+		      (char *) e->u[k] + 3*e->off[box]*fs, u);
+  }
+  if (rc == 0 && rho) {
+    rc = copy_to_host(e->prec, d.nsites, (char *) e->rho + e->off[box]*fs,
+		      rho);
+  }
+  return rc;
+}
+
+int ludwig_gb_ensemble_box_set_phi(ludwig_gb_ensemble_t * e, int box,
+				   const double * phi) {
+  if (e == NULL || box < 0 || box >= e->nbox || phi == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "ensemble box");
+  }
+  const size_t fs = field_size(e->prec);
+  lgbk_dims_t d = e->boxes_h[0][box].d;
+  return copy_from_host(e->prec, d.nsites,
+			phi, (char *) e->phi[e->parity] + e->off[box]*fs);
+}
+
+int ludwig_gb_ensemble_check(ludwig_gb_ensemble_t * e, int * nactive) {
+  if (e == NULL) return err_set(LUDWIG_GB_EINVAL, "ensemble check");
+  double * scr = NULL;
+  int rc = red_scratch(&scr);
+  if (rc) return rc;
+  const size_t es = prec_size(e->prec), fs = field_size(e->prec);
+  const int k = e->parity;
+  int changed = 0, na = 0;
+  for (int b = 0; b < e->nbox; b++) {
+    if (!e->active[b]) continue;
+    lgbk_dims_t d = e->boxes_h[0][b].d;
+    double m[6], q[4];
+    CK(lgbk_dist_moments(&d, e->prec, (char *) e->f[k] + NVEL*e->off[b]*es,
+			 1024.0, scr, m, stream_), "moments");
+    CK(lgbk_field_stats(&d, field_kprec(e->prec),
+			(char *) e->phi[k] + e->off[b]*fs, scr, q, stream_),
+       "stats");
+    if (!isfinite(m[0]) || !isfinite(q[0]) || !isfinite(q[1])) {
+      e->active[b] = 0;
+      changed = 1;
+    }
+    else {
+      na++;
+    }
+  }
+  if (changed && (rc = ens_upload_boxes(e))) return rc;
+  if (nactive) *nactive = na;
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_box_active(ludwig_gb_ensemble_t * e, int box,
+				  int * active) {
+  if (e == NULL || box < 0 || box >= e->nbox || active == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "ensemble box");
+  }
+  *active = e->active[box];
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_ensemble_sites(ludwig_gb_ensemble_t * e, long long * n) {
+  if (e == NULL || n == NULL) return err_set(LUDWIG_GB_EINVAL, "sites");
+  long long t = 0;
+  for (int b = 0; b < e->nbox; b++) {
+    if (e->active[b]) t += e->off[b + 1] - e->off[b];
+  }
+  *n = t;
+  return LUDWIG_GB_OK;
 }

@@ -406,3 +406,46 @@ def lc_steps(state, p, gamma_rot, cp, nsteps, status=None):
                          _p(s.q), _p(s.u), _p(s.rho), _p(s.force),
                          _p(s._work), int(nsteps))
     return s
+
+
+# ---------------------------------------------------------------------------
+# Domain length from the structure factor, util/length_from_sk.c:88-190
+# ---------------------------------------------------------------------------
+
+NBIN = 128
+
+
+def structure_factor(phi, faithful=True):
+    """Binned |phi(k)|^2 sums and counts over the half space k_z >= 0.
+
+    faithful=True keeps the reference's wavevector for i > N/2, dk*i - pi
+    (util/length_from_sk.c:138); faithful=False uses dk*i - 2 pi.
+    """
+    phi = np.asarray(phi, dtype=np.float64)
+    if phi.ndim == 4:
+        phi = phi[0]
+    nx, ny, nz = phi.shape
+    c = np.fft.fftn(phi)
+    shift = np.pi if faithful else 2.0 * np.pi
+    kx = 2.0 * np.pi * np.arange(nx) / nx
+    kx = np.where(np.arange(nx) > nx // 2, kx - shift, kx)
+    ky = 2.0 * np.pi * np.arange(ny) / ny
+    ky = np.where(np.arange(ny) > ny // 2, ky - shift, ky)
+    kz = 2.0 * np.pi * np.arange(nz // 2 + 1) / nz
+    KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
+    kmod = np.sqrt(KX * KX + KY * KY + KZ * KZ)
+    n = np.floor(kmod * NBIN / (np.sqrt(3.0) * np.pi)).astype(int)
+    n = np.minimum(n, NBIN - 1)
+    s = np.abs(c[:, :, :nz // 2 + 1]) ** 2
+    sk = np.bincount(n.ravel(), weights=s.ravel(), minlength=NBIN)
+    nk = np.bincount(n.ravel(), minlength=NBIN).astype(np.float64)
+    return sk, nk
+
+
+def length_from_sk(phi, faithful=True):
+    """L = 2 pi sum S dk / sum k S dk (util/length_from_sk.c:170-185)."""
+    sk, nk = structure_factor(phi, faithful)
+    dk = np.sqrt(3.0) * np.pi / NBIN
+    sbar = np.where(nk != 0, sk / np.where(nk == 0, 1, nk), 0.0)
+    kk = (np.arange(NBIN) + 0.5) * dk
+    return 2.0 * np.pi * np.sum(dk * sbar) / np.sum(kk * dk * sbar)

@@ -1121,13 +1121,12 @@ void orc_beris_edw_update(const int L[3], const orc_lc_param_t * p,
 	    for (int n = 0; n < NQAB; n++) {
 	      double v = qs[ca[n]][cb[n]];
 	      if (fluid) {
-		double fl = 0.0;
-		if (u) {
-		  fl = - fe[n*N + i] + fw[n*N + i]
-		    - fy[n*N + i] + fy[n*N + ij]
-		    - fz[n*N + i] + fz[n*N + ik];
-		}
-		v += dt*(s[ca[n]][cb[n]] + 0.0 + gamma_rot*h[n*N + i] + fl);
+		/* zero fluxes without hydrodynamics */
+		double fen = u ? fe[n*N + i] : 0.0, fwn = u ? fw[n*N + i] : 0.0;
+		double fyn = u ? fy[n*N + i] : 0.0, fyj = u ? fy[n*N + ij] : 0.0;
+		double fzn = u ? fz[n*N + i] : 0.0, fzk = u ? fz[n*N + ik] : 0.0;
+		v += dt*(s[ca[n]][cb[n]] + 0.0 + gamma_rot*h[n*N + i]
+			 - fen + fwn - fyn + fyj - fzn + fzk);
 	      }
 	      qn[n*N + i] = v;
 	    }

@@ -68,6 +68,37 @@ def op_case(name, mode, L, inputs, outputs, **extra):
     print("wrote", name)
 
 
+LC = dict(a0=0.01, gamma=3.0, kappa0=0.01, kappa1=0.01, pitch=32.0, xi=0.7,
+          Gamma=0.5, redshift=1.0, amplitude=-0.2, eta=0.5)
+
+
+def lc_run_case(name, L, steps):
+    """Blue phase I (o8m) initial condition, then the LC main loop."""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "out")
+        oracle.run_reference(kv(L, mode="lc", steps=steps, out=out, **LC))
+        res = {"L": np.array(L), "steps": steps}
+        res["q0"] = oracle.read_array(out, "q0", (5,) + L)
+        for k, nc in (("q", 5), ("u", 3), ("rho", 1), ("force", 3),
+                      ("f", 19)):
+            res[k] = oracle.read_array(out, k, (nc,) + L)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print("wrote", name)
+
+
+def lc_op_case(name, mode, L, inputs, outputs):
+    with tempfile.TemporaryDirectory() as tmp:
+        pin, pout = os.path.join(tmp, "in"), os.path.join(tmp, "out")
+        oracle.write_arrays(pin, **inputs)
+        oracle.run_reference(kv(L, mode=mode, **{"in": pin}, out=pout, **LC))
+        res = {"L": np.array(L)}
+        res.update({"in_" + k: v for k, v in inputs.items()})
+        for k, nc in outputs.items():
+            res[k] = oracle.read_array(pout, k, (nc,) + L)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print("wrote", name)
+
+
 def main(ref_root):
     if not oracle.build_reference(ref_root):
         raise SystemExit("reference sources not found at " + ref_root)
@@ -95,6 +126,16 @@ def main(ref_root):
     op_case("force_6x5x4", "force", L, dict(phi=phi), dict(force=3))
     u = 0.01 * rng.standard_normal((3,) + L)
     op_case("ch_6x5x4", "ch", L, dict(phi=phi, u=u), dict(phi=1))
+
+    lc_run_case("lc_8x8x8_s3", (8, 8, 8), 3)
+    lc_run_case("lc_16x12x8_s40", (16, 12, 8), 40)
+    L = (6, 5, 4)
+    qbp = oracle.lc_init_o8m(L, oracle.lc_param())
+    q = qbp + 0.01 * rng.standard_normal(qbp.shape)
+    lc_op_case("lc_fields_6x5x4", "lc_fields", L, dict(q=q),
+               dict(h=5, stress=9, fed=1))
+    u = 0.005 * rng.standard_normal((3,) + L)
+    lc_op_case("lc_be_6x5x4", "lc_be", L, dict(q=q, u=u), dict(q=5))
 
 
 if __name__ == "__main__":

@@ -92,3 +92,36 @@ def test_model_tables(orc):
     # opposite velocity exists for each p
     for p in range(19):
         assert any((cv[q] == -cv[p]).all() for q in range(19))
+
+
+# --- cholesteric liquid crystal (config 4 parameters) ----------------------
+
+GAMMA_ROT, ETA_LC = 0.5, 0.5
+
+
+@pytest.mark.parametrize("name", ["lc_8x8x8_s3", "lc_16x12x8_s40"])
+def test_oracle_lc_run_matches_reference(orc, name):
+    g = load(name)
+    L = L_of(g)
+    p = orc.lc_param()
+    assert np.array_equal(orc.lc_init_o8m(L, p), g["q0"])
+    st = orc.LcState(L, orc.lb_init_rest(L), g["q0"])
+    orc.lc_steps(st, p, GAMMA_ROT, orc.collide_param_m10(ETA_LC),
+                 int(g["steps"]))
+    for k in ("q", "u", "rho", "force", "f"):
+        assert np.array_equal(getattr(st, k), g[k]), k
+
+
+def test_oracle_lc_fields(orc):
+    g = load("lc_fields_6x5x4")
+    h, s, fed = orc.lc_fields(L_of(g), orc.lc_param(), g["in_q"])
+    assert np.array_equal(h, g["h"])
+    assert np.array_equal(s, g["stress"])
+    assert np.array_equal(fed, g["fed"])
+
+
+def test_oracle_beris_edwards(orc):
+    g = load("lc_be_6x5x4")
+    q = orc.lc_be_update(L_of(g), orc.lc_param(), GAMMA_ROT, g["in_q"],
+                         g["in_u"])
+    assert np.array_equal(q, g["q"])

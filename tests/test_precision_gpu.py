@@ -1,0 +1,68 @@
+"""Reduced-precision forms against the FP64 oracle (config 1, 32^3).
+
+Tolerances are the measured GB300 errors with head-room:
+  FP32-shifted after 1000 steps: max|dphi| 1.1e-6, mass drift 2.8e-11;
+  FP16 storage: max|dphi| 1.3e-5, mass drift 3.5e-8.
+The domain length L(t) of the reduced forms must be within 1% of FP64.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+A, B, KAPPA, MOB, ETA = -0.0625, 0.0625, 0.04, 0.3, 0.1
+L3 = (32, 32, 32)
+NSTEP = 1000
+
+
+@pytest.fixture(scope="module")
+def fp64_run(orc):
+    st = orc.BinaryState(L3, orc.lb_init_rest(L3),
+                         orc.spinodal_init(L3, 8361235, 0.0, 0.02))
+    orc.binary_steps(st, orc.symm_param(A, B, KAPPA), MOB,
+                     orc.collide_param_m10(ETA), NSTEP)
+    return st
+
+
+@pytest.mark.parametrize("prec,dphi_tol,drift_tol", [
+    (1, 1e-5, 1e-9),        # FP32-shifted
+    (2, 1e-4, 1e-6),        # FP16 storage
+])
+def test_reduced_precision_vs_fp64(gb, orc, fp64_run, prec, dphi_tol,
+                                   drift_tol):
+    s = gb.BinaryFluid(L3, precision=prec, mobility=MOB, eta=ETA)
+    s.phi.init_spinodal(8361235, 0.0, 0.02)
+    m0 = s.lb.moments()[0]
+    s.step(NSTEP)
+    m1 = s.lb.moments()[0]
+    got = s.phi.get()
+    assert np.abs(got - fp64_run.phi).max() < dphi_tol
+    assert abs(m1 - m0) / m0 < drift_tol
+    l64 = orc.length_from_sk(fp64_run.phi)
+    lred = s.phi.length_from_sk()[0]
+    assert abs(lred - l64) / l64 < 0.01
+    # total phi is conserved by the flux form up to rounding
+    assert abs(got.sum() - fp64_run.phi.sum()) < 1e-3
+
+
+def test_fp32_state_roundtrip(gb):
+    """Raw state out and back in leaves the trajectory unchanged."""
+    L = (16, 12, 8)
+    a = gb.BinaryFluid(L, precision=1, mobility=MOB, eta=ETA)
+    a.phi.init_spinodal(5, 0.0, 0.02)
+    a.step(7)
+    pin = gb.PinnedState(a)
+    lib = gb.lib()
+    gb._check(lib.ludwig_gb_state_to_host_async(a.lb.ptr, a.phi.ptr,
+                                                a.hydro.ptr, *pin.bufs[:3]),
+              "to_host")
+    gb.sync()
+    ref = a.state()
+    gb._check(lib.ludwig_gb_state_from_host_async(a.lb.ptr, a.phi.ptr,
+                                                  a.hydro.ptr, *pin.bufs[:3]),
+              "from_host")
+    gb.sync()
+    got = a.state()
+    for k in ("f", "phi", "u"):
+        assert np.array_equal(got[k], ref[k]), k

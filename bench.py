@@ -46,9 +46,16 @@ METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
 #   phi 2*4 + u 2*12 = 108.  rho (written for output) is not counted.
 ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108}
 
-# DRAM bytes per site of the fused FP32 kernel from ncu
-# (profiles/binary_fused_fp32_ncu.md); None until captured.
-NCU_BYTES_PER_SITE = {"fp32": None, "fp64": None, "fp16": None}
+# DRAM bytes (read + write) per site of the fused kernels from one ncu
+# capture at 160^3 (profiles/k_binary_fused_fp32_160cube.md and
+# profiles/k_binary_fused_fp64_160cube.md); a streaming kernel's traffic
+# grows in proportion to the sites, so traffic = bytes/site x sites.
+NCU_BYTES_PER_SITE = {"fp32": 179.6, "fp64": 370.5, "fp16": None}
+
+# What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
+LIMITER = {"fp32": "hbm (traffic = compulsory bytes; latency gap)",
+           "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
+           "fp16": "hbm"}
 
 
 def env_int(name, default):
@@ -241,7 +248,7 @@ def roofline(kind, ms_per_step, nsites, peak, peak_kind):
     return {"bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak,
             "traffic": None if ncu is None else ncu * nsites,
-            "algorithmic_bytes": algo,
+            "algorithmic_bytes": algo, "limiter": LIMITER[kind],
             "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
             if peak_kind == "measured" else "fallback 6.8 TB/s"}
 

@@ -456,6 +456,85 @@ int ludwig_gb_length_from_sk(field_t * phi, int faithful, double * length,
 int ludwig_gb_field_stats_noalloc(const double * d_data, long long nsites,
 				  int ncomp, double * out, void * stream);
 
+/*****************************************************************************
+ *
+ *  Learned corrector of a 2x-coarsened binary fluid.  No counterpart in the
+ *  reference.  A 4-layer 3x3x3 convolutional network (32 channels, GELU;
+ *  inputs phi, u, rho; outputs corrections of phi and u) runs on the coarse
+ *  lattice after each coarse step.  Forward and backward passes are
+ *  tensor-core implicit GEMMs (BF16 operands, FP32 accumulation); the
+ *  parameters are FP32 and trained with Adam on the GPU.
+ *
+ *  Coarse extents: nz in {32, 64} or a multiple of 128, and ny a multiple
+ *  of 128/nz when nz < 128.  Device arrays are component-major float:
+ *  in5 = [phi, u_x, u_y, u_z, rho] x nsites, t4/out4 = 4 x nsites
+ *  (normalised corrections: d phi / out_scale[0], d u_a / out_scale[1+a]).
+ *
+ *****************************************************************************/
+
+typedef struct ludwig_gb_cnn_s ludwig_gb_cnn_t;
+
+int ludwig_gb_cnn_create(const int ncoarse[3], unsigned long long seed,
+			 ludwig_gb_cnn_t ** cnn);
+int ludwig_gb_cnn_free(ludwig_gb_cnn_t * cnn);
+/* number of float parameters: 4 x (27*32*32 weights + 32 biases) */
+int ludwig_gb_cnn_nparams(void);
+int ludwig_gb_cnn_params_get(ludwig_gb_cnn_t * cnn, float * host);
+/* replaces the parameters and restarts the optimiser */
+int ludwig_gb_cnn_params_set(ludwig_gb_cnn_t * cnn, const float * host);
+/* gradients of the last loss_grad / train_step (host, nparams floats) */
+int ludwig_gb_cnn_grads_get(ludwig_gb_cnn_t * cnn, float * host);
+/* features = (in5 - in_off) * in_scale; corrections = out4 * out_scale */
+int ludwig_gb_cnn_scales_set(ludwig_gb_cnn_t * cnn, const float in_off[5],
+			     const float in_scale[5],
+			     const float out_scale[4]);
+int ludwig_gb_cnn_scales_get(ludwig_gb_cnn_t * cnn, float in_off[5],
+			     float in_scale[5], float out_scale[4]);
+int ludwig_gb_cnn_forward(ludwig_gb_cnn_t * cnn, const float * d_in5,
+			  float * d_out4);
+/* loss = (1/N) sum over sites and 4 outputs of (out4 - t4)^2 and its
+ * gradient (no update) */
+int ludwig_gb_cnn_loss_grad(ludwig_gb_cnn_t * cnn, const float * d_in5,
+			    const float * d_t4, double * loss);
+/* one Adam step (beta 0.9, 0.999, eps 1e-8) on one pair */
+int ludwig_gb_cnn_train_step(ludwig_gb_cnn_t * cnn, const float * d_in5,
+			     const float * d_t4, double lr, double * loss);
+int ludwig_gb_cnn_train_steps(ludwig_gb_cnn_t * cnn, int nsteps,
+			      const float * const * d_in5,
+			      const float * const * d_t4, double lr,
+			      double * losses);
+/* apply the network to a coarse FP32 state in place: phi, u, and f
+ * shifted by w_p rho 3 c_p . du (momentum changed by rho du) */
+int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * cnn, lb_t * lb, field_t * phi,
+			  hydro_t * hydro);
+/* one convolution / weight gradient on given fp32 device arrays
+ * (operands rounded to bf16), for checks of the kernels themselves:
+ * flip = 0: out[s][n] = b[n] + sum_t sum_c a[s+e_t][c] w[t][n][c];
+ * flip = 1: out[s][c] = sum_t sum_n a[s-e_t][n] w[t][n][c];
+ * wgrad:    dw[t][n][c] = sum_s g[s-e_t][n] a[s][c]. */
+int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * cnn, const float * d_a,
+			const float * d_w, const float * d_b, int flip,
+			float * d_out);
+int ludwig_gb_cnn_wgrad3(ludwig_gb_cnn_t * cnn, const float * d_g,
+			 const float * d_a, float * d_dw);
+
+/* Fine (2n) -> coarse (n) FP32 state: phi and rho averaged, velocities
+ * x 2, non-equilibrium stress x 4 (diffusive scaling dx x 2, dt x 4);
+ * coarse f rebuilt from its moments. */
+int ludwig_gb_coarse_restrict(lb_t * lb_fine, field_t * phi_fine,
+			      hydro_t * hydro_fine, lb_t * lb_coarse,
+			      field_t * phi_coarse, hydro_t * hydro_coarse);
+/* restricted fields of a fine FP32 state into d_out5 (coarse extents nc) */
+int ludwig_gb_fields_restrict(field_t * phi_fine, hydro_t * hydro_fine,
+			      lb_t * lb_fine, float * d_out5, const int nc[3]);
+/* [phi, u, rho] of an FP32 state into d_out5 */
+int ludwig_gb_fields_pack(field_t * phi, hydro_t * hydro, lb_t * lb,
+			  float * d_out5);
+/* Make phys the physics object the step functions read (the reference
+ * keeps one per process, src/physics.c:76; two systems with different
+ * mobilities take turns). */
+int ludwig_gb_physics_use(physics_t * phys);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,7 @@ _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
 _I3 = ctypes.c_int * 3
 _D3 = ctypes.c_double * 3
+_F = ctypes.POINTER(ctypes.c_float)
 
 
 class LbDataOptions(ctypes.Structure):
@@ -220,6 +221,27 @@ def _declare(L):
                                           ctypes.c_int),
         "ludwig_gb_ensemble_sites": ([_P, ctypes.POINTER(ctypes.c_longlong)],
                                      ctypes.c_int),
+        "ludwig_gb_physics_use": ([_P], ctypes.c_int),
+        "ludwig_gb_cnn_create": ([_I3, ctypes.c_ulonglong, pp], ctypes.c_int),
+        "ludwig_gb_cnn_free": ([_P], ctypes.c_int),
+        "ludwig_gb_cnn_nparams": ([], ctypes.c_int),
+        "ludwig_gb_cnn_params_get": ([_P, _F], ctypes.c_int),
+        "ludwig_gb_cnn_params_set": ([_P, _F], ctypes.c_int),
+        "ludwig_gb_cnn_grads_get": ([_P, _F], ctypes.c_int),
+        "ludwig_gb_cnn_scales_set": ([_P, _F, _F, _F], ctypes.c_int),
+        "ludwig_gb_cnn_scales_get": ([_P, _F, _F, _F], ctypes.c_int),
+        "ludwig_gb_cnn_forward": ([_P, _P, _P], ctypes.c_int),
+        "ludwig_gb_cnn_loss_grad": ([_P, _P, _P, _D], ctypes.c_int),
+        "ludwig_gb_cnn_train_step": ([_P, _P, _P, ctypes.c_double, _D],
+                                     ctypes.c_int),
+        "ludwig_gb_cnn_train_steps": ([_P, ctypes.c_int, pp, pp,
+                                       ctypes.c_double, _D], ctypes.c_int),
+        "ludwig_gb_cnn_correct": ([_P] * 4, ctypes.c_int),
+        "ludwig_gb_cnn_conv3": ([_P] * 4 + [ctypes.c_int, _P], ctypes.c_int),
+        "ludwig_gb_cnn_wgrad3": ([_P] * 4, ctypes.c_int),
+        "ludwig_gb_coarse_restrict": ([_P] * 6, ctypes.c_int),
+        "ludwig_gb_fields_restrict": ([_P] * 4 + [_I3], ctypes.c_int),
+        "ludwig_gb_fields_pack": ([_P] * 4, ctypes.c_int),
         "stats_field_q": ([_P, ctypes.c_int, _D], ctypes.c_int),
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
@@ -571,6 +593,7 @@ class BinaryFluid:
 
     def step_reference_order(self, nsteps=1):
         """One call per reference function, in the main-loop order."""
+        self.use_physics()
         for _ in range(nsteps):
             self.hydro.f_zero()
             self.phi.halo()
@@ -585,14 +608,20 @@ class BinaryFluid:
             self.lb.halo()
             self.lb.propagation()
 
+    def use_physics(self):
+        """Make this system's physics the one the step functions read."""
+        _check(lib().ludwig_gb_physics_use(self.phys.ptr), "physics_use")
+
     def step(self, nsteps=1):
         """The fused GB300 step (one kernel per step, graph replay)."""
+        self.use_physics()
         _check(lib().ludwig_gb_binary_step(self.lb.ptr, self.phi.ptr,
                                            self.hydro.ptr, self.map.ptr,
                                            self.fe.ptr, int(nsteps)),
                "ludwig_gb_binary_step")
 
     def step_async(self, nsteps=1):
+        self.use_physics()
         _check(lib().ludwig_gb_binary_step_async(self.lb.ptr, self.phi.ptr,
                                                  self.hydro.ptr, self.map.ptr,
                                                  self.fe.ptr, int(nsteps)),
@@ -871,3 +900,115 @@ def ensemble_config3(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
         out.append(box_param(n, eta=eta, a=-amag, b=amag, kappa=kappa,
                              mobility=mob, seed=1000 + 17 * k))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Learned corrector (no counterpart in the reference)
+# ---------------------------------------------------------------------------
+
+def _fp(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_F)
+
+
+def _f3(v, n):
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(n))
+    return a
+
+
+class Corrector(_Obj):
+    """The 3x3x3 convolutional corrector of a 2x-coarsened binary fluid.
+
+    Device arrays are passed as integer device pointers (for example
+    ``tensor.data_ptr()`` of a contiguous float32 CUDA tensor).
+    """
+    _free = "ludwig_gb_cnn_free"
+
+    def __init__(self, ncoarse, seed=1):
+        super().__init__()
+        self.n = tuple(int(v) for v in ncoarse)
+        self.ptr = _new("ludwig_gb_cnn_create", _I3(*self.n),
+                        ctypes.c_ulonglong(seed))
+
+    @staticmethod
+    def nparams():
+        return int(lib().ludwig_gb_cnn_nparams())
+
+    @property
+    def nsites(self):
+        return self.n[0] * self.n[1] * self.n[2]
+
+    def params(self):
+        h = np.zeros(self.nparams(), dtype=np.float32)
+        _check(lib().ludwig_gb_cnn_params_get(self.ptr, _fp(h)), "params_get")
+        return h
+
+    def set_params(self, p):
+        h = np.ascontiguousarray(p, dtype=np.float32)
+        assert h.size == self.nparams()
+        _check(lib().ludwig_gb_cnn_params_set(self.ptr, _fp(h)), "params_set")
+
+    def grads(self):
+        h = np.zeros(self.nparams(), dtype=np.float32)
+        _check(lib().ludwig_gb_cnn_grads_get(self.ptr, _fp(h)), "grads_get")
+        return h
+
+    def set_scales(self, in_off, in_scale, out_scale):
+        a, b, c = _f3(in_off, 5), _f3(in_scale, 5), _f3(out_scale, 4)
+        _check(lib().ludwig_gb_cnn_scales_set(self.ptr, _fp(a), _fp(b),
+                                              _fp(c)), "scales_set")
+
+    def scales(self):
+        a = np.zeros(5, np.float32)
+        b = np.zeros(5, np.float32)
+        c = np.zeros(4, np.float32)
+        _check(lib().ludwig_gb_cnn_scales_get(self.ptr, _fp(a), _fp(b),
+                                              _fp(c)), "scales_get")
+        return a, b, c
+
+    def forward(self, in5, out4):
+        _check(lib().ludwig_gb_cnn_forward(self.ptr, in5, out4), "forward")
+
+    def loss_grad(self, in5, t4):
+        loss = ctypes.c_double()
+        _check(lib().ludwig_gb_cnn_loss_grad(self.ptr, in5, t4,
+                                             ctypes.byref(loss)), "loss_grad")
+        return loss.value
+
+    def train_step(self, in5, t4, lr):
+        loss = ctypes.c_double()
+        _check(lib().ludwig_gb_cnn_train_step(self.ptr, in5, t4, float(lr),
+                                              ctypes.byref(loss)),
+               "train_step")
+        return loss.value
+
+    def correct(self, system):
+        _check(lib().ludwig_gb_cnn_correct(self.ptr, system.lb.ptr,
+                                           system.phi.ptr, system.hydro.ptr),
+               "cnn_correct")
+
+    def conv3(self, a, w, b, flip, out):
+        _check(lib().ludwig_gb_cnn_conv3(self.ptr, a, w, b, int(flip), out),
+               "cnn_conv3")
+
+    def wgrad3(self, g, a, dw):
+        _check(lib().ludwig_gb_cnn_wgrad3(self.ptr, g, a, dw), "cnn_wgrad3")
+
+
+def coarse_restrict(fine, coarse):
+    """Coarse FP32 state from a fine FP32 state of twice the extents."""
+    _check(lib().ludwig_gb_coarse_restrict(fine.lb.ptr, fine.phi.ptr,
+                                           fine.hydro.ptr, coarse.lb.ptr,
+                                           coarse.phi.ptr, coarse.hydro.ptr),
+           "coarse_restrict")
+
+
+def fields_restrict(fine, out5, ncoarse):
+    _check(lib().ludwig_gb_fields_restrict(fine.phi.ptr, fine.hydro.ptr,
+                                           fine.lb.ptr, out5,
+                                           _I3(*ncoarse)), "fields_restrict")
+
+
+def fields_pack(system, out5):
+    _check(lib().ludwig_gb_fields_pack(system.phi.ptr, system.hydro.ptr,
+                                       system.lb.ptr, out5), "fields_pack")

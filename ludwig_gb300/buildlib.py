@@ -29,8 +29,10 @@ CU_SOURCES = [
     ("lgb_sk.cu", []),
     ("lgb_lc32.cu", []),
     ("lgb_fused32.cu", []),
+    ("lgb_cnn.cu", []),
+    ("lgb_coarse.cu", []),
 ]
-C_SOURCES = ["ludwig_gb.c"]
+C_SOURCES = ["ludwig_gb.c", "ludwig_gb_cnn.c"]
 
 
 def _cuda_home():

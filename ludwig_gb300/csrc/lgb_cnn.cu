@@ -1,0 +1,928 @@
+/*****************************************************************************
+ *
+ *  lgb_cnn.cu
+ *
+ *  Kernels of the learned corrector (a 4-layer 3x3x3 convolutional network
+ *  with 32 channels on the coarse lattice).
+ *
+ *  k_conv3_tc: the convolution as an implicit GEMM,
+ *      D[m][n] = sum_t sum_c A_t[m][c] W[t][n][c],   m = 128 sites of a tile,
+ *  with M = 128, N = 32, K = 27 taps x 32 channels.  Per tap the A operand
+ *  is the tile's neighbour rows (a TMA box of contiguous padded rows, K-major,
+ *  64-byte swizzle); the weights of all 27 taps stay in shared memory.
+ *  Warp roles: warp 0 issues TMA, warp 1 issues tcgen05.mma into one of two
+ *  TMEM accumulators, warps 2-5 drain the other accumulator (tcgen05.ld) and
+ *  run the epilogue (bias, GELU, GELU', bf16 rows).  The backward-data pass
+ *  is the same kernel with flipped, transposed weights.
+ *
+ *  k_wgrad_tc: the weight gradient
+ *      dW[t][n][c] = sum_s G[s - e_t][n] X[s][c]
+ *  with K = sites: four taps are stacked along M (M = 4 taps x 32 = 128,
+ *  N = 32), both operands MN-major (channels contiguous, sites strided), so
+ *  shifted taps are again plain TMA boxes of rows.  Seven tap groups
+ *  accumulate in 7 x 32 TMEM columns over all tiles of a CTA; each CTA then
+ *  writes its partial sums and a second kernel adds them in a fixed order.
+ *
+ *  Every wait is bounded (lgb_tc.cuh); on a timeout the kernel raises the
+ *  error word, waits for its own copies and MMAs in flight, frees its tensor
+ *  memory and returns.
+ *
+ *****************************************************************************/
+
+#include <cuda_bf16.h>
+#include <cuda.h>
+
+#include "lgb_tc.cuh"
+#include "lgb_cnn.h"
+
+#define CNN_C      LGBK_CNN_C
+#define CNN_NTAP   LGBK_CNN_NTAP
+#define ROWB       64                    /* bytes per padded row */
+#define TILEB      8192                  /* 128 rows */
+#define WTAPB      2048                  /* 32 rows of weights per tap */
+
+#define CONV_STAGES  12
+#define CONV_THREADS 192
+#define CONV_TMEM_COLS 64
+#define CONV_SMEM (1024 + CNN_NTAP*WTAPB + CONV_STAGES*TILEB + 256)
+
+#define WG_XSTAGES 2
+#define WG_ASTAGES 4
+#define WG_GROUPS  7                     /* ceil(27/4) */
+#define WG_ASTAGEB (4*TILEB)
+#define WG_THREADS 192
+#define WG_TMEM_COLS 256
+#define WG_SMEM (1024 + WG_XSTAGES*TILEB + WG_ASTAGES*WG_ASTAGEB + 256)
+
+/*****************************************************************************
+ *  Geometry
+ *****************************************************************************/
+
+extern "C" int lgbk_cnn_geom(int nx, int ny, int nz, lgbk_cnn_geom_t * g) {
+  if (nx < 2 || ny < 2 || nz < 2) return 1;
+  int bz, lpt;
+  if (nz == 32 || nz == 64) { bz = nz; lpt = LGBK_CNN_TILE/nz; }
+  else if (nz % LGBK_CNN_TILE == 0) { bz = LGBK_CNN_TILE; lpt = 1; }
+  else return 1;
+  if (ny % lpt) return 1;
+  g->nx = nx; g->ny = ny; g->nz = nz;
+  g->bz = bz; g->lpt = lpt;
+  g->nsites = (long long) nx*ny*nz;
+  g->rows = (long long) (nx + 2)*(ny + 2)*(nz + 2);
+  long long nt = g->nsites/LGBK_CNN_TILE;
+  if (nt > 0x7fffffffLL || g->rows > 0x7fffffffLL) return 1;
+  g->ntiles = (int) nt;
+  return 0;
+}
+
+static int num_sms(void) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm > 0 ? nsm : 1;
+}
+
+extern "C" int lgbk_cnn_conv_blocks(const lgbk_cnn_geom_t * g) {
+  int n = num_sms();
+  return (g->ntiles < n) ? g->ntiles : n;
+}
+
+extern "C" int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g) {
+  int n = num_sms();
+  return (g->ntiles < n) ? g->ntiles : n;
+}
+
+__device__ __forceinline__ int prow(const lgbk_cnn_geom_t & g, int x, int y,
+				    int z) {
+  return ((x + 1)*(g.ny + 2) + (y + 1))*(g.nz + 2) + (z + 1);
+}
+
+__device__ __forceinline__ void tile_decode(const lgbk_cnn_geom_t & g,
+					    int tile, int & x, int & y0,
+					    int & z0) {
+  const int nzc = g.nz/g.bz;
+  const int zc = tile % nzc;
+  const int r = tile / nzc;
+  const int nyg = g.ny/g.lpt;
+  y0 = (r % nyg)*g.lpt;
+  x = r / nyg;
+  z0 = zc*g.bz;
+}
+
+__device__ __forceinline__ void tap_offsets(int t, int & dx, int & dy,
+					    int & dz) {
+  dx = t/9 - 1; dy = (t/3) % 3 - 1; dz = t % 3 - 1;
+}
+
+/* Bounded wait that ignores the abort flag: used to drain copies and MMAs
+ * already in flight before the CTA exits. */
+__device__ __forceinline__ bool tc_drain_wait(uint32_t bar, uint32_t parity,
+					      int * err) {
+  volatile int never = 0;
+  return tc_mbar_wait(bar, parity, &never, err);
+}
+
+__device__ __forceinline__ float gelu_f(float z) {
+  return 0.5f*z*(1.0f + erff(z*0.70710678118654752f));
+}
+
+__device__ __forceinline__ float gelu_d_f(float z) {
+  const float cdf = 0.5f*(1.0f + erff(z*0.70710678118654752f));
+  const float pdf = expf(-0.5f*z*z)*0.39894228040143268f;
+  return cdf + z*pdf;
+}
+
+__device__ __forceinline__ void store_row_bf16(uint8_t * dst,
+					       const float v[32]) {
+  uint4 * d4 = (uint4 *) dst;
+  #pragma unroll
+  for (int q = 0; q < 4; q++) {
+    uint32_t w[4];
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __nv_bfloat162 h = __floats2bfloat162_rn(v[8*q + 2*k],
+					       v[8*q + 2*k + 1]);
+      w[k] = *(uint32_t *) &h;
+    }
+    d4[q] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+__device__ __forceinline__ void load_row_bf16(const uint8_t * src,
+					      float v[32]) {
+  const uint4 * s4 = (const uint4 *) src;
+  #pragma unroll
+  for (int q = 0; q < 4; q++) {
+    uint4 u = s4[q];
+    uint32_t w[4] = {u.x, u.y, u.z, u.w};
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __nv_bfloat162 h = *(__nv_bfloat162 *) &w[k];
+      float2 f = __bfloat1622float2(h);
+      v[8*q + 2*k] = f.x;
+      v[8*q + 2*k + 1] = f.y;
+    }
+  }
+}
+
+/*****************************************************************************
+ *  k_conv3_tc
+ *****************************************************************************/
+
+struct ConvP {
+  lgbk_cnn_geom_t g;
+  const float * bias;
+  const uint8_t * zprev;
+  uint8_t * zout;
+  uint8_t * pout;
+  float * outf;
+  int * err;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(CONV_THREADS, 1)
+k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
+	   const __grid_constant__ CUtensorMap tm_w, const ConvP p) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc_smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t * sgen = smem_raw + (sbase - raw);
+
+  const uint32_t sW = sbase;
+  const uint32_t sA = sW + CNN_NTAP*WTAPB;
+  const uint32_t sBar = sA + CONV_STAGES*TILEB;
+  const uint32_t bFull = sBar;
+  const uint32_t bEmpty = sBar + 8*CONV_STAGES;
+  const uint32_t bW = sBar + 16*CONV_STAGES;
+  const uint32_t bTFull = bW + 8;
+  const uint32_t bTEmpty = bW + 24;
+  const uint32_t bDone = bW + 40;
+  uint32_t * tslot = (uint32_t *) (sgen + (bW + 48 - sbase));
+  volatile int * abort_flag = (volatile int *) (sgen + (bW + 52 - sbase));
+
+  const int warp = threadIdx.x/32;
+  const int lane = threadIdx.x % 32;
+  const lgbk_cnn_geom_t & g = p.g;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < CONV_STAGES; s++) {
+      tc_mbar_init(bFull + 8*s, 1);
+      tc_mbar_init(bEmpty + 8*s, 1);
+    }
+    tc_mbar_init(bW, 1);
+    tc_mbar_init(bTFull, 1);
+    tc_mbar_init(bTFull + 8, 1);
+    tc_mbar_init(bTEmpty, 128);
+    tc_mbar_init(bTEmpty + 8, 128);
+    tc_mbar_init(bDone, 1);
+    *abort_flag = 0;
+    tc_fence_barrier_init();
+  }
+  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), CONV_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    /* TMA producer */
+    tc_prefetch_map(&tm_in);
+    tc_prefetch_map(&tm_w);
+    tc_mbar_arrive_tx(bW, CNN_NTAP*WTAPB);
+    for (int t = 0; t < CNN_NTAP; t++) {
+      tc_tma_load_2d(sW + t*WTAPB, &tm_w, bW, 0, t*CNN_C);
+    }
+    int stage = 0;
+    uint32_t phase = 0;
+    uint32_t fills[CONV_STAGES];
+    for (int s = 0; s < CONV_STAGES; s++) fills[s] = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile < g.ntiles; tile += gridDim.x) {
+      int x, y0, z0;
+      tile_decode(g, tile, x, y0, z0);
+      for (int t = 0; t < CNN_NTAP; t++) {
+	if (!tc_mbar_wait(bEmpty + 8*stage, phase ^ 1u, abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	int dx, dy, dz;
+	tap_offsets(t, dx, dy, dz);
+	tc_mbar_arrive_tx(bFull + 8*stage, TILEB);
+	for (int l = 0; l < g.lpt; l++) {
+	  const int row = prow(g, x + dx, y0 + l + dy, z0 + dz);
+	  tc_tma_load_2d(sA + stage*TILEB + l*g.bz*ROWB, &tm_in,
+			 bFull + 8*stage, 0, row);
+	}
+	fills[stage] += 1;
+	if (++stage == CONV_STAGES) { stage = 0; phase ^= 1u; }
+      }
+    }
+    /* drain: every copy issued has landed before the CTA may exit */
+    tc_drain_wait(bW, 0, p.err);
+    for (int s = 0; s < CONV_STAGES; s++) {
+      if (fills[s]) tc_drain_wait(bFull + 8*s, (fills[s] - 1u) & 1u, p.err);
+    }
+  }
+  else if (warp == 1 && lane == 0) {
+    /* MMA issuer */
+    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 0, 0);
+    bool ok = tc_mbar_wait(bW, 0, abort_flag, p.err);
+    int stage = 0;
+    uint32_t phase = 0;
+    int i = 0;
+    for (int tile = blockIdx.x; ok && tile < g.ntiles; tile += gridDim.x) {
+      const int acc = i & 1;
+      const uint32_t ap = (uint32_t) (i >> 1) & 1u;
+      if (!tc_mbar_wait(bTEmpty + 8*acc, ap ^ 1u, abort_flag, p.err)) break;
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t) (acc*CNN_C);
+      for (int t = 0; t < CNN_NTAP; t++) {
+	if (!tc_mbar_wait(bFull + 8*stage, phase, abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_fence_after();
+	#pragma unroll
+	for (int kh = 0; kh < 2; kh++) {
+	  const uint64_t ad = tc_sdesc(sA + stage*TILEB + kh*32, 16, 512,
+				       LGB_TC_SWIZZLE_64B);
+	  const uint64_t bd = tc_sdesc(sW + t*WTAPB + kh*32, 16, 512,
+				       LGB_TC_SWIZZLE_64B);
+	  tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((t | kh) != 0));
+	}
+	tc_commit(bEmpty + 8*stage);
+	if (++stage == CONV_STAGES) { stage = 0; phase ^= 1u; }
+      }
+      if (!ok) break;
+      tc_commit(bTFull + 8*acc);
+      i++;
+    }
+    tc_commit(bDone);
+    tc_drain_wait(bDone, 0, p.err);
+  }
+  else if (warp >= 2) {
+    /* epilogue: warp w reads TMEM lanes 32*(w % 4) .. +31 */
+    const int q = warp & 3;
+    const int m = q*32 + lane;
+    float bias[CNN_C];
+    #pragma unroll
+    for (int n = 0; n < CNN_C; n++) bias[n] = p.bias ? p.bias[n] : 0.0f;
+    int i = 0;
+    for (int tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
+      const int acc = i & 1;
+      const uint32_t ap = (uint32_t) (i >> 1) & 1u;
+      bool okw = tc_mbar_wait(bTFull + 8*acc, ap, abort_flag, p.err);
+      if (!__all_sync(0xffffffffu, okw)) break;
+      tc_fence_after();
+      uint32_t r[32];
+      tc_tmem_ld32(tmem + (uint32_t) (acc*CNN_C) + ((uint32_t) (q*32) << 16),
+		   r);
+      tc_fence_before();
+      tc_mbar_arrive(bTEmpty + 8*acc);
+
+      int x, y0, z0;
+      tile_decode(g, tile, x, y0, z0);
+      const int l = m / g.bz;
+      const int z = z0 + (m % g.bz);
+      const int y = y0 + l;
+      const long long s = ((long long) x*g.ny + y)*g.nz + z;
+      float v[32];
+      #pragma unroll
+      for (int n = 0; n < 32; n++) v[n] = __uint_as_float(r[n]);
+
+      if (MODE == LGBK_CNN_FWD_GELU) {
+	#pragma unroll
+	for (int n = 0; n < 32; n++) v[n] += bias[n];
+	store_row_bf16(p.zout + s*ROWB, v);
+	#pragma unroll
+	for (int n = 0; n < 32; n++) v[n] = gelu_f(v[n]);
+	store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+      }
+      else if (MODE == LGBK_CNN_FWD_OUT) {
+	#pragma unroll
+	for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	  p.outf[c*g.nsites + s] = v[c] + bias[c];
+	}
+      }
+      else if (MODE == LGBK_CNN_BWD_GELU) {
+	float zp[32];
+	load_row_bf16(p.zprev + s*ROWB, zp);
+	#pragma unroll
+	for (int n = 0; n < 32; n++) v[n] *= gelu_d_f(zp[n]);
+	store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+      }
+      else {
+	float4 * o = (float4 *) (p.outf + s*CNN_C);
+	#pragma unroll
+	for (int k = 0; k < 8; k++) {
+	  o[k] = make_float4(v[4*k] + bias[4*k], v[4*k + 1] + bias[4*k + 1],
+			     v[4*k + 2] + bias[4*k + 2],
+			     v[4*k + 3] + bias[4*k + 3]);
+	}
+      }
+      i++;
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tc_tmem_dealloc(tmem, CONV_TMEM_COLS);
+  }
+}
+
+extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
+			     const void * tm_in, const void * tm_w,
+			     const float * bias, const void * zprev,
+			     void * zout, void * pout, float * outf,
+			     int * err, void * stream) {
+  ConvP p;
+  p.g = *g;
+  p.bias = bias;
+  p.zprev = (const uint8_t *) zprev;
+  p.zout = (uint8_t *) zout;
+  p.pout = (uint8_t *) pout;
+  p.outf = outf;
+  p.err = err;
+  const CUtensorMap mi = *(const CUtensorMap *) tm_in;
+  const CUtensorMap mw = *(const CUtensorMap *) tm_w;
+  cudaStream_t s = (cudaStream_t) stream;
+  const int grid = lgbk_cnn_conv_blocks(g);
+  cudaError_t e = cudaSuccess;
+  switch (mode) {
+  case LGBK_CNN_FWD_GELU:
+    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_FWD_GELU>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     CONV_SMEM);
+    if (e == cudaSuccess) {
+      k_conv3_tc<LGBK_CNN_FWD_GELU><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
+	mi, mw, p);
+    }
+    break;
+  case LGBK_CNN_FWD_OUT:
+    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_FWD_OUT>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     CONV_SMEM);
+    if (e == cudaSuccess) {
+      k_conv3_tc<LGBK_CNN_FWD_OUT><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
+	mi, mw, p);
+    }
+    break;
+  case LGBK_CNN_BWD_GELU:
+    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_BWD_GELU>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     CONV_SMEM);
+    if (e == cudaSuccess) {
+      k_conv3_tc<LGBK_CNN_BWD_GELU><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
+	mi, mw, p);
+    }
+    break;
+  case LGBK_CNN_RAW:
+    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_RAW>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     CONV_SMEM);
+    if (e == cudaSuccess) {
+      k_conv3_tc<LGBK_CNN_RAW><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
+	mi, mw, p);
+    }
+    break;
+  default:
+    return (int) cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess) return (int) e;
+  return (int) cudaGetLastError();
+}
+
+/*****************************************************************************
+ *  k_wgrad_tc
+ *****************************************************************************/
+
+struct WgP {
+  lgbk_cnn_geom_t g;
+  float * part;
+  int * err;
+};
+
+__global__ void __launch_bounds__(WG_THREADS, 1)
+k_wgrad_tc(const __grid_constant__ CUtensorMap tm_g,
+	   const __grid_constant__ CUtensorMap tm_x, const WgP p) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc_smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t * sgen = smem_raw + (sbase - raw);
+
+  const uint32_t sX = sbase;
+  const uint32_t sA = sX + WG_XSTAGES*TILEB;
+  const uint32_t sBar = sA + WG_ASTAGES*WG_ASTAGEB;
+  const uint32_t bXFull = sBar;
+  const uint32_t bXEmpty = sBar + 8*WG_XSTAGES;
+  const uint32_t bAFull = sBar + 16*WG_XSTAGES;
+  const uint32_t bAEmpty = bAFull + 8*WG_ASTAGES;
+  const uint32_t bDone = bAEmpty + 8*WG_ASTAGES;
+  uint32_t * tslot = (uint32_t *) (sgen + (bDone + 8 - sbase));
+  volatile int * abort_flag = (volatile int *) (sgen + (bDone + 12 - sbase));
+
+  const int warp = threadIdx.x/32;
+  const int lane = threadIdx.x % 32;
+  const lgbk_cnn_geom_t & g = p.g;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < WG_XSTAGES; s++) {
+      tc_mbar_init(bXFull + 8*s, 1);
+      tc_mbar_init(bXEmpty + 8*s, 1);
+    }
+    for (int s = 0; s < WG_ASTAGES; s++) {
+      tc_mbar_init(bAFull + 8*s, 1);
+      tc_mbar_init(bAEmpty + 8*s, 1);
+    }
+    tc_mbar_init(bDone, 1);
+    *abort_flag = 0;
+    tc_fence_barrier_init();
+  }
+  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), WG_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    tc_prefetch_map(&tm_g);
+    tc_prefetch_map(&tm_x);
+    int xs = 0, as = 0;
+    uint32_t xph = 0, aph = 0;
+    uint32_t xfills[WG_XSTAGES] = {0, 0};
+    uint32_t afills[WG_ASTAGES] = {0, 0, 0, 0};
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile < g.ntiles; tile += gridDim.x) {
+      int x, y0, z0;
+      tile_decode(g, tile, x, y0, z0);
+      if (!tc_mbar_wait(bXEmpty + 8*xs, xph ^ 1u, abort_flag, p.err)) break;
+      tc_mbar_arrive_tx(bXFull + 8*xs, TILEB);
+      for (int l = 0; l < g.lpt; l++) {
+	tc_tma_load_2d(sX + xs*TILEB + l*g.bz*ROWB, &tm_x, bXFull + 8*xs, 0,
+		       prow(g, x, y0 + l, z0));
+      }
+      xfills[xs] += 1;
+      if (++xs == WG_XSTAGES) { xs = 0; xph ^= 1u; }
+      for (int grp = 0; grp < WG_GROUPS; grp++) {
+	if (!tc_mbar_wait(bAEmpty + 8*as, aph ^ 1u, abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_mbar_arrive_tx(bAFull + 8*as, WG_ASTAGEB);
+	for (int j = 0; j < 4; j++) {
+	  int t = 4*grp + j;
+	  if (t > CNN_NTAP - 1) t = CNN_NTAP - 1;   /* padding block, unused */
+	  int dx, dy, dz;
+	  tap_offsets(t, dx, dy, dz);
+	  for (int l = 0; l < g.lpt; l++) {
+	    tc_tma_load_2d(sA + as*WG_ASTAGEB + j*TILEB + l*g.bz*ROWB, &tm_g,
+			   bAFull + 8*as, 0, prow(g, x - dx, y0 + l - dy,
+						  z0 - dz));
+	  }
+	}
+	afills[as] += 1;
+	if (++as == WG_ASTAGES) { as = 0; aph ^= 1u; }
+      }
+    }
+    for (int s = 0; s < WG_XSTAGES; s++) {
+      if (xfills[s]) tc_drain_wait(bXFull + 8*s, (xfills[s] - 1u) & 1u, p.err);
+    }
+    for (int s = 0; s < WG_ASTAGES; s++) {
+      if (afills[s]) tc_drain_wait(bAFull + 8*s, (afills[s] - 1u) & 1u, p.err);
+    }
+  }
+  else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 1, 1);
+    int xs = 0, as = 0;
+    uint32_t xph = 0, aph = 0;
+    int i = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile < g.ntiles; tile += gridDim.x) {
+      if (!tc_mbar_wait(bXFull + 8*xs, xph, abort_flag, p.err)) break;
+      tc_fence_after();
+      for (int grp = 0; grp < WG_GROUPS; grp++) {
+	if (!tc_mbar_wait(bAFull + 8*as, aph, abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_fence_after();
+	#pragma unroll
+	for (int k = 0; k < LGBK_CNN_TILE/16; k++) {
+	  const uint64_t ad = tc_sdesc(sA + as*WG_ASTAGEB + k*1024, TILEB, 512,
+				       LGB_TC_SWIZZLE_64B);
+	  const uint64_t bd = tc_sdesc(sX + xs*TILEB + k*1024, TILEB, 512,
+				       LGB_TC_SWIZZLE_64B);
+	  tc_mma_bf16(tmem + (uint32_t) (grp*CNN_C), ad, bd, idesc,
+		      (uint32_t) ((i | k) != 0));
+	}
+	tc_commit(bAEmpty + 8*as);
+	if (++as == WG_ASTAGES) { as = 0; aph ^= 1u; }
+      }
+      if (!ok) break;
+      tc_commit(bXEmpty + 8*xs);
+      if (++xs == WG_XSTAGES) { xs = 0; xph ^= 1u; }
+      i++;
+    }
+    tc_commit(bDone);
+    tc_drain_wait(bDone, 0, p.err);
+  }
+  else if (warp >= 2) {
+    const int q = warp & 3;
+    bool okw = tc_mbar_wait(bDone, 0, abort_flag, p.err);
+    if (__all_sync(0xffffffffu, okw)) {
+      tc_fence_after();
+      for (int grp = 0; grp < WG_GROUPS; grp++) {
+	uint32_t r[32];
+	tc_tmem_ld32(tmem + (uint32_t) (grp*CNN_C) + ((uint32_t) (q*32) << 16),
+		     r);
+	const int t = 4*grp + q;
+	if (t < CNN_NTAP) {
+	  float4 * o = (float4 *) (p.part + (((long long) blockIdx.x*CNN_NTAP
+					      + t)*CNN_C + lane)*CNN_C);
+	  #pragma unroll
+	  for (int k = 0; k < 8; k++) {
+	    o[k] = make_float4(__uint_as_float(r[4*k]),
+			       __uint_as_float(r[4*k + 1]),
+			       __uint_as_float(r[4*k + 2]),
+			       __uint_as_float(r[4*k + 3]));
+	  }
+	}
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tc_tmem_dealloc(tmem, WG_TMEM_COLS);
+  }
+}
+
+/* dw[k] = sum over blocks of part[b][k], fixed order */
+__global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
+			       float * __restrict__ dw) {
+  const int k = blockIdx.x*blockDim.x + threadIdx.x;
+  if (k >= LGBK_CNN_WL) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; b++) s += (double) part[(long long) b*LGBK_CNN_WL + k];
+  dw[k] = (float) s;
+}
+
+extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
+			      const void * tm_x, float * part, float * dw,
+			      int * err, void * stream) {
+  WgP p;
+  p.g = *g;
+  p.part = part;
+  p.err = err;
+  const CUtensorMap mg = *(const CUtensorMap *) tm_g;
+  const CUtensorMap mx = *(const CUtensorMap *) tm_x;
+  cudaStream_t s = (cudaStream_t) stream;
+  const int grid = lgbk_cnn_wgrad_blocks(g);
+  cudaError_t e = cudaFuncSetAttribute(k_wgrad_tc,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
+  if (e != cudaSuccess) return (int) e;
+  k_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(mg, mx, p);
+  k_wgrad_reduce<<<(LGBK_CNN_WL + 255)/256, 256, 0, s>>>(part, grid, dw);
+  return (int) cudaGetLastError();
+}
+
+/*****************************************************************************
+ *  Elementwise kernels
+ *****************************************************************************/
+
+/* Periodic halo of a padded-row buffer: one thread per (halo row, 16 B) */
+__global__ void k_cnn_halo(lgbk_cnn_geom_t g, uint4 * __restrict__ p) {
+  const long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i >= g.rows*4) return;
+  const long long row = i >> 2;
+  const int q = (int) (i & 3);
+  const int Z = g.nz + 2, Y = g.ny + 2;
+  const int zp = (int) (row % Z);
+  const long long r = row / Z;
+  const int yp = (int) (r % Y);
+  const int xp = (int) (r / Y);
+  const bool halo = (xp == 0 || xp == g.nx + 1 || yp == 0 || yp == g.ny + 1
+		     || zp == 0 || zp == g.nz + 1);
+  if (!halo) return;
+  const int x = (xp - 1 + g.nx) % g.nx;
+  const int y = (yp - 1 + g.ny) % g.ny;
+  const int z = (zp - 1 + g.nz) % g.nz;
+  const long long src = ((long long) (x + 1)*Y + (y + 1))*Z + (z + 1);
+  p[row*4 + q] = p[src*4 + q];
+}
+
+extern "C" int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p,
+			     void * stream) {
+  const long long n = g->rows*4;
+  k_cnn_halo<<<(unsigned int) ((n + 255)/256), 256, 0,
+    (cudaStream_t) stream>>>(*g, (uint4 *) p);
+  return (int) cudaGetLastError();
+}
+
+struct FeatP {
+  float off[5];
+  float scale[5];
+};
+
+__global__ void k_cnn_features(lgbk_cnn_geom_t g, const float * __restrict__ phi,
+			       const float * __restrict__ u,
+			       const float * __restrict__ rho, FeatP fp,
+			       uint8_t * __restrict__ p0) {
+  const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (s >= g.nsites) return;
+  const int z = (int) (s % g.nz);
+  const long long r = s / g.nz;
+  const int y = (int) (r % g.ny);
+  const int x = (int) (r / g.ny);
+  const long long N = g.nsites;
+  float v[32];
+  #pragma unroll
+  for (int c = 0; c < 32; c++) v[c] = 0.0f;
+  v[0] = __fmul_rn(__fsub_rn(phi[s], fp.off[0]), fp.scale[0]);
+  v[1] = __fmul_rn(__fsub_rn(u[s], fp.off[1]), fp.scale[1]);
+  v[2] = __fmul_rn(__fsub_rn(u[N + s], fp.off[2]), fp.scale[2]);
+  v[3] = __fmul_rn(__fsub_rn(u[2*N + s], fp.off[3]), fp.scale[3]);
+  v[4] = __fmul_rn(__fsub_rn(rho[s], fp.off[4]), fp.scale[4]);
+  store_row_bf16(p0 + (long long) prow(g, x, y, z)*ROWB, v);
+}
+
+extern "C" int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
+				 const float * u, const float * rho,
+				 const float off[5], const float scale[5],
+				 void * p0, void * stream) {
+  FeatP fp;
+  for (int c = 0; c < 5; c++) { fp.off[c] = off[c]; fp.scale[c] = scale[c]; }
+  cudaStream_t s = (cudaStream_t) stream;
+  k_cnn_features<<<(unsigned int) ((g->nsites + 255)/256), 256, 0, s>>>(
+    *g, phi, u, rho, fp, (uint8_t *) p0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int) e;
+  return lgbk_cnn_halo(g, p0, stream);
+}
+
+/* fp32 rows [s][32] -> padded bf16 rows (interior), then halo */
+__global__ void k_cnn_pack(lgbk_cnn_geom_t g, const float * __restrict__ src,
+			   uint8_t * __restrict__ p) {
+  const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (s >= g.nsites) return;
+  const int z = (int) (s % g.nz);
+  const long long r = s / g.nz;
+  const int y = (int) (r % g.ny);
+  const int x = (int) (r / g.ny);
+  float v[32];
+  #pragma unroll
+  for (int c = 0; c < 32; c++) v[c] = src[s*32 + c];
+  store_row_bf16(p + (long long) prow(g, x, y, z)*ROWB, v);
+}
+
+extern "C" int lgbk_cnn_pack_rows(const lgbk_cnn_geom_t * g, const float * src,
+				  void * p, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  k_cnn_pack<<<(unsigned int) ((g->nsites + 255)/256), 256, 0, s>>>(
+    *g, src, (uint8_t *) p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int) e;
+  return lgbk_cnn_halo(g, p, stream);
+}
+
+/* dL/dz_4 = 2 (out - t)/N on channels 0..3 (bf16 rows), block partial
+ * sums of (out - t)^2 */
+__global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ out4,
+				const float * __restrict__ t4,
+				uint8_t * __restrict__ pg,
+				double * __restrict__ part) {
+  __shared__ double red[256];
+  const long long N = g.nsites;
+  const float rn2 = (float) (2.0/(double) N);
+  double acc = 0.0;
+  for (long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x; s < N;
+       s += (long long) gridDim.x*blockDim.x) {
+    const int z = (int) (s % g.nz);
+    const long long r = s / g.nz;
+    const int y = (int) (r % g.ny);
+    const int x = (int) (r / g.ny);
+    float v[32];
+    #pragma unroll
+    for (int c = 0; c < 32; c++) v[c] = 0.0f;
+    #pragma unroll
+    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+      const float d = out4[c*N + s] - t4[c*N + s];
+      acc += (double) d*(double) d;
+      v[c] = rn2*d;
+    }
+    store_row_bf16(pg + (long long) prow(g, x, y, z)*ROWB, v);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x/2; w > 0; w /= 2) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_cnn_loss_final(const double * __restrict__ part, int n,
+				 double rn, double * __restrict__ loss) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += part[i];
+    *loss = s*rn;
+  }
+}
+
+extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
+				  const float * t4, void * pg, double * part,
+				  double * loss, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  k_cnn_loss_grad<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, out4, t4,
+						       (uint8_t *) pg, part);
+  k_cnn_loss_final<<<1, 32, 0, s>>>(part, LGBK_CNN_RED_BLOCKS,
+				    1.0/(double) g->nsites, loss);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int) e;
+  return lgbk_cnn_halo(g, pg, stream);
+}
+
+/* Bias gradient: per-block channel sums of the interior rows */
+__global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ pg,
+				double * __restrict__ part) {
+  __shared__ double red[8][32];
+  const long long N = g.nsites;
+  /* 256 threads: 8 groups of 32; lane = channel */
+  const int c = threadIdx.x % 32;
+  const int grp = threadIdx.x/32;
+  double acc = 0.0;
+  for (long long s = (long long) blockIdx.x*8 + grp; s < N;
+       s += (long long) gridDim.x*8) {
+    const int z = (int) (s % g.nz);
+    const long long r = s / g.nz;
+    const int y = (int) (r % g.ny);
+    const int x = (int) (r / g.ny);
+    const __nv_bfloat16 * row = (const __nv_bfloat16 *)
+      (pg + (long long) prow(g, x, y, z)*ROWB);
+    acc += (double) __bfloat162float(row[c]);
+  }
+  red[grp][c] = acc;
+  __syncthreads();
+  if (grp == 0) {
+    double s = 0.0;
+    for (int k = 0; k < 8; k++) s += red[k][c];
+    part[blockIdx.x*32 + c] = s;
+  }
+}
+
+__global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
+				 float * __restrict__ db) {
+  const int c = threadIdx.x;
+  if (c >= 32) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; b++) s += part[b*32 + c];
+  db[c] = (float) s;
+}
+
+extern "C" int lgbk_cnn_bias_grad(const lgbk_cnn_geom_t * g, const void * pg,
+				  double * part, float * db, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  k_cnn_bias_part<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, (const uint8_t *) pg,
+						       part);
+  k_cnn_bias_final<<<1, 32, 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
+  return (int) cudaGetLastError();
+}
+
+__global__ void k_cnn_adam(float * __restrict__ w, float * __restrict__ m,
+			   float * __restrict__ v, const float * __restrict__ gr,
+			   long long n, float lr, float b1, float b2, float eps,
+			   float bc1, float bc2) {
+  const long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = gr[i];
+  const float mi = b1*m[i] + (1.0f - b1)*gi;
+  const float vi = b2*v[i] + (1.0f - b2)*gi*gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi/bc1;
+  const float vh = vi/bc2;
+  w[i] -= lr*mh/(sqrtf(vh) + eps);
+}
+
+extern "C" int lgbk_cnn_adam(float * w, float * m, float * v,
+			     const float * grad, long long n, float lr,
+			     float beta1, float beta2, float eps, int step,
+			     void * stream) {
+  const float bc1 = (float) (1.0 - pow((double) beta1, (double) step));
+  const float bc2 = (float) (1.0 - pow((double) beta2, (double) step));
+  k_cnn_adam<<<(unsigned int) ((n + 255)/256), 256, 0, (cudaStream_t) stream>>>(
+    w, m, v, grad, n, lr, beta1, beta2, eps, bc1, bc2);
+  return (int) cudaGetLastError();
+}
+
+__global__ void k_cnn_wprep(const float * __restrict__ w,
+			    __nv_bfloat16 * __restrict__ wf,
+			    __nv_bfloat16 * __restrict__ wt) {
+  const int k = blockIdx.x*blockDim.x + threadIdx.x;
+  if (k >= LGBK_CNN_WL) return;
+  const int c = k % 32;
+  const int n = (k/32) % 32;
+  const int t = k/1024;
+  const __nv_bfloat16 h = __float2bfloat16_rn(w[k]);
+  wf[k] = h;
+  if (wt) wt[((CNN_NTAP - 1 - t)*32 + c)*32 + n] = h;
+}
+
+extern "C" int lgbk_cnn_wprep(const float * w, void * wf, void * wt,
+			      void * stream) {
+  k_cnn_wprep<<<(LGBK_CNN_WL + 255)/256, 256, 0, (cudaStream_t) stream>>>(
+    w, (__nv_bfloat16 *) wf, (__nv_bfloat16 *) wt);
+  return (int) cudaGetLastError();
+}
+
+/* Correction of the coarse state: phi, u and the momentum of f */
+struct ApplyP {
+  float os[4];
+};
+
+__global__ void k_cnn_apply(lgbk_cnn_geom_t g, const float * __restrict__ out4,
+			    ApplyP ap, float * __restrict__ phi,
+			    float * __restrict__ u, float * __restrict__ f,
+			    const float * __restrict__ rho) {
+  const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  const long long N = g.nsites;
+  if (s >= N) return;
+  phi[s] += ap.os[0]*out4[s];
+  const float du[3] = {ap.os[1]*out4[N + s], ap.os[2]*out4[2*N + s],
+		       ap.os[3]*out4[3*N + s]};
+  u[s] += du[0];
+  u[N + s] += du[1];
+  u[2*N + s] += du[2];
+  if (f) {
+    const float r3 = 3.0f*rho[s];
+    const int8_t cv[19][3] = {{0, 0, 0}, {1, 1, 0}, {1, 0, 1}, {1, 0, 0},
+			      {1, 0, -1}, {1, -1, 0}, {0, 1, 1}, {0, 1, 0},
+			      {0, 1, -1}, {0, 0, 1}, {0, 0, -1}, {0, -1, 1},
+			      {0, -1, 0}, {0, -1, -1}, {-1, 1, 0}, {-1, 0, 1},
+			      {-1, 0, 0}, {-1, 0, -1}, {-1, -1, 0}};
+    const int w36[19] = {12, 1, 1, 2, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1, 1, 1, 2,
+			 1, 1};
+    #pragma unroll
+    for (int q = 1; q < 19; q++) {
+      const float cu = cv[q][0]*du[0] + cv[q][1]*du[1] + cv[q][2]*du[2];
+      f[q*N + s] += (w36[q]*(1.0f/36.0f))*r3*cu;
+    }
+  }
+}
+
+extern "C" int lgbk_cnn_apply(const lgbk_cnn_geom_t * g, const float * out4,
+			      const float os[4], float * phi, float * u,
+			      float * f, const float * rho, void * stream) {
+  ApplyP ap;
+  for (int c = 0; c < 4; c++) ap.os[c] = os[c];
+  k_cnn_apply<<<(unsigned int) ((g->nsites + 255)/256), 256, 0,
+    (cudaStream_t) stream>>>(*g, out4, ap, phi, u, f, rho);
+  return (int) cudaGetLastError();
+}

@@ -1,0 +1,41 @@
+/*****************************************************************************
+ *
+ *  lgb_internal.h
+ *
+ *  Private interface between the two host translation units of
+ *  libludwig_gb.so: ludwig_gb.c (the reference-facing objects) gives
+ *  ludwig_gb_cnn.c (the learned corrector) device views of a binary-fluid
+ *  state.  Not installed, not part of the C ABI.
+ *
+ *****************************************************************************/
+
+#ifndef LGB_INTERNAL_H
+#define LGB_INTERNAL_H
+
+#include "ludwig_gb.h"
+#include "lgb_kernels.h"
+
+typedef struct lgb_view_s {
+  lgbk_dims_t d;
+  int prec;                   /* LUDWIG_GB_FP64 / FP32 / FP16 */
+  int pending;                /* f holds post-collision values */
+  void * f;                   /* stored distributions [19][nsites] */
+  void * phi;                 /* [nsites] */
+  void * u;                   /* [3][nsites] */
+  void * rho;                 /* [nsites] */
+  double rho0;                /* shift of the reduced-precision storage */
+  void * stream;
+} lgb_view_t;
+
+/* layout: 1 = post-collision (pending streaming), 0 = the reference's f,
+ * -1 = as stored */
+int lgb_internal_binary_view(lb_t * lb, field_t * phi, hydro_t * hydro,
+			     int layout, lgb_view_t * v);
+
+/* Declare that the stored f now holds the reference's f (pending = 0) */
+int lgb_internal_lb_set_pending(lb_t * lb, int pending);
+
+int lgb_internal_err(int code, const char * what);     /* LUDWIG_GB_* code */
+int lgb_internal_cuda(int cuda_rc, const char * where); /* cudaError_t -> ECUDA */
+
+#endif

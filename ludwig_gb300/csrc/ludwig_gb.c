@@ -31,6 +31,7 @@
 #include "lgb_stats.h"
 #include "lgb_lc.h"
 #include "lgb_sk.h"
+#include "lgb_internal.h"
 
 #define NVEL LGB_NVEL
 
@@ -2341,5 +2342,57 @@ int ludwig_gb_ensemble_sites(ludwig_gb_ensemble_t * e, long long * n) {
     if (e->active[b]) t += e->off[b + 1] - e->off[b];
   }
   *n = t;
+  return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Private views for the corrector (lgb_internal.h)
+ *****************************************************************************/
+
+int lgb_internal_binary_view(lb_t * lb, field_t * phi, hydro_t * hydro,
+			     int layout, lgb_view_t * v) {
+  if (lb == NULL || phi == NULL || hydro == NULL || v == NULL ||
+      phi->nf != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "binary view: lb, phi, hydro");
+  }
+  if (lb->cs->d.nsites != phi->cs->d.nsites ||
+      lb->cs->d.nsites != hydro->cs->d.nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "binary view: lattice mismatch");
+  }
+  int rc = LUDWIG_GB_OK;
+  if (layout == 1) rc = lb_unstream(lb);
+  else if (layout == 0) rc = lb_materialise(lb);
+  if (rc) return rc;
+  v->d = lb->cs->d;
+  v->prec = lb->prec;
+  v->pending = lb->pending;
+  v->f = lb->f;
+  v->phi = phi->data;
+  v->u = hydro->u;
+  v->rho = hydro->rho;
+  v->rho0 = lb->rho0;
+  v->stream = (void *) stream_;
+  return LUDWIG_GB_OK;
+}
+
+int lgb_internal_lb_set_pending(lb_t * lb, int pending) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb");
+  lb->pending = pending ? 1 : 0;
+  return LUDWIG_GB_OK;
+}
+
+int lgb_internal_err(int code, const char * what) {
+  return err_set(code, "%s", what);
+}
+
+int lgb_internal_cuda(int cuda_rc, const char * where) {
+  return cuda_check(cuda_rc, where);
+}
+
+/* Make p the physics object the step functions read (the reference keeps
+ * one per process; two systems with different mobilities take turns). */
+int ludwig_gb_physics_use(physics_t * p) {
+  if (p == NULL) return err_set(LUDWIG_GB_EINVAL, "physics_use: NULL");
+  phys_ref_ = p;
   return LUDWIG_GB_OK;
 }

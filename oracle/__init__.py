@@ -449,3 +449,127 @@ def length_from_sk(phi, faithful=True):
     sbar = np.where(nk != 0, sk / np.where(nk == 0, 1, nk), 0.0)
     kk = (np.arange(NBIN) + 0.5) * dk
     return 2.0 * np.pi * np.sum(dk * sbar) / np.sum(kk * dk * sbar)
+
+
+# ---------------------------------------------------------------------------
+# Learned corrector: double-precision restatement of the network
+# (cnn_oracle.c).  No reference counterpart: checked by finite differences.
+# ---------------------------------------------------------------------------
+
+CNN_C = 32
+CNN_NTAP = 27
+CNN_WL = CNN_NTAP * CNN_C * CNN_C
+CNN_PL = CNN_WL + CNN_C
+CNN_NLAYER = 4
+_F32 = ctypes.POINTER(ctypes.c_float)
+
+
+def _cnn_lib():
+    L = lib()
+    if not getattr(L, "_cnn_declared", False):
+        L.orc_cnn_forward.argtypes = [_I3, ctypes.c_int, _F32, _F32, _F32,
+                                      _F32, _P]
+        L.orc_cnn_loss_grad.argtypes = [_I3, ctypes.c_int, _F32, _F32, _F32,
+                                        _F32, _F32, _P, _P, _P]
+        L.orc_conv3_fwd.argtypes = [_I3, _P, _P, _P, _P]
+        L.orc_conv3_bwd_data.argtypes = [_I3, _P, _P, _P]
+        L.orc_conv3_wgrad.argtypes = [_I3, _P, _P, _P, _P]
+        L.orc_bf16_round.argtypes = [ctypes.c_double]
+        L.orc_bf16_round.restype = ctypes.c_double
+        L._cnn_declared = True
+    return L
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(_F32)
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_P)
+
+
+def bf16_round(a):
+    """Round to bfloat16 (nearest even) and back, elementwise (numpy)."""
+    f = np.ascontiguousarray(a, dtype=np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def cnn_split(params):
+    """Flat parameters -> (W [4,27,32,32], b [4,32]) views."""
+    p = np.asarray(params, dtype=np.float32).reshape(CNN_NLAYER, CNN_PL)
+    return (p[:, :CNN_WL].reshape(CNN_NLAYER, CNN_NTAP, CNN_C, CNN_C),
+            p[:, CNN_WL:])
+
+
+def cnn_forward(n, in5, scale, params, emulate=True):
+    """Network output [4, N] for inputs in5 [5, N] (features in5 * scale)."""
+    L = _cnn_lib()
+    N = n[0] * n[1] * n[2]
+    W, b = cnn_split(params)
+    i5, pi5 = _f32(in5)
+    sc, psc = _f32(scale)
+    w, pw = _f32(W)
+    bb, pb = _f32(b)
+    out = np.zeros((4, N))
+    rc = L.orc_cnn_forward(_I3(*n), int(emulate), pi5, psc, pw, pb,
+                           out.ctypes.data_as(_P))
+    assert rc == 0
+    return out
+
+
+def cnn_loss_grad(n, in5, scale, t4, params, emulate=True):
+    """(loss, gradient as a flat [4*(27*1024+32)] array)."""
+    L = _cnn_lib()
+    W, b = cnn_split(params)
+    i5, pi5 = _f32(in5)
+    sc, psc = _f32(scale)
+    t, pt = _f32(t4)
+    w, pw = _f32(W)
+    bb, pb = _f32(b)
+    loss = ctypes.c_double()
+    dW = np.zeros((CNN_NLAYER, CNN_WL))
+    db = np.zeros((CNN_NLAYER, CNN_C))
+    rc = L.orc_cnn_loss_grad(_I3(*n), int(emulate), pi5, psc, pt, pw, pb,
+                             ctypes.byref(loss), dW.ctypes.data_as(_P),
+                             db.ctypes.data_as(_P))
+    assert rc == 0
+    return loss.value, np.concatenate([dW, db], axis=1).ravel()
+
+
+def conv3_fwd(n, a, w, b):
+    """z[s][n] = b[n] + sum_t sum_c a[s+e_t][c] w[t][n][c] (double)."""
+    L = _cnn_lib()
+    N = n[0] * n[1] * n[2]
+    a, pa = _f64(a)
+    w, pw = _f64(w)
+    b, pb = _f64(np.zeros(CNN_C) if b is None else b)
+    z = np.zeros((N, CNN_C))
+    L.orc_conv3_fwd(_I3(*n), pa, pw, pb, z.ctypes.data_as(_P))
+    return z
+
+
+def conv3_bwd_data(n, g, w):
+    """da[s][c] = sum_t sum_o g[s-e_t][o] w[t][o][c] (double)."""
+    L = _cnn_lib()
+    N = n[0] * n[1] * n[2]
+    g, pg = _f64(g)
+    w, pw = _f64(w)
+    da = np.zeros((N, CNN_C))
+    L.orc_conv3_bwd_data(_I3(*n), pg, pw, da.ctypes.data_as(_P))
+    return da
+
+
+def conv3_wgrad(n, g, a):
+    """(dw[t][o][c] = sum_s g[s-e_t][o] a[s][c], db[o] = sum_s g[s][o])."""
+    L = _cnn_lib()
+    g, pg = _f64(g)
+    a, pa = _f64(a)
+    dw = np.zeros((CNN_NTAP, CNN_C, CNN_C))
+    db = np.zeros(CNN_C)
+    L.orc_conv3_wgrad(_I3(*n), pg, pa, dw.ctypes.data_as(_P),
+                      db.ctypes.data_as(_P))
+    return dw, db

@@ -40,8 +40,8 @@ def test_conv3_forward(gb, orc, n):
     w = bf(orc, 0.2 * rng.standard_normal((27, 32, 32)))
     b = rng.standard_normal(32).astype(np.float32)
     out = torch.empty((N, 32), dtype=torch.float32, device="cuda")
-    m.conv3(dev(a).data_ptr(), dev(w).data_ptr(), dev(b).data_ptr(), 0,
-            out.data_ptr())
+    da, dw, db = dev(a), dev(w), dev(b)      # keep the tensors alive
+    m.conv3(da.data_ptr(), dw.data_ptr(), db.data_ptr(), 0, out.data_ptr())
     ref = orc.conv3_fwd(n, a, w, b)
     got = out.cpu().numpy().astype(np.float64)
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
@@ -55,7 +55,8 @@ def test_conv3_backward_data(gb, orc, n):
     g = bf(orc, rng.standard_normal((N, 32)))
     w = bf(orc, 0.2 * rng.standard_normal((27, 32, 32)))
     out = torch.empty((N, 32), dtype=torch.float32, device="cuda")
-    m.conv3(dev(g).data_ptr(), dev(w).data_ptr(), 0, 1, out.data_ptr())
+    dg, dw = dev(g), dev(w)
+    m.conv3(dg.data_ptr(), dw.data_ptr(), 0, 1, out.data_ptr())
     ref = orc.conv3_bwd_data(n, g, w)
     got = out.cpu().numpy().astype(np.float64)
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
@@ -70,7 +71,8 @@ def test_conv3_weight_gradient(gb, orc, n):
     g = bf(orc, rng.standard_normal((N, 32)))
     a = bf(orc, rng.standard_normal((N, 32)))
     dw = torch.empty((27, 32, 32), dtype=torch.float32, device="cuda")
-    m.wgrad3(dev(g).data_ptr(), dev(a).data_ptr(), dw.data_ptr())
+    dg, da = dev(g), dev(a)
+    m.wgrad3(dg.data_ptr(), da.data_ptr(), dw.data_ptr())
     ref, _ = orc.conv3_wgrad(n, g, a)
     got = dw.cpu().numpy().astype(np.float64)
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max() * \

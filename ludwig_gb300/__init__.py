@@ -237,6 +237,7 @@ def _declare(L):
         "ludwig_gb_cnn_train_steps": ([_P, ctypes.c_int, pp, pp,
                                        ctypes.c_double, _D], ctypes.c_int),
         "ludwig_gb_cnn_correct": ([_P] * 4, ctypes.c_int),
+        "ludwig_gb_cnn_line_reuse": ([_P, ctypes.c_int], ctypes.c_int),
         "ludwig_gb_cnn_conv3": ([_P] * 4 + [ctypes.c_int, _P], ctypes.c_int),
         "ludwig_gb_cnn_wgrad3": ([_P] * 4, ctypes.c_int),
         "ludwig_gb_coarse_restrict": ([_P] * 6, ctypes.c_int),
@@ -986,6 +987,11 @@ class Corrector(_Obj):
         _check(lib().ludwig_gb_cnn_correct(self.ptr, system.lb.ptr,
                                            system.phi.ptr, system.hydro.ptr),
                "cnn_correct")
+
+    def line_reuse(self, enable=True):
+        """Line-reuse convolutions (nz a multiple of 128) on or off."""
+        _check(lib().ludwig_gb_cnn_line_reuse(self.ptr, int(bool(enable))),
+               "cnn_line_reuse")
 
     def conv3(self, a, w, b, flip, out):
         _check(lib().ludwig_gb_cnn_conv3(self.ptr, a, w, b, int(flip), out),

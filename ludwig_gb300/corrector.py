@@ -207,6 +207,57 @@ def rollout(model, nfine, seed, t0, ncoarse_steps, every, params=FINE_PARAMS,
     return out
 
 
+def time_network(model, x, t, reps=20):
+    """Wall time of one forward pass and of one training step (forward,
+    backward, Adam) on one pair, and the tensor-core work they carry."""
+    torch = _torch()
+    out = torch.empty_like(t)
+    model.forward(x.data_ptr(), out.data_ptr())
+    sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        model.forward(x.data_ptr(), out.data_ptr())
+    sync()
+    fwd = (time.perf_counter() - t0) / reps
+    lr = 1e-12
+    model.train_step(x.data_ptr(), t.data_ptr(), lr)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        model.train_step(x.data_ptr(), t.data_ptr(), lr)
+    sync()
+    step = (time.perf_counter() - t0) / reps
+    n = model.nsites
+    # executed MMA work: 4 convolutions forward, 3 backward-data and 4
+    # weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
+    flop_conv = 2.0 * n * 27 * 32 * 32
+    flop_fwd = 4 * flop_conv
+    flop_step = flop_fwd + 3 * flop_conv + 4 * flop_conv * 28.0 / 27.0
+    return {"sites": n, "forward_ms": 1e3 * fwd, "train_step_ms": 1e3 * step,
+            "forward_tflops": flop_fwd / fwd / 1e12,
+            "train_step_tflops": flop_step / step / 1e12,
+            "note": "wall time incl. the host round trip of each call"}
+
+
+def bench(n, reps=20):
+    """Forward and training-step times of the network on synthetic inputs
+    (n^3 coarse sites), per-tap and line-reuse convolutions."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    N = n ** 3
+    model = Corrector((n, n, n), seed=1)
+    x = 0.1 * torch.randn((5, N), device="cuda", generator=g)
+    x[4] += 1.0
+    t = 0.1 * torch.randn((4, N), device="cuda", generator=g)
+    torch.cuda.synchronize()
+    res = {}
+    for line in (False, True):
+        model.line_reuse(line)
+        res["line_reuse" if line else "per_tap"] = time_network(model, x, t,
+                                                                reps)
+    print(json.dumps(res))
+    return res
+
+
 def choose_method(records, tol=0.02):
     """The corrected coarse run is used only where its phi error stays
     within tol of the fine run; otherwise the plain fine lattice is used."""
@@ -227,9 +278,14 @@ def main(argv=None):
     ap.add_argument("--rollout", type=int, default=250)
     ap.add_argument("--every", type=int, default=25)
     ap.add_argument("--out", default="corrector_out")
+    ap.add_argument("--bench", type=int, default=0,
+                    help="only time the network on a BENCH^3 coarse lattice")
+    ap.add_argument("--reps", type=int, default=20)
     args = ap.parse_args(argv)
 
     load_library()
+    if args.bench:
+        return bench(args.bench, args.reps)
     os.makedirs(args.out, exist_ok=True)
     logf = open(os.path.join(args.out, "log.txt"), "w")
 
@@ -256,14 +312,21 @@ def main(argv=None):
     sync()
     t_train = time.time() - t
     base1, corr1 = one_step_errors(model, X, T)
+    timing = time_network(model, X[0], T[0])
+    log("timing %s" % json.dumps(timing))
     del X, Y, T
-    Xh, Yh = make_pairs(nfine, hold, args.t_first, args.t_gap, args.pairs)
-    Th = targets(Xh, Yh, osc)
-    hb, hc = one_step_errors(model, Xh, Th)
-    del Xh, Yh, Th
-    recs = rollout(model, nfine, hold[0], args.t_first, args.rollout,
-                   args.every, log=log)
-    method, worst = choose_method(recs)
+    hb = hc = None
+    if hold:
+        Xh, Yh = make_pairs(nfine, hold, args.t_first, args.t_gap,
+                            args.pairs)
+        Th = targets(Xh, Yh, osc)
+        hb, hc = one_step_errors(model, Xh, Th)
+        del Xh, Yh, Th
+    recs, method, worst = [], None, None
+    if hold and args.rollout > 0:
+        recs = rollout(model, nfine, hold[0], args.t_first, args.rollout,
+                       args.every, log=log)
+        method, worst = choose_method(recs)
     np.save(os.path.join(args.out, "params.npy"), model.params())
     res = {"fine": list(nfine), "coarse": list(nc), "pairs": len(seeds) *
            args.pairs, "seeds": len(seeds), "holdout_seeds": hold,
@@ -273,7 +336,7 @@ def main(argv=None):
            "one_step_train": {"plain": base1, "corrected": corr1,
                               "initial_network": corr0},
            "one_step_holdout": {"plain": hb, "corrected": hc},
-           "rollout": recs, "method_chosen": method,
+           "rollout": recs, "method_chosen": method, "timing": timing,
            "worst_rollout_error": worst,
            "scales": {"in_off": off, "in_scale": isc, "out_scale": osc}}
     with open(os.path.join(args.out, "result.json"), "w") as f:

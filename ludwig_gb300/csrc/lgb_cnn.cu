@@ -179,6 +179,49 @@ struct ConvP {
   int * err;
 };
 
+/* Epilogue of one output site (x, y, z) from its 32 accumulator columns */
+template <int MODE>
+__device__ __forceinline__ void conv_epilogue(const ConvP & p,
+					      const float bias[32], int x,
+					      int y, int z, const uint32_t r[32]) {
+  const lgbk_cnn_geom_t & g = p.g;
+  const long long s = ((long long) x*g.ny + y)*g.nz + z;
+  float v[32];
+  #pragma unroll
+  for (int n = 0; n < 32; n++) v[n] = __uint_as_float(r[n]);
+
+  if (MODE == LGBK_CNN_FWD_GELU) {
+    #pragma unroll
+    for (int n = 0; n < 32; n++) v[n] += bias[n];
+    store_row_bf16(p.zout + s*ROWB, v);
+    #pragma unroll
+    for (int n = 0; n < 32; n++) v[n] = gelu_f(v[n]);
+    store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+  }
+  else if (MODE == LGBK_CNN_FWD_OUT) {
+    #pragma unroll
+    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+      p.outf[c*g.nsites + s] = v[c] + bias[c];
+    }
+  }
+  else if (MODE == LGBK_CNN_BWD_GELU) {
+    float zp[32];
+    load_row_bf16(p.zprev + s*ROWB, zp);
+    #pragma unroll
+    for (int n = 0; n < 32; n++) v[n] *= gelu_d_f(zp[n]);
+    store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+  }
+  else {
+    float4 * o = (float4 *) (p.outf + s*CNN_C);
+    #pragma unroll
+    for (int k = 0; k < 8; k++) {
+      o[k] = make_float4(v[4*k] + bias[4*k], v[4*k + 1] + bias[4*k + 1],
+			 v[4*k + 2] + bias[4*k + 2],
+			 v[4*k + 3] + bias[4*k + 3]);
+    }
+  }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
 k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
@@ -322,44 +365,7 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
 
       int x, y0, z0;
       tile_decode(g, tile, x, y0, z0);
-      const int l = m / g.bz;
-      const int z = z0 + (m % g.bz);
-      const int y = y0 + l;
-      const long long s = ((long long) x*g.ny + y)*g.nz + z;
-      float v[32];
-      #pragma unroll
-      for (int n = 0; n < 32; n++) v[n] = __uint_as_float(r[n]);
-
-      if (MODE == LGBK_CNN_FWD_GELU) {
-	#pragma unroll
-	for (int n = 0; n < 32; n++) v[n] += bias[n];
-	store_row_bf16(p.zout + s*ROWB, v);
-	#pragma unroll
-	for (int n = 0; n < 32; n++) v[n] = gelu_f(v[n]);
-	store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
-      }
-      else if (MODE == LGBK_CNN_FWD_OUT) {
-	#pragma unroll
-	for (int c = 0; c < LGBK_CNN_NOUT; c++) {
-	  p.outf[c*g.nsites + s] = v[c] + bias[c];
-	}
-      }
-      else if (MODE == LGBK_CNN_BWD_GELU) {
-	float zp[32];
-	load_row_bf16(p.zprev + s*ROWB, zp);
-	#pragma unroll
-	for (int n = 0; n < 32; n++) v[n] *= gelu_d_f(zp[n]);
-	store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
-      }
-      else {
-	float4 * o = (float4 *) (p.outf + s*CNN_C);
-	#pragma unroll
-	for (int k = 0; k < 8; k++) {
-	  o[k] = make_float4(v[4*k] + bias[4*k], v[4*k + 1] + bias[4*k + 1],
-			     v[4*k + 2] + bias[4*k + 2],
-			     v[4*k + 3] + bias[4*k + 3]);
-	}
-      }
+      conv_epilogue<MODE>(p, bias, x, y0 + m / g.bz, z0 + (m % g.bz), r);
       i++;
     }
   }
@@ -373,11 +379,241 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
   }
 }
 
+/*****************************************************************************
+ *  k_conv3_line: the same convolution for nz a multiple of 128, reusing
+ *  neighbour lines.  A CTA walks a run of up to LN_YRUN tiles along y at
+ *  fixed (x, z-chunk); a tile needs the 9 lines (x+dx, y+dy) of 130 rows
+ *  (z0-1 .. z0+128), of which the next tile shares 6, so each tile loads
+ *  only the 3 lines at y+1 (9 at the start of a run).  Lines sit in a ring
+ *  of 4 y-slots per dx.  The A operand is stored without swizzle, as four
+ *  planes of 8 channels x 130 rows (16 bytes per row), so the three z taps
+ *  of a line are the same planes at row offsets 0, 1, 2: start address +
+ *  16 bytes per row.  L2 -> shared traffic per tile drops from 27 boxes of
+ *  128 rows to 3 lines of 130 rows.
+ *****************************************************************************/
+
+#define LN_ROWS   130
+#define LN_CHUNK  2176                  /* >= 130 x 16, 128-byte aligned */
+#define LN_SLOT   (4*LN_CHUNK)
+#define LN_NSLOT  12                    /* 3 dx x 4 y positions */
+#define LN_YRUN   16
+#define LN_TXLINE (4*LN_ROWS*16)        /* bytes of one line (4 planes) */
+#define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256)
+
+__device__ __forceinline__ void line_item(const lgbk_cnn_geom_t & g, int it,
+					  int & x, int & z0, int & ya,
+					  int & yb) {
+  const int nzc = g.nz/LGBK_CNN_TILE;
+  const int nyc = (g.ny + LN_YRUN - 1)/LN_YRUN;
+  const int zc = it % nzc;
+  const int r = it / nzc;
+  const int yc = r % nyc;
+  x = r / nyc;
+  z0 = zc*LGBK_CNN_TILE;
+  ya = yc*LN_YRUN;
+  yb = min(g.ny, ya + LN_YRUN);
+}
+
+__host__ __device__ __forceinline__ int line_items(const lgbk_cnn_geom_t & g) {
+  return g.nx*(g.nz/LGBK_CNN_TILE)*((g.ny + LN_YRUN - 1)/LN_YRUN);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(CONV_THREADS, 1)
+k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
+	     const __grid_constant__ CUtensorMap tm_w, const ConvP p) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc_smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t * sgen = smem_raw + (sbase - raw);
+
+  const uint32_t sW = sbase;
+  const uint32_t sL = sW + CNN_NTAP*WTAPB;
+  const uint32_t sBar = sL + LN_NSLOT*LN_SLOT;
+  const uint32_t bFull = sBar;                 /* 4, per tile */
+  const uint32_t bDone = sBar + 32;            /* 4, per tile */
+  const uint32_t bW = sBar + 64;
+  const uint32_t bTFull = bW + 8;
+  const uint32_t bTEmpty = bW + 24;
+  const uint32_t bFin = bW + 40;
+  uint32_t * tslot = (uint32_t *) (sgen + (bW + 48 - sbase));
+  volatile int * abort_flag = (volatile int *) (sgen + (bW + 52 - sbase));
+
+  const int warp = threadIdx.x/32;
+  const int lane = threadIdx.x % 32;
+  const lgbk_cnn_geom_t & g = p.g;
+  const int nitems = line_items(g);
+
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 4; k++) {
+      tc_mbar_init(bFull + 8*k, 1);
+      tc_mbar_init(bDone + 8*k, 1);
+    }
+    tc_mbar_init(bW, 1);
+    tc_mbar_init(bTFull, 1);
+    tc_mbar_init(bTFull + 8, 1);
+    tc_mbar_init(bTEmpty, 128);
+    tc_mbar_init(bTEmpty + 8, 128);
+    tc_mbar_init(bFin, 1);
+    *abort_flag = 0;
+    tc_fence_barrier_init();
+  }
+  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), CONV_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    tc_prefetch_map(&tm_line);
+    tc_prefetch_map(&tm_w);
+    tc_mbar_arrive_tx(bW, CNN_NTAP*WTAPB);
+    for (int t = 0; t < CNN_NTAP; t++) {
+      tc_tma_load_2d(sW + t*WTAPB, &tm_w, bW, 0, t*CNN_C);
+    }
+    uint32_t fills[4] = {0, 0, 0, 0};
+    bool ok = true;
+    int i = 0;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; y < yb; y++, i++) {
+	const bool first = (y == ya);
+	/* the slots to be overwritten were last read by tile i-1 (a new
+	 * run) or i-2 (within a run) */
+	const int k = first ? i - 1 : i - 2;
+	if (k >= 0 && !tc_mbar_wait(bDone + 8*(k & 3), (uint32_t) (k >> 2) & 1u,
+				    abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	const int nl = first ? 3 : 1;
+	const uint32_t bar = bFull + 8*(i & 3);
+	tc_mbar_arrive_tx(bar, nl*3*LN_TXLINE);
+	for (int dxi = 0; dxi < 3; dxi++) {
+	  for (int li = 0; li < nl; li++) {
+	    const int yy = first ? (y - 1 + li) : (y + 1);
+	    const int slot = dxi*4 + (yy & 3);
+	    const int row = prow(g, x + dxi - 1, yy, z0 - 1);
+	    for (int c = 0; c < 4; c++) {
+	      tc_tma_load_2d(sL + slot*LN_SLOT + c*LN_CHUNK, &tm_line, bar,
+			     8*c, row);
+	    }
+	  }
+	}
+	fills[i & 3] += 1;
+      }
+    }
+    tc_drain_wait(bW, 0, p.err);
+    for (int k = 0; k < 4; k++) {
+      if (fills[k]) tc_drain_wait(bFull + 8*k, (fills[k] - 1u) & 1u, p.err);
+    }
+  }
+  else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 0, 0);
+    bool ok = tc_mbar_wait(bW, 0, abort_flag, p.err);
+    int i = 0;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; y < yb; y++, i++) {
+	const int acc = i & 1;
+	if (!tc_mbar_wait(bTEmpty + 8*acc, ((uint32_t) (i >> 1) & 1u) ^ 1u,
+			  abort_flag, p.err) ||
+	    !tc_mbar_wait(bFull + 8*(i & 3), (uint32_t) (i >> 2) & 1u,
+			  abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_fence_after();
+	const uint32_t d = tmem + (uint32_t) (acc*CNN_C);
+	for (int t = 0; t < CNN_NTAP; t++) {
+	  const int dxi = t/9, dyi = (t/3) % 3, dzi = t % 3;
+	  const int slot = dxi*4 + ((y + dyi - 1) & 3);
+	  const uint32_t abase = sL + slot*LN_SLOT + dzi*16;
+	  #pragma unroll
+	  for (int kh = 0; kh < 2; kh++) {
+	    const uint64_t ad = tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128,
+					 0u);
+	    const uint64_t bd = tc_sdesc(sW + t*WTAPB + kh*32, 16, 512,
+					 LGB_TC_SWIZZLE_64B);
+	    tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((t | kh) != 0));
+	  }
+	}
+	tc_commit(bDone + 8*(i & 3));
+	tc_commit(bTFull + 8*acc);
+      }
+    }
+    tc_commit(bFin);
+    tc_drain_wait(bFin, 0, p.err);
+  }
+  else if (warp >= 2) {
+    const int q = warp & 3;
+    const int m = q*32 + lane;
+    float bias[CNN_C];
+    #pragma unroll
+    for (int n = 0; n < CNN_C; n++) bias[n] = p.bias ? p.bias[n] : 0.0f;
+    int i = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; y < yb; y++, i++) {
+	const int acc = i & 1;
+	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
+				abort_flag, p.err);
+	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
+	tc_fence_after();
+	uint32_t r[32];
+	tc_tmem_ld32(tmem + (uint32_t) (acc*CNN_C)
+		     + ((uint32_t) (q*32) << 16), r);
+	tc_fence_before();
+	tc_mbar_arrive(bTEmpty + 8*acc);
+	conv_epilogue<MODE>(p, bias, x, y, z0 + m, r);
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tc_tmem_dealloc(tmem, CONV_TMEM_COLS);
+  }
+}
+
+template <int MODE>
+static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi,
+			       const CUtensorMap * ml, const CUtensorMap & mw,
+			       const ConvP & p, cudaStream_t s) {
+  cudaError_t e;
+  if (ml) {
+    e = cudaFuncSetAttribute(k_conv3_line<MODE>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     LN_SMEM);
+    if (e != cudaSuccess) return e;
+    int grid = line_items(*g);
+    const int nsm = num_sms();
+    if (grid > nsm) grid = nsm;
+    k_conv3_line<MODE><<<grid, CONV_THREADS, LN_SMEM, s>>>(*ml, mw, p);
+  }
+  else {
+    e = cudaFuncSetAttribute(k_conv3_tc<MODE>,
+			     cudaFuncAttributeMaxDynamicSharedMemorySize,
+			     CONV_SMEM);
+    if (e != cudaSuccess) return e;
+    k_conv3_tc<MODE><<<lgbk_cnn_conv_blocks(g), CONV_THREADS, CONV_SMEM, s>>>(
+      mi, mw, p);
+  }
+  return cudaGetLastError();
+}
+
 extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
-			     const void * tm_in, const void * tm_w,
-			     const float * bias, const void * zprev,
-			     void * zout, void * pout, float * outf,
-			     int * err, void * stream) {
+			     const void * tm_in, const void * tm_line,
+			     const void * tm_w, const float * bias,
+			     const void * zprev, void * zout, void * pout,
+			     float * outf, int * err, void * stream) {
   ConvP p;
   p.g = *g;
   p.bias = bias;
@@ -388,51 +624,27 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
   p.err = err;
   const CUtensorMap mi = *(const CUtensorMap *) tm_in;
   const CUtensorMap mw = *(const CUtensorMap *) tm_w;
+  const CUtensorMap * ml = NULL;
+  CUtensorMap mlv;
+  if (tm_line && g->bz == LGBK_CNN_TILE && g->lpt == 1) {
+    mlv = *(const CUtensorMap *) tm_line;
+    ml = &mlv;
+  }
   cudaStream_t s = (cudaStream_t) stream;
-  const int grid = lgbk_cnn_conv_blocks(g);
-  cudaError_t e = cudaSuccess;
+  cudaError_t e;
   switch (mode) {
   case LGBK_CNN_FWD_GELU:
-    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_FWD_GELU>,
-			     cudaFuncAttributeMaxDynamicSharedMemorySize,
-			     CONV_SMEM);
-    if (e == cudaSuccess) {
-      k_conv3_tc<LGBK_CNN_FWD_GELU><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
-	mi, mw, p);
-    }
-    break;
+    e = launch_conv<LGBK_CNN_FWD_GELU>(g, mi, ml, mw, p, s); break;
   case LGBK_CNN_FWD_OUT:
-    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_FWD_OUT>,
-			     cudaFuncAttributeMaxDynamicSharedMemorySize,
-			     CONV_SMEM);
-    if (e == cudaSuccess) {
-      k_conv3_tc<LGBK_CNN_FWD_OUT><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
-	mi, mw, p);
-    }
-    break;
+    e = launch_conv<LGBK_CNN_FWD_OUT>(g, mi, ml, mw, p, s); break;
   case LGBK_CNN_BWD_GELU:
-    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_BWD_GELU>,
-			     cudaFuncAttributeMaxDynamicSharedMemorySize,
-			     CONV_SMEM);
-    if (e == cudaSuccess) {
-      k_conv3_tc<LGBK_CNN_BWD_GELU><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
-	mi, mw, p);
-    }
-    break;
+    e = launch_conv<LGBK_CNN_BWD_GELU>(g, mi, ml, mw, p, s); break;
   case LGBK_CNN_RAW:
-    e = cudaFuncSetAttribute(k_conv3_tc<LGBK_CNN_RAW>,
-			     cudaFuncAttributeMaxDynamicSharedMemorySize,
-			     CONV_SMEM);
-    if (e == cudaSuccess) {
-      k_conv3_tc<LGBK_CNN_RAW><<<grid, CONV_THREADS, CONV_SMEM, s>>>(
-	mi, mw, p);
-    }
-    break;
+    e = launch_conv<LGBK_CNN_RAW>(g, mi, ml, mw, p, s); break;
   default:
     return (int) cudaErrorInvalidValue;
   }
-  if (e != cudaSuccess) return (int) e;
-  return (int) cudaGetLastError();
+  return (int) e;
 }
 
 /*****************************************************************************

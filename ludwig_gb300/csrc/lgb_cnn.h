@@ -58,11 +58,14 @@ int lgbk_cnn_geom(int nx, int ny, int nz, lgbk_cnn_geom_t * g);
 int lgbk_cnn_conv_blocks(const lgbk_cnn_geom_t * g);
 int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
 
-/* tm_in, tm_w: host pointers to CUtensorMap objects (passed by value) */
+/* tm_in, tm_line, tm_w: host pointers to CUtensorMap objects (passed by
+ * value).  tm_in: rows, box 32 x bz, 64-byte swizzle; tm_w: weights, box
+ * 32 x 32, 64-byte swizzle; tm_line (may be NULL): rows, box 8 x 130, no
+ * swizzle, used with nz a multiple of 128 (line-reuse kernel). */
 int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, const void * tm_in,
-		  const void * tm_w, const float * bias, const void * zprev,
-		  void * zout, void * pout, float * outf, int * err,
-		  void * stream);
+		  const void * tm_line, const void * tm_w, const float * bias,
+		  const void * zprev, void * zout, void * pout, float * outf,
+		  int * err, void * stream);
 
 /* dW[t][n][c] = sum_s g[s - e_t][n] x[s][c]; part: wgrad_blocks*27*1024
  * floats of scratch; dw: 27*1024 floats */

@@ -1,0 +1,79 @@
+"""Reduced-precision forms of the binary-fluid step against FP64.
+
+The symmetric binary fluid (config-1 parameters, M = 0.3) is run from the
+same KISS99 spinodal initial condition in FP64 (the bit-exact form), in
+FP32 with distributions stored as deviations from w_p rho0, and with
+FP16 storage.  At fixed intervals it reports, for each reduced form:
+max |phi - phi_FP64|, the relative drift of the total mass since step 0,
+and the domain length L(t) from the structure factor next to FP64's.
+
+    python -m ludwig_gb300.precision --size 256 --steps 10000 --every 1000
+"""
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import FP16, FP32, FP64, BinaryFluid, load_library
+
+PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
+SEED = 8361235
+
+
+def run(size, steps, every, params=PARAMS, seed=SEED, log=print):
+    n = (size,) * 3 if np.isscalar(size) else tuple(size)
+    systems = {}
+    for name, prec in (("fp64", FP64), ("fp32", FP32), ("fp16", FP16)):
+        s = BinaryFluid(n, prec, **params)
+        s.phi.init_spinodal(seed, 0.0, 0.02)
+        systems[name] = s
+    mass0 = {k: s.lb.moments()[0] for k, s in systems.items()}
+    recs = []
+    t = 0
+    while t < steps:
+        k = min(every, steps - t)
+        t0 = time.time()
+        for s in systems.values():
+            s.step(k)
+        t += k
+        phi64 = systems["fp64"].phi.get()
+        L64 = systems["fp64"].phi.length_from_sk()[0]
+        rec = {"step": t, "L_fp64": L64, "mass_drift_fp64":
+               (systems["fp64"].lb.moments()[0] - mass0["fp64"]) /
+               mass0["fp64"]}
+        for name in ("fp32", "fp16"):
+            s = systems[name]
+            L = s.phi.length_from_sk()[0]
+            rec[name] = {
+                "max_abs_dphi": float(np.abs(s.phi.get() - phi64).max()),
+                "mass_drift_rel": (s.lb.moments()[0] - mass0[name]) /
+                mass0[name],
+                "L": L, "L_rel_err": (L - L64) / L64}
+        rec["wall_s"] = time.time() - t0
+        recs.append(rec)
+        if log:
+            log(json.dumps(rec))
+    return recs
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=10000)
+    ap.add_argument("--every", type=int, default=1000)
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args(argv)
+    load_library()
+    recs = run(args.size, args.steps, args.every)
+    res = {"size": args.size, "steps": args.steps, "params": PARAMS,
+           "seed": SEED, "records": recs}
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump(res, f, indent=1)
+    return res
+
+
+if __name__ == "__main__":
+    main()

@@ -47,6 +47,38 @@ def test_conv3_forward(gb, orc, n):
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("n", [(2, 2, 128), (8, 40, 128), (3, 5, 256),
+                               (160, 17, 128)])
+@pytest.mark.parametrize("flip", [0, 1])
+def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip):
+    """nz a multiple of 128: the line-reuse kernel (runs of tiles along y,
+    including runs of one tile and several runs per CTA) against the
+    oracle, and bit for bit against the one-box-per-tap kernel."""
+    rng = np.random.default_rng(15)
+    N = n[0] * n[1] * n[2]
+    m = gb.Corrector(n)
+    a = bf(orc, rng.standard_normal((N, 32)))
+    w = bf(orc, 0.2 * rng.standard_normal((27, 32, 32)))
+    b = rng.standard_normal(32).astype(np.float32)
+    da, dw, db = dev(a), dev(w), dev(b)
+    out_l = torch.empty((N, 32), dtype=torch.float32, device="cuda")
+    out_t = torch.empty((N, 32), dtype=torch.float32, device="cuda")
+    m.line_reuse(True)
+    m.conv3(da.data_ptr(), dw.data_ptr(), db.data_ptr(), flip,
+            out_l.data_ptr())
+    m.line_reuse(False)
+    m.conv3(da.data_ptr(), dw.data_ptr(), db.data_ptr(), flip,
+            out_t.data_ptr())
+    got = out_l.cpu().numpy().astype(np.float64)
+    if flip:
+        ref = orc.conv3_bwd_data(n, a, w)
+    else:
+        ref = orc.conv3_fwd(n, a, w, b)
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+    # same products, same accumulation order: identical results
+    assert torch.equal(out_l, out_t)
+
+
 @pytest.mark.parametrize("n", [(4, 4, 32), (2, 2, 256), (64, 32, 64)])
 def test_conv3_backward_data(gb, orc, n):
     rng = np.random.default_rng(11)
@@ -88,9 +120,9 @@ def _data(rng, N):
     return in5, t4
 
 
-def test_network_loss_and_gradient_vs_oracle(gb, orc):
-    n = (8, 8, 32)
-    N = 2048
+@pytest.mark.parametrize("n", [(8, 8, 32), (4, 4, 128)])
+def test_network_loss_and_gradient_vs_oracle(gb, orc, n):
+    N = n[0] * n[1] * n[2]
     rng = np.random.default_rng(13)
     m = gb.Corrector(n, seed=7)
     one = np.ones(5, np.float32)

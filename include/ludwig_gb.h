@@ -507,9 +507,11 @@ int ludwig_gb_cnn_train_steps(ludwig_gb_cnn_t * cnn, int nsteps,
  * shifted by w_p rho 3 c_p . du (momentum changed by rho du) */
 int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * cnn, lb_t * lb, field_t * phi,
 			  hydro_t * hydro);
-/* 1 (default): the convolutions reuse neighbour lines where nz is a
- * multiple of 128; 0: one TMA box per tap (any supported extents) */
-int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * cnn, int enable);
+/* Where nz is a multiple of 128 the convolutions reuse neighbour lines:
+ * mode 1 (default) stores a line as 4 unswizzled planes of 8 channels,
+ * mode 2 as 64-byte-swizzled rows; mode 0: one TMA box per tap (any
+ * supported extents) */
+int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * cnn, int mode);
 /* one convolution / weight gradient on given fp32 device arrays
  * (operands rounded to bf16), for checks of the kernels themselves:
  * flip = 0: out[s][n] = b[n] + sum_t sum_c a[s+e_t][c] w[t][n][c];

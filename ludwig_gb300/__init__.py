@@ -988,9 +988,10 @@ class Corrector(_Obj):
                                            system.phi.ptr, system.hydro.ptr),
                "cnn_correct")
 
-    def line_reuse(self, enable=True):
-        """Line-reuse convolutions (nz a multiple of 128) on or off."""
-        _check(lib().ludwig_gb_cnn_line_reuse(self.ptr, int(bool(enable))),
+    def line_reuse(self, mode=1):
+        """Line-reuse convolutions where nz is a multiple of 128: 1 (planes
+        of 8 channels), 2 (swizzled rows), 0/False (one box per tap)."""
+        _check(lib().ludwig_gb_cnn_line_reuse(self.ptr, int(mode)),
                "cnn_line_reuse")
 
     def conv3(self, a, w, b, flip, out):

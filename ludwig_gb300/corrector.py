@@ -250,10 +250,10 @@ def bench(n, reps=20):
     t = 0.1 * torch.randn((4, N), device="cuda", generator=g)
     torch.cuda.synchronize()
     res = {}
-    for line in (False, True):
-        model.line_reuse(line)
-        res["line_reuse" if line else "per_tap"] = time_network(model, x, t,
-                                                                reps)
+    for mode, name in ((0, "per_tap"), (1, "line_planes"),
+                       (2, "line_swizzled")):
+        model.line_reuse(mode)
+        res[name] = time_network(model, x, t, reps)
     print(json.dumps(res))
     return res
 

@@ -11,8 +11,9 @@
  *  is the tile's neighbour rows (a TMA box of contiguous padded rows, K-major,
  *  64-byte swizzle); the weights of all 27 taps stay in shared memory.
  *  Warp roles: warp 0 issues TMA, warp 1 issues tcgen05.mma into one of two
- *  TMEM accumulators, warps 2-5 drain the other accumulator (tcgen05.ld) and
- *  run the epilogue (bias, GELU, GELU', bf16 rows).  The backward-data pass
+ *  TMEM accumulators, warps 2-9 drain the other accumulator (tcgen05.ld,
+ *  two warps per TMEM lane quarter, 16 columns each) and run the epilogue
+ *  (bias, GELU, GELU', bf16 rows).  The backward-data pass
  *  is the same kernel with flipped, transposed weights.
  *
  *  k_wgrad_tc: the weight gradient
@@ -42,12 +43,13 @@
 #define WTAPB      2048                  /* 32 rows of weights per tap */
 
 #define CONV_STAGES  12
-#define CONV_THREADS 192
+#define CONV_THREADS 320               /* TMA, MMA, 8 epilogue warps */
+#define CONV_EPI_THREADS 256
 #define CONV_TMEM_COLS 64
 #define CONV_SMEM (1024 + CNN_NTAP*WTAPB + CONV_STAGES*TILEB + 256)
 
 #define WG_XSTAGES 2
-#define WG_ASTAGES 4
+#define WG_ASTAGES 6
 #define WG_GROUPS  7                     /* ceil(27/4) */
 #define WG_ASTAGEB (4*TILEB)
 #define WG_THREADS 192
@@ -165,6 +167,39 @@ __device__ __forceinline__ void load_row_bf16(const uint8_t * src,
   }
 }
 
+__device__ __forceinline__ void store_half_row_bf16(uint8_t * dst,
+						    const float v[16]) {
+  uint4 * d4 = (uint4 *) dst;
+  #pragma unroll
+  for (int q = 0; q < 2; q++) {
+    uint32_t w[4];
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __nv_bfloat162 h = __floats2bfloat162_rn(v[8*q + 2*k],
+					       v[8*q + 2*k + 1]);
+      w[k] = *(uint32_t *) &h;
+    }
+    d4[q] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+__device__ __forceinline__ void load_half_row_bf16(const uint8_t * src,
+						   float v[16]) {
+  const uint4 * s4 = (const uint4 *) src;
+  #pragma unroll
+  for (int q = 0; q < 2; q++) {
+    uint4 u = s4[q];
+    uint32_t w[4] = {u.x, u.y, u.z, u.w};
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __nv_bfloat162 h = *(__nv_bfloat162 *) &w[k];
+      float2 f = __bfloat1622float2(h);
+      v[8*q + 2*k] = f.x;
+      v[8*q + 2*k + 1] = f.y;
+    }
+  }
+}
+
 /*****************************************************************************
  *  k_conv3_tc
  *****************************************************************************/
@@ -179,42 +214,46 @@ struct ConvP {
   int * err;
 };
 
-/* Epilogue of one output site (x, y, z) from its 32 accumulator columns */
+/* Epilogue of channels c0 .. c0+15 of one output site (x, y, z) from 16
+ * accumulator columns */
 template <int MODE>
 __device__ __forceinline__ void conv_epilogue(const ConvP & p,
-					      const float bias[32], int x,
-					      int y, int z, const uint32_t r[32]) {
+					      const float bias[16], int x,
+					      int y, int z, int c0,
+					      const uint32_t r[16]) {
   const lgbk_cnn_geom_t & g = p.g;
   const long long s = ((long long) x*g.ny + y)*g.nz + z;
-  float v[32];
+  float v[16];
   #pragma unroll
-  for (int n = 0; n < 32; n++) v[n] = __uint_as_float(r[n]);
+  for (int n = 0; n < 16; n++) v[n] = __uint_as_float(r[n]);
 
   if (MODE == LGBK_CNN_FWD_GELU) {
     #pragma unroll
-    for (int n = 0; n < 32; n++) v[n] += bias[n];
-    store_row_bf16(p.zout + s*ROWB, v);
+    for (int n = 0; n < 16; n++) v[n] += bias[n];
+    store_half_row_bf16(p.zout + s*ROWB + 2*c0, v);
     #pragma unroll
-    for (int n = 0; n < 32; n++) v[n] = gelu_f(v[n]);
-    store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+    for (int n = 0; n < 16; n++) v[n] = gelu_f(v[n]);
+    store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
   }
   else if (MODE == LGBK_CNN_FWD_OUT) {
-    #pragma unroll
-    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
-      p.outf[c*g.nsites + s] = v[c] + bias[c];
+    if (c0 == 0) {
+      #pragma unroll
+      for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	p.outf[c*g.nsites + s] = v[c] + bias[c];
+      }
     }
   }
   else if (MODE == LGBK_CNN_BWD_GELU) {
-    float zp[32];
-    load_row_bf16(p.zprev + s*ROWB, zp);
+    float zp[16];
+    load_half_row_bf16(p.zprev + s*ROWB + 2*c0, zp);
     #pragma unroll
-    for (int n = 0; n < 32; n++) v[n] *= gelu_d_f(zp[n]);
-    store_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB, v);
+    for (int n = 0; n < 16; n++) v[n] *= gelu_d_f(zp[n]);
+    store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
   }
   else {
-    float4 * o = (float4 *) (p.outf + s*CNN_C);
+    float4 * o = (float4 *) (p.outf + s*CNN_C + c0);
     #pragma unroll
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 4; k++) {
       o[k] = make_float4(v[4*k] + bias[4*k], v[4*k + 1] + bias[4*k + 1],
 			 v[4*k + 2] + bias[4*k + 2],
 			 v[4*k + 3] + bias[4*k + 3]);
@@ -255,8 +294,8 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
     tc_mbar_init(bW, 1);
     tc_mbar_init(bTFull, 1);
     tc_mbar_init(bTFull + 8, 1);
-    tc_mbar_init(bTEmpty, 128);
-    tc_mbar_init(bTEmpty + 8, 128);
+    tc_mbar_init(bTEmpty, CONV_EPI_THREADS);
+    tc_mbar_init(bTEmpty + 8, CONV_EPI_THREADS);
     tc_mbar_init(bDone, 1);
     *abort_flag = 0;
     tc_fence_barrier_init();
@@ -345,11 +384,13 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
   }
   else if (warp >= 2) {
     /* epilogue: warp w reads TMEM lanes 32*(w % 4) .. +31 */
+    /* warp w reads TMEM lanes 32*(w % 4) .. +31, columns c0 .. c0+15 */
     const int q = warp & 3;
     const int m = q*32 + lane;
-    float bias[CNN_C];
+    const int c0 = 16*((warp - 2) >> 2);
+    float bias[16];
     #pragma unroll
-    for (int n = 0; n < CNN_C; n++) bias[n] = p.bias ? p.bias[n] : 0.0f;
+    for (int n = 0; n < 16; n++) bias[n] = p.bias ? p.bias[c0 + n] : 0.0f;
     int i = 0;
     for (int tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x) {
       const int acc = i & 1;
@@ -357,15 +398,16 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
       bool okw = tc_mbar_wait(bTFull + 8*acc, ap, abort_flag, p.err);
       if (!__all_sync(0xffffffffu, okw)) break;
       tc_fence_after();
-      uint32_t r[32];
-      tc_tmem_ld32(tmem + (uint32_t) (acc*CNN_C) + ((uint32_t) (q*32) << 16),
-		   r);
+      uint32_t r[16];
+      tc_tmem_ld16(tmem + (uint32_t) (acc*CNN_C + c0)
+		   + ((uint32_t) (q*32) << 16), r);
       tc_fence_before();
       tc_mbar_arrive(bTEmpty + 8*acc);
 
       int x, y0, z0;
       tile_decode(g, tile, x, y0, z0);
-      conv_epilogue<MODE>(p, bias, x, y0 + m / g.bz, z0 + (m % g.bz), r);
+      conv_epilogue<MODE>(p, bias, x, y0 + m / g.bz, z0 + (m % g.bz), c0,
+			  r);
       i++;
     }
   }
@@ -418,7 +460,13 @@ __host__ __device__ __forceinline__ int line_items(const lgbk_cnn_geom_t & g) {
   return g.nx*(g.nz/LGBK_CNN_TILE)*((g.ny + LN_YRUN - 1)/LN_YRUN);
 }
 
-template <int MODE>
+/* SWZ = 0: a line is 4 unswizzled planes (8 channels x 130 rows, 16 bytes
+ * a row; TMA box 8 x 130 each), z taps at +16 bytes per row.
+ * SWZ = 1: a line is 130 rows of 64 bytes with the 64-byte swizzle (one
+ * TMA box 32 x 130), z taps at +64 bytes per row; this relies on the
+ * swizzle being a function of the absolute shared-memory address, which
+ * the checks against the one-box-per-tap kernel establish. */
+template <int MODE, int SWZ>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
 k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	     const __grid_constant__ CUtensorMap tm_w, const ConvP p) {
@@ -452,8 +500,8 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     tc_mbar_init(bW, 1);
     tc_mbar_init(bTFull, 1);
     tc_mbar_init(bTFull + 8, 1);
-    tc_mbar_init(bTEmpty, 128);
-    tc_mbar_init(bTEmpty + 8, 128);
+    tc_mbar_init(bTEmpty, CONV_EPI_THREADS);
+    tc_mbar_init(bTEmpty + 8, CONV_EPI_THREADS);
     tc_mbar_init(bFin, 1);
     *abort_flag = 0;
     tc_fence_barrier_init();
@@ -495,9 +543,14 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	    const int yy = first ? (y - 1 + li) : (y + 1);
 	    const int slot = dxi*4 + (yy & 3);
 	    const int row = prow(g, x + dxi - 1, yy, z0 - 1);
-	    for (int c = 0; c < 4; c++) {
-	      tc_tma_load_2d(sL + slot*LN_SLOT + c*LN_CHUNK, &tm_line, bar,
-			     8*c, row);
+	    if (SWZ) {
+	      tc_tma_load_2d(sL + slot*LN_SLOT, &tm_line, bar, 0, row);
+	    }
+	    else {
+	      for (int c = 0; c < 4; c++) {
+		tc_tma_load_2d(sL + slot*LN_SLOT + c*LN_CHUNK, &tm_line, bar,
+			       8*c, row);
+	      }
 	    }
 	  }
 	}
@@ -530,11 +583,12 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	for (int t = 0; t < CNN_NTAP; t++) {
 	  const int dxi = t/9, dyi = (t/3) % 3, dzi = t % 3;
 	  const int slot = dxi*4 + ((y + dyi - 1) & 3);
-	  const uint32_t abase = sL + slot*LN_SLOT + dzi*16;
+	  const uint32_t abase = sL + slot*LN_SLOT + dzi*(SWZ ? ROWB : 16);
 	  #pragma unroll
 	  for (int kh = 0; kh < 2; kh++) {
-	    const uint64_t ad = tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128,
-					 0u);
+	    const uint64_t ad = SWZ
+	      ? tc_sdesc(abase + kh*32, 16, 512, LGB_TC_SWIZZLE_64B)
+	      : tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128, 0u);
 	    const uint64_t bd = tc_sdesc(sW + t*WTAPB + kh*32, 16, 512,
 					 LGB_TC_SWIZZLE_64B);
 	    tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((t | kh) != 0));
@@ -548,11 +602,13 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     tc_drain_wait(bFin, 0, p.err);
   }
   else if (warp >= 2) {
+    /* warp w reads TMEM lanes 32*(w % 4) .. +31, columns c0 .. c0+15 */
     const int q = warp & 3;
     const int m = q*32 + lane;
-    float bias[CNN_C];
+    const int c0 = 16*((warp - 2) >> 2);
+    float bias[16];
     #pragma unroll
-    for (int n = 0; n < CNN_C; n++) bias[n] = p.bias ? p.bias[n] : 0.0f;
+    for (int n = 0; n < 16; n++) bias[n] = p.bias ? p.bias[c0 + n] : 0.0f;
     int i = 0;
     bool ok = true;
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
@@ -564,12 +620,12 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 				abort_flag, p.err);
 	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
 	tc_fence_after();
-	uint32_t r[32];
-	tc_tmem_ld32(tmem + (uint32_t) (acc*CNN_C)
+	uint32_t r[16];
+	tc_tmem_ld16(tmem + (uint32_t) (acc*CNN_C + c0)
 		     + ((uint32_t) (q*32) << 16), r);
 	tc_fence_before();
 	tc_mbar_arrive(bTEmpty + 8*acc);
-	conv_epilogue<MODE>(p, bias, x, y, z0 + m, r);
+	conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
       }
     }
   }
@@ -583,20 +639,30 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   }
 }
 
+template <int MODE, int SWZ>
+static cudaError_t launch_line(const lgbk_cnn_geom_t * g,
+			       const CUtensorMap & ml, const CUtensorMap & mw,
+			       const ConvP & p, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_conv3_line<MODE, SWZ>,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, LN_SMEM);
+  if (e != cudaSuccess) return e;
+  int grid = line_items(*g);
+  const int nsm = num_sms();
+  if (grid > nsm) grid = nsm;
+  k_conv3_line<MODE, SWZ><<<grid, CONV_THREADS, LN_SMEM, s>>>(ml, mw, p);
+  return cudaSuccess;
+}
+
 template <int MODE>
 static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi,
-			       const CUtensorMap * ml, const CUtensorMap & mw,
-			       const ConvP & p, cudaStream_t s) {
+			       const CUtensorMap * ml, int line_kind,
+			       const CUtensorMap & mw, const ConvP & p,
+			       cudaStream_t s) {
   cudaError_t e;
   if (ml) {
-    e = cudaFuncSetAttribute(k_conv3_line<MODE>,
-			     cudaFuncAttributeMaxDynamicSharedMemorySize,
-			     LN_SMEM);
+    e = (line_kind == 2) ? launch_line<MODE, 1>(g, *ml, mw, p, s)
+                         : launch_line<MODE, 0>(g, *ml, mw, p, s);
     if (e != cudaSuccess) return e;
-    int grid = line_items(*g);
-    const int nsm = num_sms();
-    if (grid > nsm) grid = nsm;
-    k_conv3_line<MODE><<<grid, CONV_THREADS, LN_SMEM, s>>>(*ml, mw, p);
   }
   else {
     e = cudaFuncSetAttribute(k_conv3_tc<MODE>,
@@ -611,7 +677,7 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
 
 extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
 			     const void * tm_in, const void * tm_line,
-			     const void * tm_w, const float * bias,
+			     int line_kind, const void * tm_w, const float * bias,
 			     const void * zprev, void * zout, void * pout,
 			     float * outf, int * err, void * stream) {
   ConvP p;
@@ -634,13 +700,13 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
   cudaError_t e;
   switch (mode) {
   case LGBK_CNN_FWD_GELU:
-    e = launch_conv<LGBK_CNN_FWD_GELU>(g, mi, ml, mw, p, s); break;
+    e = launch_conv<LGBK_CNN_FWD_GELU>(g, mi, ml, line_kind, mw, p, s); break;
   case LGBK_CNN_FWD_OUT:
-    e = launch_conv<LGBK_CNN_FWD_OUT>(g, mi, ml, mw, p, s); break;
+    e = launch_conv<LGBK_CNN_FWD_OUT>(g, mi, ml, line_kind, mw, p, s); break;
   case LGBK_CNN_BWD_GELU:
-    e = launch_conv<LGBK_CNN_BWD_GELU>(g, mi, ml, mw, p, s); break;
+    e = launch_conv<LGBK_CNN_BWD_GELU>(g, mi, ml, line_kind, mw, p, s); break;
   case LGBK_CNN_RAW:
-    e = launch_conv<LGBK_CNN_RAW>(g, mi, ml, mw, p, s); break;
+    e = launch_conv<LGBK_CNN_RAW>(g, mi, ml, line_kind, mw, p, s); break;
   default:
     return (int) cudaErrorInvalidValue;
   }
@@ -704,8 +770,9 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_g,
     tc_prefetch_map(&tm_x);
     int xs = 0, as = 0;
     uint32_t xph = 0, aph = 0;
-    uint32_t xfills[WG_XSTAGES] = {0, 0};
-    uint32_t afills[WG_ASTAGES] = {0, 0, 0, 0};
+    uint32_t xfills[WG_XSTAGES], afills[WG_ASTAGES];
+    for (int k = 0; k < WG_XSTAGES; k++) xfills[k] = 0;
+    for (int k = 0; k < WG_ASTAGES; k++) afills[k] = 0;
     bool ok = true;
     for (int tile = blockIdx.x; ok && tile < g.ntiles; tile += gridDim.x) {
       int x, y0, z0;
@@ -1001,31 +1068,41 @@ extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
   return lgbk_cnn_halo(g, pg, stream);
 }
 
-/* Bias gradient: per-block channel sums of the interior rows */
+/* Bias gradient: per-block channel sums of the interior rows.  Blocks
+ * take whole z-lines (contiguous rows); thread t reads 16 bytes (8
+ * channels, group t % 4) of every 64th row, so a warp reads 512
+ * contiguous bytes. */
 __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ pg,
 				double * __restrict__ part) {
-  __shared__ double red[8][32];
-  const long long N = g.nsites;
-  /* 256 threads: 8 groups of 32; lane = channel */
-  const int c = threadIdx.x % 32;
-  const int grp = threadIdx.x/32;
-  double acc = 0.0;
-  for (long long s = (long long) blockIdx.x*8 + grp; s < N;
-       s += (long long) gridDim.x*8) {
-    const int z = (int) (s % g.nz);
-    const long long r = s / g.nz;
-    const int y = (int) (r % g.ny);
-    const int x = (int) (r / g.ny);
-    const __nv_bfloat16 * row = (const __nv_bfloat16 *)
-      (pg + (long long) prow(g, x, y, z)*ROWB);
-    acc += (double) __bfloat162float(row[c]);
+  __shared__ float red[256][9];
+  const int cg = threadIdx.x & 3;
+  const int r0 = threadIdx.x >> 2;
+  float acc[8];
+  #pragma unroll
+  for (int k = 0; k < 8; k++) acc[k] = 0.0f;
+  const int nlines = g.nx*g.ny;
+  for (int ln = blockIdx.x; ln < nlines; ln += gridDim.x) {
+    const int x = ln / g.ny, y = ln % g.ny;
+    const uint8_t * base = pg + (long long) prow(g, x, y, 0)*ROWB;
+    for (int z = r0; z < g.nz; z += 64) {
+      const uint4 u = *(const uint4 *) (base + (long long) z*ROWB + 16*cg);
+      const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+      #pragma unroll
+      for (int k = 0; k < 4; k++) {
+	const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
+	acc[2*k] += f.x;
+	acc[2*k + 1] += f.y;
+      }
+    }
   }
-  red[grp][c] = acc;
+  #pragma unroll
+  for (int k = 0; k < 8; k++) red[threadIdx.x][k] = acc[k];
   __syncthreads();
-  if (grp == 0) {
-    double s = 0.0;
-    for (int k = 0; k < 8; k++) s += red[k][c];
-    part[blockIdx.x*32 + c] = s;
+  if (threadIdx.x < 32) {
+    const int c = threadIdx.x;             /* channel: group c/8, entry c%8 */
+    double sum = 0.0;
+    for (int t = c/8; t < 256; t += 4) sum += (double) red[t][c % 8];
+    part[blockIdx.x*32 + c] = sum;
   }
 }
 

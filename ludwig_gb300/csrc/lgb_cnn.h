@@ -60,10 +60,12 @@ int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
 
 /* tm_in, tm_line, tm_w: host pointers to CUtensorMap objects (passed by
  * value).  tm_in: rows, box 32 x bz, 64-byte swizzle; tm_w: weights, box
- * 32 x 32, 64-byte swizzle; tm_line (may be NULL): rows, box 8 x 130, no
- * swizzle, used with nz a multiple of 128 (line-reuse kernel). */
+ * 32 x 32, 64-byte swizzle; tm_line (may be NULL; nz a multiple of 128):
+ * line_kind 1: rows, box 8 x 130, no swizzle; line_kind 2: rows, box
+ * 32 x 130, 64-byte swizzle (line-reuse kernel). */
 int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, const void * tm_in,
-		  const void * tm_line, const void * tm_w, const float * bias,
+		  const void * tm_line, int line_kind, const void * tm_w,
+		  const float * bias,
 		  const void * zprev, void * zout, void * pout, float * outf,
 		  int * err, void * stream);
 

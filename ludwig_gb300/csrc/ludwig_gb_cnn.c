@@ -42,6 +42,8 @@ struct ludwig_gb_cnn_s {
   CUtensorMap tm_wt[NL];       /* bf16 weights, flipped and transposed */
   CUtensorMap tm_actl[NL];     /* the same buffers as 8 x 130 line boxes */
   CUtensorMap tm_gl[NL + 1];
+  CUtensorMap tm_acts[NL];     /* ... and as swizzled 32 x 130 line boxes */
+  CUtensorMap tm_gs[NL + 1];
   lgbk_cnn_geom_t g;
   int line_ok;                 /* nz a multiple of 128: line-reuse kernel */
   int line_on;
@@ -110,14 +112,16 @@ static int map_rows(CUtensorMap * m, void * base, long long rows,
 
 /* The same rows as boxes of 8 channels x 130 rows without swizzle (one
  * plane of a line for the line-reuse convolution) */
-static int map_lines(CUtensorMap * m, void * base, long long rows) {
+static int map_lines(CUtensorMap * m, void * base, long long rows,
+		     int swizzled) {
   cuuint64_t dims[2] = {32, (cuuint64_t) rows};
   cuuint64_t strides[1] = {64};
-  cuuint32_t box[2] = {8, 130};
+  cuuint32_t box[2] = {swizzled ? 32u : 8u, 130};
   cuuint32_t es[2] = {1, 1};
   CUresult r = encode_(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims,
 		       strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-		       CU_TENSOR_MAP_SWIZZLE_NONE,
+		       swizzled ? CU_TENSOR_MAP_SWIZZLE_64B
+		                : CU_TENSOR_MAP_SWIZZLE_NONE,
 		       CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
 		       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -251,10 +255,12 @@ int ludwig_gb_cnn_create(const int n[3], unsigned long long seed,
   m->line_ok = (g.bz == LGBK_CNN_TILE && g.lpt == 1);
   m->line_on = m->line_ok;
   for (int l = 0; l < NL && !rc && m->line_ok; l++) {
-    rc = map_lines(&m->tm_actl[l], m->act[l], g.rows);
+    rc = map_lines(&m->tm_actl[l], m->act[l], g.rows, 0);
+    if (!rc) rc = map_lines(&m->tm_acts[l], m->act[l], g.rows, 1);
   }
   for (int l = 1; l <= NL && !rc && m->line_ok; l++) {
-    rc = map_lines(&m->tm_gl[l], m->gpad[l], g.rows);
+    rc = map_lines(&m->tm_gl[l], m->gpad[l], g.rows, 0);
+    if (!rc) rc = map_lines(&m->tm_gs[l], m->gpad[l], g.rows, 1);
   }
   if (rc) { ludwig_gb_cnn_free(m); return rc; }
 
@@ -345,15 +351,20 @@ int ludwig_gb_cnn_grads_get(ludwig_gb_cnn_t * m, float * h) {
   return rc;
 }
 
-static const void * lmap(ludwig_gb_cnn_t * m, const CUtensorMap * t) {
-  return m->line_on ? (const void *) t : NULL;
+/* line map for activation layer l (act = 1) or gradient l (act = 0) */
+static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
+  if (!m->line_on) return NULL;
+  if (m->line_on == 2) return act ? &m->tm_acts[l] : &m->tm_gs[l];
+  return act ? &m->tm_actl[l] : &m->tm_gl[l];
 }
 
 /* 1: the line-reuse convolution where the extents allow it (default);
- * 0: one box per tap */
-int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int enable) {
-  if (m == NULL) return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn");
-  m->line_on = enable ? m->line_ok : 0;
+ * 2: the same with swizzled line boxes; 0: one box per tap */
+int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int mode) {
+  if (m == NULL || mode < 0 || mode > 2) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_line_reuse: 0, 1 or 2");
+  }
+  m->line_on = m->line_ok ? mode : 0;
   return LUDWIG_GB_OK;
 }
 
@@ -385,13 +396,13 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
     const float * b = m->params + l*PL + WL;
     if (l < NL - 1) {
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, &m->tm_act[l],
-			 lmap(m, &m->tm_actl[l]), &m->tm_wf[l], b, NULL,
+			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL,
 			 m->zpre[l + 1], m->act[l + 1], NULL, m->err_dev, s);
       if (!rc) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
     }
     else {
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, &m->tm_act[l],
-			 lmap(m, &m->tm_actl[l]), &m->tm_wf[l], b, NULL, NULL,
+			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL, NULL,
 			 NULL, m->out4, m->err_dev, s);
     }
     if (rc) return ck(rc, "cnn conv");
@@ -415,7 +426,7 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
     if (rc) return ck(rc, "cnn wgrad");
     if (l == 0) break;
     rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, &m->tm_g[l + 1],
-		       lmap(m, &m->tm_gl[l + 1]), &m->tm_wt[l], NULL, m->zpre[l],
+		       lmap(m, 0, l + 1), m->line_on, &m->tm_wt[l], NULL, m->zpre[l],
 		       NULL, m->gpad[l], NULL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_halo(g, m->gpad[l], s);
     if (rc) return ck(rc, "cnn conv (backward)");
@@ -604,7 +615,7 @@ int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * m, const float * a, const float * w,
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
   if (!rc) rc = lgbk_cnn_wprep(w, m->wf[0], m->wt[0], s);
   if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, &m->tm_act[0],
-			      lmap(m, &m->tm_actl[0]),
+			      lmap(m, 1, 0), m->line_on,
 			      flip ? &m->tm_wt[0] : &m->tm_wf[0],
 			      flip ? NULL : b, NULL, NULL, NULL, out,
 			      m->err_dev, s);

@@ -50,7 +50,8 @@ def test_conv3_forward(gb, orc, n):
 @pytest.mark.parametrize("n", [(2, 2, 128), (8, 40, 128), (3, 5, 256),
                                (160, 17, 128)])
 @pytest.mark.parametrize("flip", [0, 1])
-def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip, mode):
     """nz a multiple of 128: the line-reuse kernel (runs of tiles along y,
     including runs of one tile and several runs per CTA) against the
     oracle, and bit for bit against the one-box-per-tap kernel."""
@@ -63,10 +64,10 @@ def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip):
     da, dw, db = dev(a), dev(w), dev(b)
     out_l = torch.empty((N, 32), dtype=torch.float32, device="cuda")
     out_t = torch.empty((N, 32), dtype=torch.float32, device="cuda")
-    m.line_reuse(True)
+    m.line_reuse(mode)
     m.conv3(da.data_ptr(), dw.data_ptr(), db.data_ptr(), flip,
             out_l.data_ptr())
-    m.line_reuse(False)
+    m.line_reuse(0)
     m.conv3(da.data_ptr(), dw.data_ptr(), db.data_ptr(), flip,
             out_t.data_ptr())
     got = out_l.cpu().numpy().astype(np.float64)

@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIZE = (256, 256, 256)
-LEGS = ("fp32", "e2e", "fp16", "fp64", "cpu")
+LEGS = ("fp32", "e2e", "fp16", "fp64", "lc", "ens", "cnn", "cpu")
 PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
 SEED = 8361235
 METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
@@ -44,7 +44,9 @@ METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
 # Algorithmic bytes per site update (compulsory traffic of the fused step):
 #   FP64: f 2*19*8 + phi 2*8 + u 2*3*8 = 368;  FP32: 184;  FP16: f 2*19*2 +
 #   phi 2*4 + u 2*12 = 108.  rho (written for output) is not counted.
-ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108}
+ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108,
+              # cholesteric LC: f 2*19 + Q 2*5 + u 2*3 values per site
+              "lc64": 432, "lc32": 216}
 
 # DRAM bytes (read + write) per site of the fused kernels from one ncu
 # capture at 160^3 (profiles/k_binary_fused_fp32_160cube.md and
@@ -55,7 +57,8 @@ NCU_BYTES_PER_SITE = {"fp32": 179.6, "fp64": 370.5, "fp16": None}
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
 LIMITER = {"fp32": "hbm (traffic = compulsory bytes; latency gap)",
            "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
-           "fp16": "hbm"}
+           "fp16": "hbm", "lc64": "fp64 pipe",
+           "lc32": "two kernels; stress and H written between them"}
 
 
 def env_int(name, default):
@@ -245,6 +248,8 @@ def roofline(kind, ms_per_step, nsites, peak, peak_kind):
     algo = ALGO_BYTES[kind] * nsites
     achieved = algo / (ms_per_step * 1e-3) / 1e9
     ncu = NCU_BYTES_PER_SITE.get(kind)
+    if kind not in LIMITER:
+        raise KeyError(kind)
     return {"bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak,
             "traffic": None if ncu is None else ncu * nsites,
@@ -317,6 +322,62 @@ def gpu_arm(args):
         ms64 = max_over_ranks(pg, ms64)
         s64 = None
 
+    # --- cholesteric LC, 128^3, FP32 and FP64 (config-4 model) ----------
+    lc = None
+    if "lc" in legs:
+        lc = {}
+        n_lc = (128, 128, 128)
+        sites_lc = 128 ** 3
+        for name, prec, k in (("fp32", lg.FP32, max(args.steps // 4, 10)),
+                              ("fp64", lg.FP64, 10)):
+            slc = lg.LiquidCrystal(n_lc, eta=0.5, gamma_rot=0.5,
+                                   precision=prec)
+            slc.init_o8m()
+            slc.step(3)
+            ms = slc.time(k)
+            kind = "lc32" if name == "fp32" else "lc64"
+            lc[name] = {"value": sites_lc * k / (ms * 1e-3) / 1e6,
+                        "unit": "MLUPS", "steps": k, "ms_per_step": ms / k,
+                        "roofline": roofline(kind, ms / k, sites_lc, peak,
+                                             peak_kind)}
+            slc = None
+        lc["workload"] = ("cholesteric LC 128^3, O8M blue phase I, pitch 32, "
+                          "A0=0.01 gamma=3 kappa0=kappa1=0.01 xi=0.7 "
+                          "Gamma=0.5 eta=0.5, two fused kernels per step")
+
+    # --- ensemble of 64 uneven boxes, FP32, one persistent launch -------
+    ens = None
+    if "ens" in legs:
+        e = lg.Ensemble(lg.ensemble_config3(), precision=lg.FP32)
+        best, _ = e.autotune(10)
+        ke = max(args.steps // 4, 20)
+        ms = e.time(ke)
+        ens = {"value": e.sites() * ke / (ms * 1e-3) / 1e6, "unit": "MLUPS",
+               "steps": ke, "ms_per_step": ms / ke, "sites": e.sites(),
+               "tiling": {"xchunk": best[0], "tile_y": best[1],
+                          "min_blocks": best[2]},
+               "workload": "64 periodic boxes, edges from {32,48,64,96}, "
+                           "per-box parameters, FP32-shifted, one launch "
+                           "per step under a CUDA graph"}
+        e.close()
+
+    # --- learned corrector on the 128^3 coarse lattice --------------------
+    cnn = None
+    if "cnn" in legs:
+        try:
+            from ludwig_gb300.corrector import bench as cnn_bench
+            r = cnn_bench(128, reps=max(3, min(args.steps // 20, 20)))
+            cnn = {"forward_ms": r["line_planes"]["forward_ms"],
+                   "train_step_ms": r["line_planes"]["train_step_ms"],
+                   "forward_tflops": r["line_planes"]["forward_tflops"],
+                   "train_step_tflops": r["line_planes"]["train_step_tflops"],
+                   "per_tap_forward_ms": r["per_tap"]["forward_ms"],
+                   "unit_note": "executed BF16 MMA work / wall time per call",
+                   "workload": "4-layer 3x3x3 conv net, 32 channels, 128^3 "
+                               "coarse lattice, tcgen05 BF16 / FP32"}
+        except ImportError as exc:                   # torch missing
+            cnn = {"unavailable": str(exc)}
+
     total_sites = sum_over_ranks(pg, nsites)
     per32 = ms32 / args.steps
     value = total_sites * args.steps / (ms32 * 1e-3) / 1e6
@@ -372,6 +433,9 @@ def gpu_arm(args):
                  "ms_per_step": ms16 / args.steps,
                  "roofline": roofline("fp16", ms16 / args.steps, nsites, peak,
                                       peak_kind)},
+        "lc": lc,
+        "ensemble": ens,
+        "corrector": cnn,
         "fp32_over_fp64": value / fp64_mlups,
         "mass_drift_rel_per_step_fp32": drift32,
         "phi_stats_fp32": [float(v) for v in phi_stats32],

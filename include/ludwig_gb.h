@@ -295,6 +295,9 @@ int beris_edw_h_to_host(beris_edw_t * be, double * h);
  * (lb, q, hydro) run the same step in float arithmetic. */
 int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
 		      fe_t * fe, beris_edw_t * be, int nsteps);
+/* device time (ms) of nsteps LC steps, CUDA events on the library stream */
+int ludwig_gb_time_lc(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
+		      fe_t * fe, beris_edw_t * be, int nsteps, double * ms);
 
 /*---------------------------------------------------------------------------
  * Force from the free energy: src/phi_force_stress.h:36-39,
@@ -383,6 +386,9 @@ int stats_field_q(field_t * field, int n, double out[5]);
 int stats_distribution(lb_t * lb, double out[4]);
 /* total symmetric free energy (bulk + gradient) */
 int stats_free_energy_symm(fe_symm_t * fe, double * total);
+/* LC total free energy (fe_lc_fed summed, src/stats_free_energy.c:38);
+ * FP64 fields, after field_grad_compute() of the q gradients */
+int stats_free_energy_lc(fe_lc_t * fe, double * total);
 
 /*---------------------------------------------------------------------------
  * Ensembles: many independent periodic binary-fluid boxes of any sizes and

@@ -198,6 +198,7 @@ def _declare(L):
         "beris_edw_update": ([_P] * 8, ctypes.c_int),
         "beris_edw_h_to_host": ([_P, _D], ctypes.c_int),
         "ludwig_gb_lc_step": ([_P] * 6 + [ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_time_lc": ([_P] * 6 + [ctypes.c_int, _D], ctypes.c_int),
         "ludwig_gb_length_from_sk": ([_P, ctypes.c_int, _D, _D, _D],
                                      ctypes.c_int),
         "ludwig_gb_ensemble_create": ([ctypes.c_int, ctypes.POINTER(BoxParam),
@@ -246,6 +247,7 @@ def _declare(L):
         "stats_field_q": ([_P, ctypes.c_int, _D], ctypes.c_int),
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
+        "stats_free_energy_lc": ([_P, _D], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -712,8 +714,17 @@ class FeLC(_Obj):
         p.q0 = 2.0 * 3.1415926535897932385 / pitch
         p.xi, p.redshift, p.amplitude0, p.coswt = xi, redshift, amplitude, 1.0
         self.param = p
+        self.dq = dq
         _check(lib().fe_lc_param_set(self.ptr, ctypes.byref(p)),
                "fe_lc_param_set")
+
+    def fed_total(self):
+        """Total free energy (FP64 fields): q gradients, then the sum."""
+        self.dq.compute()
+        out = ctypes.c_double()
+        _check(lib().stats_free_energy_lc(self.ptr, ctypes.byref(out)),
+               "stats_free_energy_lc")
+        return out.value
 
 
 class BerisEdw(_Obj):
@@ -783,6 +794,15 @@ class LiquidCrystal:
                                        self.hydro.ptr, self.map.ptr,
                                        self.fe.ptr, self.be.ptr,
                                        int(nsteps)), "ludwig_gb_lc_step")
+
+    def time(self, nsteps):
+        """Device time (ms) of nsteps fused LC steps."""
+        ms = ctypes.c_double()
+        _check(lib().ludwig_gb_time_lc(self.lb.ptr, self.q.ptr,
+                                       self.hydro.ptr, self.map.ptr,
+                                       self.fe.ptr, self.be.ptr, int(nsteps),
+                                       ctypes.byref(ms)), "ludwig_gb_time_lc")
+        return ms.value
 
     def state(self):
         rho, u, force = self.hydro.get()

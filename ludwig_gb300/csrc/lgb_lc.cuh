@@ -57,8 +57,8 @@ __device__ __forceinline__ void lc_expand_grad(const T * g, long long N,
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void lc_h_site(const lgbk_lc_t & p, T q[3][3],
+template <typename T, typename P>
+__device__ __forceinline__ void lc_h_site(const P & p, T q[3][3],
 					  T dq[3][3][3], T dsq[3][3],
 					  T h[3][3]) {
   const T r3 = T(1.0/3.0);
@@ -132,8 +132,8 @@ __device__ __forceinline__ void lc_h_site(const lgbk_lc_t & p, T q[3][3],
   }
 }
 
-template <typename T>
-__device__ __forceinline__ T lc_fed_site(const lgbk_lc_t & p, T q[3][3],
+template <typename T, typename P>
+__device__ __forceinline__ T lc_fed_site(const P & p, T q[3][3],
 					 T dq[3][3][3]) {
   const T r3 = T(1.0/3.0);
   const T gamma = (T) p.gamma, a0 = (T) p.a0;
@@ -187,8 +187,8 @@ __device__ __forceinline__ T lc_fed_site(const lgbk_lc_t & p, T q[3][3],
     - (T) p.epsilon*efield;
 }
 
-template <typename T>
-__device__ __forceinline__ void lc_stress_site(const lgbk_lc_t & p,
+template <typename T, typename P>
+__device__ __forceinline__ void lc_stress_site(const P & p,
 					       T q[3][3], T dq[3][3][3],
 					       T h[3][3], T sth[3][3]) {
   const T r3 = T(1.0/3.0);
@@ -281,8 +281,8 @@ __device__ __forceinline__ void lc_stress_site(const lgbk_lc_t & p,
  *
  *****************************************************************************/
 
-template <typename T>
-__global__ void k_lc_fields(lgbk_dims_t d, lgbk_lc_t p,
+template <typename T, typename P>
+__global__ void k_lc_fields(lgbk_dims_t d, P p,
 			    const T * __restrict__ q, T * __restrict__ pth,
 			    T * __restrict__ h5) {
   long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
@@ -321,6 +321,31 @@ __global__ void k_lc_fields(lgbk_dims_t d, lgbk_lc_t p,
 }
 
 
+/* Step scalars: the doubles themselves for FP64, their float copies
+ * otherwise */
+template <typename T> struct LcPar;
+template <> struct LcPar<double> {
+  static __device__ __forceinline__ double get(const lgbk_lc_step_args_t & a,
+					       int i) {
+    switch (i) {
+    case LGBK_LCF_XI: return a.xi;
+    case LGBK_LCF_GAMMA_ROT: return a.gamma_rot;
+    case LGBK_LCF_RHO0: return a.rho0;
+    case LGBK_LCF_FSCALE: return a.fscale;
+    case LGBK_LCF_RFSCALE: return 1.0/a.fscale;
+    case LGBK_LCF_FX: return a.cp.force_global[0];
+    case LGBK_LCF_FY: return a.cp.force_global[1];
+    case LGBK_LCF_FZ: return a.cp.force_global[2];
+    case LGBK_LCF_RTAU_SHEAR: return a.cp.rtau_shear;
+    default: return a.cp.rtau_bulk;
+    }
+  }
+};
+template <> struct LcPar<float> {
+  static __device__ __forceinline__ float get(const lgbk_lc_step_args_t & a,
+					      int i) { return a.fp[i]; }
+};
+
 template <typename T, typename S, bool SEQ, bool SHIFT, bool HAS_MAP>
 __global__ void k_lc_update(lgbk_dims_t d, lgbk_lc_step_args_t a) {
   long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
@@ -328,8 +353,10 @@ __global__ void k_lc_update(lgbk_dims_t d, lgbk_lc_step_args_t a) {
   const long long N = d.nsites;
   const T r3 = T(1.0/3.0);
   const T dt = T(1.0);
-  const T xi = (T) a.xi, gamma_rot = (T) a.gamma_rot;
-  const T rho0 = (T) a.rho0, fscale = (T) a.fscale;
+  const T xi = LcPar<T>::get(a, LGBK_LCF_XI);
+  const T gamma_rot = LcPar<T>::get(a, LGBK_LCF_GAMMA_ROT);
+  const T rho0 = LcPar<T>::get(a, LGBK_LCF_RHO0);
+  const T fscale = LcPar<T>::get(a, LGBK_LCF_FSCALE);
   const T rfscale = T(1.0)/fscale;
   int z = (int) (i % d.nz);
   long long r = i / d.nz;
@@ -467,12 +494,15 @@ __global__ void k_lc_update(lgbk_dims_t d, lgbk_lc_step_args_t a) {
   T ftot[3];
   #pragma unroll
   for (int ia = 0; ia < 3; ia++) {
-    ftot[ia] = ((T) a.cp.force_global[ia]) + (T(0.0) + force[ia]*T(1.0));
+    ftot[ia] = LcPar<T>::get(a, LGBK_LCF_FX + ia) + (T(0.0) + force[ia]*T(1.0));
   }
   T rho, uu[3];
   T * __restrict__ uo = (T *) a.u_out;
   if (fluid) {
-    lgb_collide_site<T, SEQ, SHIFT, true>(a.cp, rho0, fs, ftot, rho, uu);
+    lgb_collide_site<T, SEQ, SHIFT, true>(
+      LcPar<T>::get(a, LGBK_LCF_RTAU_SHEAR),
+      LcPar<T>::get(a, LGBK_LCF_RTAU_BULK), a.cp.rtau_ghost, rho0, fs, ftot,
+      rho, uu);
     ((T *) a.rho_out)[i] = rho;
   }
   else {

@@ -18,8 +18,15 @@ static dim3 gridn(long long n) {
 template <typename S>
 static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
 		     const lgbk_lc_step_args_t * a, cudaStream_t s) {
-  k_lc_fields<float><<<gridn(d->nsites), TPB, 0, s>>>(
-    *d, *p, (const float *) a->q_in, (float *) a->pth, (float *) a->h);
+  lgbk_lc_f_t pf;
+  pf.a0 = (float) p->a0; pf.q0 = (float) p->q0; pf.gamma = (float) p->gamma;
+  pf.kappa0 = (float) p->kappa0; pf.kappa1 = (float) p->kappa1;
+  pf.xi = (float) p->xi; pf.redshift = (float) p->redshift;
+  pf.rredshift = (float) p->rredshift; pf.epsilon = (float) p->epsilon;
+  for (int i = 0; i < 3; i++) pf.e0[i] = (float) p->e0[i];
+  pf.coswt = (float) p->coswt;
+  k_lc_fields<float, lgbk_lc_f_t><<<gridn(d->nsites), TPB, 0, s>>>(
+    *d, pf, (const float *) a->q_in, (float *) a->pth, (float *) a->h);
   if (a->status) {
     k_lc_update<float, S, false, true, true>
       <<<gridn(d->nsites), TPB, 0, s>>>(*d, *a);

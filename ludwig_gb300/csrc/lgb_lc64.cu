@@ -203,7 +203,7 @@ int lgbk_be_update_f64(const lgbk_dims_t * d, double xi, double gamma_rot,
 extern "C" int lgbk_lc_step_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
 				const lgbk_lc_step_args_t * a, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
-  k_lc_fields<double><<<gridn(d->nsites), TPB, 0, s>>>(
+  k_lc_fields<double, lgbk_lc_t><<<gridn(d->nsites), TPB, 0, s>>>(
     *d, *p, (const double *) a->q_in, (double *) a->pth, (double *) a->h);
   if (a->status) {
     k_lc_update<double, double, true, false, true>

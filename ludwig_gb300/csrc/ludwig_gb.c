@@ -1100,6 +1100,29 @@ static int lc_site_eval(fe_lc_t * fe, int index, int what, double * out) {
   return cuda_check(rc, "lc_site_eval");
 }
 
+/* Total free energy of the LC (src/stats_free_energy.c:38-90 with
+ * fe_lc_fed): FP64 Klein-compensated sum of the density over the sites.
+ * Needs field_grad_compute() on the q gradients first. */
+int stats_free_energy_lc(fe_lc_t * fe, double * total) {
+  if (fe == NULL || total == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
+  int rc = lc_ready(fe);
+  if (rc) return rc;
+  const lgbk_dims_t * d = &fe->q->cs->d;
+  double * tmp = NULL, * scr = NULL, r[4];
+  if ((rc = red_scratch(&scr))) return rc;
+  rc = dev_alloc((void **) &tmp, (size_t) d->nsites*sizeof(double), "fed");
+  if (rc) return rc;
+  lgbk_lc_t k;
+  lc_kparam(fe, &k);
+  rc = lgbk_lc_fed_f64(d, &k, (const double *) fe->q->data, fe->dq->grad,
+		       tmp, stream_);
+  if (rc == 0) rc = lgbk_field_stats(d, LGBK_PREC_FP64, tmp, scr, r, stream_);
+  dev_free(tmp);
+  if (rc) return cuda_check(rc, "stats_free_energy_lc");
+  *total = r[0];
+  return LUDWIG_GB_OK;
+}
+
 static int lc_fed(fe_t * base, int index, double * fed) {
   return lc_site_eval((fe_lc_t *) base, index, 0, fed);
 }
@@ -1316,8 +1339,42 @@ int beris_edw_update(beris_edw_t * be, fe_t * fe, field_t * fq,
   return LUDWIG_GB_OK;
 }
 
+static int lc_step_async(lb_t * lb, field_t * q, hydro_t * hydro,
+			 map_t * map, fe_t * fe, beris_edw_t * be, int nsteps);
+
 int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
 		      fe_t * fe, beris_edw_t * be, int nsteps) {
+  int rc = lc_step_async(lb, q, hydro, map, fe, be, nsteps);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* Device time of nsteps LC steps (CUDA events on the library stream) */
+int ludwig_gb_time_lc(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
+		      fe_t * fe, beris_edw_t * be, int nsteps, double * ms) {
+  cudaEvent_t e0, e1;
+  int rc;
+  if (ms == NULL) return err_set(LUDWIG_GB_EINVAL, "time_lc");
+  if ((rc = lc_step_async(lb, q, hydro, map, fe, be, 0))) return rc;
+  CK(cudaEventCreate(&e0), "event");
+  CK(cudaEventCreate(&e1), "event");
+  CK(cudaEventRecord(e0, stream_), "record");
+  rc = lc_step_async(lb, q, hydro, map, fe, be, nsteps);
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e1, stream_), "record");
+  if (rc == 0) rc = cuda_check(cudaEventSynchronize(e1), "sync");
+  if (rc == 0) {
+    float t = 0.0f;
+    rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+static int lc_step_async(lb_t * lb, field_t * q, hydro_t * hydro,
+			 map_t * map, fe_t * fe, beris_edw_t * be, int nsteps) {
   if (lb == NULL || q == NULL || hydro == NULL || fe == NULL || be == NULL ||
       nsteps < 0 || q->nf != 5) {
     return err_set(LUDWIG_GB_EINVAL, "ludwig_gb_lc_step");
@@ -1350,6 +1407,7 @@ int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
   a.rho_out = hydro->rho;
   a.pth = be->flux;                                /* 9 N elements */
   a.h = (const char *) be->flux + 9*N*es;          /* 5 N elements */
+  lgbk_lc_args_pack(&a);
   for (int n = 0; n < nsteps; n++) {
     a.f_in = lb->f;   a.f_out = lb->fprime;
     a.q_in = q->data; a.q_out = q->data2;
@@ -1359,7 +1417,6 @@ int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,
     void * t = q->data; q->data = q->data2; q->data2 = t;
     t = hydro->u; hydro->u = hydro->u2; hydro->u2 = t;
   }
-  CK(cudaStreamSynchronize(stream_), "sync");
   return LUDWIG_GB_OK;
 }
 

@@ -8,6 +8,7 @@ max |phi - phi_FP64|, the relative drift of the total mass since step 0,
 and the domain length L(t) from the structure factor next to FP64's.
 
     python -m ludwig_gb300.precision --size 256 --steps 10000 --every 1000
+    python -m ludwig_gb300.precision --lc --size 128 --steps 5000 --every 500
 """
 
 import argparse
@@ -58,17 +59,66 @@ def run(size, steps, every, params=PARAMS, seed=SEED, log=print):
     return recs
 
 
+LC_PARAMS = dict(a0=0.01, gamma=3.0, kappa0=0.01, kappa1=0.01, pitch=32.0,
+                 xi=0.7, redshift=1.0, amplitude=-0.2)
+
+
+def run_lc(size, steps, every, log=print):
+    """Cholesteric LC (blue phase I, O8M start) in FP64 and FP32: max |dQ|
+    and the total free energy of each run (evaluated in FP64 from its Q)
+    at fixed intervals."""
+    from . import LiquidCrystal
+    n = (size,) * 3 if np.isscalar(size) else tuple(size)
+    s64 = LiquidCrystal(n, eta=0.5, gamma_rot=0.5, precision=FP64,
+                        **LC_PARAMS)
+    s32 = LiquidCrystal(n, eta=0.5, gamma_rot=0.5, precision=FP32,
+                        **LC_PARAMS)
+    holder = LiquidCrystal(n, eta=0.5, gamma_rot=0.5, precision=FP64,
+                           **LC_PARAMS)
+    s64.init_o8m()
+    s32.q.set(s64.q.get())
+    recs = []
+    t = 0
+    while t < steps:
+        k = min(every, steps - t)
+        t0 = time.time()
+        s64.step(k)
+        s32.step(k)
+        t += k
+        q64 = s64.q.get()
+        q32 = s32.q.get()
+        f64 = s64.fe.fed_total()
+        holder.q.set(q32)
+        f32 = holder.fe.fed_total()
+        rec = {"step": t, "max_abs_dq": float(np.abs(q32 - q64).max()),
+               "max_abs_q": float(np.abs(q64).max()),
+               "fed_fp64": f64, "fed_fp32": f32,
+               "fed_rel_err": (f32 - f64) / abs(f64),
+               "wall_s": time.time() - t0}
+        recs.append(rec)
+        if log:
+            log(json.dumps(rec))
+    return recs
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--every", type=int, default=1000)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--lc", action="store_true",
+                    help="the cholesteric LC (FP64 vs FP32) instead")
     args = ap.parse_args(argv)
     load_library()
-    recs = run(args.size, args.steps, args.every)
-    res = {"size": args.size, "steps": args.steps, "params": PARAMS,
-           "seed": SEED, "records": recs}
+    if args.lc:
+        recs = run_lc(args.size, args.steps, args.every)
+        res = {"model": "cholesteric LC", "size": args.size,
+               "steps": args.steps, "params": LC_PARAMS, "records": recs}
+    else:
+        recs = run(args.size, args.steps, args.every)
+        res = {"size": args.size, "steps": args.steps, "params": PARAMS,
+               "seed": SEED, "records": recs}
     if args.out:
         with open(args.out, "w") as f:
             json.dump(res, f, indent=1)

@@ -199,6 +199,9 @@ static inline unsigned int kiss_next(unsigned int s[4]) {
   return (s[1] + (s[0] ^ b));
 }
 
+/* One draw of the generator (ns_uniform, src/noise.h:96-112) on state s */
+unsigned int orc_kiss_next(unsigned int s[4]) { return kiss_next(s); }
+
 void orc_spinodal_init(const int L[3], int seed, double phi0, double amp,
 		       double * phi) {
 

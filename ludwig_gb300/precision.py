@@ -17,10 +17,19 @@ import time
 
 import numpy as np
 
-from . import FP16, FP32, FP64, BinaryFluid, load_library
+from . import FP16, FP32, FP64, BinaryFluid, LudwigGBError, load_library
 
 PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
 SEED = 8361235
+
+
+def _mass(s):
+    """Total mass, or None once the state is no longer finite."""
+    try:
+        m = s.lb.moments()[0]
+    except LudwigGBError:
+        return None
+    return m if np.isfinite(m) else None
 
 
 def run(size, steps, every, params=PARAMS, seed=SEED, log=print):
@@ -39,18 +48,30 @@ def run(size, steps, every, params=PARAMS, seed=SEED, log=print):
         for s in systems.values():
             s.step(k)
         t += k
+        m64 = _mass(systems["fp64"])
+        if m64 is None:
+            # The FP64 run (bit-exact with the reference) has diverged: the
+            # parameters are unstable at this size; nothing to compare with.
+            rec = {"step": t, "diverged": "fp64 (bit-exact path): mass "
+                   "not finite"}
+            recs.append(rec)
+            if log:
+                log(json.dumps(rec))
+            break
         phi64 = systems["fp64"].phi.get()
         L64 = systems["fp64"].phi.length_from_sk()[0]
-        rec = {"step": t, "L_fp64": L64, "mass_drift_fp64":
-               (systems["fp64"].lb.moments()[0] - mass0["fp64"]) /
-               mass0["fp64"]}
+        rec = {"step": t, "L_fp64": L64,
+               "mass_drift_fp64": (m64 - mass0["fp64"]) / mass0["fp64"]}
         for name in ("fp32", "fp16"):
             s = systems[name]
+            m = _mass(s)
+            if m is None:
+                rec[name] = {"diverged": True}
+                continue
             L = s.phi.length_from_sk()[0]
             rec[name] = {
                 "max_abs_dphi": float(np.abs(s.phi.get() - phi64).max()),
-                "mass_drift_rel": (s.lb.moments()[0] - mass0[name]) /
-                mass0[name],
+                "mass_drift_rel": (m - mass0[name]) / mass0[name],
                 "L": L, "L_rel_err": (L - L64) / L64}
         rec["wall_s"] = time.time() - t0
         recs.append(rec)
@@ -107,6 +128,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--every", type=int, default=1000)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--eta", type=float, default=PARAMS["eta"],
+                    help="shear viscosity (binary fluid)")
     ap.add_argument("--lc", action="store_true",
                     help="the cholesteric LC (FP64 vs FP32) instead")
     args = ap.parse_args(argv)
@@ -116,8 +139,9 @@ def main(argv=None):
         res = {"model": "cholesteric LC", "size": args.size,
                "steps": args.steps, "params": LC_PARAMS, "records": recs}
     else:
-        recs = run(args.size, args.steps, args.every)
-        res = {"size": args.size, "steps": args.steps, "params": PARAMS,
+        params = dict(PARAMS, eta=args.eta)
+        recs = run(args.size, args.steps, args.every, params=params)
+        res = {"size": args.size, "steps": args.steps, "params": params,
                "seed": SEED, "records": recs}
     if args.out:
         with open(args.out, "w") as f:

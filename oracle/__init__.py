@@ -259,6 +259,60 @@ def binary_steps(state, fe, mobility, cp, nsteps, status=None):
     return s
 
 
+class Lb2State:
+    """Host state of the two-distribution binary fluid: f, g, phi, u."""
+
+    def __init__(self, L, f, g, phi=None):
+        self.L = tuple(int(v) for v in L)
+        n = self.L
+        self.f = np.ascontiguousarray(f, dtype=np.float64).copy()
+        self.g = np.ascontiguousarray(g, dtype=np.float64).copy()
+        self.phi = (np.zeros((1,) + n) if phi is None else
+                    np.ascontiguousarray(phi, dtype=np.float64).copy())
+        self.u = np.zeros((3,) + n)
+        self._scratch = np.zeros_like(self.f)
+        self._work = np.zeros((4,) + n)
+
+
+def lb2_g_from_phi(phi):
+    """src/phi_lb_coupler.c:107-135: phi into g_0, the other g_p zero."""
+    phi = np.asarray(phi, dtype=np.float64)
+    g = np.zeros((NVEL,) + phi.shape[-3:])
+    g[0] = phi.reshape(phi.shape[-3:])
+    return g
+
+
+def lb2_steps(state, fe, mobility, cp, nsteps):
+    """Advance an Lb2State by nsteps of the main loop with ndist = 2."""
+    s = state
+    L = lib()
+    L.orc_lb2_step.argtypes = [_I3, ctypes.POINTER(SymmParam),
+                               ctypes.c_double, ctypes.POINTER(CollideParam),
+                               _P, _P, _P, _P, _P, _P, ctypes.c_int]
+    L.orc_lb2_step(_dims(s.L), ctypes.byref(fe), float(mobility),
+                   ctypes.byref(cp), _p(s.f), _p(s.g), _p(s._scratch),
+                   _p(s.phi), _p(s.u), _p(s._work), int(nsteps))
+    return s
+
+
+def collide_binary(L, fe, cp, mobility, f, g, phi):
+    """One binary collision (gradients of phi computed here): (f, g, u)."""
+    Lb = lib()
+    Lb.orc_collide_binary.argtypes = [_I3, ctypes.POINTER(SymmParam),
+                                      ctypes.POINTER(CollideParam),
+                                      ctypes.c_double, _P, _P, _P, _P, _P,
+                                      _P]
+    f = np.ascontiguousarray(f, dtype=np.float64).copy()
+    g = np.ascontiguousarray(g, dtype=np.float64).copy()
+    phi = np.ascontiguousarray(phi, dtype=np.float64)
+    grad, delsq = grad_7pt(L, phi)
+    u = np.zeros((3,) + tuple(L))
+    Lb.orc_collide_binary(_dims(L), ctypes.byref(fe), ctypes.byref(cp),
+                          float(mobility), _p(f), _p(g), _p(phi), _p(grad),
+                          _p(delsq), _p(u))
+    return f, g, u
+
+
 def field_stats(L, q):
     out = np.zeros(5)
     lib().orc_field_stats(_dims(L), _p(np.ascontiguousarray(q[0] if q.ndim == 4

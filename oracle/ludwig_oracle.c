@@ -528,8 +528,23 @@ void orc_ch_update(const int L[3], const double * fw, const double * fe,
  *
  *****************************************************************************/
 
+static void collide_site_sth(const orc_collide_param_t * p,
+			     double fs[NVEL], const double force[3],
+			     const double sth[3][3], double * prho,
+			     double u[3]);
+
 static void collide_site(const orc_collide_param_t * p, double fs[NVEL],
 			 const double force[3], double * prho, double u[3]) {
+  collide_site_sth(p, fs, force, NULL, prho, u);
+}
+
+/* As collide_site; with sth the equilibrium stress includes the
+ * thermodynamic stress (src/collision.c:706-1013, lb_collision_mrt2_site):
+ * seq = rho u u + sth. */
+static void collide_site_sth(const orc_collide_param_t * p,
+			     double fs[NVEL], const double force[3],
+			     const double sth[3][3], double * prho,
+			     double u[3]) {
 
   double mode[NVEL];
   double s[3][3], seq[3][3];
@@ -568,7 +583,10 @@ static void collide_site(const orc_collide_param_t * p, double fs[NVEL],
   tr_s = 0.0;
   tr_seq = 0.0;
   for (int ia = 0; ia < 3; ia++) {
-    for (int ib = 0; ib < 3; ib++) seq[ia][ib] = rho*u[ia]*u[ib];
+    for (int ib = 0; ib < 3; ib++) {
+      seq[ia][ib] = rho*u[ia]*u[ib];
+      if (sth) seq[ia][ib] = rho*u[ia]*u[ib] + sth[ia][ib];
+    }
     tr_s   += s[ia][ia];
     tr_seq += seq[ia][ia];
   }
@@ -713,6 +731,135 @@ void orc_binary_step(const int L[3], const orc_symm_param_t * fe,
     orc_collide_mrt(L, cp, status, f, force, rho, u);
     orc_propagate(L, f, fscratch);
     memcpy(f, fscratch, NVEL*N*sizeof(double));
+  }
+}
+
+/*****************************************************************************
+ *
+ *  Two-distribution binary fluid (symmetric_lb), ndist = 2.
+ *
+ *  orc_phi_from_g: phi = sum_p g_p in order p (src/phi_lb_coupler.c:72-93).
+ *
+ *  orc_collide_binary: src/collision.c:706-1013 (lb_collision_mrt2_site)
+ *  for one step at every site: f relaxes as the single-fluid collision
+ *  with the chemical stress (src/symmetric.c:372, fe_symm_str_v) in the
+ *  equilibrium stress; then the order-parameter distribution is rebuilt
+ *  from phi, jphi (relaxed toward phi u at rate rtau2 = 2/(1 + 2 M),
+ *  src/collision.c:1951) and sphi = phi u u + mu delta, with the sums of
+ *  d3q19_mode2f_phi (src/collision.c:2849-): for each p, jdotc adds the
+ *  jphi components with c_pa != 0 and sphidotq the sphi entries with
+ *  c_pa c_pb - delta_ab/3 != 0 in row-major order; then
+ *  g_p = w_p (3 jdotc + 4.5 sphidotq) (+ phi for p = 0).
+ *
+ *  u is written at every site (no rho: the binary collision does not
+ *  store it).
+ *
+ *****************************************************************************/
+
+void orc_phi_from_g(const int L[3], const double * g, double * phi) {
+  size_t N = nsites(L);
+  #pragma omp parallel for
+  for (size_t i = 0; i < N; i++) {
+    double phi0 = 0.0;
+    for (int q = 0; q < NVEL; q++) phi0 += g[q*N + i];
+    phi[i] = phi0;
+  }
+}
+
+void orc_collide_binary(const int L[3], const orc_symm_param_t * fe,
+			const orc_collide_param_t * cp, double mobility,
+			double * f, double * g, const double * phi,
+			const double * grad, const double * delsq, double * u) {
+  size_t N = nsites(L);
+  const double rtau2 = 2.0/(1.0 + 2.0*mobility);
+  const double r3 = (1.0/3.0);
+  const double q_diag[2] = {-(1.0/3.0), (2.0/3.0)};   /* c_a^2 = 0, 1 */
+  tables_init();
+
+  #pragma omp parallel for
+  for (size_t i = 0; i < N; i++) {
+    double fs[NVEL], fa[3], uu[3], r, sth[3][3];
+    const double ph = phi[i];
+    const double gr[3] = {grad[i], grad[N + i], grad[2*N + i]};
+    const double d = delsq[i];
+
+    /* chemical stress, src/symmetric.c:372-400 */
+    {
+      const double p0 = 0.5*fe->a*ph*ph + 0.75*fe->b*ph*ph*ph*ph
+	- fe->kappa*ph*d - 0.5*fe->kappa*(gr[0]*gr[0] + gr[1]*gr[1]
+					 + gr[2]*gr[2]);
+      for (int ia = 0; ia < 3; ia++) {
+	for (int ib = 0; ib < 3; ib++) {
+	  const double dab = (ia == ib);
+	  sth[ia][ib] = p0*dab + fe->kappa*gr[ia]*gr[ib];
+	}
+      }
+    }
+
+    for (int q = 0; q < NVEL; q++) fs[q] = f[q*N + i];
+    for (int ia = 0; ia < 3; ia++) fa[ia] = cp->force_global[ia] + 0.0;
+    collide_site_sth(cp, fs, fa, (const double (*)[3]) sth, &r, uu);
+    for (int q = 0; q < NVEL; q++) f[q*N + i] = fs[q];
+    for (int ia = 0; ia < 3; ia++) u[ia*N + i] = uu[ia];
+
+    /* order parameter distribution */
+    const double mu = symm_mu_site(fe, ph, d);
+    double jphi[3] = {0.0, 0.0, 0.0};
+    for (int q = 1; q < NVEL; q++) {
+      for (int ia = 0; ia < 3; ia++) {
+	if (cv_[q][ia]) jphi[ia] += cv_[q][ia]*g[q*N + i];
+      }
+    }
+    double sphi[3][3];
+    for (int ia = 0; ia < 3; ia++) {
+      for (int ib = 0; ib < 3; ib++) {
+	const double dab = (ia == ib);
+	sphi[ia][ib] = ph*uu[ia]*uu[ib] + mu*dab;
+      }
+      jphi[ia] = jphi[ia] - rtau2*(jphi[ia] - ph*uu[ia]);
+    }
+    (void) r3;
+    for (int q = 0; q < NVEL; q++) {
+      double jdotc = 0.0, sphidotq = 0.0;
+      for (int ia = 0; ia < 3; ia++) {
+	if (cv_[q][ia] > 0) jdotc += jphi[ia];
+	if (cv_[q][ia] < 0) jdotc -= jphi[ia];
+      }
+      for (int ia = 0; ia < 3; ia++) {
+	for (int ib = 0; ib < 3; ib++) {
+	  double qab;
+	  if (ia == ib) qab = q_diag[cv_[q][ia] != 0];
+	  else qab = (double) (cv_[q][ia]*cv_[q][ib]);
+	  if (qab != 0.0) sphidotq += sphi[ia][ib]*qab;
+	}
+      }
+      double gq = wv_[q]*(jdotc*3.0 + sphidotq*4.5);
+      if (q == 0) gq = wv_[q]*(jdotc*3.0 + sphidotq*4.5) + ph;
+      g[q*N + i] = gq;
+    }
+  }
+}
+
+/* The main loop of src/ludwig.c:528-860 with ndist = 2: phi from g,
+ * gradients, binary collision, propagation of f and g.  The results are
+ * in f, g, phi (phi of the last step's start) and u.  work: 4 N doubles;
+ * scratch: 19 N doubles. */
+void orc_lb2_step(const int L[3], const orc_symm_param_t * fe,
+		  double mobility, const orc_collide_param_t * cp,
+		  double * f, double * g, double * scratch, double * phi,
+		  double * u, double * work, int nsteps) {
+  size_t N = nsites(L);
+  double * grad = work;
+  double * delsq = work + 3*N;
+  tables_init();
+  for (int step = 0; step < nsteps; step++) {
+    orc_phi_from_g(L, g, phi);
+    orc_grad_7pt(L, 1, phi, grad, delsq);
+    orc_collide_binary(L, fe, cp, mobility, f, g, phi, grad, delsq, u);
+    orc_propagate(L, f, scratch);
+    memcpy(f, scratch, NVEL*N*sizeof(double));
+    orc_propagate(L, g, scratch);
+    memcpy(g, scratch, NVEL*N*sizeof(double));
   }
 }
 

@@ -89,6 +89,17 @@ void orc_binary_step(const int L[3], const orc_symm_param_t * fe,
 		     double * rho, double * force, double * work, int nsteps);
 
 /* Statistics, src/util_sum.c:30-175, src/phi_stats.c:211-270 */
+/* Two-distribution binary fluid (symmetric_lb) */
+void orc_phi_from_g(const int L[3], const double * g, double * phi);
+void orc_collide_binary(const int L[3], const orc_symm_param_t * fe,
+			const orc_collide_param_t * cp, double mobility,
+			double * f, double * g, const double * phi,
+			const double * grad, const double * delsq, double * u);
+void orc_lb2_step(const int L[3], const orc_symm_param_t * fe,
+		  double mobility, const orc_collide_param_t * cp,
+		  double * f, double * g, double * scratch, double * phi,
+		  double * u, double * work, int nsteps);
+
 typedef struct orc_klein_s { double sum; double cs; double ccs; } orc_klein_t;
 void orc_klein_add(orc_klein_t * k, double v);
 double orc_klein_total(const orc_klein_t * k);

@@ -21,6 +21,9 @@
  *    ref_shim mode=force    size=.. A= B= K= in=PREFIX out=PREFIX
  *    ref_shim mode=ch       size=.. A= B= K= M= in=PREFIX out=PREFIX
  *    ref_shim mode=step     size=.. A= B= K= M= eta= steps= in=PREFIX out=PREFIX
+ *    ref_shim mode=lb2      ndist=2 size=.. steps=N A= B= K= M= eta= seed=
+ *                           (symmetric_lb: two distributions)
+ *    ref_shim mode=collide2 ndist=2 size=.. in=PREFIX out=PREFIX
  *    ref_shim mode=lc       size=.. steps= a0= gamma= kappa0= kappa1= pitch= xi=
  *                           Gamma= redshift= amplitude= eta= out=PREFIX
  *    ref_shim mode=lc_fields size=.. (lc parameters) in=PREFIX out=PREFIX
@@ -62,6 +65,7 @@
 #include "blue_phase_init.h"
 #include "blue_phase_beris_edwards.h"
 #include "colloids.h"
+#include "phi_lb_coupler.h"
 
 static const char * arg(int argc, char ** argv, const char * key,
 			const char * def) {
@@ -213,6 +217,7 @@ static void sys_create(int argc, char ** argv, sys_t * s) {
   }
   {
     lb_data_options_t opts = lb_data_options_default();
+    opts.ndist = atoi(arg(argc, argv, "ndist", "1"));
     lb_data_create(s->pe, s->cs, &opts, &s->lb);
     lb_init_rest_f(s->lb, 1.0);
   }
@@ -256,6 +261,43 @@ static void sys_step(sys_t * s) {
   lb_propagation(s->lb);
 }
 
+/* One time step of the two-distribution binary fluid (symmetric_lb):
+ * src/ludwig.c:528-860 with ndist = 2 (phi from g, gradients, no order
+ * parameter dynamics outside the collision). */
+
+static void sys_step_lb2(sys_t * s) {
+  double zero[3] = {0.0, 0.0, 0.0};
+  physics_control_next_step(s->phys);
+  hydro_f_zero(s->hydro, zero);
+  phi_lb_to_field(s->phi, s->lb);
+  field_halo(s->phi);
+  field_grad_compute(s->dphi);
+  hydro_u_zero(s->hydro, zero);
+  lb_collide(s->lb, s->hydro, s->map, NULL, (fe_t *) s->fe, NULL);
+  lb_halo(s->lb);
+  lb_propagation(s->lb);
+}
+
+static void lb_get_dist(cs_t * cs, lb_t * lb, int nd, double * out) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int p = 0; p < NVEL; p++)
+	out[canon(p,x,y,z)] = lb->f[LB_ADDR(lb->nsite, lb->ndist, NVEL,
+					     index, nd, p)];
+    }
+}
+
+static void lb_put_dist(cs_t * cs, lb_t * lb, int nd, const double * in) {
+  for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+    for (int z = 0; z < L[2]; z++) {
+      int index = cs_index(cs, x+1, y+1, z+1);
+      for (int p = 0; p < NVEL; p++)
+	lb->f[LB_ADDR(lb->nsite, lb->ndist, NVEL, index, nd, p)]
+	  = in[canon(p,x,y,z)];
+    }
+}
+
 static void sys_dump(sys_t * s, const char * out) {
   size_t n = nint();
   double * a = malloc(NVEL*n*sizeof(double));
@@ -264,6 +306,9 @@ static void sys_dump(sys_t * s, const char * out) {
   field_get(s->cs, s->hydro->rho, a);    writef(out, "rho", a, n);
   field_get(s->cs, s->hydro->force, a);  writef(out, "force", a, 3*n);
   lb_get(s->cs, s->lb, a);               writef(out, "f", a, NVEL*n);
+  if (s->lb->ndist == 2) {
+    lb_get_dist(s->cs, s->lb, 1, a);     writef(out, "g", a, NVEL*n);
+  }
   free(a);
 }
 
@@ -445,6 +490,36 @@ int main(int argc, char ** argv) {
       sys_dump(&s, p0);
     }
     for (int n = 0; n < steps; n++) sys_step(&s);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "lb2") == 0) {
+    /* symmetric_lb: spinodal phi moved into g (src/phi_lb_coupler.c:107),
+     * then the main loop with ndist = 2 */
+    int seed = atoi(arg(argc, argv, "seed", "13"));
+    double amp = argd(argc, argv, "noise", 0.02);
+    double phi0 = argd(argc, argv, "phi0", 0.0);
+    int steps = atoi(arg(argc, argv, "steps", "1"));
+    if (s.lb->ndist != 2) { fprintf(stderr, "lb2 needs ndist=2\n"); return 2; }
+    field_phi_init_spinodal(s.phi, seed, phi0, amp);
+    phi_lb_from_field(s.phi, s.lb);
+    for (int n = 0; n < steps; n++) sys_step_lb2(&s);
+    sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "collide2") == 0) {
+    /* one binary collision (lb_collision_binary) on given f, g, phi
+     * (gradients from phi) */
+    size_t n = nint();
+    double * f = readf(in, "f", NVEL*n);
+    double * g = readf(in, "g", NVEL*n);
+    double * phi = readf(in, "phi", n);
+    if (s.lb->ndist != 2) { fprintf(stderr, "collide2 needs ndist=2\n");
+      return 2; }
+    lb_put_dist(s.cs, s.lb, 0, f);
+    lb_put_dist(s.cs, s.lb, 1, g);
+    field_put(s.cs, s.phi, phi);
+    field_halo(s.phi);
+    field_grad_compute(s.dphi);
+    lb_collide(s.lb, s.hydro, s.map, NULL, (fe_t *) s.fe, NULL);
     sys_dump(&s, out);
   }
   else if (strcmp(mode, "step") == 0) {

@@ -7,7 +7,7 @@ phi_force_calculation, phi_cahn_hilliard and the main-loop step of
 src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
 
 Needs the reference sources (only where they are present):
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2]
 """
 
 import os
@@ -99,9 +99,51 @@ def lc_op_case(name, mode, L, inputs, outputs):
     print("wrote", name)
 
 
-def main(ref_root):
+LB2 = dict(A=-0.0625, B=0.0625, K=0.04, M=0.45, eta=0.1)
+
+
+def lb2_run_case(name, L, steps, seed):
+    """symmetric_lb (two distributions): spinodal phi moved into g, then
+    the main loop with ndist = 2; mobility 0.45 (stable on this route)."""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "out")
+        oracle.run_reference(kv(L, mode="lb2", ndist=2, steps=steps,
+                                seed=seed, noise=0.02, phi0=0.0, out=out,
+                                **LB2))
+        res = {"L": np.array(L), "steps": steps, "seed": seed}
+        for k, nc in (("phi", 1), ("u", 3), ("f", 19), ("g", 19)):
+            res[k] = oracle.read_array(out, k, (nc,) + L)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+    print("wrote", name)
+
+
+def lb2_cases():
+    rng = np.random.default_rng(20261204)
+    lb2_run_case("lb2_8x6x4_s10", (8, 6, 4), 10, 8361235)
+    lb2_run_case("lb2_12x10x8_s60", (12, 10, 8), 60, 91)
+    L = (6, 5, 4)
+    f = oracle.lb_init_rest(L) * (1.0 + 1e-3 * rng.standard_normal((19,) + L))
+    phi = rng.uniform(-1, 1, (1,) + L)
+    g = 1e-2 * rng.standard_normal((19,) + L)
+    g[0] = phi[0] - g[1:].sum(axis=0)
+    with tempfile.TemporaryDirectory() as tmp:
+        pin, pout = os.path.join(tmp, "in"), os.path.join(tmp, "out")
+        oracle.write_arrays(pin, f=f, g=g, phi=phi)
+        oracle.run_reference(kv(L, mode="collide2", ndist=2, **{"in": pin},
+                                out=pout, **LB2))
+        res = {"L": np.array(L), "in_f": f, "in_g": g, "in_phi": phi}
+        for k, nc in (("f", 19), ("g", 19), ("u", 3)):
+            res[k] = oracle.read_array(pout, k, (nc,) + L)
+    np.savez_compressed(os.path.join(HERE, "collide2_6x5x4.npz"), **res)
+    print("wrote collide2_6x5x4")
+
+
+def main(ref_root, only=None):
     if not oracle.build_reference(ref_root):
         raise SystemExit("reference sources not found at " + ref_root)
+    if only == "lb2":
+        lb2_cases()
+        return
     rng = np.random.default_rng(20261203)
 
     run_case("run_8x6x4_s10", (8, 6, 4), 10, 8361235)
@@ -136,7 +178,10 @@ def main(ref_root):
                dict(h=5, stress=9, fed=1))
     u = 0.005 * rng.standard_normal((3,) + L)
     lc_op_case("lc_be_6x5x4", "lc_be", L, dict(q=q, u=u), dict(q=5))
+    lb2_cases()
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a[7:] for a in sys.argv[1:] if a.startswith("--only=")]
+    main(args[0] if args else "/root/reference", only[0] if only else None)

@@ -125,3 +125,29 @@ def test_oracle_beris_edwards(orc):
     q = orc.lc_be_update(L_of(g), orc.lc_param(), GAMMA_ROT, g["in_q"],
                          g["in_u"])
     assert np.array_equal(q, g["q"])
+
+
+# ---------------------------------------------------------------------------
+# Two-distribution binary fluid (symmetric_lb, ndist = 2), mobility 0.45
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", ["lb2_8x6x4_s10", "lb2_12x10x8_s60"])
+def test_oracle_lb2_run_matches_reference(orc, name):
+    g = load(name)
+    L = L_of(g)
+    phi0 = orc.spinodal_init(L, int(g["seed"]), 0.0, 0.02)
+    st = orc.Lb2State(L, orc.lb_init_rest(L), orc.lb2_g_from_phi(phi0))
+    orc.lb2_steps(st, orc.symm_param(A, B, KAPPA), 0.45,
+                  orc.collide_param_m10(ETA), int(g["steps"]))
+    for k in ("f", "g", "phi", "u"):
+        assert np.array_equal(getattr(st, k), g[k]), k
+
+
+def test_oracle_binary_collision_matches_reference(orc):
+    g = load("collide2_6x5x4")
+    f, gg, u = orc.collide_binary(L_of(g), orc.symm_param(A, B, KAPPA),
+                                  orc.collide_param_m10(ETA), 0.45,
+                                  g["in_f"], g["in_g"], g["in_phi"])
+    assert np.array_equal(f, g["f"])
+    assert np.array_equal(gg, g["g"])
+    assert np.array_equal(u, g["u"])

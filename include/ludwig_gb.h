@@ -127,6 +127,17 @@ int lb_init_rest_f(lb_t * lb, double rho0);                /* lb_data.c:659 */
 int lb_halo(lb_t * lb);                                     /* lb_data.c:754 */
 int lb_f_to_host(lb_t * lb, double * f);       /* 19 x nsites, reference f */
 int lb_f_from_host(lb_t * lb, const double * f);
+/* ndist = 2 (symmetric_lb): the order-parameter distribution g */
+int lb_g_to_host(lb_t * lb, double * g);       /* 19 x nsites, reference g */
+int lb_g_from_host(lb_t * lb, const double * g);
+/* src/phi_lb_coupler.h: phi = sum_p g_p; g_0 = phi, other g_p = 0 */
+int phi_lb_to_field(field_t * phi, lb_t * lb);
+int phi_lb_from_field(field_t * phi, lb_t * lb);
+/* nsteps of the main loop with ndist = 2 (src/ludwig.c:528-860):
+ * phi_lb_to_field, field_grad_compute, binary lb_collide
+ * (src/collision.c:604-1013), lb_propagation.  FP64, bit-exact. */
+int ludwig_gb_lb2_step(lb_t * lb, field_t * phi, hydro_t * hydro, fe_t * fe,
+		       int nsteps);
 
 /* src/collision.h:27, src/collision.c:143 */
 int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
@@ -152,6 +163,10 @@ int field_halo(field_t * obj);                              /* field.c:371 */
 int field_to_host(field_t * obj, double * data);
 int field_from_host(field_t * obj, const double * data);
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp);
+/* src/field_phi_init.c:38: phi = phistar tanh((r - radius)/xi) about the
+ * box centre */
+int field_phi_init_drop(field_t * phi, double xi, double radius,
+			double phistar, int is_centred);
                                                     /* field_phi_init.c:484 */
 
 /*---------------------------------------------------------------------------
@@ -161,6 +176,15 @@ int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p);
 int field_grad_free(field_grad_t * obj);
 /* src/field_grad.c:319 -> src/gradient_3d_7pt_fluid.c:231 */
 int field_grad_compute(field_grad_t * obj);
+/* The stencil of field_grad_compute: 7 (default, 3d_7pt_fluid) or 27
+ * (3d_27pt_fluid, src/gradient_3d_27pt_fluid.c); the reference selects it
+ * with field_grad_set(fg, grad_3d_27pt_fluid_d2, NULL).  The fused steps
+ * use 7 points and reject 27. */
+int field_grad_stencil_set(field_grad_t * fg, int npoints);
+/* src/advection.c:82: order of the advective fluxes of phi_cahn_hilliard
+ * and beris_edw_update (1 upwind, default; 2 centred; 3 upwind-biased);
+ * the fused steps use 1 and reject the others */
+int advection_order_set(int n);
 /* grad: 3*nf x nsites ([n][ia]), delsq: nf x nsites */
 int field_grad_to_host(field_grad_t * obj, double * grad, double * delsq);
 

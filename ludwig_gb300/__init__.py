@@ -136,6 +136,11 @@ def _declare(L):
         "lb_f_to_host": ([_P, _D], ctypes.c_int),
         "lb_f_from_host": ([_P, _D], ctypes.c_int),
         "lb_collide": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+        "lb_g_to_host": ([_P, _D], ctypes.c_int),
+        "lb_g_from_host": ([_P, _D], ctypes.c_int),
+        "phi_lb_to_field": ([_P, _P], ctypes.c_int),
+        "phi_lb_from_field": ([_P, _P], ctypes.c_int),
+        "ludwig_gb_lb2_step": ([_P] * 4 + [ctypes.c_int], ctypes.c_int),
         "lb_propagation": ([_P], ctypes.c_int),
         "field_create": ([_P, _P, _P, ctypes.c_char_p,
                           ctypes.POINTER(FieldOptions), pp], ctypes.c_int),
@@ -145,9 +150,13 @@ def _declare(L):
         "field_from_host": ([_P, _D], ctypes.c_int),
         "field_phi_init_spinodal": ([_P, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double], ctypes.c_int),
+        "field_phi_init_drop": ([_P] + [ctypes.c_double] * 3 + [ctypes.c_int],
+                                ctypes.c_int),
         "field_grad_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
         "field_grad_free": ([_P], ctypes.c_int),
         "field_grad_compute": ([_P], ctypes.c_int),
+        "field_grad_stencil_set": ([_P, ctypes.c_int], ctypes.c_int),
+        "advection_order_set": ([ctypes.c_int], ctypes.c_int),
         "field_grad_to_host": ([_P, _D, _D], ctypes.c_int),
         "hydro_create": ([_P, _P, _P, ctypes.POINTER(HydroOptions), pp],
                          ctypes.c_int),
@@ -345,11 +354,13 @@ class LB(_Obj):
     """lb_t: D3Q19 distributions (src/lb_data.c)."""
     _free = "lb_free"
 
-    def __init__(self, cs, precision=FP64, nrelax=0, fp16_scale=0.0):
+    def __init__(self, cs, precision=FP64, nrelax=0, fp16_scale=0.0,
+                 ndist=1):
         super().__init__()
         self.cs = cs
         self.precision = precision
-        o = LbDataOptions(3, 19, 1, int(nrelax), int(precision),
+        self.ndist = int(ndist)
+        o = LbDataOptions(3, 19, int(ndist), int(nrelax), int(precision),
                           float(fp16_scale))
         self.ptr = _new("lb_data_create", cs.pe.ptr, cs.ptr, ctypes.byref(o))
 
@@ -365,6 +376,17 @@ class LB(_Obj):
         f = np.ascontiguousarray(f, dtype=np.float64)
         assert f.shape == (NVEL,) + self.cs.ntotal
         _check(lib().lb_f_from_host(self.ptr, _dp(f)), "lb_f_from_host")
+
+    def get_g(self):
+        """The order-parameter distribution (ndist = 2)."""
+        g = np.zeros((NVEL,) + self.cs.ntotal)
+        _check(lib().lb_g_to_host(self.ptr, _dp(g)), "lb_g_to_host")
+        return g
+
+    def set_g(self, g):
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        assert g.shape == (NVEL,) + self.cs.ntotal
+        _check(lib().lb_g_from_host(self.ptr, _dp(g)), "lb_g_from_host")
 
     def collide(self, hydro, map_=None, fe=None):
         _check(lib().lb_collide(self.ptr, hydro.ptr,
@@ -413,6 +435,13 @@ class Field(_Obj):
         _check(lib().field_phi_init_spinodal(self.ptr, int(seed), float(phi0),
                                              float(amp)), "spinodal")
 
+    def init_drop(self, xi, radius, phistar=1.0, centred=False):
+        """A drop of the given radius and interface width (src/
+        field_phi_init.c:38)."""
+        _check(lib().field_phi_init_drop(self.ptr, float(xi), float(radius),
+                                         float(phistar), int(bool(centred))),
+               "field_phi_init_drop")
+
     def length_from_sk(self, faithful=True):
         """Domain length L from the structure factor (and S, counts)."""
         L = ctypes.c_double()
@@ -440,6 +469,11 @@ class FieldGrad(_Obj):
 
     def compute(self):
         _check(lib().field_grad_compute(self.ptr), "field_grad_compute")
+
+    def set_stencil(self, npoints):
+        """7 (default) or 27 points (src/gradient_3d_27pt_fluid.c)."""
+        _check(lib().field_grad_stencil_set(self.ptr, int(npoints)),
+               "field_grad_stencil_set")
 
     def get(self):
         nf = self.field.nf
@@ -636,8 +670,70 @@ class BinaryFluid:
                 "rho": rho, "force": force}
 
 
+class BinaryFluidLB:
+    """The two-distribution binary fluid (symmetric_lb, ndist = 2): the
+    order parameter is the zeroth moment of a second distribution g and
+    evolves in the collision (src/collision.c:604-1013).  FP64."""
+
+    def __init__(self, ntotal, a=-0.0625, b=0.0625, kappa=0.04,
+                 mobility=0.45, eta=0.1, eta_bulk=None, rho0=1.0,
+                 fbody=(0.0, 0.0, 0.0), device=0):
+        self.pe = PE(device)
+        self.cs = Coords(self.pe, ntotal)
+        self.phys = Physics(self.pe, rho0=rho0, eta=eta, eta_bulk=eta_bulk,
+                            mobility=mobility, fbody=fbody)
+        self.lb = LB(self.cs, FP64, ndist=2)
+        self.phi = Field(self.cs, 1, 2, FP64, "phi")
+        self.dphi = FieldGrad(self.phi, 2)
+        self.hydro = Hydro(self.cs, FP64)
+        self.map = Map(self.cs)
+        self.fe = FeSymm(self.cs, self.phi, self.dphi, a, b, kappa)
+        self.lb.init_rest(rho0)
+
+    def use_physics(self):
+        _check(lib().ludwig_gb_physics_use(self.phys.ptr), "physics_use")
+
+    def init_spinodal(self, seed, phi0=0.0, amp=0.02):
+        """Spinodal phi moved into g (src/phi_lb_coupler.c:107)."""
+        self.phi.init_spinodal(seed, phi0, amp)
+        _check(lib().phi_lb_from_field(self.phi.ptr, self.lb.ptr),
+               "phi_lb_from_field")
+
+    def step_reference_order(self, nsteps=1):
+        """One call per reference function, in the main-loop order."""
+        self.use_physics()
+        for _ in range(nsteps):
+            self.hydro.f_zero()
+            _check(lib().phi_lb_to_field(self.phi.ptr, self.lb.ptr),
+                   "phi_lb_to_field")
+            self.phi.halo()
+            self.dphi.compute()
+            self.hydro.u_zero()
+            self.lb.collide(self.hydro, self.map, self.fe)
+            self.lb.halo()
+            self.lb.propagation()
+
+    def step(self, nsteps=1):
+        """Three kernels per step, streaming folded into the next pull."""
+        self.use_physics()
+        _check(lib().ludwig_gb_lb2_step(self.lb.ptr, self.phi.ptr,
+                                        self.hydro.ptr, self.fe.ptr,
+                                        int(nsteps)), "ludwig_gb_lb2_step")
+
+    def state(self):
+        _, u, _ = self.hydro.get()
+        return {"f": self.lb.get(), "g": self.lb.get_g(),
+                "phi": self.phi.get(), "u": u}
+
+
 def sync():
     _check(lib().ludwig_gb_sync(), "ludwig_gb_sync")
+
+
+def advection_order(n):
+    """Order of the advective fluxes (1, 2, 3) of the per-function
+    Cahn-Hilliard and Beris-Edwards steps (src/advection.c:82)."""
+    _check(lib().advection_order_set(int(n)), "advection_order_set")
 
 
 def tune(xchunk, tile_y, min_blocks=0):
@@ -705,22 +801,25 @@ class FeLC(_Obj):
 
     def __init__(self, cs, q, dq, a0=0.01, gamma=3.0, kappa0=0.01,
                  kappa1=0.01, pitch=32.0, xi=0.7, redshift=1.0,
-                 amplitude=-0.2):
+                 amplitude=-0.2, q0=None):
         super().__init__()
         self.ptr = _new("fe_lc_create", cs.pe.ptr, cs.ptr, None, q.ptr,
                         dq.ptr)
         p = FeLcParam()
         p.a0, p.gamma, p.kappa0, p.kappa1 = a0, gamma, kappa0, kappa1
-        p.q0 = 2.0 * 3.1415926535897932385 / pitch
+        p.q0 = (2.0 * 3.1415926535897932385 / pitch) if q0 is None else q0
         p.xi, p.redshift, p.amplitude0, p.coswt = xi, redshift, amplitude, 1.0
         self.param = p
         self.dq = dq
         _check(lib().fe_lc_param_set(self.ptr, ctypes.byref(p)),
                "fe_lc_param_set")
 
-    def fed_total(self):
-        """Total free energy (FP64 fields): q gradients, then the sum."""
-        self.dq.compute()
+    def fed_total(self, recompute=True):
+        """Total free energy (FP64 fields).  recompute: take the gradients
+        of the current q first; otherwise use the stored ones (those of
+        the last step, as the reference's statistics do after a step)."""
+        if recompute:
+            self.dq.compute()
         out = ctypes.c_double()
         _check(lib().stats_free_energy_lc(self.ptr, ctypes.byref(out)),
                "stats_free_energy_lc")
@@ -908,8 +1007,10 @@ class Ensemble:
 def ensemble_config3(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
     """Config 3: boxes with edges drawn per axis from `edges`, viscosity
     U[0.02, 0.2], kappa U[0.02, 0.08], A = -B with |A| U[0.03, 0.1],
-    mobility min(0.45, 1/(12 (12 kappa - |A|))) (half the 7-point
-    stability bound), phi0 +-0.01 from per-box seeds."""
+    mobility min(0.45, 1/(12 (12 kappa + 2|A|))) (half the stability
+    bound of the explicit 7-point Cahn-Hilliard step in the saturated
+    phases, where the bulk free energy's curvature is 2|A|), phi0 +-0.01
+    from per-box seeds."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(nbox):
@@ -917,7 +1018,7 @@ def ensemble_config3(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
         eta = float(rng.uniform(0.02, 0.2))
         kappa = float(rng.uniform(0.02, 0.08))
         amag = float(rng.uniform(0.03, 0.1))
-        mob = min(0.45, 1.0 / (12.0 * (12.0 * kappa - amag)))
+        mob = min(0.45, 1.0 / (12.0 * (12.0 * kappa + 2.0 * amag)))
         out.append(box_param(n, eta=eta, a=-amag, b=amag, kappa=kappa,
                              mobility=mob, seed=1000 + 17 * k))
     return out

@@ -26,6 +26,7 @@ CU_SOURCES = [
     ("lgb_fused64.cu", ["--fmad=false"]),
     ("lgb_stats.cu", ["--fmad=false"]),
     ("lgb_lc64.cu", ["--fmad=false"]),
+    ("lgb_lb2.cu", ["--fmad=false"]),
     ("lgb_sk.cu", []),
     ("lgb_lc32.cu", []),
     ("lgb_fused32.cu", []),

@@ -127,11 +127,34 @@ __device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
  *****************************************************************************/
 
 template <typename T, bool SEQ, bool SHIFT, bool GZERO>
+__device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
+						     const double * rtau_ghost,
+						     T rho0, T fs[LGB_NVEL],
+						     const T force[3],
+						     const T (*sth)[3],
+						     T & rho_out, T u[3]);
+
+template <typename T, bool SEQ, bool SHIFT, bool GZERO>
 __device__ __forceinline__ void lgb_collide_site(T rtau, T rtau_bulk,
 						 const double * rtau_ghost,
 						 T rho0, T fs[LGB_NVEL],
 						 const T force[3], T & rho_out,
 						 T u[3]) {
+  lgb_collide_site_sth<T, SEQ, SHIFT, GZERO>(rtau, rtau_bulk, rtau_ghost,
+					     rho0, fs, force, nullptr,
+					     rho_out, u);
+}
+
+/* As lgb_collide_site; a non-null sth adds the thermodynamic stress to the
+ * equilibrium stress, seq = rho u u + sth (the two-distribution binary
+ * collision, src/collision.c:706-1013). */
+template <typename T, bool SEQ, bool SHIFT, bool GZERO>
+__device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
+						     const double * rtau_ghost,
+						     T rho0, T fs[LGB_NVEL],
+						     const T force[3],
+						     const T (*sth)[3],
+						     T & rho_out, T u[3]) {
   T mode[LGB_NVEL];
   constexpr int NM = GZERO ? 10 : LGB_NVEL;
 
@@ -157,7 +180,10 @@ __device__ __forceinline__ void lgb_collide_site(T rtau, T rtau_bulk,
   #pragma unroll
   for (int ia = 0; ia < 3; ia++) {
     #pragma unroll
-    for (int ib = 0; ib < 3; ib++) seq[ia][ib] = rho*u[ia]*u[ib];
+    for (int ib = 0; ib < 3; ib++) {
+      if (sth) seq[ia][ib] = rho*u[ia]*u[ib] + sth[ia][ib];
+      else     seq[ia][ib] = rho*u[ia]*u[ib];
+    }
     tr_s   += s[ia][ia];
     tr_seq += seq[ia][ia];
   }
@@ -195,6 +221,18 @@ __device__ __forceinline__ void lgb_collide_site(T rtau, T rtau_bulk,
 
   if (SEQ) d3q19_mode2f_seq<T, NM>(mode, fs);
   else     d3q19_mode2f_fast<T, NM>(mode, fs);
+
+  if (!SEQ) {
+    /* Reduced precision: the rounded mode -> f coefficients do not sum
+     * exactly to the conserved moments, and the stress modes (which carry
+     * rho u u, always positive) then leak mass with one sign every step.
+     * Rebuild the rest population from the conserved mode 0 instead, so
+     * that the population sum equals mode 0 up to unbiased rounding. */
+    T r = mode[0];
+    #pragma unroll
+    for (int p = 1; p < LGB_NVEL; p++) r -= fs[p];
+    fs[0] = r;
+  }
 
   rho_out = rho;
 }

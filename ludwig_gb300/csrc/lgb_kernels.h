@@ -52,6 +52,8 @@ enum lgbk_prec {
 /* Reference-semantics FP64 kernels (one per reference kernel) */
 int lgbk_grad7_f64(const lgbk_dims_t * d, int nf, const double * field,
 		   double * grad, double * delsq, void * stream);
+int lgbk_grad27_f64(const lgbk_dims_t * d, int nf, const double * field,
+		    double * grad, double * delsq, void * stream);
 int lgbk_symm_stress_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
 			 const double * phi, const double * grad,
 			 const double * delsq, double * pth, void * stream);
@@ -60,6 +62,9 @@ int lgbk_symm_mu_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
 		     void * stream);
 int lgbk_force_div_f64(const lgbk_dims_t * d, const double * pth,
 		       double * force, void * stream);
+int lgbk_advect_f64(const lgbk_dims_t * d, int order, int nf,
+		    const double * field, const double * u, double * fw,
+		    double * fe, double * fy, double * fz, void * stream);
 int lgbk_advect_upwind_f64(const lgbk_dims_t * d, int nf,
 			   const double * field, const double * u,
 			   double * fw, double * fe, double * fy, double * fz,
@@ -157,6 +162,19 @@ int lgbk_store_to_f64(const lgbk_dims_t * d, int prec, int ncomp,
 /* Streaming of reduced-precision distributions (dir as above) */
 int lgbk_propagate_store(const lgbk_dims_t * d, int prec, int dir,
 			 const void * f, void * fprime, void * stream);
+
+/* Two-distribution binary fluid (lgb_lb2.cu); pull = 1 when the stored
+ * arrays hold post-collision values awaiting streaming */
+int lgbk_phi_from_g_f64(const lgbk_dims_t * d, int pull, const double * g,
+			double * phi, void * stream);
+int lgbk_g_from_phi_f64(const lgbk_dims_t * d, const double * phi,
+			double * g, void * stream);
+int lgbk_collide_binary_f64(const lgbk_dims_t * d, const lgbk_symm_t * fe,
+			    const lgbk_collide_t * cp, double mobility,
+			    int pull, const double * f_in, const double * g_in,
+			    const double * phi, const double * grad,
+			    const double * delsq, double * f_out,
+			    double * g_out, double * u_out, void * stream);
 
 
 #ifdef __cplusplus

@@ -280,6 +280,99 @@ __global__ void k_fill(double * a, long long n, double v) {
   if (i < n) a[i] = v;
 }
 
+/* 2nd-order (centred) advective fluxes, src/advection.c:770-900, in the
+ * reference's operation order (the face mask is 1 on a periodic box) */
+__global__ void k_advect_2nd(lgbk_dims_t d, int nf,
+			     const double * __restrict__ fld,
+			     const double * __restrict__ u,
+			     double * __restrict__ fw, double * __restrict__ fe,
+			     double * __restrict__ fy, double * __restrict__ fz) {
+  long long i0 = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i0 >= d.nsites) return;
+  int x, y, z;
+  site_xyz(d, i0, x, y, z);
+  const long long N = d.nsites;
+  const double mask = 1.0;
+  long long i1 = lgb_site_w(d, x-1, y, z);
+  for (int n = 0; n < nf; n++) {
+    fw[n*N + i0] = 0.5*(u[i0] + u[i1])*mask*0.5*(fld[n*N + i1] + fld[n*N + i0]);
+  }
+  i1 = lgb_site_w(d, x+1, y, z);
+  for (int n = 0; n < nf; n++) {
+    fe[n*N + i0] = 0.5*(u[i0] + u[i1])*mask*0.5*(fld[n*N + i0] + fld[n*N + i1]);
+  }
+  i1 = lgb_site_w(d, x, y+1, z);
+  for (int n = 0; n < nf; n++) {
+    fy[n*N + i0] = 0.5*(u[N + i0] + u[N + i1])*mask*0.5
+      *(fld[n*N + i0] + fld[n*N + i1]);
+  }
+  i1 = lgb_site_w(d, x, y, z+1);
+  for (int n = 0; n < nf; n++) {
+    fz[n*N + i0] = 0.5*(u[2*N + i0] + u[2*N + i1])*mask*0.5
+      *(fld[n*N + i0] + fld[n*N + i1]);
+  }
+}
+
+/* 3rd-order upwind-biased fluxes, src/advection.c:946-1135: the face value
+ * a1 f(two upwind) + a2 f(upwind) + a3 f(downwind) */
+__global__ void k_advect_3rd(lgbk_dims_t d, int nf,
+			     const double * __restrict__ fld,
+			     const double * __restrict__ u,
+			     double * __restrict__ fw, double * __restrict__ fe,
+			     double * __restrict__ fy, double * __restrict__ fz) {
+  long long i0 = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i0 >= d.nsites) return;
+  int x, y, z;
+  site_xyz(d, i0, x, y, z);
+  const long long N = d.nsites;
+  const double a1 = -0.213933, a2 = 0.927865, a3 = 0.286067;
+  const double mask = 1.0;
+  {
+    const long long m2 = lgb_site_w(d, x-2, y, z), m1 = lgb_site_w(d, x-1, y, z);
+    const long long p1 = lgb_site_w(d, x+1, y, z), p2 = lgb_site_w(d, x+2, y, z);
+    double uf = 0.5*mask*(u[i0] + u[m1]);
+    for (int n = 0; n < nf; n++) {
+      const double * f = fld + n*N;
+      double d1, d2, d3;
+      if (uf > 0.0) { d1 = f[m2]; d2 = f[m1]; d3 = f[i0]; }
+      else          { d1 = f[p1]; d2 = f[i0]; d3 = f[m1]; }
+      fw[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+    }
+    uf = 0.5*mask*(u[i0] + u[p1]);
+    for (int n = 0; n < nf; n++) {
+      const double * f = fld + n*N;
+      double d1, d2, d3;
+      if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+      else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+      fe[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+    }
+  }
+  {
+    const long long m1 = lgb_site_w(d, x, y-1, z), p1 = lgb_site_w(d, x, y+1, z);
+    const long long p2 = lgb_site_w(d, x, y+2, z);
+    const double uf = 0.5*mask*(u[N + i0] + u[N + p1]);
+    for (int n = 0; n < nf; n++) {
+      const double * f = fld + n*N;
+      double d1, d2, d3;
+      if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+      else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+      fy[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+    }
+  }
+  {
+    const long long m1 = lgb_site_w(d, x, y, z-1), p1 = lgb_site_w(d, x, y, z+1);
+    const long long p2 = lgb_site_w(d, x, y, z+2);
+    const double uf = 0.5*mask*(u[2*N + i0] + u[2*N + p1]);
+    for (int n = 0; n < nf; n++) {
+      const double * f = fld + n*N;
+      double d1, d2, d3;
+      if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+      else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+      fz[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+    }
+  }
+}
+
 /*****************************************************************************
  *
  *  Launchers
@@ -289,6 +382,74 @@ __global__ void k_fill(double * a, long long n, double v) {
 #define LAUNCH_RET return (int) cudaGetLastError()
 
 extern "C" {
+
+/* 27-point gradient and Laplacian (src/gradient_3d_27pt_fluid.c:219-362):
+ * (0.5/9) times the sum over the nine neighbour pairs of the +1 / -1
+ * planes, and (1/9)(sum of the 26 neighbours - 26 f), in the reference's
+ * order of terms. */
+__global__ void k_grad27(lgbk_dims_t d, int nf, const double * __restrict__ fld,
+			 double * __restrict__ grad,
+			 double * __restrict__ delsq) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i >= d.nsites) return;
+  int x, y, z;
+  site_xyz(d, i, x, y, z);
+  const long long N = d.nsites;
+  const double r9 = (1.0/9.0);
+  long long nb[3][3][3];
+  #pragma unroll
+  for (int a = 0; a < 3; a++)
+    #pragma unroll
+    for (int b = 0; b < 3; b++)
+      #pragma unroll
+      for (int c = 0; c < 3; c++)
+	nb[a][b][c] = lgb_site_w(d, x + a - 1, y + b - 1, z + c - 1);
+  for (int n = 0; n < nf; n++) {
+    const double * fn = fld + n*N;
+    double sx = 0.0, sy = 0.0, sz = 0.0, sl = 0.0;
+    #pragma unroll
+    for (int a = 0; a < 3; a++) {
+      #pragma unroll
+      for (int b = 0; b < 3; b++) {
+	if (a == 0 && b == 0) sx = +fn[nb[2][a][b]];
+	else sx = sx + fn[nb[2][a][b]];
+	sx = sx - fn[nb[0][a][b]];
+	if (a == 0 && b == 0) sy = +fn[nb[a][2][b]];
+	else sy = sy + fn[nb[a][2][b]];
+	sy = sy - fn[nb[a][0][b]];
+	if (a == 0 && b == 0) sz = +fn[nb[a][b][2]];
+	else sz = sz + fn[nb[a][b][2]];
+	sz = sz - fn[nb[a][b][0]];
+      }
+    }
+    bool first = true;
+    #pragma unroll
+    for (int a = 0; a < 3; a++) {
+      #pragma unroll
+      for (int b = 0; b < 3; b++) {
+	#pragma unroll
+	for (int c = 0; c < 3; c++) {
+	  if (a == 1 && b == 1 && c == 1) continue;
+	  if (first) sl = +fn[nb[a][b][c]];
+	  else sl = sl + fn[nb[a][b][c]];
+	  first = false;
+	}
+      }
+    }
+    sl = sl - 26.0*fn[i];
+    grad[(3*n + 0)*N + i] = 0.5*r9*sx;
+    grad[(3*n + 1)*N + i] = 0.5*r9*sy;
+    grad[(3*n + 2)*N + i] = 0.5*r9*sz;
+    delsq[n*N + i] = r9*sl;
+  }
+}
+
+int lgbk_grad27_f64(const lgbk_dims_t * d, int nf, const double * field,
+		    double * grad, double * delsq, void * stream) {
+  k_grad27<<<grid_for(d->nsites), LGB_TPB, 0, (cudaStream_t) stream>>>(
+    *d, nf, field, grad, delsq);
+  return (int) cudaGetLastError();
+}
 
 int lgbk_grad7_f64(const lgbk_dims_t * d, int nf, const double * field,
 		   double * grad, double * delsq, void * stream) {
@@ -317,6 +478,26 @@ int lgbk_force_div_f64(const lgbk_dims_t * d, const double * pth,
 		       double * force, void * stream) {
   k_force_div<<<grid_for(d->nsites), LGB_TPB, 0, (cudaStream_t) stream>>>(
     *d, pth, force);
+  LAUNCH_RET;
+}
+
+/* order 1 (upwind), 2 (centred) or 3 (upwind-biased) */
+int lgbk_advect_f64(const lgbk_dims_t * d, int order, int nf,
+		    const double * field, const double * u, double * fw,
+		    double * fe, double * fy, double * fz, void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  if (order == 2) {
+    k_advect_2nd<<<grid_for(d->nsites), LGB_TPB, 0, s>>>(*d, nf, field, u,
+							 fw, fe, fy, fz);
+  }
+  else if (order == 3) {
+    k_advect_3rd<<<grid_for(d->nsites), LGB_TPB, 0, s>>>(*d, nf, field, u,
+							 fw, fe, fy, fz);
+  }
+  else {
+    k_advect_upwind<<<grid_for(d->nsites), LGB_TPB, 0, s>>>(*d, nf, field, u,
+							    fw, fe, fy, fz);
+  }
   LAUNCH_RET;
 }
 

@@ -201,6 +201,29 @@ __global__ void k_symm_fed(lgbk_dims_t d, lgbk_symm_t fe,
   if (threadIdx.x == 0) write_partial<1>(part, k, vmin, vmax);
 }
 
+/* As k_symm_fed with stored gradients (any stencil): FP64 fields */
+__global__ void k_symm_fed_g(lgbk_dims_t d, lgbk_symm_t fe,
+			     const double * __restrict__ phi,
+			     const double * __restrict__ grad,
+			     double * __restrict__ part) {
+  Klein k[1];
+  k[0].zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  const long long N = d.nsites;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+       i < N; i += (long long) gridDim.x*blockDim.x) {
+    const double g[3] = {grad[i], grad[N + i], grad[2*N + i]};
+    const double p = phi[i];
+    double fed = (0.5*fe.a + 0.25*fe.b*p*p)*p*p
+      + 0.5*fe.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
+    k[0].add(fed);
+    vmin = fmin(vmin, fed);
+    vmax = fmax(vmax, fed);
+  }
+  block_reduce<1>(k, vmin, vmax);
+  if (threadIdx.x == 0) write_partial<1>(part, k, vmin, vmax);
+}
+
 #define RED_TPB 256
 
 static int finish(int nk, double * scratch, double * out_host,
@@ -255,6 +278,19 @@ extern "C" int lgbk_dist_moments(const lgbk_dims_t * d, int prec,
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
   return finish(4, scratch, out_host, s);
+}
+
+extern "C" int lgbk_symm_fed_total_grad(const lgbk_dims_t * d,
+					const lgbk_symm_t * fe,
+					const double * phi,
+					const double * grad, double * scratch,
+					double out_host[3], void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  k_symm_fed_g<<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(*d, *fe, phi, grad,
+						   scratch);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return finish(1, scratch, out_host, s);
 }
 
 extern "C" int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,

@@ -30,6 +30,11 @@ int lgbk_dist_moments(const lgbk_dims_t * d, int prec, const void * f,
 		      double scale, double * scratch, double out_host[6],
 		      void * stream);
 /* out = {total free energy, min, max} */
+/* the same from stored FP64 gradients (grad: 3 x nsites) */
+int lgbk_symm_fed_total_grad(const lgbk_dims_t * d, const lgbk_symm_t * fe,
+			     const double * phi, const double * grad,
+			     double * scratch, double out_host[3],
+			     void * stream);
 int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,
 			const lgbk_symm_t * fe, const void * phi,
 			double * scratch, double out_host[3], void * stream);

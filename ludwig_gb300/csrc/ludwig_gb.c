@@ -72,6 +72,17 @@ static double * red_scratch_ = NULL;
 static int tune_xchunk_ = 16;
 static int tune_ty_ = 8;
 static int tune_minb_ = 3;
+static int advection_order_ = 1;
+
+/* src/advection.c:82: order of the advective fluxes of the per-function
+ * Cahn-Hilliard and Beris-Edwards steps: 1 (upwind, the default), 2 or 3.
+ * The fused steps use order 1 and reject the others. */
+int advection_order_set(int n) {
+  if (n < 1 || n > 3) return err_set(LUDWIG_GB_EINVAL, "advection order "
+				     "1, 2 or 3");
+  advection_order_ = n;
+  return LUDWIG_GB_OK;
+}
 
 static int lib_init(void) {
   if (stream_ == NULL) {
@@ -273,6 +284,9 @@ struct lb_data_s {
   void * f;
   void * fprime;
   int pending;                 /* stored values await streaming */
+  int ndist;                   /* 1, or 2 with the order parameter in g */
+  void * g;                    /* ndist = 2: g and its second buffer */
+  void * gprime;
 };
 
 lb_data_options_t lb_data_options_default(void) {
@@ -287,8 +301,11 @@ int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
   if (cs == NULL || !cs->initialised || plb == NULL) {
     return err_set(LUDWIG_GB_EINVAL, "lb_data_create: cs not initialised");
   }
-  if (o.ndim != 3 || o.nvel != 19 || o.ndist != 1) {
-    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: D3Q19, ndist 1 only");
+  if (o.ndim != 3 || o.nvel != 19 || (o.ndist != 1 && o.ndist != 2)) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: D3Q19, ndist 1 or 2");
+  }
+  if (o.ndist == 2 && o.precision != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: ndist 2 is FP64");
   }
   if (o.precision < LUDWIG_GB_FP64 || o.precision > LUDWIG_GB_FP16) {
     return err_set(LUDWIG_GB_EINVAL, "lb_data_create: precision");
@@ -305,10 +322,22 @@ int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
   lb->rho0 = phys_ref_ ? phys_ref_->rho0 : 1.0;
 
   size_t bytes = NVEL*(size_t) cs->d.nsites*prec_size(lb->prec);
+  lb->ndist = o.ndist;
   if ((rc = dev_alloc(&lb->f, bytes, "f")) ||
       (rc = dev_alloc(&lb->fprime, bytes, "fprime"))) {
     lb_free(lb);
     return rc;
+  }
+  if (lb->ndist == 2) {
+    if ((rc = dev_alloc(&lb->g, bytes, "g")) ||
+	(rc = dev_alloc(&lb->gprime, bytes, "gprime"))) {
+      lb_free(lb);
+      return rc;
+    }
+    if (cudaMemsetAsync(lb->g, 0, bytes, stream_) != cudaSuccess) {
+      lb_free(lb);
+      return err_set(LUDWIG_GB_ECUDA, "lb_data_create: memset g");
+    }
   }
   *plb = lb;
   return lb_init_rest_f(lb, lb->rho0);
@@ -318,6 +347,8 @@ int lb_free(lb_t * lb) {
   if (lb) {
     dev_free(lb->f);
     dev_free(lb->fprime);
+    dev_free(lb->g);
+    dev_free(lb->gprime);
     free(lb);
   }
   return LUDWIG_GB_OK;
@@ -327,22 +358,37 @@ static void lb_swap(lb_t * lb) {
   void * t = lb->f; lb->f = lb->fprime; lb->fprime = t;
 }
 
-/* Make the stored array hold the reference's f (apply pending streaming) */
+static void lb_swap_g(lb_t * lb) {
+  void * t = lb->g; lb->g = lb->gprime; lb->gprime = t;
+}
+
+/* Make the stored arrays hold the reference's f (and g) (apply pending
+ * streaming) */
 static int lb_materialise(lb_t * lb) {
   if (!lb->pending) return LUDWIG_GB_OK;
   CK(lgbk_propagate_store(&lb->cs->d, lb->prec, +1, lb->f, lb->fprime,
 			  stream_), "propagate");
   lb_swap(lb);
+  if (lb->ndist == 2) {
+    CK(lgbk_propagate_store(&lb->cs->d, lb->prec, +1, lb->g, lb->gprime,
+			    stream_), "propagate g");
+    lb_swap_g(lb);
+  }
   lb->pending = 0;
   return LUDWIG_GB_OK;
 }
 
-/* Make the stored array hold post-collision values (pending = 1) */
+/* Make the stored arrays hold post-collision values (pending = 1) */
 static int lb_unstream(lb_t * lb) {
   if (lb->pending) return LUDWIG_GB_OK;
   CK(lgbk_propagate_store(&lb->cs->d, lb->prec, -1, lb->f, lb->fprime,
 			  stream_), "unstream");
   lb_swap(lb);
+  if (lb->ndist == 2) {
+    CK(lgbk_propagate_store(&lb->cs->d, lb->prec, -1, lb->g, lb->gprime,
+			    stream_), "unstream g");
+    lb_swap_g(lb);
+  }
   lb->pending = 1;
   return LUDWIG_GB_OK;
 }
@@ -409,6 +455,10 @@ int lb_f_to_host(lb_t * lb, double * fh) {
 
 int lb_f_from_host(lb_t * lb, const double * fh) {
   if (lb == NULL || fh == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_f");
+  if (lb->ndist == 2) {
+    int rc0 = lb_materialise(lb);        /* g keeps its streamed values */
+    if (rc0) return rc0;
+  }
   const lgbk_dims_t * d = &lb->cs->d;
   size_t n = NVEL*(size_t) d->nsites;
   if (lb->prec == LUDWIG_GB_FP64) {
@@ -554,6 +604,37 @@ static unsigned int kiss(unsigned int s[4]) {
   return (s[1] + (s[0] ^ b));
 }
 
+/* src/field_phi_init.c:38-82: a drop phi(r) = phistar tanh((r - radius)/xi)
+ * about the centre of the box (is_centred adds Lmin = 0.5, as the
+ * reference's corrected form); sites at integer positions 1..L. */
+int field_phi_init_drop(field_t * phi, double xi, double radius,
+			double phistar, int is_centred) {
+  if (phi == NULL || phi->nf != 1 || !(xi > 0.0)) {
+    return err_set(LUDWIG_GB_EINVAL, "field_phi_init_drop");
+  }
+  const lgbk_dims_t * d = &phi->cs->d;
+  double * h = (double *) malloc((size_t) d->nsites*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "field_phi_init_drop");
+  const double lmin = 0.5;
+  const double rxi0 = 1.0/xi;
+  double centre[3];
+  const int n[3] = {d->nx, d->ny, d->nz};
+  for (int a = 0; a < 3; a++) centre[a] = is_centred*lmin + 0.5*n[a];
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	double pos[3] = {1.0*(x + 1) - centre[0], 1.0*(y + 1) - centre[1],
+			 1.0*(z + 1) - centre[2]};
+	double r = sqrt(pos[0]*pos[0] + pos[1]*pos[1] + pos[2]*pos[2]);
+	h[((size_t) x*d->ny + y)*d->nz + z] = phistar*tanh(rxi0*(r - radius));
+      }
+    }
+  }
+  int rc = field_from_host(phi, h);
+  free(h);
+  return rc;
+}
+
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
   if (phi == NULL || phi->nf != 1) {
     return err_set(LUDWIG_GB_EINVAL, "field_phi_init_spinodal: scalar field");
@@ -584,6 +665,7 @@ int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
 struct field_grad_s {
   field_t * field;
   int level;
+  int stencil;                 /* 7 (3d_7pt_fluid) or 27 (3d_27pt_fluid) */
   double * grad;
   double * delsq;
 };
@@ -597,6 +679,7 @@ int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p) {
   if (g == NULL) return err_set(LUDWIG_GB_ENOMEM, "field_grad_create");
   g->field = f;
   g->level = level;
+  g->stencil = 7;
   *p = g;
   return LUDWIG_GB_OK;
 }
@@ -614,6 +697,28 @@ static int grad_alloc(field_grad_t * g) {
   return rc;
 }
 
+/* The reference selects the stencil with field_grad_set(fg,
+ * grad_3d_7pt_fluid_d2 | grad_3d_27pt_fluid_d2, NULL) (src/field_grad.c);
+ * here by its number of points. */
+int field_grad_stencil_set(field_grad_t * g, int npoints) {
+  if (g == NULL || (npoints != 7 && npoints != 27)) {
+    return err_set(LUDWIG_GB_EINVAL, "field_grad_stencil_set: 7 or 27");
+  }
+  g->stencil = npoints;
+  return LUDWIG_GB_OK;
+}
+
+static int grad_launch(field_grad_t * g) {
+  if (g->stencil == 27) {
+    return lgbk_grad27_f64(&g->field->cs->d, g->field->nf,
+			   (const double *) g->field->data, g->grad, g->delsq,
+			   stream_);
+  }
+  return lgbk_grad7_f64(&g->field->cs->d, g->field->nf,
+			(const double *) g->field->data, g->grad, g->delsq,
+			stream_);
+}
+
 int field_grad_compute(field_grad_t * g) {
   if (g == NULL) return err_set(LUDWIG_GB_EINVAL, "field_grad_compute");
   if (g->field->prec != LUDWIG_GB_FP64) {
@@ -621,9 +726,7 @@ int field_grad_compute(field_grad_t * g) {
   }
   int rc = grad_alloc(g);
   if (rc) return rc;
-  CK(lgbk_grad7_f64(&g->field->cs->d, g->field->nf,
-		    (const double *) g->field->data, g->grad, g->delsq,
-		    stream_), "grad7");
+  CK(grad_launch(g), "field_grad_compute");
   CK(cudaStreamSynchronize(stream_), "sync");
   return LUDWIG_GB_OK;
 }
@@ -1321,7 +1424,7 @@ int beris_edw_update(beris_edw_t * be, fe_t * fe, field_t * fq,
   if (hydro) {
     double * fw = be->flux, * fe_ = fw + N5, * fy = fw + 2*N5;
     double * fz = fw + 3*N5;
-    CK(lgbk_advect_upwind_f64(d, 5, (const double *) fq->data,
+    CK(lgbk_advect_f64(d, advection_order_, 5, (const double *) fq->data,
 			      (const double *) hydro->u, fw, fe_, fy, fz,
 			      stream_), "advect");
     CK(lgbk_flux_no_normal_f64(d, 5, map_dev(map), fw, fe_, fy, fz, stream_),
@@ -1387,6 +1490,14 @@ static int lc_step_async(lb_t * lb, field_t * q, hydro_t * hydro,
 		   "FP64 or all reduced precision");
   }
   fe_lc_t * lc = (fe_lc_t *) fe;
+  if (lc->dq && lc->dq->stencil != 7) {
+    return err_set(LUDWIG_GB_EINVAL, "lc_step: the fused step uses "
+		   "7-point gradients");
+  }
+  if (advection_order_ != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "lc_step: the fused step uses "
+		   "first-order advection");
+  }
   lgbk_lc_t k;
   lc_kparam(lc, &k);
   lgbk_lc_step_args_t a;
@@ -1487,7 +1598,7 @@ int phi_cahn_hilliard(phi_ch_t * pch, fe_t * fe, field_t * phi,
 
   double * fw = pch->flux, * fe_ = fw + N, * fy = fw + 2*N, * fz = fw + 3*N;
   if (hydro) {
-    CK(lgbk_advect_upwind_f64(d, 1, (const double *) phi->data,
+    CK(lgbk_advect_f64(d, advection_order_, 1, (const double *) phi->data,
 			      (const double *) hydro->u, fw, fe_, fy, fz,
 			      stream_), "advect");
   }
@@ -1544,6 +1655,130 @@ static int collide_param(lb_t * lb, lgbk_collide_t * cp) {
   return LUDWIG_GB_OK;
 }
 
+/*****************************************************************************
+ *  Two-distribution binary fluid (symmetric_lb, ndist = 2)
+ *****************************************************************************/
+
+/* lb_collision_binary (src/collision.c:604-1013): needs the symmetric free
+ * energy and the gradients of phi (field_grad_compute) of this step.  The
+ * reference applies it at every site (no status test); so does this. */
+static int lb_collide_binary(lb_t * lb, hydro_t * hydro, map_t * map,
+			     fe_t * fe, const lgbk_collide_t * cp) {
+  (void) map;
+  fe_symm_t * s = NULL;
+  physics_t * ph = NULL;
+  int rc = fe_symm_get(fe, &s);
+  if (rc == 0) rc = phys_get(&ph);
+  if (rc) return rc;
+  if (s->dphi == NULL || s->dphi->grad == NULL) {
+    return err_set(LUDWIG_GB_ESTATE, "binary collision: call "
+		   "field_grad_compute() on phi first");
+  }
+  if (s->phi->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "binary collision: FP64 phi");
+  }
+  lgbk_symm_t sp = {s->param.a, s->param.b, s->param.kappa};
+  CK(lgbk_collide_binary_f64(&lb->cs->d, &sp, cp, ph->mobility, lb->pending,
+			     (const double *) lb->f, (const double *) lb->g,
+			     (const double *) s->phi->data, s->dphi->grad,
+			     s->dphi->delsq, (double *) lb->fprime,
+			     (double *) lb->gprime, (double *) hydro->u,
+			     stream_), "collide binary");
+  lb_swap(lb);
+  lb_swap_g(lb);
+  lb->pending = 0;                 /* the stored arrays are post-collision */
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* src/phi_lb_coupler.c:49: phi = sum_p g_p */
+int phi_lb_to_field(field_t * phi, lb_t * lb) {
+  if (phi == NULL || lb == NULL || lb->ndist != 2 || phi->nf != 1 ||
+      phi->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_lb_to_field: ndist 2, FP64 phi");
+  }
+  CK(lgbk_phi_from_g_f64(&lb->cs->d, lb->pending, (const double *) lb->g,
+			 (double *) phi->data, stream_), "phi_from_g");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* src/phi_lb_coupler.c:107: g_0 = phi, the other g_p = 0 */
+int phi_lb_from_field(field_t * phi, lb_t * lb) {
+  if (phi == NULL || lb == NULL || lb->ndist != 2 || phi->nf != 1 ||
+      phi->prec != LUDWIG_GB_FP64) {
+    return err_set(LUDWIG_GB_EINVAL, "phi_lb_from_field: ndist 2, FP64 phi");
+  }
+  int rc = lb_materialise(lb);
+  if (rc) return rc;
+  CK(lgbk_g_from_phi_f64(&lb->cs->d, (const double *) phi->data,
+			 (double *) lb->g, stream_), "g_from_phi");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* The reference's g (19 x nsites) */
+int lb_g_to_host(lb_t * lb, double * gh) {
+  if (lb == NULL || gh == NULL || lb->ndist != 2) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_g_to_host: ndist 2");
+  }
+  int rc = lb_materialise(lb);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(gh, lb->g, NVEL*(size_t) lb->cs->d.nsites*sizeof(double),
+		     cudaMemcpyDeviceToHost, stream_), "lb_g_to_host");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+int lb_g_from_host(lb_t * lb, const double * gh) {
+  if (lb == NULL || gh == NULL || lb->ndist != 2) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_g_from_host: ndist 2");
+  }
+  int rc = lb_materialise(lb);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(lb->g, gh, NVEL*(size_t) lb->cs->d.nsites*sizeof(double),
+		     cudaMemcpyHostToDevice, stream_), "lb_g_from_host");
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
+/* nsteps of the main loop with ndist = 2 (src/ludwig.c:528-860):
+ * phi_lb_to_field, field_grad_compute, lb_collide (binary), lb_propagation;
+ * three kernels per step, streaming folded into the next pull. */
+int ludwig_gb_lb2_step(lb_t * lb, field_t * phi, hydro_t * hydro, fe_t * fe,
+		       int nsteps) {
+  fe_symm_t * s = NULL;
+  physics_t * ph = NULL;
+  int rc = fe_symm_get(fe, &s);
+  if (rc == 0) rc = phys_get(&ph);
+  if (rc) return rc;
+  if (lb == NULL || phi == NULL || hydro == NULL || lb->ndist != 2 ||
+      s->phi != phi || s->dphi == NULL || nsteps < 0) {
+    return err_set(LUDWIG_GB_EINVAL, "lb2_step: ndist 2 lb, phi of fe");
+  }
+  lgbk_collide_t cp;
+  if ((rc = collide_param(lb, &cp))) return rc;
+  if ((rc = grad_alloc(s->dphi))) return rc;
+  lgbk_symm_t sp = {s->param.a, s->param.b, s->param.kappa};
+  const lgbk_dims_t * d = &lb->cs->d;
+  for (int n = 0; n < nsteps; n++) {
+    CK(lgbk_phi_from_g_f64(d, lb->pending, (const double *) lb->g,
+			   (double *) phi->data, stream_), "phi_from_g");
+    CK(grad_launch(s->dphi), "field_grad_compute");
+    CK(lgbk_collide_binary_f64(d, &sp, &cp, ph->mobility, lb->pending,
+			       (const double *) lb->f, (const double *) lb->g,
+			       (const double *) phi->data, s->dphi->grad,
+			       s->dphi->delsq, (double *) lb->fprime,
+			       (double *) lb->gprime, (double *) hydro->u,
+			       stream_), "collide binary");
+    lb_swap(lb);
+    lb_swap_g(lb);
+    lb->pending = 1;                    /* lb_propagation */
+  }
+  CK(cudaStreamSynchronize(stream_), "sync");
+  return LUDWIG_GB_OK;
+}
+
 int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
 	       fe_t * fe, visc_t * visc) {
   (void) fe;
@@ -1558,6 +1793,7 @@ int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
   lgbk_collide_t cp;
   int rc = collide_param(lb, &cp);
   if (rc) return rc;
+  if (lb->ndist == 2) return lb_collide_binary(lb, hydro, map, fe, &cp);
   if ((rc = lb_materialise(lb))) return rc;
   CK(lgbk_collide_f64(&lb->cs->d, &cp, map_dev(map), (double *) lb->f,
 		      (const double *) hydro->force, (double *) hydro->rho,
@@ -1609,6 +1845,14 @@ static int binary_args(lb_t * lb, field_t * phi, hydro_t * hydro,
   if (lb->cs->d.nsites != phi->cs->d.nsites ||
       lb->cs->d.nsites != hydro->cs->d.nsites) {
     return err_set(LUDWIG_GB_EINVAL, "binary_step: lattice mismatch");
+  }
+  if (s->dphi && s->dphi->stencil != 7) {
+    return err_set(LUDWIG_GB_EINVAL, "binary_step: the fused step uses "
+		   "7-point gradients (call the per-function path for 27)");
+  }
+  if (advection_order_ != 1) {
+    return err_set(LUDWIG_GB_EINVAL, "binary_step: the fused step uses "
+		   "first-order advection");
   }
   memset(a, 0, sizeof(*a));
   if ((rc = collide_param(lb, &a->cp))) return rc;
@@ -1772,8 +2016,21 @@ int stats_free_energy_symm(fe_symm_t * fe, double * total) {
   int rc = red_scratch(&scr);
   if (rc) return rc;
   lgbk_symm_t sp = {fe->param.a, fe->param.b, fe->param.kappa};
-  CK(lgbk_symm_fed_total(&fe->phi->cs->d, field_kprec(fe->phi->prec), &sp,
-			 fe->phi->data, scr, r, stream_), "fed");
+  if (fe->dphi && fe->dphi->stencil != 7) {
+    /* the stored gradients of the last field_grad_compute, as the
+     * reference's fe_symm_fed (src/symmetric.c:285) reads them */
+    if (fe->dphi->grad == NULL || fe->phi->prec != LUDWIG_GB_FP64) {
+      return err_set(LUDWIG_GB_ESTATE, "stats_free_energy_symm: call "
+		     "field_grad_compute() first");
+    }
+    CK(lgbk_symm_fed_total_grad(&fe->phi->cs->d, &sp,
+				(const double *) fe->phi->data,
+				fe->dphi->grad, scr, r, stream_), "fed");
+  }
+  else {
+    CK(lgbk_symm_fed_total(&fe->phi->cs->d, field_kprec(fe->phi->prec), &sp,
+			   fe->phi->data, scr, r, stream_), "fed");
+  }
   *total = r[0];
   return LUDWIG_GB_OK;
 }

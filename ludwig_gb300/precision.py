@@ -130,6 +130,10 @@ def main(argv=None):
     ap.add_argument("--out", default=None)
     ap.add_argument("--eta", type=float, default=PARAMS["eta"],
                     help="shear viscosity (binary fluid)")
+    ap.add_argument("--mobility", type=float, default=PARAMS["mobility"],
+                    help="mobility (binary fluid); the explicit 7-point "
+                    "Cahn-Hilliard step needs M < 2/(12(2|A| + 12 kappa)) "
+                    "once the domains saturate")
     ap.add_argument("--lc", action="store_true",
                     help="the cholesteric LC (FP64 vs FP32) instead")
     args = ap.parse_args(argv)
@@ -139,7 +143,7 @@ def main(argv=None):
         res = {"model": "cholesteric LC", "size": args.size,
                "steps": args.steps, "params": LC_PARAMS, "records": recs}
     else:
-        params = dict(PARAMS, eta=args.eta)
+        params = dict(PARAMS, eta=args.eta, mobility=args.mobility)
         recs = run(args.size, args.steps, args.every, params=params)
         res = {"size": args.size, "steps": args.steps, "params": params,
                "seed": SEED, "records": recs}

@@ -172,6 +172,18 @@ def grad_7pt(L, field):
     return grad, delsq
 
 
+def grad_27pt(L, field):
+    """src/gradient_3d_27pt_fluid.c:219-362 (fluid sites only)."""
+    field = np.ascontiguousarray(field, dtype=np.float64)
+    nf = field.shape[0]
+    grad = np.zeros((3 * nf,) + tuple(L))
+    delsq = np.zeros((nf,) + tuple(L))
+    Lb = lib()
+    Lb.orc_grad_27pt.argtypes = [_I3, ctypes.c_int, _P, _P, _P]
+    Lb.orc_grad_27pt(_dims(L), nf, _p(field), _p(grad), _p(delsq))
+    return grad, delsq
+
+
 def symm_stress(L, fe, phi, grad, delsq):
     pth = np.zeros((9,) + tuple(L))
     lib().orc_symm_stress(_dims(L), ctypes.byref(fe), _p(phi), _p(grad),

@@ -286,6 +286,80 @@ void orc_grad_7pt(const int L[3], int nf, const double * field,
  *
  *****************************************************************************/
 
+/*****************************************************************************
+ *
+ *  orc_grad_27pt
+ *
+ *  src/gradient_3d_27pt_fluid.c:219-362 (grad_3d_27pt_kernel, del^2):
+ *  each gradient component is (0.5/9) times the sum over the nine
+ *  neighbour pairs of the +1 and -1 planes, in the reference's order, and
+ *  del^2 is (1/9)(sum of the 26 neighbours - 26 phi).
+ *
+ *****************************************************************************/
+
+void orc_grad_27pt(const int L[3], int nf, const double * field,
+		   double * grad, double * delsq) {
+  size_t N = nsites(L);
+  const double r9 = (1.0/9.0);
+  #pragma omp parallel for
+  for (int x = 0; x < L[0]; x++) {
+    for (int y = 0; y < L[1]; y++) {
+      for (int z = 0; z < L[2]; z++) {
+	size_t i = site(L, x, y, z);
+	for (int n = 0; n < nf; n++) {
+	  const double * fn = field + (size_t) n*N;
+#define F(dx, dy, dz) fn[site(L, x + (dx), y + (dy), z + (dz))]
+	  double sx = 0.0, sy = 0.0, sz = 0.0, sl = 0.0;
+	  int first = 1;
+	  for (int a = -1; a <= 1; a++) {
+	    for (int b = -1; b <= 1; b++) {
+	      if (first) sx = +F(1, a, b);
+	      else sx = sx + F(1, a, b);
+	      sx = sx - F(-1, a, b);
+	      first = 0;
+	    }
+	  }
+	  first = 1;
+	  for (int a = -1; a <= 1; a++) {
+	    for (int b = -1; b <= 1; b++) {
+	      if (first) sy = +F(a, 1, b);
+	      else sy = sy + F(a, 1, b);
+	      sy = sy - F(a, -1, b);
+	      first = 0;
+	    }
+	  }
+	  first = 1;
+	  for (int a = -1; a <= 1; a++) {
+	    for (int b = -1; b <= 1; b++) {
+	      if (first) sz = +F(a, b, 1);
+	      else sz = sz + F(a, b, 1);
+	      sz = sz - F(a, b, -1);
+	      first = 0;
+	    }
+	  }
+	  first = 1;
+	  for (int a = -1; a <= 1; a++) {
+	    for (int b = -1; b <= 1; b++) {
+	      for (int c = -1; c <= 1; c++) {
+		if (a == 0 && b == 0 && c == 0) continue;
+		if (first) sl = +F(a, b, c);
+		else sl = sl + F(a, b, c);
+		first = 0;
+	      }
+	    }
+	  }
+	  sl = sl - 26.0*F(0, 0, 0);
+#undef F
+	  grad[(3*n + 0)*N + i] = 0.5*r9*sx;
+	  grad[(3*n + 1)*N + i] = 0.5*r9*sy;
+	  grad[(3*n + 2)*N + i] = 0.5*r9*sz;
+	  delsq[n*N + i] = r9*sl;
+	}
+      }
+    }
+  }
+}
+
 static inline double symm_mu_site(const orc_symm_param_t * fe, double phi,
 				  double delsq) {
   return fe->a*phi + fe->b*phi*phi*phi - fe->kappa*delsq;
@@ -408,6 +482,138 @@ void orc_advect_upwind(const int L[3], int nf, const double * field,
       }
     }
   }
+}
+
+/*****************************************************************************
+ *
+ *  orc_advect_2nd: centred fluxes, src/advection.c:770-900
+ *  (advection_2nd_kernel_v): face velocity 0.5 (u0 + u1), flux
+ *  ((0.5 (u0 + u1)) 1) 0.5 (phi_a + phi_b), west face (phi(x-1) + phi(x)),
+ *  the others (phi(x) + phi(x+1)).
+ *
+ *  orc_advect_3rd: three-point upwind-biased fluxes, src/advection.c:
+ *  946-1135 (advection_le_3rd_kernel_v): u_face = (0.5 1)(u0 + u1),
+ *  flux = u_face (a1 fd1 + a2 fd2 + a3 fd3) with a1 = -0.213933,
+ *  a2 = 0.927865, a3 = 0.286067 and fd1..3 the values two sites upwind,
+ *  one upwind and one downwind of the face.
+ *
+ *****************************************************************************/
+
+void orc_advect_2nd(const int L[3], int nf, const double * field,
+		    const double * u, double * fw, double * fe,
+		    double * fy, double * fz) {
+  size_t N = nsites(L);
+  #pragma omp parallel for
+  for (int x = 0; x < L[0]; x++) {
+    for (int y = 0; y < L[1]; y++) {
+      for (int z = 0; z < L[2]; z++) {
+	size_t i0 = site(L, x, y, z), i1;
+	const double mask = 1.0;
+	i1 = site(L, x-1, y, z);
+	for (int n = 0; n < nf; n++) {
+	  fw[n*N + i0] = 0.5*(u[i0] + u[i1])*mask*0.5
+	    *(field[n*N + i1] + field[n*N + i0]);
+	}
+	i1 = site(L, x+1, y, z);
+	for (int n = 0; n < nf; n++) {
+	  fe[n*N + i0] = 0.5*(u[i0] + u[i1])*mask*0.5
+	    *(field[n*N + i0] + field[n*N + i1]);
+	}
+	i1 = site(L, x, y+1, z);
+	for (int n = 0; n < nf; n++) {
+	  fy[n*N + i0] = 0.5*(u[N + i0] + u[N + i1])*mask*0.5
+	    *(field[n*N + i0] + field[n*N + i1]);
+	}
+	i1 = site(L, x, y, z+1);
+	for (int n = 0; n < nf; n++) {
+	  fz[n*N + i0] = 0.5*(u[2*N + i0] + u[2*N + i1])*mask*0.5
+	    *(field[n*N + i0] + field[n*N + i1]);
+	}
+      }
+    }
+  }
+}
+
+void orc_advect_3rd(const int L[3], int nf, const double * field,
+		    const double * u, double * fw, double * fe,
+		    double * fy, double * fz) {
+  size_t N = nsites(L);
+  const double a1 = -0.213933;
+  const double a2 =  0.927865;
+  const double a3 =  0.286067;
+  #pragma omp parallel for
+  for (int x = 0; x < L[0]; x++) {
+    for (int y = 0; y < L[1]; y++) {
+      for (int z = 0; z < L[2]; z++) {
+	const size_t i0 = site(L, x, y, z);
+	const double mask = 1.0;
+	/* x: m2 = x-2, m1 = x-1, p1 = x+1, p2 = x+2 */
+	{
+	  const size_t m2 = site(L, x-2, y, z), m1 = site(L, x-1, y, z);
+	  const size_t p1 = site(L, x+1, y, z), p2 = site(L, x+2, y, z);
+	  double uf = 0.5*mask*(u[i0] + u[m1]);
+	  for (int n = 0; n < nf; n++) {
+	    const double * f = field + n*N;
+	    double d1, d2, d3;
+	    if (uf > 0.0) { d1 = f[m2]; d2 = f[m1]; d3 = f[i0]; }
+	    else          { d1 = f[p1]; d2 = f[i0]; d3 = f[m1]; }
+	    fw[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+	  }
+	  uf = 0.5*mask*(u[i0] + u[p1]);
+	  for (int n = 0; n < nf; n++) {
+	    const double * f = field + n*N;
+	    double d1, d2, d3;
+	    if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+	    else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+	    fe[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+	  }
+	}
+	/* y face between y and y+1 */
+	{
+	  const size_t m1 = site(L, x, y-1, z), p1 = site(L, x, y+1, z);
+	  const size_t p2 = site(L, x, y+2, z);
+	  double uf = 0.5*mask*(u[N + i0] + u[N + p1]);
+	  for (int n = 0; n < nf; n++) {
+	    const double * f = field + n*N;
+	    double d1, d2, d3;
+	    if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+	    else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+	    fy[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+	  }
+	}
+	/* z face between z and z+1 */
+	{
+	  const size_t m1 = site(L, x, y, z-1), p1 = site(L, x, y, z+1);
+	  const size_t p2 = site(L, x, y, z+2);
+	  double uf = 0.5*mask*(u[2*N + i0] + u[2*N + p1]);
+	  for (int n = 0; n < nf; n++) {
+	    const double * f = field + n*N;
+	    double d1, d2, d3;
+	    if (uf < 0.0) { d1 = f[p2]; d2 = f[p1]; d3 = f[i0]; }
+	    else          { d1 = f[m1]; d2 = f[i0]; d3 = f[p1]; }
+	    fz[n*N + i0] = uf*(a1*d1 + a2*d2 + a3*d3);
+	  }
+	}
+      }
+    }
+  }
+}
+
+/* Advection order of the Cahn-Hilliard step (src/advection.c:82,
+ * advection_order_set): 1 (default), 2 or 3 */
+static int adv_order_ = 1;
+void orc_advection_order_set(int n) { adv_order_ = n; }
+
+/* Gradient stencil of the binary step: 7 (default) or 27 points */
+static int grad_stencil_ = 7;
+void orc_gradient_stencil_set(int n) { grad_stencil_ = n; }
+
+static void advect_order(const int L[3], int nf, const double * field,
+			 const double * u, double * fw, double * fe,
+			 double * fy, double * fz) {
+  if (adv_order_ == 2) orc_advect_2nd(L, nf, field, u, fw, fe, fy, fz);
+  else if (adv_order_ == 3) orc_advect_3rd(L, nf, field, u, fw, fe, fy, fz);
+  else orc_advect_upwind(L, nf, field, u, fw, fe, fy, fz);
 }
 
 /*****************************************************************************
@@ -715,13 +921,14 @@ void orc_binary_step(const int L[3], const orc_symm_param_t * fe,
   for (int step = 0; step < nsteps; step++) {
 
     memset(force, 0, 3*N*sizeof(double));
-    orc_grad_7pt(L, 1, phi, grad, delsq);
+    if (grad_stencil_ == 27) orc_grad_27pt(L, 1, phi, grad, delsq);
+    else orc_grad_7pt(L, 1, phi, grad, delsq);
     orc_symm_stress(L, fe, phi, grad, delsq, pth);
     orc_force_divergence(L, pth, force);
 
     {
       double * fw = pth, * fe_ = pth + N, * fy = pth + 2*N, * fz = pth + 3*N;
-      orc_advect_upwind(L, 1, phi, u, fw, fe_, fy, fz);
+      advect_order(L, 1, phi, u, fw, fe_, fy, fz);
       orc_ch_flux_mu(L, fe, mobility, phi, delsq, fw, fe_, fy, fz);
       orc_flux_no_normal(L, 1, status, fw, fe_, fy, fz);
       orc_ch_update(L, fw, fe_, fy, fz, phi);

@@ -59,6 +59,8 @@ void orc_lb_init_rest(const int L[3], double rho0, double * f);
 /* Hot-path functions */
 void orc_grad_7pt(const int L[3], int nf, const double * field,
 		  double * grad, double * delsq);
+void orc_grad_27pt(const int L[3], int nf, const double * field,
+		   double * grad, double * delsq);
 void orc_symm_mu(const int L[3], const orc_symm_param_t * fe,
 		 const double * phi, const double * delsq, double * mu);
 void orc_symm_stress(const int L[3], const orc_symm_param_t * fe,
@@ -68,6 +70,14 @@ void orc_force_divergence(const int L[3], const double * pth, double * force);
 void orc_advect_upwind(const int L[3], int nf, const double * field,
 		       const double * u, double * fw, double * fe,
 		       double * fy, double * fz);
+void orc_advect_2nd(const int L[3], int nf, const double * field,
+		    const double * u, double * fw, double * fe,
+		    double * fy, double * fz);
+void orc_advect_3rd(const int L[3], int nf, const double * field,
+		    const double * u, double * fw, double * fe,
+		    double * fy, double * fz);
+void orc_advection_order_set(int n);
+void orc_gradient_stencil_set(int n);
 void orc_ch_flux_mu(const int L[3], const orc_symm_param_t * fe,
 		    double mobility, const double * phi, const double * delsq,
 		    double * fw, double * fe_, double * fy, double * fz);

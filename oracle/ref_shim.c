@@ -14,6 +14,7 @@
  *
  *  Usage (key=value arguments):
  *    ref_shim mode=run    size=X,Y,Z steps=N A= B= K= M= eta= seed= noise=
+ *                         [grad=7|27] [order=1|2|3]
  *                         phi0= out=PREFIX
  *    ref_shim mode=collide  size=.. eta= in=PREFIX out=PREFIX
  *    ref_shim mode=propagate size=.. in=PREFIX out=PREFIX
@@ -49,6 +50,7 @@
 #include "field.h"
 #include "field_grad.h"
 #include "gradient_3d_7pt_fluid.h"
+#include "gradient_3d_27pt_fluid.h"
 #include "symmetric.h"
 #include "phi_force.h"
 #include "phi_force_stress.h"
@@ -66,6 +68,7 @@
 #include "blue_phase_beris_edwards.h"
 #include "colloids.h"
 #include "phi_lb_coupler.h"
+#include "advection.h"
 
 static const char * arg(int argc, char ** argv, const char * key,
 			const char * def) {
@@ -192,8 +195,14 @@ static void sys_create(int argc, char ** argv, sys_t * s) {
     field_options_t opts = field_options_ndata_nhalo(1, 2);
     field_create(s->pe, s->cs, s->le, "phi", &opts, &s->phi);
     field_grad_create(s->pe, s->phi, 2, &s->dphi);
-    field_grad_set(s->dphi, grad_3d_7pt_fluid_d2, NULL);
+    if (atoi(arg(argc, argv, "grad", "7")) == 27) {
+      field_grad_set(s->dphi, grad_3d_27pt_fluid_d2, NULL);
+    }
+    else {
+      field_grad_set(s->dphi, grad_3d_7pt_fluid_d2, NULL);
+    }
   }
+  advection_order_set(atoi(arg(argc, argv, "order", "1")));
   {
     fe_symm_param_t p = {0};
     p.a     = argd(argc, argv, "A", -0.0625);
@@ -550,6 +559,36 @@ int main(int argc, char ** argv) {
     lb_halo(s.lb);
     lb_propagation(s.lb);
     sys_dump(&s, out);
+  }
+  else if (strcmp(mode, "grad27") == 0) {
+    /* field_grad_compute with grad_3d_27pt_fluid_d2 */
+    int nf = atoi(arg(argc, argv, "nf", "1"));
+    size_t n = nint();
+    field_t * fld = NULL;
+    field_grad_t * fg = NULL;
+    field_options_t opts = field_options_ndata_nhalo(nf, 2);
+    field_create(s.pe, s.cs, s.le, "f27", &opts, &fld);
+    field_grad_create(s.pe, fld, 2, &fg);
+    field_grad_set(fg, grad_3d_27pt_fluid_d2, NULL);
+    double * a = readf(in, "phi", nf*n);
+    field_put(s.cs, fld, a);
+    field_halo(fld);
+    field_grad_compute(fg);
+    double * g = malloc(3*nf*n*sizeof(double));
+    double * dl = malloc(nf*n*sizeof(double));
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(s.cs, x+1, y+1, z+1);
+	for (int k = 0; k < nf; k++) {
+	  for (int ia = 0; ia < 3; ia++) {
+	    g[canon(3*k + ia, x, y, z)] =
+	      fg->grad[addr_rank2(fg->nsite, nf, 3, index, k, ia)];
+	  }
+	  dl[canon(k, x, y, z)] = fg->delsq[addr_rank1(fg->nsite, nf, index, k)];
+	}
+      }
+    writef(out, "grad", g, 3*nf*n);
+    writef(out, "delsq", dl, nf*n);
   }
   else if (strcmp(mode, "grad") == 0) {
     size_t n = nint();

@@ -7,7 +7,7 @@ phi_force_calculation, phi_cahn_hilliard and the main-loop step of
 src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
 
 Needs the reference sources (only where they are present):
-    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2]
+    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2|grad27|logs|advection]
 """
 
 import os
@@ -33,17 +33,20 @@ def kv(L, **extra):
 
 
 def run_case(name, L, steps, seed, status=None, keep=("phi", "u", "rho",
-                                                       "force", "f")):
+                                                       "force", "f"),
+             **extra):
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, "out")
         args = kv(L, mode="run", steps=steps, seed=seed, noise=0.02,
-                  phi0=0.0, out=out, dump0=1, **SYMM)
+                  phi0=0.0, out=out, dump0=1, **SYMM, **extra)
         if status is not None:
             sp = os.path.join(tmp, "status.bin")
             status.astype(np.uint8).tofile(sp)
             args["status"] = sp
         oracle.run_reference(args)
         res = {"L": np.array(L), "steps": steps, "seed": seed}
+        for k, v in extra.items():
+            res[k] = v
         if status is not None:
             res["status"] = status.astype(np.uint8)
         res["phi0"] = oracle.read_array(out + "0", "phi", (1,) + L)
@@ -138,11 +141,93 @@ def lb2_cases():
     print("wrote collide2_6x5x4")
 
 
+def grad27_cases():
+    rng = np.random.default_rng(20261205)
+    L = (6, 5, 4)
+    for nf in (1, 5):
+        a = rng.uniform(-1, 1, (nf,) + L)
+        with tempfile.TemporaryDirectory() as tmp:
+            pin, pout = os.path.join(tmp, "in"), os.path.join(tmp, "out")
+            oracle.write_arrays(pin, phi=a)
+            oracle.run_reference(kv(L, mode="grad27", nf=nf, **{"in": pin},
+                                    out=pout))
+            res = {"L": np.array(L), "in_phi": a}
+            res["grad"] = oracle.read_array(pout, "grad", (3 * nf,) + L)
+            res["delsq"] = oracle.read_array(pout, "delsq", (nf,) + L)
+        name = "grad27_nf%d_6x5x4" % nf
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print("wrote", name)
+
+
+REGRESSION_LOGS = ("serial-spin-fd1", "serial-spin-lb1", "serial-init-bp1",
+                   "serial-symm-dr1")
+
+
+def parse_log(path):
+    """Statistics blocks of a reference regression log: a list (initial
+    conditions, then each statistics step) of {tag: [numbers]}."""
+    blocks, cur = [], None
+    for line in open(path):
+        t = line.strip()
+        if t.startswith("Initial conditions") or \
+                t.startswith("Starting time step loop") or \
+                t.startswith("Completed cycle"):
+            if cur:
+                blocks.append(cur)
+            cur = {}
+            continue
+        if cur is None or not t.startswith("["):
+            continue
+        tag, rest = t[1:].split("]", 1)
+        vals = []
+        for w in rest.split():
+            try:
+                vals.append(float(w))
+            except ValueError:
+                pass
+        if vals:
+            cur.setdefault(tag.strip(), vals)
+    if cur:
+        blocks.append(cur)
+    return [b for b in blocks if b]
+
+
+def regression_logs(ref_root):
+    """Numbers of the reference's own regression logs for the cases this
+    path covers (read as text), into tests/golden/regression_logs.json."""
+    import json
+    d = os.path.join(ref_root, "tests", "regression", "d3q19-short")
+    out = {name: parse_log(os.path.join(d, name + ".log"))
+           for name in REGRESSION_LOGS}
+    with open(os.path.join(HERE, "regression_logs.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote regression_logs.json")
+
+
+def advection_cases():
+    """Runs with the 2nd- and 3rd-order advective fluxes and the 27-point
+    gradient (src/advection.c, src/gradient_3d_27pt_fluid.c)."""
+    run_case("run_adv2_8x6x4_s10", (8, 6, 4), 10, 8361235, order=2)
+    run_case("run_adv3_12x10x8_s30", (12, 10, 8), 30, 77, order=3)
+    run_case("run_adv2_g27_10x8x6_s12", (10, 8, 6), 12, 4242, order=2,
+             grad=27)
+    run_case("run_adv3_g27_8x8x8_s20", (8, 8, 8), 20, 99, order=3, grad=27)
+
+
 def main(ref_root, only=None):
     if not oracle.build_reference(ref_root):
         raise SystemExit("reference sources not found at " + ref_root)
     if only == "lb2":
         lb2_cases()
+        return
+    if only == "grad27":
+        grad27_cases()
+        return
+    if only == "logs":
+        regression_logs(ref_root)
+        return
+    if only == "advection":
+        advection_cases()
         return
     rng = np.random.default_rng(20261203)
 
@@ -179,6 +264,9 @@ def main(ref_root, only=None):
     u = 0.005 * rng.standard_normal((3,) + L)
     lc_op_case("lc_be_6x5x4", "lc_be", L, dict(q=q, u=u), dict(q=5))
     lb2_cases()
+    grad27_cases()
+    advection_cases()
+    regression_logs(ref_root)
 
 
 if __name__ == "__main__":

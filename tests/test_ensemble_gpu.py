@@ -18,7 +18,7 @@ def small_ensemble(gb, nbox=5):
         n = [int(rng.choice([8, 12, 16, 20])) for _ in range(3)]
         kappa = float(rng.uniform(0.02, 0.08))
         amag = float(rng.uniform(0.03, 0.1))
-        mob = min(0.45, 1.0 / (12.0 * (12.0 * kappa - amag)))
+        mob = min(0.45, 1.0 / (12.0 * (12.0 * kappa + 2.0 * amag)))
         params.append(gb.box_param(n, eta=float(rng.uniform(0.02, 0.2)),
                                    a=-amag, b=amag, kappa=kappa, mobility=mob,
                                    seed=100 + k))

@@ -151,3 +151,36 @@ def test_oracle_binary_collision_matches_reference(orc):
     assert np.array_equal(f, g["f"])
     assert np.array_equal(gg, g["g"])
     assert np.array_equal(u, g["u"])
+
+
+@pytest.mark.parametrize("nf", [1, 5])
+def test_oracle_grad27(orc, nf):
+    g = load("grad27_nf%d_6x5x4" % nf)
+    grad, delsq = orc.grad_27pt(L_of(g), g["in_phi"])
+    assert np.array_equal(grad, g["grad"])
+    assert np.array_equal(delsq, g["delsq"])
+
+
+@pytest.mark.parametrize("name", ["run_adv2_8x6x4_s10", "run_adv3_12x10x8_s30",
+                                  "run_adv2_g27_10x8x6_s12",
+                                  "run_adv3_g27_8x8x8_s20"])
+def test_oracle_advection_orders_match_reference(orc, name):
+    """2nd/3rd-order advective fluxes (and the 27-point gradient) through
+    the whole step."""
+    import ctypes
+    g = load(name)
+    L = L_of(g)
+    lib = orc.lib()
+    lib.orc_advection_order_set.argtypes = [ctypes.c_int]
+    lib.orc_gradient_stencil_set.argtypes = [ctypes.c_int]
+    lib.orc_advection_order_set(int(g["order"]))
+    lib.orc_gradient_stencil_set(int(g["grad"]) if "grad" in g else 7)
+    try:
+        st = orc.BinaryState(L, orc.lb_init_rest(L), g["phi0"])
+        orc.binary_steps(st, orc.symm_param(A, B, KAPPA), MOB,
+                         orc.collide_param_m10(ETA), int(g["steps"]))
+        for k in ("phi", "u", "f"):
+            assert np.array_equal(getattr(st, k), g[k]), k
+    finally:
+        lib.orc_advection_order_set(1)
+        lib.orc_gradient_stencil_set(7)

@@ -1,0 +1,136 @@
+"""The GPU FP64 path against the reference's own regression logs.
+
+The statistics the reference printed for three of its regression runs
+(tests/regression/d3q19-short/*.log, read as text into
+tests/golden/regression_logs.json by tests/golden/make_golden.py) are
+recomputed here from the same inputs through this library's reference-
+order API:
+
+* serial-spin-fd1: symmetric binary fluid, 64^3, 27-point gradients,
+  finite-difference Cahn-Hilliard, 10 steps;
+* serial-spin-lb1: the same fluid on the two-distribution route
+  (symmetric_lb), 27-point gradients, 10 steps;
+* serial-init-bp1: cholesteric blue phase I (O8M), 32^3, redshift 0.83,
+  one step;
+* serial-symm-dr1: a drop of radius 16 in the symmetric binary fluid,
+  64^3, 27-point gradients, second-order advection, one step.
+
+Values are compared to the digits the log prints (8 significant digits
+for most, 11 for the free energy); sums whose terms cancel (momentum,
+variance of rho) to an absolute bound.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+with open(os.path.join(GOLDEN, "regression_logs.json")) as _f:
+    LOGS = json.load(_f)
+
+
+def close(got, ref, rel):
+    """Printed value ref (rounded to its digits) against got."""
+    return abs(got - ref) <= rel * abs(ref) + 1e-300
+
+
+def check_scalars(got, ref, rel=6e-8):
+    """total, mean, variance, min, max."""
+    names = ("total", "mean", "variance", "min", "max")
+    for k in range(5):
+        if abs(ref[k]) < 1e-10:           # printed as noise around zero
+            assert abs(got[k] - ref[k]) < 1e-9, (names[k], got[k], ref[k])
+        else:
+            assert close(got[k], ref[k], rel), (names[k], got[k], ref[k])
+
+
+def rho_stats(f):
+    rho = f.sum(axis=0)
+    return rho.sum(), rho.min(), rho.max()
+
+
+def check_common(s, ref, u, f, mom):
+    tot, rmin, rmax = rho_stats(f)
+    assert close(tot, ref["rho"][0], 1e-9)
+    assert close(rmin, ref["rho"][3], 1e-10)
+    assert close(rmax, ref["rho"][4], 1e-10)
+    for a in range(3):
+        assert abs(mom[1 + a] - ref["total"][a]) < 1e-13
+        assert close(u[a].min(), ref["minimum"][a], 1e-7)
+        assert close(u[a].max(), ref["maximum"][a], 1e-7)
+
+
+def test_serial_spin_fd1(gb):
+    ref = LOGS["serial-spin-fd1"]
+    s = gb.BinaryFluid((64, 64, 64), gb.FP64, a=-0.00625, b=0.00625,
+                       kappa=0.004, mobility=1.25, eta=0.00625)
+    s.dphi.set_stencil(27)
+    s.phi.init_spinodal(8361235, 0.0, 0.1)
+    check_scalars(s.phi.stats(), ref[0]["phi"])
+    s.step_reference_order(10)
+    check_scalars(s.phi.stats(), ref[1]["phi"])
+    # the binary logs print the free energy per site
+    assert close(s.fe.fed_total() / 64 ** 3, ref[1]["fed"][1], 1e-9)
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_serial_spin_lb1(gb):
+    ref = LOGS["serial-spin-lb1"]
+    s = gb.BinaryFluidLB((64, 64, 64), a=-0.00625, b=0.00625, kappa=0.004,
+                         mobility=3.75, eta=0.00625)
+    s.dphi.set_stencil(27)
+    s.init_spinodal(8361235, 0.0, 0.1)
+    check_scalars(s.phi.stats(), ref[0]["phi"])
+    s.step_reference_order(10)
+    # statistics from phi = sum g after the step, gradients of the step
+    gb.lib().phi_lb_to_field(s.phi.ptr, s.lb.ptr)
+    check_scalars(s.phi.stats(), ref[1]["phi"])
+    assert close(s.fe.fed_total() / 64 ** 3, ref[1]["fed"][1], 1e-9)
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_serial_init_bp1(gb):
+    ref = LOGS["serial-init-bp1"]
+    s = gb.LiquidCrystal((32, 32, 32), eta=1.666666666666, gamma_rot=0.1,
+                         a0=0.014384711, gamma=3.1764706, kappa0=0.01,
+                         kappa1=0.01, xi=0.7, redshift=0.83, amplitude=-0.2,
+                         q0=0.27768018)
+    s.init_o8m()
+    tags = ("Qxx", "Qxy", "Qxz", "Qyy", "Qyz")
+    for n, t in enumerate(tags):
+        check_scalars(s.q.stats(n), ref[0][t])
+    assert close(s.fe.fed_total(), ref[0]["fe"][1], 1e-9)
+    s.step_reference_order(1)
+    for n, t in enumerate(tags):
+        check_scalars(s.q.stats(n), ref[1][t])
+    # after a step the reference's statistics use the gradients of the step
+    assert close(s.fe.fed_total(recompute=False), ref[1]["fe"][1], 1e-9)
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_serial_symm_dr1(gb):
+    ref = LOGS["serial-symm-dr1"]
+    A, K = -0.00625, 0.004
+    s = gb.BinaryFluid((64, 64, 64), gb.FP64, a=A, b=-A, kappa=K,
+                       mobility=1.25, eta=0.00625)
+    s.dphi.set_stencil(27)
+    gb.advection_order(2)
+    try:
+        s.phi.init_drop(np.sqrt(-2.0 * K / A), 16.0, 1.0, False)
+        check_scalars(s.phi.stats(), ref[0]["phi"])
+        s.dphi.compute()
+        assert close(s.fe.fed_total() / 64 ** 3, ref[0]["fed"][1], 1e-9)
+        s.step_reference_order(1)
+        check_scalars(s.phi.stats(), ref[1]["phi"])
+        assert close(s.fe.fed_total() / 64 ** 3, ref[1]["fed"][1], 1e-9)
+        _, u, _ = s.hydro.get()
+        check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+    finally:
+        gb.advection_order(1)

@@ -289,15 +289,22 @@ def gpu_arm(args):
     # --- end to end through the C ABI with host buffers --------------------
     e2e_steps = max(3, min(args.steps, 20))
     ms_e2e, h2d, d2h = float("nan"), 0, 0
+    ms_e2e_serial = float("nan")
     if "e2e" in legs:
-        pinned = lg.PinnedState(s32)
-        lg.time_binary_e2e(s32, pinned, 1)                 # warm-up
+        # every step: upload the state from pinned host memory, one fused
+        # step, download the result; the copies of consecutive steps overlap
+        pin_in, pin_out = lg.PinnedState(s32), lg.PinnedState(s32)
+        lg.time_binary_e2e_overlap(s32, pin_in, pin_out, 2)    # warm-up
         barrier(pg)
-        ms_e2e = lg.time_binary_e2e(s32, pinned, e2e_steps)
+        ms_e2e = lg.time_binary_e2e_overlap(s32, pin_in, pin_out, e2e_steps)
         barrier(pg)
         ms_e2e = max_over_ranks(pg, ms_e2e)
-        h2d, d2h = pinned.bytes_in, pinned.bytes_out
-        pinned.close()
+        h2d, d2h = pin_in.bytes_in, pin_out.bytes_out
+        # the same, each step's copies and step in sequence on one stream
+        lg.time_binary_e2e(s32, pin_in, 1)
+        ms_e2e_serial = lg.time_binary_e2e(s32, pin_in, e2e_steps)
+        pin_in.close()
+        pin_out.close()
     s32 = None
 
     # --- FP16 storage -------------------------------------------------------
@@ -384,6 +391,7 @@ def gpu_arm(args):
     fp64_mlups = total_sites * k64 / (ms64 * 1e-3) / 1e6
     fp16_mlups = nsites * args.steps / (ms16 * 1e-3) / 1e6 * world
     e2e = total_sites * e2e_steps / (ms_e2e * 1e-3) / 1e6
+    e2e_serial = nsites * e2e_steps / (ms_e2e_serial * 1e-3) / 1e6
 
     if rank != 0:
         return 0
@@ -422,7 +430,12 @@ def gpu_arm(args):
         "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "how": "per step: f, phi, u H2D from pinned host memory, one "
-                       "fused step, f, phi, u, rho D2H (C ABI)"},
+                       "fused step, f, phi, u, rho D2H (C ABI); two device "
+                       "buffer sets so that the upload of step k+1 overlaps "
+                       "the download of step k",
+                "serial": {"value": e2e_serial, "unit": "MLUPS",
+                           "how": "the same with copies and step in "
+                                  "sequence on one stream"}},
         "gpu_launches": args.steps,
         "clocks": clk,
         "fp64": {"value": fp64_mlups, "unit": "MLUPS", "steps": k64,

@@ -39,7 +39,8 @@ enum {
   LUDWIG_GB_ECUDA    = 3,    /* CUDA runtime error */
   LUDWIG_GB_ESTATE   = 4,    /* object in the wrong state for this call */
   LUDWIG_GB_ETIMEOUT = 5,    /* a bounded device wait ran out */
-  LUDWIG_GB_ENOTFINITE = 6   /* NaN or Inf detected in a reduction */
+  LUDWIG_GB_ENOTFINITE = 6,  /* NaN or Inf detected in a reduction */
+  LUDWIG_GB_EIO      = 7     /* a snapshot file could not be written/read */
 };
 
 const char * ludwig_gb_last_error(void);
@@ -291,6 +292,12 @@ int fe_lc_param(fe_lc_t * fe, fe_lc_param_t * values);
  * euler_angles must be zero) */
 int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 			const double euler_angles[3]);
+/* Blue phase II, src/blue_phase_init.c:155 (no rotation) */
+int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
+		       const double euler_angles[3]);
+/* Uniform uniaxial nematic along n, src/blue_phase_init.c:836 */
+int blue_phase_nematic_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
+			    const double n[3]);
 
 /* Beris-Edwards: src/blue_phase_beris_edwards.h:28-49 */
 typedef struct beris_edw_param_s {
@@ -399,6 +406,19 @@ int ludwig_gb_time_binary_e2e(lb_t * lb, field_t * phi, hydro_t * hydro,
 			      map_t * map, fe_t * fe, int nsteps, void * f_h,
 			      void * phi_h, void * u_h, void * rho_h,
 			      double * ms);
+/* The same with the copies of consecutive steps overlapped: every step
+ * uploads the same host input (in_*), takes one fused step and downloads
+ * the result (out_*: f, phi, u, rho); two device buffer sets alternate and
+ * the upload of step k+1 runs while the download of step k does.  All
+ * host buffers pinned (ludwig_gb_host_alloc).  On return the objects hold
+ * the input state. */
+int ludwig_gb_time_binary_e2e_overlap(lb_t * lb, field_t * phi,
+				      hydro_t * hydro, map_t * map, fe_t * fe,
+				      int nsteps, const void * in_f,
+				      const void * in_phi, const void * in_u,
+				      void * out_f, void * out_phi,
+				      void * out_u, void * out_rho,
+				      double * ms);
 
 /*---------------------------------------------------------------------------
  * Statistics (FP64 accumulation, compensated), src/phi_stats.c:91-140,
@@ -413,6 +433,14 @@ int stats_free_energy_symm(fe_symm_t * fe, double * total);
 /* LC total free energy (fe_lc_fed summed, src/stats_free_energy.c:38);
  * FP64 fields, after field_grad_compute() of the q gradients */
 int stats_free_energy_lc(fe_lc_t * fe, double * total);
+/* fe_lc_stats_info without walls or colloids (src/fe_lc_stats.c:55-150):
+ * out = {f, v, f/v, f_bulk/v, f_grad/v, redshift} over the fluid sites of
+ * map (all sites for NULL); after field_grad_compute() of the q gradients */
+int fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]);
+/* stats_velocity_minmax (src/stats_velocity.c:54-125): out = {min u_x,
+ * u_y, u_z, max u_x, u_y, u_z, volume flux x, y, z} over the fluid sites
+ * of map (all sites for NULL); min starts at FLT_MAX, max at FLT_MIN */
+int stats_velocity_minmax(hydro_t * hydro, map_t * map, double out[9]);
 
 /*---------------------------------------------------------------------------
  * Ensembles: many independent periodic binary-fluid boxes of any sizes and
@@ -569,6 +597,40 @@ int ludwig_gb_fields_pack(field_t * phi, hydro_t * hydro, lb_t * lb,
  * keeps one per process, src/physics.c:76; two systems with different
  * mobilities take turns). */
 int ludwig_gb_physics_use(physics_t * phys);
+
+/*---------------------------------------------------------------------------
+ * Snapshot (restart) files in the reference's format: one file per object
+ * in the current directory, single rank, as lb_io_write/lb_io_read
+ * (src/lb_data.c:1716-1830) and field_io_write/field_io_read
+ * (src/field.c:1633-1737) write and read them:
+ *   data      "<stub>-%9.9d.001-001" (stub "dist" or the field's name):
+ *             the sites in x, y, z order (z fastest), one record each:
+ *             binary, ndist*19 (or nf) native doubles; or ascii, " %22.15e"
+ *             per value with a newline after each velocity's ndist values
+ *             (lb) or after the nf values (field);
+ *   metadata  "<stub>-metadata.001-001" (JSON, written with the first data
+ *             file of the object).
+ * Reduced-precision objects are written as the doubles of the reference's
+ * f and read back into their own precision.
+ *-------------------------------------------------------------------------*/
+enum io_record_format_enum {IO_RECORD_INVALID, IO_RECORD_ASCII,
+			    IO_RECORD_BINARY};
+typedef struct io_event_s io_event_t;       /* accepted; may be NULL */
+/* record formats of input and output (default binary), the
+ * lb_data_options_t / field_options_t iodata.input/output.iorformat */
+int lb_io_record_format_set(lb_t * lb, int iorformat_in, int iorformat_out);
+int field_io_record_format_set(field_t * field, int iorformat_in,
+			       int iorformat_out);
+int lb_io_write(lb_t * lb, int timestep, io_event_t * event);
+int lb_io_read(lb_t * lb, int timestep, io_event_t * event);
+int field_io_write(field_t * field, int timestep, io_event_t * event);
+int field_io_read(field_t * field, int timestep, io_event_t * event);
+/* hydro_io_write / hydro_io_read (src/hydro.c:941-967): the fields "rho"
+ * (1 value a site) and "vel" (3) in the field format */
+int hydro_io_record_format_set(hydro_t * hydro, int iorformat_in,
+			       int iorformat_out);
+int hydro_io_write(hydro_t * hydro, int timestep, io_event_t * event);
+int hydro_io_read(hydro_t * hydro, int timestep, io_event_t * event);
 
 #ifdef __cplusplus
 }

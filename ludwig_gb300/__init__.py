@@ -51,6 +51,7 @@ _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
 _I3 = ctypes.c_int * 3
 _D3 = ctypes.c_double * 3
+_IORF = {"ascii": 1, "binary": 2}          # enum io_record_format_enum
 _F = ctypes.POINTER(ctypes.c_float)
 
 
@@ -134,6 +135,18 @@ def _declare(L):
         "lb_init_rest_f": ([_P, ctypes.c_double], ctypes.c_int),
         "lb_halo": ([_P], ctypes.c_int),
         "lb_f_to_host": ([_P, _D], ctypes.c_int),
+        "lb_io_record_format_set": ([_P, ctypes.c_int, ctypes.c_int],
+                                    ctypes.c_int),
+        "field_io_record_format_set": ([_P, ctypes.c_int, ctypes.c_int],
+                                       ctypes.c_int),
+        "lb_io_write": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "lb_io_read": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "field_io_write": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "field_io_read": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "hydro_io_record_format_set": ([_P, ctypes.c_int, ctypes.c_int],
+                                       ctypes.c_int),
+        "hydro_io_write": ([_P, ctypes.c_int, _P], ctypes.c_int),
+        "hydro_io_read": ([_P, ctypes.c_int, _P], ctypes.c_int),
         "lb_f_from_host": ([_P, _D], ctypes.c_int),
         "lb_collide": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
         "lb_g_to_host": ([_P, _D], ctypes.c_int),
@@ -195,11 +208,18 @@ def _declare(L):
                                   ctypes.c_int),
         "ludwig_gb_time_binary_e2e": ([_P] * 5 + [ctypes.c_int] + [_P] * 4
                                       + [_D], ctypes.c_int),
+        "ludwig_gb_time_binary_e2e_overlap": ([_P] * 5 + [ctypes.c_int]
+                                              + [_P] * 7 + [_D],
+                                              ctypes.c_int),
         "fe_lc_create": ([_P, _P, _P, _P, _P, pp], ctypes.c_int),
         "fe_lc_free": ([_P], ctypes.c_int),
         "fe_lc_param_set": ([_P, ctypes.POINTER(FeLcParam)], ctypes.c_int),
         "blue_phase_O8M_init": ([_P, ctypes.POINTER(FeLcParam), _P, _D],
                                 ctypes.c_int),
+        "blue_phase_O2_init": ([_P, ctypes.POINTER(FeLcParam), _P, _D],
+                               ctypes.c_int),
+        "blue_phase_nematic_init": ([_P, ctypes.POINTER(FeLcParam), _P, _D],
+                                    ctypes.c_int),
         "beris_edw_create": ([_P, _P, _P, pp], ctypes.c_int),
         "beris_edw_free": ([_P], ctypes.c_int),
         "beris_edw_param_set": ([_P, ctypes.POINTER(BerisEdwParam)],
@@ -257,6 +277,8 @@ def _declare(L):
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
         "stats_free_energy_lc": ([_P, _D], ctypes.c_int),
+        "fe_lc_stats_info": ([_P, _P, _D], ctypes.c_int),
+        "stats_velocity_minmax": ([_P, _P, _D], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -377,6 +399,19 @@ class LB(_Obj):
         assert f.shape == (NVEL,) + self.cs.ntotal
         _check(lib().lb_f_from_host(self.ptr, _dp(f)), "lb_f_from_host")
 
+    def io_format(self, fmt_in="binary", fmt_out="binary"):
+        """Record formats ("binary" or "ascii") of lb_io_read / write."""
+        _check(lib().lb_io_record_format_set(self.ptr, _IORF[fmt_in],
+                                             _IORF[fmt_out]), "io format")
+
+    def io_write(self, step):
+        """lb_io_write: dist-<step>.001-001 (and its metadata) in the
+        current directory, in the reference's format."""
+        _check(lib().lb_io_write(self.ptr, int(step), None), "lb_io_write")
+
+    def io_read(self, step):
+        _check(lib().lb_io_read(self.ptr, int(step), None), "lb_io_read")
+
     def get_g(self):
         """The order-parameter distribution (ndist = 2)."""
         g = np.zeros((NVEL,) + self.cs.ntotal)
@@ -414,6 +449,7 @@ class Field(_Obj):
         super().__init__()
         self.cs = cs
         self.nf = nf
+        self.name = name
         o = FieldOptions(int(nf), int(nhalo), int(precision))
         self.ptr = _new("field_create", cs.pe.ptr, cs.ptr, None,
                         name.encode(), ctypes.byref(o))
@@ -427,6 +463,20 @@ class Field(_Obj):
         a = np.ascontiguousarray(a, dtype=np.float64)
         assert a.shape == (self.nf,) + self.cs.ntotal
         _check(lib().field_from_host(self.ptr, _dp(a)), "field_from_host")
+
+    def io_format(self, fmt_in="binary", fmt_out="binary"):
+        """Record formats ("binary" or "ascii") of field_io_read / write."""
+        _check(lib().field_io_record_format_set(self.ptr, _IORF[fmt_in],
+                                                _IORF[fmt_out]), "io format")
+
+    def io_write(self, step):
+        """field_io_write: <name>-<step>.001-001 (and its metadata) in the
+        current directory, in the reference's format."""
+        _check(lib().field_io_write(self.ptr, int(step), None),
+               "field_io_write")
+
+    def io_read(self, step):
+        _check(lib().field_io_read(self.ptr, int(step), None), "field_io_read")
 
     def halo(self):
         _check(lib().field_halo(self.ptr), "field_halo")
@@ -524,6 +574,29 @@ class Hydro(_Obj):
 
     def u_halo(self):
         _check(lib().hydro_u_halo(self.ptr), "hydro_u_halo")
+
+    def io_format(self, fmt_in="binary", fmt_out="binary"):
+        _check(lib().hydro_io_record_format_set(self.ptr, _IORF[fmt_in],
+                                                _IORF[fmt_out]), "io format")
+
+    def io_write(self, step):
+        """hydro_io_write: the fields "rho" and "vel" in the reference's
+        format, in the current directory."""
+        _check(lib().hydro_io_write(self.ptr, int(step), None),
+               "hydro_io_write")
+
+    def io_read(self, step):
+        _check(lib().hydro_io_read(self.ptr, int(step), None), "hydro_io_read")
+
+    def velocity_minmax(self, map=None):
+        """(umin[3], umax[3], volume flux[3]) over the fluid sites, as
+        stats_velocity_minmax prints them."""
+        out = np.zeros(9)
+        _check(lib().stats_velocity_minmax(self.ptr,
+                                           map.ptr if map else None,
+                                           _dp(out)),
+               "stats_velocity_minmax")
+        return out[0:3], out[3:6], out[6:9]
 
 
 class Map(_Obj):
@@ -777,6 +850,24 @@ def time_binary(system, nsteps):
     return ms.value
 
 
+def time_binary_e2e_overlap(system, pin_in, pin_out, nsteps):
+    """End-to-end time (ms) of nsteps steps, each uploading the same host
+    input (pin_in, filled here from the system's state) and downloading
+    its result to pin_out, with the copies of consecutive steps
+    overlapped."""
+    ms = ctypes.c_double()
+    s = system
+    L = lib()
+    _check(L.ludwig_gb_state_to_host_async(s.lb.ptr, s.phi.ptr, s.hydro.ptr,
+                                           *pin_in.bufs[:3]), "state_to_host")
+    sync()
+    _check(L.ludwig_gb_time_binary_e2e_overlap(
+        s.lb.ptr, s.phi.ptr, s.hydro.ptr, s.map.ptr, s.fe.ptr, int(nsteps),
+        *pin_in.bufs[:3], *pin_out.bufs, ctypes.byref(ms)),
+        "time_binary_e2e_overlap")
+    return ms.value
+
+
 def time_binary_e2e(system, pinned, nsteps):
     ms = ctypes.c_double()
     s = system
@@ -801,7 +892,7 @@ class FeLC(_Obj):
 
     def __init__(self, cs, q, dq, a0=0.01, gamma=3.0, kappa0=0.01,
                  kappa1=0.01, pitch=32.0, xi=0.7, redshift=1.0,
-                 amplitude=-0.2, q0=None):
+                 amplitude=-0.2, q0=None, epsilon=0.0, e0=(0.0, 0.0, 0.0)):
         super().__init__()
         self.ptr = _new("fe_lc_create", cs.pe.ptr, cs.ptr, None, q.ptr,
                         dq.ptr)
@@ -809,6 +900,11 @@ class FeLC(_Obj):
         p.a0, p.gamma, p.kappa0, p.kappa1 = a0, gamma, kappa0, kappa1
         p.q0 = (2.0 * 3.1415926535897932385 / pitch) if q0 is None else q0
         p.xi, p.redshift, p.amplitude0, p.coswt = xi, redshift, amplitude, 1.0
+        # dielectric anisotropy (fe_lc_param_set divides it by 12 pi) and
+        # a static external field
+        p.epsilon = epsilon
+        for a in range(3):
+            p.e0[a] = e0[a]
         self.param = p
         self.dq = dq
         _check(lib().fe_lc_param_set(self.ptr, ctypes.byref(p)),
@@ -824,6 +920,16 @@ class FeLC(_Obj):
         _check(lib().stats_free_energy_lc(self.ptr, ctypes.byref(out)),
                "stats_free_energy_lc")
         return out.value
+
+    def stats_info(self, map=None, recompute=True):
+        """The columns of the reference's "[fe]" line: (f, v, f/v,
+        f_bulk/v, f_grad/v, redshift) over the fluid sites."""
+        if recompute:
+            self.dq.compute()
+        out = np.zeros(6)
+        _check(lib().fe_lc_stats_info(self.ptr, map.ptr if map else None,
+                                      _dp(out)), "fe_lc_stats_info")
+        return out
 
 
 class BerisEdw(_Obj):
@@ -853,10 +959,13 @@ class LiquidCrystal:
     """All objects of the cholesteric LC with hydrodynamics (config 4)."""
 
     def __init__(self, ntotal, eta=0.5, gamma_rot=0.5, device=0,
-                 precision=FP64, **lc):
+                 precision=FP64, eta_bulk=None, hydrodynamics=True, **lc):
         self.pe = PE(device)
         self.cs = Coords(self.pe, ntotal)
-        self.phys = Physics(self.pe, rho0=1.0, eta=eta)
+        self.phys = Physics(self.pe, rho0=1.0, eta=eta, eta_bulk=eta_bulk)
+        # hydrodynamics off: Q relaxes without flow (no force, no LB step),
+        # as the reference's "hydrodynamics off"
+        self.hydrodynamics = bool(hydrodynamics)
         self.lb = LB(self.cs, precision)
         self.q = Field(self.cs, 5, 2, precision, "q")
         self.dq = FieldGrad(self.q, 2)
@@ -873,8 +982,24 @@ class LiquidCrystal:
                                          ctypes.byref(self.fe.param),
                                          self.q.ptr, zero), "o8m")
 
+    def init_o2(self):
+        zero = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+        _check(lib().blue_phase_O2_init(self.cs.ptr,
+                                        ctypes.byref(self.fe.param),
+                                        self.q.ptr, zero), "o2")
+
+    def init_nematic(self, n):
+        _check(lib().blue_phase_nematic_init(self.cs.ptr,
+                                             ctypes.byref(self.fe.param),
+                                             self.q.ptr, _D3(*n)), "nematic")
+
     def step_reference_order(self, nsteps=1):
         for _ in range(nsteps):
+            if not self.hydrodynamics:
+                self.q.halo()
+                self.dq.compute()
+                self.be.update(self.fe, self.q, self.dq, None, self.map)
+                continue
             self.hydro.f_zero()
             self.q.halo()
             self.dq.compute()

@@ -33,7 +33,7 @@ CU_SOURCES = [
     ("lgb_cnn.cu", []),
     ("lgb_coarse.cu", []),
 ]
-C_SOURCES = ["ludwig_gb.c", "ludwig_gb_cnn.c"]
+C_SOURCES = ["ludwig_gb.c", "ludwig_gb_cnn.c", "ludwig_gb_io.c"]
 
 
 def _cuda_home():

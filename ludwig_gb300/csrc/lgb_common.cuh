@@ -112,6 +112,83 @@ __device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
   return lgb_symm_p0<T>((T) fe.a, (T) fe.b, (T) fe.kappa, phi, delsq, g);
 }
 
+#ifndef LGB_MASS_SUM
+#define LGB_MASS_SUM 2
+#endif
+
+/* s + c += x with the rounding error of the addition kept in c
+ * (Neumaier's compensated summation) */
+template <typename T>
+__device__ __forceinline__ void lgb_sum2(T & s, T & c, T x) {
+  const T t = s + x;
+  c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+  s = t;
+}
+
+/* Sum of populations fs[p0..18] as h + l with h exact (error-free
+ * splitting, as in Rump, Ogita and Oishi's AccSum): for |x| < 8 and
+ * C = 1.5*2^4, fl(x + C) - C is x rounded to a multiple of ulp(C) = 2^-19
+ * (FP32), exactly, and x minus it is exact too.  The rounded parts then
+ * add without error while the partial sums stay below 2^24 ulp(C) = 32;
+ * only the remainders (|r| <= 2^-20) are summed with rounding. */
+template <typename T, int P0>
+__device__ __forceinline__ void lgb_mass_split(const T fs[LGB_NVEL], T & h,
+					       T & l) {
+  const T C = T(24.0);
+  h = T(0.0); l = T(0.0);
+  #pragma unroll
+  for (int p = P0; p < LGB_NVEL; p++) {
+    const T a = fs[p] + C;
+    const T hx = a - C;
+    h += hx;
+    l += fs[p] - hx;
+  }
+}
+
+/* The same on pairs of populations with the packed FP32x2 operations */
+template <int P0>
+__device__ __forceinline__ void lgb_mass_split2(const float fs[LGB_NVEL],
+						float & h, float & l) {
+  const float2 c2 = make_float2(24.0f, 24.0f);
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  float2 h2 = make_float2(0.0f, 0.0f), l2 = h2;
+  #pragma unroll
+  for (int p = 1; p < LGB_NVEL; p += 2) {
+    const float2 x = make_float2(fs[p], fs[p + 1]);
+    const float2 a = __fadd2_rn(x, c2);
+    const float2 hx = __ffma2_rn(c2, m1, a);         /* a - C, exact */
+    const float2 lx = __ffma2_rn(hx, m1, x);         /* x - hx, exact */
+    h2 = __fadd2_rn(h2, hx);
+    l2 = __fadd2_rn(l2, lx);
+  }
+  h = h2.x + h2.y;
+  l = l2.x + l2.y;
+  if (P0 == 0) {
+    const float a = fs[0] + 24.0f;
+    const float hx = a - 24.0f;
+    h += hx;
+    l += fs[0] - hx;
+  }
+}
+
+template <typename T, int P0>
+__device__ __forceinline__ void lgb_mass(const T fs[LGB_NVEL], T & h, T & l) {
+  lgb_mass_split<T, P0>(fs, h, l);
+}
+
+#if LGB_MASS_SUM == 2
+template <>
+__device__ __forceinline__ void lgb_mass<float, 0>(const float fs[LGB_NVEL],
+						   float & h, float & l) {
+  lgb_mass_split2<0>(fs, h, l);
+}
+template <>
+__device__ __forceinline__ void lgb_mass<float, 1>(const float fs[LGB_NVEL],
+						   float & h, float & l) {
+  lgb_mass_split2<1>(fs, h, l);
+}
+#endif
+
 /*****************************************************************************
  *
  *  lgb_collide_site
@@ -157,6 +234,19 @@ __device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
 						     T & rho_out, T u[3]) {
   T mode[LGB_NVEL];
   constexpr int NM = GZERO ? 10 : LGB_NVEL;
+
+  /* Reduced precision: the mass of the incoming populations as an
+   * unevaluated sum hi + lo (compensated, Neumaier) */
+  T mass_hi = T(0.0), mass_lo = T(0.0);
+  if (!SEQ) {
+#if LGB_MASS_SUM == 0
+    mass_hi = fs[0];
+    #pragma unroll
+    for (int p = 1; p < LGB_NVEL; p++) lgb_sum2(mass_hi, mass_lo, fs[p]);
+#else
+    lgb_mass<T, 0>(fs, mass_hi, mass_lo);
+#endif
+  }
 
   if (SEQ) d3q19_f2mode_seq<T, NM>(fs, mode);
   else     d3q19_f2mode_fast<T, NM>(fs, mode);
@@ -226,12 +316,20 @@ __device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
     /* Reduced precision: the rounded mode -> f coefficients do not sum
      * exactly to the conserved moments, and the stress modes (which carry
      * rho u u, always positive) then leak mass with one sign every step.
-     * Rebuild the rest population from the conserved mode 0 instead, so
-     * that the population sum equals mode 0 up to unbiased rounding. */
-    T r = mode[0];
+     * Rebuild the rest population from the incoming mass instead, with
+     * error-free (split) sums on both sides, so that the populations' sum
+     * equals the incoming sum up to one rounding of the rest population
+     * and the rounding of the small remainders. */
+#if LGB_MASS_SUM == 0
+    T s = mass_hi, c = mass_lo;
     #pragma unroll
-    for (int p = 1; p < LGB_NVEL; p++) r -= fs[p];
-    fs[0] = r;
+    for (int p = 1; p < LGB_NVEL; p++) lgb_sum2(s, c, -fs[p]);
+    fs[0] = s + c;
+#else
+    T h, l;
+    lgb_mass<T, 1>(fs, h, l);
+    fs[0] = (mass_hi - h) + (mass_lo - l);
+#endif
   }
 
   rho_out = rho;

@@ -132,15 +132,16 @@ __device__ __forceinline__ void lc_h_site(const P & p, T q[3][3],
   }
 }
 
+/* The invariants of the free energy: q2 = Q_ab Q_ab, q3 = Q_ab Q_bc Q_ca,
+ * dq0 = (d_b Q_ab)^2, dq1 = (e_acd d_c Q_db + 2 q0 Q_ab)^2, in the order of
+ * src/blue_phase.c:284-340 (the same order as blue_phase_fbg,
+ * src/fe_lc_stats.c:721-806, for a symmetric Q) */
 template <typename T, typename P>
-__device__ __forceinline__ T lc_fed_site(const P & p, T q[3][3],
-					 T dq[3][3][3]) {
-  const T r3 = T(1.0/3.0);
-  const T gamma = (T) p.gamma, a0 = (T) p.a0;
+__device__ __forceinline__ void lc_invariants(const P & p, T q[3][3],
+					      T dq[3][3][3], T & q2, T & q3,
+					      T & dq0, T & dq1) {
   const T q0 = (T) p.q0*(T) p.rredshift;
-  const T kappa0 = (T) p.kappa0*(T) p.redshift*(T) p.redshift;
-  const T kappa1 = (T) p.kappa1*(T) p.redshift*(T) p.redshift;
-  T q2 = T(0.0), q3 = T(0.0), dq0 = T(0.0), dq1 = T(0.0), efield = T(0.0);
+  q2 = T(0.0); q3 = T(0.0); dq0 = T(0.0); dq1 = T(0.0);
 
   #pragma unroll
   for (int ia = 0; ia < 3; ia++)
@@ -173,6 +174,17 @@ __device__ __forceinline__ T lc_fed_site(const P & p, T q[3][3],
       dq1 += sum*sum;
     }
   }
+}
+
+template <typename T, typename P>
+__device__ __forceinline__ T lc_fed_site(const P & p, T q[3][3],
+					 T dq[3][3][3]) {
+  const T r3 = T(1.0/3.0);
+  const T gamma = (T) p.gamma, a0 = (T) p.a0;
+  const T kappa0 = (T) p.kappa0*(T) p.redshift*(T) p.redshift;
+  const T kappa1 = (T) p.kappa1*(T) p.redshift*(T) p.redshift;
+  T q2, q3, dq0, dq1, efield = T(0.0);
+  lc_invariants<T>(p, q, dq, q2, q3, dq0, dq1);
   #pragma unroll
   for (int ia = 0; ia < 3; ia++) {
     const T ea = (T) p.e0[ia]*(T) p.coswt;
@@ -185,6 +197,25 @@ __device__ __forceinline__ T lc_fed_site(const P & p, T q[3][3],
   return T(0.5)*a0*(T(1.0) - r3*gamma)*q2 - r3*a0*gamma*q3
     + T(0.25)*a0*gamma*q2*q2 + T(0.5)*kappa0*dq0 + T(0.5)*kappa1*dq1
     - (T) p.epsilon*efield;
+}
+
+/* Bulk and gradient parts of the free-energy density, blue_phase_fbg
+ * (src/fe_lc_stats.c:721-806): no electric-field term */
+template <typename T, typename P>
+__device__ __forceinline__ void lc_fbg_site(const P & p, T q[3][3],
+					    T dq[3][3][3], T & fbulk,
+					    T & fgrad) {
+  const T r3 = T(1.0/3.0);
+  const T gamma = (T) p.gamma, a0 = (T) p.a0;
+  const T kappa0 = (T) p.kappa0*(T) p.redshift*(T) p.redshift;
+  const T kappa1 = (T) p.kappa1*(T) p.redshift*(T) p.redshift;
+  T q2, q3, dq0, dq1;
+  lc_invariants<T>(p, q, dq, q2, q3, dq0, dq1);
+  fbulk = T(0.5)*a0*(T(1.0) - r3*gamma)*q2;
+  fbulk = fbulk - r3*a0*gamma*q3;
+  fbulk = fbulk + T(0.25)*a0*gamma*q2*q2;
+  fgrad = T(0.5)*kappa0*dq0;
+  fgrad = fgrad + T(0.5)*kappa1*dq1;
 }
 
 template <typename T, typename P>

@@ -80,6 +80,10 @@ int lgbk_lc_h_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
 int lgbk_lc_fed_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
 		    const double * q, const double * grad, double * fed,
 		    void * stream);
+/* out: 3 x nsites = fed, bulk part, gradient part (blue_phase_fbg) */
+int lgbk_lc_fbg_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
+		    const double * q, const double * grad, double * out,
+		    void * stream);
 int lgbk_be_update_f64(const lgbk_dims_t * d, double xi, double gamma_rot,
 		       const uint8_t * status, const double * u,
 		       const double * flux, const double * h, double * q,

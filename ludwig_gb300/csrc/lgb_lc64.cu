@@ -73,6 +73,24 @@ __global__ void k_lc_fed(lgbk_dims_t d, lgbk_lc_t p,
   fed[i] = lc_fed_site<double>(p, qs, dq);
 }
 
+/* fed, bulk and gradient parts in three columns (the statistics of
+ * fe_lc_stats_info, src/fe_lc_stats.c:55-150) */
+__global__ void k_lc_fbg(lgbk_dims_t d, lgbk_lc_t p,
+			 const double * __restrict__ q,
+			 const double * __restrict__ grad,
+			 double * __restrict__ out) {
+  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (i >= d.nsites) return;
+  const long long N = d.nsites;
+  double qs[3][3], dq[3][3][3], fb, fg;
+  lc_expand(q, N, i, qs);
+  lc_expand_grad(grad, N, i, dq);
+  out[i] = lc_fed_site<double>(p, qs, dq);
+  lc_fbg_site<double>(p, qs, dq, fb, fg);
+  out[N + i] = fb;
+  out[2*N + i] = fg;
+}
+
 /* u and the fluxes may be NULL (no hydrodynamics: zero fluxes, no S) */
 __global__ void k_be_update(lgbk_dims_t d, double xi, double gamma_rot,
 			    const uint8_t * __restrict__ st,
@@ -182,6 +200,14 @@ int lgbk_lc_fed_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
 		    void * stream) {
   k_lc_fed<<<gridn(d->nsites), TPB, 0, (cudaStream_t) stream>>>(
     *d, *p, q, grad, fed);
+  return (int) cudaGetLastError();
+}
+
+int lgbk_lc_fbg_f64(const lgbk_dims_t * d, const lgbk_lc_t * p,
+		    const double * q, const double * grad, double * out,
+		    void * stream) {
+  k_lc_fbg<<<gridn(d->nsites), TPB, 0, (cudaStream_t) stream>>>(
+    *d, *p, q, grad, out);
   return (int) cudaGetLastError();
 }
 

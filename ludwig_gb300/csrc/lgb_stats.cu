@@ -138,6 +138,29 @@ __global__ void k_field_stats(long long n, const T * __restrict__ a,
   if (threadIdx.x == 0) write_partial<2>(part, k, vmin, vmax);
 }
 
+/* NK columns a[j*n + i] summed over the sites whose status is fluid (all
+ * sites when st is NULL); min and max of column 0 over the same sites */
+template <typename T, int NK>
+__global__ void k_masked_cols(long long n, const T * __restrict__ a,
+			      const uint8_t * __restrict__ st,
+			      double * __restrict__ part) {
+  Klein k[NK];
+  #pragma unroll
+  for (int j = 0; j < NK; j++) k[j].zero();
+  double vmin = +INFINITY, vmax = -INFINITY;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
+       i += (long long) gridDim.x*blockDim.x) {
+    if (st && st[i] != 0) continue;
+    #pragma unroll
+    for (int j = 0; j < NK; j++) k[j].add(ldv(a + j*n + i));
+    double v = ldv(a + i);
+    vmin = fmin(vmin, v);
+    vmax = fmax(vmax, v);
+  }
+  block_reduce<NK>(k, vmin, vmax);
+  if (threadIdx.x == 0) write_partial<NK>(part, k, vmin, vmax);
+}
+
 /* Distribution moments: mass and momentum of stored (possibly shifted) f */
 template <typename S>
 __global__ void k_dist_moments(long long n, const S * __restrict__ f,
@@ -232,6 +255,7 @@ static int finish(int nk, double * scratch, double * out_host,
   switch (nk) {
   case 1: k_final<1><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
   case 2: k_final<2><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  case 3: k_final<3><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
   default: k_final<4><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
   }
   cudaError_t err = cudaGetLastError();
@@ -257,6 +281,32 @@ extern "C" int lgbk_field_stats(const lgbk_dims_t * d, int prec,
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
   return finish(2, scratch, out_host, s);
+}
+
+extern "C" int lgbk_masked_cols(const lgbk_dims_t * d, int prec, int ncol,
+				const void * a, const uint8_t * status,
+				double * scratch, double * out_host,
+				void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  const long long n = d->nsites;
+  if (ncol == 1 && prec == LGBK_PREC_FP64) {
+    k_masked_cols<double, 1><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      n, (const double *) a, status, scratch);
+  }
+  else if (ncol == 1) {
+    k_masked_cols<float, 1><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      n, (const float *) a, status, scratch);
+  }
+  else if (ncol == 3 && prec == LGBK_PREC_FP64) {
+    k_masked_cols<double, 3><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
+      n, (const double *) a, status, scratch);
+  }
+  else {
+    return (int) cudaErrorInvalidValue;
+  }
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return finish(ncol, scratch, out_host, s);
 }
 
 extern "C" int lgbk_dist_moments(const lgbk_dims_t * d, int prec,

@@ -24,6 +24,12 @@ extern "C" {
 /* out = {sum, sum of squares, min, max} of n = nsites values */
 int lgbk_field_stats(const lgbk_dims_t * d, int prec, const void * a,
 		     double * scratch, double out_host[4], void * stream);
+/* ncol (1 or 3; 3 in FP64 only) columns a[j*nsites + i] summed over the
+ * sites with status 0 (all sites for status NULL): out = {sum_0 ..
+ * sum_{ncol-1}, min of column 0, max of column 0} */
+int lgbk_masked_cols(const lgbk_dims_t * d, int prec, int ncol, const void * a,
+		     const uint8_t * status, double * scratch,
+		     double * out_host, void * stream);
 /* out = {sum f, sum f c_x, sum f c_y, sum f c_z, min, max of site sums};
  * for shifted storage the sums are of f - w rho0 */
 int lgbk_dist_moments(const lgbk_dims_t * d, int prec, const void * f,

@@ -17,6 +17,7 @@
  *****************************************************************************/
 
 #include <assert.h>
+#include <float.h>
 #include <limits.h>
 #include <math.h>
 #include <stdarg.h>
@@ -287,6 +288,7 @@ struct lb_data_s {
   int ndist;                   /* 1, or 2 with the order parameter in g */
   void * g;                    /* ndist = 2: g and its second buffer */
   void * gprime;
+  lgb_io_state_t io;           /* snapshot files */
 };
 
 lb_data_options_t lb_data_options_default(void) {
@@ -494,6 +496,7 @@ struct field_s {
   char name[32];
   void * data;
   void * data2;                /* second buffer for the fused step */
+  lgb_io_state_t io;           /* snapshot files */
 };
 
 field_options_t field_options_ndata_nhalo(int ndata, int nhalo) {
@@ -753,6 +756,8 @@ struct hydro_s {
   void * u;
   void * u2;
   void * force;
+  lgb_io_state_t io_rho;       /* snapshot files "rho" and "vel" */
+  lgb_io_state_t io_vel;
 };
 
 hydro_options_t hydro_options_default(void) {
@@ -854,6 +859,7 @@ struct map_s {
   cs_t * cs;
   uint8_t * status;
   int all_fluid;
+  long long nfluid;
 };
 
 int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj) {
@@ -867,6 +873,7 @@ int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj) {
   if (m == NULL) return err_set(LUDWIG_GB_ENOMEM, "map_create");
   m->cs = cs;
   m->all_fluid = 1;
+  m->nfluid = cs->d.nsites;
   if ((rc = dev_alloc((void **) &m->status, (size_t) cs->d.nsites, "map"))) {
     free(m);
     return rc;
@@ -885,13 +892,15 @@ int map_free(map_t * m) {
 int map_status_from_host(map_t * m, const uint8_t * status) {
   if (m == NULL || status == NULL) return err_set(LUDWIG_GB_EINVAL, "map");
   long long n = m->cs->d.nsites;
-  m->all_fluid = 1;
+  long long nfluid = 0;
   for (long long i = 0; i < n; i++) {
     if (status[i] >= MAP_STATUS_MAX) {
       return err_set(LUDWIG_GB_EINVAL, "map status value out of range");
     }
-    if (status[i] != MAP_FLUID) m->all_fluid = 0;
+    if (status[i] == MAP_FLUID) nfluid += 1;
   }
+  m->nfluid = nfluid;
+  m->all_fluid = (nfluid == n);
   CK(cudaMemcpyAsync(m->status, status, (size_t) n, cudaMemcpyHostToDevice,
 		     stream_), "map");
   CK(cudaStreamSynchronize(stream_), "sync");
@@ -1226,6 +1235,41 @@ int stats_free_energy_lc(fe_lc_t * fe, double * total) {
   return LUDWIG_GB_OK;
 }
 
+/* The statistics fe_lc_stats_info prints without walls or colloids
+ * (src/fe_lc_stats.c:55-150): out = {f, v, f/v, f_bulk/v, f_grad/v,
+ * redshift}, sums over the fluid sites of the map (all sites for map
+ * NULL).  Needs field_grad_compute() on the q gradients first. */
+int fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]) {
+  if (fe == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
+  int rc = lc_ready(fe);
+  if (rc) return rc;
+  const lgbk_dims_t * d = &fe->q->cs->d;
+  if (map && map->cs->d.nsites != d->nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "fe_lc_stats_info: map size");
+  }
+  double * tmp = NULL, * scr = NULL, r[5];
+  if ((rc = red_scratch(&scr))) return rc;
+  rc = dev_alloc((void **) &tmp, (size_t) 3*d->nsites*sizeof(double), "fbg");
+  if (rc) return rc;
+  lgbk_lc_t k;
+  lc_kparam(fe, &k);
+  const uint8_t * st = (map && !map->all_fluid) ? map->status : NULL;
+  rc = lgbk_lc_fbg_f64(d, &k, (const double *) fe->q->data, fe->dq->grad,
+		       tmp, stream_);
+  if (rc == 0) rc = lgbk_masked_cols(d, LGBK_PREC_FP64, 3, tmp, st, scr, r,
+				     stream_);
+  dev_free(tmp);
+  if (rc) return cuda_check(rc, "fe_lc_stats_info");
+  double v = (double) (map ? map->nfluid : d->nsites);
+  out[0] = r[0];
+  out[1] = v;
+  out[2] = r[0]/v;
+  out[3] = r[1]/v;
+  out[4] = r[2]/v;
+  out[5] = fe->param.redshift;
+  return LUDWIG_GB_OK;
+}
+
 static int lc_fed(fe_t * base, int index, double * fed) {
   return lc_site_eval((fe_lc_t *) base, index, 0, fed);
 }
@@ -1354,6 +1398,78 @@ int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
 	h[4*N + i] = a*(root2*cosz*cosx + root2*siny*sinx - siny*cosz);
       }
     }
+  }
+  int rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
+/* Blue phase II, src/blue_phase_init.c:155-235 (no rotation) */
+int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
+		       const double euler_angles[3]) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O2_init");
+  }
+  if (euler_angles && (euler_angles[0] != 0.0 || euler_angles[1] != 0.0 ||
+		       euler_angles[2] != 0.0)) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O2_init: rotation not "
+		   "supported");
+  }
+  const lgbk_dims_t * d = &cs->d;
+  const long long N = d->nsites;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "o2");
+  const double q0 = param->q0, a = param->amplitude0;
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	long long i = ((long long) x*d->ny + y)*d->nz + z;
+	double r[3];
+	r[0] = (double) (x + 1) - 0.5*d->nx;
+	r[1] = (double) (y + 1) - 0.5*d->ny;
+	r[2] = (double) (z + 1) - 0.5*d->nz;
+	r[0] += 0.5*d->nx; r[1] += 0.5*d->ny; r[2] += 0.5*d->nz;
+	double cosx = cos(2.0*q0*r[0]), sinx = sin(2.0*q0*r[0]);
+	double cosy = cos(2.0*q0*r[1]), siny = sin(2.0*q0*r[1]);
+	double cosz = cos(2.0*q0*r[2]), sinz = sin(2.0*q0*r[2]);
+	h[0*N + i] = a*(cosz - cosy);
+	h[1*N + i] = a*sinz;
+	h[2*N + i] = a*siny;
+	h[3*N + i] = a*(cosx - cosz);
+	h[4*N + i] = a*sinx;
+      }
+    }
+  }
+  int rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
+/* Uniform uniaxial nematic along n (normalised here),
+ * src/blue_phase_init.c:836-872 with fe_lc_q_uniaxial,
+ * src/blue_phase.c:1406: Q_ab = (A/2)(3 n_a n_b - d_ab) */
+int blue_phase_nematic_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
+			    const double n[3]) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5 || n == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_nematic_init");
+  }
+  const double mod = sqrt(n[0]*n[0] + n[1]*n[1] + n[2]*n[2]);
+  if (!(mod > 0.0)) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_nematic_init: |n| = 0");
+  }
+  double nh[3], q[3][3];
+  for (int a = 0; a < 3; a++) nh[a] = n[a]/mod;
+  for (int a = 0; a < 3; a++) {
+    for (int b = 0; b < 3; b++) {
+      q[a][b] = 0.5*param->amplitude0*(3.0*nh[a]*nh[b] - (double) (a == b));
+    }
+  }
+  const double q5[5] = {q[0][0], q[0][1], q[0][2], q[1][1], q[1][2]};
+  const long long N = cs->d.nsites;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "nematic");
+  for (int c = 0; c < 5; c++) {
+    for (long long i = 0; i < N; i++) h[c*N + i] = q5[c];
   }
   int rc = field_from_host(fq, h);
   free(h);
@@ -1992,6 +2108,34 @@ int stats_field_q(field_t * field, int n, double out[5]) {
   return LUDWIG_GB_OK;
 }
 
+/* Velocity statistics, src/stats_velocity.c:54-125: out = {min u_x, u_y,
+ * u_z, max u_x, u_y, u_z, volume flux (sum u) x, y, z} over the fluid
+ * sites of the map (all sites for map NULL).  As there, the minimum
+ * starts from FLT_MAX and the maximum from FLT_MIN (the smallest positive
+ * float), so a component that is negative everywhere reports FLT_MIN as
+ * its maximum. */
+int stats_velocity_minmax(hydro_t * hydro, map_t * map, double out[9]) {
+  if (hydro == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
+  const lgbk_dims_t * d = &hydro->cs->d;
+  if (map && map->cs->d.nsites != d->nsites) {
+    return err_set(LUDWIG_GB_EINVAL, "stats_velocity_minmax: map size");
+  }
+  double * scr = NULL, r[3];
+  int rc = red_scratch(&scr);
+  if (rc) return rc;
+  const uint8_t * st = (map && !map->all_fluid) ? map->status : NULL;
+  for (int a = 0; a < 3; a++) {
+    const char * u = (const char *) hydro->u
+      + (size_t) a*d->nsites*field_size(hydro->prec);
+    CK(lgbk_masked_cols(d, field_kprec(hydro->prec), 1, u, st, scr, r,
+			stream_), "stats_velocity");
+    out[a] = fmin((double) FLT_MAX, r[1]);
+    out[3 + a] = fmax((double) FLT_MIN, r[2]);
+    out[6 + a] = r[0];
+  }
+  return LUDWIG_GB_OK;
+}
+
 int stats_distribution(lb_t * lb, double out[4]) {
   if (lb == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
   double * scr = NULL, r[6];
@@ -2152,6 +2296,112 @@ int ludwig_gb_time_binary_e2e(lb_t * lb, field_t * phi, hydro_t * hydro,
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return rc;
+}
+
+/* End to end with the copies of consecutive steps overlapped: every step
+ * copies the same host input (in_*: stored f, phi, u) to the device, takes
+ * one fused step and copies the result (out_*: f, phi, u, rho) back.  Two
+ * device buffer sets alternate between steps, and three streams (host to
+ * device, step, device to host) let the upload of step k+1 run while the
+ * download of step k does.  On return the objects hold the input state. */
+int ludwig_gb_time_binary_e2e_overlap(lb_t * lb, field_t * phi,
+				      hydro_t * hydro, map_t * map, fe_t * fe,
+				      int nsteps, const void * in_f,
+				      const void * in_phi, const void * in_u,
+				      void * out_f, void * out_phi,
+				      void * out_u, void * out_rho,
+				      double * ms) {
+  if (ms == NULL || nsteps < 1 || in_f == NULL || in_phi == NULL ||
+      in_u == NULL || out_f == NULL || out_phi == NULL || out_u == NULL ||
+      out_rho == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "time_binary_e2e_overlap");
+  }
+  lgbk_binary_args_t a[2];
+  int rc = binary_args(lb, phi, hydro, map, fe, &a[0]);
+  if (rc) return rc;
+  if ((rc = lb_unstream(lb))) return rc;
+  a[0].f_in = lb->f;       a[0].f_out = lb->fprime;
+  a[0].phi_in = phi->data; a[0].phi_out = phi->data2;
+  a[0].u_in = hydro->u;    a[0].u_out = hydro->u2;
+  a[0].rho_out = hydro->rho;
+  size_t fb, pb, ub;
+  ludwig_gb_state_bytes(lb, &fb, &pb, &ub);
+  const size_t sz[7] = {fb, fb, pb, pb, ub, ub, pb};
+  void * b[7] = {NULL};
+  for (int k = 0; rc == 0 && k < 7; k++) rc = dev_alloc(b + k, sz[k], "e2e");
+  a[1] = a[0];
+  a[1].f_in = b[0];   a[1].f_out = b[1];
+  a[1].phi_in = b[2]; a[1].phi_out = b[3];
+  a[1].u_in = b[4];   a[1].u_out = b[5];
+  a[1].rho_out = b[6];
+  const lgbk_dims_t * d = &lb->cs->d;
+  cudaStream_t st[3] = {NULL, NULL, NULL};
+  cudaEvent_t ev[3][2], e0 = NULL, e1 = NULL;
+  memset(ev, 0, sizeof(ev));
+  for (int i = 0; rc == 0 && i < 3; i++) {
+    rc = cuda_check(cudaStreamCreateWithFlags(st + i, cudaStreamNonBlocking),
+		    "stream");
+    for (int x = 0; rc == 0 && x < 2; x++) {
+      rc = cuda_check(cudaEventCreateWithFlags(&ev[i][x],
+					       cudaEventDisableTiming), "event");
+    }
+  }
+  if (rc == 0) rc = cuda_check(cudaEventCreate(&e0), "event");
+  if (rc == 0) rc = cuda_check(cudaEventCreate(&e1), "event");
+  /* start after everything queued on the library stream */
+  if (rc == 0) rc = cuda_check(cudaStreamSynchronize(stream_), "sync");
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e0, st[0]), "record");
+  for (int k = 0; rc == 0 && k < nsteps; k++) {
+    const int x = k & 1;
+    const lgbk_binary_args_t * ax = a + x;
+    /* upload: buffer set x is free once its previous download is done */
+    if (k >= 2) rc = cuda_check(cudaStreamWaitEvent(st[0], ev[2][x], 0),
+				"wait");
+    if (rc == 0) rc = cudaMemcpyAsync((void *) ax->f_in, in_f, fb,
+				      cudaMemcpyHostToDevice, st[0]);
+    if (rc == 0) rc = cudaMemcpyAsync((void *) ax->phi_in, in_phi, pb,
+				      cudaMemcpyHostToDevice, st[0]);
+    if (rc == 0) rc = cudaMemcpyAsync((void *) ax->u_in, in_u, ub,
+				      cudaMemcpyHostToDevice, st[0]);
+    if (rc == 0) rc = cudaEventRecord(ev[0][x], st[0]);
+    /* step */
+    if (rc == 0) rc = cudaStreamWaitEvent(st[1], ev[0][x], 0);
+    if (rc == 0) rc = lgbk_binary_step(d, lb->prec, ax, tune_xchunk_, tune_ty_,
+				       tune_minb_, st[1]);
+    if (rc == 0) rc = cudaEventRecord(ev[1][x], st[1]);
+    /* download */
+    if (rc == 0) rc = cudaStreamWaitEvent(st[2], ev[1][x], 0);
+    if (rc == 0) rc = cudaMemcpyAsync(out_f, ax->f_out, fb,
+				      cudaMemcpyDeviceToHost, st[2]);
+    if (rc == 0) rc = cudaMemcpyAsync(out_phi, ax->phi_out, pb,
+				      cudaMemcpyDeviceToHost, st[2]);
+    if (rc == 0) rc = cudaMemcpyAsync(out_u, ax->u_out, ub,
+				      cudaMemcpyDeviceToHost, st[2]);
+    if (rc == 0) rc = cudaMemcpyAsync(out_rho, ax->rho_out, pb,
+				      cudaMemcpyDeviceToHost, st[2]);
+    if (rc == 0) rc = cudaEventRecord(ev[2][x], st[2]);
+    if (rc) rc = cuda_check(rc, "e2e_overlap");
+  }
+  if (rc == 0) rc = cuda_check(cudaEventRecord(e1, st[2]), "record");
+  if (rc == 0) rc = cuda_check(cudaEventSynchronize(e1), "sync");
+  if (rc == 0) {
+    float t = 0.0f;
+    rc = cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+  }
+  for (int i = 0; i < 3; i++) {
+    if (st[i]) cudaStreamSynchronize(st[i]);
+  }
+  for (int i = 0; i < 3; i++) {
+    for (int x = 0; x < 2; x++) if (ev[i][x]) cudaEventDestroy(ev[i][x]);
+    if (st[i]) cudaStreamDestroy(st[i]);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  for (int k = 0; k < 7; k++) dev_free(b[k]);
+  /* set 0 holds the uploaded input: f in the stored, unstreamed form */
+  lb->pending = 1;
   return rc;
 }
 
@@ -2692,6 +2942,43 @@ int lgb_internal_binary_view(lb_t * lb, field_t * phi, hydro_t * hydro,
 int lgb_internal_lb_set_pending(lb_t * lb, int pending) {
   if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb");
   lb->pending = pending ? 1 : 0;
+  return LUDWIG_GB_OK;
+}
+
+int lgb_internal_lb_io(lb_t * lb, int ntotal[3], int * ndist,
+		       lgb_io_state_t ** io) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "lb");
+  for (int a = 0; a < 3; a++) ntotal[a] = lb->cs->ntotal[a];
+  *ndist = lb->ndist;
+  *io = &lb->io;
+  if (lb->io.fmt_in == 0) lb->io.fmt_in = IO_RECORD_BINARY;
+  if (lb->io.fmt_out == 0) lb->io.fmt_out = IO_RECORD_BINARY;
+  return LUDWIG_GB_OK;
+}
+
+int lgb_internal_field_io(field_t * f, int ntotal[3], int * nf,
+			  const char ** name, lgb_io_state_t ** io) {
+  if (f == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  for (int a = 0; a < 3; a++) ntotal[a] = f->cs->ntotal[a];
+  *nf = f->nf;
+  *name = f->name;
+  *io = &f->io;
+  if (f->io.fmt_in == 0) f->io.fmt_in = IO_RECORD_BINARY;
+  if (f->io.fmt_out == 0) f->io.fmt_out = IO_RECORD_BINARY;
+  return LUDWIG_GB_OK;
+}
+
+int lgb_internal_hydro_io(hydro_t * h, int ntotal[3], lgb_io_state_t ** rho,
+			  lgb_io_state_t ** vel) {
+  if (h == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro");
+  for (int a = 0; a < 3; a++) ntotal[a] = h->cs->ntotal[a];
+  lgb_io_state_t * s[2] = {&h->io_rho, &h->io_vel};
+  for (int k = 0; k < 2; k++) {
+    if (s[k]->fmt_in == 0) s[k]->fmt_in = IO_RECORD_BINARY;
+    if (s[k]->fmt_out == 0) s[k]->fmt_out = IO_RECORD_BINARY;
+  }
+  *rho = s[0];
+  *vel = s[1];
   return LUDWIG_GB_OK;
 }
 

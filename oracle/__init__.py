@@ -639,3 +639,88 @@ def conv3_wgrad(n, g, a):
     L.orc_conv3_wgrad(_I3(*n), pg, pa, dw.ctypes.data_as(_P),
                       db.ctypes.data_as(_P))
     return dw, db
+
+
+# ---------------------------------------------------------------------------
+# Snapshot files (restatement of the reference's file format)
+# ---------------------------------------------------------------------------
+
+def _metadata_json(L, fmt, count):
+    """The JSON of io_metadata_to_json (src/io_metadata.c:159) as cJSON
+    prints it, for one rank and one file."""
+    b = fmt == "binary"
+    t = "\t"
+    lines = [
+        "{",
+        t + '"coords":' + t + "{",
+        t * 2 + '"options":' + t + "{",
+        t * 3 + '"System size (total)":' + t + "[%d, %d, %d]," % tuple(L),
+        t * 3 + '"Periodic boundaries":' + t + "[1, 1, 1],",
+        t * 3 + '"Left-end limit Lmin":' + t + "[0.5, 0.5, 0.5]",
+        t * 2 + "},",
+        t * 2 + '"lees_edwards":' + t + "{",
+        t * 3 + '"Number of planes":' + t + "0",
+        t * 2 + "}",
+        t + "},",
+        t + '"io_options":' + t + "{",
+        t * 2 + '"Mode":' + t + '"mpiio",',
+        t * 2 + '"Record format":' + t + '"%s",' % fmt,
+        t * 2 + '"Metadata version":' + t + "3,",
+        t * 2 + '"Report":' + t + "false,",
+        t * 2 + '"Asynchronous":' + t + "false,",
+        t * 2 + '"Compression level":' + t + "0,",
+        t * 2 + '"I/O grid":' + t + "[1, 1, 1]",
+        t + "},",
+        t + '"io_element":' + t + "{",
+        t * 2 + '"MPI_Datatype":' + t + ('"MPI_DOUBLE",' if b
+                                         else '"MPI_CHAR",'),
+        t * 2 + '"Size (bytes)":' + t + ("8," if b else "1,"),
+        t * 2 + '"Count":' + t + "%d," % count,
+        t * 2 + '"Endianness":' + t + '"LITTLE_ENDIAN"',
+        t + "},",
+        t + '"io_subfile":' + t + "{",
+        t * 2 + '"Number of files":' + t + "1,",
+        t * 2 + '"File index":' + t + "0,",
+        t * 2 + '"Topology":' + t + "[1, 1, 1],",
+        t * 2 + '"Coordinate":' + t + "[0, 0, 0],",
+        t * 2 + '"Data ndims":' + t + "3,",
+        t * 2 + '"File size (sites)":' + t + "[%d, %d, %d]," % tuple(L),
+        t * 2 + '"File offset (sites)":' + t + "[0, 0, 0]",
+        t + "}",
+        "}"]
+    return "\n".join(lines).encode()
+
+
+def snapshot_files(L, step, f=None, ndist=1, fields=None, fmt="binary"):
+    """{file name: bytes} of lb_io_write (src/lb_data.c:1716, records of
+    lb_write_buf(_ascii) :1533-1610) and field_io_write (src/field.c:1633,
+    records of field_write_buf(_ascii) :896-965; hydro_io_write,
+    src/hydro.c:941, writes the fields "rho" and "vel") for
+    component-major arrays f [ndist*19, L] and fields {name: [nf, L]}:
+    sites in x, y, z order."""
+    out = {}
+    n = L[0] * L[1] * L[2]
+
+    def records(a, nrow, ncol):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(ncol, nrow, n)
+        if fmt == "binary":
+            # record: value (col, row) at col*nrow + row
+            return np.ascontiguousarray(
+                a.transpose(2, 0, 1)).astype("<f8").tobytes()
+        buf = []
+        for i in range(n):
+            for r in range(nrow):
+                buf.append("".join(" %22.15e" % a[c, r, i]
+                                   for c in range(ncol)) + "\n")
+        return "".join(buf).encode()
+
+    if f is not None:
+        cnt = ndist * 19 if fmt == "binary" else 19 * (ndist * 23 + 1)
+        out["dist-metadata.001-001"] = _metadata_json(L, fmt, cnt)
+        out["dist-%09d.001-001" % step] = records(f, 19, ndist)
+    for stub, a in (fields or {}).items():
+        nf = a.shape[0]
+        cnt = nf if fmt == "binary" else nf * 23 + 1
+        out["%s-metadata.001-001" % stub] = _metadata_json(L, fmt, cnt)
+        out["%s-%09d.001-001" % (stub, step)] = records(a, 1, nf)
+    return out

@@ -30,6 +30,12 @@
  *    ref_shim mode=lc_fields size=.. (lc parameters) in=PREFIX out=PREFIX
  *    ref_shim mode=lc_be    size=.. (lc parameters) in=PREFIX out=PREFIX
  *    ref_shim mode=lc_step  size=.. (lc parameters) steps= in=PREFIX out=PREFIX
+ *    ref_shim mode=io_write size=.. ndist=1|2 nf=1|5 fmt=binary|ascii
+ *                           step=N in=PREFIX dir=DIR [hydro=1]
+ *                           (lb_io_write, field_io_write and, with
+ *                           hydro=1, hydro_io_write into DIR)
+ *    ref_shim mode=io_read  size=.. ndist= nf= fmt= step=N dir=DIR out=PREFIX
+ *                           (lb_io_read and field_io_read from DIR)
  *  Any mode accepts status=FILE (uint8 per site, canonical order; 0 fluid).
  *
  *  The call sequence of mode=run/step follows src/ludwig.c:528-860 for
@@ -69,6 +75,8 @@
 #include "colloids.h"
 #include "phi_lb_coupler.h"
 #include "advection.h"
+#include "io_event.h"
+#include <unistd.h>
 
 static const char * arg(int argc, char ** argv, const char * key,
 			const char * def) {
@@ -471,6 +479,108 @@ static int lc_main(int argc, char ** argv, const char * mode) {
   return 0;
 }
 
+/* Snapshot files through the reference's own I/O (src/lb_data.c:1716-1830,
+ * src/field.c:1633-1737): one file per object, single rank. */
+static int io_main(int argc, char ** argv, const char * mode) {
+  const int ndist = atoi(arg(argc, argv, "ndist", "1"));
+  const int nf = atoi(arg(argc, argv, "nf", "1"));
+  const int step = atoi(arg(argc, argv, "step", "0"));
+  const char * dir = arg(argc, argv, "dir", ".");
+  const io_record_format_enum_t fmt =
+    strcmp(arg(argc, argv, "fmt", "binary"), "ascii") == 0
+    ? IO_RECORD_ASCII : IO_RECORD_BINARY;
+  pe_t * pe = NULL;
+  cs_t * cs = NULL;
+  lb_t * lb = NULL;
+  field_t * fld = NULL;
+  pe_create(MPI_COMM_WORLD, PE_QUIET, &pe);
+  cs_create(pe, &cs);
+  cs_nhalo_set(cs, 2);
+  cs_ntotal_set(cs, L);
+  cs_init(cs);
+  {
+    lb_data_options_t opts = lb_data_options_default();
+    opts.ndist = ndist;
+    opts.iodata.input.iorformat = fmt;
+    opts.iodata.output.iorformat = fmt;
+    lb_data_create(pe, cs, &opts, &lb);
+  }
+  {
+    field_options_t opts = field_options_ndata_nhalo(nf, 2);
+    opts.iodata.input.iorformat = fmt;
+    opts.iodata.output.iorformat = fmt;
+    field_create(pe, cs, NULL, (nf == 5) ? "q" : "phi", &opts, &fld);
+  }
+  hydro_t * hydro = NULL;
+  if (atoi(arg(argc, argv, "hydro", "0"))) {
+    hydro_options_t opts = hydro_options_default();
+    opts.rho.iodata.input.iorformat = fmt;
+    opts.rho.iodata.output.iorformat = fmt;
+    opts.u.iodata.input.iorformat = fmt;
+    opts.u.iodata.output.iorformat = fmt;
+    hydro_create(pe, cs, NULL, &opts, &hydro);
+  }
+  const size_t n = nint();
+  io_event_t event = {0};
+  if (strcmp(mode, "io_write") == 0 && hydro) {
+    const char * in = arg(argc, argv, "in", NULL);
+    double * rho = readf(in, "rho", n);
+    double * u = readf(in, "u", 3*n);
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(cs, x+1, y+1, z+1);
+	field_t * fr = hydro->rho, * fu = hydro->u;
+	fr->data[addr_rank1(fr->nsites, 1, index, 0)] = rho[canon(0,x,y,z)];
+	for (int a = 0; a < 3; a++)
+	  fu->data[addr_rank1(fu->nsites, 3, index, a)] = u[canon(a,x,y,z)];
+      }
+    hydro_memcpy(hydro, tdpMemcpyHostToDevice);
+  }
+  if (strcmp(mode, "io_write") == 0) {
+    const char * in = arg(argc, argv, "in", NULL);
+    double * f = readf(in, "f", (size_t) ndist*NVEL*n);
+    double * q = readf(in, "phi", (size_t) nf*n);
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(cs, x+1, y+1, z+1);
+	for (int d = 0; d < ndist; d++) for (int p = 0; p < NVEL; p++)
+	  lb->f[LB_ADDR(lb->nsite, ndist, NVEL, index, d, p)]
+	    = f[canon(d*NVEL + p, x, y, z)];
+	for (int c = 0; c < nf; c++)
+	  fld->data[addr_rank1(fld->nsites, nf, index, c)] = q[canon(c,x,y,z)];
+      }
+    lb_memcpy(lb, tdpMemcpyHostToDevice);
+    field_memcpy(fld, tdpMemcpyHostToDevice);
+    if (chdir(dir) != 0) return 2;
+    if (lb_io_write(lb, step, &event)) return 3;
+    if (field_io_write(fld, step, &event)) return 3;
+    if (hydro && hydro_io_write(hydro, step, &event)) return 3;
+  }
+  else {
+    const char * out = arg(argc, argv, "out", "ref");
+    char cwd[1024];
+    if (getcwd(cwd, sizeof(cwd)) == NULL || chdir(dir) != 0) return 2;
+    if (lb_io_read(lb, step, &event)) return 3;
+    if (field_io_read(fld, step, &event)) return 3;
+    if (chdir(cwd) != 0) return 2;
+    double * f = malloc((size_t) ndist*NVEL*n*sizeof(double));
+    double * q = malloc((size_t) nf*n*sizeof(double));
+    for (int x = 0; x < L[0]; x++) for (int y = 0; y < L[1]; y++)
+      for (int z = 0; z < L[2]; z++) {
+	int index = cs_index(cs, x+1, y+1, z+1);
+	for (int d = 0; d < ndist; d++) for (int p = 0; p < NVEL; p++)
+	  f[canon(d*NVEL + p, x, y, z)]
+	    = lb->f[LB_ADDR(lb->nsite, ndist, NVEL, index, d, p)];
+	for (int c = 0; c < nf; c++)
+	  q[canon(c,x,y,z)] = fld->data[addr_rank1(fld->nsites, nf, index, c)];
+      }
+    writef(out, "f", f, (size_t) ndist*NVEL*n);
+    writef(out, "phi", q, (size_t) nf*n);
+  }
+  MPI_Finalize();
+  return 0;
+}
+
 int main(int argc, char ** argv) {
 
   const char * mode = arg(argc, argv, "mode", "run");
@@ -484,6 +594,7 @@ int main(int argc, char ** argv) {
 	     L, L+1, L+2) != 3) return 2;
 
   if (strncmp(mode, "lc", 2) == 0) return lc_main(argc, argv, mode);
+  if (strncmp(mode, "io_", 3) == 0) return io_main(argc, argv, mode);
 
   sys_create(argc, argv, &s);
 

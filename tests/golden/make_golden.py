@@ -7,7 +7,7 @@ phi_force_calculation, phi_cahn_hilliard and the main-loop step of
 src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
 
 Needs the reference sources (only where they are present):
-    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2|grad27|logs|advection]
+    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2|grad27|logs|advection|io]
 """
 
 import os
@@ -160,7 +160,8 @@ def grad27_cases():
 
 
 REGRESSION_LOGS = ("serial-spin-fd1", "serial-spin-lb1", "serial-init-bp1",
-                   "serial-symm-dr1")
+                   "serial-symm-dr1", "serial-init-bp2", "serial-relx-bp1",
+                   "serial-chol-fld")
 
 
 def parse_log(path):
@@ -214,6 +215,46 @@ def advection_cases():
     run_case("run_adv3_g27_8x8x8_s20", (8, 8, 8), 20, 99, order=3, grad=27)
 
 
+IO_CASES = (("io_d1_phi_bin", (3, 2, 2), 1, 1, "binary", 10, 1),
+            ("io_d2_phi_asc", (3, 2, 2), 2, 1, "ascii", 20, 1),
+            ("io_d1_q_asc", (2, 3, 2), 1, 5, "ascii", 0, 0),
+            ("io_d1_q_bin", (4, 2, 3), 1, 5, "binary", 123456789, 0))
+
+
+def io_cases():
+    """Snapshot files written by the reference's lb_io_write and
+    field_io_write (src/lb_data.c:1716, src/field.c:1633), with the
+    arrays that went in; each file's bytes are kept."""
+    rng = np.random.default_rng(20251)
+    for name, L, ndist, nf, fmt, step, hydro in IO_CASES:
+        n = L[0] * L[1] * L[2]
+        f = (rng.standard_normal((ndist * 19,) + L) * 0.05
+             + 1.0 / 19.0)
+        q = rng.standard_normal((nf,) + L) * 0.3
+        q.flat[0] = 1.0e-300          # exponent with three digits
+        rho = 1.0 + 0.01 * rng.standard_normal((1,) + L)
+        u = 0.02 * rng.standard_normal((3,) + L)
+        with tempfile.TemporaryDirectory() as tmp:
+            pin = os.path.join(tmp, "in")
+            oracle.write_arrays(pin, f=f, phi=q, rho=rho, u=u)
+            d = os.path.join(tmp, "files")
+            os.mkdir(d)
+            oracle.run_reference(kv(L, mode="io_write", ndist=ndist, nf=nf,
+                                    fmt=fmt, step=step, dir=d, hydro=hydro,
+                                    **{"in": pin}))
+            res = {"L": np.array(L), "ndist": ndist, "nf": nf, "fmt": fmt,
+                   "step": step, "in_f": f, "in_phi": q, "hydro": hydro}
+            if hydro:
+                res.update(in_rho=rho, in_u=u)
+            names = sorted(os.listdir(d))
+            res["files"] = np.array(names)
+            for k, fn in enumerate(names):
+                with open(os.path.join(d, fn), "rb") as fh:
+                    res["file%d" % k] = np.frombuffer(fh.read(), np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print("wrote", name, n, "sites", names)
+
+
 def main(ref_root, only=None):
     if not oracle.build_reference(ref_root):
         raise SystemExit("reference sources not found at " + ref_root)
@@ -228,6 +269,9 @@ def main(ref_root, only=None):
         return
     if only == "advection":
         advection_cases()
+        return
+    if only == "io":
+        io_cases()
         return
     rng = np.random.default_rng(20261203)
 
@@ -266,6 +310,7 @@ def main(ref_root, only=None):
     lb2_cases()
     grad27_cases()
     advection_cases()
+    io_cases()
     regression_logs(ref_root)
 
 

@@ -184,3 +184,23 @@ def test_oracle_advection_orders_match_reference(orc, name):
     finally:
         lib.orc_advection_order_set(1)
         lib.orc_gradient_stencil_set(7)
+
+
+IO_CASES = ["io_d1_phi_bin", "io_d2_phi_asc", "io_d1_q_asc", "io_d1_q_bin"]
+
+
+@pytest.mark.parametrize("name", IO_CASES)
+def test_oracle_snapshot_files_match_reference(orc, name):
+    """Snapshot files of lb_io_write / field_io_write, byte for byte."""
+    g = load(name)
+    nf = int(g["nf"])
+    fields = {"q" if nf == 5 else "phi": g["in_phi"]}
+    if int(g["hydro"]):
+        fields.update(rho=g["in_rho"], vel=g["in_u"])
+    got = orc.snapshot_files(L_of(g), int(g["step"]), f=g["in_f"],
+                             ndist=int(g["ndist"]), fields=fields,
+                             fmt=str(g["fmt"]))
+    names = [str(s) for s in g["files"]]
+    assert sorted(got) == names
+    for k, fn in enumerate(names):
+        assert got[fn] == g["file%d" % k].tobytes(), fn

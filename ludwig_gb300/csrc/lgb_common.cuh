@@ -112,19 +112,6 @@ __device__ __forceinline__ T lgb_symm_p0(const lgbk_symm_t & fe, T phi,
   return lgb_symm_p0<T>((T) fe.a, (T) fe.b, (T) fe.kappa, phi, delsq, g);
 }
 
-#ifndef LGB_MASS_SUM
-#define LGB_MASS_SUM 2
-#endif
-
-/* s + c += x with the rounding error of the addition kept in c
- * (Neumaier's compensated summation) */
-template <typename T>
-__device__ __forceinline__ void lgb_sum2(T & s, T & c, T x) {
-  const T t = s + x;
-  c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
-  s = t;
-}
-
 /* Sum of populations fs[p0..18] as h + l with h exact (error-free
  * splitting, as in Rump, Ogita and Oishi's AccSum): for |x| < 8 and
  * C = 1.5*2^4, fl(x + C) - C is x rounded to a multiple of ulp(C) = 2^-19
@@ -176,7 +163,6 @@ __device__ __forceinline__ void lgb_mass(const T fs[LGB_NVEL], T & h, T & l) {
   lgb_mass_split<T, P0>(fs, h, l);
 }
 
-#if LGB_MASS_SUM == 2
 template <>
 __device__ __forceinline__ void lgb_mass<float, 0>(const float fs[LGB_NVEL],
 						   float & h, float & l) {
@@ -187,7 +173,6 @@ __device__ __forceinline__ void lgb_mass<float, 1>(const float fs[LGB_NVEL],
 						   float & h, float & l) {
   lgb_mass_split2<1>(fs, h, l);
 }
-#endif
 
 /*****************************************************************************
  *
@@ -236,17 +221,9 @@ __device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
   constexpr int NM = GZERO ? 10 : LGB_NVEL;
 
   /* Reduced precision: the mass of the incoming populations as an
-   * unevaluated sum hi + lo (compensated, Neumaier) */
+   * unevaluated sum hi + lo, hi exact (error-free splitting) */
   T mass_hi = T(0.0), mass_lo = T(0.0);
-  if (!SEQ) {
-#if LGB_MASS_SUM == 0
-    mass_hi = fs[0];
-    #pragma unroll
-    for (int p = 1; p < LGB_NVEL; p++) lgb_sum2(mass_hi, mass_lo, fs[p]);
-#else
-    lgb_mass<T, 0>(fs, mass_hi, mass_lo);
-#endif
-  }
+  if (!SEQ) lgb_mass<T, 0>(fs, mass_hi, mass_lo);
 
   if (SEQ) d3q19_f2mode_seq<T, NM>(fs, mode);
   else     d3q19_f2mode_fast<T, NM>(fs, mode);
@@ -320,16 +297,9 @@ __device__ __forceinline__ void lgb_collide_site_sth(T rtau, T rtau_bulk,
      * error-free (split) sums on both sides, so that the populations' sum
      * equals the incoming sum up to one rounding of the rest population
      * and the rounding of the small remainders. */
-#if LGB_MASS_SUM == 0
-    T s = mass_hi, c = mass_lo;
-    #pragma unroll
-    for (int p = 1; p < LGB_NVEL; p++) lgb_sum2(s, c, -fs[p]);
-    fs[0] = s + c;
-#else
     T h, l;
     lgb_mass<T, 1>(fs, h, l);
     fs[0] = (mass_hi - h) + (mass_lo - l);
-#endif
   }
 
   rho_out = rho;

@@ -289,6 +289,223 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
     for (int ib = 0; ib < 3; ib++) sth[ia][ib] = -sth[ia][ib];
 }
 
+/*****************************************************************************
+ *
+ *  Reduced-operation forms for the float path (any summation order is
+ *  allowed there).  The reference's loops above carry every Levi-Civita
+ *  and Kronecker product, zeros included (a product by a zero constant
+ *  cannot be dropped under IEEE rules); written with the intermediates
+ *  below, the same quantities take about a third of the operations:
+ *
+ *    R_ab  = e_acd d_c Q_bd         (curl of Q; tr R is the pseudoscalar)
+ *    QQ_ab = Q_ac Q_bc              (q3 = QQ_ab Q_ab)
+ *    v_c   = d_d Q_cd               (dq0 = v.v; the kappa0 stress term)
+ *    M_ab  = H_ac Qt_cb, Qt = Q + I/3  (the xi terms and [Q, H])
+ *    G_ab  = d_a Q_cd d_b Q_cd,  X_ab = d_a Q_cd d_c Q_bd
+ *    C_ab  = e_bce d_a Q_cd Q_de    (from the off-diagonal of dQ_a . Q)
+ *
+ *  H (src/blue_phase.c:1016-1110):
+ *    H = c1 Q + a0 gamma (QQ - q2/3 I) + kappa0 d2Q
+ *        - 2 kappa1 q0 (R + R^T) + (4/3) kappa1 q0 tr R I + eps (E E - E^2/3 I)
+ *    c1 = -a0 (1 - gamma/3) - a0 gamma q2 - 4 kappa1 q0^2
+ *  stress (src/blue_phase.c:827-930), before its final sign:
+ *    f I + 2 xi Qt (Q:H) - xi (M + M^T) - kappa0 K - kappa1 G + kappa1 X
+ *        - 2 kappa1 q0 C + (M^T - M),   K_ab = d_a Q_bc v_c
+ *
+ *****************************************************************************/
+
+struct LcFast {
+  float q[3][3], dq[3][3][3];
+  float R[3][3], QQ[3][3], v[3];
+  float q2, fed;
+};
+
+__device__ __forceinline__ void lc_fast_prepare(LcFast & w) {
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) {
+      /* R_ab = sum_{c,d} e_acd dq[c][b][d]: two terms */
+      const int c = (a + 1) % 3, d = (a + 2) % 3;
+      w.R[a][b] = w.dq[c][b][d] - w.dq[d][b][c];
+    }
+  }
+  float q2 = 0.0f;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) q2 = fmaf(w.q[a][b], w.q[a][b], q2);
+  }
+  w.q2 = q2;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = a; b < 3; b++) {
+      float t = 0.0f;
+      #pragma unroll
+      for (int c = 0; c < 3; c++) t = fmaf(w.q[a][c], w.q[b][c], t);
+      w.QQ[a][b] = t;
+      w.QQ[b][a] = t;
+    }
+  }
+  #pragma unroll
+  for (int c = 0; c < 3; c++) {
+    w.v[c] = w.dq[0][c][0] + w.dq[1][c][1] + w.dq[2][c][2];
+  }
+}
+
+/* Free-energy density (src/blue_phase.c:309-400) */
+template <typename P>
+__device__ __forceinline__ float lc_fast_fed(const P & p, const LcFast & w) {
+  const float r3 = 1.0f/3.0f;
+  const float gamma = (float) p.gamma, a0 = (float) p.a0;
+  const float q0 = (float) p.q0*(float) p.rredshift;
+  const float rs2 = (float) p.redshift*(float) p.redshift;
+  const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
+  float q3 = 0.0f, dq1 = 0.0f, efield = 0.0f;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) {
+      q3 = fmaf(w.QQ[a][b], w.q[a][b], q3);
+      const float t = fmaf(2.0f*q0, w.q[a][b], w.R[a][b]);
+      dq1 = fmaf(t, t, dq1);
+    }
+  }
+  const float dq0 = w.v[0]*w.v[0] + w.v[1]*w.v[1] + w.v[2]*w.v[2];
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) {
+      efield += (float) p.e0[a]*w.q[a][b]*(float) p.e0[b];
+    }
+  }
+  efield *= (float) p.coswt*(float) p.coswt;
+  return 0.5f*a0*(1.0f - r3*gamma)*w.q2 - r3*a0*gamma*q3
+    + 0.25f*a0*gamma*w.q2*w.q2 + 0.5f*kappa0*dq0 + 0.5f*kappa1*dq1
+    - (float) p.epsilon*efield;
+}
+
+/* Molecular field H (symmetric, traceless) */
+template <typename P>
+__device__ __forceinline__ void lc_fast_h(const P & p, const LcFast & w,
+					  const float dsq[3][3],
+					  float h[3][3]) {
+  const float r3 = 1.0f/3.0f;
+  const float gamma = (float) p.gamma, a0 = (float) p.a0;
+  const float q0 = (float) p.q0*(float) p.rredshift;
+  const float rs2 = (float) p.redshift*(float) p.redshift;
+  const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
+  const float c1 = -a0*(1.0f - r3*gamma) - a0*gamma*w.q2
+    - 4.0f*kappa1*q0*q0;
+  const float ag = a0*gamma;
+  const float k2 = -2.0f*kappa1*q0;
+  const float eq = w.R[0][0] + w.R[1][1] + w.R[2][2];
+  float e[3], e2 = 0.0f;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    e[a] = (float) p.e0[a]*(float) p.coswt;
+    e2 += e[a]*e[a];
+  }
+  const float diag = -r3*ag*w.q2 + 4.0f*r3*kappa1*q0*eq
+    - (float) p.epsilon*r3*e2;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = a; b < 3; b++) {
+      float t = c1*w.q[a][b] + ag*w.QQ[a][b] + kappa0*dsq[a][b]
+	+ k2*(w.R[a][b] + w.R[b][a]) + (float) p.epsilon*e[a]*e[b];
+      if (a == b) t += diag;
+      h[a][b] = t;
+      h[b][a] = t;
+    }
+  }
+}
+
+/* Chiral stress including the antisymmetric part, with the final sign */
+template <typename P>
+__device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
+					       const float h[3][3],
+					       float sth[3][3]) {
+  const float r3 = 1.0f/3.0f;
+  const float xi = (float) p.xi;
+  const float q0 = (float) p.q0*(float) p.rredshift;
+  const float rs2 = (float) p.redshift*(float) p.redshift;
+  const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
+  const float fed = w.fed;
+  float qh = 0.0f;
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) qh = fmaf(w.q[a][b], h[a][b], qh);
+  }
+  /* M = H Qt */
+  float M[3][3];
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) {
+      float t = r3*h[a][b];
+      #pragma unroll
+      for (int c = 0; c < 3; c++) t = fmaf(h[a][c], w.q[c][b], t);
+      M[a][b] = t;
+    }
+  }
+  /* off-diagonal of dQ_a . Q for the chiral term */
+  float C[3][3];
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float Pm[3][3];
+    #pragma unroll
+    for (int c = 0; c < 3; c++) {
+      #pragma unroll
+      for (int e = 0; e < 3; e++) {
+	if (c == e) continue;
+	float t = 0.0f;
+	#pragma unroll
+	for (int d = 0; d < 3; d++) t = fmaf(w.dq[a][c][d], w.q[d][e], t);
+	Pm[c][e] = t;
+      }
+    }
+    C[a][0] = Pm[1][2] - Pm[2][1];
+    C[a][1] = Pm[2][0] - Pm[0][2];
+    C[a][2] = Pm[0][1] - Pm[1][0];
+  }
+  #pragma unroll
+  for (int a = 0; a < 3; a++) {
+    #pragma unroll
+    for (int b = 0; b < 3; b++) {
+      float G = 0.0f, X = 0.0f, K = 0.0f;
+      #pragma unroll
+      for (int c = 0; c < 3; c++) {
+	K = fmaf(w.dq[a][b][c], w.v[c], K);
+	#pragma unroll
+	for (int d = 0; d < 3; d++) {
+	  G = fmaf(w.dq[a][c][d], w.dq[b][c][d], G);
+	  X = fmaf(w.dq[a][c][d], w.dq[c][b][d], X);
+	}
+      }
+      const float qt = w.q[a][b] + ((a == b) ? r3 : 0.0f);
+      float t = 2.0f*xi*qt*qh - xi*(M[a][b] + M[b][a]) - kappa0*K
+	- kappa1*G + kappa1*X - 2.0f*kappa1*q0*C[a][b]
+	+ (M[b][a] - M[a][b]);
+      if (a == b) t += fed;
+      sth[a][b] = -t;
+    }
+  }
+}
+
+/* H, free energy and stress of one site from Q and its gradients */
+template <typename P>
+__device__ __forceinline__ void lc_fast_site(const P & p, LcFast & w,
+					     const float dsq[3][3],
+					     float h[3][3], float sth[3][3]) {
+  lc_fast_prepare(w);
+  w.fed = lc_fast_fed(p, w);
+  lc_fast_h(p, w, dsq, h);
+  lc_fast_stress(p, w, h, sth);
+}
+
 #endif
 
 #ifndef LGB_LC_STEP_KERNELS
@@ -337,12 +554,21 @@ __global__ void k_lc_fields(lgbk_dims_t d, P p,
     dl[n] = fn[xp] + fn[xm] + fn[yp] + fn[ym] + fn[zp] + fn[zm]
       - T(6.0)*fn[i];
   }
-  T qs[3][3], dq[3][3][3], dsq[3][3], hs[3][3], s[3][3];
-  lc_expand(q, N, i, qs);
-  lc_expand_grad(g, 1, 0, dq);
+  T dsq[3][3], hs[3][3], s[3][3];
   lc_expand(dl, 1, 0, dsq);
-  lc_h_site<T>(p, qs, dq, dsq, hs);
-  lc_stress_site<T>(p, qs, dq, hs, s);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    LcFast w;
+    lc_expand(q, N, i, w.q);
+    lc_expand_grad(g, 1, 0, w.dq);
+    lc_fast_site(p, w, dsq, hs, s);
+  }
+  else {
+    T qs[3][3], dq[3][3][3];
+    lc_expand(q, N, i, qs);
+    lc_expand_grad(g, 1, 0, dq);
+    lc_h_site<T>(p, qs, dq, dsq, hs);
+    lc_stress_site<T>(p, qs, dq, hs, s);
+  }
   #pragma unroll
   for (int ia = 0; ia < 3; ia++)
     #pragma unroll
@@ -438,7 +664,39 @@ __global__ void k_lc_update(lgbk_dims_t d, lgbk_lc_step_args_t a) {
   /* Beris-Edwards update of the 5 components */
   if (fluid) {
     T s[3][3];
-    {
+    if constexpr (sizeof(T) == sizeof(float)) {
+      /* S = -2 xi Qt (Q:W) + A Qt + (A Qt)^T with A = xi D + Omega, for the
+       * five stored components only (the same S as below) */
+      T w[3][3];
+      #pragma unroll
+      for (int ia = 0; ia < 3; ia++) {
+	w[ia][0] = T(0.5)*(u[ia*N + nb[0]] - u[ia*N + nb[1]]);
+	w[ia][1] = T(0.5)*(u[ia*N + nb[2]] - u[ia*N + nb[3]]);
+	w[ia][2] = T(0.5)*(u[ia*N + nb[4]] - u[ia*N + nb[5]]);
+      }
+      const T tr = r3*(w[0][0] + w[1][1] + w[2][2]);
+      w[0][0] -= tr; w[1][1] -= tr; w[2][2] -= tr;
+      T tqw = T(0.0), A[3][3], qt[3][3];
+      #pragma unroll
+      for (int ia = 0; ia < 3; ia++) {
+	#pragma unroll
+	for (int ib = 0; ib < 3; ib++) {
+	  tqw += qs[ia][ib]*w[ib][ia];
+	  A[ia][ib] = T(0.5)*(xi*(w[ia][ib] + w[ib][ia]) + (w[ia][ib] - w[ib][ia]));
+	  qt[ia][ib] = qs[ia][ib] + ((ia == ib) ? r3 : T(0.0));
+	}
+      }
+      auto aq = [&](int a, int b) {
+	return A[a][0]*qt[0][b] + A[a][1]*qt[1][b] + A[a][2]*qt[2][b];
+      };
+      const T m2 = -T(2.0)*xi*tqw;
+      s[0][0] = m2*qt[0][0] + T(2.0)*aq(0, 0);
+      s[0][1] = m2*qt[0][1] + aq(0, 1) + aq(1, 0);
+      s[0][2] = m2*qt[0][2] + aq(0, 2) + aq(2, 0);
+      s[1][1] = m2*qt[1][1] + T(2.0)*aq(1, 1);
+      s[1][2] = m2*qt[1][2] + aq(1, 2) + aq(2, 1);
+    }
+    else {
       T w[3][3], dd[3][3], om[3][3];
       #pragma unroll
       for (int ia = 0; ia < 3; ia++) {

@@ -58,7 +58,9 @@ NCU_BYTES_PER_SITE = {"fp32": 179.6, "fp64": 370.5, "fp16": None}
 LIMITER = {"fp32": "hbm (traffic = compulsory bytes; latency gap)",
            "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
            "fp16": "hbm", "lc64": "fp64 pipe",
-           "lc32": "two kernels; stress and H written between them"}
+           "lc32": "two kernels: fields + Beris-Edwards (FP32 issue "
+                   "bound), force + collision (HBM, 2.5-D); the stress "
+                   "(9 values a site) crosses HBM between them"}
 
 
 def env_int(name, default):
@@ -350,7 +352,7 @@ def gpu_arm(args):
             slc = None
         lc["workload"] = ("cholesteric LC 128^3, O8M blue phase I, pitch 32, "
                           "A0=0.01 gamma=3 kappa0=kappa1=0.01 xi=0.7 "
-                          "Gamma=0.5 eta=0.5, two fused kernels per step")
+                          "Gamma=0.5 eta=0.5, two kernels per step")
 
     # --- ensemble of 64 uneven boxes, FP32, one persistent launch -------
     ens = None

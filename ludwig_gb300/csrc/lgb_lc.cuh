@@ -525,7 +525,8 @@ __device__ __forceinline__ void lc_fast_site(const P & p, LcFast & w,
  *                pulled populations and the M10 collision with the force.
  *                Q and u are double-buffered (neighbours read old values).
  *
- *  Same arithmetic, in the same order, as the per-function kernels.
+ *  Same arithmetic, in the same order, as the per-function kernels (the
+ *  FP64 step; the float step is lgb_lc32.cuh).
  *
  *****************************************************************************/
 
@@ -554,21 +555,12 @@ __global__ void k_lc_fields(lgbk_dims_t d, P p,
     dl[n] = fn[xp] + fn[xm] + fn[yp] + fn[ym] + fn[zp] + fn[zm]
       - T(6.0)*fn[i];
   }
-  T dsq[3][3], hs[3][3], s[3][3];
+  T qs[3][3], dq[3][3][3], dsq[3][3], hs[3][3], s[3][3];
+  lc_expand(q, N, i, qs);
+  lc_expand_grad(g, 1, 0, dq);
   lc_expand(dl, 1, 0, dsq);
-  if constexpr (sizeof(T) == sizeof(float)) {
-    LcFast w;
-    lc_expand(q, N, i, w.q);
-    lc_expand_grad(g, 1, 0, w.dq);
-    lc_fast_site(p, w, dsq, hs, s);
-  }
-  else {
-    T qs[3][3], dq[3][3][3];
-    lc_expand(q, N, i, qs);
-    lc_expand_grad(g, 1, 0, dq);
-    lc_h_site<T>(p, qs, dq, dsq, hs);
-    lc_stress_site<T>(p, qs, dq, hs, s);
-  }
+  lc_h_site<T>(p, qs, dq, dsq, hs);
+  lc_stress_site<T>(p, qs, dq, hs, s);
   #pragma unroll
   for (int ia = 0; ia < 3; ia++)
     #pragma unroll
@@ -664,39 +656,7 @@ __global__ void k_lc_update(lgbk_dims_t d, lgbk_lc_step_args_t a) {
   /* Beris-Edwards update of the 5 components */
   if (fluid) {
     T s[3][3];
-    if constexpr (sizeof(T) == sizeof(float)) {
-      /* S = -2 xi Qt (Q:W) + A Qt + (A Qt)^T with A = xi D + Omega, for the
-       * five stored components only (the same S as below) */
-      T w[3][3];
-      #pragma unroll
-      for (int ia = 0; ia < 3; ia++) {
-	w[ia][0] = T(0.5)*(u[ia*N + nb[0]] - u[ia*N + nb[1]]);
-	w[ia][1] = T(0.5)*(u[ia*N + nb[2]] - u[ia*N + nb[3]]);
-	w[ia][2] = T(0.5)*(u[ia*N + nb[4]] - u[ia*N + nb[5]]);
-      }
-      const T tr = r3*(w[0][0] + w[1][1] + w[2][2]);
-      w[0][0] -= tr; w[1][1] -= tr; w[2][2] -= tr;
-      T tqw = T(0.0), A[3][3], qt[3][3];
-      #pragma unroll
-      for (int ia = 0; ia < 3; ia++) {
-	#pragma unroll
-	for (int ib = 0; ib < 3; ib++) {
-	  tqw += qs[ia][ib]*w[ib][ia];
-	  A[ia][ib] = T(0.5)*(xi*(w[ia][ib] + w[ib][ia]) + (w[ia][ib] - w[ib][ia]));
-	  qt[ia][ib] = qs[ia][ib] + ((ia == ib) ? r3 : T(0.0));
-	}
-      }
-      auto aq = [&](int a, int b) {
-	return A[a][0]*qt[0][b] + A[a][1]*qt[1][b] + A[a][2]*qt[2][b];
-      };
-      const T m2 = -T(2.0)*xi*tqw;
-      s[0][0] = m2*qt[0][0] + T(2.0)*aq(0, 0);
-      s[0][1] = m2*qt[0][1] + aq(0, 1) + aq(1, 0);
-      s[0][2] = m2*qt[0][2] + aq(0, 2) + aq(2, 0);
-      s[1][1] = m2*qt[1][1] + T(2.0)*aq(1, 1);
-      s[1][2] = m2*qt[1][2] + aq(1, 2) + aq(2, 1);
-    }
-    else {
+    {
       T w[3][3], dd[3][3], om[3][3];
       #pragma unroll
       for (int ia = 0; ia < 3; ia++) {

@@ -7,12 +7,34 @@
  *
  *****************************************************************************/
 
-#include "lgb_lc.cuh"
+#include "lgb_lc32.cuh"
 
-#define TPB 128
+/* Tile of the force + collision kernel and resident CTAs per SM */
+#define LC32_TY 8
+#define LC32_MINB 2
+#define LC32_XCHUNK 16
 
-static dim3 gridn(long long n) {
-  return dim3((unsigned int) ((n + TPB - 1)/TPB));
+template <typename S, bool HAS_MAP>
+static int launch_collide(const lgbk_dims_t * d, const lgbk_lc_step_args_t * a,
+			  cudaStream_t s) {
+  auto kern = k_lc32_collide<S, HAS_MAP, LC32_TY, LC32_MINB>;
+  const size_t smem = LcCollideSmem<LC32_TY>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*LC32_TY, smem);
+  if (occ < 1) occ = 1;
+  const int ntz = (d->nz + 31)/32, nty = (d->ny + LC32_TY - 1)/LC32_TY;
+  const int ncx = (d->nx + LC32_XCHUNK - 1)/LC32_XCHUNK;
+  long long items = (long long) ntz*nty*ncx;
+  long long grid = (long long) nsm*occ;
+  if (grid > items) grid = items;
+  kern<<<(unsigned int) grid, dim3(32, LC32_TY), smem, s>>>(*d, *a,
+							     LC32_XCHUNK);
+  return (int) cudaGetLastError();
 }
 
 template <typename S>
@@ -25,17 +47,20 @@ static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
   pf.rredshift = (float) p->rredshift; pf.epsilon = (float) p->epsilon;
   for (int i = 0; i < 3; i++) pf.e0[i] = (float) p->e0[i];
   pf.coswt = (float) p->coswt;
-  k_lc_fields<float, lgbk_lc_f_t><<<gridn(d->nsites), TPB, 0, s>>>(
-    *d, pf, (const float *) a->q_in, (float *) a->pth, (float *) a->h);
+  const dim3 fgrid((unsigned int) (((d->nz + 31)/32)
+				   *((d->ny + LC32_FY - 1)/LC32_FY)),
+		    (unsigned int) d->nx);
+  const dim3 fblock(32, LC32_FY);
   if (a->status) {
-    k_lc_update<float, S, false, true, true>
-      <<<gridn(d->nsites), TPB, 0, s>>>(*d, *a);
+    k_lc32_fields_be<true><<<fgrid, fblock, 0, s>>>(*d, pf, *a);
   }
   else {
-    k_lc_update<float, S, false, true, false>
-      <<<gridn(d->nsites), TPB, 0, s>>>(*d, *a);
+    k_lc32_fields_be<false><<<fgrid, fblock, 0, s>>>(*d, pf, *a);
   }
-  return (int) cudaGetLastError();
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  return a->status ? launch_collide<S, true>(d, a, s)
+		   : launch_collide<S, false>(d, a, s);
 }
 
 extern "C" int lgbk_lc_step(const lgbk_dims_t * d, int prec,

@@ -191,38 +191,50 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int xchunk,
       }
     };
 
-    /* Gradient, stress and chemical potential of plane x on tile + 1 */
-    auto compute_D = [&](int x) {
+    /* Gradient, stress and chemical potential of plane x at the site k of
+     * the tile + 1 (halo-1 coordinates + 1: ly = k / DZ, lz = k % DZ) */
+    auto d_site = [&](int x, int k) {
       const T * pc = sphi + pslot(x)*NPHI;
       const T * pp = sphi + pslot(x + 1)*NPHI;
       const T * pm = sphi + pslot(x - 1)*NPHI;
       T * D = sD + dslot(x)*SM::NDC*ND;
+      const int ly = k / DZ, lz = k % DZ;
+      const int q = (ly + 1)*PZ + (lz + 1);    /* same site in phi plane */
+      T c = pc[q];
+      T xp = pp[q], xm = pm[q];
+      T yp = pc[q + PZ], ym = pc[q - PZ];
+      T zp = pc[q + 1], zm = pc[q - 1];
+      T g[3];
+      g[0] = T(0.5)*(xp - xm);
+      g[1] = T(0.5)*(yp - ym);
+      g[2] = T(0.5)*(zp - zm);
+      T delsq = xp + xm + yp + ym + zp + zm - T(6.0)*c;
+      T p0 = lgb_symm_p0<T>(pa, pb, kappa, c, delsq, g);
+      T p0z = p0*T(0.0);
       #pragma unroll
-      for (int j = 0; j < KD; j++) {
-	const int k = tid + j*NTHR;
-	if (k >= ND) break;
-	const int ly = k / DZ, lz = k % DZ;    /* halo-1 coordinates + 1 */
-	const int q = (ly + 1)*PZ + (lz + 1);  /* same site in phi plane */
-	T c = pc[q];
-	T xp = pp[q], xm = pm[q];
-	T yp = pc[q + PZ], ym = pc[q - PZ];
-	T zp = pc[q + 1], zm = pc[q - 1];
-	T g[3];
-	g[0] = T(0.5)*(xp - xm);
-	g[1] = T(0.5)*(yp - ym);
-	g[2] = T(0.5)*(zp - zm);
-	T delsq = xp + xm + yp + ym + zp + zm - T(6.0)*c;
-	T p0 = lgb_symm_p0<T>(pa, pb, kappa, c, delsq, g);
-	T p0z = p0*T(0.0);
+      for (int ia = 0; ia < 3; ia++) {
 	#pragma unroll
-	for (int ia = 0; ia < 3; ia++) {
-	  #pragma unroll
-	  for (int ib = 0; ib < 3; ib++) {
-	    D[(3*ia + ib)*ND + k] = ((ia == ib) ? p0 : p0z) + kappa*g[ia]*g[ib];
-	  }
+	for (int ib = 0; ib < 3; ib++) {
+	  D[(3*ia + ib)*ND + k] = ((ia == ib) ? p0 : p0z) + kappa*g[ia]*g[ib];
 	}
-	D[9*ND + k] = lgb_symm_mu<T>(pa, pb, kappa, c, delsq);
       }
+      D[9*ND + k] = lgb_symm_mu<T>(pa, pb, kappa, c, delsq);
+    };
+    /* The whole tile + 1 of plane x: every thread its own site, the first
+     * NB threads one site of the halo ring each.  A thread therefore
+     * writes D at its own site itself, and may read it back without a
+     * barrier. */
+    constexpr int NB = ND - NTHR;                 /* 2 DZ + 2 TY ring sites */
+    int hring = -1;
+    if (tid < NB) {
+      if (tid < DZ) hring = tid;                            /* row 0 */
+      else if (tid < 2*DZ) hring = (TY + 1)*DZ + (tid - DZ); /* last row */
+      else if (tid < 2*DZ + TY) hring = (1 + tid - 2*DZ)*DZ;  /* column 0 */
+      else hring = (1 + tid - 2*DZ - TY)*DZ + DZ - 1;          /* last col */
+    }
+    auto compute_D = [&](int x) {
+      d_site(x, cidx);
+      if (hring >= 0) d_site(x, hring);
     };
 
     const int yg = y0 + ty, zg = z0 + tz;
@@ -298,8 +310,10 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int xchunk,
 	load_u(x + 1);
       }
       __pipeline_commit();
+      /* D(x+1): each thread's own site is its own work (read back below
+       * without a barrier); the neighbours' values of D(x+1) are read only
+       * in the next plane, after its barrier */
       compute_D(x + 1);
-      __syncthreads();
 
       if (active) {
 	const T * Dc = sD + dslot(x)*SM::NDC*ND;

@@ -374,8 +374,9 @@ int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
 int ludwig_gb_sync(void);
 /* The CUDA stream (cudaStream_t) every launch of the library uses. */
 void * ludwig_gb_stream(void);
-/* Tuning of the fused kernel: planes per x chunk, tile height (4, 8, 16)
- * and resident CTAs per SM for tile height 8 (2..4; 0 = default). */
+/* Tuning of the fused kernel: planes per x chunk (0, the default: an equal
+ * share of the (tile, plane) pairs per resident CTA), tile height (4, 8,
+ * 16) and resident CTAs per SM for tile height 8 (2..4; 0 = default). */
 int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks);
 
 /*---------------------------------------------------------------------------

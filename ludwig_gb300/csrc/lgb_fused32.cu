@@ -36,9 +36,9 @@ static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
   if (occ < 1) occ = 1;
 
   int ntz = (d->nz + 31)/32, nty = (d->ny + TY - 1)/TY;
-  int ncx = (d->nx + xchunk - 1)/xchunk;
-  long long items = (long long) ntz*nty*ncx;
   long long grid = (long long) nsm*occ;
+  xchunk = lgbk_auto_xchunk(xchunk, d->nx, ntz*nty, grid);
+  long long items = (long long) ntz*nty*((d->nx + xchunk - 1)/xchunk);
   if (grid > items) grid = items;
 
   kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(*d, *a, xchunk);
@@ -76,7 +76,6 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 				const lgbk_binary_args_t * a, int xchunk,
 				int ty, int minb, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
-  if (xchunk <= 0) xchunk = 32;
   if (ty <= 0) ty = 8;
   switch (prec) {
   case LGBK_PREC_FP64:

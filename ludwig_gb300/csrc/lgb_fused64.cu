@@ -28,9 +28,9 @@ static int launch64(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
   if (occ < 1) occ = 1;
 
   int ntz = (d->nz + 31)/32, nty = (d->ny + TY - 1)/TY;
-  int ncx = (d->nx + xchunk - 1)/xchunk;
-  long long items = (long long) ntz*nty*ncx;
   long long grid = (long long) nsm*occ;
+  xchunk = lgbk_auto_xchunk(xchunk, d->nx, ntz*nty, grid);
+  long long items = (long long) ntz*nty*((d->nx + xchunk - 1)/xchunk);
   if (grid > items) grid = items;
 
   kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(*d, *a, xchunk);
@@ -41,7 +41,6 @@ extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
 				    const lgbk_binary_args_t * a, int xchunk,
 				    int ty, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
-  if (xchunk <= 0) xchunk = 32;
   if (a->cp.ghosts_zero) {
     return a->status ? launch64<true, true>(d, a, xchunk, ty, s)
                      : launch64<true, false>(d, a, xchunk, ty, s);

@@ -12,7 +12,6 @@
 /* Tile of the force + collision kernel and resident CTAs per SM */
 #define LC32_TY 8
 #define LC32_MINB 2
-#define LC32_XCHUNK 16
 
 template <typename S, bool HAS_MAP>
 static int launch_collide(const lgbk_dims_t * d, const lgbk_lc_step_args_t * a,
@@ -28,12 +27,13 @@ static int launch_collide(const lgbk_dims_t * d, const lgbk_lc_step_args_t * a,
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*LC32_TY, smem);
   if (occ < 1) occ = 1;
   const int ntz = (d->nz + 31)/32, nty = (d->ny + LC32_TY - 1)/LC32_TY;
-  const int ncx = (d->nx + LC32_XCHUNK - 1)/LC32_XCHUNK;
-  long long items = (long long) ntz*nty*ncx;
   long long grid = (long long) nsm*occ;
+  /* about 1.5 items per CTA (16 planes at 128^3: 0.170 ms per LC step,
+   * against 0.177 ms with 13-plane chunks) */
+  const int xchunk = lgbk_auto_xchunk(0, d->nx, ntz*nty, grid, 3);
+  const long long items = (long long) ntz*nty*((d->nx + xchunk - 1)/xchunk);
   if (grid > items) grid = items;
-  kern<<<(unsigned int) grid, dim3(32, LC32_TY), smem, s>>>(*d, *a,
-							     LC32_XCHUNK);
+  kern<<<(unsigned int) grid, dim3(32, LC32_TY), smem, s>>>(*d, *a, xchunk);
   return (int) cudaGetLastError();
 }
 

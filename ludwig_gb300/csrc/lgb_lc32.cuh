@@ -215,15 +215,17 @@ k_lc32_collide(lgbk_dims_t d, lgbk_lc_step_args_t a, int xchunk) {
 
   const int ntz = (d.nz + TZ - 1)/TZ;
   const int nty = (d.ny + TY - 1)/TY;
+
+  /* work items (tile, chunk of xchunk planes), z tiles fastest so that
+   * neighbouring CTAs stream neighbouring rows of the same planes */
   const int ncx = (d.nx + xchunk - 1)/xchunk;
   const int nitems = ntz*nty*ncx;
-
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int itz = item % ntz;
     const int ity = (item / ntz) % nty;
-    const int icx = item / (ntz*nty);
-    const int z0 = itz*TZ, y0 = ity*TY, x0 = icx*xchunk;
+    const int x0 = (item / (ntz*nty))*xchunk;
     const int xe = min(x0 + xchunk, d.nx);
+    const int z0 = itz*TZ, y0 = ity*TY;
 
     /* Copy tasks: the first DY*10 threads each own one (row r, part t)
      * of the tile -- t < 8 a 16-byte chunk of the row interior, t = 8, 9

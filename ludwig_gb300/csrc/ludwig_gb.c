@@ -70,7 +70,7 @@ const char * ludwig_gb_version(void) { return "ludwig-gb300 0.1"; }
 
 static cudaStream_t stream_ = NULL;
 static double * red_scratch_ = NULL;
-static int tune_xchunk_ = 16;
+static int tune_xchunk_ = 0;         /* 0: balanced shares of the planes */
 static int tune_ty_ = 8;
 static int tune_minb_ = 3;
 static int advection_order_ = 1;
@@ -114,10 +114,10 @@ int ludwig_gb_sync(void) {
 }
 
 int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks) {
-  if (xchunk < 1 || (tile_y != 4 && tile_y != 8 && tile_y != 16) ||
+  if (xchunk < 0 || (tile_y != 4 && tile_y != 8 && tile_y != 16) ||
       min_blocks < 0 || min_blocks > 4) {
-    return err_set(LUDWIG_GB_EINVAL, "tune: xchunk >= 1, tile_y in {4,8,16},"
-		   " min_blocks in 0..4");
+    return err_set(LUDWIG_GB_EINVAL, "tune: xchunk >= 0 (0: balanced "
+		   "shares), tile_y in {4,8,16}, min_blocks in 0..4");
   }
   tune_xchunk_ = xchunk;
   tune_ty_ = tile_y;

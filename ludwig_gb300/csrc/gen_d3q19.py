@@ -216,21 +216,27 @@ def gen_fast():
             terms.append((c, mm, cond))
         return terms
 
-    def expr_of(terms):
-        if not terms:
-            return "T(0.0)"
+    def grouped(terms):
         groups, order = {}, []
-        for c, mm, cond in terms:
+        for c, mm in terms:
             if c not in groups:
                 groups[c] = []
                 order.append(c)
-            groups[c].append("(NM > %d ? m[%d] : T(0.0))" % (mm, mm)
-                             if cond else "m[%d]" % mm)
-        out = []
-        for c in order:
-            s = " + ".join(groups[c])
-            out.append("%s*(%s)" % (lit(c), s))
-        return " + ".join(out)
+            groups[c].append("m[%d]" % mm)
+        return " + ".join("%s*(%s)" % (lit(c), " + ".join(groups[c]))
+                          for c in order)
+
+    def expr_of(terms):
+        """Hydrodynamic terms, then the ghost terms as one added part that
+        is -0.0 (an exact additive identity, which the compiler drops) when
+        the ghost modes are not carried (NM = 10)."""
+        hydro = [(c, mm) for c, mm, cond in terms if not cond]
+        ghost = [(c, mm) for c, mm, cond in terms if cond]
+        h = grouped(hydro) if hydro else "T(0.0)"
+        if not ghost:
+            return h
+        top = max(mm for _, mm in ghost)
+        return "%s + (NM > %d ? (%s) : T(-0.0))" % (h, top, grouped(ghost))
 
     lines.append("  f[0] = %s;" % expr_of(part(0, False)))
     for (p, q) in pairs:

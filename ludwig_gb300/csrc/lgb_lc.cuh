@@ -7,8 +7,11 @@
  *  (:309-400), chiral stress including the antisymmetric part (:827-930,
  *  with its final minus sign) and the Beris-Edwards site update
  *  (src/blue_phase_beris_edwards.c:538-840).  The loops follow the
- *  reference's loop forms, term by term; compiled for FP64 with
- *  --fmad=false they give the same bits as the oracle's restatement.
+ *  reference's loop forms, term by term, except that products by a zero
+ *  Levi-Civita or Kronecker entry are not formed (adding a zero to a sum
+ *  leaves its value unchanged; only the sign of an exact zero can
+ *  differ); compiled for FP64 with --fmad=false they give the same values
+ *  as the oracle's restatement.
  *
  *  Q is stored as its 5 independent components XX, XY, XZ, YY, YZ
  *  (Q_zz = -Q_xx - Q_yy); gradients as grad[(3*n + ia)*N], delsq[n*N].
@@ -82,7 +85,7 @@ __device__ __forceinline__ void lc_h_site(const P & p, T q[3][3],
       #pragma unroll
       for (int ic = 0; ic < 3; ic++) sum += q[ia][ic]*q[ib][ic];
       h[ia][ib] = -a0*(T(1.0) - r3*gamma)*q[ia][ib]
-	+ a0*gamma*(sum - r3*q2*dab)
+	+ a0*gamma*((ia == ib) ? (sum - r3*q2*dab) : sum)
 	- a0*gamma*q2*q[ia][ib];
     }
   }
@@ -93,7 +96,8 @@ __device__ __forceinline__ void lc_h_site(const P & p, T q[3][3],
     for (int ic = 0; ic < 3; ic++)
       #pragma unroll
       for (int ia = 0; ia < 3; ia++)
-	eq += ((T) lgb_eps(ib, ic, ia))*dq[ib][ic][ia];
+	if (lgb_eps(ib, ic, ia) != 0)
+	  eq += ((T) lgb_eps(ib, ic, ia))*dq[ib][ic][ia];
 
   #pragma unroll
   for (int ia = 0; ia < 3; ia++) {
@@ -105,13 +109,28 @@ __device__ __forceinline__ void lc_h_site(const P & p, T q[3][3],
       for (int ic = 0; ic < 3; ic++) {
 	#pragma unroll
 	for (int id = 0; id < 3; id++) {
-	  sum += (((T) lgb_eps(ia, ic, id))*dq[ic][ib][id]
-		  + ((T) lgb_eps(ib, ic, id))*dq[ic][ia][id]);
+	  const int e1 = lgb_eps(ia, ic, id), e2 = lgb_eps(ib, ic, id);
+	  if (e1 != 0 && e2 != 0) {
+	    sum += (((T) e1)*dq[ic][ib][id] + ((T) e2)*dq[ic][ia][id]);
+	  }
+	  else if (e1 != 0) {
+	    sum += ((T) e1)*dq[ic][ib][id];
+	  }
+	  else if (e2 != 0) {
+	    sum += ((T) e2)*dq[ic][ia][id];
+	  }
 	}
       }
-      h[ia][ib] += kappa0*dsq[ia][ib]
-	- T(2.0)*kappa1*q0*sum + T(4.0)*r3*kappa1*q0*eq*dab
-	- T(4.0)*kappa1*q0*q0*q[ia][ib];
+      if (ia == ib) {
+	h[ia][ib] += kappa0*dsq[ia][ib]
+	  - T(2.0)*kappa1*q0*sum + T(4.0)*r3*kappa1*q0*eq*dab
+	  - T(4.0)*kappa1*q0*q0*q[ia][ib];
+      }
+      else {
+	h[ia][ib] += kappa0*dsq[ia][ib]
+	  - T(2.0)*kappa1*q0*sum
+	  - T(4.0)*kappa1*q0*q0*q[ia][ib];
+      }
     }
   }
 
@@ -169,7 +188,8 @@ __device__ __forceinline__ void lc_invariants(const P & p, T q[3][3],
       for (int ic = 0; ic < 3; ic++)
 	#pragma unroll
 	for (int id = 0; id < 3; id++)
-	  sum += ((T) lgb_eps(ia, ic, id))*dq[ic][ib][id];
+	  if (lgb_eps(ia, ic, id) != 0)
+	    sum += ((T) lgb_eps(ia, ic, id))*dq[ic][ib][id];
       sum += T(2.0)*q0*q[ia][ib];
       dq1 += sum*sum;
     }
@@ -240,7 +260,8 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
     #pragma unroll
     for (int ib = 0; ib < 3; ib++) {
       const T dab = (T) (ia == ib);
-      sth[ia][ib] = -p0*dab + T(2.0)*xi*(q[ia][ib] + r3*dab)*qh;
+      if (ia == ib) sth[ia][ib] = -p0*dab + T(2.0)*xi*(q[ia][ib] + r3*dab)*qh;
+      else          sth[ia][ib] = T(2.0)*xi*q[ia][ib]*qh;
     }
   }
   #pragma unroll
@@ -250,8 +271,9 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
       #pragma unroll
       for (int ic = 0; ic < 3; ic++) {
 	const T dbc = (T) (ib == ic), dac = (T) (ia == ic);
-	sth[ia][ib] += -xi*h[ia][ic]*(q[ib][ic] + r3*dbc)
-	  -xi*(q[ia][ic] + r3*dac)*h[ib][ic];
+	const T qbc = (ib == ic) ? (q[ib][ic] + r3*dbc) : q[ib][ic];
+	const T qac = (ia == ic) ? (q[ia][ic] + r3*dac) : q[ia][ic];
+	sth[ia][ib] += -xi*h[ia][ic]*qbc - xi*qac*h[ib][ic];
       }
     }
   }
@@ -268,8 +290,10 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
 	    + kappa1*dq[ia][ic][id]*dq[ic][ib][id];
 	  #pragma unroll
 	  for (int ie = 0; ie < 3; ie++) {
-	    sth[ia][ib] += -T(2.0)*kappa1*q0*dq[ia][ic][id]
-	      *((T) lgb_eps(ib, ic, ie))*q[id][ie];
+	    if (lgb_eps(ib, ic, ie) != 0) {
+	      sth[ia][ib] += -T(2.0)*kappa1*q0*dq[ia][ic][id]
+		*((T) lgb_eps(ib, ic, ie))*q[id][ie];
+	    }
 	  }
 	}
       }

@@ -145,3 +145,18 @@ def test_lc_fp32_one_step_close_to_fp64(gb, solid, precision):
         scale = np.abs(sa[k]).max()
         err = np.abs(sa[k] - sb[k]).max()
         assert err < tol * scale, (k, err, scale)
+
+
+def test_lc_fp32_ragged_lattice_close_to_fp64(gb):
+    """The float LC kernels on extents that are no multiple of the tile or
+    of 4 (P planes copied element by element)."""
+    L = (11, 9, 37)
+    a = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5)
+    b = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5, precision=gb.FP32)
+    for s in (a, b):
+        s.init_o8m()
+        s.step(20)
+    qa, qb = a.q.get(), b.q.get()
+    assert np.abs(qa - qb).max() < 1e-5 * np.abs(qa).max()
+    ua, ub = a.state()["u"], b.state()["u"]
+    assert np.abs(ua - ub).max() < 1e-3 * np.abs(ua).max()

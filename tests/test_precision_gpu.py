@@ -1,7 +1,9 @@
 """Reduced-precision forms against the FP64 oracle (config 1, 32^3).
 
 Tolerances are the measured GB300 errors with head-room:
-  FP32-shifted after 1000 steps: max|dphi| 1.1e-6, mass drift 2.8e-11;
+  FP32-shifted after 1000 steps: max|dphi| 1.1e-6; mass drift below 1e-10
+  (the rest population is rebuilt from error-free sums of the incoming
+  and outgoing populations; 1.3e-12 after 1e4 steps at 256^3);
   FP16 storage: max|dphi| 1.3e-5, mass drift 3.5e-8.
 The domain length L(t) of the reduced forms must be within 1% of FP64.
 """
@@ -26,7 +28,7 @@ def fp64_run(orc):
 
 
 @pytest.mark.parametrize("prec,dphi_tol,drift_tol", [
-    (1, 1e-5, 1e-9),        # FP32-shifted
+    (1, 1e-5, 1e-10),       # FP32-shifted
     (2, 1e-4, 1e-6),        # FP16 storage
 ])
 def test_reduced_precision_vs_fp64(gb, orc, fp64_run, prec, dphi_tol,
@@ -66,3 +68,16 @@ def test_fp32_state_roundtrip(gb):
     got = a.state()
     for k in ("f", "phi", "u"):
         assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("L", [(17, 13, 37), (9, 24, 70)])
+def test_fp32_ragged_lattice_close_to_fp64(gb, L):
+    """Extents that are no multiple of the tile (8 x 32) or of 4: partial
+    tiles, periodic halos wrapped element by element, short x-chunks."""
+    a = gb.BinaryFluid(L, precision=gb.FP64, mobility=MOB, eta=ETA)
+    b = gb.BinaryFluid(L, precision=gb.FP32, mobility=MOB, eta=ETA)
+    for s in (a, b):
+        s.phi.init_spinodal(77, 0.0, 0.02)
+        s.step(40)
+    assert np.abs(a.phi.get() - b.phi.get()).max() < 1e-6
+    assert np.abs(a.lb.get() - b.lb.get()).max() < 1e-6

@@ -164,6 +164,9 @@ int field_halo(field_t * obj);                              /* field.c:371 */
 int field_to_host(field_t * obj, double * data);
 int field_from_host(field_t * obj, const double * data);
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp);
+/* Spinodal patches of +-1, src/field_phi_init.c:537 */
+int field_phi_init_spinodal_patches(field_t * phi, int seed, int patch,
+				    double volminus1);
 /* src/field_phi_init.c:38: phi = phistar tanh((r - radius)/xi) about the
  * box centre */
 int field_phi_init_drop(field_t * phi, double xi, double radius,
@@ -288,11 +291,11 @@ int fe_lc_free(fe_lc_t * fe);
 /* blue_phase.c:241: epsilon is divided by 12 pi, rredshift = 1/redshift */
 int fe_lc_param_set(fe_lc_t * fe, const fe_lc_param_t * values);
 int fe_lc_param(fe_lc_t * fe, fe_lc_param_t * values);
-/* Blue phase I initial condition, src/blue_phase_init.c:59 (no rotation:
- * euler_angles must be zero) */
+/* Blue phase I initial condition, src/blue_phase_init.c:59; euler_angles
+ * (degrees, Z-X-Z; NULL for none) rotate the structure about the centre */
 int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 			const double euler_angles[3]);
-/* Blue phase II, src/blue_phase_init.c:155 (no rotation) */
+/* Blue phase II, src/blue_phase_init.c:155 (Euler angles as above) */
 int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 		       const double euler_angles[3]);
 /* Uniform uniaxial nematic along n, src/blue_phase_init.c:836 */

@@ -163,6 +163,8 @@ def _declare(L):
         "field_from_host": ([_P, _D], ctypes.c_int),
         "field_phi_init_spinodal": ([_P, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double], ctypes.c_int),
+        "field_phi_init_spinodal_patches": ([_P, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double], ctypes.c_int),
         "field_phi_init_drop": ([_P] + [ctypes.c_double] * 3 + [ctypes.c_int],
                                 ctypes.c_int),
         "field_grad_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
@@ -484,6 +486,12 @@ class Field(_Obj):
     def init_spinodal(self, seed, phi0=0.0, amp=0.02):
         _check(lib().field_phi_init_spinodal(self.ptr, int(seed), float(phi0),
                                              float(amp)), "spinodal")
+
+    def init_patches(self, seed, patch, volminus1):
+        """Cubes of patch^3 sites of -1 (probability volminus1) or +1
+        (src/field_phi_init.c:537)."""
+        _check(lib().field_phi_init_spinodal_patches(
+            self.ptr, int(seed), int(patch), float(volminus1)), "patches")
 
     def init_drop(self, xi, radius, phistar=1.0, centred=False):
         """A drop of the given radius and interface width (src/
@@ -976,17 +984,19 @@ class LiquidCrystal:
         self.pth = Pth(self.cs)
         self.lb.init_rest(1.0)
 
-    def init_o8m(self):
-        zero = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+    def init_o8m(self, euler_angles=(0.0, 0.0, 0.0)):
+        """Blue phase I; euler_angles (degrees, Z-X-Z) rotate it."""
         _check(lib().blue_phase_O8M_init(self.cs.ptr,
                                          ctypes.byref(self.fe.param),
-                                         self.q.ptr, zero), "o8m")
+                                         self.q.ptr, _D3(*euler_angles)),
+               "o8m")
 
-    def init_o2(self):
-        zero = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+    def init_o2(self, euler_angles=(0.0, 0.0, 0.0)):
+        """Blue phase II; euler_angles (degrees, Z-X-Z) rotate it."""
         _check(lib().blue_phase_O2_init(self.cs.ptr,
                                         ctypes.byref(self.fe.param),
-                                        self.q.ptr, zero), "o2")
+                                        self.q.ptr, _D3(*euler_angles)),
+               "o2")
 
     def init_nematic(self, n):
         _check(lib().blue_phase_nematic_init(self.cs.ptr,

@@ -638,6 +638,18 @@ int field_phi_init_drop(field_t * phi, double xi, double radius,
   return rc;
 }
 
+/* The first uniform draw of the per-site generator of site (x, y, z)
+ * (0-based), src/noise.c:278-340 and noise_uniform_double_reap */
+static double site_uniform(unsigned int seed0, int x, int y, int z) {
+  unsigned int sl[4], st[4];
+  sl[0] = seed0 + (unsigned int) (x + 1);
+  sl[1] = 12953u + (unsigned int) (y + 1);
+  sl[2] = 712357u + (unsigned int) (z + 1);
+  sl[3] = 22383979u;
+  for (int k = 0; k < 4; k++) st[k] = kiss(sl);
+  return (1.0/UINT_MAX)*kiss(st);
+}
+
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
   if (phi == NULL || phi->nf != 1) {
     return err_set(LUDWIG_GB_EINVAL, "field_phi_init_spinodal: scalar field");
@@ -649,14 +661,37 @@ int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
   for (int x = 0; x < d->nx; x++) {
     for (int y = 0; y < d->ny; y++) {
       for (int z = 0; z < d->nz; z++) {
-	unsigned int sl[4], st[4];
-	sl[0] = seed0 + (unsigned int) (x + 1);
-	sl[1] = 12953u + (unsigned int) (y + 1);
-	sl[2] = 712357u + (unsigned int) (z + 1);
-	sl[3] = 22383979u;
-	for (int k = 0; k < 4; k++) st[k] = kiss(sl);
-	double ran = (1.0/UINT_MAX)*kiss(st);
+	double ran = site_uniform(seed0, x, y, z);
 	h[((long long) x*d->ny + y)*d->nz + z] = phi0 + amp*(ran - 0.5);
+      }
+    }
+  }
+  int rc = field_from_host(phi, h);
+  free(h);
+  return rc;
+}
+
+/* Spinodal patches, src/field_phi_init.c:537-590: cubes of patch^3 sites
+ * (cut at the upper edges) of phi = -1 where the draw of the cube's first
+ * site is below volminus1, +1 elsewhere */
+int field_phi_init_spinodal_patches(field_t * phi, int seed, int patch,
+				    double volminus1) {
+  if (phi == NULL || phi->nf != 1 || patch < 1) {
+    return err_set(LUDWIG_GB_EINVAL, "field_phi_init_spinodal_patches");
+  }
+  const lgbk_dims_t * d = &phi->cs->d;
+  double * h = (double *) malloc(d->nsites*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "patches");
+  unsigned int seed0 = (seed > 1) ? (unsigned int) seed : 13u;
+  for (int x = 0; x < d->nx; x += patch) {
+    for (int y = 0; y < d->ny; y += patch) {
+      for (int z = 0; z < d->nz; z += patch) {
+	const double phi1 = (site_uniform(seed0, x, y, z) < volminus1)
+	  ? -1.0 : 1.0;
+	for (int ip = x; ip < x + patch && ip < d->nx; ip++)
+	  for (int jp = y; jp < y + patch && jp < d->ny; jp++)
+	    for (int kp = z; kp < z + patch && kp < d->nz; kp++)
+	      h[((long long) ip*d->ny + jp)*d->nz + kp] = phi1;
       }
     }
   }
@@ -1363,16 +1398,54 @@ int fe_lc_param(fe_lc_t * fe, fe_lc_param_t * values) {
 
 /* src/blue_phase_init.c:59-132 without rotation; global coordinates are
  * 1-based */
+/* Euler rotation (Z, X, Z) of the blue-phase initial conditions,
+ * src/blue_phase_init.c:1358-1445: angles in degrees, applied with a
+ * minus sign (a clockwise rotation of the argument turns Q
+ * counterclockwise); r' = M2 M1 M0 r summed in the reference's order. */
+typedef struct euler_rot_s { double m[3][3][3]; } euler_rot_t;
+
+static void rot_axis(double M[3][3], int dim, double alpha) {
+  const double c = cos(alpha), s = sin(alpha);
+  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) M[i][j] = 0.0;
+  if (dim == 0) {
+    M[0][0] = 1.0; M[1][1] = c; M[1][2] = -s; M[2][1] = s; M[2][2] = c;
+  }
+  else if (dim == 1) {
+    M[0][0] = c; M[0][2] = -s; M[1][1] = 1.0; M[2][0] = s; M[2][2] = c;
+  }
+  else {
+    M[0][0] = c; M[0][1] = -s; M[1][0] = s; M[1][1] = c; M[2][2] = 1.0;
+  }
+}
+
+static void euler_rot_create(const double deg[3], euler_rot_t * rot) {
+  const double pi = 3.1415926535897932385;
+  const int axis[3] = {2, 0, 2};
+  for (int k = 0; k < 3; k++) {
+    const double a = deg ? -1.0*pi*deg[k]/180.0 : 0.0;
+    rot_axis(rot->m[k], axis[k], a);
+  }
+}
+
+static void euler_rotate(const euler_rot_t * rot, double r[3]) {
+  const double r0[3] = {r[0], r[1], r[2]};
+  for (int k = 0; k < 3; k++) {
+    double t = 0.0;
+    for (int l = 0; l < 3; l++)
+      for (int m = 0; m < 3; m++)
+	for (int n = 0; n < 3; n++)
+	  t += rot->m[2][k][l]*rot->m[1][l][m]*rot->m[0][m][n]*r0[n];
+    r[k] = t;
+  }
+}
+
 int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
 			const double euler_angles[3]) {
   if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5) {
     return err_set(LUDWIG_GB_EINVAL, "blue_phase_O8M_init");
   }
-  if (euler_angles && (euler_angles[0] != 0.0 || euler_angles[1] != 0.0 ||
-		       euler_angles[2] != 0.0)) {
-    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O8M_init: rotation not "
-		   "supported");
-  }
+  euler_rot_t rot;
+  euler_rot_create(euler_angles, &rot);
   const lgbk_dims_t * d = &cs->d;
   const long long N = d->nsites;
   double * h = (double *) malloc(5*(size_t) N*sizeof(double));
@@ -1387,6 +1460,7 @@ int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
 	r[0] = (double) (x + 1) - 0.5*d->nx;
 	r[1] = (double) (y + 1) - 0.5*d->ny;
 	r[2] = (double) (z + 1) - 0.5*d->nz;
+	euler_rotate(&rot, r);
 	r[0] += 0.5*d->nx; r[1] += 0.5*d->ny; r[2] += 0.5*d->nz;
 	double cosx = cos(root2*q0*r[0]), sinx = sin(root2*q0*r[0]);
 	double cosy = cos(root2*q0*r[1]), siny = sin(root2*q0*r[1]);
@@ -1404,17 +1478,14 @@ int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
   return rc;
 }
 
-/* Blue phase II, src/blue_phase_init.c:155-235 (no rotation) */
+/* Blue phase II, src/blue_phase_init.c:155-235 */
 int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
 		       const double euler_angles[3]) {
   if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5) {
     return err_set(LUDWIG_GB_EINVAL, "blue_phase_O2_init");
   }
-  if (euler_angles && (euler_angles[0] != 0.0 || euler_angles[1] != 0.0 ||
-		       euler_angles[2] != 0.0)) {
-    return err_set(LUDWIG_GB_EINVAL, "blue_phase_O2_init: rotation not "
-		   "supported");
-  }
+  euler_rot_t rot;
+  euler_rot_create(euler_angles, &rot);
   const lgbk_dims_t * d = &cs->d;
   const long long N = d->nsites;
   double * h = (double *) malloc(5*(size_t) N*sizeof(double));
@@ -1428,6 +1499,7 @@ int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
 	r[0] = (double) (x + 1) - 0.5*d->nx;
 	r[1] = (double) (y + 1) - 0.5*d->ny;
 	r[2] = (double) (z + 1) - 0.5*d->nz;
+	euler_rotate(&rot, r);
 	r[0] += 0.5*d->nx; r[1] += 0.5*d->ny; r[2] += 0.5*d->nz;
 	double cosx = cos(2.0*q0*r[0]), sinx = sin(2.0*q0*r[0]);
 	double cosy = cos(2.0*q0*r[1]), siny = sin(2.0*q0*r[1]);

@@ -161,7 +161,8 @@ def grad27_cases():
 
 REGRESSION_LOGS = ("serial-spin-fd1", "serial-spin-lb1", "serial-init-bp1",
                    "serial-symm-dr1", "serial-init-bp2", "serial-relx-bp1",
-                   "serial-chol-fld")
+                   "serial-chol-fld", "serial-init-br1", "serial-init-br2",
+                   "serial-symm-pat")
 
 
 def parse_log(path):

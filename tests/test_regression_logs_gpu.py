@@ -17,7 +17,12 @@ order API:
 * serial-init-bp2: blue phase II (O2), 32^3, redshift 0.91, one step;
 * serial-relx-bp1: blue phase I relaxing without hydrodynamics, 100 steps;
 * serial-chol-fld: a uniform nematic in a static electric field, 16^3,
-  second-order advection, 10 steps.
+  second-order advection, 10 steps;
+* serial-init-br1, serial-init-br2: blue phases I and II rotated by Euler
+  angles (90, 0, 0) and (45, 45, 0), one step;
+* serial-symm-pat: spinodal patches (2^3 cubes of +-1, 10 % of -1) in the
+  symmetric binary fluid, 64^3, 27-point gradients, second-order
+  advection, one step.
 
 Values are compared to the digits the log prints (8 significant digits
 for most, 11 for the free energy); sums whose terms cancel (momentum,
@@ -241,6 +246,48 @@ def test_serial_chol_fld(gb):
         s.step_reference_order(10)
         lc_stats(s, ref[1], 16 ** 3)
         check_fe_line(s.fe.stats_info(s.map, recompute=False), ref[1]["fe"])
+        _, u, _ = s.hydro.get()
+        check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+    finally:
+        gb.advection_order(1)
+
+
+@pytest.mark.parametrize("name,init,angles,lc", [
+    ("serial-init-br1", "o8m", (90.0, 0.0, 0.0),
+     dict(a0=0.014384711, gamma=3.1764706, kappa0=0.01, kappa1=0.01,
+          xi=0.7, redshift=0.83, amplitude=-0.2, q0=0.27768018)),
+    ("serial-init-br2", "o2", (45.0, 45.0, 0.0),
+     dict(a0=0.0069, gamma=3.0, kappa0=0.02, kappa1=0.02, xi=0.7,
+          redshift=0.91, amplitude=0.3, q0=0.1963495)),
+])
+def test_serial_init_rotated(gb, name, init, angles, lc):
+    ref = LOGS[name]
+    s = gb.LiquidCrystal((32, 32, 32), eta=1.666666666666, gamma_rot=0.1,
+                         **lc)
+    getattr(s, "init_" + init)(angles)
+    lc_stats(s, ref[0], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map), ref[0]["fe"])
+    s.step_reference_order(1)
+    lc_stats(s, ref[1], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map, recompute=False), ref[1]["fe"])
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_serial_symm_pat(gb):
+    ref = LOGS["serial-symm-pat"]
+    s = gb.BinaryFluid((64, 64, 64), gb.FP64, a=-0.00625, b=0.00625,
+                       kappa=0.004, mobility=1.25, eta=0.00625)
+    s.dphi.set_stencil(27)
+    gb.advection_order(2)
+    try:
+        s.phi.init_patches(8361235, 2, 0.1)
+        check_scalars(s.phi.stats(), ref[0]["phi"], 64 ** 3)
+        s.dphi.compute()
+        assert close(s.fe.fed_total() / 64 ** 3, ref[0]["fed"][1], 1e-9)
+        s.step_reference_order(1)
+        check_scalars(s.phi.stats(), ref[1]["phi"], 64 ** 3)
+        assert close(s.fe.fed_total() / 64 ** 3, ref[1]["fed"][1], 1e-9)
         _, u, _ = s.hydro.get()
         check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
     finally:

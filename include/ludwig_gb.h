@@ -298,6 +298,8 @@ int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 /* Blue phase II, src/blue_phase_init.c:155 (Euler angles as above) */
 int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 		       const double euler_angles[3]);
+/* Random uniaxial directors (seed 13), src/blue_phase_init.c:1170 */
+int blue_phase_random_q_init(cs_t * cs, fe_lc_param_t * param, field_t * q);
 /* Uniform uniaxial nematic along n, src/blue_phase_init.c:836 */
 int blue_phase_nematic_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 			    const double n[3]);

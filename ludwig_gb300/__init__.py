@@ -222,6 +222,8 @@ def _declare(L):
                                ctypes.c_int),
         "blue_phase_nematic_init": ([_P, ctypes.POINTER(FeLcParam), _P, _D],
                                     ctypes.c_int),
+        "blue_phase_random_q_init": ([_P, ctypes.POINTER(FeLcParam), _P],
+                                     ctypes.c_int),
         "beris_edw_create": ([_P, _P, _P, pp], ctypes.c_int),
         "beris_edw_free": ([_P], ctypes.c_int),
         "beris_edw_param_set": ([_P, ctypes.POINTER(BerisEdwParam)],
@@ -997,6 +999,12 @@ class LiquidCrystal:
                                         ctypes.byref(self.fe.param),
                                         self.q.ptr, _D3(*euler_angles)),
                "o2")
+
+    def init_random(self):
+        """Random uniaxial directors (the reference's seed 13)."""
+        _check(lib().blue_phase_random_q_init(self.cs.ptr,
+                                              ctypes.byref(self.fe.param),
+                                              self.q.ptr), "random_q")
 
     def init_nematic(self, n):
         _check(lib().blue_phase_nematic_init(self.cs.ptr,

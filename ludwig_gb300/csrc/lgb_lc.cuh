@@ -333,8 +333,9 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
  *        - 2 kappa1 q0 (R + R^T) + (4/3) kappa1 q0 tr R I + eps (E E - E^2/3 I)
  *    c1 = -a0 (1 - gamma/3) - a0 gamma q2 - 4 kappa1 q0^2
  *  stress (src/blue_phase.c:827-930), before its final sign:
- *    f I + 2 xi Qt (Q:H) - xi (M + M^T) - kappa0 K - kappa1 G + kappa1 X
- *        - 2 kappa1 q0 C + (M^T - M),   K_ab = d_a Q_bc v_c
+ *    f I + 2 xi Qt (Q:H) - xi (M + M^T) - kappa0 K + kappa1 (X - G)
+ *        - 2 kappa1 q0 C + (M^T - M),   K_ab = d_a Q_bc v_c,
+ *    X - G = d_a Q_cd (d_c Q_bd - d_b Q_cd) over c != b
  *
  *****************************************************************************/
 
@@ -495,23 +496,36 @@ __device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
     C[a][1] = Pm[2][0] - Pm[0][2];
     C[a][2] = Pm[0][1] - Pm[1][0];
   }
+  /* X - G = d_a Q_cd (d_c Q_bd - d_b Q_cd): the bracket is antisymmetric
+   * in (c, b) and vanishes for c = b */
+  float Dm[3][3][3];
+  #pragma unroll
+  for (int c = 0; c < 3; c++) {
+    #pragma unroll
+    for (int b = c + 1; b < 3; b++) {
+      #pragma unroll
+      for (int d = 0; d < 3; d++) {
+	const float t = w.dq[c][b][d] - w.dq[b][c][d];
+	Dm[c][b][d] = t;
+	Dm[b][c][d] = -t;
+      }
+    }
+  }
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = 0; b < 3; b++) {
-      float G = 0.0f, X = 0.0f, K = 0.0f;
+      float XG = 0.0f, K = 0.0f;
       #pragma unroll
       for (int c = 0; c < 3; c++) {
 	K = fmaf(w.dq[a][b][c], w.v[c], K);
+	if (c == b) continue;
 	#pragma unroll
-	for (int d = 0; d < 3; d++) {
-	  G = fmaf(w.dq[a][c][d], w.dq[b][c][d], G);
-	  X = fmaf(w.dq[a][c][d], w.dq[c][b][d], X);
-	}
+	for (int d = 0; d < 3; d++) XG = fmaf(w.dq[a][c][d], Dm[c][b][d], XG);
       }
       const float qt = w.q[a][b] + ((a == b) ? r3 : 0.0f);
       float t = 2.0f*xi*qt*qh - xi*(M[a][b] + M[b][a]) - kappa0*K
-	- kappa1*G + kappa1*X - 2.0f*kappa1*q0*C[a][b]
+	+ kappa1*XG - 2.0f*kappa1*q0*C[a][b]
 	+ (M[b][a] - M[a][b]);
       if (a == b) t += fed;
       sth[a][b] = -t;

@@ -638,16 +638,24 @@ int field_phi_init_drop(field_t * phi, double xi, double radius,
   return rc;
 }
 
-/* The first uniform draw of the per-site generator of site (x, y, z)
- * (0-based), src/noise.c:278-340 and noise_uniform_double_reap */
-static double site_uniform(unsigned int seed0, int x, int y, int z) {
+/* The first n uniform draws of the per-site generator of site (x, y, z)
+ * (0-based), src/noise.c:278-340 and noise_uniform_double_reap
+ * (src/noise.c:437): each draw advances the site's state */
+static void site_uniforms(unsigned int seed0, int x, int y, int z, int n,
+			  double * out) {
   unsigned int sl[4], st[4];
   sl[0] = seed0 + (unsigned int) (x + 1);
   sl[1] = 12953u + (unsigned int) (y + 1);
   sl[2] = 712357u + (unsigned int) (z + 1);
   sl[3] = 22383979u;
   for (int k = 0; k < 4; k++) st[k] = kiss(sl);
-  return (1.0/UINT_MAX)*kiss(st);
+  for (int k = 0; k < n; k++) out[k] = (1.0/UINT_MAX)*kiss(st);
+}
+
+static double site_uniform(unsigned int seed0, int x, int y, int z) {
+  double r;
+  site_uniforms(seed0, x, y, z, 1, &r);
+  return r;
 }
 
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp) {
@@ -1542,6 +1550,43 @@ int blue_phase_nematic_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
   if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "nematic");
   for (int c = 0; c < 5; c++) {
     for (long long i = 0; i < N; i++) h[c*N + i] = q5[c];
+  }
+  int rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
+/* Random uniaxial directors, src/blue_phase_init.c:1170-1212 (seed 13,
+ * two draws per site: azimuth 2 pi (1/2 - r1), polar acos(2 r2 - 1)) */
+int blue_phase_random_q_init(cs_t * cs, fe_lc_param_t * param, field_t * fq) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_random_q_init");
+  }
+  const double pi = 3.1415926535897932385;
+  const lgbk_dims_t * d = &cs->d;
+  const long long N = d->nsites;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "random_q");
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	const long long i = ((long long) x*d->ny + y)*d->nz + z;
+	double r[2], n[3], q[3][3];
+	site_uniforms(13u, x, y, z, 2, r);
+	const double phase1 = 2.0*pi*(0.5 - r[0]);
+	const double phase2 = acos(2.0*r[1] - 1.0);
+	n[0] = cos(phase1)*sin(phase2);
+	n[1] = sin(phase1)*sin(phase2);
+	n[2] = cos(phase2);
+	for (int a = 0; a < 3; a++) {
+	  for (int b = 0; b < 3; b++) {
+	    q[a][b] = 0.5*param->amplitude0*(3.0*n[a]*n[b] - (double) (a == b));
+	  }
+	}
+	h[0*N + i] = q[0][0]; h[1*N + i] = q[0][1]; h[2*N + i] = q[0][2];
+	h[3*N + i] = q[1][1]; h[4*N + i] = q[1][2];
+      }
+    }
   }
   int rc = field_from_host(fq, h);
   free(h);

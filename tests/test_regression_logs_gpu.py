@@ -22,7 +22,8 @@ order API:
   angles (90, 0, 0) and (45, 45, 0), one step;
 * serial-symm-pat: spinodal patches (2^3 cubes of +-1, 10 % of -1) in the
   symmetric binary fluid, 64^3, 27-point gradients, second-order
-  advection, one step.
+  advection, one step;
+* serial-init-lcr: random uniaxial directors (amplitude 0.01), one step.
 
 Values are compared to the digits the log prints (8 significant digits
 for most, 11 for the free energy); sums whose terms cancel (momentum,
@@ -292,3 +293,19 @@ def test_serial_symm_pat(gb):
         check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
     finally:
         gb.advection_order(1)
+
+
+def test_serial_init_lcr(gb):
+    ref = LOGS["serial-init-lcr"]
+    s = gb.LiquidCrystal((32, 32, 32), eta=0.1, gamma_rot=0.1,
+                         a0=0.014384711, gamma=3.1764706, kappa0=0.01,
+                         kappa1=0.01, xi=0.7, redshift=1.0, amplitude=0.01,
+                         q0=0.27768018)
+    s.init_random()
+    lc_stats(s, ref[0], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map), ref[0]["fe"])
+    s.step_reference_order(1)
+    lc_stats(s, ref[1], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map, recompute=False), ref[1]["fe"])
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())

@@ -298,6 +298,13 @@ int blue_phase_O8M_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 /* Blue phase II, src/blue_phase_init.c:155 (Euler angles as above) */
 int blue_phase_O2_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 		       const double euler_angles[3]);
+/* Cholesteric helix along X, Y or Z (0, 1, 2), src/blue_phase_init.c:763 */
+int blue_phase_twist_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
+			  int helical_axis);
+/* Random directors (amplitude 0.01) in the box rmin..rmax (1-based,
+ * inclusive), src/blue_phase_init.c:1279 */
+int blue_phase_random_q_rectangle(cs_t * cs, fe_lc_param_t * param,
+				  field_t * q, int rmin[3], int rmax[3]);
 /* Random uniaxial directors (seed 13), src/blue_phase_init.c:1170 */
 int blue_phase_random_q_init(cs_t * cs, fe_lc_param_t * param, field_t * q);
 /* Uniform uniaxial nematic along n, src/blue_phase_init.c:836 */

@@ -224,6 +224,12 @@ def _declare(L):
                                     ctypes.c_int),
         "blue_phase_random_q_init": ([_P, ctypes.POINTER(FeLcParam), _P],
                                      ctypes.c_int),
+        "blue_phase_twist_init": ([_P, ctypes.POINTER(FeLcParam), _P,
+                                   ctypes.c_int], ctypes.c_int),
+        "blue_phase_random_q_rectangle": ([_P, ctypes.POINTER(FeLcParam), _P,
+                                           ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)],
+                                          ctypes.c_int),
         "beris_edw_create": ([_P, _P, _P, pp], ctypes.c_int),
         "beris_edw_free": ([_P], ctypes.c_int),
         "beris_edw_param_set": ([_P, ctypes.POINTER(BerisEdwParam)],
@@ -1005,6 +1011,21 @@ class LiquidCrystal:
         _check(lib().blue_phase_random_q_init(self.cs.ptr,
                                               ctypes.byref(self.fe.param),
                                               self.q.ptr), "random_q")
+
+    def init_cholesteric(self, axis):
+        """Cholesteric helix along axis 0, 1 or 2 (X, Y, Z)."""
+        _check(lib().blue_phase_twist_init(self.cs.ptr,
+                                           ctypes.byref(self.fe.param),
+                                           self.q.ptr, int(axis)), "twist")
+
+    def random_rectangle(self, rmin, rmax):
+        """Random directors (amplitude 0.01) in the box rmin..rmax
+        (1-based, inclusive) on top of the current Q."""
+        a = (ctypes.c_int * 3)(*rmin)
+        b = (ctypes.c_int * 3)(*rmax)
+        _check(lib().blue_phase_random_q_rectangle(
+            self.cs.ptr, ctypes.byref(self.fe.param), self.q.ptr, a, b),
+            "random_q_rectangle")
 
     def init_nematic(self, n):
         _check(lib().blue_phase_nematic_init(self.cs.ptr,

@@ -1593,6 +1593,94 @@ int blue_phase_random_q_init(cs_t * cs, fe_lc_param_t * param, field_t * fq) {
   return rc;
 }
 
+/* Cholesteric helix along axis 0, 1, 2 (X, Y, Z), src/blue_phase_init.c:
+ * 763-825: n = (0, cos q0 x, sin q0 x), (cos q0 y, 0, -sin q0 y) or
+ * (cos q0 z, sin q0 z, 0) with 1-based coordinates; Q uniaxial along n */
+int blue_phase_twist_init(cs_t * cs, fe_lc_param_t * param, field_t * fq,
+			  int helical_axis) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5 ||
+      helical_axis < 0 || helical_axis > 2) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_twist_init");
+  }
+  const lgbk_dims_t * d = &cs->d;
+  const long long N = d->nsites;
+  const double q0 = param->q0;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "twist");
+  for (int x = 0; x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	const long long i = ((long long) x*d->ny + y)*d->nz + z;
+	double n[3] = {0.0, 0.0, 0.0}, q[3][3];
+	if (helical_axis == 0) {
+	  n[1] = cos(q0*(x + 1)); n[2] = sin(q0*(x + 1));
+	}
+	else if (helical_axis == 1) {
+	  n[0] = cos(q0*(y + 1)); n[2] = -sin(q0*(y + 1));
+	}
+	else {
+	  n[0] = cos(q0*(z + 1)); n[1] = sin(q0*(z + 1));
+	}
+	for (int a = 0; a < 3; a++) {
+	  for (int b = 0; b < 3; b++) {
+	    q[a][b] = 0.5*param->amplitude0*(3.0*n[a]*n[b] - (double) (a == b));
+	  }
+	}
+	h[0*N + i] = q[0][0]; h[1*N + i] = q[0][1]; h[2*N + i] = q[0][2];
+	h[3*N + i] = q[1][1]; h[4*N + i] = q[1][2];
+      }
+    }
+  }
+  int rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
+/* Random uniaxial directors of amplitude 0.01 superposed (replacing Q) on
+ * the sites of the box rmin..rmax (1-based, inclusive),
+ * src/blue_phase_init.c:1279-1345 (seed 13, as the random initial
+ * condition) */
+int blue_phase_random_q_rectangle(cs_t * cs, fe_lc_param_t * param,
+				  field_t * fq, int rmin[3], int rmax[3]) {
+  if (cs == NULL || param == NULL || fq == NULL || fq->nf != 5 ||
+      rmin == NULL || rmax == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "blue_phase_random_q_rectangle");
+  }
+  const double pi = 3.1415926535897932385;
+  const double a0 = 0.01;
+  const lgbk_dims_t * d = &cs->d;
+  const long long N = d->nsites;
+  double * h = (double *) malloc(5*(size_t) N*sizeof(double));
+  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "random_q_rectangle");
+  int rc = field_to_host(fq, h);
+  for (int x = 0; rc == 0 && x < d->nx; x++) {
+    for (int y = 0; y < d->ny; y++) {
+      for (int z = 0; z < d->nz; z++) {
+	if (x + 1 < rmin[0] || x + 1 > rmax[0] || y + 1 < rmin[1] ||
+	    y + 1 > rmax[1] || z + 1 < rmin[2] || z + 1 > rmax[2]) continue;
+	const long long i = ((long long) x*d->ny + y)*d->nz + z;
+	double r[2], n[3], q[3][3];
+	site_uniforms(13u, x, y, z, 2, r);
+	const double phase1 = 2.0*pi*(0.5 - r[0]);
+	const double phase2 = acos(2.0*r[1] - 1.0);
+	n[0] = cos(phase1)*sin(phase2);
+	n[1] = sin(phase1)*sin(phase2);
+	n[2] = cos(phase2);
+	for (int a = 0; a < 3; a++) {
+	  for (int b = 0; b < 3; b++) {
+	    q[a][b] = 0.5*a0*(3.0*n[a]*n[b] - (double) (a == b));
+	  }
+	}
+	h[0*N + i] = q[0][0]; h[1*N + i] = q[0][1]; h[2*N + i] = q[0][2];
+	h[3*N + i] = q[1][1]; h[4*N + i] = q[1][2];
+      }
+    }
+  }
+  if (rc == 0) rc = field_from_host(fq, h);
+  free(h);
+  return rc;
+}
+
 struct beris_edw_s {
   cs_t * cs;
   beris_edw_param_t param;

@@ -162,7 +162,7 @@ def grad27_cases():
 REGRESSION_LOGS = ("serial-spin-fd1", "serial-spin-lb1", "serial-init-bp1",
                    "serial-symm-dr1", "serial-init-bp2", "serial-relx-bp1",
                    "serial-chol-fld", "serial-init-br1", "serial-init-br2",
-                   "serial-symm-pat", "serial-init-lcr")
+                   "serial-symm-pat", "serial-init-lcr", "serial-init-lcb")
 
 
 def parse_log(path):

@@ -23,7 +23,9 @@ order API:
 * serial-symm-pat: spinodal patches (2^3 cubes of +-1, 10 % of -1) in the
   symmetric binary fluid, 64^3, 27-point gradients, second-order
   advection, one step;
-* serial-init-lcr: random uniaxial directors (amplitude 0.01), one step.
+* serial-init-lcr: random uniaxial directors (amplitude 0.01), one step;
+* serial-init-lcb: a cholesteric helix along x with a 2^3 box of random
+  directors at its centre, one step.
 
 Values are compared to the digits the log prints (8 significant digits
 for most, 11 for the free energy); sums whose terms cancel (momentum,
@@ -302,6 +304,23 @@ def test_serial_init_lcr(gb):
                          kappa1=0.01, xi=0.7, redshift=1.0, amplitude=0.01,
                          q0=0.27768018)
     s.init_random()
+    lc_stats(s, ref[0], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map), ref[0]["fe"])
+    s.step_reference_order(1)
+    lc_stats(s, ref[1], 32 ** 3)
+    check_fe_line(s.fe.stats_info(s.map, recompute=False), ref[1]["fe"])
+    _, u, _ = s.hydro.get()
+    check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_serial_init_lcb(gb):
+    ref = LOGS["serial-init-lcb"]
+    s = gb.LiquidCrystal((32, 32, 32), eta=0.1, gamma_rot=0.1,
+                         a0=0.014384711, gamma=3.1764706, kappa0=0.01,
+                         kappa1=0.01, xi=0.7, redshift=1.0, amplitude=0.01,
+                         q0=0.27768018)
+    s.init_cholesteric(0)
+    s.random_rectangle((16, 16, 16), (17, 17, 17))
     lc_stats(s, ref[0], 32 ** 3)
     check_fe_line(s.fe.stats_info(s.map), ref[0]["fe"])
     s.step_reference_order(1)

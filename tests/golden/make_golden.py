@@ -162,7 +162,8 @@ def grad27_cases():
 REGRESSION_LOGS = ("serial-spin-fd1", "serial-spin-lb1", "serial-init-bp1",
                    "serial-symm-dr1", "serial-init-bp2", "serial-relx-bp1",
                    "serial-chol-fld", "serial-init-br1", "serial-init-br2",
-                   "serial-symm-pat", "serial-init-lcr", "serial-init-lcb")
+                   "serial-symm-pat", "serial-init-lcr", "serial-init-lcb",
+                   "d3q19-io/iodrop-mpi1-io1", "d3q19-io/iodrop-mpi1-io3")
 
 
 def parse_log(path):
@@ -198,9 +199,11 @@ def regression_logs(ref_root):
     """Numbers of the reference's own regression logs for the cases this
     path covers (read as text), into tests/golden/regression_logs.json."""
     import json
-    d = os.path.join(ref_root, "tests", "regression", "d3q19-short")
-    out = {name: parse_log(os.path.join(d, name + ".log"))
-           for name in REGRESSION_LOGS}
+    d = os.path.join(ref_root, "tests", "regression")
+    out = {}
+    for name in REGRESSION_LOGS:
+        sub = name if "/" in name else "d3q19-short/" + name
+        out[name.split("/")[-1]] = parse_log(os.path.join(d, sub + ".log"))
     with open(os.path.join(HERE, "regression_logs.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote regression_logs.json")

@@ -25,7 +25,10 @@ order API:
   advection, one step;
 * serial-init-lcr: random uniaxial directors (amplitude 0.01), one step;
 * serial-init-lcb: a cholesteric helix along x with a 2^3 box of random
-  directors at its centre, one step.
+  directors at its centre, one step;
+* d3q19-io/iodrop-mpi1-io1 and -io3: a drop of radius 8 (32^3, 27-point
+  gradients, second-order advection) run 20 steps straight, and run 10
+  steps, written to snapshot files, read back and run 10 more.
 
 Values are compared to the digits the log prints (8 significant digits
 for most, 11 for the free energy); sums whose terms cancel (momentum,
@@ -328,3 +331,43 @@ def test_serial_init_lcb(gb):
     check_fe_line(s.fe.stats_info(s.map, recompute=False), ref[1]["fe"])
     _, u, _ = s.hydro.get()
     check_common(s, ref[1], u, s.lb.get(), s.lb.moments())
+
+
+def test_iodrop_restart(gb, tmp_path, monkeypatch):
+    """The restart of d3q19-io/iodrop-mpi1-io3: 10 steps, snapshot files
+    (distributions, phi, rho and velocity), a new system read from them,
+    10 more steps; the statistics at step 20 are those of the
+    uninterrupted run (-io1) and of the reference's own restart (-io3)."""
+    io1, io3 = LOGS["iodrop-mpi1-io1"], LOGS["iodrop-mpi1-io3"]
+    A, K, N = -0.00625, 0.004, 32 ** 3
+    monkeypatch.chdir(tmp_path)
+    gb.advection_order(2)
+    try:
+        def system():
+            s = gb.BinaryFluid((32, 32, 32), gb.FP64, a=A, b=-A, kappa=K,
+                               mobility=1.25, eta=0.00625)
+            s.dphi.set_stencil(27)
+            return s
+        a = system()
+        a.phi.init_drop(np.sqrt(-2.0 * K / A), 8.0, 1.0, False)
+        check_scalars(a.phi.stats(), io1[0]["phi"], N)
+        a.step_reference_order(10)
+        check_scalars(a.phi.stats(), io1[1]["phi"], N)
+        assert close(a.fe.fed_total() / N, io1[1]["fed"][1], 1e-9)
+        a.lb.io_write(10)
+        a.phi.io_write(10)
+        a.hydro.io_write(10)
+        b = system()
+        b.lb.io_read(10)
+        b.phi.io_read(10)
+        b.hydro.io_read(10)
+        check_scalars(b.phi.stats(), io3[0]["phi"], N)
+        a.step_reference_order(10)
+        b.step_reference_order(10)
+        for s, ref in ((a, io1[2]), (b, io3[1])):
+            check_scalars(s.phi.stats(), ref["phi"], N)
+            assert close(s.fe.fed_total() / N, ref["fed"][1], 1e-9)
+        assert np.array_equal(a.phi.get(), b.phi.get())
+        assert np.array_equal(a.lb.get(), b.lb.get())
+    finally:
+        gb.advection_order(1)

@@ -360,7 +360,7 @@ def gpu_arm(args):
         # the 64 boxes are shared out over the ranks (no exchange between
         # boxes); one rank runs them all
         from ludwig_gb300 import shard
-        boxes = lg.ensemble_config3()
+        boxes = lg.ensemble_uneven_boxes()
         mine = shard.shard_boxes(boxes, world)[rank]
         e = lg.Ensemble([boxes[i] for i in mine], precision=lg.FP32)
         best, _ = e.autotune(10)

@@ -696,7 +696,8 @@ def phi_cahn_hilliard(pch, fe, phi, hydro, map_=None):
 
 
 class BinaryFluid:
-    """All objects of a symmetric binary fluid (the configs' model)."""
+    """All objects of a symmetric binary fluid (D3Q19 M10, 7- or 27-point
+    gradients, stress divergence, finite-difference Cahn-Hilliard)."""
 
     def __init__(self, ntotal, precision=FP64, a=-0.0625, b=0.0625,
                  kappa=0.04, mobility=0.3, eta=0.1, eta_bulk=None, rho0=1.0,
@@ -972,7 +973,8 @@ class BerisEdw(_Obj):
 
 
 class LiquidCrystal:
-    """All objects of the cholesteric LC with hydrodynamics (config 4)."""
+    """All objects of the cholesteric liquid crystal (Landau-de Gennes,
+    Beris-Edwards), with or without hydrodynamics."""
 
     def __init__(self, ntotal, eta=0.5, gamma_rot=0.5, device=0,
                  precision=FP64, eta_bulk=None, hydrodynamics=True, **lc):
@@ -1168,8 +1170,8 @@ class Ensemble:
         return n.value
 
 
-def ensemble_config3(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
-    """Config 3: boxes with edges drawn per axis from `edges`, viscosity
+def ensemble_uneven_boxes(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
+    """64 uneven boxes: edges drawn per axis from `edges`, viscosity
     U[0.02, 0.2], kappa U[0.02, 0.08], A = -B with |A| U[0.03, 0.1],
     mobility min(0.45, 1/(12 (12 kappa + 2|A|))) (half the stability
     bound of the explicit 7-point Cahn-Hilliard step in the saturated

@@ -94,7 +94,7 @@ def test_model_tables(orc):
         assert any((cv[q] == -cv[p]).all() for q in range(19))
 
 
-# --- cholesteric liquid crystal (config 4 parameters) ----------------------
+# --- cholesteric liquid crystal, blue phase I (A0 0.01, gamma 3, pitch 32) ---
 
 GAMMA_ROT, ETA_LC = 0.5, 0.5
 

@@ -1,4 +1,4 @@
-"""Reduced-precision forms against the FP64 oracle (config 1, 32^3).
+"""Reduced-precision forms against the FP64 oracle (32^3 spinodal, M = 0.3).
 
 Tolerances are the measured GB300 errors with head-room:
   FP32-shifted after 1000 steps: max|dphi| 1.1e-6; mass drift below 1e-10

@@ -15,14 +15,14 @@ sys.path.insert(0, ROOT)
 from ludwig_gb300 import shard  # noqa: E402
 
 
-def config3_extents(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
+def uneven_box_extents(nbox=64, seed=20261203, edges=(32, 48, 64, 96)):
     rng = np.random.default_rng(seed)
     return [[int(rng.choice(edges)) for _ in range(3)] for _ in range(nbox)]
 
 
 @pytest.mark.parametrize("world", [1, 2, 3, 4, 8])
 def test_shards_partition_and_balance(world):
-    boxes = config3_extents()
+    boxes = uneven_box_extents()
     shards = shard.shard_boxes(boxes, world)
     flat = sorted(i for s in shards for i in s)
     assert flat == list(range(len(boxes)))
@@ -49,7 +49,7 @@ def _worker(rank, world, port, q):
     import bench
     w, r, local, pg = bench.dist_setup()
     try:
-        boxes = config3_extents()
+        boxes = uneven_box_extents()
         mine = shard.shard_boxes(boxes, w)[r]
         stats = [shard.box_sites(boxes[i]) for i in mine]
         full = shard.gather_box_stats(pg, len(boxes), mine, stats)
@@ -74,7 +74,7 @@ def test_two_ranks_gloo():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    boxes = config3_extents()
+    boxes = uneven_box_extents()
     want = [shard.box_sites(b) for b in boxes]
     for r, full, sites, slowest in res:
         assert full == want                  # every box once, in order

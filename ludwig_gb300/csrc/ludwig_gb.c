@@ -2960,6 +2960,7 @@ int ludwig_gb_ensemble_autotune(ludwig_gb_ensemble_t * e, int trial_steps,
 				int best[3], double * ms_best) {
   static const int cand[][3] = {{16, 4, 0}, {32, 4, 0}, {8, 4, 0},
 				{16, 8, 4}, {32, 8, 4}, {16, 8, 3},
+				{32, 8, 3}, {64, 8, 3}, {96, 8, 3},
 				{32, 16, 2}};
   const int ncand = (int) (sizeof(cand)/sizeof(cand[0]));
   if (e == NULL || trial_steps < 2) {

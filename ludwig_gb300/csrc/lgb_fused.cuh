@@ -148,6 +148,9 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
   const T pa = KP<T>::get(a, LGBK_P_A);
   const T pb = KP<T>::get(a, LGBK_P_B);
   const T kappa = KP<T>::get(a, LGBK_P_KAPPA);
+  /* Reduced-precision forms (float): free of the reference's operation
+   * order, so cancelling terms and additions of zero are left out */
+  constexpr bool RED = (sizeof(T) == 4);
 
   const int cidx = (ty + 1)*DZ + (tz + 1);       /* own site in D/u */
   const int pidx = (ty + 2)*PZ + (tz + 2);       /* own site in phi */
@@ -226,12 +229,14 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
       g[2] = T(0.5)*(zp - zm);
       T delsq = xp + xm + yp + ym + zp + zm - T(6.0)*c;
       T p0 = lgb_symm_p0<T>(pa, pb, kappa, c, delsq, g);
-      T p0z = p0*T(0.0);
+      T p0z = RED ? T(0.0) : p0*T(0.0);
       #pragma unroll
       for (int ia = 0; ia < 3; ia++) {
 	#pragma unroll
 	for (int ib = 0; ib < 3; ib++) {
-	  D[(3*ia + ib)*ND + k] = ((ia == ib) ? p0 : p0z) + kappa*g[ia]*g[ib];
+	  if (RED && ia != ib) D[(3*ia + ib)*ND + k] = kappa*g[ia]*g[ib];
+	  else D[(3*ia + ib)*ND + k] = ((ia == ib) ? p0 : p0z)
+		 + kappa*g[ia]*g[ib];
 	}
       }
       D[9*ND + k] = lgb_symm_mu<T>(pa, pb, kappa, c, delsq);
@@ -277,7 +282,7 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
     compute_D(x0 - 1);
     __syncthreads();
 
-    T prevP[3], prev_mu, prev_phi, prev_ux;
+    T prevP[3], prev_mu, prev_phi, prev_ux, prev_fe = T(0.0);
     {
       const T * D = sD + dslot(x0 - 1)*SM::NDC*ND;
       #pragma unroll
@@ -295,7 +300,9 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 
     for (int x = x0; x < xe; x++) {
 
-      const long long s0 = (long long) x*NP + syz;
+      /* site index: 32-bit unsigned (the host refuses lattices of 2^32
+       * sites or more), pointers formed from per-component bases */
+      const unsigned s0 = (unsigned) x*NP + syz;
       const int oxp = (x == 0) ? (d.nx - 1)*NP : -NP;
       const int oxm = (x == d.nx - 1) ? -(d.nx - 1)*NP : NP;
 
@@ -303,7 +310,6 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
        * stencil phase, so their latency overlaps it. */
       T fs[LGB_NVEL];
       if (active) {
-	const S * fb = f_in + s0;
 	Unroll<LGB_NVEL>::run([&](auto P) {
 	  constexpr int p = decltype(P)::value;
 	  int off = 0;
@@ -313,7 +319,8 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 	  if (Cv<p>::Y == -1) off += oym;
 	  if (Cv<p>::Z == +1) off += ozp;
 	  if (Cv<p>::Z == -1) off += ozm;
-	  fs[p] = FStore<S, T>::ld(fb + p*N + off, rfscale);
+	  const S * fp = f_in + p*N;
+	  fs[p] = FStore<S, T>::ld(fp + (s0 + off), rfscale);
 	});
       }
 
@@ -347,12 +354,20 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 	  const T * Pz = Dc + (3*ia + 2)*ND;
 	  T pxc = Px[cidx];
 	  T fa;
-	  fa  = -T(0.5)*(Dn[(3*ia)*ND + cidx] + pxc);
-	  fa +=  T(0.5)*(prevP[ia] + pxc);
-	  fa -=  T(0.5)*(Py[cidx + DZ] + Py[cidx]);
-	  fa +=  T(0.5)*(Py[cidx - DZ] + Py[cidx]);
-	  fa -=  T(0.5)*(Pz[cidx + 1] + Pz[cidx]);
-	  fa +=  T(0.5)*(Pz[cidx - 1] + Pz[cidx]);
+	  if (RED) {
+	    /* the face values' own-site halves cancel */
+	    fa = T(0.5)*((prevP[ia] - Dn[(3*ia)*ND + cidx])
+			 + (Py[cidx - DZ] - Py[cidx + DZ])
+			 + (Pz[cidx - 1] - Pz[cidx + 1]));
+	  }
+	  else {
+	    fa  = -T(0.5)*(Dn[(3*ia)*ND + cidx] + pxc);
+	    fa +=  T(0.5)*(prevP[ia] + pxc);
+	    fa -=  T(0.5)*(Py[cidx + DZ] + Py[cidx]);
+	    fa +=  T(0.5)*(Py[cidx - DZ] + Py[cidx]);
+	    fa -=  T(0.5)*(Pz[cidx + 1] + Pz[cidx]);
+	    fa +=  T(0.5)*(Pz[cidx - 1] + Pz[cidx]);
+	  }
 	  force[ia] = fa;
 	  prevP[ia] = pxc;
 	}
@@ -363,7 +378,10 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 	const T muc = Dc[9*ND + cidx];
 	const T uxc = su[cidx], uyc = su[ND + cidx], uzc = su[2*ND + cidx];
 	T fw, fe, fy, fym, fz, fzm;
-	{
+	if (RED && x > x0) {
+	  fw = prev_fe;      /* the x-1 site's east face is this west face */
+	}
+	else {
 	  T uf = T(0.5)*(uxc + prev_ux);
 	  fw = uf*((uf > T(0.0)) ? prev_phi : phic);
 	  fw -= mobility*(muc - prev_mu);
@@ -413,6 +431,7 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 
 	/* src/phi_cahn_hilliard.c:1040-1045 with wz = 1 */
 	phi_out[s0] = phic - (+ fe - fw + fy - fym + fz - fzm);
+	prev_fe = fe;
 
 	prev_ux = uxc;
 	prev_mu = muc;
@@ -422,12 +441,13 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 	T ftot[3];
 	#pragma unroll
 	for (int ia = 0; ia < 3; ia++) {
-	  ftot[ia] = KP<T>::get(a, LGBK_P_FX + ia)
-	    + (T(0.0) + force[ia]*T(1.0));
+	  if (RED) ftot[ia] = KP<T>::get(a, LGBK_P_FX + ia) + force[ia];
+	  else     ftot[ia] = KP<T>::get(a, LGBK_P_FX + ia)
+		     + (T(0.0) + force[ia]*T(1.0));
 	}
 	if (force_out) {
 	  #pragma unroll
-	  for (int ia = 0; ia < 3; ia++) force_out[ia*N + s0] = force[ia];
+	  for (int ia = 0; ia < 3; ia++) (force_out + ia*N)[s0] = force[ia];
 	}
 
 	T rho, uu[3];
@@ -440,13 +460,12 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 	else {
 	  uu[0] = uu[1] = uu[2] = T(0.0);
 	}
-	S * ob = f_out + s0;
 	#pragma unroll
 	for (int p = 0; p < LGB_NVEL; p++) {
-	  FStore<S, T>::st(ob + p*N, fs[p], fscale);
+	  FStore<S, T>::st(f_out + p*N + s0, fs[p], fscale);
 	}
 	#pragma unroll
-	for (int ia = 0; ia < 3; ia++) u_out[ia*N + s0] = uu[ia];
+	for (int ia = 0; ia < 3; ia++) (u_out + ia*N)[s0] = uu[ia];
       }
     }
     __pipeline_wait_prior(0);

@@ -77,6 +77,7 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 				int ty, int minb, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
   if (ty <= 0) ty = 8;
+  if (d->nsites >= LGBK_MAX_SITES) return (int) cudaErrorInvalidValue;
   switch (prec) {
   case LGBK_PREC_FP64:
     return lgbk_binary_step_f64(d, a, xchunk, ty, stream);

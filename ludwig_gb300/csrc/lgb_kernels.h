@@ -30,6 +30,11 @@ typedef struct lgbk_dims_s {
   long long nsites;
 } lgbk_dims_t;
 
+/* The fused steps index sites with 32-bit unsigned integers: a lattice
+ * (or ensemble box) holds fewer sites than this.  At the smallest storage
+ * (108 B per site, FP16) 2^32 sites would need 464 GB. */
+#define LGBK_MAX_SITES (1LL << 32)
+
 typedef struct lgbk_symm_s {
   double a, b, kappa;
 } lgbk_symm_t;

@@ -2766,8 +2766,13 @@ int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
 	return err_set(LUDWIG_GB_EINVAL, "ensemble: box %d extent < 2", b);
       }
     }
-    e->off[b + 1] = e->off[b]
-      + (long long) p[b].ntotal[0]*p[b].ntotal[1]*p[b].ntotal[2];
+    long long nb = (long long) p[b].ntotal[0]*p[b].ntotal[1]*p[b].ntotal[2];
+    if (nb >= LGBK_MAX_SITES) {
+      ludwig_gb_ensemble_free(e);
+      return err_set(LUDWIG_GB_EINVAL, "ensemble: box %d has 2^32 sites "
+		     "or more", b);
+    }
+    e->off[b + 1] = e->off[b] + nb;
     e->active[b] = 1;
   }
   e->ntot = e->off[nbox];

@@ -303,8 +303,10 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
       /* site index: 32-bit unsigned (the host refuses lattices of 2^32
        * sites or more), pointers formed from per-component bases */
       const unsigned s0 = (unsigned) x*NP + syz;
-      const int oxp = (x == 0) ? (d.nx - 1)*NP : -NP;
-      const int oxm = (x == d.nx - 1) ? -(d.nx - 1)*NP : NP;
+      /* x offsets of the pull sources, modulo 2^32 */
+      const unsigned oxp = (x == 0) ? (unsigned) (d.nx - 1)*NP : 0u - NP;
+      const unsigned oxm = (x == d.nx - 1) ? 0u - (unsigned) (d.nx - 1)*NP
+	: (unsigned) NP;
 
       /* Pulled populations f_p(x - c_p): issued first, consumed after the
        * stencil phase, so their latency overlaps it. */
@@ -312,7 +314,7 @@ binary_item(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
       if (active) {
 	Unroll<LGB_NVEL>::run([&](auto P) {
 	  constexpr int p = decltype(P)::value;
-	  int off = 0;
+	  unsigned off = 0;
 	  if (Cv<p>::X == +1) off += oxp;
 	  if (Cv<p>::X == -1) off += oxm;
 	  if (Cv<p>::Y == +1) off += oyp;

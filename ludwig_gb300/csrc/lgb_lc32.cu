@@ -67,6 +67,7 @@ extern "C" int lgbk_lc_step(const lgbk_dims_t * d, int prec,
 			    const lgbk_lc_t * p, const lgbk_lc_step_args_t * a,
 			    void * stream) {
   if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
+  if (d->nsites >= LGBK_MAX_SITES) return (int) cudaErrorInvalidValue;
   switch (prec) {
   case LGBK_PREC_FP64: return lgbk_lc_step_f64(d, p, a, stream);
   case LGBK_PREC_FP32: return lc_step32<float>(d, p, a, (cudaStream_t) stream);

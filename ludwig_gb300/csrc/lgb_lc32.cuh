@@ -47,12 +47,15 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
   if (z >= d.nz || y >= d.ny) return;
   const long long N = d.nsites;
   const int NP = d.ny*d.nz;
-  const long long i = (long long) x*NP + y*d.nz + z;
+  /* 32-bit unsigned site indices (the host refuses 2^32 sites or more);
+   * pointers are formed from per-component bases */
+  const unsigned i = (unsigned) x*NP + y*d.nz + z;
   const float r3 = 1.0f/3.0f;
   /* neighbours: 0 x+1, 1 x-1, 2 y+1, 3 y-1, 4 z+1, 5 z-1 */
-  const long long nb[6] = {
-    i + ((x == d.nx - 1) ? -(long long) (d.nx - 1)*NP : NP),
-    i + ((x == 0) ? (long long) (d.nx - 1)*NP : -NP),
+  const unsigned xw = (unsigned) (d.nx - 1)*NP;   /* x wrap, modulo 2^32 */
+  const unsigned nb[6] = {
+    (x == d.nx - 1) ? i - xw : i + NP,
+    (x == 0) ? i + xw : i - NP,
     i + ((y == d.ny - 1) ? -(d.ny - 1)*d.nz : d.nz),
     i + ((y == 0) ? (d.ny - 1)*d.nz : -d.nz),
     i + ((z == d.nz - 1) ? -(d.nz - 1) : 1),
@@ -102,12 +105,12 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
   #pragma unroll
   for (int ia = 0; ia < 3; ia++)
     #pragma unroll
-    for (int ib = 0; ib < 3; ib++) pth[(3*ia + ib)*N + i] = sth[ia][ib];
+    for (int ib = 0; ib < 3; ib++) (pth + (3*ia + ib)*N)[i] = sth[ia][ib];
 
   const bool fluid = !HAS_MAP || st[i] == 0;
   if (!fluid) {
     #pragma unroll
-    for (int n = 0; n < 5; n++) qo[n*N + i] = qc[n];
+    for (int n = 0; n < 5; n++) (qo + n*N)[i] = qc[n];
     return;
   }
 
@@ -169,7 +172,7 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
     const float fz = mz*uzp*((uzp < 0.0f) ? qn[n][4] : qc[n]);
     const float fyj = mym*uym*((uym < 0.0f) ? qc[n] : qn[n][3]);
     const float fzk = mzm*uzm*((uzm < 0.0f) ? qc[n] : qn[n][5]);
-    qo[n*N + i] = qc[n] + (s5[n] + gamma_rot*hv[n] - fe + fw - fy + fyj
+    (qo + n*N)[i] = qc[n] + (s5[n] + gamma_rot*hv[n] - fe + fw - fy + fyj
 			   - fz + fzk);
   }
 }

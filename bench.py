@@ -331,7 +331,7 @@ def gpu_arm(args):
         ms64 = max_over_ranks(pg, ms64)
         s64 = None
 
-    # --- cholesteric LC, 128^3, FP32 and FP64 (config-4 model) ----------
+    # --- cholesteric LC (blue phase I), 128^3, FP32 and FP64 ------------
     lc = None
     if "lc" in legs:
         lc = {}

@@ -1,6 +1,6 @@
 """Reduced-precision forms of the binary-fluid step against FP64.
 
-The symmetric binary fluid (config-1 parameters, M = 0.3) is run from the
+The symmetric binary fluid (A = -B = -0.0625, kappa = 0.04, M = 0.3) is run from the
 same KISS99 spinodal initial condition in FP64 (the bit-exact form), in
 FP32 with distributions stored as deviations from w_p rho0, and with
 FP16 storage.  At fixed intervals it reports, for each reduced form:

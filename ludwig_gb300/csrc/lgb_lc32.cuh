@@ -34,11 +34,15 @@
 #include "lgb_lc.cuh"
 
 /* Launch shape of k_lc32_fields_be: blocks of 32 (z) x LC32_FY (y) sites,
- * grid (z tiles * y tiles, nx) */
-#define LC32_FY 4
+ * grid (z tiles * y tiles, nx), LC32_FMINB blocks per SM (a cap of 102
+ * registers, no spills).  Measured LC step at 128^3 (FY, blocks/SM):
+ * (4, 4) 0.169 ms, (4, 5) 0.162, (4, 6) 0.171 (spills), (2, 10) 0.162,
+ * (8, 2) 0.173. */
+#define LC32_FY 2
+#define LC32_FMINB 10
 
 template <bool HAS_MAP>
-__global__ void __launch_bounds__(32*LC32_FY, 4)
+__global__ void __launch_bounds__(32*LC32_FY, LC32_FMINB)
 k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
   const int ntz = (d.nz + 31)/32;
   const int z = (blockIdx.x % ntz)*32 + threadIdx.x;

@@ -334,14 +334,11 @@ k_lc32_collide(lgbk_dims_t d, lgbk_lc_step_args_t a, int xchunk) {
 	  const float * Py = Pc + (3*ia + 1)*ND;
 	  const float * Pz = Pc + (3*ia + 2)*ND;
 	  const float pxc = Px[cidx];
-	  float fa;
-	  fa  = -0.5f*(Pn[(3*ia)*ND + cidx] + pxc);
-	  fa +=  0.5f*(prevP[ia] + pxc);
-	  fa -=  0.5f*(Py[cidx + DZ] + Py[cidx]);
-	  fa +=  0.5f*(Py[cidx - DZ] + Py[cidx]);
-	  fa -=  0.5f*(Pz[cidx + 1] + Pz[cidx]);
-	  fa +=  0.5f*(Pz[cidx - 1] + Pz[cidx]);
-	  force[ia] = fa;
+	  /* minus the divergence of the face values 0.5 (P(s) + P(s + e));
+	   * the own-site halves cancel */
+	  force[ia] = 0.5f*((prevP[ia] - Pn[(3*ia)*ND + cidx])
+			    + (Py[cidx - DZ] - Py[cidx + DZ])
+			    + (Pz[cidx - 1] - Pz[cidx + 1]));
 	  prevP[ia] = pxc;
 	}
 	const bool fluid = !HAS_MAP || st[s0] == 0;

@@ -55,11 +55,13 @@ ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108,
 NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": None}
 
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
-LIMITER = {"fp32": "hbm (traffic = compulsory bytes; latency gap)",
+LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",
            "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
-           "fp16": "hbm", "lc64": "fp64 pipe",
-           "lc32": "two kernels: fields + Beris-Edwards (FP32 issue "
-                   "bound), force + collision (HBM, 2.5-D); the stress "
+           "fp16": "issue (same instructions as fp32 plus conversions; "
+                   "108 B/site)",
+           "lc64": "fp64 pipe",
+           "lc32": "two kernels: fields + Beris-Edwards (issue and load "
+                   "latency), force + collision (HBM, 2.5-D); the stress "
                    "(9 values a site) crosses HBM between them"}
 
 

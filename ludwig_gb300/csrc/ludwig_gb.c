@@ -212,6 +212,10 @@ int cs_init(cs_t * cs) {
   cs->d.ny = cs->ntotal[1];
   cs->d.nz = cs->ntotal[2];
   cs->d.nsites = (long long) cs->d.nx*cs->d.ny*cs->d.nz;
+  if (cs->d.nsites >= LGBK_MAX_SITES) {
+    return err_set(LUDWIG_GB_EINVAL, "cs_init: %lld sites; the lattice "
+		   "must hold fewer than 2^32", cs->d.nsites);
+  }
   cs->initialised = 1;
   return LUDWIG_GB_OK;
 }

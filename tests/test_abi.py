@@ -43,3 +43,23 @@ def test_error_reporting_without_device(gb):
     rc = L.cs_ntotal_set(None, (ctypes.c_int * 3)(4, 4, 4))
     assert rc == 1
     assert b"cs" in L.ludwig_gb_last_error()
+
+
+def test_lattice_size_limit_without_device(gb):
+    """Site indices are 32-bit unsigned: cs_init refuses 2^32 sites."""
+    L = gb.lib()
+    cs = ctypes.c_void_p()
+    assert L.cs_create(None, ctypes.byref(cs)) == 0
+    try:
+        assert L.cs_ntotal_set(cs, (ctypes.c_int * 3)(2048, 2048, 1024)) == 0
+        assert L.cs_init(cs) == 1
+        assert b"2^32" in L.ludwig_gb_last_error()
+    finally:
+        L.cs_free(cs)
+    cs = ctypes.c_void_p()
+    assert L.cs_create(None, ctypes.byref(cs)) == 0
+    try:
+        assert L.cs_ntotal_set(cs, (ctypes.c_int * 3)(2048, 2048, 1023)) == 0
+        assert L.cs_init(cs) == 0
+    finally:
+        L.cs_free(cs)

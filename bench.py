@@ -49,10 +49,11 @@ ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108,
               "lc64": 432, "lc32": 216}
 
 # DRAM bytes (read + write) per site of the fused kernels from one ncu
-# capture at 160^3 (profiles/k_binary_fused_fp32_160cube.md and
-# profiles/k_binary_fused_fp64_160cube.md); a streaming kernel's traffic
+# capture at 160^3 (profiles/k_binary_fused_fp32_160cube.md,
+# profiles/k_binary_fused_fp64_160cube.md and
+# profiles/k_binary_fused_fp16_160cube.md); a streaming kernel's traffic
 # grows in proportion to the sites, so traffic = bytes/site x sites.
-NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": None}
+NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4}
 
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
 LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",

@@ -81,3 +81,30 @@ def test_fp32_ragged_lattice_close_to_fp64(gb, L):
         s.step(40)
     assert np.abs(a.phi.get() - b.phi.get()).max() < 1e-6
     assert np.abs(a.lb.get() - b.lb.get()).max() < 1e-6
+
+
+@pytest.mark.parametrize("prec,tol_phi,tol_f", [(1, 1e-6, 1e-6),
+                                                (2, 1e-5, 1e-5)])
+def test_reduced_with_solid_sites_close_to_fp64(gb, prec, tol_phi, tol_f):
+    """The map branch of the reduced forms (no-flux faces next to solid
+    sites, no collision on them) against the FP64 path, which matches the
+    oracle bit for bit with the same map; a ragged z extent."""
+    L = (12, 10, 40)
+    rng = np.random.default_rng(6)
+    status = (rng.uniform(size=L) < 0.1).astype(np.uint8)
+    a = gb.BinaryFluid(L, precision=gb.FP64, mobility=MOB, eta=ETA)
+    b = gb.BinaryFluid(L, precision=prec, mobility=MOB, eta=ETA)
+    for s in (a, b):
+        s.map.set_status(status)
+        s.phi.init_spinodal(8361235, 0.0, 0.02)
+    phi0 = b.phi.get()
+    for s in (a, b):
+        s.step(50)
+    pa, pb = a.phi.get(), b.phi.get()
+    assert np.abs(pa - pb).max() < tol_phi
+    assert np.abs(a.lb.get() - b.lb.get()).max() < tol_f
+    # no flux through a face next to a solid site: total phi is kept
+    assert abs(pb.sum() - phi0.sum()) < 1e-4
+    # solid sites keep their phi
+    solid = status == 1
+    assert np.array_equal(pb[0][solid], phi0[0][solid])

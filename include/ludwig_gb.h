@@ -517,7 +517,9 @@ int ludwig_gb_length_from_sk(field_t * phi, int faithful, double * length,
  * cudaMalloc): d_data is the caller's device array of ncomp x nsites
  * doubles (component-major), out the caller's host array of 5*ncomp
  * doubles, per component {total, mean, variance, min, max} as
- * stats_field_q.  stream is a cudaStream_t (NULL: the default stream).
+ * stats_field_q computes them, but over every site of d_data (there is no
+ * status map; stats_field_q skips solid sites).  stream is a cudaStream_t
+ * (NULL: the default stream).
  * Partial sums go to a static device array sized for at most
  * LUDWIG_GB_NOALLOC_MAX_NCOMP components; larger ncomp is rejected with
  * LUDWIG_GB_EINVAL.  The first call on each device looks up that array's

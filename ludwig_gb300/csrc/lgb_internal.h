@@ -16,6 +16,10 @@
 #include "ludwig_gb.h"
 #include "lgb_kernels.h"
 
+#ifdef __cplusplus
+extern "C" {
+#endif
+
 typedef struct lgb_view_s {
   lgbk_dims_t d;
   int prec;                   /* LUDWIG_GB_FP64 / FP32 / FP16 */
@@ -54,5 +58,9 @@ int lgb_internal_hydro_io(hydro_t * h, int ntotal[3], lgb_io_state_t ** rho,
 
 int lgb_internal_err(int code, const char * what);     /* LUDWIG_GB_* code */
 int lgb_internal_cuda(int cuda_rc, const char * where); /* cudaError_t -> ECUDA */
+
+#ifdef __cplusplus
+}
+#endif
 
 #endif

@@ -14,7 +14,11 @@
  *
  *****************************************************************************/
 
+#include <atomic>
+#include <cstdio>
+
 #include "lgb_fused.cuh"
+#include "lgb_internal.h"
 #include "lgb_stats.h"
 #include "ludwig_gb.h"
 
@@ -375,18 +379,23 @@ extern "C" int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,
  *  allocates.
  *
  *  The array is a file-scope __device__ variable: every GPU that loads the
- *  library holds it (LUDWIG_GB_NOALLOC_SCRATCH_DOUBLES doubles, 328 KB)
- *  until the process exits.  Host code cannot use the name of a __device__
+ *  library holds it (NOALLOC_MAX_NCOMP*NOALLOC_SLOT doubles, 328 KB) until
+ *  the process exits.  Host code cannot use the name of a __device__
  *  variable as a device address (on the host it names a stand-in object),
  *  so the device address is looked up with cudaGetSymbolAddress once per
  *  device, with that device current, on the first call made on it.  That
- *  first call should therefore come before any stream capture.
+ *  first call should therefore come before any stream capture.  The
+ *  per-device addresses are cached in atomics, so first calls from several
+ *  host threads at once are well defined (they store the same address).
  *
  *  All calls share the one array and it keeps whatever the last call left
  *  there: each call writes every partial record it later reads, so nothing
  *  has to be cleared first.  Calls whose work overlaps on the GPU (several
  *  host threads, or several streams) race on the array; the caller must
  *  order them, for instance by using one stream.
+ *
+ *  Every site of d_data is counted: there is no status map, unlike
+ *  stats_field_q, which skips solid sites.
  *
  *****************************************************************************/
 
@@ -398,7 +407,14 @@ extern "C" int lgbk_symm_fed_total(const lgbk_dims_t * d, int prec,
 static __device__ __align__(256) double
   lgb_noalloc_scratch[NOALLOC_MAX_NCOMP*NOALLOC_SLOT];
 
-static double * noalloc_addr_[NOALLOC_DEVICES];
+static std::atomic<double *> noalloc_addr_[NOALLOC_DEVICES];
+
+static int noalloc_cuda(cudaError_t err, const char * where) {
+  char msg[256];
+  snprintf(msg, sizeof(msg), "ludwig_gb_field_stats_noalloc: %s: %s", where,
+	   cudaGetErrorString(err));
+  return lgb_internal_err(LUDWIG_GB_ECUDA, msg);
+}
 
 extern "C" int ludwig_gb_field_stats_noalloc(const double * d_data,
 					     long long nsites, int ncomp,
@@ -411,34 +427,52 @@ extern "C" int ludwig_gb_field_stats_noalloc(const double * d_data,
 		"static scratch sized for the documented maximum");
 
   /* More components than the static array holds partials for */
-  if (ncomp < 1 || ncomp > NOALLOC_MAX_NCOMP) return LUDWIG_GB_EINVAL;
-  if (d_data == NULL || out == NULL || nsites <= 0) return LUDWIG_GB_EINVAL;
+  if (ncomp < 1 || ncomp > NOALLOC_MAX_NCOMP) {
+    char msg[160];
+    snprintf(msg, sizeof(msg), "ludwig_gb_field_stats_noalloc: ncomp = %d; "
+	     "the static scratch holds 1 to %d components", ncomp,
+	     NOALLOC_MAX_NCOMP);
+    return lgb_internal_err(LUDWIG_GB_EINVAL, msg);
+  }
+  if (d_data == NULL || out == NULL || nsites <= 0) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL, "ludwig_gb_field_stats_noalloc:"
+			    " NULL data or result, or nsites <= 0");
+  }
 
   cudaError_t err = cudaGetDevice(&dev);
-  if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
-  if (dev < 0 || dev >= NOALLOC_DEVICES) return LUDWIG_GB_EINVAL;
-  if (noalloc_addr_[dev] == NULL) {
+  if (err != cudaSuccess) return noalloc_cuda(err, "cudaGetDevice");
+  if (dev < 0 || dev >= NOALLOC_DEVICES) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL, "ludwig_gb_field_stats_noalloc:"
+			    " device ordinal beyond the address cache (64)");
+  }
+  double * base = noalloc_addr_[dev].load(std::memory_order_acquire);
+  if (base == NULL) {
     /* once per device, with that device current */
     void * p = NULL;
     err = cudaGetSymbolAddress(&p, lgb_noalloc_scratch);
-    if (err != cudaSuccess || p == NULL) return LUDWIG_GB_ECUDA;
-    noalloc_addr_[dev] = (double *) p;
+    if (err != cudaSuccess) return noalloc_cuda(err, "cudaGetSymbolAddress");
+    if (p == NULL) {
+      return lgb_internal_err(LUDWIG_GB_ECUDA, "ludwig_gb_field_stats_noalloc:"
+			      " cudaGetSymbolAddress returned NULL");
+    }
+    base = (double *) p;
+    noalloc_addr_[dev].store(base, std::memory_order_release);
   }
 
   for (int n = 0; n < ncomp; n++) {
-    double * part = noalloc_addr_[dev] + (size_t) n*NOALLOC_SLOT;
+    double * part = base + (size_t) n*NOALLOC_SLOT;
     double * fin = part + (size_t) LGBK_RED_BLOCKS*NOALLOC_REC;
     k_field_stats<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
       nsites, d_data + (size_t) n*nsites, part);
     k_final<2><<<1, 32, 0, s>>>(part, LGBK_RED_BLOCKS, fin);
     err = cudaGetLastError();
-    if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+    if (err != cudaSuccess) return noalloc_cuda(err, "kernel launch");
     err = cudaMemcpyAsync(raw[n], fin, 4*sizeof(double),
 			  cudaMemcpyDeviceToHost, s);
-    if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+    if (err != cudaSuccess) return noalloc_cuda(err, "cudaMemcpyAsync");
   }
   err = cudaStreamSynchronize(s);
-  if (err != cudaSuccess) return LUDWIG_GB_ECUDA;
+  if (err != cudaSuccess) return noalloc_cuda(err, "cudaStreamSynchronize");
 
   for (int n = 0; n < ncomp; n++) {
     double rvol = 1.0/(double) nsites;

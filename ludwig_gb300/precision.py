@@ -9,6 +9,11 @@ and the domain length L(t) from the structure factor next to FP64's.
 
     python -m ludwig_gb300.precision --size 256 --steps 10000 --every 1000
     python -m ludwig_gb300.precision --lc --size 128 --steps 5000 --every 500
+    python -m ludwig_gb300.precision --ensemble --steps 1000
+
+For ensembles (many boxes of uneven sizes and parameters in one launch),
+every box of the FP32 ensemble is compared with the same box of an FP64
+ensemble: max |phi - phi_FP64| and the relative mass drift since step 0.
 """
 
 import argparse
@@ -122,6 +127,48 @@ def run_lc(size, steps, every, log=print):
     return recs
 
 
+def _box_mass(ens, b):
+    """Total mass of one box: the sum of its distributions, in FP64 (the
+    reference f of a reduced-precision box is w_p rho0 plus the stored
+    deviation, converted exactly)."""
+    f = ens.box(b, f=True)["f"]
+    return float(np.sum(f, dtype=np.float64))
+
+
+def ensemble_error(params, steps, log=None):
+    """Per-box error of the FP32-shifted ensemble against the FP64 one after
+    `steps` steps.  Returns one record a box (edges, max |dphi|, max |phi|,
+    relative mass drift of the FP32 box since step 0 and of the FP64 box)
+    and the maxima over the boxes."""
+    from . import Ensemble
+    e32 = Ensemble(params, precision=FP32)
+    e64 = Ensemble(params, precision=FP64)
+    m0 = [float(np.prod(p.ntotal)) * p.rho0 for p in params]
+    e32.step(steps)
+    e64.step(steps)
+    boxes = []
+    for b, p in enumerate(params):
+        g32 = e32.box(b)
+        g64 = e64.box(b)
+        m32 = _box_mass(e32, b)
+        m64 = _box_mass(e64, b)
+        rec = {"box": b, "ntotal": list(p.ntotal),
+               "max_abs_dphi": float(np.abs(g32["phi"] - g64["phi"]).max()),
+               "max_abs_phi": float(np.abs(g64["phi"]).max()),
+               "mass_drift_rel": abs(m32 - m0[b]) / m0[b],
+               "mass_drift_rel_fp64": abs(m64 - m0[b]) / m0[b]}
+        boxes.append(rec)
+        if log:
+            log(json.dumps(rec))
+    e32.close()
+    e64.close()
+    return {"steps": steps, "nbox": len(params),
+            "max_dphi_max": max(r["max_abs_dphi"] for r in boxes),
+            "drift_max": max(r["mass_drift_rel"] for r in boxes),
+            "drift_max_fp64": max(r["mass_drift_rel_fp64"] for r in boxes),
+            "boxes": boxes}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--size", type=int, default=256)
@@ -136,9 +183,16 @@ def main(argv=None):
                     "once the domains saturate")
     ap.add_argument("--lc", action="store_true",
                     help="the cholesteric LC (FP64 vs FP32) instead")
+    ap.add_argument("--ensemble", action="store_true",
+                    help="the 64-box uneven ensemble (FP32 vs FP64 per box)")
     args = ap.parse_args(argv)
     load_library()
-    if args.lc:
+    if args.ensemble:
+        from . import ensemble_uneven_boxes
+        res = ensemble_error(ensemble_uneven_boxes(), args.steps,
+                             log=print)
+        res["model"] = "ensemble of 64 uneven binary-fluid boxes"
+    elif args.lc:
         recs = run_lc(args.size, args.steps, args.every)
         res = {"model": "cholesteric LC", "size": args.size,
                "steps": args.steps, "params": LC_PARAMS, "records": recs}

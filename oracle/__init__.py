@@ -34,13 +34,28 @@ def build(quiet=True):
         print(out.stdout)
 
 
-def build_reference(ref_root="/root/reference", jobs=8):
+def reference_root():
+    """Where the reference's sources are: $LUDWIG_REFERENCE_ROOT, else the
+    default REF of the build recipe oracle/ref.mk."""
+    env = os.environ.get("LUDWIG_REFERENCE_ROOT")
+    if env:
+        return env
+    with open(os.path.join(HERE, "ref.mk")) as fh:
+        for line in fh:
+            if line.startswith("REF") and "?=" in line:
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+def build_reference(ref_root=None, jobs=8):
     """Build the reference itself (serial+OpenMP) into oracle/_ref.
 
     Only possible where the reference sources are present; used to pin the
     oracle and to regenerate golden fixtures.
     """
-    if not os.path.isdir(ref_root):
+    if ref_root is None:
+        ref_root = reference_root()
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     out = subprocess.run(["make", "-f", os.path.join(HERE, "ref.mk"),
                           "REF=" + ref_root, "-j%d" % jobs],

@@ -7,9 +7,11 @@ phi_force_calculation, phi_cahn_hilliard and the main-loop step of
 src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
 
 Needs the reference sources (only where they are present):
-    python tests/golden/make_golden.py [/path/to/reference] [--only=lb2|grad27|logs|advection|io]
+    python tests/golden/make_golden.py [/path/to/reference]
+(default: $LUDWIG_REFERENCE_ROOT, else REF of oracle/ref.mk) [--only=lb2|grad27|logs|advection|io|config1]
 """
 
+import hashlib
 import os
 import sys
 import tempfile
@@ -32,9 +34,15 @@ def kv(L, **extra):
     return d
 
 
+def sha256_of(a):
+    """SHA-256 of an array's values as little-endian doubles in C order: a
+    compact bit-for-bit pin of a field too large to commit whole."""
+    return hashlib.sha256(np.ascontiguousarray(a, "<f8").tobytes()).hexdigest()
+
+
 def run_case(name, L, steps, seed, status=None, keep=("phi", "u", "rho",
                                                        "force", "f"),
-             **extra):
+             hashed=(), **extra):
     with tempfile.TemporaryDirectory() as tmp:
         out = os.path.join(tmp, "out")
         args = kv(L, mode="run", steps=steps, seed=seed, noise=0.02,
@@ -53,6 +61,9 @@ def run_case(name, L, steps, seed, status=None, keep=("phi", "u", "rho",
         ncomp = dict(phi=1, u=3, rho=1, force=3, f=19)
         for k in keep:
             res[k] = oracle.read_array(out, k, (ncomp[k],) + L)
+        for k in hashed:
+            res["sha256_" + k] = np.array(
+                sha256_of(oracle.read_array(out, k, (ncomp[k],) + L)))
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
     print("wrote", name)
 
@@ -277,6 +288,10 @@ def main(ref_root, only=None):
     if only == "io":
         io_cases()
         return
+    if only == "config1":
+        run_case("run_32cube_s1000", (32, 32, 32), 1000, 8361235,
+                 keep=("phi",), hashed=("f", "u", "rho", "force"))
+        return
     rng = np.random.default_rng(20261203)
 
     run_case("run_8x6x4_s10", (8, 6, 4), 10, 8361235)
@@ -285,7 +300,8 @@ def main(ref_root, only=None):
     st = (rng.uniform(size=(10, 8, 6)) < 0.1).astype(np.uint8)
     run_case("run_map_10x8x6_s12", (10, 8, 6), 12, 4242, status=st,
              keep=("phi", "u", "f"))
-    run_case("run_32cube_s1000", (32, 32, 32), 1000, 8361235, keep=("phi",))
+    run_case("run_32cube_s1000", (32, 32, 32), 1000, 8361235, keep=("phi",),
+             hashed=("f", "u", "rho", "force"))
 
     L = (6, 5, 4)
     f = oracle.lb_init_rest(L) * (1.0 + 1e-3 * rng.standard_normal((19,) + L))
@@ -321,4 +337,5 @@ def main(ref_root, only=None):
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a[7:] for a in sys.argv[1:] if a.startswith("--only=")]
-    main(args[0] if args else "/root/reference", only[0] if only else None)
+    main(args[0] if args else oracle.reference_root(),
+         only[0] if only else None)

@@ -1,7 +1,7 @@
 """Parity of the CUDA binary-fluid path with the CPU oracle (FP64: exact).
 
 The oracle is pinned bit for bit to the reference's own build
-(tests/test_oracle_pin.py, tests/golden/).  Every FP64 comparison here is
+(tests/test_oracle_golden.py against the fixtures of tests/golden/).  Every FP64 comparison here is
 exact equality of every value.
 """
 

@@ -91,3 +91,18 @@ def test_diverging_box_is_quarantined(gb):
         assert np.array_equal(a.box(k)["phi"], b.box(k)["phi"])
     n = sum(int(np.prod(params[k].ntotal)) for k in (0, 1, 3))
     assert a.sites() == n
+
+
+def test_config3_fp32_per_box_error_vs_fp64(gb):
+    """The 64-box uneven ensemble (edges from {32, 48, 64, 96} per axis,
+    viscosity, kappa and A = -B drawn per box) in FP32-shifted against the
+    same ensemble in FP64, box by box: max |dphi| and the relative mass
+    drift of every FP32 box, which must stay within the reduced-precision
+    bounds (mass drift at most 1e-10, the bound set for 10^4 steps)."""
+    from ludwig_gb300.precision import ensemble_error
+    res = ensemble_error(gb.ensemble_uneven_boxes(), 200)
+    assert res["nbox"] == 64
+    for r in res["boxes"]:
+        assert r["max_abs_dphi"] < 1e-4, r
+        assert r["mass_drift_rel"] < 1e-10, r
+        assert r["mass_drift_rel_fp64"] < 1e-12, r

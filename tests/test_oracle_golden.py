@@ -4,6 +4,7 @@ tests/golden/make_golden.py ran the reference (built from its own sources)
 on these inputs; the oracle must reproduce every value exactly.
 """
 
+import hashlib
 import os
 
 import numpy as np
@@ -44,6 +45,10 @@ def test_oracle_1000_steps_matches_reference(orc):
     orc.binary_steps(st, orc.symm_param(A, B, KAPPA), MOB,
                      orc.collide_param_m10(ETA), 1000)
     assert np.array_equal(st.phi, g["phi"])
+    # f, u, rho and force are pinned by the SHA-256 of the reference's arrays
+    for k in ("f", "u", "rho", "force"):
+        a = np.ascontiguousarray(getattr(st, k), "<f8")
+        assert hashlib.sha256(a.tobytes()).hexdigest() == str(g["sha256_" + k]), k
 
 
 def test_oracle_collide(orc):

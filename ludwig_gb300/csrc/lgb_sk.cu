@@ -9,11 +9,16 @@
  *  this is a diagnostic computed between steps, not part of the step.
  *
  *  Binning follows the reference: half space k_z in [0, N/2], 128 bins of
- *  width sqrt(3) pi / 128.  With faithful = 1 the reference's wavevector
- *  for i > N/2 is dk*i - pi (its util/length_from_sk.c:138, which
- *  subtracts pi rather than 2 pi); faithful = 0 uses dk*i - 2 pi.  The
- *  corner |k| = sqrt(3) pi falls in the last bin (the reference would
- *  index one past the end there).
+ *  width sqrt(3) pi / 128.  With faithful = 1 the bin of each wavevector
+ *  is the one the reference's program computes: its wavevector for i > N/2
+ *  is dk*i - pi (util/length_from_sk.c:138, which subtracts pi rather than
+ *  2 pi), and it forms the wavevectors and |k| in FP32 (a bin edge decided
+ *  in FP64 instead moves whole shells of a lamellar pattern to the next
+ *  bin).  faithful = 0 uses dk*i - 2 pi in FP64.  An index of 128 (only
+ *  possible at the corner |k| = sqrt(3) pi, where the reference would
+ *  write one past its arrays) falls in the last bin; at 128^3 the FP32
+ *  corner rounds into bin 127 in the reference too.  The sums are FP64
+ *  (the reference sums in FP32).
  *
  *****************************************************************************/
 
@@ -67,6 +72,40 @@ __global__ void k_to_complex(long long n, const T * __restrict__ a,
   if (i < n) c[i] = make_double2((double) a[i], 0.0);
 }
 
+/* Bin of the wavevector (ii, j, k) as util/length_from_sk.c:126-166
+ * computes it: the wavevectors, their squares, sums and |k| in FP32, one
+ * rounding per operation (the _rn intrinsics keep the compiler from
+ * contracting them into fused multiply-adds), kmax = float(pi), dk =
+ * float(2 kmax / nx) for every axis (the program assumes a cube), k -= kmax
+ * for indices above n/2, and the bin floor(|k| 128 / (sqrt(3) kmax)) in
+ * double. */
+__device__ int bin_reference(const lgbk_dims_t & d, int ii, int j, int k) {
+  const float kmax = 3.14159265358979323846f;
+  const float dk = __double2float_rn(__ddiv_rn(2.0*(double) kmax,
+					       (double) d.nx));
+  float kx = __fmul_rn(dk, (float) ii);
+  if (ii > d.nx/2) kx = __fsub_rn(kx, kmax);
+  float ky = __fmul_rn(dk, (float) j);
+  if (j > d.ny/2) ky = __fsub_rn(ky, kmax);
+  float kz = __fmul_rn(dk, (float) k);
+  float s = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)),
+		      __fmul_rn(kz, kz));
+  float kmod = __double2float_rn(__dsqrt_rn((double) s));
+  double r = __ddiv_rn(__dmul_rn((double) kmod, (double) LGBK_SK_NBIN),
+		       __dmul_rn(__dsqrt_rn(3.0), (double) kmax));
+  return (int) floor(r);
+}
+
+/* Bin with the wavevector 2 pi i / n - 2 pi for i > n/2, in FP64 */
+__device__ int bin_corrected(const lgbk_dims_t & d, int ii, int j, int k) {
+  const double pi = 3.14159265358979323846;
+  double kx = 2.0*pi*ii/d.nx; if (ii > d.nx/2) kx -= 2.0*pi;
+  double ky = 2.0*pi*j/d.ny;  if (j > d.ny/2) ky -= 2.0*pi;
+  double kz = 2.0*pi*k/d.nz;
+  double kmod = sqrt(kx*kx + ky*ky + kz*kz);
+  return (int) floor(kmod*LGBK_SK_NBIN/(sqrt(3.0)*pi));
+}
+
 __global__ void k_bin_sk(lgbk_dims_t d, int faithful,
 			 const double2 * __restrict__ c,
 			 double * __restrict__ sk, double * __restrict__ nk) {
@@ -78,13 +117,7 @@ __global__ void k_bin_sk(lgbk_dims_t d, int faithful,
   long long r = i / nzh;
   int j = (int) (r % d.ny);
   int ii = (int) (r / d.ny);
-  const double pi = 3.14159265358979323846;
-  const double shift = faithful ? pi : 2.0*pi;
-  double kx = 2.0*pi*ii/d.nx; if (ii > d.nx/2) kx -= shift;
-  double ky = 2.0*pi*j/d.ny;  if (j > d.ny/2) ky -= shift;
-  double kz = 2.0*pi*k/d.nz;
-  double kmod = sqrt(kx*kx + ky*ky + kz*kz);
-  int n = (int) floor(kmod*LGBK_SK_NBIN/(sqrt(3.0)*pi));
+  int n = faithful ? bin_reference(d, ii, j, k) : bin_corrected(d, ii, j, k);
   if (n >= LGBK_SK_NBIN) n = LGBK_SK_NBIN - 1;
   const double2 v = c[((long long) ii*d.ny + j)*d.nz + k];
   atomicAdd(sk + n, v.x*v.x + v.y*v.y);

@@ -496,26 +496,54 @@ def lc_steps(state, p, gamma_rot, cp, nsteps, status=None):
 NBIN = 128
 
 
+def _wavevectors_reference(n, nref):
+    """k_i of util/length_from_sk.c:126-139 in its own arithmetic: FP32,
+    kmax = float(4 atan 1), dk = float(2 kmax / nref) (nref = the x extent,
+    the program assumes a cube), kx = dk*i, and kx -= kmax for i > n/2."""
+    f32 = np.float32
+    kmax = f32(4.0 * np.arctan(1.0))
+    dk = f32(2.0 * np.float64(kmax) / nref)
+    i = np.arange(n)
+    k = (dk * i.astype(f32)).astype(f32)
+    return np.where(i > n // 2, (k - kmax).astype(f32), k).astype(f32), kmax
+
+
 def structure_factor(phi, faithful=True):
     """Binned |phi(k)|^2 sums and counts over the half space k_z >= 0.
 
-    faithful=True keeps the reference's wavevector for i > N/2, dk*i - pi
-    (util/length_from_sk.c:138); faithful=False uses dk*i - 2 pi.
+    faithful=True is the reference's program (util/length_from_sk.c:111-
+    166): its wavevector for i > N/2 is dk*i - pi (:138), and the
+    wavevectors and |k| are FP32, |k| = float(sqrt(double(kx kx + ky ky +
+    kz kz))) with the products and sums rounded to FP32 one by one; the
+    bin is floor(|k| 128 / (sqrt(3) kmax)) in double.  The transform and the
+    sums here are FP64 (the reference sums in FP32).
+    faithful=False uses dk*i - 2 pi and FP64 throughout.
     """
     phi = np.asarray(phi, dtype=np.float64)
     if phi.ndim == 4:
         phi = phi[0]
     nx, ny, nz = phi.shape
     c = np.fft.fftn(phi)
-    shift = np.pi if faithful else 2.0 * np.pi
-    kx = 2.0 * np.pi * np.arange(nx) / nx
-    kx = np.where(np.arange(nx) > nx // 2, kx - shift, kx)
-    ky = 2.0 * np.pi * np.arange(ny) / ny
-    ky = np.where(np.arange(ny) > ny // 2, ky - shift, ky)
-    kz = 2.0 * np.pi * np.arange(nz // 2 + 1) / nz
-    KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
-    kmod = np.sqrt(KX * KX + KY * KY + KZ * KZ)
-    n = np.floor(kmod * NBIN / (np.sqrt(3.0) * np.pi)).astype(int)
+    if faithful:
+        f32 = np.float32
+        kx, kmax = _wavevectors_reference(nx, nx)
+        ky, _ = _wavevectors_reference(ny, nx)
+        kz = _wavevectors_reference(nz, nx)[0][:nz // 2 + 1]
+        KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
+        s2 = ((KX * KX).astype(f32) + (KY * KY).astype(f32)).astype(f32)
+        s2 = (s2 + (KZ * KZ).astype(f32)).astype(f32)
+        kmod = np.sqrt(s2.astype(np.float64)).astype(f32)
+        n = np.floor(kmod.astype(np.float64) * NBIN
+                     / (np.sqrt(3.0) * np.float64(kmax))).astype(int)
+    else:
+        kx = 2.0 * np.pi * np.arange(nx) / nx
+        kx = np.where(np.arange(nx) > nx // 2, kx - 2.0 * np.pi, kx)
+        ky = 2.0 * np.pi * np.arange(ny) / ny
+        ky = np.where(np.arange(ny) > ny // 2, ky - 2.0 * np.pi, ky)
+        kz = 2.0 * np.pi * np.arange(nz // 2 + 1) / nz
+        KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
+        kmod = np.sqrt(KX * KX + KY * KY + KZ * KZ)
+        n = np.floor(kmod * NBIN / (np.sqrt(3.0) * np.pi)).astype(int)
     n = np.minimum(n, NBIN - 1)
     s = np.abs(c[:, :, :nz // 2 + 1]) ** 2
     sk = np.bincount(n.ravel(), weights=s.ravel(), minlength=NBIN)

@@ -19,7 +19,10 @@ OBJS    := $(patsubst %.c,$(OUT)/obj/%.o,$(notdir $(SRCS)))
 
 vpath %.c $(REF)/src $(REF)/target $(REF)/mpi_s
 
-all: $(OUT)/libludwig_ref.a $(OUT)/Ludwig.exe $(OUT)/ref_shim
+HERE    := $(dir $(lastword $(MAKEFILE_LIST)))
+
+all: $(OUT)/libludwig_ref.a $(OUT)/Ludwig.exe $(OUT)/ref_shim \
+     $(OUT)/length_from_sk
 
 $(OUT)/obj/%.o: %.c
 	@mkdir -p $(OUT)/obj
@@ -31,7 +34,16 @@ $(OUT)/libludwig_ref.a: $(OBJS)
 $(OUT)/Ludwig.exe: $(REF)/src/main.c $(OUT)/libludwig_ref.a
 	$(CC) $(CFLAGS) $< $(OUT)/libludwig_ref.a -lm -o $@
 
-$(OUT)/ref_shim: $(dir $(lastword $(MAKEFILE_LIST)))ref_shim.c $(OUT)/libludwig_ref.a
+$(OUT)/ref_shim: $(HERE)ref_shim.c $(OUT)/libludwig_ref.a
 	$(CC) $(CFLAGS) $< $(OUT)/libludwig_ref.a -lm -o $@
+
+# The reference's L(t) utility, unmodified (it reads a 128^3 binary phi
+# file), against the FFTW3 interface of oracle/fftw_api (FFTW3 itself is
+# not installed; the five calls it makes are implemented there).
+$(OUT)/length_from_sk: $(REF)/util/length_from_sk.c $(HERE)fftw_api/fftw_dft.c \
+                       $(HERE)fftw_api/fftw3.h
+	@mkdir -p $(OUT)
+	$(CC) -O2 -fopenmp -ffp-contract=off -w -I$(HERE)fftw_api \
+	  $(REF)/util/length_from_sk.c $(HERE)fftw_api/fftw_dft.c -lm -o $@
 
 .PHONY: all

@@ -8,11 +8,12 @@ src/ludwig.c) on seeded inputs.  Inputs and outputs are saved as .npz.
 
 Needs the reference sources (only where they are present):
     python tests/golden/make_golden.py [/path/to/reference]
-(default: $LUDWIG_REFERENCE_ROOT, else REF of oracle/ref.mk) [--only=lb2|grad27|logs|advection|io|config1]
+(default: $LUDWIG_REFERENCE_ROOT, else REF of oracle/ref.mk) [--only=lb2|grad27|logs|advection|io|config1|length]
 """
 
 import hashlib
 import os
+import subprocess
 import sys
 import tempfile
 
@@ -270,6 +271,54 @@ def io_cases():
         print("wrote", name, n, "sites", names)
 
 
+def length_fields(L=(128, 128, 128)):
+    """Order-parameter fields for the L(t) fixtures that need no
+    transcendental function (so that any machine builds the same doubles):
+    a sphere of radius 24 (phi = 1 inside, -1 outside, by integer squared
+    distance) and lamellae of period 16 along x."""
+    x, y, z = np.meshgrid(*(np.arange(n) for n in L), indexing="ij")
+    c = [n // 2 for n in L]
+    r2 = (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2
+    sphere = np.where(r2 < 24 * 24, 1.0, -1.0)
+    lamellae = np.where((x // 8) % 2 == 0, 1.0, -1.0)
+    return {"sphere_r24": sphere[None], "lamellae_p16": lamellae[None]}
+
+
+def length_cases():
+    """The reference's util/length_from_sk.c (unmodified, compiled against
+    oracle/fftw_api by oracle/ref.mk; it reads 128^3 binary phi files) on
+    four 128^3 fields: the spinodal start (seed 8361235), the reference's
+    own binary-fluid run from it after 600 steps (config 1's parameters),
+    a sphere and lamellae.  Saved: the printed L (as printed, "%g") and the
+    SHA-256 of each field's doubles; the fields are rebuilt by the test."""
+    L = (128, 128, 128)
+    exe = os.path.join(ROOT, "oracle", "_ref", "length_from_sk")
+    res = {"L": np.array(L)}
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "out")
+        oracle.run_reference(kv(L, mode="run", steps=600, seed=8361235,
+                                noise=0.02, phi0=0.0, out=out, dump0=1,
+                                **SYMM), threads=os.cpu_count())
+        fields = {"spinodal_s0": oracle.read_array(out + "0", "phi", (1,) + L),
+                  "spinodal_s600": oracle.read_array(out, "phi", (1,) + L)}
+        fields.update(length_fields(L))
+        names = []
+        for name, phi in fields.items():
+            path = os.path.join(tmp, name)
+            np.ascontiguousarray(phi, "<f8").tofile(path)
+            txt = subprocess.run([exe, path], capture_output=True, text=True,
+                                 check=True).stdout.strip()
+            # "L = <file> <value>"
+            res["L_" + name] = np.array(float(txt.split()[-1]))
+            res["printed_" + name] = np.array(txt.split()[-1])
+            res["sha256_" + name] = np.array(sha256_of(phi))
+            names.append(name)
+            print(name, txt.split()[-1])
+        res["names"] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, "length_from_sk_128cube.npz"), **res)
+    print("wrote length_from_sk_128cube")
+
+
 def main(ref_root, only=None):
     if not oracle.build_reference(ref_root):
         raise SystemExit("reference sources not found at " + ref_root)
@@ -287,6 +336,9 @@ def main(ref_root, only=None):
         return
     if only == "io":
         io_cases()
+        return
+    if only == "length":
+        length_cases()
         return
     if only == "config1":
         run_case("run_32cube_s1000", (32, 32, 32), 1000, 8361235,
@@ -331,6 +383,7 @@ def main(ref_root, only=None):
     grad27_cases()
     advection_cases()
     io_cases()
+    length_cases()
     regression_logs(ref_root)
 
 

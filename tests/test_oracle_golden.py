@@ -209,3 +209,30 @@ def test_oracle_snapshot_files_match_reference(orc, name):
     assert sorted(got) == names
     for k, fn in enumerate(names):
         assert got[fn] == g["file%d" % k].tobytes(), fn
+
+
+def _length_fields():
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden import length_fields
+    return length_fields((128, 128, 128))
+
+
+def test_oracle_length_matches_reference_program(orc):
+    """util/length_from_sk.c itself (compiled against oracle/fftw_api) on
+    128^3 fields: the oracle's faithful L agrees with the printed value to
+    its 6 significant digits (the program sums in FP32, the oracle in
+    FP64: 1e-5 relative covers both)."""
+    g = load("length_from_sk_128cube")
+    fields = _length_fields()
+    fields["spinodal_s0"] = orc.spinodal_init((128, 128, 128), 8361235,
+                                              0.0, 0.02)
+    for name, phi in fields.items():
+        a = np.ascontiguousarray(phi, "<f8")
+        assert hashlib.sha256(a.tobytes()).hexdigest() == str(
+            g["sha256_" + name]), name
+        ref = float(g["L_" + name])
+        got = orc.length_from_sk(phi, True)
+        assert abs(got - ref) <= 1e-5 * ref, (name, got, ref)
+        assert "%g" % got == str(g["printed_" + name]) or abs(
+            got - ref) <= 5e-6 * ref, (name, got, ref)

@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIZE = (256, 256, 256)
-LEGS = ("fp32", "e2e", "fp16", "fp64", "lc", "ens", "cnn", "cpu")
+LEGS = ("fp32", "e2e", "fp16", "fp64", "dropin", "lc", "ens", "cnn", "cpu")
 PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
 SEED = 8361235
 METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
@@ -48,15 +48,41 @@ ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108,
               # cholesteric LC: f 2*19 + Q 2*5 + u 2*3 values per site
               "lc64": 432, "lc32": 216}
 
-# DRAM bytes (read + write) per site of the fused kernels from one ncu
-# capture at 160^3 (profiles/k_binary_fused_fp32_160cube.md,
-# profiles/k_binary_fused_fp64_160cube.md and
-# profiles/k_binary_fused_fp16_160cube.md); a streaming kernel's traffic
-# grows in proportion to the sites, so traffic = bytes/site x sites.
-NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4}
+# Algorithmic bytes per site of one step through the per-function C API in
+# the main-loop order (each kernel reads its input arrays once and writes
+# its outputs once; intermediates stored as the reference stores them):
+# binary fluid FP64: hydro_f_zero 24, gradient 40 (phi -> grad, delsq),
+# stress 112 (phi, grad, delsq -> P), force divergence 120 (P, force r/w),
+# upwind fluxes 64 (phi, u -> 4 fluxes), chemical-potential fluxes 80
+# (phi, delsq, 4 fluxes r/w), phi update 48 (4 fluxes, phi r/w),
+# hydro_u_zero 24, collision pulling the pending propagation 360 (f, force
+# -> f, rho, u) = 872.  Cholesteric FP64: 24 + gradients 200 (Q -> 15
+# gradients, 5 Laplacians) + stress 272 + force 120 + upwind fluxes 224
+# (Q, u -> 20 fluxes) + molecular field 240 (Q, gradients -> H) +
+# Beris-Edwards 304 (u, 20 fluxes, H, Q r/w) + 24 + 360 = 1768.
+DROPIN_BYTES = {"dropin_binary64": 872, "dropin_lc64": 1768}
+
+# DRAM bytes (read + write) per site of the fused kernels, from one ncu
+# capture each (binary fluid at 160^3, cholesteric at 128^3; the fused
+# float LC step is two kernels, 32.5 + 34.0 + 114.8 + 72.5); a streaming
+# kernel's traffic grows in proportion to the sites, so traffic =
+# bytes/site x sites.
+NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4,
+                      "lc32": 253.8}
+
+# Corrector FLOPs per coarse site and forward pass (3x3x3 convolutions):
+# executed as 4 layers of 32 x 32 channels, 2*27*32*32 each; useful are
+# the real layer shapes 5 -> 32 -> 32 -> 32 -> 4: 2*27*(5*32 + 2*32*32 +
+# 32*4) = 126,144.
+CNN_EXEC_FLOP = 4 * 2 * 27 * 32 * 32
+CNN_USEFUL_FLOP = 2 * 27 * (5 * 32 + 2 * 32 * 32 + 32 * 4)
 
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
 LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",
+           "dropin_binary64": "one kernel per reference function, FP64 "
+                              "(--fmad=false); intermediates through HBM",
+           "dropin_lc64": "one kernel per reference function, FP64; "
+                          "intermediates through HBM",
            "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
            "fp16": "issue (same instructions as fp32 plus conversions; "
                    "108 B/site)",
@@ -250,7 +276,7 @@ def make_system(lg, prec):
 
 
 def roofline(kind, ms_per_step, nsites, peak, peak_kind):
-    algo = ALGO_BYTES[kind] * nsites
+    algo = (ALGO_BYTES.get(kind) or DROPIN_BYTES[kind]) * nsites
     achieved = algo / (ms_per_step * 1e-3) / 1e9
     ncu = NCU_BYTES_PER_SITE.get(kind)
     if kind not in LIMITER:
@@ -334,6 +360,53 @@ def gpu_arm(args):
         ms64 = max_over_ranks(pg, ms64)
         s64 = None
 
+    # --- the drop-in path: one C-API call per reference function ---------
+    dropin = None
+    if "dropin" in legs:
+        dropin = {}
+        sb = make_system(lg, lg.FP64)
+        sb.step_reference_order(2)
+        lg.sync()
+        kd = 10
+        t0 = time.perf_counter()
+        sb.step_reference_order(kd)
+        lg.sync()
+        dt = time.perf_counter() - t0
+        dropin["binary_fp64"] = {
+            "value": nsites * kd / dt / 1e6, "unit": "MLUPS", "steps": kd,
+            "ms_per_step": 1e3 * dt / kd,
+            "roofline": roofline("dropin_binary64", 1e3 * dt / kd, nsites, peak,
+                                 peak_kind),
+            "workload": "256^3 binary fluid FP64, per step: hydro_f_zero, "
+                        "field_halo, field_grad_compute, "
+                        "phi_force_calculation, hydro_u_halo, "
+                        "phi_cahn_hilliard, hydro_u_zero, lb_collide, "
+                        "lb_halo, lb_propagation (each call synchronous), "
+                        "host wall time"}
+        sb = None
+        n_lc = (128, 128, 128)
+        slc = lg.LiquidCrystal(n_lc, eta=0.5, gamma_rot=0.5,
+                               precision=lg.FP64)
+        slc.init_o8m()
+        slc.step_reference_order(2)
+        lg.sync()
+        t0 = time.perf_counter()
+        slc.step_reference_order(kd)
+        lg.sync()
+        dt = time.perf_counter() - t0
+        sites_lc = 128 ** 3
+        dropin["lc_fp64"] = {
+            "value": sites_lc * kd / dt / 1e6, "unit": "MLUPS", "steps": kd,
+            "ms_per_step": 1e3 * dt / kd,
+            "roofline": roofline("dropin_lc64", 1e3 * dt / kd, sites_lc, peak,
+                                 peak_kind),
+            "workload": "128^3 cholesteric BP I FP64, per step: "
+                        "hydro_f_zero, field_halo, field_grad_compute, "
+                        "phi_force_calculation, hydro_u_halo, "
+                        "beris_edw_update, hydro_u_zero, lb_collide, "
+                        "lb_halo, lb_propagation, host wall time"}
+        slc = None
+
     # --- cholesteric LC (blue phase I), 128^3, FP32 and FP64 ------------
     lc = None
     if "lc" in legs:
@@ -383,6 +456,19 @@ def gpu_arm(args):
                            "per step under a CUDA graph; boxes shared out "
                            "over the ranks by size"}
         e.close()
+        # config 3's per-box error: every FP32 box against the same box
+        # run in FP64, after the same number of steps
+        from ludwig_gb300.precision import ensemble_error
+        ksteps = 200
+        err = ensemble_error([boxes[i] for i in mine], ksteps)
+        ens["per_box_error"] = {
+            "steps": ksteps, "boxes": err["nbox"],
+            "max_dphi_max": err["max_dphi_max"],
+            "drift_max": err["drift_max"],
+            "drift_max_fp64": err["drift_max_fp64"],
+            "how": "FP32-shifted ensemble vs FP64 ensemble of the same "
+                   "boxes: max over boxes of max|dphi| and of the relative "
+                   "mass drift since step 0"}
 
     # --- learned corrector on the 128^3 coarse lattice --------------------
     cnn = None
@@ -390,12 +476,20 @@ def gpu_arm(args):
         try:
             from ludwig_gb300.corrector import bench as cnn_bench
             r = cnn_bench(128, reps=max(3, min(args.steps // 20, 20)))
-            cnn = {"forward_ms": r["line_planes"]["forward_ms"],
+            fwd = r["line_planes"]["forward_ms"]
+            ncs = 128 ** 3
+            cnn = {"forward_ms": fwd,
                    "train_step_ms": r["line_planes"]["train_step_ms"],
                    "forward_tflops": r["line_planes"]["forward_tflops"],
+                   "forward_tflops_useful":
+                       CNN_USEFUL_FLOP * ncs / (fwd * 1e-3) / 1e12,
+                   "useful_over_executed": CNN_USEFUL_FLOP / CNN_EXEC_FLOP,
                    "train_step_tflops": r["line_planes"]["train_step_tflops"],
                    "per_tap_forward_ms": r["per_tap"]["forward_ms"],
-                   "unit_note": "executed BF16 MMA work / wall time per call",
+                   "unit_note": "forward_tflops: executed BF16 MMA work "
+                                "(4 layers of 32x32 channels) / wall time "
+                                "per call; forward_tflops_useful: the real "
+                                "layer shapes 5-32-32-32-4",
                    "workload": "4-layer 3x3x3 conv net, 32 channels, 128^3 "
                                "coarse lattice, tcgen05 BF16 / FP32"}
         except ImportError as exc:                   # torch missing
@@ -408,6 +502,18 @@ def gpu_arm(args):
     fp16_mlups = nsites * args.steps / (ms16 * 1e-3) / 1e6 * world
     e2e = total_sites * e2e_steps / (ms_e2e * 1e-3) / 1e6
     e2e_serial = nsites * e2e_steps / (ms_e2e_serial * 1e-3) / 1e6
+
+    if cnn is not None and "forward_ms" in cnn and ms32 == ms32:
+        # one coarse step (128^3, a quarter of the fine step's sites x 1/2
+        # per axis) plus one forward pass stands for 4 fine steps at 256^3
+        per32_fine = ms32 / args.steps
+        coarse_ms = per32_fine / 8.0
+        cnn["cost_ratio_vs_4_fine_steps"] = (
+            (coarse_ms + cnn["forward_ms"]) / (4.0 * per32_fine))
+        cnn["cost_note"] = ("(coarse FP32 step, estimated as 1/8 of the "
+                            "fine step, + forward) / (4 fine FP32 steps "
+                            "at 256^3); < 1 means the corrected coarse run "
+                            "is cheaper")
 
     if rank != 0:
         return 0
@@ -456,12 +562,17 @@ def gpu_arm(args):
         "clocks": clk,
         "fp64": {"value": fp64_mlups, "unit": "MLUPS", "steps": k64,
                  "ms_per_step": ms64 / k64,
+                 "vs_cpu_baseline": (fp64_mlups / cpu["value"]
+                                     if cpu and cpu.get("value") else None),
+                 "vs_cpu_note": "FP64 on both sides: the bit-exact GPU step "
+                                "over cpu_baseline (the oracle, FP64)",
                  "roofline": roofline("fp64", ms64 / k64, nsites, peak,
                                       peak_kind)},
         "fp16": {"value": fp16_mlups, "unit": "MLUPS",
                  "ms_per_step": ms16 / args.steps,
                  "roofline": roofline("fp16", ms16 / args.steps, nsites, peak,
                                       peak_kind)},
+        "dropin": dropin,
         "lc": lc,
         "ensemble": ens,
         "corrector": cnn,

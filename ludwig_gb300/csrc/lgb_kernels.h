@@ -87,6 +87,12 @@ int lgbk_ch_update_f64(const lgbk_dims_t * d, const double * fw,
 int lgbk_collide_f64(const lgbk_dims_t * d, const lgbk_collide_t * cp,
 		     const uint8_t * status, double * f, const double * force,
 		     double * rho, double * u, void * stream);
+/* the same after a pending propagation: populations pulled from fpost
+ * (post-collision values), results to fout (a second array) */
+int lgbk_collide_pull_f64(const lgbk_dims_t * d, const lgbk_collide_t * cp,
+			  const uint8_t * status, const double * fpost,
+			  double * fout, const double * force, double * rho,
+			  double * u, void * stream);
 /* dir = +1: fprime_p(x) = f_p(x - c_p) (propagation); dir = -1: inverse */
 int lgbk_propagate_f64(const lgbk_dims_t * d, int dir, const double * f,
 		       double * fprime, void * stream);

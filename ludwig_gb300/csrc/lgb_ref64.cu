@@ -229,28 +229,51 @@ __global__ void k_ch_update(lgbk_dims_t d, const double * __restrict__ fw,
 	     + wz*fz[i] - wz*fz[lgb_site_w(d, x, y, z-1)]);
 }
 
-/* src/collision.c:221-593 (lb_collision_mrt1 / _site) */
+/* src/collision.c:221-593 (lb_collision_mrt1 / _site).  With PULL the
+ * input holds post-collision values whose streaming is still pending: each
+ * population is pulled from its upstream site (the permutation of
+ * src/propagation.c:153-197) and the result goes to a second array, so
+ * that lb_propagation followed by lb_collide reads and writes f once.
+ * Solid sites keep their (streamed) populations. */
 
-template <bool GZERO>
+template <bool GZERO, bool PULL>
 __global__ void k_collide(lgbk_dims_t d, lgbk_collide_t cp,
 			  const uint8_t * __restrict__ st,
-			  double * __restrict__ f,
+			  const double * fin, double * fout,
 			  const double * __restrict__ force,
 			  double * __restrict__ rho, double * __restrict__ u) {
   long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
   if (i >= d.nsites) return;
   const long long N = d.nsites;
   double fs[LGB_NVEL], fa[3], uu[3], r;
-  #pragma unroll
-  for (int p = 0; p < LGB_NVEL; p++) fs[p] = f[p*N + i];
+  if (PULL) {
+    int x, y, z;
+    site_xyz(d, i, x, y, z);
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) {
+      long long j = lgb_site_w(d, x - lgb_cv_c[p][0], y - lgb_cv_c[p][1],
+			       z - lgb_cv_c[p][2]);
+      fs[p] = fin[p*N + j];
+    }
+  }
+  else {
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) fs[p] = fin[p*N + i];
+  }
   #pragma unroll
   for (int ia = 0; ia < 3; ia++) {
     fa[ia] = cp.force_global[ia] + (force ? force[ia*N + i] : 0.0);
   }
-  lgb_collide_site<double, true, false, GZERO>(cp, 0.0, fs, fa, r, uu);
-  if (st == NULL || st[i] == 0) {
+  const bool fluid = (st == NULL || st[i] == 0);
+  if (PULL && !fluid) {
     #pragma unroll
-    for (int p = 0; p < LGB_NVEL; p++) f[p*N + i] = fs[p];
+    for (int p = 0; p < LGB_NVEL; p++) fout[p*N + i] = fs[p];
+    return;
+  }
+  lgb_collide_site<double, true, false, GZERO>(cp, 0.0, fs, fa, r, uu);
+  if (fluid) {
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) fout[p*N + i] = fs[p];
     rho[i] = r;
     #pragma unroll
     for (int ia = 0; ia < 3; ia++) u[ia*N + i] = uu[ia];
@@ -540,12 +563,27 @@ int lgbk_collide_f64(const lgbk_dims_t * d, const lgbk_collide_t * cp,
 		     const uint8_t * status, double * f, const double * force,
 		     double * rho, double * u, void * stream) {
   if (cp->ghosts_zero) {
-    k_collide<true><<<grid_for(d->nsites), LGB_TPB, 0,
-      (cudaStream_t) stream>>>(*d, *cp, status, f, force, rho, u);
+    k_collide<true, false><<<grid_for(d->nsites), LGB_TPB, 0,
+      (cudaStream_t) stream>>>(*d, *cp, status, f, f, force, rho, u);
   }
   else {
-    k_collide<false><<<grid_for(d->nsites), LGB_TPB, 0,
-      (cudaStream_t) stream>>>(*d, *cp, status, f, force, rho, u);
+    k_collide<false, false><<<grid_for(d->nsites), LGB_TPB, 0,
+      (cudaStream_t) stream>>>(*d, *cp, status, f, f, force, rho, u);
+  }
+  LAUNCH_RET;
+}
+
+int lgbk_collide_pull_f64(const lgbk_dims_t * d, const lgbk_collide_t * cp,
+			  const uint8_t * status, const double * fpost,
+			  double * fout, const double * force, double * rho,
+			  double * u, void * stream) {
+  if (cp->ghosts_zero) {
+    k_collide<true, true><<<grid_for(d->nsites), LGB_TPB, 0,
+      (cudaStream_t) stream>>>(*d, *cp, status, fpost, fout, force, rho, u);
+  }
+  else {
+    k_collide<false, true><<<grid_for(d->nsites), LGB_TPB, 0,
+      (cudaStream_t) stream>>>(*d, *cp, status, fpost, fout, force, rho, u);
   }
   LAUNCH_RET;
 }

@@ -2119,10 +2119,21 @@ int lb_collide(lb_t * lb, hydro_t * hydro, map_t * map, noise_t * noise,
   int rc = collide_param(lb, &cp);
   if (rc) return rc;
   if (lb->ndist == 2) return lb_collide_binary(lb, hydro, map, fe, &cp);
-  if ((rc = lb_materialise(lb))) return rc;
-  CK(lgbk_collide_f64(&lb->cs->d, &cp, map_dev(map), (double *) lb->f,
-		      (const double *) hydro->force, (double *) hydro->rho,
-		      (double *) hydro->u, stream_), "collide");
+  if (lb->pending) {
+    /* streaming still pending: pull and collide in one pass, into f' */
+    CK(lgbk_collide_pull_f64(&lb->cs->d, &cp, map_dev(map),
+			     (const double *) lb->f, (double *) lb->fprime,
+			     (const double *) hydro->force,
+			     (double *) hydro->rho, (double *) hydro->u,
+			     stream_), "collide");
+    lb_swap(lb);
+    lb->pending = 0;
+  }
+  else {
+    CK(lgbk_collide_f64(&lb->cs->d, &cp, map_dev(map), (double *) lb->f,
+			(const double *) hydro->force, (double *) hydro->rho,
+			(double *) hydro->u, stream_), "collide");
+  }
   CK(cudaStreamSynchronize(stream_), "sync");
   return LUDWIG_GB_OK;
 }

@@ -7,11 +7,25 @@
  *
  *  The hot-path entry points keep the names, argument lists and meaning of
  *  the reference functions they replace (cited per declaration as
- *  path:line within the reference tree).  Objects are opaque handles that
- *  own device memory; data stay resident on the device between calls.
- *  Host arrays passed to the *_to_host / *_from_host functions use one
- *  layout: interior sites only, component-major, z fastest,
- *      a[((n*Lx + x)*Ly + y)*Lz + z],   x, y, z = 0 .. L-1.
+ *  path:line within the reference tree), and the structures a caller fills
+ *  or reads (option structures, parameter structures, the free-energy
+ *  object fe_t and its function table fe_vt_t) have the reference's
+ *  members in the reference's order, so that code compiled against the
+ *  reference's headers and code compiled against this one agree on every
+ *  offset.  Objects are opaque handles that own device memory; data stay
+ *  resident on the device between calls.
+ *
+ *  Site indices passed to the free-energy function table and to the
+ *  per-site field accessors are the reference's cs_index() numbering
+ *  (src/coords.c:617): halo sites included, index = xs*(nhalo + ic - 1) +
+ *  ys*(nhalo + jc - 1) + (nhalo + kc - 1) with ic = 1 .. Lx (halo sites
+ *  1 - nhalo .. Lx + nhalo) and strides zs = 1, ys = Lz + 2 nhalo,
+ *  xs = (Ly + 2 nhalo) ys; a halo site is the periodic image of the
+ *  interior site it copies.  Host arrays of the *_to_host / *_from_host
+ *  functions hold the interior sites only, component-major, z fastest,
+ *      a[((n*Lx + x)*Ly + y)*Lz + z],   x, y, z = 0 .. L-1;
+ *  the ludwig_gb_*_to_host_cs functions write the reference's own host
+ *  layout (all cs_index sites, in its AOS or SOA data model).
  *  Every function returns 0 on success or a LUDWIG_GB_E* code, with a
  *  message from ludwig_gb_last_error().  Nothing traps on the device.
  *  Calls are synchronous: results are complete when a call returns.
@@ -90,6 +104,15 @@ int cs_ntotal_set(cs_t * cs, const int ntotal[3]);
 int cs_nhalo_set(cs_t * cs, int nhalo);
 int cs_init(cs_t * cs);
 int cs_nlocal(cs_t * cs, int nlocal[3]);
+/* src/coords.h:98-107: the site numbering of the free-energy slots and of
+ * the ludwig_gb_*_cs functions */
+int cs_ntotal(cs_t * cs, int ntotal[3]);
+int cs_nhalo(cs_t * cs, int * nhalo);
+int cs_nsites(cs_t * cs, int * nsites);
+int cs_strides(cs_t * cs, int * xs, int * ys, int * zs);
+int cs_nall(cs_t * cs, int nall[3]);
+int cs_index(cs_t * cs, int ic, int jc, int kc);
+int cs_index_to_ijk(cs_t * cs, int index, int coords[3]);
 
 /*---------------------------------------------------------------------------
  * Physical parameters: src/physics.h:20-37.  As in the reference, the most
@@ -108,21 +131,71 @@ int physics_ref(physics_t ** ref);
 /*---------------------------------------------------------------------------
  * Distributions: src/lb_data.h:30-47,162-171 (D3Q19, ndist = 1)
  *-------------------------------------------------------------------------*/
-typedef enum {LB_RELAXATION_M10, LB_RELAXATION_BGK, LB_RELAXATION_TRT}
-  lb_relaxation_enum_t;
+/* I/O options carried by the option structures, src/io_options.h:25-62
+ * and src/io_info_args.h:33-38 (the snapshot functions below read
+ * iorformat; the rest is accepted and recorded) */
+enum io_mode_enum {IO_MODE_INVALID, IO_MODE_MPIIO};
+enum io_record_format_enum {IO_RECORD_INVALID, IO_RECORD_ASCII,
+			    IO_RECORD_BINARY};
+enum io_metadata_version_enum {IO_METADATA_INVALID, IO_METADATA_SINGLE_V1,
+			       IO_METADATA_MULTI_V1, IO_METADATA_V2};
+typedef enum io_mode_enum             io_mode_enum_t;
+typedef enum io_record_format_enum    io_record_format_enum_t;
+typedef enum io_metadata_version_enum io_metadata_version_enum_t;
+
+typedef struct io_options_s {
+  io_mode_enum_t             mode;
+  io_record_format_enum_t    iorformat;
+  io_metadata_version_enum_t metadata_version;
+  int                        report;
+  int                        asynchronous;
+  int                        compression_levl;
+  int                        iogrid[3];
+} io_options_t;
+
+typedef struct io_info_args_s {
+  io_options_t input;
+  io_options_t output;
+  int grid[3];
+  int iofreq;
+} io_info_args_t;
+
+/* src/io_options.c, src/io_info_args.c: MPIIO, binary, single-file V1,
+ * grid 1 1 1 */
+io_options_t io_options_default(void);
+io_info_args_t io_info_args_default(void);
+
+/*---------------------------------------------------------------------------
+ * Distributions: src/lb_data.h:162-171, src/lb_data_options.h:20-47
+ * (D3Q19, ndist = 1 or 2)
+ *-------------------------------------------------------------------------*/
+typedef enum lb_relaxation_enum {LB_RELAXATION_M10, LB_RELAXATION_BGK,
+				 LB_RELAXATION_TRT} lb_relaxation_enum_t;
+typedef enum lb_halo_enum {LB_HALO_FULL = 1, LB_HALO_REDUCED = 2}
+  lb_halo_enum_t;
 
 typedef struct lb_data_options_s {
   int ndim;                      /* 3 */
   int nvel;                      /* 19 */
-  int ndist;                     /* 1 */
+  int ndist;                     /* 1, or 2 (symmetric_lb) */
   lb_relaxation_enum_t nrelax;   /* default M10 */
-  int precision;                 /* ludwig_gb_prec_t; default FP64 */
-  double fp16_scale;             /* FP16 storage scale; 0 = default 1024 */
+  lb_halo_enum_t halo;           /* recorded (the halo is implicit) */
+  int reportimbalance;           /* recorded */
+  int usefirsttouch;             /* recorded */
+  io_info_args_t iodata;         /* record formats of the snapshot files */
 } lb_data_options_t;
 
 lb_data_options_t lb_data_options_default(void);
+lb_data_options_t lb_data_options_ndim_nvel_ndist(int ndim, int nvel,
+						  int ndist);
+/* Objects created by the reference-named functions are FP64 (the
+ * drop-in).  The reduced-precision forms are created here; fp16_scale is
+ * the FP16 storage scale of f - w_p rho0 (0: the default). */
 int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
 		   lb_t ** lb);
+int ludwig_gb_lb_data_create(pe_t * pe, cs_t * cs,
+			     const lb_data_options_t * opts, int precision,
+			     double fp16_scale, lb_t ** lb);
 int lb_free(lb_t * lb);
 int lb_init_rest_f(lb_t * lb, double rho0);                /* lb_data.c:659 */
 int lb_halo(lb_t * lb);                                     /* lb_data.c:754 */
@@ -149,20 +222,41 @@ int lb_propagation(lb_t * lb);
 /*---------------------------------------------------------------------------
  * Fields: src/field.h:97-119, src/field_options.h
  *-------------------------------------------------------------------------*/
+typedef enum field_halo_enum {FIELD_HALO_HOST, FIELD_HALO_TARGET,
+			      FIELD_HALO_OPENMP} field_halo_enum_t;
+
 typedef struct field_options_s {
   int ndata;                     /* components: 1 (phi) or 5 (Q) */
   int nhcomm;                    /* halo width requested (recorded) */
-  int precision;                 /* ludwig_gb_prec_t */
+  field_halo_enum_t haloscheme;  /* recorded */
+  int haloverbose;               /* recorded */
+  int usefirsttouch;             /* recorded */
+  io_info_args_t iodata;         /* record formats of the snapshot files */
 } field_options_t;
 
+field_options_t field_options_default(void);
 field_options_t field_options_ndata_nhalo(int ndata, int nhalo);
 int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
 		 const field_options_t * opts, field_t ** pobj);
+/* field_create with an arithmetic and storage precision (FP64 or FP32) */
+int ludwig_gb_field_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			   const char * name, const field_options_t * opts,
+			   int precision, field_t ** pobj);
 int field_free(field_t * obj);
 int field_nf(field_t * obj, int * nf);
 int field_halo(field_t * obj);                              /* field.c:371 */
 int field_to_host(field_t * obj, double * data);
 int field_from_host(field_t * obj, const double * data);
+/* Per-site values at a cs_index() site, src/field.h:109-120 (one small
+ * device copy per call: for host code that visits a few sites) */
+int field_scalar(field_t * obj, int index, double * phi);
+int field_scalar_set(field_t * obj, int index, double phi);
+int field_vector(field_t * obj, int index, double p[3]);
+int field_vector_set(field_t * obj, int index, const double p[3]);
+int field_tensor(field_t * obj, int index, double q[3][3]);
+int field_tensor_set(field_t * obj, int index, double q[3][3]);
+int field_scalar_array(field_t * obj, int index, double * array);
+int field_scalar_array_set(field_t * obj, int index, const double * array);
 int field_phi_init_spinodal(field_t * phi, int seed, double phi0, double amp);
 /* Spinodal patches of +-1, src/field_phi_init.c:537 */
 int field_phi_init_spinodal_patches(field_t * phi, int seed, int patch,
@@ -177,7 +271,7 @@ int field_phi_init_drop(field_t * phi, double xi, double radius,
  * Gradients: src/field_grad.h:44-50 (3d_7pt_fluid stencil)
  *-------------------------------------------------------------------------*/
 int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p);
-int field_grad_free(field_grad_t * obj);
+void field_grad_free(field_grad_t * obj);
 /* src/field_grad.c:319 -> src/gradient_3d_7pt_fluid.c:231 */
 int field_grad_compute(field_grad_t * obj);
 /* The stencil of field_grad_compute: 7 (default, 3d_7pt_fluid) or 27
@@ -196,13 +290,21 @@ int field_grad_to_host(field_grad_t * obj, double * grad, double * delsq);
  * Hydrodynamic fields: src/hydro.h:28-61
  *-------------------------------------------------------------------------*/
 typedef struct hydro_options_s {
-  int nhcomm;
-  int precision;
+  int nhcomm;                    /* halo width (recorded) */
+  field_options_t rho;           /* density (its iodata: file "rho") */
+  field_options_t u;             /* velocity (its iodata: file "vel") */
+  field_options_t force;
+  field_options_t eta;           /* viscosity field: unused */
 } hydro_options_t;
 
 hydro_options_t hydro_options_default(void);
+hydro_options_t hydro_options_nhalo(int nhalo);
 int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
 		 const hydro_options_t * opts, hydro_t ** pobj);
+/* hydro_create with an arithmetic and storage precision (FP64 or FP32) */
+int ludwig_gb_hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			   const hydro_options_t * opts, int precision,
+			   hydro_t ** pobj);
 int hydro_free(hydro_t * obj);
 int hydro_f_zero(hydro_t * obj, const double fzero[3]);    /* hydro.c:244 */
 int hydro_u_zero(hydro_t * obj, const double uzero[3]);    /* hydro.c:217 */
@@ -212,43 +314,118 @@ int hydro_from_host(hydro_t * obj, const double * rho, const double * u,
 		    const double * force);
 
 /*---------------------------------------------------------------------------
+ * The reference's host layout (what lb_memcpy / field_memcpy /
+ * hydro_memcpy leave in its host arrays, src/lb_data.h:144,
+ * src/field.c:329, src/hydro.c:306-331): every cs_index() site, halo sites
+ * holding the periodic images (as after lb_halo / field_halo), component
+ * k of K at
+ *     DATA_MODEL_AOS (the reference's default CPU build):  a[K*index + k]
+ *     DATA_MODEL_SOA (built with ADDR_SOA, its GPU builds): a[nsites*k + index]
+ * with nsites from cs_nsites().  Components: lb k = n*19 + p (n the
+ * distribution), fields k = n, hydro u and force k = ia, rho K = 1.  The
+ * reduced-precision forms are converted to double.  The _from_ functions
+ * read the interior sites only.  (src/memory.h:151-170, data_model_enum)
+ *-------------------------------------------------------------------------*/
+typedef enum data_model_enum_type {DATA_MODEL_AOS, DATA_MODEL_SOA,
+				   DATA_MODEL_AOSOA} data_model_enum_t;
+
+int ludwig_gb_lb_to_host_cs(lb_t * lb, int data_model, double * f);
+int ludwig_gb_lb_from_host_cs(lb_t * lb, int data_model, const double * f);
+int ludwig_gb_field_to_host_cs(field_t * obj, int data_model, double * data);
+int ludwig_gb_field_from_host_cs(field_t * obj, int data_model,
+				 const double * data);
+/* any of rho, u, force may be NULL */
+int ludwig_gb_hydro_to_host_cs(hydro_t * obj, int data_model, double * rho,
+			       double * u, double * force);
+
+/*---------------------------------------------------------------------------
  * Site status map: src/map.h:26-63 (MAP_FLUID = 0)
  *-------------------------------------------------------------------------*/
 enum map_status {MAP_FLUID, MAP_BOUNDARY, MAP_COLLOID, MAP_STATUS_MAX};
-int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj);
-int map_free(map_t * obj);
+
+/* src/map_options.h:21-26 */
+typedef struct map_options_s {
+  int ndata;                     /* 0 only (no per-site data) */
+  int is_porous_media;           /* 0 only */
+  const char * filestub;         /* recorded */
+  io_info_args_t iodata;         /* recorded */
+} map_options_t;
+
+map_options_t map_options_default(void);
+map_options_t map_options_ndata(int ndata);
+/* src/map.h:51-53 (every site starts as MAP_FLUID) */
+int map_create(pe_t * pe, cs_t * cs, const map_options_t * options,
+	       map_t ** map);
+int map_free(map_t ** map);
+/* status of every interior site (uint8, site order as the host arrays) */
 int map_status_from_host(map_t * obj, const uint8_t * status);
 
 /*---------------------------------------------------------------------------
- * Free energy: the fe_t interface of src/free_energy.h:54-80
+ * Free energy: the fe_t interface of src/free_energy.h:27-76, member for
+ * member.  The slots take cs_index() site indices (halo sites are the
+ * periodic images); the vectorised (_v) slots have NSIMDVL = 1, as the
+ * reference's default build.  Implemented: FE_SYMMETRIC (free, target,
+ * fed, mu, stress, str_symm, stress_v, str_symm_v) and FE_LC (free,
+ * target, fed, stress, str_symm, str_anti, htensor and the four _v
+ * slots); the other slots are NULL, as in the reference's tables
+ * (src/symmetric.c:46-61, src/blue_phase.c:35-50).  Each slot call reads
+ * the few values it needs from the device: a per-site host interface, as
+ * in the reference's host tables.
  *-------------------------------------------------------------------------*/
-typedef enum fe_id_enum {FE_SYMMETRIC = 1, FE_LC = 2} fe_id_enum_t;
+#ifndef NSIMDVL
+#define NSIMDVL 1
+#endif
 
-typedef int  (* fe_free_ft)(fe_t * fe);
-typedef int  (* fe_target_ft)(fe_t * fe, fe_t ** target);
-typedef int  (* fe_fed_ft)(fe_t * fe, int index, double * fed);
-typedef int  (* fe_mu_ft)(fe_t * fe, int index, double * mu);
-typedef int  (* fe_str_ft)(fe_t * fe, int index, double s[3][3]);
-typedef int  (* fe_htensor_ft)(fe_t * fe, int index, double h[3][3]);
+enum fe_id_enum {FE_NULL,
+		 FE_SYMMETRIC,
+		 FE_BRAZOVSKII,
+		 FE_SURFACTANT,
+		 FE_POLAR,
+		 FE_LC,
+		 FE_ELECTRO,
+		 FE_ELECTRO_SYMMETRIC,
+		 FE_LC_DROPLET,
+		 FE_TERNARY};
+typedef enum fe_id_enum fe_id_enum_t;
 
-typedef struct fe_vt_s {
-  fe_free_ft    free;
-  fe_target_ft  target;
-  fe_fed_ft     fed;          /* free energy density at site index */
-  fe_mu_ft      mu;           /* chemical potential (symmetric) */
-  fe_str_ft     stress;       /* full chemical stress */
-  fe_str_ft     str_symm;     /* symmetric part */
-  fe_str_ft     str_anti;     /* antisymmetric part (NULL if none) */
-  fe_htensor_ft htensor;      /* molecular field (LC), else NULL */
-} fe_vt_t;
+typedef struct fe_vt_s fe_vt_t;
 
-struct fe_s {
-  fe_id_enum_t id;
-  int use_stress_relaxation;
-  const fe_vt_t * func;
+typedef int (* fe_free_ft)(fe_t * fe);
+typedef int (* fe_id_ft)(fe_t * fe);
+typedef int (* fe_target_ft)(fe_t * fe, fe_t ** target);
+typedef int (* fe_fed_ft)(fe_t * fe, int index, double * fed);
+typedef int (* fe_mu_ft)(fe_t * fe, int index, double * mu);
+typedef int (* fe_str_ft)(fe_t * fe, int index, double s[3][3]);
+typedef int (* fe_mu_solv_ft)(fe_t * fe, int index, int k, double * mu);
+typedef int (* fe_hvector_ft)(fe_t * fe, int index, double h[3]);
+typedef int (* fe_htensor_ft)(fe_t * fe, int index, double h[3][3]);
+typedef void (* fe_htensor_v_ft)(fe_t * fe, int index,
+				 double h[3][3][NSIMDVL]);
+typedef void (* fe_stress_v_ft)(fe_t * fe, int index,
+				double s[3][3][NSIMDVL]);
+
+struct fe_vt_s {
+  fe_free_ft free;              /* destructor */
+  fe_target_ft target;          /* the object itself (no device copy) */
+  fe_fed_ft fed;                /* free energy density */
+  fe_mu_ft mu;                  /* chemical potential */
+  fe_mu_solv_ft mu_solv;        /* NULL */
+  fe_str_ft stress;             /* chemical stress (total) */
+  fe_str_ft str_symm;           /* symmetric part */
+  fe_str_ft str_anti;           /* antisymmetric part */
+  fe_hvector_ft hvector;        /* NULL */
+  fe_htensor_ft htensor;        /* molecular field */
+  fe_htensor_v_ft htensor_v;
+  fe_stress_v_ft stress_v;
+  fe_stress_v_ft str_symm_v;
+  fe_stress_v_ft str_anti_v;
 };
 
-/* index = ((x*Ly + y)*Lz + z) of an interior site (0-based) */
+struct fe_s {
+  fe_vt_t * func;
+  int id;                       /* enum fe_id_enum */
+  int use_stress_relaxation;    /* 0 only */
+};
 
 /* src/symmetric.h:38-51 */
 typedef struct fe_symm_param_s {
@@ -265,8 +442,24 @@ int fe_symm_free(fe_symm_t * fe);
 int fe_symm_param_set(fe_symm_t * fe, fe_symm_param_t values);
 int fe_symm_param(fe_symm_t * fe, fe_symm_param_t * values);
 
-/* Cholesteric liquid crystal: src/blue_phase.h:37-75 (Q as 5 components
- * XX, XY, XZ, YY, YZ of a field with ndata = 5) */
+/* Cholesteric liquid crystal: src/blue_phase.h:51-74 (Q as 5 components
+ * XX, XY, XZ, YY, YZ of a field with ndata = 5); anchoring:
+ * src/lc_anchoring.h:20-35 (no walls or colloids here: recorded only) */
+typedef enum lc_anchoring_enum {
+  LC_ANCHORING_NONE = 0,
+  LC_ANCHORING_PLANAR,
+  LC_ANCHORING_NORMAL,
+  LC_ANCHORING_FIXED,
+  LC_ANCHORING_INVALID
+} lc_anchoring_enum_t;
+
+typedef struct lc_anchoring_param_s {
+  lc_anchoring_enum_t type;
+  double w1;
+  double w2;
+  double nfix[3];
+} lc_anchoring_param_t;
+
 typedef struct fe_lc_param_s {
   double a0;
   double q0;
@@ -283,6 +476,8 @@ typedef struct fe_lc_param_s {
   double coswt;               /* field phase (1 for a static field) */
   int is_redshift_updated;    /* 0 only */
   int is_active;              /* 0 only */
+  lc_anchoring_param_t coll;  /* colloid anchoring: unused */
+  lc_anchoring_param_t wall;  /* wall anchoring: unused */
 } fe_lc_param_t;
 
 int fe_lc_create(pe_t * pe, cs_t * cs, lees_edw_t * le, field_t * q,
@@ -312,11 +507,13 @@ int blue_phase_nematic_init(cs_t * cs, fe_lc_param_t * param, field_t * q,
 			    const double n[3]);
 
 /* Beris-Edwards: src/blue_phase_beris_edwards.h:28-49 */
+#define NQAB 5
 typedef struct beris_edw_param_s {
   double xi;                  /* effective aspect ratio */
   double gamma;               /* rotational diffusion constant Gamma */
   int noise;                  /* 0 only */
   double var;
+  double tmatrix[3][3][NQAB]; /* noise basis: unused (noise off) */
 } beris_edw_param_t;
 
 int beris_edw_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
@@ -446,14 +643,17 @@ int stats_free_energy_symm(fe_symm_t * fe, double * total);
 /* LC total free energy (fe_lc_fed summed, src/stats_free_energy.c:38);
  * FP64 fields, after field_grad_compute() of the q gradients */
 int stats_free_energy_lc(fe_lc_t * fe, double * total);
-/* fe_lc_stats_info without walls or colloids (src/fe_lc_stats.c:55-150):
- * out = {f, v, f/v, f_bulk/v, f_grad/v, redshift} over the fluid sites of
- * map (all sites for NULL); after field_grad_compute() of the q gradients */
-int fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]);
-/* stats_velocity_minmax (src/stats_velocity.c:54-125): out = {min u_x,
- * u_y, u_z, max u_x, u_y, u_z, volume flux x, y, z} over the fluid sites
- * of map (all sites for NULL); min starts at FLT_MAX, max at FLT_MIN */
-int stats_velocity_minmax(hydro_t * hydro, map_t * map, double out[9]);
+/* The numbers fe_lc_stats_info prints (src/fe_lc_stats.c:55-150), without
+ * walls or colloids: out = {f, v, f/v, f_bulk/v, f_grad/v, redshift} over
+ * the fluid sites of map (all sites for NULL); after field_grad_compute()
+ * of the q gradients */
+int ludwig_gb_fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]);
+/* The numbers stats_velocity_minmax prints (src/stats_velocity.c:54-125):
+ * out = {min u_x, u_y, u_z, max u_x, u_y, u_z, volume flux x, y, z} over
+ * the fluid sites of map (all sites for NULL); min starts at FLT_MAX, max
+ * at FLT_MIN */
+int ludwig_gb_stats_velocity_minmax(hydro_t * hydro, map_t * map,
+				    double out[9]);
 
 /*---------------------------------------------------------------------------
  * Ensembles: many independent periodic binary-fluid boxes of any sizes and
@@ -628,8 +828,6 @@ int ludwig_gb_physics_use(physics_t * phys);
  * Reduced-precision objects are written as the doubles of the reference's
  * f and read back into their own precision.
  *-------------------------------------------------------------------------*/
-enum io_record_format_enum {IO_RECORD_INVALID, IO_RECORD_ASCII,
-			    IO_RECORD_BINARY};
 typedef struct io_event_s io_event_t;       /* accepted; may be NULL */
 /* record formats of input and output (default binary), the
  * lb_data_options_t / field_options_t iodata.input/output.iorformat */

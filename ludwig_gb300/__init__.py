@@ -55,19 +55,47 @@ _IORF = {"ascii": 1, "binary": 2}          # enum io_record_format_enum
 _F = ctypes.POINTER(ctypes.c_float)
 
 
+class IoOptions(ctypes.Structure):
+    """io_options_t (src/io_options.h:46-54)"""
+    _fields_ = [("mode", ctypes.c_int), ("iorformat", ctypes.c_int),
+                ("metadata_version", ctypes.c_int), ("report", ctypes.c_int),
+                ("asynchronous", ctypes.c_int),
+                ("compression_levl", ctypes.c_int),
+                ("iogrid", ctypes.c_int * 3)]
+
+
+class IoInfoArgs(ctypes.Structure):
+    """io_info_args_t (src/io_info_args.h:33-38)"""
+    _fields_ = [("input", IoOptions), ("output", IoOptions),
+                ("grid", ctypes.c_int * 3), ("iofreq", ctypes.c_int)]
+
+
 class LbDataOptions(ctypes.Structure):
+    """lb_data_options_t (src/lb_data_options.h:32-42)"""
     _fields_ = [("ndim", ctypes.c_int), ("nvel", ctypes.c_int),
                 ("ndist", ctypes.c_int), ("nrelax", ctypes.c_int),
-                ("precision", ctypes.c_int), ("fp16_scale", ctypes.c_double)]
+                ("halo", ctypes.c_int), ("reportimbalance", ctypes.c_int),
+                ("usefirsttouch", ctypes.c_int), ("iodata", IoInfoArgs)]
 
 
 class FieldOptions(ctypes.Structure):
+    """field_options_t (src/field_options.h:28-37)"""
     _fields_ = [("ndata", ctypes.c_int), ("nhcomm", ctypes.c_int),
-                ("precision", ctypes.c_int)]
+                ("haloscheme", ctypes.c_int), ("haloverbose", ctypes.c_int),
+                ("usefirsttouch", ctypes.c_int), ("iodata", IoInfoArgs)]
 
 
 class HydroOptions(ctypes.Structure):
-    _fields_ = [("nhcomm", ctypes.c_int), ("precision", ctypes.c_int)]
+    """hydro_options_t (src/hydro_options.h:22-30)"""
+    _fields_ = [("nhcomm", ctypes.c_int), ("rho", FieldOptions),
+                ("u", FieldOptions), ("force", FieldOptions),
+                ("eta", FieldOptions)]
+
+
+class MapOptions(ctypes.Structure):
+    """map_options_t (src/map_options.h:21-26)"""
+    _fields_ = [("ndata", ctypes.c_int), ("is_porous_media", ctypes.c_int),
+                ("filestub", ctypes.c_char_p), ("iodata", IoInfoArgs)]
 
 
 class FeSymmParam(ctypes.Structure):
@@ -89,6 +117,12 @@ class BoxParam(ctypes.Structure):
                 ("noise", ctypes.c_double)]
 
 
+class LcAnchoringParam(ctypes.Structure):
+    """lc_anchoring_param_t (src/lc_anchoring.h:30-35)"""
+    _fields_ = [("type", ctypes.c_int), ("w1", ctypes.c_double),
+                ("w2", ctypes.c_double), ("nfix", ctypes.c_double * 3)]
+
+
 class FeLcParam(ctypes.Structure):
     _fields_ = [("a0", ctypes.c_double), ("q0", ctypes.c_double),
                 ("gamma", ctypes.c_double), ("kappa0", ctypes.c_double),
@@ -99,12 +133,14 @@ class FeLcParam(ctypes.Structure):
                 ("amplitude0", ctypes.c_double), ("e0", ctypes.c_double * 3),
                 ("coswt", ctypes.c_double),
                 ("is_redshift_updated", ctypes.c_int),
-                ("is_active", ctypes.c_int)]
+                ("is_active", ctypes.c_int),
+                ("coll", LcAnchoringParam), ("wall", LcAnchoringParam)]
 
 
 class BerisEdwParam(ctypes.Structure):
     _fields_ = [("xi", ctypes.c_double), ("gamma", ctypes.c_double),
-                ("noise", ctypes.c_int), ("var", ctypes.c_double)]
+                ("noise", ctypes.c_int), ("var", ctypes.c_double),
+                ("tmatrix", ctypes.c_double * 45)]
 
 
 def _declare(L):
@@ -131,6 +167,44 @@ def _declare(L):
         "physics_fbody_set": ([_P, _D3], ctypes.c_int),
         "lb_data_create": ([_P, _P, ctypes.POINTER(LbDataOptions), pp],
                            ctypes.c_int),
+        "ludwig_gb_lb_data_create": ([_P, _P, ctypes.POINTER(LbDataOptions),
+                                      ctypes.c_int, ctypes.c_double, pp],
+                                     ctypes.c_int),
+        "lb_data_options_default": ([], LbDataOptions),
+        "lb_data_options_ndim_nvel_ndist": ([ctypes.c_int] * 3, LbDataOptions),
+        "field_options_default": ([], FieldOptions),
+        "field_options_ndata_nhalo": ([ctypes.c_int] * 2, FieldOptions),
+        "hydro_options_default": ([], HydroOptions),
+        "hydro_options_nhalo": ([ctypes.c_int], HydroOptions),
+        "map_options_default": ([], MapOptions),
+        "map_options_ndata": ([ctypes.c_int], MapOptions),
+        "io_options_default": ([], IoOptions),
+        "io_info_args_default": ([], IoInfoArgs),
+        "ludwig_gb_field_create": ([_P, _P, _P, ctypes.c_char_p,
+                                    ctypes.POINTER(FieldOptions), ctypes.c_int,
+                                    pp], ctypes.c_int),
+        "ludwig_gb_hydro_create": ([_P, _P, _P, ctypes.POINTER(HydroOptions),
+                                    ctypes.c_int, pp], ctypes.c_int),
+        "cs_index": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+                     ctypes.c_int),
+        "cs_nsites": ([_P, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "cs_nhalo": ([_P, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "cs_strides": ([_P] + [ctypes.POINTER(ctypes.c_int)] * 3,
+                       ctypes.c_int),
+        "cs_index_to_ijk": ([_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+                            ctypes.c_int),
+        "field_scalar": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "field_scalar_set": ([_P, ctypes.c_int, ctypes.c_double],
+                             ctypes.c_int),
+        "field_tensor": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "field_scalar_array": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "ludwig_gb_lb_to_host_cs": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "ludwig_gb_lb_from_host_cs": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "ludwig_gb_field_to_host_cs": ([_P, ctypes.c_int, _D], ctypes.c_int),
+        "ludwig_gb_field_from_host_cs": ([_P, ctypes.c_int, _D],
+                                         ctypes.c_int),
+        "ludwig_gb_hydro_to_host_cs": ([_P, ctypes.c_int, _D, _D, _D],
+                                       ctypes.c_int),
         "lb_free": ([_P], ctypes.c_int),
         "lb_init_rest_f": ([_P, ctypes.c_double], ctypes.c_int),
         "lb_halo": ([_P], ctypes.c_int),
@@ -168,7 +242,7 @@ def _declare(L):
         "field_phi_init_drop": ([_P] + [ctypes.c_double] * 3 + [ctypes.c_int],
                                 ctypes.c_int),
         "field_grad_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
-        "field_grad_free": ([_P], ctypes.c_int),
+        "field_grad_free": ([_P], None),
         "field_grad_compute": ([_P], ctypes.c_int),
         "field_grad_stencil_set": ([_P, ctypes.c_int], ctypes.c_int),
         "advection_order_set": ([ctypes.c_int], ctypes.c_int),
@@ -181,8 +255,9 @@ def _declare(L):
         "hydro_u_halo": ([_P], ctypes.c_int),
         "hydro_to_host": ([_P, _D, _D, _D], ctypes.c_int),
         "hydro_from_host": ([_P, _D, _D, _D], ctypes.c_int),
-        "map_create": ([_P, _P, ctypes.c_int, pp], ctypes.c_int),
-        "map_free": ([_P], ctypes.c_int),
+        "map_create": ([_P, _P, ctypes.POINTER(MapOptions), pp],
+                       ctypes.c_int),
+        "map_free": ([pp], ctypes.c_int),
         "map_status_from_host": ([_P, ctypes.POINTER(ctypes.c_uint8)],
                                  ctypes.c_int),
         "fe_symm_create": ([_P, _P, _P, _P, pp], ctypes.c_int),
@@ -287,8 +362,8 @@ def _declare(L):
         "stats_distribution": ([_P, _D], ctypes.c_int),
         "stats_free_energy_symm": ([_P, _D], ctypes.c_int),
         "stats_free_energy_lc": ([_P, _D], ctypes.c_int),
-        "fe_lc_stats_info": ([_P, _P, _D], ctypes.c_int),
-        "stats_velocity_minmax": ([_P, _P, _D], ctypes.c_int),
+        "ludwig_gb_fe_lc_stats_info": ([_P, _P, _D], ctypes.c_int),
+        "ludwig_gb_stats_velocity_minmax": ([_P, _P, _D], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -392,9 +467,10 @@ class LB(_Obj):
         self.cs = cs
         self.precision = precision
         self.ndist = int(ndist)
-        o = LbDataOptions(3, 19, int(ndist), int(nrelax), int(precision),
-                          float(fp16_scale))
-        self.ptr = _new("lb_data_create", cs.pe.ptr, cs.ptr, ctypes.byref(o))
+        o = lib().lb_data_options_ndim_nvel_ndist(3, 19, int(ndist))
+        o.nrelax = int(nrelax)
+        self.ptr = _new("ludwig_gb_lb_data_create", cs.pe.ptr, cs.ptr,
+                        ctypes.byref(o), int(precision), float(fp16_scale))
 
     def init_rest(self, rho0=1.0):
         _check(lib().lb_init_rest_f(self.ptr, float(rho0)), "lb_init_rest_f")
@@ -460,9 +536,9 @@ class Field(_Obj):
         self.cs = cs
         self.nf = nf
         self.name = name
-        o = FieldOptions(int(nf), int(nhalo), int(precision))
-        self.ptr = _new("field_create", cs.pe.ptr, cs.ptr, None,
-                        name.encode(), ctypes.byref(o))
+        o = lib().field_options_ndata_nhalo(int(nf), int(nhalo))
+        self.ptr = _new("ludwig_gb_field_create", cs.pe.ptr, cs.ptr, None,
+                        name.encode(), ctypes.byref(o), int(precision))
 
     def get(self):
         a = np.zeros((self.nf,) + self.cs.ntotal)
@@ -556,9 +632,9 @@ class Hydro(_Obj):
     def __init__(self, cs, precision=FP64):
         super().__init__()
         self.cs = cs
-        o = HydroOptions(1, int(precision))
-        self.ptr = _new("hydro_create", cs.pe.ptr, cs.ptr, None,
-                        ctypes.byref(o))
+        o = lib().hydro_options_default()
+        self.ptr = _new("ludwig_gb_hydro_create", cs.pe.ptr, cs.ptr, None,
+                        ctypes.byref(o), int(precision))
 
     def get(self):
         n = self.cs.ntotal
@@ -608,20 +684,25 @@ class Hydro(_Obj):
         """(umin[3], umax[3], volume flux[3]) over the fluid sites, as
         stats_velocity_minmax prints them."""
         out = np.zeros(9)
-        _check(lib().stats_velocity_minmax(self.ptr,
-                                           map.ptr if map else None,
-                                           _dp(out)),
-               "stats_velocity_minmax")
+        _check(lib().ludwig_gb_stats_velocity_minmax(
+            self.ptr, map.ptr if map else None, _dp(out)),
+            "stats_velocity_minmax")
         return out[0:3], out[3:6], out[6:9]
 
 
 class Map(_Obj):
-    _free = "map_free"
-
     def __init__(self, cs):
         super().__init__()
         self.cs = cs
-        self.ptr = _new("map_create", cs.pe.ptr, cs.ptr, 0)
+        self.options = lib().map_options_default()
+        self.ptr = _new("map_create", cs.pe.ptr, cs.ptr,
+                        ctypes.byref(self.options))
+
+    def close(self):
+        if self.ptr is not None:
+            p = ctypes.c_void_p(self.ptr.value)
+            lib().map_free(ctypes.byref(p))
+            self.ptr = None
 
     def set_status(self, status):
         s = np.ascontiguousarray(status, dtype=np.uint8)
@@ -944,8 +1025,8 @@ class FeLC(_Obj):
         if recompute:
             self.dq.compute()
         out = np.zeros(6)
-        _check(lib().fe_lc_stats_info(self.ptr, map.ptr if map else None,
-                                      _dp(out)), "fe_lc_stats_info")
+        _check(lib().ludwig_gb_fe_lc_stats_info(
+            self.ptr, map.ptr if map else None, _dp(out)), "fe_lc_stats_info")
         return out
 
 

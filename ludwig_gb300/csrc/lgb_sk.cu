@@ -96,14 +96,23 @@ __device__ int bin_reference(const lgbk_dims_t & d, int ii, int j, int k) {
   return (int) floor(r);
 }
 
-/* Bin with the wavevector 2 pi i / n - 2 pi for i > n/2, in FP64 */
+/* Bin with the wavevector 2 pi i / n - 2 pi for i > n/2, in FP64, one
+ * rounding per operation in the order ((kx kx + ky ky) + kz kz): diagonal
+ * wavevectors (m, m, m) of a cube whose side is a multiple of 128 lie
+ * exactly on bin edges, so a fused multiply-add would move them. */
 __device__ int bin_corrected(const lgbk_dims_t & d, int ii, int j, int k) {
   const double pi = 3.14159265358979323846;
-  double kx = 2.0*pi*ii/d.nx; if (ii > d.nx/2) kx -= 2.0*pi;
-  double ky = 2.0*pi*j/d.ny;  if (j > d.ny/2) ky -= 2.0*pi;
-  double kz = 2.0*pi*k/d.nz;
-  double kmod = sqrt(kx*kx + ky*ky + kz*kz);
-  return (int) floor(kmod*LGBK_SK_NBIN/(sqrt(3.0)*pi));
+  const double twopi = 2.0*pi;
+  double kx = __ddiv_rn(__dmul_rn(twopi, (double) ii), (double) d.nx);
+  if (ii > d.nx/2) kx = __dsub_rn(kx, twopi);
+  double ky = __ddiv_rn(__dmul_rn(twopi, (double) j), (double) d.ny);
+  if (j > d.ny/2) ky = __dsub_rn(ky, twopi);
+  double kz = __ddiv_rn(__dmul_rn(twopi, (double) k), (double) d.nz);
+  double s = __dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)),
+		       __dmul_rn(kz, kz));
+  double kmod = __dsqrt_rn(s);
+  return (int) floor(__ddiv_rn(__dmul_rn(kmod, (double) LGBK_SK_NBIN),
+			       __dmul_rn(__dsqrt_rn(3.0), pi)));
 }
 
 __global__ void k_bin_sk(lgbk_dims_t d, int faithful,

@@ -228,6 +228,79 @@ int cs_nlocal(cs_t * cs, int nlocal[3]) {
   return LUDWIG_GB_OK;
 }
 
+int cs_ntotal(cs_t * cs, int ntotal[3]) {
+  if (cs == NULL || ntotal == NULL) return err_set(LUDWIG_GB_EINVAL, "cs");
+  for (int i = 0; i < 3; i++) ntotal[i] = cs->ntotal[i];
+  return LUDWIG_GB_OK;
+}
+
+int cs_nhalo(cs_t * cs, int * nhalo) {
+  if (cs == NULL || nhalo == NULL) return err_set(LUDWIG_GB_EINVAL, "cs");
+  *nhalo = cs->nhalo;
+  return LUDWIG_GB_OK;
+}
+
+/* Extents with the halo, src/coords.c (cs_nall) */
+int cs_nall(cs_t * cs, int nall[3]) {
+  if (cs == NULL || nall == NULL) return err_set(LUDWIG_GB_EINVAL, "cs");
+  for (int i = 0; i < 3; i++) nall[i] = cs->ntotal[i] + 2*cs->nhalo;
+  return LUDWIG_GB_OK;
+}
+
+int cs_nsites(cs_t * cs, int * nsites) {
+  int n[3];
+  int rc = cs_nall(cs, n);
+  if (rc) return rc;
+  if (nsites == NULL) return err_set(LUDWIG_GB_EINVAL, "cs_nsites");
+  *nsites = n[0]*n[1]*n[2];
+  return LUDWIG_GB_OK;
+}
+
+int cs_strides(cs_t * cs, int * xs, int * ys, int * zs) {
+  int n[3];
+  int rc = cs_nall(cs, n);
+  if (rc) return rc;
+  *xs = n[1]*n[2];
+  *ys = n[2];
+  *zs = 1;
+  return LUDWIG_GB_OK;
+}
+
+/* src/coords.c:617-631: ic, jc, kc from 1 - nhalo to L + nhalo */
+int cs_index(cs_t * cs, int ic, int jc, int kc) {
+  int xs = 0, ys = 0, zs = 0;
+  if (cs_strides(cs, &xs, &ys, &zs)) return -1;
+  return xs*(cs->nhalo + ic - 1) + ys*(cs->nhalo + jc - 1)
+    + zs*(cs->nhalo + kc - 1);
+}
+
+/* src/coords.c:790-801 */
+int cs_index_to_ijk(cs_t * cs, int index, int coords[3]) {
+  int xs = 0, ys = 0, zs = 0;
+  int rc = cs_strides(cs, &xs, &ys, &zs);
+  if (rc) return rc;
+  coords[0] = (1 - cs->nhalo) + index/xs;
+  coords[1] = (1 - cs->nhalo) + (index % xs)/ys;
+  coords[2] = (1 - cs->nhalo) + index % ys;
+  return LUDWIG_GB_OK;
+}
+
+/* Interior site (0-based, ((x*Ly + y)*Lz + z)) of a cs_index() site: halo
+ * sites are the periodic images of the interior sites they copy.  -1 if
+ * the index is not a site of the lattice with its halo. */
+static long long cs_interior(const cs_t * cs, int index) {
+  const int h = cs->nhalo;
+  const int ny = cs->ntotal[1] + 2*h, nz = cs->ntotal[2] + 2*h;
+  const long long nall = (long long) (cs->ntotal[0] + 2*h)*ny*nz;
+  if (index < 0 || index >= nall) return -1;
+  int c[3] = {index/(ny*nz), (index % (ny*nz))/nz, index % nz};
+  for (int a = 0; a < 3; a++) {
+    int n = cs->ntotal[a];
+    c[a] = ((c[a] - h) % n + n) % n;
+  }
+  return ((long long) c[0]*cs->ntotal[1] + c[1])*cs->ntotal[2] + c[2];
+}
+
 struct physics_s {
   double rho0;
   double eta_shear;
@@ -295,13 +368,60 @@ struct lb_data_s {
   lgb_io_state_t io;           /* snapshot files */
 };
 
+/* src/io_options.c:26-40, src/io_info_args.c:28-35 */
+io_options_t io_options_default(void) {
+  io_options_t o = {IO_MODE_MPIIO, IO_RECORD_BINARY, IO_METADATA_V2, 0, 0, 0,
+		    {1, 1, 1}};
+  return o;
+}
+
+io_info_args_t io_info_args_default(void) {
+  io_info_args_t a;
+  a.input = io_options_default();
+  a.output = io_options_default();
+  a.grid[0] = a.grid[1] = a.grid[2] = 1;
+  a.iofreq = 0;
+  return a;
+}
+
+/* record format of a side of iodata (binary unless ascii is asked for) */
+static int io_format_of(const io_options_t * o) {
+  return (o->iorformat == IO_RECORD_ASCII) ? IO_RECORD_ASCII
+    : IO_RECORD_BINARY;
+}
+
+/* src/lb_data_options.c:28-57 */
 lb_data_options_t lb_data_options_default(void) {
-  lb_data_options_t o = {3, 19, 1, LB_RELAXATION_M10, LUDWIG_GB_FP64, 0.0};
+  lb_data_options_t o;
+  memset(&o, 0, sizeof(o));
+  o.ndim = 3;
+  o.nvel = 19;
+  o.ndist = 1;
+  o.nrelax = LB_RELAXATION_M10;
+  o.halo = LB_HALO_FULL;
+  o.reportimbalance = 0;
+  o.usefirsttouch = 0;
+  o.iodata = io_info_args_default();
+  return o;
+}
+
+lb_data_options_t lb_data_options_ndim_nvel_ndist(int ndim, int nvel,
+						  int ndist) {
+  lb_data_options_t o = lb_data_options_default();
+  o.ndim = ndim;
+  o.nvel = nvel;
+  o.ndist = ndist;
   return o;
 }
 
 int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
 		   lb_t ** plb) {
+  return ludwig_gb_lb_data_create(pe, cs, opts, LUDWIG_GB_FP64, 0.0, plb);
+}
+
+int ludwig_gb_lb_data_create(pe_t * pe, cs_t * cs,
+			     const lb_data_options_t * opts, int precision,
+			     double fp16_scale, lb_t ** plb) {
   (void) pe;
   lb_data_options_t o = opts ? *opts : lb_data_options_default();
   if (cs == NULL || !cs->initialised || plb == NULL) {
@@ -310,11 +430,14 @@ int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
   if (o.ndim != 3 || o.nvel != 19 || (o.ndist != 1 && o.ndist != 2)) {
     return err_set(LUDWIG_GB_EINVAL, "lb_data_create: D3Q19, ndist 1 or 2");
   }
-  if (o.ndist == 2 && o.precision != LUDWIG_GB_FP64) {
+  if (o.ndist == 2 && precision != LUDWIG_GB_FP64) {
     return err_set(LUDWIG_GB_EINVAL, "lb_data_create: ndist 2 is FP64");
   }
-  if (o.precision < LUDWIG_GB_FP64 || o.precision > LUDWIG_GB_FP16) {
+  if (precision < LUDWIG_GB_FP64 || precision > LUDWIG_GB_FP16) {
     return err_set(LUDWIG_GB_EINVAL, "lb_data_create: precision");
+  }
+  if (o.nrelax < LB_RELAXATION_M10 || o.nrelax > LB_RELAXATION_TRT) {
+    return err_set(LUDWIG_GB_EINVAL, "lb_data_create: nrelax");
   }
   int rc = lib_init();
   if (rc) return rc;
@@ -322,9 +445,11 @@ int lb_data_create(pe_t * pe, cs_t * cs, const lb_data_options_t * opts,
   lb_t * lb = (lb_t *) calloc(1, sizeof(lb_t));
   if (lb == NULL) return err_set(LUDWIG_GB_ENOMEM, "lb_data_create");
   lb->cs = cs;
-  lb->prec = o.precision;
+  lb->prec = precision;
   lb->nrelax = o.nrelax;
-  lb->fscale = (o.fp16_scale > 0.0) ? o.fp16_scale : 1024.0;
+  lb->fscale = (fp16_scale > 0.0) ? fp16_scale : 1024.0;
+  lb->io.fmt_in = io_format_of(&o.iodata.input);
+  lb->io.fmt_out = io_format_of(&o.iodata.output);
   lb->rho0 = phys_ref_ ? phys_ref_->rho0 : 1.0;
 
   size_t bytes = NVEL*(size_t) cs->d.nsites*prec_size(lb->prec);
@@ -503,13 +628,34 @@ struct field_s {
   lgb_io_state_t io;           /* snapshot files */
 };
 
+/* src/field_options.c:27-52 */
+field_options_t field_options_default(void) {
+  field_options_t o;
+  memset(&o, 0, sizeof(o));
+  o.ndata = 1;
+  o.nhcomm = 0;
+  o.haloscheme = FIELD_HALO_TARGET;
+  o.haloverbose = 0;
+  o.usefirsttouch = 0;
+  o.iodata = io_info_args_default();
+  return o;
+}
+
 field_options_t field_options_ndata_nhalo(int ndata, int nhalo) {
-  field_options_t o = {ndata, nhalo, LUDWIG_GB_FP64};
+  field_options_t o = field_options_default();
+  o.ndata = ndata;
+  o.nhcomm = nhalo;
   return o;
 }
 
 int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
 		 const field_options_t * opts, field_t ** pobj) {
+  return ludwig_gb_field_create(pe, cs, le, name, opts, LUDWIG_GB_FP64, pobj);
+}
+
+int ludwig_gb_field_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			   const char * name, const field_options_t * opts,
+			   int precision, field_t ** pobj) {
   (void) pe;
   if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
   if (cs == NULL || !cs->initialised || opts == NULL || pobj == NULL) {
@@ -518,6 +664,9 @@ int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
   if (opts->ndata < 1 || opts->ndata > 5) {
     return err_set(LUDWIG_GB_EINVAL, "field_create: ndata in 1..5");
   }
+  if (precision != LUDWIG_GB_FP64 && precision != LUDWIG_GB_FP32) {
+    return err_set(LUDWIG_GB_EINVAL, "field_create: FP64 or FP32");
+  }
   int rc = lib_init();
   if (rc) return rc;
   field_t * f = (field_t *) calloc(1, sizeof(field_t));
@@ -525,7 +674,9 @@ int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
   f->cs = cs;
   f->nf = opts->ndata;
   f->nhcomm = opts->nhcomm;
-  f->prec = opts->precision;
+  f->prec = precision;
+  f->io.fmt_in = io_format_of(&opts->iodata.input);
+  f->io.fmt_out = io_format_of(&opts->iodata.output);
   snprintf(f->name, sizeof(f->name), "%s", name ? name : "field");
   size_t bytes = (size_t) f->nf*cs->d.nsites*field_size(f->prec);
   if ((rc = dev_alloc(&f->data, bytes, "field")) ||
@@ -734,9 +885,8 @@ int field_grad_create(pe_t * pe, field_t * f, int level, field_grad_t ** p) {
   return LUDWIG_GB_OK;
 }
 
-int field_grad_free(field_grad_t * g) {
+void field_grad_free(field_grad_t * g) {
   if (g) { dev_free(g->grad); dev_free(g->delsq); free(g); }
-  return LUDWIG_GB_OK;
 }
 
 static int grad_alloc(field_grad_t * g) {
@@ -807,17 +957,37 @@ struct hydro_s {
   lgb_io_state_t io_vel;
 };
 
-hydro_options_t hydro_options_default(void) {
-  hydro_options_t o = {1, LUDWIG_GB_FP64};
+/* src/hydro_options.c:32-72 */
+hydro_options_t hydro_options_nhalo(int nhalo) {
+  hydro_options_t o;
+  memset(&o, 0, sizeof(o));
+  o.nhcomm = nhalo;
+  o.rho = field_options_ndata_nhalo(1, nhalo);
+  o.u = field_options_ndata_nhalo(3, nhalo);
+  o.force = field_options_ndata_nhalo(3, nhalo);
+  o.eta = field_options_ndata_nhalo(1, nhalo);
   return o;
+}
+
+hydro_options_t hydro_options_default(void) {
+  return hydro_options_nhalo(1);
 }
 
 int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
 		 const hydro_options_t * opts, hydro_t ** pobj) {
+  return ludwig_gb_hydro_create(pe, cs, le, opts, LUDWIG_GB_FP64, pobj);
+}
+
+int ludwig_gb_hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
+			   const hydro_options_t * opts, int precision,
+			   hydro_t ** pobj) {
   (void) pe;
   if (le != NULL) return err_set(LUDWIG_GB_EINVAL, "Lees-Edwards planes");
   if (cs == NULL || !cs->initialised || pobj == NULL) {
     return err_set(LUDWIG_GB_EINVAL, "hydro_create");
+  }
+  if (precision != LUDWIG_GB_FP64 && precision != LUDWIG_GB_FP32) {
+    return err_set(LUDWIG_GB_EINVAL, "hydro_create: FP64 or FP32");
   }
   hydro_options_t o = opts ? *opts : hydro_options_default();
   int rc = lib_init();
@@ -825,7 +995,11 @@ int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
   hydro_t * h = (hydro_t *) calloc(1, sizeof(hydro_t));
   if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "hydro_create");
   h->cs = cs;
-  h->prec = o.precision;
+  h->prec = precision;
+  h->io_rho.fmt_in = io_format_of(&o.rho.iodata.input);
+  h->io_rho.fmt_out = io_format_of(&o.rho.iodata.output);
+  h->io_vel.fmt_in = io_format_of(&o.u.iodata.input);
+  h->io_vel.fmt_out = io_format_of(&o.u.iodata.output);
   size_t n = (size_t) cs->d.nsites, es = field_size(h->prec);
   if ((rc = dev_alloc(&h->rho, n*es, "rho")) ||
       (rc = dev_alloc(&h->u, 3*n*es, "u")) ||
@@ -909,10 +1083,32 @@ struct map_s {
   long long nfluid;
 };
 
-int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj) {
+/* src/map_options.c:26-52 */
+map_options_t map_options_default(void) {
+  map_options_t o;
+  memset(&o, 0, sizeof(o));
+  o.ndata = 0;
+  o.is_porous_media = 0;
+  o.filestub = "map";
+  o.iodata = io_info_args_default();
+  return o;
+}
+
+map_options_t map_options_ndata(int ndata) {
+  map_options_t o = map_options_default();
+  o.ndata = ndata;
+  return o;
+}
+
+int map_create(pe_t * pe, cs_t * cs, const map_options_t * options,
+	       map_t ** pobj) {
   (void) pe;
-  if (cs == NULL || !cs->initialised || pobj == NULL || ndata != 0) {
-    return err_set(LUDWIG_GB_EINVAL, "map_create: ndata 0 only");
+  if (cs == NULL || !cs->initialised || pobj == NULL || options == NULL) {
+    return err_set(LUDWIG_GB_EINVAL, "map_create");
+  }
+  if (options->ndata != 0 || options->is_porous_media != 0) {
+    return err_set(LUDWIG_GB_EINVAL, "map_create: ndata 0 and no porous "
+		   "media only");
   }
   int rc = lib_init();
   if (rc) return rc;
@@ -931,8 +1127,13 @@ int map_create(pe_t * pe, cs_t * cs, int ndata, map_t ** pobj) {
   return LUDWIG_GB_OK;
 }
 
-int map_free(map_t * m) {
-  if (m) { dev_free(m->status); free(m); }
+/* src/map.h:53: frees *map and sets it to NULL */
+int map_free(map_t ** pm) {
+  if (pm && *pm) {
+    dev_free((*pm)->status);
+    free(*pm);
+    *pm = NULL;
+  }
   return LUDWIG_GB_OK;
 }
 
@@ -1001,12 +1202,26 @@ static int grad_site(field_grad_t * g, int index, double gr[3], double * dsq) {
   return LUDWIG_GB_OK;
 }
 
+/* The slots of the function tables take cs_index() sites (halo sites are
+ * periodic images); the device arrays hold the interior sites. */
+static int slot_site(const field_t * f, int index, int * i) {
+  long long k = cs_interior(f->cs, index);
+  if (k < 0) {
+    return err_set(LUDWIG_GB_EINVAL, "free energy: index %d is not a "
+		   "cs_index() site", index);
+  }
+  *i = (int) k;
+  return LUDWIG_GB_OK;
+}
+
 /* src/symmetric.c:285-300 */
 static int symm_fed(fe_t * base, int index, double * fed) {
   fe_symm_t * fe = (fe_symm_t *) base;
   double phi, g[3];
-  int rc = site_get(fe->phi, 0, index, &phi);
-  if (rc == 0) rc = grad_site(fe->dphi, index, g, NULL);
+  int i = 0;
+  int rc = slot_site(fe->phi, index, &i);
+  if (rc == 0) rc = site_get(fe->phi, 0, i, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, i, g, NULL);
   if (rc) return rc;
   *fed = (0.5*fe->param.a + 0.25*fe->param.b*phi*phi)*phi*phi
     + 0.5*fe->param.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
@@ -1017,8 +1232,10 @@ static int symm_fed(fe_t * base, int index, double * fed) {
 static int symm_mu(fe_t * base, int index, double * mu) {
   fe_symm_t * fe = (fe_symm_t *) base;
   double phi, g[3], dsq;
-  int rc = site_get(fe->phi, 0, index, &phi);
-  if (rc == 0) rc = grad_site(fe->dphi, index, g, &dsq);
+  int i = 0;
+  int rc = slot_site(fe->phi, index, &i);
+  if (rc == 0) rc = site_get(fe->phi, 0, i, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, i, g, &dsq);
   if (rc) return rc;
   *mu = fe->param.a*phi + fe->param.b*phi*phi*phi - fe->param.kappa*dsq;
   return LUDWIG_GB_OK;
@@ -1028,8 +1245,10 @@ static int symm_mu(fe_t * base, int index, double * mu) {
 static int symm_str(fe_t * base, int index, double s[3][3]) {
   fe_symm_t * fe = (fe_symm_t *) base;
   double phi, g[3], dsq;
-  int rc = site_get(fe->phi, 0, index, &phi);
-  if (rc == 0) rc = grad_site(fe->dphi, index, g, &dsq);
+  int i = 0;
+  int rc = slot_site(fe->phi, index, &i);
+  if (rc == 0) rc = site_get(fe->phi, 0, i, &phi);
+  if (rc == 0) rc = grad_site(fe->dphi, i, g, &dsq);
   if (rc) return rc;
   double kappa = fe->param.kappa;
   double p0 = 0.5*fe->param.a*phi*phi + 0.75*fe->param.b*phi*phi*phi*phi
@@ -1043,11 +1262,35 @@ static int symm_str(fe_t * base, int index, double s[3][3]) {
   return LUDWIG_GB_OK;
 }
 
+/* src/symmetric.c:372-400: the stress at the NSIMDVL (= 1) sites from
+ * index.  The slot type returns nothing: a failure leaves s untouched and
+ * the message in ludwig_gb_last_error(). */
+static void symm_str_v(fe_t * base, int index, double s[3][3][NSIMDVL]) {
+  double t[3][3];
+  if (symm_str(base, index, t)) return;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib][0] = t[ia][ib];
+}
+
 static int symm_free(fe_t * base) { return fe_symm_free((fe_symm_t *) base); }
 static int symm_target(fe_t * base, fe_t ** t) { *t = base; return 0; }
 
-static const fe_vt_t fe_symm_vt_ = {
-  symm_free, symm_target, symm_fed, symm_mu, symm_str, symm_str, NULL, NULL
+/* src/symmetric.c:46-61, slot for slot */
+static fe_vt_t fe_symm_vt_ = {
+  symm_free,               /* free */
+  symm_target,             /* target */
+  symm_fed,                /* fed */
+  symm_mu,                 /* mu */
+  NULL,                    /* mu_solv */
+  symm_str,                /* stress */
+  symm_str,                /* str_symm */
+  NULL,                    /* str_anti */
+  NULL,                    /* hvector */
+  NULL,                    /* htensor */
+  NULL,                    /* htensor_v */
+  symm_str_v,              /* stress_v */
+  symm_str_v,              /* str_symm_v */
+  NULL                     /* str_anti_v */
 };
 
 int fe_symm_create(pe_t * pe, cs_t * cs, field_t * phi, field_grad_t * dphi,
@@ -1060,6 +1303,7 @@ int fe_symm_create(pe_t * pe, cs_t * cs, field_t * phi, field_grad_t * dphi,
   if (fe == NULL) return err_set(LUDWIG_GB_ENOMEM, "fe_symm_create");
   fe->super.id = FE_SYMMETRIC;
   fe->super.func = &fe_symm_vt_;
+  fe->super.use_stress_relaxation = 0;
   /* Defaults of src/symmetric.c:40-42 */
   fe->param.a = -0.003125;
   fe->param.b = +0.003125;
@@ -1236,9 +1480,8 @@ static int lc_site_eval(fe_lc_t * fe, int index, int what, double * out) {
   int ncomp = (what == 0) ? 1 : ((what == 1) ? 9 : 5);
   int rc = lc_ready(fe);
   if (rc) return rc;
-  if (index < 0 || index >= d->nsites) {
-    return err_set(LUDWIG_GB_EINVAL, "site index out of range");
-  }
+  int i = 0;
+  if ((rc = slot_site(fe->q, index, &i))) return rc;
   rc = dev_alloc((void **) &tmp, (size_t) ncomp*d->nsites*sizeof(double),
 		 "lc_site");
   if (rc) return rc;
@@ -1252,7 +1495,7 @@ static int lc_site_eval(fe_lc_t * fe, int index, int what, double * out) {
 				    tmp, stream_);
   if (rc == 0) rc = cudaStreamSynchronize(stream_);
   for (int n = 0; rc == 0 && n < ncomp; n++) {
-    rc = cudaMemcpy(out + n, tmp + (size_t) n*d->nsites + index,
+    rc = cudaMemcpy(out + n, tmp + (size_t) n*d->nsites + i,
 		    sizeof(double), cudaMemcpyDeviceToHost);
   }
   dev_free(tmp);
@@ -1286,7 +1529,7 @@ int stats_free_energy_lc(fe_lc_t * fe, double * total) {
  * (src/fe_lc_stats.c:55-150): out = {f, v, f/v, f_bulk/v, f_grad/v,
  * redshift}, sums over the fluid sites of the map (all sites for map
  * NULL).  Needs field_grad_compute() on the q gradients first. */
-int fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]) {
+int ludwig_gb_fe_lc_stats_info(fe_lc_t * fe, map_t * map, double out[6]) {
   if (fe == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
   int rc = lc_ready(fe);
   if (rc) return rc;
@@ -1325,24 +1568,6 @@ static int lc_stress(fe_t * base, int index, double s[3][3]) {
   return lc_site_eval((fe_lc_t *) base, index, 1, &s[0][0]);
 }
 
-static int lc_str_symm(fe_t * base, int index, double s[3][3]) {
-  double t[3][3];
-  int rc = lc_stress(base, index, t);
-  if (rc) return rc;
-  for (int ia = 0; ia < 3; ia++)
-    for (int ib = 0; ib < 3; ib++) s[ia][ib] = 0.5*(t[ia][ib] + t[ib][ia]);
-  return LUDWIG_GB_OK;
-}
-
-static int lc_str_anti(fe_t * base, int index, double s[3][3]) {
-  double t[3][3];
-  int rc = lc_stress(base, index, t);
-  if (rc) return rc;
-  for (int ia = 0; ia < 3; ia++)
-    for (int ib = 0; ib < 3; ib++) s[ia][ib] = 0.5*(t[ia][ib] - t[ib][ia]);
-  return LUDWIG_GB_OK;
-}
-
 static int lc_htensor(fe_t * base, int index, double h[3][3]) {
   double h5[5];
   int rc = lc_site_eval((fe_lc_t *) base, index, 2, h5);
@@ -1353,12 +1578,97 @@ static int lc_htensor(fe_t * base, int index, double h[3][3]) {
   return LUDWIG_GB_OK;
 }
 
+/* The antisymmetric piece of the stress, -(Q_ac H_bc - H_ac Q_bc) summed
+ * over c (src/blue_phase.c:780-812), from Q and H at the site */
+static int lc_qh(fe_t * base, int index, double q[3][3], double h[3][3]) {
+  fe_lc_t * fe = (fe_lc_t *) base;
+  int rc = field_tensor(fe->q, index, q);
+  if (rc == 0) rc = lc_htensor(base, index, h);
+  return rc;
+}
+
+static int lc_str_anti(fe_t * base, int index, double s[3][3]) {
+  double q[3][3], h[3][3];
+  int rc = lc_qh(base, index, q, h);
+  if (rc) return rc;
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      s[ia][ib] = 0.0;
+      for (int ic = 0; ic < 3; ic++) {
+	s[ia][ib] -= (q[ia][ic]*h[ib][ic] - h[ia][ic]*q[ib][ic]);
+      }
+    }
+  }
+  return LUDWIG_GB_OK;
+}
+
+/* The stress with its antisymmetric piece taken out
+ * (src/blue_phase.c:729-770) */
+static int lc_str_symm(fe_t * base, int index, double s[3][3]) {
+  double q[3][3], h[3][3];
+  int rc = lc_stress(base, index, s);
+  if (rc == 0) rc = lc_qh(base, index, q, h);
+  if (rc) return rc;
+  for (int ia = 0; ia < 3; ia++) {
+    for (int ib = 0; ib < 3; ib++) {
+      for (int ic = 0; ic < 3; ic++) {
+	s[ia][ib] += q[ia][ic]*h[ib][ic] - h[ia][ic]*q[ib][ic];
+      }
+    }
+  }
+  return LUDWIG_GB_OK;
+}
+
+/* Vectorised slots at NSIMDVL = 1 (src/blue_phase.c:1669-2279): the site
+ * index; a failure leaves the output untouched, message in
+ * ludwig_gb_last_error() */
+static void lc_htensor_v(fe_t * base, int index, double h[3][3][NSIMDVL]) {
+  double t[3][3];
+  if (lc_htensor(base, index, t)) return;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) h[ia][ib][0] = t[ia][ib];
+}
+
+static void lc_stress_v(fe_t * base, int index, double s[3][3][NSIMDVL]) {
+  double t[3][3];
+  if (lc_stress(base, index, t)) return;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib][0] = t[ia][ib];
+}
+
+static void lc_str_symm_v(fe_t * base, int index, double s[3][3][NSIMDVL]) {
+  double t[3][3];
+  if (lc_str_symm(base, index, t)) return;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib][0] = t[ia][ib];
+}
+
+static void lc_str_anti_v(fe_t * base, int index, double s[3][3][NSIMDVL]) {
+  double t[3][3];
+  if (lc_str_anti(base, index, t)) return;
+  for (int ia = 0; ia < 3; ia++)
+    for (int ib = 0; ib < 3; ib++) s[ia][ib][0] = t[ia][ib];
+}
+
 static int lc_free(fe_t * base) { return fe_lc_free((fe_lc_t *) base); }
 static int lc_target(fe_t * base, fe_t ** t) { *t = base; return 0; }
 
-static const fe_vt_t fe_lc_vt_ = {
-  lc_free, lc_target, lc_fed, NULL, lc_stress, lc_str_symm, lc_str_anti,
-  lc_htensor
+/* src/blue_phase.c:35-50, slot for slot */
+static fe_vt_t fe_lc_vt_ = {
+  lc_free,                 /* free */
+  lc_target,               /* target */
+  lc_fed,                  /* fed */
+  NULL,                    /* mu */
+  NULL,                    /* mu_solv */
+  lc_stress,               /* stress */
+  lc_str_symm,             /* str_symm */
+  lc_str_anti,             /* str_anti */
+  NULL,                    /* hvector */
+  lc_htensor,              /* htensor */
+  lc_htensor_v,            /* htensor_v */
+  lc_stress_v,             /* stress_v */
+  lc_str_symm_v,           /* str_symm_v */
+  lc_str_anti_v            /* str_anti_v */
 };
 
 int fe_lc_create(pe_t * pe, cs_t * cs, lees_edw_t * le, field_t * q,
@@ -2334,7 +2644,8 @@ int stats_field_q(field_t * field, int n, double out[5]) {
  * starts from FLT_MAX and the maximum from FLT_MIN (the smallest positive
  * float), so a component that is negative everywhere reports FLT_MIN as
  * its maximum. */
-int stats_velocity_minmax(hydro_t * hydro, map_t * map, double out[9]) {
+int ludwig_gb_stats_velocity_minmax(hydro_t * hydro, map_t * map,
+				    double out[9]) {
   if (hydro == NULL || out == NULL) return err_set(LUDWIG_GB_EINVAL, "stats");
   const lgbk_dims_t * d = &hydro->cs->d;
   if (map && map->cs->d.nsites != d->nsites) {
@@ -3206,6 +3517,201 @@ int lgb_internal_hydro_io(hydro_t * h, int ntotal[3], lgb_io_state_t ** rho,
   *rho = s[0];
   *vel = s[1];
   return LUDWIG_GB_OK;
+}
+
+/*****************************************************************************
+ *  Per-site field values at cs_index() sites (src/field.c field_scalar,
+ *  field_vector, field_tensor, field_scalar_array and their _set forms)
+ *****************************************************************************/
+
+/* Read (write = 0) or write count components n0 .. n0+count-1 of the
+ * interior site behind cs_index() site index */
+static int field_site_rw(field_t * f, int index, int n0, int count,
+			 double * v, int write) {
+  if (f == NULL || v == NULL) return err_set(LUDWIG_GB_EINVAL, "field site");
+  if (n0 + count > f->nf) {
+    return err_set(LUDWIG_GB_EINVAL, "field site: %d components asked of "
+		   "a field of %d", n0 + count, f->nf);
+  }
+  long long i = cs_interior(f->cs, index);
+  if (i < 0) return err_set(LUDWIG_GB_EINVAL, "field site: index %d is not "
+			    "a cs_index() site", index);
+  const size_t N = (size_t) f->cs->d.nsites, es = field_size(f->prec);
+  for (int k = 0; k < count; k++) {
+    char * a = (char *) f->data + ((size_t) (n0 + k)*N + (size_t) i)*es;
+    if (f->prec == LUDWIG_GB_FP64) {
+      if (write) CK(cudaMemcpy(a, v + k, 8, cudaMemcpyHostToDevice), "site");
+      else CK(cudaMemcpy(v + k, a, 8, cudaMemcpyDeviceToHost), "site");
+    }
+    else {
+      float t = (float) v[k];
+      if (write) CK(cudaMemcpy(a, &t, 4, cudaMemcpyHostToDevice), "site");
+      else {
+	CK(cudaMemcpy(&t, a, 4, cudaMemcpyDeviceToHost), "site");
+	v[k] = t;
+      }
+    }
+  }
+  return LUDWIG_GB_OK;
+}
+
+int field_scalar(field_t * f, int index, double * phi) {
+  return field_site_rw(f, index, 0, 1, phi, 0);
+}
+
+int field_scalar_set(field_t * f, int index, double phi) {
+  return field_site_rw(f, index, 0, 1, &phi, 1);
+}
+
+int field_vector(field_t * f, int index, double p[3]) {
+  if (f && f->nf != 3) return err_set(LUDWIG_GB_EINVAL, "field_vector: nf 3");
+  return field_site_rw(f, index, 0, 3, p, 0);
+}
+
+int field_vector_set(field_t * f, int index, const double p[3]) {
+  if (f && f->nf != 3) return err_set(LUDWIG_GB_EINVAL, "field_vector: nf 3");
+  double v[3] = {p[0], p[1], p[2]};
+  return field_site_rw(f, index, 0, 3, v, 1);
+}
+
+/* Q from the 5 stored components XX, XY, XZ, YY, YZ (src/field.c) */
+int field_tensor(field_t * f, int index, double q[3][3]) {
+  if (f && f->nf != 5) return err_set(LUDWIG_GB_EINVAL, "field_tensor: nf 5");
+  double v[5];
+  int rc = field_site_rw(f, index, 0, 5, v, 0);
+  if (rc) return rc;
+  q[0][0] = v[0]; q[0][1] = v[1]; q[0][2] = v[2];
+  q[1][0] = q[0][1]; q[1][1] = v[3]; q[1][2] = v[4];
+  q[2][0] = q[0][2]; q[2][1] = q[1][2]; q[2][2] = 0.0 - q[0][0] - q[1][1];
+  return LUDWIG_GB_OK;
+}
+
+int field_tensor_set(field_t * f, int index, double q[3][3]) {
+  if (f && f->nf != 5) return err_set(LUDWIG_GB_EINVAL, "field_tensor: nf 5");
+  double v[5] = {q[0][0], q[0][1], q[0][2], q[1][1], q[1][2]};
+  return field_site_rw(f, index, 0, 5, v, 1);
+}
+
+int field_scalar_array(field_t * f, int index, double * array) {
+  return field_site_rw(f, index, 0, f ? f->nf : 0, array, 0);
+}
+
+int field_scalar_array_set(field_t * f, int index, const double * array) {
+  double v[5];
+  if (f == NULL || array == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  for (int k = 0; k < f->nf; k++) v[k] = array[k];
+  return field_site_rw(f, index, 0, f->nf, v, 1);
+}
+
+/*****************************************************************************
+ *  The reference's host layout: every cs_index() site, halo sites holding
+ *  the periodic images, AOS (a[K*index + k]) or SOA (a[nsites*k + index])
+ *  (src/memory.h:151-170, src/lb_data.h:144)
+ *****************************************************************************/
+
+/* out[layout(index, k)] = in[k][interior(index)] over all cs_index() sites
+ * (to = 1), or in the other direction over the interior sites (to = 0) */
+static int host_layout(const cs_t * cs, int model, int K, double * in,
+		       double * out, int to) {
+  if (model != DATA_MODEL_AOS && model != DATA_MODEL_SOA) {
+    return err_set(LUDWIG_GB_EINVAL, "data model: DATA_MODEL_AOS or "
+		   "DATA_MODEL_SOA");
+  }
+  const int h = cs->nhalo;
+  const int nall[3] = {cs->ntotal[0] + 2*h, cs->ntotal[1] + 2*h,
+		       cs->ntotal[2] + 2*h};
+  const long long nsites = (long long) nall[0]*nall[1]*nall[2];
+  const long long N = cs->d.nsites;
+  for (int x = 0; x < nall[0]; x++) {
+    int ix = ((x - h) % cs->ntotal[0] + cs->ntotal[0]) % cs->ntotal[0];
+    for (int y = 0; y < nall[1]; y++) {
+      int iy = ((y - h) % cs->ntotal[1] + cs->ntotal[1]) % cs->ntotal[1];
+      for (int z = 0; z < nall[2]; z++) {
+	int iz = ((z - h) % cs->ntotal[2] + cs->ntotal[2]) % cs->ntotal[2];
+	int interior = (x >= h && x < h + cs->ntotal[0] && y >= h &&
+			y < h + cs->ntotal[1] && z >= h &&
+			z < h + cs->ntotal[2]);
+	if (!to && !interior) continue;
+	long long index = ((long long) x*nall[1] + y)*nall[2] + z;
+	long long i = ((long long) ix*cs->ntotal[1] + iy)*cs->ntotal[2] + iz;
+	for (int k = 0; k < K; k++) {
+	  long long a = (model == DATA_MODEL_AOS) ? K*index + k
+	    : nsites*k + index;
+	  if (to) out[a] = in[k*N + i];
+	  else in[k*N + i] = out[a];
+	}
+      }
+    }
+  }
+  return LUDWIG_GB_OK;
+}
+
+static int host_tmp(long long n, double ** p) {
+  *p = (double *) malloc((size_t) n*sizeof(double));
+  return (*p == NULL) ? err_set(LUDWIG_GB_ENOMEM, "host buffer")
+    : LUDWIG_GB_OK;
+}
+
+int ludwig_gb_lb_to_host_cs(lb_t * lb, int model, double * f) {
+  if (lb == NULL || f == NULL) return err_set(LUDWIG_GB_EINVAL, "lb");
+  const long long N = lb->cs->d.nsites;
+  double * t = NULL;
+  int rc = host_tmp(NVEL*lb->ndist*N, &t);
+  if (rc == 0) rc = lb_f_to_host(lb, t);
+  if (rc == 0 && lb->ndist == 2) rc = lb_g_to_host(lb, t + NVEL*N);
+  if (rc == 0) rc = host_layout(lb->cs, model, NVEL*lb->ndist, t, f, 1);
+  free(t);
+  return rc;
+}
+
+int ludwig_gb_lb_from_host_cs(lb_t * lb, int model, const double * f) {
+  if (lb == NULL || f == NULL) return err_set(LUDWIG_GB_EINVAL, "lb");
+  const long long N = lb->cs->d.nsites;
+  double * t = NULL;
+  int rc = host_tmp(NVEL*lb->ndist*N, &t);
+  if (rc == 0) rc = host_layout(lb->cs, model, NVEL*lb->ndist, t,
+				(double *) f, 0);
+  if (rc == 0) rc = lb_f_from_host(lb, t);
+  if (rc == 0 && lb->ndist == 2) rc = lb_g_from_host(lb, t + NVEL*N);
+  free(t);
+  return rc;
+}
+
+int ludwig_gb_field_to_host_cs(field_t * obj, int model, double * data) {
+  if (obj == NULL || data == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  double * t = NULL;
+  int rc = host_tmp(obj->nf*obj->cs->d.nsites, &t);
+  if (rc == 0) rc = field_to_host(obj, t);
+  if (rc == 0) rc = host_layout(obj->cs, model, obj->nf, t, data, 1);
+  free(t);
+  return rc;
+}
+
+int ludwig_gb_field_from_host_cs(field_t * obj, int model,
+				 const double * data) {
+  if (obj == NULL || data == NULL) return err_set(LUDWIG_GB_EINVAL, "field");
+  double * t = NULL;
+  int rc = host_tmp(obj->nf*obj->cs->d.nsites, &t);
+  if (rc == 0) rc = host_layout(obj->cs, model, obj->nf, t, (double *) data,
+				0);
+  if (rc == 0) rc = field_from_host(obj, t);
+  free(t);
+  return rc;
+}
+
+int ludwig_gb_hydro_to_host_cs(hydro_t * obj, int model, double * rho,
+			       double * u, double * force) {
+  if (obj == NULL) return err_set(LUDWIG_GB_EINVAL, "hydro");
+  const long long N = obj->cs->d.nsites;
+  double * t = NULL;
+  int rc = host_tmp(7*N, &t);
+  if (rc == 0) rc = hydro_to_host(obj, t, t + N, t + 4*N);
+  if (rc == 0 && rho) rc = host_layout(obj->cs, model, 1, t, rho, 1);
+  if (rc == 0 && u) rc = host_layout(obj->cs, model, 3, t + N, u, 1);
+  if (rc == 0 && force) rc = host_layout(obj->cs, model, 3, t + 4*N, force,
+					 1);
+  free(t);
+  return rc;
 }
 
 int lgb_internal_err(int code, const char * what) {

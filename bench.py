@@ -36,7 +36,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIZE = (256, 256, 256)
-LEGS = ("fp32", "e2e", "fp16", "fp64", "dropin", "lc", "ens", "cnn", "cpu")
+LEGS = ("fp32", "e2e", "fp16", "fp64", "dropin", "lb2", "lc", "ens", "cnn",
+        "cpu")
 PARAMS = dict(a=-0.0625, b=0.0625, kappa=0.04, mobility=0.3, eta=0.1)
 SEED = 8361235
 METRIC = "D3Q19 binary-fluid MLUPS at 256^3, FP32-shifted (FP64 beside it)"
@@ -60,7 +61,12 @@ ALGO_BYTES = {"fp64": 368, "fp32": 184, "fp16": 108,
 # gradients, 5 Laplacians) + stress 272 + force 120 + upwind fluxes 224
 # (Q, u -> 20 fluxes) + molecular field 240 (Q, gradients -> H) +
 # Beris-Edwards 304 (u, 20 fluxes, H, Q r/w) + 24 + 360 = 1768.
-DROPIN_BYTES = {"dropin_binary64": 872, "dropin_lc64": 1768}
+DROPIN_BYTES = {"dropin_binary64": 872, "dropin_lc64": 1768,
+                # symmetric_lb (two distributions), one step of three
+                # kernels: phi from g (g 152 -> phi 8), gradients (phi 8 ->
+                # grad 24, delsq 8), collision pulling f and g (f, g 304,
+                # phi, grad, delsq 40 -> f, g 304, u 24) = 872
+                "lb2_64": 872}
 
 # DRAM bytes (read + write) per site of the fused kernels, from one ncu
 # capture each (binary fluid at 160^3, cholesteric at 128^3; the fused
@@ -87,6 +93,7 @@ LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",
            "fp16": "issue (same instructions as fp32 plus conversions; "
                    "108 B/site)",
            "lc64": "fp64 pipe",
+           "lb2_64": "fp64 pipe (two collisions a site, --fmad=false)",
            "lc32": "two kernels: fields + Beris-Edwards (issue and load "
                    "latency), force + collision (HBM, 2.5-D); the stress "
                    "(9 values a site) crosses HBM between them"}
@@ -407,6 +414,31 @@ def gpu_arm(args):
                         "lb_halo, lb_propagation, host wall time"}
         slc = None
 
+    # --- symmetric_lb (order parameter as a second distribution), FP64 ----
+    lb2 = None
+    if "lb2" in legs:
+        n2 = (128, 128, 128)
+        s2 = lg.BinaryFluidLB(n2, a=PARAMS["a"], b=PARAMS["b"],
+                              kappa=PARAMS["kappa"], mobility=0.45,
+                              eta=PARAMS["eta"])
+        s2.init_spinodal(SEED, 0.0, 0.02)
+        s2.step(3)
+        lg.sync()
+        k2 = 10
+        t0 = time.perf_counter()
+        s2.step(k2)
+        lg.sync()
+        dt = time.perf_counter() - t0
+        sites2 = 128 ** 3
+        lb2 = {"value": sites2 * k2 / dt / 1e6, "unit": "MLUPS", "steps": k2,
+               "ms_per_step": 1e3 * dt / k2,
+               "roofline": roofline("lb2_64", 1e3 * dt / k2, sites2, peak,
+                                    peak_kind),
+               "workload": "128^3 binary fluid with symmetric_lb (ndist=2, "
+                           "M=0.45), FP64 bit-exact, 3 kernels a step, host "
+                           "wall time"}
+        s2 = None
+
     # --- cholesteric LC (blue phase I), 128^3, FP32 and FP64 ------------
     lc = None
     if "lc" in legs:
@@ -573,6 +605,7 @@ def gpu_arm(args):
                  "roofline": roofline("fp16", ms16 / args.steps, nsites, peak,
                                       peak_kind)},
         "dropin": dropin,
+        "lb2": lb2,
         "lc": lc,
         "ensemble": ens,
         "corrector": cnn,

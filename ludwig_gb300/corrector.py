@@ -254,7 +254,6 @@ def bench(n, reps=20):
                        (2, "line_swizzled")):
         model.line_reuse(mode)
         res[name] = time_network(model, x, t, reps)
-    print(json.dumps(res))
     return res
 
 
@@ -285,7 +284,9 @@ def main(argv=None):
 
     load_library()
     if args.bench:
-        return bench(args.bench, args.reps)
+        res = bench(args.bench, args.reps)
+        print(json.dumps(res))
+        return res
     os.makedirs(args.out, exist_ok=True)
     logf = open(os.path.join(args.out, "log.txt"), "w")
 

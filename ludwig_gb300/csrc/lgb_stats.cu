@@ -9,8 +9,14 @@
  *
  *  Two passes, both deterministic: a fixed grid of LGBK_RED_BLOCKS blocks
  *  writes per-block partials to a scratch array, then one block combines
- *  them in block order.  Within a block, partials are combined through
- *  warp shuffles and shared memory in a fixed tree order.
+ *  them in a fixed order.  Each thread first sums its own sites (at most
+ *  ceil(n / 262144) of them, a grid-stride loop) in plain FP64 -- the
+ *  compensated sum costs a dozen FP64 operations a term, and FP64 is the
+ *  scarce pipe of this GPU -- then the per-thread sums are combined with
+ *  Klein's doubly compensated sum through warp shuffles, shared memory
+ *  and the final block, in a fixed tree order.  The rounding error is that
+ *  of at most 512 FP64 additions per thread at 512^3, far below the
+ *  relative 1e-13 the conservation checks resolve.
  *
  *****************************************************************************/
 
@@ -98,27 +104,53 @@ __device__ void write_partial(double * part, const Klein k[NK], double vmin,
   p[3*NK + 1] = vmax;
 }
 
+/* One block of RED_FINAL threads: thread t combines the partial records
+ * t, t + RED_FINAL, ... in that order, then the block combines the
+ * threads' sums (block_reduce, fixed tree order). */
+#define RED_FINAL 256
+
 template <int NK>
-__global__ void k_final(const double * __restrict__ part, int nblocks,
-			double * __restrict__ out) {
-  /* one warp; lane j < NK combines word j in block order */
-  Klein k;
-  k.zero();
+__global__ void __launch_bounds__(RED_FINAL)
+k_final(const double * __restrict__ part, int nblocks,
+	double * __restrict__ out) {
+  Klein k[NK];
+  #pragma unroll
+  for (int j = 0; j < NK; j++) k[j].zero();
   double vmin = +INFINITY, vmax = -INFINITY;
-  for (int b = 0; b < nblocks; b++) {
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
     const double * p = part + (size_t) b*(3*NK + 2);
-    if ((int) threadIdx.x < NK) {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) {
       Klein o;
-      o.sum = p[3*threadIdx.x]; o.cs = p[3*threadIdx.x + 1];
-      o.ccs = p[3*threadIdx.x + 2];
-      k.add(o);
+      o.sum = p[3*j]; o.cs = p[3*j + 1]; o.ccs = p[3*j + 2];
+      k[j].add(o);
     }
     vmin = fmin(vmin, p[3*NK]);
     vmax = fmax(vmax, p[3*NK + 1]);
   }
-  if ((int) threadIdx.x < NK) out[threadIdx.x] = k.total();
-  if (threadIdx.x == 0) { out[NK] = vmin; out[NK + 1] = vmax; }
+  block_reduce<NK>(k, vmin, vmax);
+  if (threadIdx.x == 0) {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) out[j] = k[j].total();
+    out[NK] = vmin;
+    out[NK + 1] = vmax;
+  }
 }
+
+/* A thread's own sums: plain FP64 over its sites, folded into Klein sums
+ * once at the end */
+template <int NK>
+struct Plain {
+  double v[NK];
+  __device__ __forceinline__ void zero() {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) v[j] = 0.0;
+  }
+  __device__ __forceinline__ void to(Klein k[NK]) const {
+    #pragma unroll
+    for (int j = 0; j < NK; j++) { k[j].zero(); k[j].add(v[j]); }
+  }
+};
 
 template <typename T>
 __device__ __forceinline__ double ldv(const T * p) { return (double) *p; }
@@ -127,17 +159,19 @@ __device__ __forceinline__ double ldv(const T * p) { return (double) *p; }
 template <typename T>
 __global__ void k_field_stats(long long n, const T * __restrict__ a,
 			      double * __restrict__ part) {
+  Plain<2> t;
   Klein k[2];
-  k[0].zero(); k[1].zero();
+  t.zero();
   double vmin = +INFINITY, vmax = -INFINITY;
   for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
        i += (long long) gridDim.x*blockDim.x) {
     double v = ldv(a + i);
-    k[0].add(v);
-    k[1].add(v*v);
+    t.v[0] += v;
+    t.v[1] += v*v;
     vmin = fmin(vmin, v);
     vmax = fmax(vmax, v);
   }
+  t.to(k);
   block_reduce<2>(k, vmin, vmax);
   if (threadIdx.x == 0) write_partial<2>(part, k, vmin, vmax);
 }
@@ -148,19 +182,20 @@ template <typename T, int NK>
 __global__ void k_masked_cols(long long n, const T * __restrict__ a,
 			      const uint8_t * __restrict__ st,
 			      double * __restrict__ part) {
+  Plain<NK> t;
   Klein k[NK];
-  #pragma unroll
-  for (int j = 0; j < NK; j++) k[j].zero();
+  t.zero();
   double vmin = +INFINITY, vmax = -INFINITY;
   for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
        i += (long long) gridDim.x*blockDim.x) {
     if (st && st[i] != 0) continue;
     #pragma unroll
-    for (int j = 0; j < NK; j++) k[j].add(ldv(a + j*n + i));
+    for (int j = 0; j < NK; j++) t.v[j] += ldv(a + j*n + i);
     double v = ldv(a + i);
     vmin = fmin(vmin, v);
     vmax = fmax(vmax, v);
   }
+  t.to(k);
   block_reduce<NK>(k, vmin, vmax);
   if (threadIdx.x == 0) write_partial<NK>(part, k, vmin, vmax);
 }
@@ -169,9 +204,9 @@ __global__ void k_masked_cols(long long n, const T * __restrict__ a,
 template <typename S>
 __global__ void k_dist_moments(long long n, const S * __restrict__ f,
 			       double rscale, double * __restrict__ part) {
+  Plain<4> t;
   Klein k[4];
-  #pragma unroll
-  for (int j = 0; j < 4; j++) k[j].zero();
+  t.zero();
   double vmin = +INFINITY, vmax = -INFINITY;
   for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
        i += (long long) gridDim.x*blockDim.x) {
@@ -188,10 +223,11 @@ __global__ void k_dist_moments(long long n, const S * __restrict__ f,
       jy += lgb_cv_c[p][1]*fp[p];
       jz += lgb_cv_c[p][2]*fp[p];
     }
-    k[0].add(m); k[1].add(jx); k[2].add(jy); k[3].add(jz);
+    t.v[0] += m; t.v[1] += jx; t.v[2] += jy; t.v[3] += jz;
     vmin = fmin(vmin, m);
     vmax = fmax(vmax, m);
   }
+  t.to(k);
   block_reduce<4>(k, vmin, vmax);
   if (threadIdx.x == 0) write_partial<4>(part, k, vmin, vmax);
 }
@@ -201,8 +237,9 @@ template <typename T>
 __global__ void k_symm_fed(lgbk_dims_t d, lgbk_symm_t fe,
 			   const T * __restrict__ phi,
 			   double * __restrict__ part) {
+  Plain<1> t;
   Klein k[1];
-  k[0].zero();
+  t.zero();
   double vmin = +INFINITY, vmax = -INFINITY;
   for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
        i < d.nsites; i += (long long) gridDim.x*blockDim.x) {
@@ -220,10 +257,11 @@ __global__ void k_symm_fed(lgbk_dims_t d, lgbk_symm_t fe,
     double p = ldv(phi + i);
     double fed = (0.5*fe.a + 0.25*fe.b*p*p)*p*p
       + 0.5*fe.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
-    k[0].add(fed);
+    t.v[0] += fed;
     vmin = fmin(vmin, fed);
     vmax = fmax(vmax, fed);
   }
+  t.to(k);
   block_reduce<1>(k, vmin, vmax);
   if (threadIdx.x == 0) write_partial<1>(part, k, vmin, vmax);
 }
@@ -233,8 +271,9 @@ __global__ void k_symm_fed_g(lgbk_dims_t d, lgbk_symm_t fe,
 			     const double * __restrict__ phi,
 			     const double * __restrict__ grad,
 			     double * __restrict__ part) {
+  Plain<1> t;
   Klein k[1];
-  k[0].zero();
+  t.zero();
   double vmin = +INFINITY, vmax = -INFINITY;
   const long long N = d.nsites;
   for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
@@ -243,10 +282,11 @@ __global__ void k_symm_fed_g(lgbk_dims_t d, lgbk_symm_t fe,
     const double p = phi[i];
     double fed = (0.5*fe.a + 0.25*fe.b*p*p)*p*p
       + 0.5*fe.kappa*(g[0]*g[0] + g[1]*g[1] + g[2]*g[2]);
-    k[0].add(fed);
+    t.v[0] += fed;
     vmin = fmin(vmin, fed);
     vmax = fmax(vmax, fed);
   }
+  t.to(k);
   block_reduce<1>(k, vmin, vmax);
   if (threadIdx.x == 0) write_partial<1>(part, k, vmin, vmax);
 }
@@ -257,10 +297,10 @@ static int finish(int nk, double * scratch, double * out_host,
 		  cudaStream_t s) {
   double * out = scratch + (size_t) LGBK_RED_BLOCKS*LGBK_RED_REC;
   switch (nk) {
-  case 1: k_final<1><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
-  case 2: k_final<2><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
-  case 3: k_final<3><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
-  default: k_final<4><<<1, 32, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  case 1: k_final<1><<<1, RED_FINAL, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  case 2: k_final<2><<<1, RED_FINAL, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  case 3: k_final<3><<<1, RED_FINAL, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
+  default: k_final<4><<<1, RED_FINAL, 0, s>>>(scratch, LGBK_RED_BLOCKS, out); break;
   }
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
@@ -464,7 +504,7 @@ extern "C" int ludwig_gb_field_stats_noalloc(const double * d_data,
     double * fin = part + (size_t) LGBK_RED_BLOCKS*NOALLOC_REC;
     k_field_stats<double><<<LGBK_RED_BLOCKS, RED_TPB, 0, s>>>(
       nsites, d_data + (size_t) n*nsites, part);
-    k_final<2><<<1, 32, 0, s>>>(part, LGBK_RED_BLOCKS, fin);
+    k_final<2><<<1, RED_FINAL, 0, s>>>(part, LGBK_RED_BLOCKS, fin);
     err = cudaGetLastError();
     if (err != cudaSuccess) return noalloc_cuda(err, "kernel launch");
     err = cudaMemcpyAsync(raw[n], fin, 4*sizeof(double),

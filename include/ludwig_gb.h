@@ -238,7 +238,8 @@ field_options_t field_options_default(void);
 field_options_t field_options_ndata_nhalo(int ndata, int nhalo);
 int field_create(pe_t * pe, cs_t * cs, lees_edw_t * le, const char * name,
 		 const field_options_t * opts, field_t ** pobj);
-/* field_create with an arithmetic and storage precision (FP64 or FP32) */
+/* field_create with the precision of the state it belongs to (FP64; FP32
+ * and FP16 states keep their fields in float) */
 int ludwig_gb_field_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
 			   const char * name, const field_options_t * opts,
 			   int precision, field_t ** pobj);
@@ -301,7 +302,8 @@ hydro_options_t hydro_options_default(void);
 hydro_options_t hydro_options_nhalo(int nhalo);
 int hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
 		 const hydro_options_t * opts, hydro_t ** pobj);
-/* hydro_create with an arithmetic and storage precision (FP64 or FP32) */
+/* hydro_create with the precision of the state it belongs to (FP64; FP32
+ * and FP16 states keep rho, u and the force in float) */
 int ludwig_gb_hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
 			   const hydro_options_t * opts, int precision,
 			   hydro_t ** pobj);

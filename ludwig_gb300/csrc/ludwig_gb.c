@@ -664,8 +664,8 @@ int ludwig_gb_field_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
   if (opts->ndata < 1 || opts->ndata > 5) {
     return err_set(LUDWIG_GB_EINVAL, "field_create: ndata in 1..5");
   }
-  if (precision != LUDWIG_GB_FP64 && precision != LUDWIG_GB_FP32) {
-    return err_set(LUDWIG_GB_EINVAL, "field_create: FP64 or FP32");
+  if (precision < LUDWIG_GB_FP64 || precision > LUDWIG_GB_FP16) {
+    return err_set(LUDWIG_GB_EINVAL, "field_create: precision");
   }
   int rc = lib_init();
   if (rc) return rc;
@@ -986,8 +986,8 @@ int ludwig_gb_hydro_create(pe_t * pe, cs_t * cs, lees_edw_t * le,
   if (cs == NULL || !cs->initialised || pobj == NULL) {
     return err_set(LUDWIG_GB_EINVAL, "hydro_create");
   }
-  if (precision != LUDWIG_GB_FP64 && precision != LUDWIG_GB_FP32) {
-    return err_set(LUDWIG_GB_EINVAL, "hydro_create: FP64 or FP32");
+  if (precision < LUDWIG_GB_FP64 || precision > LUDWIG_GB_FP16) {
+    return err_set(LUDWIG_GB_EINVAL, "hydro_create: precision");
   }
   hydro_options_t o = opts ? *opts : hydro_options_default();
   int rc = lib_init();

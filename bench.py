@@ -301,6 +301,7 @@ def gpu_arm(args):
     import ludwig_gb300 as lg
     lg.load_library()
     lg.PE(local)                      # select the device for this rank
+    lg.tune_sites(args.sites)
     nsites = SIZE[0] * SIZE[1] * SIZE[2]
     peak, peak_kind = measured_peaks()
 
@@ -636,6 +637,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256,
                     help="lattice edge (default 256; smaller for profiling)")
+    ap.add_argument("--sites", type=int, default=2, choices=[1, 2],
+                    help="sites per thread of the float fused step")
     ap.add_argument("--legs", default=",".join(LEGS),
                     help="comma list of %s" % ",".join(LEGS))
     args = ap.parse_args()

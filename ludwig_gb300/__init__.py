@@ -151,6 +151,7 @@ def _declare(L):
         "ludwig_gb_stream": ([], _P),
         "ludwig_gb_sync": ([], ctypes.c_int),
         "ludwig_gb_tune_set": ([ctypes.c_int] * 3, ctypes.c_int),
+        "ludwig_gb_tune_sites": ([ctypes.c_int], ctypes.c_int),
         "pe_create": ([ctypes.c_int, pp], ctypes.c_int),
         "pe_free": ([_P], ctypes.c_int),
         "cs_create": ([_P, pp], ctypes.c_int),
@@ -910,6 +911,12 @@ def advection_order(n):
 def tune(xchunk, tile_y, min_blocks=0):
     _check(lib().ludwig_gb_tune_set(int(xchunk), int(tile_y),
                                     int(min_blocks)), "tune")
+
+
+def tune_sites(sites_per_thread):
+    """Sites per thread of the float fused step: 2 (packed FP32x2, the
+    default) or 1."""
+    _check(lib().ludwig_gb_tune_sites(int(sites_per_thread)), "tune_sites")
 
 
 class PinnedState:

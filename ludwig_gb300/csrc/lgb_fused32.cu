@@ -12,6 +12,7 @@
  *****************************************************************************/
 
 #include "lgb_fused.cuh"
+#include "lgb_fused2.cuh"
 
 extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
 				    const lgbk_binary_args_t * a, int xchunk,
@@ -45,13 +46,48 @@ static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
   return (int) cudaGetLastError();
 }
 
+/* Two sites per thread (packed FP32x2): TYT x 32 threads, tiles of 2 TYT
+ * rows, MINB resident CTAs per SM */
+template <typename S, int TYT, int MINB>
+static int launch32_two(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
+			int xchunk, cudaStream_t stream) {
+  auto kern = k_binary_fused2<S, TYT, MINB>;
+  size_t smem = FusedSmem<float, 2*TYT>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TYT, smem);
+  if (occ < 1) occ = 1;
+
+  int ntz = (d->nz + 31)/32, nty = (d->ny + 2*TYT - 1)/(2*TYT);
+  long long grid = (long long) nsm*occ;
+  xchunk = lgbk_auto_xchunk(xchunk, d->nx, ntz*nty, grid);
+  long long items = (long long) ntz*nty*((d->nx + xchunk - 1)/xchunk);
+  if (grid > items) grid = items;
+
+  kern<<<(unsigned int) grid, dim3(32, TYT), smem, stream>>>(*d, *a, xchunk);
+  return (int) cudaGetLastError();
+}
+
 /* Tile height and resident CTAs per SM (register cap 65536/(32*TY*MINB)):
  * (8,4) and (16,2) and (4,8) cap at 64 registers, (8,3) at 85, (8,2) at 128.
  * minb = 0 picks the default for the tile height. */
 template <typename S>
 static int dispatch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
-		      int xchunk, int ty, int minb, cudaStream_t s) {
+		      int xchunk, int ty, int minb, int sites,
+		      cudaStream_t s) {
   const bool m = (a->status != NULL);
+  if (sites == 2 && !m) {
+    /* tile rows 8 (4 thread rows) or 16 (8 thread rows) */
+    if (ty == 16) return launch32_two<S, 8, 2>(d, a, xchunk, s);
+    if (minb == 2) return launch32_two<S, 4, 2>(d, a, xchunk, s);
+    if (minb == 4) return launch32_two<S, 4, 4>(d, a, xchunk, s);
+    return launch32_two<S, 4, 3>(d, a, xchunk, s);
+  }
   if (ty == 4) {
     return m ? launch32<S, true, 4, 8>(d, a, xchunk, s)
              : launch32<S, false, 4, 8>(d, a, xchunk, s);
@@ -74,7 +110,7 @@ static int dispatch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
 
 extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 				const lgbk_binary_args_t * a, int xchunk,
-				int ty, int minb, void * stream) {
+				int ty, int minb, int sites, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
   if (ty <= 0) ty = 8;
   if (d->nsites >= LGBK_MAX_SITES) return (int) cudaErrorInvalidValue;
@@ -83,10 +119,10 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
     return lgbk_binary_step_f64(d, a, xchunk, ty, stream);
   case LGBK_PREC_FP32:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<float>(d, a, xchunk, ty, minb, s);
+    return dispatch32<float>(d, a, xchunk, ty, minb, sites, s);
   case LGBK_PREC_FP16:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<__half>(d, a, xchunk, ty, minb, s);
+    return dispatch32<__half>(d, a, xchunk, ty, minb, sites, s);
   default:
     return (int) cudaErrorInvalidValue;
   }
@@ -120,10 +156,41 @@ static int launch_ens32(const lgbk_box_t * boxes, const void * items,
   return (int) cudaGetLastError();
 }
 
+template <typename S, int TYT, int MINB>
+static int launch_ens32_two(const lgbk_box_t * boxes, const void * items,
+			    int nitems, int xchunk, cudaStream_t stream) {
+  auto kern = k_binary_ensemble2<S, TYT, MINB>;
+  size_t smem = FusedSmem<float, 2*TYT>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TYT, smem);
+  if (occ < 1) occ = 1;
+  long long grid = (long long) nsm*occ;
+  if (grid > nitems) grid = nitems;
+  if (grid < 1) return 0;
+  kern<<<(unsigned int) grid, dim3(32, TYT), smem, stream>>>(
+    boxes, (const int2 *) items, nitems, xchunk);
+  return (int) cudaGetLastError();
+}
+
+/* tile rows ty: 8 and 16 with two sites per thread (sites = 2, no map),
+ * otherwise one */
 template <typename S>
 static int dispatch_ens32(const lgbk_box_t * b, const void * it, int n,
-			  int xchunk, int ty, int minb, int m,
+			  int xchunk, int ty, int minb, int m, int sites,
 			  cudaStream_t s) {
+  if (sites == 2 && !m && ty == 16) {
+    return launch_ens32_two<S, 8, 2>(b, it, n, xchunk, s);
+  }
+  if (sites == 2 && !m && ty == 8) {
+    if (minb == 4) return launch_ens32_two<S, 4, 4>(b, it, n, xchunk, s);
+    if (minb == 2) return launch_ens32_two<S, 4, 2>(b, it, n, xchunk, s);
+    return launch_ens32_two<S, 4, 3>(b, it, n, xchunk, s);
+  }
   if (ty == 4) {
     return m ? launch_ens32<S, true, 4, 8>(b, it, n, xchunk, s)
              : launch_ens32<S, false, 4, 8>(b, it, n, xchunk, s);
@@ -142,7 +209,7 @@ static int dispatch_ens32(const lgbk_box_t * b, const void * it, int n,
 
 extern "C" int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes,
 				  const void * items, int nitems, int xchunk,
-				  int ty, int minb, int has_map,
+				  int ty, int minb, int has_map, int sites,
 				  void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
   switch (prec) {
@@ -151,10 +218,10 @@ extern "C" int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes,
 				  stream);
   case LGBK_PREC_FP32:
     return dispatch_ens32<float>(boxes, items, nitems, xchunk, ty, minb,
-				 has_map, s);
+				 has_map, sites, s);
   case LGBK_PREC_FP16:
     return dispatch_ens32<__half>(boxes, items, nitems, xchunk, ty, minb,
-				  has_map, s);
+				  has_map, sites, s);
   default:
     return (int) cudaErrorInvalidValue;
   }

@@ -154,14 +154,16 @@ typedef struct lgbk_box_s {
  * built for tile height ty and xchunk by lgbk_ensemble_items(). */
 int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes_dev,
 		       const void * items_dev, int nitems, int xchunk, int ty,
-		       int minb, int has_map, void * stream);
+		       int minb, int has_map, int sites, void * stream);
 /* Number of work items of one box (and fill items if non-NULL, host) */
 int lgbk_ensemble_items(const lgbk_dims_t * d, int box, int xchunk, int ty,
 			int * items);
 
+/* sites = 2: two sites per thread in packed FP32x2 (float forms without a
+ * status map); otherwise one */
 int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 		     const lgbk_binary_args_t * a, int xchunk, int ty, int minb,
-		     void * stream);
+		     int sites, void * stream);
 
 /* Conversions between FP64 canonical state and reduced storage */
 int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,

@@ -73,6 +73,7 @@ static double * red_scratch_ = NULL;
 static int tune_xchunk_ = 0;         /* 0: balanced shares of the planes */
 static int tune_ty_ = 8;
 static int tune_minb_ = 3;
+static int tune_sites_ = 2;          /* sites per thread, float forms */
 static int advection_order_ = 1;
 
 /* src/advection.c:82: order of the advective fluxes of the per-function
@@ -122,6 +123,14 @@ int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks) {
   tune_xchunk_ = xchunk;
   tune_ty_ = tile_y;
   tune_minb_ = min_blocks;
+  return LUDWIG_GB_OK;
+}
+
+int ludwig_gb_tune_sites(int sites_per_thread) {
+  if (sites_per_thread != 1 && sites_per_thread != 2) {
+    return err_set(LUDWIG_GB_EINVAL, "tune_sites: 1 or 2");
+  }
+  tune_sites_ = sites_per_thread;
   return LUDWIG_GB_OK;
 }
 
@@ -2464,7 +2473,7 @@ int lb_propagation(lb_t * lb) {
 typedef struct graph_cache_s {
   lgbk_binary_args_t args;     /* arguments of the first step of the pair */
   int prec;
-  int xchunk, ty, minb;
+  int xchunk, ty, minb, sites;
   lgbk_dims_t d;
   cudaGraphExec_t exec;
   int valid;
@@ -2533,6 +2542,7 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
     graph_cache_t * g = gcache_ + i;
     if (g->valid && g->prec == prec && g->xchunk == tune_xchunk_ &&
 	g->ty == tune_ty_ && g->minb == tune_minb_ &&
+	g->sites == tune_sites_ &&
 	memcmp(&g->d, d, sizeof(*d)) == 0 &&
 	memcmp(&g->args, a, sizeof(*a)) == 0) {
       *exec = g->exec;
@@ -2554,8 +2564,8 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed),
      "BeginCapture");
-  int rc1 = lgbk_binary_step(d, prec, a, tune_xchunk_, tune_ty_, tune_minb_, stream_);
-  int rc2 = lgbk_binary_step(d, prec, &b, tune_xchunk_, tune_ty_, tune_minb_, stream_);
+  int rc1 = lgbk_binary_step(d, prec, a, tune_xchunk_, tune_ty_, tune_minb_, tune_sites_, stream_);
+  int rc2 = lgbk_binary_step(d, prec, &b, tune_xchunk_, tune_ty_, tune_minb_, tune_sites_, stream_);
   int rc3 = cudaStreamEndCapture(stream_, &graph);
   if (rc1 || rc2 || rc3) {
     return cuda_check(rc1 ? rc1 : (rc2 ? rc2 : rc3), "graph capture");
@@ -2569,6 +2579,7 @@ static int pair_graph(const lgbk_binary_args_t * a, int prec,
   slot->xchunk = tune_xchunk_;
   slot->ty = tune_ty_;
   slot->minb = tune_minb_;
+  slot->sites = tune_sites_;
   slot->valid = 1;
   *exec = slot->exec;
   return LUDWIG_GB_OK;
@@ -2594,7 +2605,7 @@ int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
     }
   }
   if (nsteps % 2) {
-    CK(lgbk_binary_step(d, lb->prec, &a, tune_xchunk_, tune_ty_, tune_minb_,
+    CK(lgbk_binary_step(d, lb->prec, &a, tune_xchunk_, tune_ty_, tune_minb_, tune_sites_,
 			 stream_),
        "binary_step");
     binary_swap(lb, phi, hydro);
@@ -2899,7 +2910,7 @@ int ludwig_gb_time_binary_e2e_overlap(lb_t * lb, field_t * phi,
     /* step */
     if (rc == 0) rc = cudaStreamWaitEvent(st[1], ev[0][x], 0);
     if (rc == 0) rc = lgbk_binary_step(d, lb->prec, ax, tune_xchunk_, tune_ty_,
-				       tune_minb_, st[1]);
+				       tune_minb_, tune_sites_, st[1]);
     if (rc == 0) rc = cudaEventRecord(ev[1][x], st[1]);
     /* download */
     if (rc == 0) rc = cudaStreamWaitEvent(st[2], ev[1][x], 0);
@@ -3213,7 +3224,8 @@ int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
 
 static int ens_launch(ludwig_gb_ensemble_t * e, int k) {
   return lgbk_ensemble_step(e->prec, e->boxes_d[k], e->items_d, e->nitems,
-			    e->xchunk, e->ty, e->minb, 0, stream_);
+			    e->xchunk, e->ty, e->minb, 0, tune_sites_,
+			    stream_);
 }
 
 static int ens_step_async(ludwig_gb_ensemble_t * e, int nsteps) {

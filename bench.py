@@ -90,8 +90,9 @@ LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",
            "dropin_lc64": "one kernel per reference function, FP64; "
                           "intermediates through HBM",
            "fp64": "fp64 pipe (83.5% active at 160^3, ncu)",
-           "fp16": "issue (same instructions as fp32 plus conversions; "
-                   "108 B/site)",
+           "fp16": "two sites per thread in packed FP32x2, next plane's "
+                   "populations prefetched; issue and dependency waits at "
+                   "12 warps per SM (108 B/site)",
            "lc64": "fp64 pipe",
            "lb2_64": "fp64 pipe (two collisions a site, --fmad=false)",
            "lc32": "two kernels: fields + Beris-Edwards (issue and load "
@@ -637,8 +638,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256,
                     help="lattice edge (default 256; smaller for profiling)")
-    ap.add_argument("--sites", type=int, default=2, choices=[1, 2],
-                    help="sites per thread of the float fused step")
+    ap.add_argument("--sites", type=int, default=0, choices=[0, 1, 2],
+                    help="sites per thread of the float fused step (0: the "
+                    "faster form of each precision)")
     ap.add_argument("--legs", default=",".join(LEGS),
                     help="comma list of %s" % ",".join(LEGS))
     args = ap.parse_args()

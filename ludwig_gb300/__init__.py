@@ -914,8 +914,8 @@ def tune(xchunk, tile_y, min_blocks=0):
 
 
 def tune_sites(sites_per_thread):
-    """Sites per thread of the float fused step: 2 (packed FP32x2, the
-    default) or 1."""
+    """Sites per thread of the float fused step: 2 (packed FP32x2), 1, or
+    0 (the default: 2 for FP16 storage, 1 for FP32)."""
     _check(lib().ludwig_gb_tune_sites(int(sites_per_thread)), "tune_sites")
 
 

@@ -259,15 +259,16 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
 
   const vf2 half(0.5f), zero(0.0f);
 
-  for (int x = x0; x < xe; x++) {
+  /* Pulled populations f_p(x - c_p) of both sites, as stored (raw); the
+   * loads of plane x + 1 are issued before plane x is computed, so that
+   * they are in flight through the whole of its arithmetic. */
+  S fr[LGB_NVEL][2];
+  auto issue_pull = [&](int x) {
     const unsigned xs = (unsigned) x*NP;
     const unsigned sA = xs + syzA, sB = xs + syzB;
     const unsigned oxp = (x == 0) ? (unsigned) (d.nx - 1)*NP : 0u - NP;
     const unsigned oxm = (x == d.nx - 1) ? 0u - (unsigned) (d.nx - 1)*NP
       : (unsigned) NP;
-
-    /* pulled populations of both sites, issued first */
-    vf2 fs[LGB_NVEL];
     Unroll<LGB_NVEL>::run([&](auto P) {
       constexpr int p = decltype(P)::value;
       unsigned offx = 0, offz = 0;
@@ -279,9 +280,25 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
       if (Cv<p>::Y == +1) { offA += (unsigned) oypA; offB += (unsigned) oypB; }
       if (Cv<p>::Y == -1) { offA += (unsigned) oymA; offB += (unsigned) oymB; }
       const S * fp = f_in + p*N;
-      fs[p] = vf2(FStore2<S>::ld(fp + (sA + offA), rfscale),
-		  FStore2<S>::ld(fp + (sB + offB), rfscale));
+      fr[p][0] = fp[sA + offA];
+      fr[p][1] = fp[sB + offB];
     });
+  };
+  issue_pull(x0);
+
+  for (int x = x0; x < xe; x++) {
+    const unsigned xs = (unsigned) x*NP;
+    const unsigned sA = xs + syzA, sB = xs + syzB;
+    const unsigned oxm = (x == d.nx - 1) ? 0u - (unsigned) (d.nx - 1)*NP
+      : (unsigned) NP;
+
+    vf2 fs[LGB_NVEL];
+    #pragma unroll
+    for (int p = 0; p < LGB_NVEL; p++) {
+      fs[p] = vf2(FStore<S, float>::ld(&fr[p][0], rfscale),
+		  FStore<S, float>::ld(&fr[p][1], rfscale));
+    }
+    if (x + 1 < xe) issue_pull(x + 1);
 
     __pipeline_wait_prior(0);
     __syncthreads();

@@ -119,10 +119,12 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
     return lgbk_binary_step_f64(d, a, xchunk, ty, stream);
   case LGBK_PREC_FP32:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<float>(d, a, xchunk, ty, minb, sites, s);
+    return dispatch32<float>(d, a, xchunk, ty, minb, (sites == 2) ? 2 : 1,
+			     s);
   case LGBK_PREC_FP16:
     if (!a->cp.ghosts_zero) return (int) cudaErrorInvalidValue;
-    return dispatch32<__half>(d, a, xchunk, ty, minb, sites, s);
+    return dispatch32<__half>(d, a, xchunk, ty, minb, (sites == 1) ? 1 : 2,
+			      s);
   default:
     return (int) cudaErrorInvalidValue;
   }
@@ -218,10 +220,10 @@ extern "C" int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes,
 				  stream);
   case LGBK_PREC_FP32:
     return dispatch_ens32<float>(boxes, items, nitems, xchunk, ty, minb,
-				 has_map, sites, s);
+				 has_map, (sites == 2) ? 2 : 1, s);
   case LGBK_PREC_FP16:
     return dispatch_ens32<__half>(boxes, items, nitems, xchunk, ty, minb,
-				  has_map, sites, s);
+				  has_map, (sites == 1) ? 1 : 2, s);
   default:
     return (int) cudaErrorInvalidValue;
   }

@@ -73,7 +73,8 @@ static double * red_scratch_ = NULL;
 static int tune_xchunk_ = 0;         /* 0: balanced shares of the planes */
 static int tune_ty_ = 8;
 static int tune_minb_ = 3;
-static int tune_sites_ = 2;          /* sites per thread, float forms */
+static int tune_sites_ = 0;          /* sites per thread, float forms;
+					0: two for FP16 storage, one for FP32 */
 static int advection_order_ = 1;
 
 /* src/advection.c:82: order of the advective fluxes of the per-function
@@ -127,8 +128,8 @@ int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks) {
 }
 
 int ludwig_gb_tune_sites(int sites_per_thread) {
-  if (sites_per_thread != 1 && sites_per_thread != 2) {
-    return err_set(LUDWIG_GB_EINVAL, "tune_sites: 1 or 2");
+  if (sites_per_thread < 0 || sites_per_thread > 2) {
+    return err_set(LUDWIG_GB_EINVAL, "tune_sites: 0 (by form), 1 or 2");
   }
   tune_sites_ = sites_per_thread;
   return LUDWIG_GB_OK;

@@ -28,7 +28,7 @@ def run(gb, L, prec, nsteps, sites, xchunk=0, ty=8, minb=0, seed=8361235):
         s.step(nsteps)
         return s.state()
     finally:
-        gb.tune_sites(2)
+        gb.tune_sites(0)
         gb.tune(0, 8, 3)
 
 

@@ -32,30 +32,13 @@
 #include "lgb_fused.cuh"
 #include "lgb_vf2.cuh"
 
-/* The stored distributions of two sites to and from a vf2: float as it
- * is; half converted lane by lane, with the storage scale applied to both
- * lanes by one packed multiplication */
+/* Per-lane typed load/store of the stored distributions */
 template <typename S> struct FStore2 {
-  static __device__ __forceinline__ vf2 ld(S a, S b, const vf2 &) {
-    return vf2((float) a, (float) b);
+  static __device__ __forceinline__ float ld(const S * p, float rs) {
+    return FStore<S, float>::ld(p, rs);
   }
-  static __device__ __forceinline__ vf2 scaled(const vf2 & v, const vf2 &) {
-    return v;
-  }
-  static __device__ __forceinline__ void st(S * p, float v) { *p = (S) v; }
-};
-
-template <> struct FStore2<__half> {
-  static __device__ __forceinline__ vf2 ld(__half a, __half b,
-					   const vf2 & rscale) {
-    return vf2(__half2float(a), __half2float(b))*rscale;
-  }
-  static __device__ __forceinline__ vf2 scaled(const vf2 & v,
-					       const vf2 & scale) {
-    return v*scale;
-  }
-  static __device__ __forceinline__ void st(__half * p, float v) {
-    *p = __float2half_rn(v);
+  static __device__ __forceinline__ void st(S * p, float v, float s) {
+    FStore<S, float>::st(p, v, s);
   }
 };
 
@@ -126,7 +109,6 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
   const float pb_s = a.pf[LGBK_P_B];
   const float kappa_s = a.pf[LGBK_P_KAPPA];
   const vf2 mobility(mobility_s), pa(pa_s), pb(pb_s), kappa(kappa_s);
-  const vf2 vfscale(fscale), vrfscale(rfscale);
 
   /* own sites in the D/u planes (rows 2 ty + 1, 2 ty + 2 with the halo)
    * and in the phi planes (rows 2 ty + 2, 2 ty + 3) */
@@ -313,7 +295,8 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
     vf2 fs[LGB_NVEL];
     #pragma unroll
     for (int p = 0; p < LGB_NVEL; p++) {
-      fs[p] = FStore2<S>::ld(fr[p][0], fr[p][1], vrfscale);
+      fs[p] = vf2(FStore<S, float>::ld(&fr[p][0], rfscale),
+		  FStore<S, float>::ld(&fr[p][1], rfscale));
     }
     if (x + 1 < xe) issue_pull(x + 1);
 
@@ -417,17 +400,13 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
     lgb_collide_site<vf2, false, true, true>(
       vf2(a.pf[LGBK_P_RTAU_SHEAR]), vf2(a.pf[LGBK_P_RTAU_BULK]),
       a.cp.rtau_ghost, vf2(rho0), fs, ftot, rho, uu);
-    #pragma unroll
-    for (int p = 0; p < LGB_NVEL; p++) {
-      fs[p] = FStore2<S>::scaled(fs[p], vfscale);
-    }
 
     if (actA) {
       phi_out[sA] = phinew.v.x;
       rho_out[sA] = rho.v.x;
       #pragma unroll
       for (int p = 0; p < LGB_NVEL; p++) {
-	FStore2<S>::st(f_out + p*N + sA, fs[p].v.x);
+	FStore2<S>::st(f_out + p*N + sA, fs[p].v.x, fscale);
       }
       #pragma unroll
       for (int ia = 0; ia < 3; ia++) (u_out + ia*N)[sA] = uu[ia].v.x;
@@ -441,7 +420,7 @@ binary_item2(const lgbk_dims_t & d, const lgbk_binary_args_t & a, int itz,
       rho_out[sB] = rho.v.y;
       #pragma unroll
       for (int p = 0; p < LGB_NVEL; p++) {
-	FStore2<S>::st(f_out + p*N + sB, fs[p].v.y);
+	FStore2<S>::st(f_out + p*N + sB, fs[p].v.y, fscale);
       }
       #pragma unroll
       for (int ia = 0; ia < 3; ia++) (u_out + ia*N)[sB] = uu[ia].v.y;

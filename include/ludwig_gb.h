@@ -64,7 +64,8 @@ const char * ludwig_gb_version(void);
 typedef enum ludwig_gb_prec_e {
   LUDWIG_GB_FP64 = 0,        /* double; the drop-in, reference-exact */
   LUDWIG_GB_FP32 = 1,        /* float; f stored as f - w_p rho0 */
-  LUDWIG_GB_FP16 = 2         /* float arithmetic; (f - w_p rho0)*scale as half */
+  LUDWIG_GB_FP16 = 2         /* float arithmetic; (f - w_p rho0)*scale as
+				half, the scale derived from the range */
 } ludwig_gb_prec_t;
 
 /* Opaque objects (names as in the reference) */
@@ -578,8 +579,16 @@ int phi_cahn_hilliard(phi_ch_t * pch, fe_t * fe, field_t * phi,
  *-------------------------------------------------------------------------*/
 int ludwig_gb_binary_step(lb_t * lb, field_t * phi, hydro_t * hydro,
 			  map_t * map, fe_t * fe, int nsteps);
-/* As above without synchronising: the steps are queued on the library's
- * stream; ludwig_gb_sync() waits for them. */
+/* FP16 storage keeps f - w_p rho0 times a power-of-two scale derived from
+ * the field's range: the largest deviation maps into [2^10, 2^11), room to
+ * grow 32-fold before half precision's largest value.  The scale is derived when f
+ * is set from the host (lb_f_from_host), again every 256 steps of
+ * ludwig_gb_binary_step, and on this call, which requantises the stored
+ * values (scale: the new value, may be NULL; no-op for FP32 and FP64). */
+int ludwig_gb_lb_fp16_rescale(lb_t * lb, double * scale);
+/* As ludwig_gb_binary_step without synchronising (and without the FP16
+ * rescaling): the steps are queued on the library's stream;
+ * ludwig_gb_sync() waits for them. */
 int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
 				map_t * map, fe_t * fe, int nsteps);
 int ludwig_gb_sync(void);

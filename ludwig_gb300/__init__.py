@@ -152,6 +152,7 @@ def _declare(L):
         "ludwig_gb_sync": ([], ctypes.c_int),
         "ludwig_gb_tune_set": ([ctypes.c_int] * 3, ctypes.c_int),
         "ludwig_gb_tune_sites": ([ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_lb_fp16_rescale": ([_P, _D], ctypes.c_int),
         "pe_create": ([ctypes.c_int, pp], ctypes.c_int),
         "pe_free": ([_P], ctypes.c_int),
         "cs_create": ([_P, pp], ctypes.c_int),
@@ -520,6 +521,14 @@ class LB(_Obj):
 
     def propagation(self):
         _check(lib().lb_propagation(self.ptr), "lb_propagation")
+
+    def fp16_rescale(self):
+        """Derive the FP16 storage scale from the range of the stored
+        deviations (returns the scale; 1 for FP32/FP64)."""
+        sc = ctypes.c_double()
+        _check(lib().ludwig_gb_lb_fp16_rescale(self.ptr, ctypes.byref(sc)),
+               "fp16_rescale")
+        return sc.value
 
     def moments(self):
         out = np.zeros(4)

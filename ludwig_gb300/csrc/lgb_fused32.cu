@@ -11,6 +11,8 @@
  *
  *****************************************************************************/
 
+#include <cstring>
+
 #include "lgb_fused.cuh"
 #include "lgb_fused2.cuh"
 
@@ -352,5 +354,60 @@ extern "C" int lgbk_propagate_store(const lgbk_dims_t * d, int prec, int dir,
     k_propagate_store<__half><<<g256(d->nsites), 256, 0, s>>>(
       *d, dir, (const __half *) f, (__half *) fprime);
   }
+  return (int) cudaGetLastError();
+}
+
+/*****************************************************************************
+ *
+ *  FP16 storage scale: the largest stored magnitude, and a rescaling of the
+ *  stored values by a power of two (exact unless a value leaves the range
+ *  of half precision).
+ *
+ *****************************************************************************/
+
+__global__ void k_half_absmax(long long n, const __half * __restrict__ a,
+			      unsigned int * __restrict__ out) {
+  float m = 0.0f;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
+       i += (long long) gridDim.x*blockDim.x) {
+    m = fmaxf(m, fabsf(__half2float(a[i])));
+  }
+  #pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+  }
+  /* non-negative floats order as their bit patterns */
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void k_half_scale(long long n, __half * __restrict__ a,
+			     float factor) {
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < n;
+       i += (long long) gridDim.x*blockDim.x) {
+    a[i] = __float2half_rn(__half2float(a[i])*factor);
+  }
+}
+
+extern "C" int lgbk_half_absmax(long long n, const void * a,
+				unsigned int * dev_word, float * host_max,
+				void * stream) {
+  cudaStream_t s = (cudaStream_t) stream;
+  cudaError_t err = cudaMemsetAsync(dev_word, 0, sizeof(unsigned int), s);
+  if (err != cudaSuccess) return (int) err;
+  k_half_absmax<<<1024, 256, 0, s>>>(n, (const __half *) a, dev_word);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return (int) err;
+  unsigned int w = 0;
+  err = cudaMemcpyAsync(&w, dev_word, sizeof(w), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return (int) err;
+  memcpy(host_max, &w, sizeof(float));
+  return 0;
+}
+
+extern "C" int lgbk_half_scale(long long n, void * a, float factor,
+			       void * stream) {
+  k_half_scale<<<1024, 256, 0, (cudaStream_t) stream>>>(n, (__half *) a,
+							factor);
   return (int) cudaGetLastError();
 }

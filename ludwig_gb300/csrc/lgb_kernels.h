@@ -165,6 +165,12 @@ int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 		     const lgbk_binary_args_t * a, int xchunk, int ty, int minb,
 		     int sites, void * stream);
 
+/* FP16 storage: largest stored magnitude (dev_word: one device word of
+ * scratch) and rescaling of n stored values by factor */
+int lgbk_half_absmax(long long n, const void * a, unsigned int * dev_word,
+		     float * host_max, void * stream);
+int lgbk_half_scale(long long n, void * a, float factor, void * stream);
+
 /* Conversions between FP64 canonical state and reduced storage */
 int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,
 		      double shift_rho0, double scale, const double * src,

@@ -73,6 +73,7 @@ static double * red_scratch_ = NULL;
 static int tune_xchunk_ = 0;         /* 0: balanced shares of the planes */
 static int tune_ty_ = 8;
 static int tune_minb_ = 3;
+#define LGB_FP16_RESCALE_STEPS 256
 static int tune_sites_ = 0;          /* sites per thread, float forms;
 					0: two for FP16 storage, one for FP32 */
 static int advection_order_ = 1;
@@ -367,7 +368,8 @@ struct lb_data_s {
   cs_t * cs;
   int prec;
   lb_relaxation_enum_t nrelax;
-  double fscale;
+  double fscale;                /* FP16 storage: f - w_p rho0 scaled by it */
+  int fp16_since;               /* steps since the scale was last derived */
   double rho0;                 /* shift of the reduced-precision storage */
   void * f;
   void * fprime;
@@ -594,6 +596,22 @@ int lb_f_to_host(lb_t * lb, double * fh) {
   return LUDWIG_GB_OK;
 }
 
+/* FP16 storage scale for deviations of magnitude up to maxdev: the power of
+ * two that maps maxdev into [2^10, 2^11) (room for the deviations to grow
+ * 32-fold before half precision's largest value, 65504, between two
+ * derivations; the relative precision of half does not depend on the
+ * scale, which only keeps the values out of the subnormal range), between
+ * 1 and 2^24; 0 if maxdev is zero (keep the scale) */
+static double fp16_scale_for(double maxdev) {
+  if (!(maxdev > 0.0) || !isfinite(maxdev)) return 0.0;
+  int e = 0;
+  (void) frexp(2048.0/maxdev, &e);             /* 2048/maxdev in [2^(e-1), 2^e) */
+  double sc = ldexp(1.0, e - 1);
+  if (sc < 1.0) sc = 1.0;
+  if (sc > 16777216.0) sc = 16777216.0;
+  return sc;
+}
+
 int lb_f_from_host(lb_t * lb, const double * fh) {
   if (lb == NULL || fh == NULL) return err_set(LUDWIG_GB_EINVAL, "lb_f");
   if (lb->ndist == 2) {
@@ -607,6 +625,22 @@ int lb_f_from_host(lb_t * lb, const double * fh) {
 		       stream_), "lb_f_from_host");
   }
   else {
+    if (lb->prec == LUDWIG_GB_FP16) {
+      /* the storage scale from the range of the deviations handed over */
+      static const int w36[NVEL] = {12, 1, 1, 2, 1, 1, 1, 2, 1, 2, 2, 1, 2,
+				    1, 1, 1, 2, 1, 1};
+      double m = 0.0;
+      for (int p = 0; p < NVEL; p++) {
+	const double w = lb->rho0*((double) w36[p]/36.0);
+	const double * fp = fh + (size_t) p*d->nsites;
+	for (long long i = 0; i < d->nsites; i++) {
+	  m = fmax(m, fabs(fp[i] - w));
+	}
+      }
+      double sc = fp16_scale_for(m);
+      if (sc > 0.0) lb->fscale = sc;
+      lb->fp16_since = 0;
+    }
     double * tmp = NULL;
     int rc = dev_alloc((void **) &tmp, n*sizeof(double), "convert");
     if (rc) return rc;
@@ -2614,8 +2648,57 @@ int ludwig_gb_binary_step_async(lb_t * lb, field_t * phi, hydro_t * hydro,
   return LUDWIG_GB_OK;
 }
 
+/* Derive the FP16 storage scale of lb from the range of its stored
+ * deviations and requantise them (a power-of-two factor: exact unless a
+ * value leaves half precision's range).  No-op for other precisions. */
+int ludwig_gb_lb_fp16_rescale(lb_t * lb, double * scale) {
+  if (lb == NULL) return err_set(LUDWIG_GB_EINVAL, "fp16_rescale: lb NULL");
+  if (lb->prec != LUDWIG_GB_FP16) {
+    if (scale) *scale = 1.0;
+    return LUDWIG_GB_OK;
+  }
+  const long long n = NVEL*lb->cs->d.nsites;
+  unsigned int * word = NULL;
+  int rc = dev_alloc((void **) &word, sizeof(unsigned int), "absmax");
+  if (rc) return rc;
+  float mstored = 0.0f;
+  rc = lgbk_half_absmax(n, lb->f, word, &mstored, stream_);
+  dev_free(word);
+  if (rc) return cuda_check(rc, "fp16_rescale");
+  if (!isfinite(mstored)) {
+    return err_set(LUDWIG_GB_ENOTFINITE, "fp16_rescale: stored values not "
+		   "finite");
+  }
+  const double sc = fp16_scale_for((double) mstored/lb->fscale);
+  if (sc > 0.0 && sc != lb->fscale) {
+    CK(lgbk_half_scale(n, lb->f, (float) (sc/lb->fscale), stream_),
+       "fp16_rescale");
+    CK(cudaStreamSynchronize(stream_), "sync");
+    lb->fscale = sc;
+  }
+  lb->fp16_since = 0;
+  if (scale) *scale = lb->fscale;
+  return LUDWIG_GB_OK;
+}
+
 int ludwig_gb_binary_step(lb_t * lb, field_t * phi, hydro_t * hydro,
 			  map_t * map, fe_t * fe, int nsteps) {
+  if (lb != NULL && lb->prec == LUDWIG_GB_FP16 && nsteps > 0) {
+    /* FP16 storage: the scale is derived again from the range every
+     * LGB_FP16_RESCALE_STEPS steps */
+    while (nsteps > 0) {
+      int k = LGB_FP16_RESCALE_STEPS - lb->fp16_since;
+      if (k > nsteps) k = nsteps;
+      int rc = ludwig_gb_binary_step_async(lb, phi, hydro, map, fe, k);
+      if (rc) return rc;
+      nsteps -= k;
+      lb->fp16_since += k;
+      if (lb->fp16_since >= LGB_FP16_RESCALE_STEPS) {
+	if ((rc = ludwig_gb_lb_fp16_rescale(lb, NULL))) return rc;
+      }
+    }
+    return ludwig_gb_sync();
+  }
   int rc = ludwig_gb_binary_step_async(lb, phi, hydro, map, fe, nsteps);
   if (rc) return rc;
   return ludwig_gb_sync();

@@ -108,3 +108,30 @@ def test_reduced_with_solid_sites_close_to_fp64(gb, prec, tol_phi, tol_f):
     # solid sites keep their phi
     solid = status == 1
     assert np.array_equal(pb[0][solid], phi0[0][solid])
+
+
+def test_fp16_scale_derived_from_the_range(gb):
+    """FP16 storage: the scale maps the largest stored deviation into
+    [2^10, 2^11), is a power of two, is derived again by the stepping and
+    on request, and requantising by it leaves the trajectory close to the
+    FP32 one."""
+    L = (24, 20, 16)
+    s16 = gb.BinaryFluid(L, precision=2, mobility=MOB, eta=ETA)
+    s32 = gb.BinaryFluid(L, precision=1, mobility=MOB, eta=ETA)
+    for s in (s16, s32):
+        s.phi.init_spinodal(8361235, 0.0, 0.02)
+        s.step(300)                 # crosses one derivation at step 256
+    sc = s16.lb.fp16_rescale()
+    assert sc == 2.0 ** round(np.log2(sc))
+    f = s16.lb.get()
+    w = np.array([12, 1, 1, 2, 1, 1, 1, 2, 1, 2, 2, 1, 2, 1, 1, 1, 2, 1, 1],
+                 dtype=float) / 36.0
+    dev = np.abs(f - w[:, None, None, None]).max()
+    assert 2.0 ** 10 <= dev * sc < 2.0 ** 11 * (1 + 1e-3)
+    assert s16.lb.fp16_rescale() == sc          # idempotent
+    s16.step(100)
+    s32.step(100)
+    assert np.abs(s16.phi.get() - s32.phi.get()).max() < 1e-4
+    # handing f over from the host derives the scale from its range
+    s16.lb.set(f)
+    assert s16.lb.fp16_rescale() == sc

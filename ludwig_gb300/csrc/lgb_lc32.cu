@@ -8,6 +8,7 @@
  *****************************************************************************/
 
 #include "lgb_lc32.cuh"
+#include "lgb_lc32_2.cuh"
 
 /* Tile of the force + collision kernel and resident CTAs per SM */
 #define LC32_TY 8
@@ -37,6 +38,29 @@ static int launch_collide(const lgbk_dims_t * d, const lgbk_lc_step_args_t * a,
   return (int) cudaGetLastError();
 }
 
+/* The same with two sites per thread (tiles of 2 TYT rows) */
+template <typename S, int TYT, int MINB>
+static int launch_collide2(const lgbk_dims_t * d,
+			   const lgbk_lc_step_args_t * a, cudaStream_t s) {
+  auto kern = k_lc32_collide2<S, TYT, MINB>;
+  const size_t smem = LcCollideSmem<2*TYT>::bytes();
+  cudaError_t err = cudaFuncSetAttribute(kern,
+    cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (err != cudaSuccess) return (int) err;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32*TYT, smem);
+  if (occ < 1) occ = 1;
+  const int ntz = (d->nz + 31)/32, nty = (d->ny + 2*TYT - 1)/(2*TYT);
+  long long grid = (long long) nsm*occ;
+  const int xchunk = lgbk_auto_xchunk(0, d->nx, ntz*nty, grid, 3);
+  const long long items = (long long) ntz*nty*((d->nx + xchunk - 1)/xchunk);
+  if (grid > items) grid = items;
+  kern<<<(unsigned int) grid, dim3(32, TYT), smem, s>>>(*d, *a, xchunk);
+  return (int) cudaGetLastError();
+}
+
 template <typename S>
 static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
 		     const lgbk_lc_step_args_t * a, cudaStream_t s) {
@@ -59,8 +83,10 @@ static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
   }
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
-  return a->status ? launch_collide<S, true>(d, a, s)
-		   : launch_collide<S, false>(d, a, s);
+  if (a->status) return launch_collide<S, true>(d, a, s);
+  /* two sites per thread unless one is asked for */
+  if (a->sites != 1) return launch_collide2<S, 4, 3>(d, a, s);
+  return launch_collide<S, false>(d, a, s);
 }
 
 extern "C" int lgbk_lc_step(const lgbk_dims_t * d, int prec,

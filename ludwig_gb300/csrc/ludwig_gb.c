@@ -2194,6 +2194,7 @@ static int lc_step_async(lb_t * lb, field_t * q, hydro_t * hydro,
   a.gamma_rot = be->param.gamma;
   a.rho0 = lb->rho0;
   a.fscale = lb->fscale;
+  a.sites = tune_sites_;
   a.rho_out = hydro->rho;
   a.pth = be->flux;                                /* 9 N elements */
   a.h = (const char *) be->flux + 9*N*es;          /* 5 N elements */

@@ -53,3 +53,21 @@ def test_two_sites_independent_of_tiling(gb, prec):
         got = run(gb, L, prec, 9, 2, xchunk, ty, minb)
         for k in ("phi", "u", "rho", "f"):
             assert np.array_equal(got[k], ref[k]), (xchunk, ty, minb, k)
+
+
+@pytest.mark.parametrize("L", [(16, 16, 32), (12, 10, 40)])
+def test_lc_two_site_collision_matches_one_site(gb, L):
+    """The float LC step with the two-site force + collision kernel against
+    the one-site kernel: same arithmetic, float rounding apart."""
+    out = {}
+    for sites in (1, 2):
+        gb.tune_sites(sites)
+        try:
+            s = gb.LiquidCrystal(L, precision=1)
+            s.init_o8m()
+            s.step(20)
+            out[sites] = s.state()
+        finally:
+            gb.tune_sites(0)
+    for k in ("q", "u", "rho", "f"):
+        assert np.abs(out[2][k] - out[1][k]).max() < 1e-6, k

@@ -598,12 +598,13 @@ void * ludwig_gb_stream(void);
  * share of the (tile, plane) pairs per resident CTA), tile height (4, 8,
  * 16) and resident CTAs per SM for tile height 8 (2..4; 0 = default). */
 int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks);
-/* Sites per thread of the float forms of the fused step: 2 (two rows of
+/* Sites per thread of the float forms of the fused steps: 2 (two rows of
  * the tile per thread, packed FP32x2 arithmetic, the pulled populations of
  * the next plane loaded while the current one is computed; the tile then
- * has tile_y rows in tile_y/2 thread rows), 1, or 0 (the default: 2 for
- * FP16 storage, 1 for FP32, the faster form of each on GB300).  A status
- * map with solid sites always uses 1. */
+ * has tile_y rows in tile_y/2 thread rows), 1, or 0 (the default: the
+ * faster form of each on GB300: 2 for the binary fluid with FP16 storage,
+ * 1 for it in FP32 and for the cholesteric's force + collision kernel).
+ * A status map with solid sites always uses 1. */
 int ludwig_gb_tune_sites(int sites_per_thread);
 
 /*---------------------------------------------------------------------------

@@ -50,8 +50,8 @@ typedef struct lgbk_lc_step_args_s {
   double xi, gamma_rot, rho0, fscale;
   lgbk_collide_t cp;
   float fp[LGBK_LCF_N];                     /* filled by lgbk_lc_args_pack */
-  int sites;          /* float forms: sites per thread of the collision
-			 kernel (2, 1; 0: by form) */
+  int sites;          /* float forms: 2 for the two-site collision
+			 kernel, otherwise one site per thread */
 } lgbk_lc_step_args_t;
 
 static inline void lgbk_lc_args_pack(lgbk_lc_step_args_t * a) {

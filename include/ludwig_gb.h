@@ -128,6 +128,19 @@ int physics_eta_bulk_set(physics_t * phys, double zeta);
 int physics_mobility_set(physics_t * phys, double mobility);
 int physics_fbody_set(physics_t * phys, const double f[3]);
 int physics_ref(physics_t ** ref);
+/* Frequency of the external electric field (src/physics.h:30,47): with a
+ * frequency f the LC free energy's field carries the phase
+ * coswt = cos(2 pi f t) at the current time t, evaluated before every use
+ * of its parameters (fe_lc_param_commit, src/blue_phase.c:210-226) */
+int physics_e0_frequency_set(physics_t * phys, double e0_frequency);
+int physics_e0_frequency(physics_t * phys, double * e0_frequency);
+/* Time step control, src/physics.c:600-668: a run of nstep steps from
+ * nstart; next_step advances the counter (positive while steps remain),
+ * time is t_start + t_current - 1 in lattice units */
+int physics_control_init_time(physics_t * phys, int nstart, int nstep);
+int physics_control_next_step(physics_t * phys);
+int physics_control_timestep(physics_t * phys);
+int physics_control_time(physics_t * phys, double * t);
 
 /*---------------------------------------------------------------------------
  * Distributions: src/lb_data.h:30-47,162-171 (D3Q19, ndist = 1)
@@ -531,9 +544,11 @@ int beris_edw_update(beris_edw_t * be, fe_t * fe, field_t * fq,
 int beris_edw_h_to_host(beris_edw_t * be, double * h);
 
 /* Fused GB300 step of the cholesteric: nsteps iterations of the main loop
- * of src/ludwig.c:528-860 (q gradients, molecular field and chiral stress,
- * stress-divergence force, Beris-Edwards update with upwind fluxes,
- * collision, streaming) in two kernel launches per step.  FP64 objects
+ * of src/ludwig.c:528-860 (the physics object's step counter advanced,
+ * q gradients, molecular field and chiral stress, stress-divergence force,
+ * Beris-Edwards update with upwind fluxes, collision, streaming) in two
+ * kernel launches per step; a time-dependent field's phase is taken at
+ * each step's time.  FP64 objects
  * give the results of the functions above called one by one; FP32 objects
  * (lb, q, hydro) run the same step in float arithmetic. */
 int ludwig_gb_lc_step(lb_t * lb, field_t * q, hydro_t * hydro, map_t * map,

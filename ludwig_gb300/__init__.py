@@ -167,6 +167,12 @@ def _declare(L):
         "physics_eta_bulk_set": ([_P, ctypes.c_double], ctypes.c_int),
         "physics_mobility_set": ([_P, ctypes.c_double], ctypes.c_int),
         "physics_fbody_set": ([_P, _D3], ctypes.c_int),
+        "physics_e0_frequency_set": ([_P, ctypes.c_double], ctypes.c_int),
+        "physics_control_init_time": ([_P, ctypes.c_int, ctypes.c_int],
+                                      ctypes.c_int),
+        "physics_control_next_step": ([_P], ctypes.c_int),
+        "physics_control_timestep": ([_P], ctypes.c_int),
+        "physics_control_time": ([_P, _D], ctypes.c_int),
         "lb_data_create": ([_P, _P, ctypes.POINTER(LbDataOptions), pp],
                            ctypes.c_int),
         "ludwig_gb_lb_data_create": ([_P, _P, ctypes.POINTER(LbDataOptions),

@@ -318,6 +318,10 @@ struct physics_s {
   double eta_bulk;
   double mobility;
   double fbody[3];
+  double e0_frequency;          /* frequency of the external electric field */
+  int t_start;                  /* time step control, src/physics.c:600-668 */
+  int nsteps;
+  int t_current;
 };
 
 static physics_t * phys_ref_ = NULL;
@@ -343,6 +347,47 @@ int physics_free(physics_t * phys) {
 }
 
 int physics_ref(physics_t ** ref) { *ref = phys_ref_; return LUDWIG_GB_OK; }
+
+int physics_e0_frequency_set(physics_t * p, double f) {
+  if (p == NULL) return err_set(LUDWIG_GB_EINVAL, "physics");
+  p->e0_frequency = f;
+  return LUDWIG_GB_OK;
+}
+
+int physics_e0_frequency(physics_t * p, double * f) {
+  if (p == NULL || f == NULL) return err_set(LUDWIG_GB_EINVAL, "physics");
+  *f = p->e0_frequency;
+  return LUDWIG_GB_OK;
+}
+
+/* src/physics.c:658-668 */
+int physics_control_init_time(physics_t * p, int nstart, int nstep) {
+  if (p == NULL) return err_set(LUDWIG_GB_EINVAL, "physics");
+  p->t_start = nstart;
+  p->nsteps = nstep;
+  p->t_current = nstart;
+  return LUDWIG_GB_OK;
+}
+
+/* src/physics.c:641-647: advance the step counter; positive while steps
+ * of the run remain */
+int physics_control_next_step(physics_t * p) {
+  if (p == NULL) return 0;
+  p->t_current += 1;
+  return p->t_start + p->nsteps - p->t_current + 1;
+}
+
+int physics_control_timestep(physics_t * p) {
+  return (p == NULL) ? 0 : p->t_current;
+}
+
+/* src/physics.c:622-630: the time in lattice units, 1.0 in the first
+ * iteration of a run started at 0 */
+int physics_control_time(physics_t * p, double * t) {
+  if (p == NULL || t == NULL) return err_set(LUDWIG_GB_EINVAL, "physics");
+  *t = 1.0*(p->t_start + p->t_current - 1.0);
+  return LUDWIG_GB_OK;
+}
 int physics_rho0_set(physics_t * p, double v) { p->rho0 = v; return 0; }
 int physics_eta_shear_set(physics_t * p, double v) { p->eta_shear = v; return 0; }
 int physics_eta_bulk_set(physics_t * p, double v) { p->eta_bulk = v; return 0; }
@@ -1479,7 +1524,20 @@ struct fe_lc_s {
   field_grad_t * dq;
 };
 
-static void lc_kparam(const fe_lc_t * fe, lgbk_lc_t * k) {
+/* The phase of a time-dependent electric field, as fe_lc_param_commit
+ * (src/blue_phase.c:210-226) sets it before every use of the parameters:
+ * coswt = cos(2 pi f t) at the physics object's current time; a static
+ * field (frequency zero) keeps the parameter block's value. */
+static void lc_commit_field(fe_lc_t * fe) {
+  if (phys_ref_ == NULL || phys_ref_->e0_frequency == 0.0) return;
+  const double pi = 4.0*atan(1.0);
+  double t = 0.0;
+  physics_control_time(phys_ref_, &t);
+  fe->param.coswt = cos(2.0*pi*phys_ref_->e0_frequency*t);
+}
+
+static void lc_kparam(fe_lc_t * fe, lgbk_lc_t * k) {
+  lc_commit_field(fe);
   memset(k, 0, sizeof(*k));
   k->a0 = fe->param.a0;
   k->q0 = fe->param.q0;
@@ -2200,6 +2258,13 @@ static int lc_step_async(lb_t * lb, field_t * q, hydro_t * hydro,
   a.h = (const char *) be->flux + 9*N*es;          /* 5 N elements */
   lgbk_lc_args_pack(&a);
   for (int n = 0; n < nsteps; n++) {
+    /* one iteration of the main loop: the step counter first
+     * (src/ludwig.c:528), then a time-dependent field's phase at the new
+     * time (fe_lc_param_commit, src/blue_phase.c:210) */
+    if (phys_ref_ != NULL) physics_control_next_step(phys_ref_);
+    if (phys_ref_ != NULL && phys_ref_->e0_frequency != 0.0) {
+      lc_kparam(lc, &k);
+    }
     a.f_in = lb->f;   a.f_out = lb->fprime;
     a.q_in = q->data; a.q_out = q->data2;
     a.u_in = hydro->u; a.u_out = hydro->u2;

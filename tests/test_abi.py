@@ -154,3 +154,23 @@ def test_cs_index_numbering_without_device(gb):
             assert tuple(c3) == (ic, jc, kc)
     finally:
         L.cs_free(cs)
+
+
+def test_physics_time_control_without_device(gb):
+    """physics_control_* as src/physics.c:600-668: next_step advances the
+    counter and stays positive while steps of the run remain; the time is
+    t_start + t_current - 1."""
+    L = gb.lib()
+    ph = ctypes.c_void_p()
+    assert L.physics_create(None, ctypes.byref(ph)) == 0
+    try:
+        assert L.physics_control_init_time(ph, 10, 3) == 0
+        t = ctypes.c_double()
+        left = [L.physics_control_next_step(ph) for _ in range(4)]
+        assert left == [3, 2, 1, 0]
+        assert L.physics_control_timestep(ph) == 14
+        assert L.physics_control_time(ph, ctypes.byref(t)) == 0
+        assert t.value == 10 + 14 - 1.0
+        assert L.physics_e0_frequency_set(ph, 0.25) == 0
+    finally:
+        L.physics_free(ph)

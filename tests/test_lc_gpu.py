@@ -1,6 +1,7 @@
 """Parity of the CUDA liquid-crystal path (FP64) with the oracle and with
 golden fixtures made by the reference itself: every value exact."""
 
+import ctypes
 import os
 
 import numpy as np
@@ -160,3 +161,52 @@ def test_lc_fp32_ragged_lattice_close_to_fp64(gb):
     assert np.abs(qa - qb).max() < 1e-5 * np.abs(qa).max()
     ua, ub = a.state()["u"], b.state()["u"]
     assert np.abs(ua - ub).max() < 1e-3 * np.abs(ua).max()
+
+
+def test_lc_time_dependent_field(gb):
+    """A time-dependent electric field (src/blue_phase.c:210-226): the phase
+    coswt = cos(2 pi f t) at the physics object's time, taken before each
+    step.  The fused step (which advances the step counter itself) equals
+    the per-function calls with physics_control_next_step before each
+    step, and both equal a static field whose phase is set by hand to
+    cos(2 pi f t_n), t_n = t_start + n - 1 (src/physics.c:622-630)."""
+    import math
+    L, freq, nsteps = (12, 10, 8), 0.013, 6
+    kw = dict(eta=0.5, gamma_rot=0.5, epsilon=0.7, e0=(0.01, -0.02, 0.005))
+    lib = gb.lib()
+    fused = gb.LiquidCrystal(L, **kw)
+    calls = gb.LiquidCrystal(L, **kw)
+    manual = gb.LiquidCrystal(L, **kw)
+    for s in (fused, calls, manual):
+        s.init_o8m()
+        lib.physics_control_init_time(s.phys.ptr, 0, nsteps)
+    for s in (fused, calls):
+        lib.physics_e0_frequency_set(s.phys.ptr, freq)
+
+    lib.ludwig_gb_physics_use(fused.phys.ptr)
+    fused.step(nsteps)
+    assert lib.physics_control_timestep(fused.phys.ptr) == nsteps
+
+    lib.ludwig_gb_physics_use(calls.phys.ptr)
+    for _ in range(nsteps):
+        lib.physics_control_next_step(calls.phys.ptr)
+        calls.step_reference_order(1)
+
+    lib.ludwig_gb_physics_use(manual.phys.ptr)
+    p = manual.fe.param
+    for n in range(1, nsteps + 1):
+        p.coswt = math.cos(2.0 * math.pi * freq * (0 + n - 1.0))
+        gb._check(lib.fe_lc_param_set(manual.fe.ptr, ctypes.byref(p)),
+                  "fe_lc_param_set")
+        manual.step(1)
+
+    a, b, c = fused.state(), calls.state(), manual.state()
+    for k in ("q", "u", "rho", "f"):
+        assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(a[k], c[k]), k
+    # and the field did act: a static field gives another trajectory
+    static = gb.LiquidCrystal(L, **kw)
+    static.init_o8m()
+    lib.ludwig_gb_physics_use(static.phys.ptr)
+    static.step(nsteps)
+    assert not np.array_equal(static.q.get(), a["q"])

@@ -89,6 +89,48 @@ def make_pairs(nfine, seeds, t_first, t_gap, npairs, params=FINE_PARAMS,
     return X, Y
 
 
+def make_rollout_pairs(model, nfine, seeds, t_first, t_gap, nstarts, depth,
+                       params=FINE_PARAMS, log=None):
+    """Pairs along the corrected coarse run itself ("pushforward"): from
+    each restricted fine state the coarse lattice takes `depth` steps,
+    corrected by the current network after each but the last; step j's
+    fields are paired with the restricted fine state 4 j fine steps after
+    the start.  The network then learns to correct the states its own
+    rollout reaches, error included, toward the fine trajectory (pairs of
+    depth 1 are those of make_pairs).  Returns (X, Y) as make_pairs."""
+    torch = _torch()
+    nc = tuple(n // 2 for n in nfine)
+    Nc = nc[0] * nc[1] * nc[2]
+    P = len(seeds) * nstarts * depth
+    X = torch.empty((P, 5, Nc), dtype=torch.float32, device="cuda")
+    Y = torch.empty((P, 5, Nc), dtype=torch.float32, device="cuda")
+    coarse = BinaryFluid(nc, FP32, **coarse_params(params))
+    i = 0
+    for seed in seeds:
+        t0 = time.time()
+        fine = _fine(nfine, seed, params)
+        fine.step(t_first)
+        for k in range(nstarts):
+            coarse_restrict(fine, coarse)
+            for j in range(depth):
+                fine.step(4)
+                fields_restrict(fine, Y[i].data_ptr(), nc)
+                coarse.step(1)
+                fields_pack(coarse, X[i].data_ptr())
+                if j + 1 < depth:
+                    sync()
+                    model.correct(coarse)
+                i += 1
+            if k + 1 < nstarts:
+                fine.step(t_gap - 4 * depth)
+        sync()
+        del fine
+        if log:
+            log("rollout pairs: seed %d done (%.1f s)"
+                % (seed, time.time() - t0))
+    return X, Y
+
+
 def scales_from(X, Y):
     """Feature normalisation and target scales from the data."""
     x = X.double()
@@ -276,6 +318,14 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--rollout", type=int, default=250)
     ap.add_argument("--every", type=int, default=25)
+    ap.add_argument("--pushforward", type=int, default=0,
+                    help="after the first training, pairs along the "
+                    "corrected coarse run of this depth (coarse steps), "
+                    "then training on them (0: none)")
+    ap.add_argument("--pf-starts", type=int, default=4,
+                    help="rollout starts per seed for the pushforward pairs")
+    ap.add_argument("--pf-rounds", type=int, default=1)
+    ap.add_argument("--pf-epochs", type=int, default=4)
     ap.add_argument("--out", default="corrector_out")
     ap.add_argument("--bench", type=int, default=0,
                     help="only time the network on a BENCH^3 coarse lattice")
@@ -295,6 +345,9 @@ def main(argv=None):
         logf.write(msg + "\n")
         logf.flush()
 
+    if 4 * args.pushforward > args.t_gap:
+        ap.error("--pushforward %d needs --t-gap >= %d"
+                 % (args.pushforward, 4 * args.pushforward))
     nfine = (args.fine,) * 3
     nc = tuple(n // 2 for n in nfine)
     seeds = [1000 + s for s in range(args.seeds)]
@@ -316,6 +369,20 @@ def main(argv=None):
     timing = time_network(model, X[0], T[0])
     log("timing %s" % json.dumps(timing))
     del X, Y, T
+    pf_hist = []
+    for rnd in range(args.pushforward and args.pf_rounds):
+        # rollout stability: train on the states the corrected rollout
+        # reaches (scales kept from the first data set)
+        t = time.time()
+        Xr, Yr = make_rollout_pairs(model, nfine, seeds, args.t_first,
+                                    args.t_gap, args.pf_starts,
+                                    args.pushforward, log=log)
+        Tr = targets(Xr, Yr, osc)
+        pf_hist.append(train(model, Xr, Tr, args.pf_epochs, args.lr * 0.3,
+                             seed=1 + rnd, log=log))
+        sync()
+        log("pushforward round %d: %.1f s" % (rnd, time.time() - t))
+        del Xr, Yr, Tr
     hb = hc = None
     if hold:
         Xh, Yh = make_pairs(nfine, hold, args.t_first, args.t_gap,
@@ -333,7 +400,9 @@ def main(argv=None):
            args.pairs, "seeds": len(seeds), "holdout_seeds": hold,
            "epochs": args.epochs, "data_s": t_data, "train_s": t_train,
            "train_steps": args.epochs * len(seeds) * args.pairs,
-           "loss_history": hist,
+           "loss_history": hist, "pushforward_depth": args.pushforward,
+           "pushforward_rounds": args.pushforward and args.pf_rounds,
+           "pushforward_loss_history": pf_hist,
            "one_step_train": {"plain": base1, "corrected": corr1,
                               "initial_network": corr0},
            "one_step_holdout": {"plain": hb, "corrected": hc},

@@ -254,3 +254,31 @@ def test_rollout_and_fallback(trained):
     method, worst = cr.choose_method(recs)
     assert method in ("coarse+corrector", "fine")
     assert (method == "fine") == (worst > 0.02)
+
+
+def test_rollout_pairs(trained, gb):
+    """Pushforward pairs: depth 1 gives the one-step pairs bit for bit;
+    at depth 2 the second input is one coarse step from the corrected
+    first, and its target is the restricted fine state 8 fine steps on."""
+    cr, m, _, _ = trained
+    nfine, nc = (64, 64, 64), (32, 32, 32)
+    X1, Y1 = cr.make_pairs(nfine, [21], 800, 100, 2)
+    Xr, Yr = cr.make_rollout_pairs(m, nfine, [21], 800, 100, 2, 1)
+    assert torch.equal(X1, Xr) and torch.equal(Y1, Yr)
+
+    X2, Y2 = cr.make_rollout_pairs(m, nfine, [21], 800, 100, 1, 2)
+    assert torch.equal(X2[0], X1[0]) and torch.equal(Y2[0], Y1[0])
+    fine = cr._fine(nfine, 21, cr.FINE_PARAMS)
+    fine.step(800)
+    coarse = gb.BinaryFluid(nc, gb.FP32, **cr.coarse_params(cr.FINE_PARAMS))
+    gb.coarse_restrict(fine, coarse)
+    coarse.step(1)
+    m.correct(coarse)
+    coarse.step(1)
+    fine.step(8)
+    x = torch.empty_like(X2[1])
+    y = torch.empty_like(Y2[1])
+    gb.fields_pack(coarse, x.data_ptr())
+    gb.fields_restrict(fine, y.data_ptr(), nc)
+    gb.sync()
+    assert torch.equal(x, X2[1]) and torch.equal(y, Y2[1])

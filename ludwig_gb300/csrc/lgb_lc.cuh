@@ -23,6 +23,7 @@
 
 #include "lgb_common.cuh"
 #include "lgb_lc.h"
+#include "lgb_vf2.cuh"
 
 /* Levi-Civita symbol as a compile-time value */
 LGB_HD constexpr int lgb_eps(int a, int b, int c) {
@@ -339,13 +340,25 @@ __device__ __forceinline__ void lc_stress_site(const P & p,
  *
  *****************************************************************************/
 
-struct LcFast {
-  float q[3][3], dq[3][3][3];
-  float R[3][3], QQ[3][3], v[3];
-  float q2, fed;
+template <typename T>
+struct LcFastT {
+  T q[3][3], dq[3][3][3];
+  T R[3][3], QQ[3][3], v[3];
+  T q2, fed;
 };
+using LcFast = LcFastT<float>;
 
-__device__ __forceinline__ void lc_fast_prepare(LcFast & w) {
+/* a*b + c: fused for float (fmaf), one packed FMA for a pair of sites */
+__device__ __forceinline__ float lc_fma(float a, float b, float c) {
+  return fmaf(a, b, c);
+}
+__device__ __forceinline__ vf2 lc_fma(const vf2 & a, const vf2 & b,
+				      const vf2 & c) {
+  return a*b + c;
+}
+
+template <typename T>
+__device__ __forceinline__ void lc_fast_prepare(LcFastT<T> & w) {
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
@@ -355,20 +368,20 @@ __device__ __forceinline__ void lc_fast_prepare(LcFast & w) {
       w.R[a][b] = w.dq[c][b][d] - w.dq[d][b][c];
     }
   }
-  float q2 = 0.0f;
+  T q2(0.0f);
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
-    for (int b = 0; b < 3; b++) q2 = fmaf(w.q[a][b], w.q[a][b], q2);
+    for (int b = 0; b < 3; b++) q2 = lc_fma(w.q[a][b], w.q[a][b], q2);
   }
   w.q2 = q2;
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = a; b < 3; b++) {
-      float t = 0.0f;
+      T t(0.0f);
       #pragma unroll
-      for (int c = 0; c < 3; c++) t = fmaf(w.q[a][c], w.q[b][c], t);
+      for (int c = 0; c < 3; c++) t = lc_fma(w.q[a][c], w.q[b][c], t);
       w.QQ[a][b] = t;
       w.QQ[b][a] = t;
     }
@@ -380,24 +393,24 @@ __device__ __forceinline__ void lc_fast_prepare(LcFast & w) {
 }
 
 /* Free-energy density (src/blue_phase.c:309-400) */
-template <typename P>
-__device__ __forceinline__ float lc_fast_fed(const P & p, const LcFast & w) {
+template <typename T, typename P>
+__device__ __forceinline__ T lc_fast_fed(const P & p, const LcFastT<T> & w) {
   const float r3 = 1.0f/3.0f;
   const float gamma = (float) p.gamma, a0 = (float) p.a0;
   const float q0 = (float) p.q0*(float) p.rredshift;
   const float rs2 = (float) p.redshift*(float) p.redshift;
   const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
-  float q3 = 0.0f, dq1 = 0.0f, efield = 0.0f;
+  T q3(0.0f), dq1(0.0f), efield(0.0f);
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = 0; b < 3; b++) {
-      q3 = fmaf(w.QQ[a][b], w.q[a][b], q3);
-      const float t = fmaf(2.0f*q0, w.q[a][b], w.R[a][b]);
-      dq1 = fmaf(t, t, dq1);
+      q3 = lc_fma(w.QQ[a][b], w.q[a][b], q3);
+      const T t = lc_fma(T(2.0f*q0), w.q[a][b], w.R[a][b]);
+      dq1 = lc_fma(t, t, dq1);
     }
   }
-  const float dq0 = w.v[0]*w.v[0] + w.v[1]*w.v[1] + w.v[2]*w.v[2];
+  const T dq0 = w.v[0]*w.v[0] + w.v[1]*w.v[1] + w.v[2]*w.v[2];
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
@@ -412,33 +425,32 @@ __device__ __forceinline__ float lc_fast_fed(const P & p, const LcFast & w) {
 }
 
 /* Molecular field H (symmetric, traceless) */
-template <typename P>
-__device__ __forceinline__ void lc_fast_h(const P & p, const LcFast & w,
-					  const float dsq[3][3],
-					  float h[3][3]) {
+template <typename T, typename P>
+__device__ __forceinline__ void lc_fast_h(const P & p, const LcFastT<T> & w,
+					  const T dsq[3][3], T h[3][3]) {
   const float r3 = 1.0f/3.0f;
   const float gamma = (float) p.gamma, a0 = (float) p.a0;
   const float q0 = (float) p.q0*(float) p.rredshift;
   const float rs2 = (float) p.redshift*(float) p.redshift;
   const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
-  const float c1 = -a0*(1.0f - r3*gamma) - a0*gamma*w.q2
+  const T c1 = -a0*(1.0f - r3*gamma) - a0*gamma*w.q2
     - 4.0f*kappa1*q0*q0;
   const float ag = a0*gamma;
   const float k2 = -2.0f*kappa1*q0;
-  const float eq = w.R[0][0] + w.R[1][1] + w.R[2][2];
+  const T eq = w.R[0][0] + w.R[1][1] + w.R[2][2];
   float e[3], e2 = 0.0f;
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     e[a] = (float) p.e0[a]*(float) p.coswt;
     e2 += e[a]*e[a];
   }
-  const float diag = -r3*ag*w.q2 + 4.0f*r3*kappa1*q0*eq
+  const T diag = -r3*ag*w.q2 + 4.0f*r3*kappa1*q0*eq
     - (float) p.epsilon*r3*e2;
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = a; b < 3; b++) {
-      float t = c1*w.q[a][b] + ag*w.QQ[a][b] + kappa0*dsq[a][b]
+      T t = c1*w.q[a][b] + ag*w.QQ[a][b] + kappa0*dsq[a][b]
 	+ k2*(w.R[a][b] + w.R[b][a]) + (float) p.epsilon*e[a]*e[b];
       if (a == b) t += diag;
       h[a][b] = t;
@@ -448,47 +460,47 @@ __device__ __forceinline__ void lc_fast_h(const P & p, const LcFast & w,
 }
 
 /* Chiral stress including the antisymmetric part, with the final sign */
-template <typename P>
-__device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
-					       const float h[3][3],
-					       float sth[3][3]) {
+template <typename T, typename P>
+__device__ __forceinline__ void lc_fast_stress(const P & p,
+					       const LcFastT<T> & w,
+					       const T h[3][3], T sth[3][3]) {
   const float r3 = 1.0f/3.0f;
   const float xi = (float) p.xi;
   const float q0 = (float) p.q0*(float) p.rredshift;
   const float rs2 = (float) p.redshift*(float) p.redshift;
   const float kappa0 = (float) p.kappa0*rs2, kappa1 = (float) p.kappa1*rs2;
-  const float fed = w.fed;
-  float qh = 0.0f;
+  const T fed = w.fed;
+  T qh(0.0f);
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
-    for (int b = 0; b < 3; b++) qh = fmaf(w.q[a][b], h[a][b], qh);
+    for (int b = 0; b < 3; b++) qh = lc_fma(w.q[a][b], h[a][b], qh);
   }
   /* M = H Qt */
-  float M[3][3];
+  T M[3][3];
   #pragma unroll
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = 0; b < 3; b++) {
-      float t = r3*h[a][b];
+      T t = r3*h[a][b];
       #pragma unroll
-      for (int c = 0; c < 3; c++) t = fmaf(h[a][c], w.q[c][b], t);
+      for (int c = 0; c < 3; c++) t = lc_fma(h[a][c], w.q[c][b], t);
       M[a][b] = t;
     }
   }
   /* off-diagonal of dQ_a . Q for the chiral term */
-  float C[3][3];
+  T C[3][3];
   #pragma unroll
   for (int a = 0; a < 3; a++) {
-    float Pm[3][3];
+    T Pm[3][3];
     #pragma unroll
     for (int c = 0; c < 3; c++) {
       #pragma unroll
       for (int e = 0; e < 3; e++) {
 	if (c == e) continue;
-	float t = 0.0f;
+	T t(0.0f);
 	#pragma unroll
-	for (int d = 0; d < 3; d++) t = fmaf(w.dq[a][c][d], w.q[d][e], t);
+	for (int d = 0; d < 3; d++) t = lc_fma(w.dq[a][c][d], w.q[d][e], t);
 	Pm[c][e] = t;
       }
     }
@@ -498,14 +510,14 @@ __device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
   }
   /* X - G = d_a Q_cd (d_c Q_bd - d_b Q_cd): the bracket is antisymmetric
    * in (c, b) and vanishes for c = b */
-  float Dm[3][3][3];
+  T Dm[3][3][3];
   #pragma unroll
   for (int c = 0; c < 3; c++) {
     #pragma unroll
     for (int b = c + 1; b < 3; b++) {
       #pragma unroll
       for (int d = 0; d < 3; d++) {
-	const float t = w.dq[c][b][d] - w.dq[b][c][d];
+	const T t = w.dq[c][b][d] - w.dq[b][c][d];
 	Dm[c][b][d] = t;
 	Dm[b][c][d] = -t;
       }
@@ -515,16 +527,16 @@ __device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
   for (int a = 0; a < 3; a++) {
     #pragma unroll
     for (int b = 0; b < 3; b++) {
-      float XG = 0.0f, K = 0.0f;
+      T XG(0.0f), K(0.0f);
       #pragma unroll
       for (int c = 0; c < 3; c++) {
-	K = fmaf(w.dq[a][b][c], w.v[c], K);
+	K = lc_fma(w.dq[a][b][c], w.v[c], K);
 	if (c == b) continue;
 	#pragma unroll
-	for (int d = 0; d < 3; d++) XG = fmaf(w.dq[a][c][d], Dm[c][b][d], XG);
+	for (int d = 0; d < 3; d++) XG = lc_fma(w.dq[a][c][d], Dm[c][b][d], XG);
       }
-      const float qt = w.q[a][b] + ((a == b) ? r3 : 0.0f);
-      float t = 2.0f*xi*qt*qh - xi*(M[a][b] + M[b][a]) - kappa0*K
+      const T qt = w.q[a][b] + ((a == b) ? r3 : 0.0f);
+      T t = 2.0f*xi*qt*qh - xi*(M[a][b] + M[b][a]) - kappa0*K
 	+ kappa1*XG - 2.0f*kappa1*q0*C[a][b]
 	+ (M[b][a] - M[a][b]);
       if (a == b) t += fed;
@@ -533,11 +545,12 @@ __device__ __forceinline__ void lc_fast_stress(const P & p, const LcFast & w,
   }
 }
 
-/* H, free energy and stress of one site from Q and its gradients */
-template <typename P>
-__device__ __forceinline__ void lc_fast_site(const P & p, LcFast & w,
-					     const float dsq[3][3],
-					     float h[3][3], float sth[3][3]) {
+/* H, free energy and stress of one site (or a pair) from Q and its
+ * gradients */
+template <typename T, typename P>
+__device__ __forceinline__ void lc_fast_site(const P & p, LcFastT<T> & w,
+					     const T dsq[3][3],
+					     T h[3][3], T sth[3][3]) {
   lc_fast_prepare(w);
   w.fed = lc_fast_fed(p, w);
   lc_fast_h(p, w, dsq, h);

@@ -61,6 +61,26 @@ static int launch_collide2(const lgbk_dims_t * d,
   return (int) cudaGetLastError();
 }
 
+/* Fields + Beris-Edwards with two sites per thread (tiles of 2 LC32_F2Y
+ * rows, LC32_F2MINB blocks per SM; 168 registers and a few spilled).
+ * Measured LC step at 128^3 with this kernel and the one-site collision:
+ * (F2Y, blocks/SM) (2, 5) 0.1725 ms, (2, 4) 0.179 (238 registers, no
+ * spills), (1, 8) 0.178, (4, 2) 0.179, against 0.160 with the one-site
+ * kernel: the pair's registers cut the resident warps from 20 to 8-10 per
+ * SM, which costs more latency hiding than the packed arithmetic saves. */
+#define LC32_F2Y 2
+#define LC32_F2MINB 5
+
+static int launch_fields2(const lgbk_dims_t * d, const lgbk_lc_f_t * pf,
+			  const lgbk_lc_step_args_t * a, cudaStream_t s) {
+  const dim3 grid((unsigned int) (((d->nz + 31)/32)
+				  *((d->ny + 2*LC32_F2Y - 1)/(2*LC32_F2Y))),
+		  (unsigned int) d->nx);
+  k_lc32_fields_be2<LC32_F2Y, LC32_F2MINB><<<grid, dim3(32, LC32_F2Y), 0, s>>>(
+    *d, *pf, *a);
+  return (int) cudaGetLastError();
+}
+
 template <typename S>
 static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
 		     const lgbk_lc_step_args_t * a, cudaStream_t s) {
@@ -75,17 +95,23 @@ static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
 				   *((d->ny + LC32_FY - 1)/LC32_FY)),
 		    (unsigned int) d->nx);
   const dim3 fblock(32, LC32_FY);
+  cudaError_t err = cudaSuccess;
   if (a->status) {
     k_lc32_fields_be<true><<<fgrid, fblock, 0, s>>>(*d, pf, *a);
+    err = cudaGetLastError();
+  }
+  else if (a->sites == 2) {
+    err = (cudaError_t) launch_fields2(d, &pf, a, s);
   }
   else {
     k_lc32_fields_be<false><<<fgrid, fblock, 0, s>>>(*d, pf, *a);
+    err = cudaGetLastError();
   }
-  cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;
   if (a->status) return launch_collide<S, true>(d, a, s);
   /* two sites per thread only when asked for: at 128^3 the one-site
-   * kernel is the faster (0.161 against 0.171 ms per LC step, FP32) */
+   * kernels are the faster (0.161 against 0.171 ms per LC step with the
+   * two-site collision, FP32) */
   if (a->sites == 2) return launch_collide2<S, 4, 3>(d, a, s);
   return launch_collide<S, false>(d, a, s);
 }

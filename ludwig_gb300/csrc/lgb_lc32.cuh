@@ -41,6 +41,120 @@
 #define LC32_FY 2
 #define LC32_FMINB 10
 
+/* lane-wise c = (u > 0) ? a : b for one site or a pair */
+__device__ __forceinline__ float lc_sel_gt0(float u, float a, float b) {
+  return (u > 0.0f) ? a : b;
+}
+__device__ __forceinline__ vf2 lc_sel_gt0(const vf2 & u, const vf2 & a,
+					  const vf2 & b) {
+  return sel_gt0(u, a, b);
+}
+__device__ __forceinline__ float lc_sel_lt0(float u, float a, float b) {
+  return (u < 0.0f) ? a : b;
+}
+__device__ __forceinline__ vf2 lc_sel_lt0(const vf2 & u, const vf2 & a,
+					  const vf2 & b) {
+  return sel_lt0(u, a, b);
+}
+
+/* H and the chiral stress P of a site (T = float) or of a pair of sites
+ * (T = vf2) from Q at the site and its six neighbours (0 x+1, 1 x-1,
+ * 2 y+1, 3 y-1, 4 z+1, 5 z-1); w keeps Q for the update */
+template <typename T, typename P>
+__device__ __forceinline__ void lc32_fields_site(const P & p, const T qc[5],
+						 const T qn[5][6],
+						 LcFastT<T> & w, T h[3][3],
+						 T sth[3][3]) {
+  T dsq[3][3];
+  {
+    T g[15], dl[5];
+    #pragma unroll
+    for (int n = 0; n < 5; n++) {
+      g[3*n + 0] = 0.5f*(qn[n][0] - qn[n][1]);
+      g[3*n + 1] = 0.5f*(qn[n][2] - qn[n][3]);
+      g[3*n + 2] = 0.5f*(qn[n][4] - qn[n][5]);
+      dl[n] = qn[n][0] + qn[n][1] + qn[n][2] + qn[n][3] + qn[n][4]
+	+ qn[n][5] - 6.0f*qc[n];
+    }
+    lc_expand(qc, 1, 0, w.q);
+    lc_expand_grad(g, 1, 0, w.dq);
+    lc_expand(dl, 1, 0, dsq);
+  }
+  lc_fast_site(p, w, dsq, h, sth);
+}
+
+/* Beris-Edwards update of a site or a pair: S = -2 xi Qt (Q:W) + A Qt +
+ * (A Qt)^T with A = xi D + Omega, the upwind fluxes of Q with the face
+ * velocities, and the no-flux mask m (neighbour order as above; used only
+ * with HAS_MAP) */
+template <typename T, bool HAS_MAP>
+__device__ __forceinline__ void lc32_be_site(float xi, float gamma_rot,
+					     const LcFastT<T> & w,
+					     const T h[3][3], const T qc[5],
+					     const T qn[5][6], const T uc[3],
+					     const T un[3][6], const T m[6],
+					     T qo[5]) {
+  const float r3 = 1.0f/3.0f;
+  T s5[5];
+  {
+    T wv[3][3];
+    #pragma unroll
+    for (int c = 0; c < 3; c++) {
+      wv[c][0] = 0.5f*(un[c][0] - un[c][1]);
+      wv[c][1] = 0.5f*(un[c][2] - un[c][3]);
+      wv[c][2] = 0.5f*(un[c][4] - un[c][5]);
+    }
+    const T tr = r3*(wv[0][0] + wv[1][1] + wv[2][2]);
+    wv[0][0] -= tr; wv[1][1] -= tr; wv[2][2] -= tr;
+    T tqw(0.0f), A[3][3], qt[3][3];
+    #pragma unroll
+    for (int ia = 0; ia < 3; ia++) {
+      #pragma unroll
+      for (int ib = 0; ib < 3; ib++) {
+	tqw += w.q[ia][ib]*wv[ib][ia];
+	A[ia][ib] = 0.5f*(xi*(wv[ia][ib] + wv[ib][ia])
+			  + (wv[ia][ib] - wv[ib][ia]));
+	qt[ia][ib] = w.q[ia][ib] + ((ia == ib) ? r3 : 0.0f);
+      }
+    }
+    auto aq = [&](int ia, int ib) -> T {
+      return A[ia][0]*qt[0][ib] + A[ia][1]*qt[1][ib] + A[ia][2]*qt[2][ib];
+    };
+    const T m2 = -2.0f*xi*tqw;
+    s5[0] = m2*qt[0][0] + 2.0f*aq(0, 0);
+    s5[1] = m2*qt[0][1] + aq(0, 1) + aq(1, 0);
+    s5[2] = m2*qt[0][2] + aq(0, 2) + aq(2, 0);
+    s5[3] = m2*qt[1][1] + 2.0f*aq(1, 1);
+    s5[4] = m2*qt[1][2] + aq(1, 2) + aq(2, 1);
+  }
+
+  /* upwind face velocities, masked by the no-flux condition */
+  const T uw = 0.5f*(uc[0] + un[0][1]);
+  const T ue = 0.5f*(uc[0] + un[0][0]);
+  const T uyp = 0.5f*(uc[1] + un[1][2]);
+  const T uym = 0.5f*(un[1][3] + uc[1]);
+  const T uzp = 0.5f*(uc[2] + un[2][4]);
+  const T uzm = 0.5f*(un[2][5] + uc[2]);
+  const T muw = HAS_MAP ? T(m[1]*uw) : uw;
+  const T mue = HAS_MAP ? T(m[0]*ue) : ue;
+  const T muyp = HAS_MAP ? T(m[2]*uyp) : uyp;
+  const T muzp = HAS_MAP ? T(m[4]*uzp) : uzp;
+  const T muym = HAS_MAP ? T(m[3]*uym) : uym;
+  const T muzm = HAS_MAP ? T(m[5]*uzm) : uzm;
+  const T hv[5] = {h[0][0], h[0][1], h[0][2], h[1][1], h[1][2]};
+  #pragma unroll
+  for (int n = 0; n < 5; n++) {
+    const auto fw = muw*lc_sel_gt0(uw, qn[n][1], qc[n]);
+    const auto fe = mue*lc_sel_lt0(ue, qn[n][0], qc[n]);
+    const auto fy = muyp*lc_sel_lt0(uyp, qn[n][2], qc[n]);
+    const auto fz = muzp*lc_sel_lt0(uzp, qn[n][4], qc[n]);
+    const auto fyj = muym*lc_sel_lt0(uym, qc[n], qn[n][3]);
+    const auto fzk = muzm*lc_sel_lt0(uzm, qc[n], qn[n][5]);
+    qo[n] = qc[n] + (s5[n] + gamma_rot*hv[n] - fe + fw - fy + fyj
+		     - fz + fzk);
+  }
+}
+
 template <bool HAS_MAP>
 __global__ void __launch_bounds__(32*LC32_FY, LC32_FMINB)
 k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
@@ -54,7 +168,6 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
   /* 32-bit unsigned site indices (the host refuses 2^32 sites or more);
    * pointers are formed from per-component bases */
   const unsigned i = (unsigned) x*NP + y*d.nz + z;
-  const float r3 = 1.0f/3.0f;
   /* neighbours: 0 x+1, 1 x-1, 2 y+1, 3 y-1, 4 z+1, 5 z-1 */
   const unsigned xw = (unsigned) (d.nx - 1)*NP;   /* x wrap, modulo 2^32 */
   const unsigned nb[6] = {
@@ -90,22 +203,8 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
 
   /* H and P */
   LcFast w;
-  float h[3][3], sth[3][3], dsq[3][3];
-  {
-    float g[15], dl[5];
-    #pragma unroll
-    for (int n = 0; n < 5; n++) {
-      g[3*n + 0] = 0.5f*(qn[n][0] - qn[n][1]);
-      g[3*n + 1] = 0.5f*(qn[n][2] - qn[n][3]);
-      g[3*n + 2] = 0.5f*(qn[n][4] - qn[n][5]);
-      dl[n] = qn[n][0] + qn[n][1] + qn[n][2] + qn[n][3] + qn[n][4]
-	+ qn[n][5] - 6.0f*qc[n];
-    }
-    lc_expand(qc, 1, 0, w.q);
-    lc_expand_grad(g, 1, 0, w.dq);
-    lc_expand(dl, 1, 0, dsq);
-  }
-  lc_fast_site(p, w, dsq, h, sth);
+  float h[3][3], sth[3][3];
+  lc32_fields_site(p, qc, qn, w, h, sth);
   #pragma unroll
   for (int ia = 0; ia < 3; ia++)
     #pragma unroll
@@ -118,67 +217,16 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
     return;
   }
 
-  /* Beris-Edwards: S = -2 xi Qt (Q:W) + A Qt + (A Qt)^T, A = xi D + Omega */
-  const float xi = a.fp[LGBK_LCF_XI];
-  const float gamma_rot = a.fp[LGBK_LCF_GAMMA_ROT];
-  float s5[5];
-  {
-    float wv[3][3];
-    #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      wv[c][0] = 0.5f*(un[c][0] - un[c][1]);
-      wv[c][1] = 0.5f*(un[c][2] - un[c][3]);
-      wv[c][2] = 0.5f*(un[c][4] - un[c][5]);
-    }
-    const float tr = r3*(wv[0][0] + wv[1][1] + wv[2][2]);
-    wv[0][0] -= tr; wv[1][1] -= tr; wv[2][2] -= tr;
-    float tqw = 0.0f, A[3][3], qt[3][3];
-    #pragma unroll
-    for (int ia = 0; ia < 3; ia++) {
-      #pragma unroll
-      for (int ib = 0; ib < 3; ib++) {
-	tqw += w.q[ia][ib]*wv[ib][ia];
-	A[ia][ib] = 0.5f*(xi*(wv[ia][ib] + wv[ib][ia])
-			  + (wv[ia][ib] - wv[ib][ia]));
-	qt[ia][ib] = w.q[ia][ib] + ((ia == ib) ? r3 : 0.0f);
-      }
-    }
-    auto aq = [&](int ia, int ib) {
-      return A[ia][0]*qt[0][ib] + A[ia][1]*qt[1][ib] + A[ia][2]*qt[2][ib];
-    };
-    const float m2 = -2.0f*xi*tqw;
-    s5[0] = m2*qt[0][0] + 2.0f*aq(0, 0);
-    s5[1] = m2*qt[0][1] + aq(0, 1) + aq(1, 0);
-    s5[2] = m2*qt[0][2] + aq(0, 2) + aq(2, 0);
-    s5[3] = m2*qt[1][1] + 2.0f*aq(1, 1);
-    s5[4] = m2*qt[1][2] + aq(1, 2) + aq(2, 1);
-  }
-
-  /* upwind face velocities and the no-flux mask */
-  const float uw = 0.5f*(uc[0] + un[0][1]);
-  const float ue = 0.5f*(uc[0] + un[0][0]);
-  const float uyp = 0.5f*(uc[1] + un[1][2]);
-  const float uym = 0.5f*(un[1][3] + uc[1]);
-  const float uzp = 0.5f*(uc[2] + un[2][4]);
-  const float uzm = 0.5f*(un[2][5] + uc[2]);
-  float mw = 1.0f, me = 1.0f, my = 1.0f, mz = 1.0f, mym = 1.0f, mzm = 1.0f;
+  float msk[6] = {1.0f, 1.0f, 1.0f, 1.0f, 1.0f, 1.0f};
   if (HAS_MAP) {
-    mw = (float) (st[nb[1]] == 0); me = (float) (st[nb[0]] == 0);
-    my = (float) (st[nb[2]] == 0); mz = (float) (st[nb[4]] == 0);
-    mym = (float) (st[nb[3]] == 0); mzm = (float) (st[nb[5]] == 0);
+    #pragma unroll
+    for (int k = 0; k < 6; k++) msk[k] = (float) (st[nb[k]] == 0);
   }
-  const float hv[5] = {h[0][0], h[0][1], h[0][2], h[1][1], h[1][2]};
+  float qnew[5];
+  lc32_be_site<float, HAS_MAP>(a.fp[LGBK_LCF_XI], a.fp[LGBK_LCF_GAMMA_ROT],
+			       w, h, qc, qn, uc, un, msk, qnew);
   #pragma unroll
-  for (int n = 0; n < 5; n++) {
-    const float fw = mw*uw*((uw > 0.0f) ? qn[n][1] : qc[n]);
-    const float fe = me*ue*((ue < 0.0f) ? qn[n][0] : qc[n]);
-    const float fy = my*uyp*((uyp < 0.0f) ? qn[n][2] : qc[n]);
-    const float fz = mz*uzp*((uzp < 0.0f) ? qn[n][4] : qc[n]);
-    const float fyj = mym*uym*((uym < 0.0f) ? qc[n] : qn[n][3]);
-    const float fzk = mzm*uzm*((uzm < 0.0f) ? qc[n] : qn[n][5]);
-    (qo + n*N)[i] = qc[n] + (s5[n] + gamma_rot*hv[n] - fe + fw - fy + fyj
-			   - fz + fzk);
-  }
+  for (int n = 0; n < 5; n++) (qo + n*N)[i] = qnew[n];
 }
 
 /* A plane of P in shared memory: 9 components x (TY + 2) rows of RZ

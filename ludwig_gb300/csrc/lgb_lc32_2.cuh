@@ -2,11 +2,19 @@
  *
  *  lgb_lc32_2.cuh
  *
- *  The force + collision kernel of the float LC step (k_lc32_collide in
- *  lgb_lc32.cuh) with two sites per thread: thread (ty, tz) owns the sites
- *  of rows 2 ty and 2 ty + 1 of a 2 TYT x 32 (y, z) tile at column tz and
- *  computes both in packed FP32x2 arithmetic (vf2).  The pulled
- *  populations of plane x + 1 are loaded while plane x is computed.
+ *  The two kernels of the float LC step (lgb_lc32.cuh) with two sites per
+ *  thread: thread (ty, tz) owns the sites of rows 2 ty and 2 ty + 1 of a
+ *  2 TYT x 32 (y, z) tile at column tz and computes both in packed FP32x2
+ *  arithmetic (vf2).
+ *
+ *  k_lc32_fields_be2: Q gradients, H, the chiral stress P and the
+ *  Beris-Edwards update of the pair (the site functions of k_lc32_fields_be
+ *  on vf2).  Of the y neighbours, the lower site's y + 1 is the upper
+ *  site and the upper site's y - 1 the lower, so a pair loads 12 values of
+ *  each field where two single sites load 14.
+ *
+ *  k_lc32_collide2: the force + collision kernel; the pulled populations
+ *  of plane x + 1 are loaded while plane x is computed.
  *
  *  Same data flow as the one-site kernel: planes of the chiral stress P
  *  (9 components, tile + 1 halo) stream into a 3-slot shared-memory ring
@@ -23,6 +31,81 @@
 
 #include "lgb_lc32.cuh"
 #include "lgb_vf2.cuh"
+
+template <int TYT, int MINB>
+__global__ void __launch_bounds__(32*TYT, MINB)
+k_lc32_fields_be2(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
+  const int ntz = (d.nz + 31)/32;
+  const int z = (blockIdx.x % ntz)*32 + threadIdx.x;
+  const int yA = (blockIdx.x / ntz)*(2*TYT) + 2*threadIdx.y;
+  const int x = blockIdx.y;
+  if (z >= d.nz || yA >= d.ny) return;
+  /* the upper site is row yA + 1, or row 0 when yA is the last row: then
+   * it is computed (in bounds) and not stored */
+  const bool actB = yA + 1 < d.ny;
+  const int yB = actB ? yA + 1 : 0;
+  const long long N = d.nsites;
+  const int NP = d.ny*d.nz;
+  const unsigned iA = (unsigned) x*NP + yA*d.nz + z;
+  const unsigned iB = (unsigned) x*NP + yB*d.nz + z;
+  /* neighbour offsets (modulo 2^32) shared by the two sites: x and z */
+  const unsigned xw = (unsigned) (d.nx - 1)*NP;
+  const unsigned oxp = (x == d.nx - 1) ? 0u - xw : (unsigned) NP;
+  const unsigned oxm = (x == 0) ? xw : 0u - (unsigned) NP;
+  const unsigned ozp = (z == d.nz - 1) ? 0u - (unsigned) (d.nz - 1) : 1u;
+  const unsigned ozm = (z == 0) ? (unsigned) (d.nz - 1) : 0u - 1u;
+  /* the lower site's y - 1 and the upper site's y + 1 */
+  const unsigned iAym = (yA == 0) ? iA + (unsigned) (d.ny - 1)*d.nz
+    : iA - (unsigned) d.nz;
+  const unsigned iByp = (yB == d.ny - 1) ? iB - (unsigned) (d.ny - 1)*d.nz
+    : iB + (unsigned) d.nz;
+  const float * __restrict__ q = (const float *) a.q_in;
+  const float * __restrict__ u = (const float *) a.u_in;
+  float * __restrict__ qo = (float *) a.q_out;
+  float * __restrict__ pth = (float *) a.pth;
+
+  /* neighbour order: 0 x+1, 1 x-1, 2 y+1, 3 y-1, 4 z+1, 5 z-1 */
+  auto load = [&](const float * f, vf2 & c, vf2 nbr[6]) {
+    const float a0 = f[iA], b0 = f[iB];
+    c = vf2(a0, b0);
+    nbr[0] = vf2(f[iA + oxp], f[iB + oxp]);
+    nbr[1] = vf2(f[iA + oxm], f[iB + oxm]);
+    nbr[2] = vf2(b0, f[iByp]);
+    nbr[3] = vf2(f[iAym], a0);
+    nbr[4] = vf2(f[iA + ozp], f[iB + ozp]);
+    nbr[5] = vf2(f[iA + ozm], f[iB + ozm]);
+  };
+  vf2 qc[5], qn[5][6];
+  #pragma unroll
+  for (int n = 0; n < 5; n++) load(q + n*N, qc[n], qn[n]);
+  vf2 uc[3], un[3][6];
+  #pragma unroll
+  for (int c = 0; c < 3; c++) load(u + c*N, uc[c], un[c]);
+
+  LcFastT<vf2> w;
+  vf2 h[3][3], sth[3][3];
+  lc32_fields_site(p, qc, qn, w, h, sth);
+  #pragma unroll
+  for (int ia = 0; ia < 3; ia++) {
+    #pragma unroll
+    for (int ib = 0; ib < 3; ib++) {
+      float * pc = pth + (3*ia + ib)*N;
+      pc[iA] = sth[ia][ib].v.x;
+      if (actB) pc[iB] = sth[ia][ib].v.y;
+    }
+  }
+  const vf2 msk[6] = {vf2(1.0f), vf2(1.0f), vf2(1.0f), vf2(1.0f), vf2(1.0f),
+		      vf2(1.0f)};
+  vf2 qnew[5];
+  lc32_be_site<vf2, false>(a.fp[LGBK_LCF_XI], a.fp[LGBK_LCF_GAMMA_ROT], w,
+			   h, qc, qn, uc, un, msk, qnew);
+  #pragma unroll
+  for (int n = 0; n < 5; n++) {
+    float * qn_out = qo + n*N;
+    qn_out[iA] = qnew[n].v.x;
+    if (actB) qn_out[iB] = qnew[n].v.y;
+  }
+}
 
 template <typename S, int TYT, int MINB>
 __global__ void __launch_bounds__(32*TYT, MINB)

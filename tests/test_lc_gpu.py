@@ -111,15 +111,25 @@ def test_lc_fp32_close_to_fp64(gb):
     assert np.abs(qa - qb).max() < 1e-5 * np.abs(qa).max() * 100
 
 
-@pytest.mark.parametrize("solid", [False, True])
+@pytest.mark.parametrize("solid,sites", [(False, 0), (True, 0), (False, 2)])
 @pytest.mark.parametrize("precision", [1, 2])
-def test_lc_fp32_one_step_close_to_fp64(gb, solid, precision):
+def test_lc_fp32_one_step_close_to_fp64(gb, solid, sites, precision):
     """One reduced-precision step (float arithmetic; f stored as float or
     scaled half) against one FP64 step from the same perturbed blue phase
     with flow, with and without solid sites: the float path's
     reduced-operation H, stress and Beris-Edwards forms (any summation
     order) and its split kernels must agree with the reference-order FP64
-    path to float rounding (half storage: to its 11-bit mantissa)."""
+    path to float rounding (half storage: to its 11-bit mantissa).  Both
+    kernels of the float step with one site per thread and with two (packed
+    FP32x2; all-fluid lattices only)."""
+    gb.tune_sites(sites)
+    try:
+        _one_step_close(gb, solid, precision)
+    finally:
+        gb.tune_sites(0)
+
+
+def _one_step_close(gb, solid, precision):
     L = (16, 12, 40)
     rng = np.random.default_rng(11)
     a = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5, redshift=0.9,
@@ -148,15 +158,21 @@ def test_lc_fp32_one_step_close_to_fp64(gb, solid, precision):
         assert err < tol * scale, (k, err, scale)
 
 
-def test_lc_fp32_ragged_lattice_close_to_fp64(gb):
+@pytest.mark.parametrize("sites", [0, 2])
+def test_lc_fp32_ragged_lattice_close_to_fp64(gb, sites):
     """The float LC kernels on extents that are no multiple of the tile or
-    of 4 (P planes copied element by element)."""
+    of 4 (P planes copied element by element; with two sites a thread, an
+    odd number of rows leaves the last thread one site)."""
     L = (11, 9, 37)
     a = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5)
     b = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5, precision=gb.FP32)
-    for s in (a, b):
-        s.init_o8m()
-        s.step(20)
+    gb.tune_sites(sites)
+    try:
+        for s in (a, b):
+            s.init_o8m()
+            s.step(20)
+    finally:
+        gb.tune_sites(0)
     qa, qb = a.q.get(), b.q.get()
     assert np.abs(qa - qb).max() < 1e-5 * np.abs(qa).max()
     ua, ub = a.state()["u"], b.state()["u"]

@@ -55,10 +55,12 @@ def test_two_sites_independent_of_tiling(gb, prec):
             assert np.array_equal(got[k], ref[k]), (xchunk, ty, minb, k)
 
 
-@pytest.mark.parametrize("L", [(16, 16, 32), (12, 10, 40)])
-def test_lc_two_site_collision_matches_one_site(gb, L):
-    """The float LC step with the two-site force + collision kernel against
-    the one-site kernel: same arithmetic, float rounding apart."""
+@pytest.mark.parametrize("L", [(16, 16, 32), (12, 10, 40), (12, 11, 40)])
+def test_lc_two_site_kernels_match_one_site(gb, L):
+    """The float LC step with both kernels two sites a thread (fields +
+    Beris-Edwards, force + collision) against the one-site kernels: same
+    arithmetic, float rounding apart (ny = 11: the last thread of each
+    column has one site)."""
     out = {}
     for sites in (1, 2):
         gb.tune_sites(sites)

@@ -80,7 +80,7 @@ NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4,
 # executed as 4 layers of 32 x 32 channels, 2*27*32*32 each; useful are
 # the real layer shapes 5 -> 32 -> 32 -> 32 -> 4: 2*27*(5*32 + 2*32*32 +
 # 32*4) = 126,144.
-CNN_EXEC_FLOP = 4 * 2 * 27 * 32 * 32
+CNN_EXEC_FLOP = 2 * 27 * 32 * (16 + 3 * 32)    # first layer: K = 16
 CNN_USEFUL_FLOP = 2 * 27 * (5 * 32 + 2 * 32 * 32 + 32 * 4)
 
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
@@ -510,19 +510,22 @@ def gpu_arm(args):
         try:
             from ludwig_gb300.corrector import bench as cnn_bench
             r = cnn_bench(128, reps=max(3, min(args.steps // 20, 20)))
-            fwd = r["line_planes"]["forward_ms"]
+            d = r["default"]
+            fwd = d["forward_ms"]
             ncs = 128 ** 3
             cnn = {"forward_ms": fwd,
-                   "train_step_ms": r["line_planes"]["train_step_ms"],
-                   "forward_tflops": r["line_planes"]["forward_tflops"],
+                   "train_step_ms": d["train_step_ms"],
+                   "forward_tflops": d["forward_tflops"],
                    "forward_tflops_useful":
                        CNN_USEFUL_FLOP * ncs / (fwd * 1e-3) / 1e12,
                    "useful_over_executed": CNN_USEFUL_FLOP / CNN_EXEC_FLOP,
-                   "train_step_tflops": r["line_planes"]["train_step_tflops"],
-                   "per_tap_forward_ms": r["per_tap"]["forward_ms"],
+                   "train_step_tflops": d["train_step_tflops"],
+                   "forward_ms_by_form": {k: v["forward_ms"]
+                                          for k, v in r.items()},
                    "unit_note": "forward_tflops: executed BF16 MMA work "
-                                "(4 layers of 32x32 channels) / wall time "
-                                "per call; forward_tflops_useful: the real "
+                                "(layers of 32x32 channels, the first "
+                                "with 16 input channels) / wall time per "
+                                "call; forward_tflops_useful: the real "
                                 "layer shapes 5-32-32-32-4",
                    "workload": "4-layer 3x3x3 conv net, 32 channels, 128^3 "
                                "coarse lattice, tcgen05 BF16 / FP32"}

@@ -269,10 +269,11 @@ def time_network(model, x, t, reps=20):
     sync()
     step = (time.perf_counter() - t0) / reps
     n = model.nsites
-    # executed MMA work: 4 convolutions forward, 3 backward-data and 4
-    # weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
+    # executed MMA work: 4 convolutions forward (the first with K = 16 of
+    # its 32 input channels: the 5 features and zeros), 3 backward-data
+    # and 4 weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
     flop_conv = 2.0 * n * 27 * 32 * 32
-    flop_fwd = 4 * flop_conv
+    flop_fwd = 3.5 * flop_conv
     flop_step = flop_fwd + 3 * flop_conv + 4 * flop_conv * 28.0 / 27.0
     return {"sites": n, "forward_ms": 1e3 * fwd, "train_step_ms": 1e3 * step,
             "forward_tflops": flop_fwd / fwd / 1e12,
@@ -291,9 +292,9 @@ def bench(n, reps=20):
     x[4] += 1.0
     t = 0.1 * torch.randn((4, N), device="cuda", generator=g)
     torch.cuda.synchronize()
-    res = {}
+    res = {"default": time_network(model, x, t, reps)}
     for mode, name in ((0, "per_tap"), (1, "line_planes"),
-                       (2, "line_swizzled")):
+                       (2, "line_swizzled"), (3, "line_three_taps")):
         model.line_reuse(mode)
         res[name] = time_network(model, x, t, reps)
     return res

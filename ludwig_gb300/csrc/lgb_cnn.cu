@@ -212,6 +212,7 @@ struct ConvP {
   uint8_t * pout;
   float * outf;
   int * err;
+  int khn;                    /* K halves of 16 input channels: 1 or 2 */
 };
 
 /* Epilogue of channels c0 .. c0+15 of one output site (x, y, z) from 16
@@ -366,6 +367,7 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
 	tc_fence_after();
 	#pragma unroll
 	for (int kh = 0; kh < 2; kh++) {
+	  if (kh >= p.khn) break;
 	  const uint64_t ad = tc_sdesc(sA + stage*TILEB + kh*32, 16, 512,
 				       LGB_TC_SWIZZLE_64B);
 	  const uint64_t bd = tc_sdesc(sW + t*WTAPB + kh*32, 16, 512,
@@ -426,21 +428,26 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
  *  neighbour lines.  A CTA walks a run of up to LN_YRUN tiles along y at
  *  fixed (x, z-chunk); a tile needs the 9 lines (x+dx, y+dy) of 130 rows
  *  (z0-1 .. z0+128), of which the next tile shares 6, so each tile loads
- *  only the 3 lines at y+1 (9 at the start of a run).  Lines sit in a ring
- *  of 4 y-slots per dx.  The A operand is stored without swizzle, as four
- *  planes of 8 channels x 130 rows (16 bytes per row), so the three z taps
- *  of a line are the same planes at row offsets 0, 1, 2: start address +
- *  16 bytes per row.  L2 -> shared traffic per tile drops from 27 boxes of
- *  128 rows to 3 lines of 130 rows.
+ *  only the 3 lines at y+1 (9 at the start of a run).  The three lines of
+ *  one y (dx = -1, 0, 1) fill one of LN_NY ring slots in load order; a
+ *  slot is refilled once the MMAs of the last tile that reads it have
+ *  completed, so loads run up to LN_NY - 3 tiles ahead of the MMAs.  The A
+ *  operand is stored without swizzle, as four planes of 8 channels x 130
+ *  rows (16 bytes per row), so the three z taps of a line are the same
+ *  planes at row offsets 0, 1, 2: start address + 16 bytes per row.
+ *  L2 -> shared traffic per tile drops from 27 boxes of 128 rows to 3
+ *  lines of 130 rows.
  *****************************************************************************/
 
 #define LN_ROWS   130
 #define LN_CHUNK  2176                  /* >= 130 x 16, 128-byte aligned */
 #define LN_SLOT   (4*LN_CHUNK)
-#define LN_NSLOT  12                    /* 3 dx x 4 y positions */
+#define LN_NY     6                     /* y-line slots of the ring */
+#define LN_NSLOT  (3*LN_NY)             /* 3 dx x LN_NY y-lines */
 #define LN_YRUN   16
 #define LN_TXLINE (4*LN_ROWS*16)        /* bytes of one line (4 planes) */
-#define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256)
+#define LN_XCH   2048                  /* boundary-row exchange (CYC) */
+#define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256 + LN_XCH)
 
 __device__ __forceinline__ void line_item(const lgbk_cnn_geom_t & g, int it,
 					  int & x, int & z0, int & ya,
@@ -465,8 +472,20 @@ __host__ __device__ __forceinline__ int line_items(const lgbk_cnn_geom_t & g) {
  * SWZ = 1: a line is 130 rows of 64 bytes with the 64-byte swizzle (one
  * TMA box 32 x 130), z taps at +64 bytes per row; this relies on the
  * swizzle being a function of the absolute shared-memory address, which
- * the checks against the one-box-per-tap kernel establish. */
-template <int MODE, int SWZ>
+ * the checks against the one-box-per-tap kernel establish.
+ *
+ * CYC = 1 (nz = 128: a line is the whole periodic z extent): the three z
+ * taps of a line share one MMA of N = 96, A = the line's 128 interior rows
+ * and B = the three taps' weights (consecutive in shared memory), so the
+ * A tile is read once per line instead of three times.  The accumulator
+ * holds D_dz[r] = sum over the lines of x(r) W_dz in columns 32 (dz + 1)
+ * .. + 31, and the output is out(r) = D_-1[r - 1] + D_0[r] + D_+1[r + 1]
+ * with r - 1, r + 1 taken modulo 128: the epilogue moves the two shifted
+ * terms one TMEM lane with warp shuffles, and across the four warps of a
+ * channel half through shared memory (an mbarrier per channel half and
+ * tile parity, bounded waits).  Sums in another order than the one-box-per-tap kernel: equal to
+ * FP32 rounding, not bit for bit. */
+template <int MODE, int SWZ, int CYC>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
 k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	     const __grid_constant__ CUtensorMap tm_w, const ConvP p) {
@@ -478,14 +497,19 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   const uint32_t sW = sbase;
   const uint32_t sL = sW + CNN_NTAP*WTAPB;
   const uint32_t sBar = sL + LN_NSLOT*LN_SLOT;
-  const uint32_t bFull = sBar;                 /* 4, per tile */
-  const uint32_t bDone = sBar + 32;            /* 4, per tile */
-  const uint32_t bW = sBar + 64;
+  const uint32_t bFull = sBar;                 /* LN_NY, per ring slot */
+  const uint32_t bRel = sBar + 8*LN_NY;        /* LN_NY, per ring slot */
+  const uint32_t bW = sBar + 16*LN_NY;
   const uint32_t bTFull = bW + 8;
   const uint32_t bTEmpty = bW + 24;
   const uint32_t bFin = bW + 40;
   uint32_t * tslot = (uint32_t *) (sgen + (bW + 48 - sbase));
   volatile int * abort_flag = (volatile int *) (sgen + (bW + 52 - sbase));
+  const uint32_t bX = bW + 56;                 /* 4: [channel half][parity] */
+  float * xch = (float *) (sgen + (sBar + 256 - sbase));
+  /* accumulator columns per tile and TMEM columns allocated */
+  constexpr uint32_t NACC = CYC ? 3*CNN_C : CNN_C;
+  constexpr uint32_t TCOLS = CYC ? 256 : CONV_TMEM_COLS;
 
   const int warp = threadIdx.x/32;
   const int lane = threadIdx.x % 32;
@@ -493,10 +517,11 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   const int nitems = line_items(g);
 
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < LN_NY; k++) {
       tc_mbar_init(bFull + 8*k, 1);
-      tc_mbar_init(bDone + 8*k, 1);
+      tc_mbar_init(bRel + 8*k, 1);
     }
+    for (int k = 0; k < 4; k++) tc_mbar_init(bX + 8*k, 8);
     tc_mbar_init(bW, 1);
     tc_mbar_init(bTFull, 1);
     tc_mbar_init(bTFull + 8, 1);
@@ -506,7 +531,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     *abort_flag = 0;
     tc_fence_barrier_init();
   }
-  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), CONV_TMEM_COLS);
+  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), TCOLS);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -519,73 +544,104 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     for (int t = 0; t < CNN_NTAP; t++) {
       tc_tma_load_2d(sW + t*WTAPB, &tm_w, bW, 0, t*CNN_C);
     }
-    uint32_t fills[4] = {0, 0, 0, 0};
+    /* y-lines are numbered in load order (sq); line sq fills ring slot
+     * sq % LN_NY, after line sq - LN_NY has been released */
+    uint32_t sq = 0;
     bool ok = true;
-    int i = 0;
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
-      for (int y = ya; y < yb; y++, i++) {
+      for (int y = ya; ok && y < yb; y++) {
 	const bool first = (y == ya);
-	/* the slots to be overwritten were last read by tile i-1 (a new
-	 * run) or i-2 (within a run) */
-	const int k = first ? i - 1 : i - 2;
-	if (k >= 0 && !tc_mbar_wait(bDone + 8*(k & 3), (uint32_t) (k >> 2) & 1u,
-				    abort_flag, p.err)) {
-	  ok = false;
-	  break;
-	}
 	const int nl = first ? 3 : 1;
-	const uint32_t bar = bFull + 8*(i & 3);
-	tc_mbar_arrive_tx(bar, nl*3*LN_TXLINE);
-	for (int dxi = 0; dxi < 3; dxi++) {
-	  for (int li = 0; li < nl; li++) {
-	    const int yy = first ? (y - 1 + li) : (y + 1);
-	    const int slot = dxi*4 + (yy & 3);
+	for (int li = 0; li < nl; li++, sq++) {
+	  const int yy = first ? (y - 1 + li) : (y + 1);
+	  const uint32_t r = sq % LN_NY;
+	  if (sq >= LN_NY &&
+	      !tc_mbar_wait(bRel + 8*r, (sq/LN_NY - 1u) & 1u, abort_flag,
+			    p.err)) {
+	    ok = false;
+	    break;
+	  }
+	  const uint32_t bar = bFull + 8*r;
+	  tc_mbar_arrive_tx(bar, 3*LN_TXLINE);
+	  for (int dxi = 0; dxi < 3; dxi++) {
+	    const uint32_t dst = sL + (uint32_t) (dxi*LN_NY + r)*LN_SLOT;
 	    const int row = prow(g, x + dxi - 1, yy, z0 - 1);
 	    if (SWZ) {
-	      tc_tma_load_2d(sL + slot*LN_SLOT, &tm_line, bar, 0, row);
+	      tc_tma_load_2d(dst, &tm_line, bar, 0, row);
 	    }
 	    else {
 	      for (int c = 0; c < 4; c++) {
-		tc_tma_load_2d(sL + slot*LN_SLOT + c*LN_CHUNK, &tm_line, bar,
-			       8*c, row);
+		tc_tma_load_2d(dst + c*LN_CHUNK, &tm_line, bar, 8*c, row);
 	      }
 	    }
 	  }
 	}
-	fills[i & 3] += 1;
       }
     }
     tc_drain_wait(bW, 0, p.err);
-    for (int k = 0; k < 4; k++) {
-      if (fills[k]) tc_drain_wait(bFull + 8*k, (fills[k] - 1u) & 1u, p.err);
+    /* the last fill of every slot used (earlier fills were consumed before
+     * their slot was refilled) */
+    for (uint32_t r = 0; r < LN_NY && r < sq; r++) {
+      const uint32_t nfill = (sq - r + LN_NY - 1)/LN_NY;
+      tc_drain_wait(bFull + 8*r, (nfill - 1u) & 1u, p.err);
     }
   }
   else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 0, 0);
+    constexpr uint32_t idesc = tc_idesc_bf16(128, (int) NACC, 0, 0);
     bool ok = tc_mbar_wait(bW, 0, abort_flag, p.err);
+    uint32_t sq = 0;                   /* y-lines consumed, as loaded */
     int i = 0;
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
       for (int y = ya; y < yb; y++, i++) {
 	const int acc = i & 1;
+	const bool first = (y == ya), last = (y == yb - 1);
 	if (!tc_mbar_wait(bTEmpty + 8*acc, ((uint32_t) (i >> 1) & 1u) ^ 1u,
-			  abort_flag, p.err) ||
-	    !tc_mbar_wait(bFull + 8*(i & 3), (uint32_t) (i >> 2) & 1u,
 			  abort_flag, p.err)) {
 	  ok = false;
 	  break;
 	}
+	for (int li = 0; ok && li < (first ? 3 : 1); li++, sq++) {
+	  ok = tc_mbar_wait(bFull + 8*(sq % LN_NY), (sq/LN_NY) & 1u,
+			    abort_flag, p.err);
+	}
+	if (!ok) break;
 	tc_fence_after();
-	const uint32_t d = tmem + (uint32_t) (acc*CNN_C);
+	/* ring slots of the lines y-1, y, y+1 */
+	const uint32_t rr[3] = {(sq - 3u) % LN_NY, (sq - 2u) % LN_NY,
+				(sq - 1u) % LN_NY};
+	const uint32_t d = tmem + (uint32_t) acc*NACC;
+	if (CYC) {
+	  /* one MMA per line (dx, dy) and K half: the three z taps' weights
+	   * (taps 3 ln .. 3 ln + 2) as N = 96, A = rows z0 .. z0 + 127 */
+	  #pragma unroll
+	  for (int ln = 0; ln < 9; ln++) {
+	    const uint32_t slot = (uint32_t) (ln/3)*LN_NY + rr[ln % 3];
+	    const uint32_t abase = sL + slot*LN_SLOT + (SWZ ? ROWB : 16);
+	    #pragma unroll
+	    for (int kh = 0; kh < 2; kh++) {
+	      if (kh >= p.khn) break;
+	      const uint64_t ad = SWZ
+		? tc_sdesc(abase + kh*32, 16, 512, LGB_TC_SWIZZLE_64B)
+		: tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128, 0u);
+	      const uint64_t bd = tc_sdesc(sW + 3*ln*WTAPB + kh*32, 16, 512,
+					   LGB_TC_SWIZZLE_64B);
+	      tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((ln | kh) != 0));
+	    }
+	  }
+	}
+	else {
+	#pragma unroll
 	for (int t = 0; t < CNN_NTAP; t++) {
 	  const int dxi = t/9, dyi = (t/3) % 3, dzi = t % 3;
-	  const int slot = dxi*4 + ((y + dyi - 1) & 3);
+	  const uint32_t slot = (uint32_t) dxi*LN_NY + rr[dyi];
 	  const uint32_t abase = sL + slot*LN_SLOT + dzi*(SWZ ? ROWB : 16);
 	  #pragma unroll
 	  for (int kh = 0; kh < 2; kh++) {
+	    if (kh >= p.khn) break;
 	    const uint64_t ad = SWZ
 	      ? tc_sdesc(abase + kh*32, 16, 512, LGB_TC_SWIZZLE_64B)
 	      : tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128, 0u);
@@ -594,7 +650,14 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	    tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((t | kh) != 0));
 	  }
 	}
-	tc_commit(bDone + 8*(i & 3));
+	}
+	/* the next tile of the run does not read line y-1; after the last
+	 * tile of a run none of the three is read again */
+	tc_commit(bRel + 8*rr[0]);
+	if (last) {
+	  tc_commit(bRel + 8*rr[1]);
+	  tc_commit(bRel + 8*rr[2]);
+	}
 	tc_commit(bTFull + 8*acc);
       }
     }
@@ -621,10 +684,50 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
 	tc_fence_after();
 	uint32_t r[16];
-	tc_tmem_ld16(tmem + (uint32_t) (acc*CNN_C + c0)
-		     + ((uint32_t) (q*32) << 16), r);
-	tc_fence_before();
-	tc_mbar_arrive(bTEmpty + 8*acc);
+	const uint32_t ta = tmem + (uint32_t) acc*NACC + (uint32_t) c0
+	  + ((uint32_t) (q*32) << 16);
+	if (CYC) {
+	  uint32_t rm[16], rp[16];
+	  tc_tmem_ld16(ta, rm);                      /* D_-1, this row */
+	  tc_tmem_ld16(ta + CNN_C, r);               /* D_0 */
+	  tc_tmem_ld16(ta + 2*CNN_C, rp);            /* D_+1 */
+	  tc_fence_before();
+	  tc_mbar_arrive(bTEmpty + 8*acc);
+	  /* rows 32 q - 1 and 32 q + 32 belong to the neighbouring warps
+	   * of this channel half: publish this warp's edge rows */
+	  const int grp = (warp - 2) >> 2;
+	  const int xb = grp*2 + (i & 1);
+	  float * mine = xch + (xb*4 + q)*32;
+	  /* lanes 31 and 0 each publish and arrive (8 arrivals a phase) */
+	  if (lane == 31) {
+	    #pragma unroll
+	    for (int n = 0; n < 16; n++) mine[n] = __uint_as_float(rm[n]);
+	    tc_mbar_arrive(bX + 8*xb);
+	  }
+	  if (lane == 0) {
+	    #pragma unroll
+	    for (int n = 0; n < 16; n++) mine[16 + n] = __uint_as_float(rp[n]);
+	    tc_mbar_arrive(bX + 8*xb);
+	  }
+	  const bool okx = tc_mbar_wait(bX + 8*xb, (uint32_t) (i >> 1) & 1u,
+					abort_flag, p.err);
+	  if (!__all_sync(0xffffffffu, okx)) { ok = false; break; }
+	  const float * prev = xch + (xb*4 + ((q + 3) & 3))*32;
+	  const float * next = xch + (xb*4 + ((q + 1) & 3))*32 + 16;
+	  #pragma unroll
+	  for (int n = 0; n < 16; n++) {
+	    float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[n]), 1);
+	    float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[n]), 1);
+	    if (lane == 0) dm = prev[n];
+	    if (lane == 31) dp = next[n];
+	    r[n] = __float_as_uint((__uint_as_float(r[n]) + dm) + dp);
+	  }
+	}
+	else {
+	  tc_tmem_ld16(ta, r);
+	  tc_fence_before();
+	  tc_mbar_arrive(bTEmpty + 8*acc);
+	}
 	conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
       }
     }
@@ -635,21 +738,22 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    tc_tmem_dealloc(tmem, CONV_TMEM_COLS);
+    tc_tmem_dealloc(tmem, TCOLS);
   }
 }
 
-template <int MODE, int SWZ>
+template <int MODE, int SWZ, int CYC>
 static cudaError_t launch_line(const lgbk_cnn_geom_t * g,
 			       const CUtensorMap & ml, const CUtensorMap & mw,
 			       const ConvP & p, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_conv3_line<MODE, SWZ>,
+  cudaError_t e = cudaFuncSetAttribute(k_conv3_line<MODE, SWZ, CYC>,
     cudaFuncAttributeMaxDynamicSharedMemorySize, LN_SMEM);
   if (e != cudaSuccess) return e;
   int grid = line_items(*g);
   const int nsm = num_sms();
   if (grid > nsm) grid = nsm;
-  k_conv3_line<MODE, SWZ><<<grid, CONV_THREADS, LN_SMEM, s>>>(ml, mw, p);
+  k_conv3_line<MODE, SWZ, CYC><<<grid, CONV_THREADS, LN_SMEM, s>>>(ml, mw,
+								    p);
   return cudaSuccess;
 }
 
@@ -660,8 +764,16 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
 			       cudaStream_t s) {
   cudaError_t e;
   if (ml) {
-    e = (line_kind == 2) ? launch_line<MODE, 1>(g, *ml, mw, p, s)
-                         : launch_line<MODE, 0>(g, *ml, mw, p, s);
+    if (line_kind == 3) {
+      if (g->nz != LGBK_CNN_TILE) return cudaErrorInvalidValue;
+      e = launch_line<MODE, 0, 1>(g, *ml, mw, p, s);
+    }
+    else if (line_kind == 2) {
+      e = launch_line<MODE, 1, 0>(g, *ml, mw, p, s);
+    }
+    else {
+      e = launch_line<MODE, 0, 0>(g, *ml, mw, p, s);
+    }
     if (e != cudaSuccess) return e;
   }
   else {
@@ -675,7 +787,7 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
   return cudaGetLastError();
 }
 
-extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
+extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
 			     const void * tm_in, const void * tm_line,
 			     int line_kind, const void * tm_w, const float * bias,
 			     const void * zprev, void * zout, void * pout,
@@ -688,6 +800,8 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode,
   p.pout = (uint8_t *) pout;
   p.outf = outf;
   p.err = err;
+  if (kin != 16 && kin != CNN_C) return (int) cudaErrorInvalidValue;
+  p.khn = kin/16;
   const CUtensorMap mi = *(const CUtensorMap *) tm_in;
   const CUtensorMap mw = *(const CUtensorMap *) tm_w;
   const CUtensorMap * ml = NULL;

@@ -62,8 +62,12 @@ int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
  * value).  tm_in: rows, box 32 x bz, 64-byte swizzle; tm_w: weights, box
  * 32 x 32, 64-byte swizzle; tm_line (may be NULL; nz a multiple of 128):
  * line_kind 1: rows, box 8 x 130, no swizzle; line_kind 2: rows, box
- * 32 x 130, 64-byte swizzle (line-reuse kernel). */
-int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, const void * tm_in,
+ * 32 x 130, 64-byte swizzle (line-reuse kernel); line_kind 3 (nz = 128):
+ * the kind-1 map, three z taps per MMA. */
+/* kin: input channels read, 32 or 16 (the first layer: channels 16..31 of
+ * its input rows are zero, so their products are left out) */
+int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
+		  const void * tm_in,
 		  const void * tm_line, int line_kind, const void * tm_w,
 		  const float * bias,
 		  const void * zprev, void * zout, void * pout, float * outf,

@@ -359,11 +359,14 @@ static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
 }
 
 /* 1: the line-reuse convolution where the extents allow it (default);
- * 2: the same with swizzled line boxes; 0: one box per tap */
+ * 2: the same with swizzled line boxes; 3: the same with the three z taps
+ * of a line in one MMA where nz = 128 (1 otherwise); 0: one box per tap */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int mode) {
-  if (m == NULL || mode < 0 || mode > 2) {
-    return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_line_reuse: 0, 1 or 2");
+  if (m == NULL || mode < 0 || mode > 3) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL,
+			    "cnn_line_reuse: 0, 1, 2 or 3");
   }
+  if (mode == 3 && m->g.nz != LGBK_CNN_TILE) mode = 1;
   m->line_on = m->line_ok ? mode : 0;
   return LUDWIG_GB_OK;
 }
@@ -384,6 +387,12 @@ static int check_err(ludwig_gb_cnn_t * m) {
   return LUDWIG_GB_OK;
 }
 
+/* Input channels a layer's convolution reads: the first layer's input
+ * rows hold the LGBK_CNN_NIN features and zeros */
+static int kin_of(int l) {
+  return (l == 0 && LGBK_CNN_NIN <= 16) ? 16 : LGBK_CNN_C;
+}
+
 /* a_0 from [phi, u, rho] pointers, then the four layers -> out4 */
 static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
 		   const float * rho) {
@@ -395,13 +404,13 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
   for (int l = 0; l < NL; l++) {
     const float * b = m->params + l*PL + WL;
     if (l < NL - 1) {
-      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, &m->tm_act[l],
+      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, kin_of(l), &m->tm_act[l],
 			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL,
 			 m->zpre[l + 1], m->act[l + 1], NULL, m->err_dev, s);
       if (!rc) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
     }
     else {
-      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, &m->tm_act[l],
+      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l), &m->tm_act[l],
 			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL, NULL,
 			 NULL, m->out4, m->err_dev, s);
     }
@@ -425,7 +434,7 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
 				     m->grads + l*PL + WL, s);
     if (rc) return ck(rc, "cnn wgrad");
     if (l == 0) break;
-    rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, &m->tm_g[l + 1],
+    rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, LGBK_CNN_C, &m->tm_g[l + 1],
 		       lmap(m, 0, l + 1), m->line_on, &m->tm_wt[l], NULL, m->zpre[l],
 		       NULL, m->gpad[l], NULL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_halo(g, m->gpad[l], s);
@@ -614,7 +623,7 @@ int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * m, const float * a, const float * w,
   cudaStream_t s = lib_stream();
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
   if (!rc) rc = lgbk_cnn_wprep(w, m->wf[0], m->wt[0], s);
-  if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, &m->tm_act[0],
+  if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, LGBK_CNN_C, &m->tm_act[0],
 			      lmap(m, 1, 0), m->line_on,
 			      flip ? &m->tm_wt[0] : &m->tm_wf[0],
 			      flip ? NULL : b, NULL, NULL, NULL, out,

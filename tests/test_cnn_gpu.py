@@ -50,11 +50,13 @@ def test_conv3_forward(gb, orc, n):
 @pytest.mark.parametrize("n", [(2, 2, 128), (8, 40, 128), (3, 5, 256),
                                (160, 17, 128)])
 @pytest.mark.parametrize("flip", [0, 1])
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip, mode):
     """nz a multiple of 128: the line-reuse kernel (runs of tiles along y,
     including runs of one tile and several runs per CTA) against the
-    oracle, and bit for bit against the one-box-per-tap kernel."""
+    oracle, and bit for bit against the one-box-per-tap kernel; mode 3
+    (three z taps per MMA, nz = 128; shifted partial sums added in the
+    epilogue) to FP32 rounding of the per-tap kernel."""
     rng = np.random.default_rng(15)
     N = n[0] * n[1] * n[2]
     m = gb.Corrector(n)
@@ -76,8 +78,13 @@ def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip, mode):
     else:
         ref = orc.conv3_fwd(n, a, w, b)
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
-    # same products, same accumulation order: identical results
-    assert torch.equal(out_l, out_t)
+    if mode == 3 and n[2] == 128:
+        # the same products summed in another order
+        d = (out_l - out_t).abs().max().item()
+        assert d <= 1e-5 * out_t.abs().max().item(), d
+    else:
+        # same products, same accumulation order: identical results
+        assert torch.equal(out_l, out_t)
 
 
 @pytest.mark.parametrize("n", [(4, 4, 32), (2, 2, 256), (64, 32, 64)])

@@ -590,6 +590,13 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   }
   else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = tc_idesc_bf16(128, (int) NACC, 0, 0);
+    /* descriptors of the first ring slot and of the first tap's weights */
+    const uint64_t ad0 = SWZ
+      ? tc_sdesc(sL, 16, 512, LGB_TC_SWIZZLE_64B)
+      : tc_sdesc(sL, LN_CHUNK, 128, 0u);
+    const uint64_t bd0 = tc_sdesc(sW, 16, 512, LGB_TC_SWIZZLE_64B);
+    const uint32_t alo0 = (uint32_t) ad0, ahi = (uint32_t) (ad0 >> 32);
+    const uint32_t blo0 = (uint32_t) bd0, bhi = (uint32_t) (bd0 >> 32);
     bool ok = tc_mbar_wait(bW, 0, abort_flag, p.err);
     uint32_t sq = 0;                   /* y-lines consumed, as loaded */
     int i = 0;
@@ -610,46 +617,46 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	}
 	if (!ok) break;
 	tc_fence_after();
-	/* ring slots of the lines y-1, y, y+1 */
+	/* low descriptor words of the lines y-1, y, y+1 at dx = -1 (ring
+	 * slots of the three y-lines); dx steps by LN_NY slots, z taps and
+	 * K halves by fixed byte offsets: one addition per MMA operand */
 	const uint32_t rr[3] = {(sq - 3u) % LN_NY, (sq - 2u) % LN_NY,
 				(sq - 1u) % LN_NY};
+	const uint32_t aln[3] = {alo0 + rr[0]*(LN_SLOT >> 4),
+				 alo0 + rr[1]*(LN_SLOT >> 4),
+				 alo0 + rr[2]*(LN_SLOT >> 4)};
+	constexpr uint32_t DXS = LN_NY*LN_SLOT >> 4;
+	constexpr uint32_t DZS = (SWZ ? ROWB : 16) >> 4;
+	constexpr uint32_t KHA = (SWZ ? 32 : 2*LN_CHUNK) >> 4;
+	constexpr uint32_t KHB = 32 >> 4;
 	const uint32_t d = tmem + (uint32_t) acc*NACC;
 	if (CYC) {
 	  /* one MMA per line (dx, dy) and K half: the three z taps' weights
 	   * (taps 3 ln .. 3 ln + 2) as N = 96, A = rows z0 .. z0 + 127 */
 	  #pragma unroll
 	  for (int ln = 0; ln < 9; ln++) {
-	    const uint32_t slot = (uint32_t) (ln/3)*LN_NY + rr[ln % 3];
-	    const uint32_t abase = sL + slot*LN_SLOT + (SWZ ? ROWB : 16);
+	    const uint32_t a = aln[ln % 3] + (uint32_t) (ln/3)*DXS + DZS;
 	    #pragma unroll
 	    for (int kh = 0; kh < 2; kh++) {
 	      if (kh >= p.khn) break;
-	      const uint64_t ad = SWZ
-		? tc_sdesc(abase + kh*32, 16, 512, LGB_TC_SWIZZLE_64B)
-		: tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128, 0u);
-	      const uint64_t bd = tc_sdesc(sW + 3*ln*WTAPB + kh*32, 16, 512,
-					   LGB_TC_SWIZZLE_64B);
-	      tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((ln | kh) != 0));
+	      tc_mma_bf16_w(d, a + kh*KHA, ahi, blo0 + (3*ln*WTAPB >> 4)
+			    + kh*KHB, bhi, idesc,
+			    (uint32_t) ((ln | kh) != 0));
 	    }
 	  }
 	}
 	else {
-	#pragma unroll
-	for (int t = 0; t < CNN_NTAP; t++) {
-	  const int dxi = t/9, dyi = (t/3) % 3, dzi = t % 3;
-	  const uint32_t slot = (uint32_t) dxi*LN_NY + rr[dyi];
-	  const uint32_t abase = sL + slot*LN_SLOT + dzi*(SWZ ? ROWB : 16);
 	  #pragma unroll
-	  for (int kh = 0; kh < 2; kh++) {
-	    if (kh >= p.khn) break;
-	    const uint64_t ad = SWZ
-	      ? tc_sdesc(abase + kh*32, 16, 512, LGB_TC_SWIZZLE_64B)
-	      : tc_sdesc(abase + kh*2*LN_CHUNK, LN_CHUNK, 128, 0u);
-	    const uint64_t bd = tc_sdesc(sW + t*WTAPB + kh*32, 16, 512,
-					 LGB_TC_SWIZZLE_64B);
-	    tc_mma_bf16(d, ad, bd, idesc, (uint32_t) ((t | kh) != 0));
+	  for (int t = 0; t < CNN_NTAP; t++) {
+	    const int dxi = t/9, dyi = (t/3) % 3, dzi = t % 3;
+	    const uint32_t a = aln[dyi] + (uint32_t) dxi*DXS + dzi*DZS;
+	    #pragma unroll
+	    for (int kh = 0; kh < 2; kh++) {
+	      if (kh >= p.khn) break;
+	      tc_mma_bf16_w(d, a + kh*KHA, ahi, blo0 + (t*WTAPB >> 4)
+			    + kh*KHB, bhi, idesc, (uint32_t) ((t | kh) != 0));
+	    }
 	  }
-	}
 	}
 	/* the next tile of the run does not read line y-1; after the last
 	 * tile of a run none of the three is read again */
@@ -688,9 +695,10 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	  + ((uint32_t) (q*32) << 16);
 	if (CYC) {
 	  uint32_t rm[16], rp[16];
-	  tc_tmem_ld16(ta, rm);                      /* D_-1, this row */
-	  tc_tmem_ld16(ta + CNN_C, r);               /* D_0 */
-	  tc_tmem_ld16(ta + 2*CNN_C, rp);            /* D_+1 */
+	  tc_tmem_ld16_async(ta, rm);                /* D_-1, this row */
+	  tc_tmem_ld16_async(ta + CNN_C, r);         /* D_0 */
+	  tc_tmem_ld16_async(ta + 2*CNN_C, rp);      /* D_+1 */
+	  tc_tmem_wait_ld16x3(rm, r, rp);
 	  tc_fence_before();
 	  tc_mbar_arrive(bTEmpty + 8*acc);
 	  /* rows 32 q - 1 and 32 q + 32 belong to the neighbouring warps

@@ -126,6 +126,25 @@ __device__ __forceinline__ void tc_mma_bf16(uint32_t d, uint64_t adesc,
 	       : "memory");
 }
 
+/* The same with each descriptor as two 32-bit words (low: start address
+ * and leading byte offset; high: stride byte offset, version, layout), so
+ * that a loop can step a descriptor's start address with one integer
+ * addition of (byte offset >> 4) to the low word (the address field cannot
+ * carry out: shared-memory addresses are below 2^18) */
+__device__ __forceinline__ void tc_mma_bf16_w(uint32_t d, uint32_t alo,
+					      uint32_t ahi, uint32_t blo,
+					      uint32_t bhi, uint32_t idesc,
+					      uint32_t accumulate) {
+  asm volatile("{\n\t.reg .pred p;\n\t.reg .b64 ad, bd;\n\t"
+	       "mov.b64 ad, {%1, %2};\n\t"
+	       "mov.b64 bd, {%3, %4};\n\t"
+	       "setp.ne.b32 p, %6, 0;\n\t"
+	       "tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n\t}"
+	       :: "r"(d), "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc),
+		  "r"(accumulate)
+	       : "memory");
+}
+
 /* Arrive on an mbarrier once every earlier tcgen05 op of this thread has
  * completed (frees the shared-memory operands, publishes the TMEM result) */
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
@@ -163,6 +182,41 @@ __device__ __forceinline__ void tc_tmem_ld16(uint32_t taddr, uint32_t r[16]) {
 		 "=r"(r[14]), "=r"(r[15])
 	       : "r"(taddr) : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+/* The same without the wait: the registers are valid only after
+ * tc_tmem_wait_ld16x3 on them */
+__device__ __forceinline__ void tc_tmem_ld16_async(uint32_t taddr,
+						   uint32_t r[16]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+	       "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+	       "%14, %15}, [%16];"
+	       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+		 "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+		 "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+		 "=r"(r[14]), "=r"(r[15])
+	       : "r"(taddr) : "memory");
+}
+
+/* Wait for the TMEM loads in flight; the registers of three x16 loads are
+ * operands, so that no use of them moves above the wait */
+__device__ __forceinline__ void tc_tmem_wait_ld16x3(uint32_t a[16],
+						    uint32_t b[16],
+						    uint32_t c[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+	       : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]),
+		 "+r"(a[5]), "+r"(a[6]), "+r"(a[7]), "+r"(a[8]), "+r"(a[9]),
+		 "+r"(a[10]), "+r"(a[11]), "+r"(a[12]), "+r"(a[13]),
+		 "+r"(a[14]), "+r"(a[15]),
+		 "+r"(b[0]), "+r"(b[1]), "+r"(b[2]), "+r"(b[3]), "+r"(b[4]),
+		 "+r"(b[5]), "+r"(b[6]), "+r"(b[7]), "+r"(b[8]), "+r"(b[9]),
+		 "+r"(b[10]), "+r"(b[11]), "+r"(b[12]), "+r"(b[13]),
+		 "+r"(b[14]), "+r"(b[15]),
+		 "+r"(c[0]), "+r"(c[1]), "+r"(c[2]), "+r"(c[3]), "+r"(c[4]),
+		 "+r"(c[5]), "+r"(c[6]), "+r"(c[7]), "+r"(c[8]), "+r"(c[9]),
+		 "+r"(c[10]), "+r"(c[11]), "+r"(c[12]), "+r"(c[13]),
+		 "+r"(c[14]), "+r"(c[15])
+	       :: "memory");
 }
 
 /* Shared-memory matrix descriptor (tcgen05): start, leading and stride

@@ -815,10 +815,10 @@ int ludwig_gb_cnn_train_steps(ludwig_gb_cnn_t * cnn, int nsteps,
 int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * cnn, lb_t * lb, field_t * phi,
 			  hydro_t * hydro);
 /* Where nz is a multiple of 128 the convolutions reuse neighbour lines:
- * mode 1 (default) stores a line as 4 unswizzled planes of 8 channels,
- * mode 2 as 64-byte-swizzled rows, mode 3 (nz = 128; mode 1 otherwise)
- * as mode 1 with the three z taps of a line in one tensor-core MMA;
- * mode 0: one TMA box per tap (any supported extents) */
+ * mode 1 stores a line as 4 unswizzled planes of 8 channels, mode 2 as
+ * 64-byte-swizzled rows, mode 3 (nz = 128; mode 1 otherwise) as mode 1
+ * with the three z taps of a line in one tensor-core MMA; mode 0: one TMA
+ * box per tap (any supported extents).  Default: 3 where nz = 128, else 1 */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * cnn, int mode);
 /* one convolution / weight gradient on given fp32 device arrays
  * (operands rounded to bf16), for checks of the kernels themselves:

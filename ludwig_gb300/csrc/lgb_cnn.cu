@@ -231,7 +231,8 @@ __device__ __forceinline__ void conv_epilogue(const ConvP & p,
   if (MODE == LGBK_CNN_FWD_GELU) {
     #pragma unroll
     for (int n = 0; n < 16; n++) v[n] += bias[n];
-    store_half_row_bf16(p.zout + s*ROWB + 2*c0, v);
+    /* pre-activation, kept for a backward pass (training only) */
+    if (p.zout) store_half_row_bf16(p.zout + s*ROWB + 2*c0, v);
     #pragma unroll
     for (int n = 0; n < 16; n++) v[n] = gelu_f(v[n]);
     store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
@@ -467,6 +468,18 @@ __host__ __device__ __forceinline__ int line_items(const lgbk_cnn_geom_t & g) {
   return g.nx*(g.nz/LGBK_CNN_TILE)*((g.ny + LN_YRUN - 1)/LN_YRUN);
 }
 
+/* 16-byte shared-memory store and load (32-bit shared addresses) */
+__device__ __forceinline__ void lds_st4(uint32_t a, const uint32_t v[4]) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+	       :: "r"(a), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3])
+	       : "memory");
+}
+__device__ __forceinline__ void lds_ld4(uint32_t a, uint32_t v[4]) {
+  asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];"
+	       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+	       : "r"(a) : "memory");
+}
+
 /* SWZ = 0: a line is 4 unswizzled planes (8 channels x 130 rows, 16 bytes
  * a row; TMA box 8 x 130 each), z taps at +16 bytes per row.
  * SWZ = 1: a line is 130 rows of 64 bytes with the 64-byte swizzle (one
@@ -506,7 +519,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   uint32_t * tslot = (uint32_t *) (sgen + (bW + 48 - sbase));
   volatile int * abort_flag = (volatile int *) (sgen + (bW + 52 - sbase));
   const uint32_t bX = bW + 56;                 /* 4: [channel half][parity] */
-  float * xch = (float *) (sgen + (sBar + 256 - sbase));
+  const uint32_t sXch = sBar + 256;            /* [half][parity][quarter] */
   /* accumulator columns per tile and TMEM columns allocated */
   constexpr uint32_t NACC = CYC ? 3*CNN_C : CNN_C;
   constexpr uint32_t TCOLS = CYC ? 256 : CONV_TMEM_COLS;
@@ -703,31 +716,46 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	  tc_mbar_arrive(bTEmpty + 8*acc);
 	  /* rows 32 q - 1 and 32 q + 32 belong to the neighbouring warps
 	   * of this channel half: publish this warp's edge rows */
+	  /* 16-byte shared-memory accesses only: the tensor core's operand
+	   * reads keep the shared-memory banks busy, and each access waits
+	   * its turn (four-byte accesses here cost more than the MMAs) */
 	  const int grp = (warp - 2) >> 2;
 	  const int xb = grp*2 + (i & 1);
-	  float * mine = xch + (xb*4 + q)*32;
-	  /* lanes 31 and 0 each publish and arrive (8 arrivals a phase) */
+	  const uint32_t sx = sXch + (uint32_t) (xb*4)*128u;
+	  /* lanes 31 and 0 each publish and arrive (8 arrivals a phase):
+	   * slot q holds lane 31's D_-1 (bytes 0-63), lane 0's D_+1 (64-127) */
 	  if (lane == 31) {
 	    #pragma unroll
-	    for (int n = 0; n < 16; n++) mine[n] = __uint_as_float(rm[n]);
+	    for (int k = 0; k < 4; k++) {
+	      lds_st4(sx + (uint32_t) q*128u + 16u*k, rm + 4*k);
+	    }
 	    tc_mbar_arrive(bX + 8*xb);
 	  }
 	  if (lane == 0) {
 	    #pragma unroll
-	    for (int n = 0; n < 16; n++) mine[16 + n] = __uint_as_float(rp[n]);
+	    for (int k = 0; k < 4; k++) {
+	      lds_st4(sx + (uint32_t) q*128u + 64u + 16u*k, rp + 4*k);
+	    }
 	    tc_mbar_arrive(bX + 8*xb);
 	  }
 	  const bool okx = tc_mbar_wait(bX + 8*xb, (uint32_t) (i >> 1) & 1u,
 					abort_flag, p.err);
 	  if (!__all_sync(0xffffffffu, okx)) { ok = false; break; }
-	  const float * prev = xch + (xb*4 + ((q + 3) & 3))*32;
-	  const float * next = xch + (xb*4 + ((q + 1) & 3))*32 + 16;
+	  /* lane 0: row 32 q - 1's D_-1; lane 31: row 32 q + 32's D_+1 */
+	  uint32_t ev[16];
+	  if (lane == 0 || lane == 31) {
+	    const uint32_t src = (lane == 0)
+	      ? sx + (uint32_t) ((q + 3) & 3)*128u
+	      : sx + (uint32_t) ((q + 1) & 3)*128u + 64u;
+	    #pragma unroll
+	    for (int k = 0; k < 4; k++) lds_ld4(src + 16u*k, ev + 4*k);
+	  }
 	  #pragma unroll
 	  for (int n = 0; n < 16; n++) {
 	    float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[n]), 1);
 	    float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[n]), 1);
-	    if (lane == 0) dm = prev[n];
-	    if (lane == 31) dp = next[n];
+	    if (lane == 0) dm = __uint_as_float(ev[n]);
+	    if (lane == 31) dp = __uint_as_float(ev[n]);
 	    r[n] = __float_as_uint((__uint_as_float(r[n]) + dm) + dp);
 	  }
 	}

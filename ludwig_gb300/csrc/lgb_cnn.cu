@@ -1066,29 +1066,52 @@ extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
  *****************************************************************************/
 
 /* Periodic halo of a padded-row buffer: one thread per (halo row, 16 B) */
+/* Periodic images of the padded rows: only the halo rows are visited, as
+ * three disjoint sets (the two x faces whole; the two y faces for interior
+ * x; the two z faces for interior x and y), 4 threads (16 bytes each) per
+ * row; each image is copied from its interior source row. */
 __global__ void k_cnn_halo(lgbk_cnn_geom_t g, uint4 * __restrict__ p) {
   const long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  if (i >= g.rows*4) return;
-  const long long row = i >> 2;
-  const int q = (int) (i & 3);
   const int Z = g.nz + 2, Y = g.ny + 2;
-  const int zp = (int) (row % Z);
-  const long long r = row / Z;
-  const int yp = (int) (r % Y);
-  const int xp = (int) (r / Y);
-  const bool halo = (xp == 0 || xp == g.nx + 1 || yp == 0 || yp == g.ny + 1
-		     || zp == 0 || zp == g.nz + 1);
-  if (!halo) return;
+  const long long nxf = 2LL*Y*Z, nyf = 2LL*g.nx*Z, nzf = 2LL*g.nx*g.ny;
+  const long long h = i >> 2;
+  const int q = (int) (i & 3);
+  int xp, yp, zp;
+  if (h < nxf) {
+    zp = (int) (h % Z);
+    const long long r = h / Z;
+    yp = (int) (r % Y);
+    xp = (r / Y) ? g.nx + 1 : 0;
+  }
+  else if (h < nxf + nyf) {
+    const long long k = h - nxf;
+    zp = (int) (k % Z);
+    const long long r = k / Z;
+    xp = 1 + (int) (r % g.nx);
+    yp = (r / g.nx) ? g.ny + 1 : 0;
+  }
+  else if (h < nxf + nyf + nzf) {
+    const long long k = h - nxf - nyf;
+    yp = 1 + (int) (k % g.ny);
+    const long long r = k / g.ny;
+    xp = 1 + (int) (r % g.nx);
+    zp = (r / g.nx) ? g.nz + 1 : 0;
+  }
+  else {
+    return;
+  }
   const int x = (xp - 1 + g.nx) % g.nx;
   const int y = (yp - 1 + g.ny) % g.ny;
   const int z = (zp - 1 + g.nz) % g.nz;
+  const long long row = ((long long) xp*Y + yp)*Z + zp;
   const long long src = ((long long) (x + 1)*Y + (y + 1))*Z + (z + 1);
   p[row*4 + q] = p[src*4 + q];
 }
 
 extern "C" int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p,
 			     void * stream) {
-  const long long n = g->rows*4;
+  const long long Z = g->nz + 2, Y = g->ny + 2;
+  const long long n = 4*(2*Y*Z + 2LL*g->nx*Z + 2LL*g->nx*g->ny);
   k_cnn_halo<<<(unsigned int) ((n + 255)/256), 256, 0,
     (cudaStream_t) stream>>>(*g, (uint4 *) p);
   return (int) cudaGetLastError();

@@ -1042,21 +1042,244 @@ __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
   dw[k] = (float) s;
 }
 
+/*****************************************************************************
+ *  k_wgrad_line: the weight gradient for nz a multiple of 128, reusing
+ *  gradient lines as k_conv3_line reuses activation lines.
+ *
+ *  dW[t][co][ci] = sum_s g(s - e_t)[co] x(s)[ci].  A CTA walks runs of
+ *  tiles along y (128 sites in z at fixed x, y); per tile the x rows are
+ *  one box (B: N = 32 input channels, K = sites), and the gradient is read
+ *  from the 9 lines (x - dx, y - dy) of 130 rows held in a ring (three
+ *  new lines per tile, 64-byte swizzled rows).  One MMA takes, as its
+ *  M = 128 rows, the three dx lines of one (dy, dz) side by side (the dx
+ *  banks of the ring are a constant stride apart: the leading byte offset
+ *  of an MN-major operand) plus a fourth bank that holds no data (its
+ *  accumulator rows are not read), with the z shift as a start offset of
+ *  1 - dz rows in the swizzled lines.  9 (dy, dz) groups x 8 K steps per
+ *  tile; the accumulators (9 x 32 TMEM columns) hold the CTA's sums over
+ *  all its tiles and are written once at the end.
+ *****************************************************************************/
+
+#define WL_NY      5                    /* y-line slots per dx bank */
+#define WL_XST     2                    /* x-row tile stages */
+#define WL_BANK    (WL_NY*LN_SLOT)      /* bytes per dx bank */
+#define WL_THREADS 192
+#define WL_TMEM_COLS 512
+#define WL_SMEM (1024 + 4*WL_BANK + WL_XST*TILEB + 256)
+
+template <int DUMMY>
+__global__ void __launch_bounds__(WL_THREADS, 1)
+k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
+	     const __grid_constant__ CUtensorMap tm_x, const WgP p) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc_smem_u32(smem_raw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t * sgen = smem_raw + (sbase - raw);
+
+  const uint32_t sL = sbase;                    /* 4 dx banks (the 4th empty) */
+  const uint32_t sX = sL + 4*WL_BANK;
+  const uint32_t sBar = sX + WL_XST*TILEB;
+  const uint32_t bFull = sBar;                  /* WL_NY */
+  const uint32_t bRel = sBar + 8*WL_NY;         /* WL_NY */
+  const uint32_t bXFull = sBar + 16*WL_NY;      /* WL_XST */
+  const uint32_t bXEmpty = bXFull + 8*WL_XST;   /* WL_XST */
+  const uint32_t bDone = bXEmpty + 8*WL_XST;
+  uint32_t * tslot = (uint32_t *) (sgen + (bDone + 8 - sbase));
+  volatile int * abort_flag = (volatile int *) (sgen + (bDone + 12 - sbase));
+
+  const int warp = threadIdx.x/32;
+  const int lane = threadIdx.x % 32;
+  const lgbk_cnn_geom_t & g = p.g;
+  const int nitems = line_items(g);
+
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < WL_NY; k++) {
+      tc_mbar_init(bFull + 8*k, 1);
+      tc_mbar_init(bRel + 8*k, 1);
+    }
+    for (int k = 0; k < WL_XST; k++) {
+      tc_mbar_init(bXFull + 8*k, 1);
+      tc_mbar_init(bXEmpty + 8*k, 1);
+    }
+    tc_mbar_init(bDone, 1);
+    *abort_flag = 0;
+    tc_fence_barrier_init();
+  }
+  if (warp == 1) tc_tmem_alloc(tc_smem_u32(tslot), WL_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    tc_prefetch_map(&tm_gline);
+    tc_prefetch_map(&tm_x);
+    uint32_t sq = 0, nx = 0;           /* gradient lines and x tiles loaded */
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; ok && y < yb; y++) {
+	/* x rows of the tile */
+	const uint32_t xs = nx % WL_XST;
+	if (nx >= WL_XST &&
+	    !tc_mbar_wait(bXEmpty + 8*xs, (nx/WL_XST - 1u) & 1u, abort_flag,
+			  p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_mbar_arrive_tx(bXFull + 8*xs, TILEB);
+	tc_tma_load_2d(sX + xs*TILEB, &tm_x, bXFull + 8*xs, 0,
+		       prow(g, x, y, z0));
+	nx++;
+	/* gradient lines y - 1 .. y + 1 (a new run) or y + 1 */
+	const bool first = (y == ya);
+	for (int li = 0; li < (first ? 3 : 1); li++, sq++) {
+	  const int yy = first ? (y - 1 + li) : (y + 1);
+	  const uint32_t r = sq % WL_NY;
+	  if (sq >= WL_NY &&
+	      !tc_mbar_wait(bRel + 8*r, (sq/WL_NY - 1u) & 1u, abort_flag,
+			    p.err)) {
+	    ok = false;
+	    break;
+	  }
+	  tc_mbar_arrive_tx(bFull + 8*r, 3*LN_ROWS*ROWB);
+	  for (int dxi = 0; dxi < 3; dxi++) {
+	    tc_tma_load_2d(sL + (uint32_t) dxi*WL_BANK + r*LN_SLOT, &tm_gline,
+			   bFull + 8*r, 0, prow(g, x + dxi - 1, yy, z0 - 1));
+	  }
+	}
+      }
+    }
+    for (uint32_t k = 0; k < WL_XST && k < nx; k++) {
+      const uint32_t nf = (nx - k + WL_XST - 1)/WL_XST;
+      tc_drain_wait(bXFull + 8*k, (nf - 1u) & 1u, p.err);
+    }
+    for (uint32_t k = 0; k < WL_NY && k < sq; k++) {
+      const uint32_t nf = (sq - k + WL_NY - 1)/WL_NY;
+      tc_drain_wait(bFull + 8*k, (nf - 1u) & 1u, p.err);
+    }
+  }
+  else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 1, 1);
+    const uint64_t ad0 = tc_sdesc(sL, WL_BANK, 512, LGB_TC_SWIZZLE_64B);
+    const uint64_t bd0 = tc_sdesc(sX, TILEB, 512, LGB_TC_SWIZZLE_64B);
+    const uint32_t alo0 = (uint32_t) ad0, ahi = (uint32_t) (ad0 >> 32);
+    const uint32_t blo0 = (uint32_t) bd0, bhi = (uint32_t) (bd0 >> 32);
+    uint32_t sq = 0, nx = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; y < yb; y++) {
+	const bool first = (y == ya), last = (y == yb - 1);
+	const uint32_t xs = nx % WL_XST;
+	ok = tc_mbar_wait(bXFull + 8*xs, (nx/WL_XST) & 1u, abort_flag, p.err);
+	for (int li = 0; ok && li < (first ? 3 : 1); li++, sq++) {
+	  ok = tc_mbar_wait(bFull + 8*(sq % WL_NY), (sq/WL_NY) & 1u,
+			    abort_flag, p.err);
+	}
+	if (!ok) break;
+	tc_fence_after();
+	/* ring slots of the lines y - 1, y, y + 1 (dy = 1, 0, -1) */
+	const uint32_t rr[3] = {(sq - 3u) % WL_NY, (sq - 2u) % WL_NY,
+				(sq - 1u) % WL_NY};
+	const uint32_t bx = blo0 + xs*(TILEB >> 4);
+	#pragma unroll
+	for (int j = 0; j < 3; j++) {
+	  const uint32_t aj = alo0 + rr[j]*(LN_SLOT >> 4);
+	  #pragma unroll
+	  for (int dzi = 0; dzi < 3; dzi++) {
+	    /* z shift dz = dzi - 1: rows from 1 - dz = 2 - dzi */
+	    const uint32_t a = aj + (uint32_t) ((2 - dzi)*ROWB >> 4);
+	    const uint32_t d = tmem + (uint32_t) ((3*j + dzi)*CNN_C);
+	    #pragma unroll
+	    for (int k = 0; k < LGBK_CNN_TILE/16; k++) {
+	      tc_mma_bf16_w(d, a + k*(1024 >> 4), ahi, bx + k*(1024 >> 4), bhi,
+			    idesc, (uint32_t) ((nx | k) != 0));
+	    }
+	  }
+	}
+	tc_commit(bXEmpty + 8*xs);
+	nx++;
+	tc_commit(bRel + 8*rr[0]);
+	if (last) {
+	  tc_commit(bRel + 8*rr[1]);
+	  tc_commit(bRel + 8*rr[2]);
+	}
+      }
+    }
+    tc_commit(bDone);
+    tc_drain_wait(bDone, 0, p.err);
+  }
+  else if (warp >= 2) {
+    /* warp w reads TMEM lanes 32 q .. (q = w % 4): bank q = dx 1 - q */
+    const int q = warp & 3;
+    bool okw = tc_mbar_wait(bDone, 0, abort_flag, p.err);
+    if (__all_sync(0xffffffffu, okw) && q < 3) {
+      tc_fence_after();
+      for (int j = 0; j < 3; j++) {
+	for (int dzi = 0; dzi < 3; dzi++) {
+	  uint32_t r[32];
+	  tc_tmem_ld32(tmem + (uint32_t) ((3*j + dzi)*CNN_C)
+		       + ((uint32_t) (q*32) << 16), r);
+	  /* dx = 1 - q, dy = 1 - j, dz = dzi - 1 */
+	  const int t = (2 - q)*9 + (2 - j)*3 + dzi;
+	  float4 * o = (float4 *) (p.part + (((long long) blockIdx.x*CNN_NTAP
+					      + t)*CNN_C + lane)*CNN_C);
+	  #pragma unroll
+	  for (int k = 0; k < 8; k++) {
+	    o[k] = make_float4(__uint_as_float(r[4*k]),
+			       __uint_as_float(r[4*k + 1]),
+			       __uint_as_float(r[4*k + 2]),
+			       __uint_as_float(r[4*k + 3]));
+	  }
+	}
+      }
+    }
+    else if (q == 3) {
+      /* the fourth bank's rows hold no tap; the TMEM loads above are
+       * warp-collective per quarter, so this warp has nothing to do */
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    tc_fence_after();
+    tc_tmem_dealloc(tmem, WL_TMEM_COLS);
+  }
+}
+
 extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
-			      const void * tm_x, float * part, float * dw,
-			      int * err, void * stream) {
+			      const void * tm_gline, const void * tm_x,
+			      float * part, float * dw, int * err,
+			      void * stream) {
   WgP p;
   p.g = *g;
   p.part = part;
   p.err = err;
-  const CUtensorMap mg = *(const CUtensorMap *) tm_g;
   const CUtensorMap mx = *(const CUtensorMap *) tm_x;
   cudaStream_t s = (cudaStream_t) stream;
-  const int grid = lgbk_cnn_wgrad_blocks(g);
-  cudaError_t e = cudaFuncSetAttribute(k_wgrad_tc,
-    cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
-  if (e != cudaSuccess) return (int) e;
-  k_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(mg, mx, p);
+  int grid = lgbk_cnn_wgrad_blocks(g);
+  cudaError_t e;
+  if (tm_gline && g->bz == LGBK_CNN_TILE && g->lpt == 1) {
+    const CUtensorMap ml = *(const CUtensorMap *) tm_gline;
+    const int items = line_items(*g);
+    if (grid > items) grid = items;
+    e = cudaFuncSetAttribute(k_wgrad_line<0>,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, WL_SMEM);
+    if (e != cudaSuccess) return (int) e;
+    k_wgrad_line<0><<<grid, WL_THREADS, WL_SMEM, s>>>(ml, mx, p);
+  }
+  else {
+    const CUtensorMap mg = *(const CUtensorMap *) tm_g;
+    e = cudaFuncSetAttribute(k_wgrad_tc,
+      cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
+    if (e != cudaSuccess) return (int) e;
+    k_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(mg, mx, p);
+  }
   k_wgrad_reduce<<<(LGBK_CNN_WL + 255)/256, 256, 0, s>>>(part, grid, dw);
   return (int) cudaGetLastError();
 }
@@ -1065,7 +1288,6 @@ extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
  *  Elementwise kernels
  *****************************************************************************/
 
-/* Periodic halo of a padded-row buffer: one thread per (halo row, 16 B) */
 /* Periodic images of the padded rows: only the halo rows are visited, as
  * three disjoint sets (the two x faces whole; the two y faces for interior
  * x; the two z faces for interior x and y), 4 threads (16 bytes each) per

@@ -433,8 +433,9 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
   if (rc) return ck(rc, "cnn loss");
   for (int l = NL - 1; l >= 0; l--) {
     /* dL/dz_{l+1} is in gpad[l+1]; the layer input is act[l] */
-    rc = lgbk_cnn_wgrad(g, &m->tm_g[l + 1], &m->tm_act[l], m->part,
-			m->grads + l*PL, m->err_dev, s);
+    rc = lgbk_cnn_wgrad(g, &m->tm_g[l + 1],
+			m->line_on ? &m->tm_gs[l + 1] : NULL, &m->tm_act[l],
+			m->part, m->grads + l*PL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_bias_grad(g, m->gpad[l + 1], m->red,
 				     m->grads + l*PL + WL, s);
     if (rc) return ck(rc, "cnn wgrad");
@@ -650,8 +651,9 @@ int ludwig_gb_cnn_wgrad3(ludwig_gb_cnn_t * m, const float * gr,
   cudaStream_t s = lib_stream();
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
   if (!rc) rc = lgbk_cnn_pack_rows(&m->g, gr, m->gpad[1], s);
-  if (!rc) rc = lgbk_cnn_wgrad(&m->g, &m->tm_g[1], &m->tm_act[0], m->part,
-			       dw, m->err_dev, s);
+  if (!rc) rc = lgbk_cnn_wgrad(&m->g, &m->tm_g[1],
+			       m->line_on ? &m->tm_gs[1] : NULL, &m->tm_act[0],
+			       m->part, dw, m->err_dev, s);
   if (rc) return ck(rc, "cnn_wgrad3");
   rc = check_err(m);
   if (!rc) rc = ck(cudaStreamSynchronize(s), "sync");

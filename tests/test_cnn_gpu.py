@@ -102,12 +102,18 @@ def test_conv3_backward_data(gb, orc, n):
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("n", [(4, 4, 32), (2, 4, 64), (2, 2, 256),
-                               (64, 32, 64)])
-def test_conv3_weight_gradient(gb, orc, n):
+@pytest.mark.parametrize("n,line", [((4, 4, 32), 1), ((2, 4, 64), 1),
+                                    ((2, 2, 256), 1), ((64, 32, 64), 1),
+                                    ((2, 2, 256), 0), ((2, 2, 128), 1),
+                                    ((8, 40, 128), 1), ((3, 17, 128), 1)])
+def test_conv3_weight_gradient(gb, orc, n, line):
+    """Per-tap kernel, and for nz a multiple of 128 the line-reuse kernel
+    (gradient lines in a ring, the three dx lines of a (dy, dz) as one
+    MMA's rows; runs of one to 16 tiles along y, several per CTA)."""
     rng = np.random.default_rng(12)
     N = n[0] * n[1] * n[2]
     m = gb.Corrector(n)
+    m.line_reuse(line)
     g = bf(orc, rng.standard_normal((N, 32)))
     a = bf(orc, rng.standard_normal((N, 32)))
     dw = torch.empty((27, 32, 32), dtype=torch.float32, device="cuda")

@@ -1476,17 +1476,29 @@ __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ 
   #pragma unroll
   for (int k = 0; k < 8; k++) acc[k] = 0.0f;
   const int nlines = g.nx*g.ny;
-  for (int ln = blockIdx.x; ln < nlines; ln += gridDim.x) {
-    const int x = ln / g.ny, y = ln % g.ny;
-    const uint8_t * base = pg + (long long) prow(g, x, y, 0)*ROWB;
+  /* four lines at a time, their loads issued before any is summed */
+  for (int l0 = blockIdx.x; l0 < nlines; l0 += 4*gridDim.x) {
     for (int z = r0; z < g.nz; z += 64) {
-      const uint4 u = *(const uint4 *) (base + (long long) z*ROWB + 16*cg);
-      const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+      uint4 u[4];
       #pragma unroll
-      for (int k = 0; k < 4; k++) {
-	const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
-	acc[2*k] += f.x;
-	acc[2*k + 1] += f.y;
+      for (int j = 0; j < 4; j++) {
+	const int ln = l0 + j*gridDim.x;
+	u[j] = make_uint4(0u, 0u, 0u, 0u);
+	if (ln < nlines) {
+	  const int x = ln / g.ny, y = ln % g.ny;
+	  u[j] = *(const uint4 *) (pg + ((long long) prow(g, x, y, z)*ROWB
+					 + 16*cg));
+	}
+      }
+      #pragma unroll
+      for (int j = 0; j < 4; j++) {
+	const uint32_t w[4] = {u[j].x, u[j].y, u[j].z, u[j].w};
+	#pragma unroll
+	for (int k = 0; k < 4; k++) {
+	  const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
+	  acc[2*k] += f.x;
+	  acc[2*k + 1] += f.y;
+	}
       }
     }
   }
@@ -1501,13 +1513,22 @@ __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ 
   }
 }
 
+/* 256 threads: thread (j, c) sums the partials b = j, j + 8, ... of
+ * channel c, then thread c adds the eight in order j = 0 .. 7 */
 __global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
 				 float * __restrict__ db) {
-  const int c = threadIdx.x;
-  if (c >= 32) return;
+  __shared__ double red[8][32];
+  const int c = threadIdx.x & 31, j = threadIdx.x >> 5;
   double s = 0.0;
-  for (int b = 0; b < nblk; b++) s += part[b*32 + c];
-  db[c] = (float) s;
+  for (int b = j; b < nblk; b += 8) s += part[b*32 + c];
+  red[j][c] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    #pragma unroll
+    for (int k = 0; k < 8; k++) t += red[k][c];
+    db[c] = (float) t;
+  }
 }
 
 extern "C" int lgbk_cnn_bias_grad(const lgbk_cnn_geom_t * g, const void * pg,
@@ -1515,7 +1536,7 @@ extern "C" int lgbk_cnn_bias_grad(const lgbk_cnn_geom_t * g, const void * pg,
   cudaStream_t s = (cudaStream_t) stream;
   k_cnn_bias_part<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, (const uint8_t *) pg,
 						       part);
-  k_cnn_bias_final<<<1, 32, 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
+  k_cnn_bias_final<<<1, 256, 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
   return (int) cudaGetLastError();
 }
 

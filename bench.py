@@ -515,6 +515,8 @@ def gpu_arm(args):
             ncs = 128 ** 3
             cnn = {"forward_ms": fwd,
                    "train_step_ms": d["train_step_ms"],
+                   "forward_call_ms": d["forward_call_ms"],
+                   "train_step_call_ms": d["train_step_call_ms"],
                    "forward_tflops": d["forward_tflops"],
                    "forward_tflops_useful":
                        CNN_USEFUL_FLOP * ncs / (fwd * 1e-3) / 1e12,
@@ -525,8 +527,10 @@ def gpu_arm(args):
                    "unit_note": "forward_tflops: executed BF16 MMA work "
                                 "(layers of 32x32 channels, the first "
                                 "with 16 input channels) / wall time per "
-                                "call; forward_tflops_useful: the real "
-                                "layer shapes 5-32-32-32-4",
+                                "pass, passes issued back to back; "
+                                "forward_tflops_useful: the real layer "
+                                "shapes 5-32-32-32-4; *_call_ms: one call "
+                                "and one host check per pass",
                    "workload": "4-layer 3x3x3 conv net, 32 channels, 128^3 "
                                "coarse lattice, tcgen05 BF16 / FP32"}
         except ImportError as exc:                   # torch missing

@@ -799,6 +799,12 @@ int ludwig_gb_cnn_scales_get(ludwig_gb_cnn_t * cnn, float in_off[5],
 			     float in_scale[5], float out_scale[4]);
 int ludwig_gb_cnn_forward(ludwig_gb_cnn_t * cnn, const float * d_in5,
 			  float * d_out4);
+/* n forward passes issued back to back on the library's stream (inputs
+ * and outputs: n device pointers each); the error word of the tensor-core
+ * kernels is read once, after the last */
+int ludwig_gb_cnn_forward_n(ludwig_gb_cnn_t * cnn, int n,
+			    const float * const * d_in5,
+			    float * const * d_out4);
 /* loss = (1/N) sum over sites and 4 outputs of (out4 - t4)^2 and its
  * gradient (no update) */
 int ludwig_gb_cnn_loss_grad(ludwig_gb_cnn_t * cnn, const float * d_in5,

@@ -354,6 +354,7 @@ def _declare(L):
         "ludwig_gb_cnn_scales_set": ([_P, _F, _F, _F], ctypes.c_int),
         "ludwig_gb_cnn_scales_get": ([_P, _F, _F, _F], ctypes.c_int),
         "ludwig_gb_cnn_forward": ([_P, _P, _P], ctypes.c_int),
+        "ludwig_gb_cnn_forward_n": ([_P, ctypes.c_int, pp, pp], ctypes.c_int),
         "ludwig_gb_cnn_loss_grad": ([_P, _P, _P, _D], ctypes.c_int),
         "ludwig_gb_cnn_train_step": ([_P, _P, _P, ctypes.c_double, _D],
                                      ctypes.c_int),
@@ -1359,6 +1360,22 @@ class Corrector(_Obj):
 
     def forward(self, in5, out4):
         _check(lib().ludwig_gb_cnn_forward(self.ptr, in5, out4), "forward")
+
+    def forward_n(self, in5s, out4s):
+        """Several forward passes back to back (device pointers), one error
+        check after the last."""
+        n = len(in5s)
+        a = (ctypes.c_void_p * max(n, 1))(*in5s)
+        b = (ctypes.c_void_p * max(n, 1))(*out4s)
+        _check(lib().ludwig_gb_cnn_forward_n(self.ptr, n, a, b), "forward_n")
+
+    def train_steps(self, in5s, t4s, lr):
+        """Several Adam steps back to back without reading the losses."""
+        n = len(in5s)
+        a = (ctypes.c_void_p * max(n, 1))(*in5s)
+        b = (ctypes.c_void_p * max(n, 1))(*t4s)
+        _check(lib().ludwig_gb_cnn_train_steps(self.ptr, n, a, b, float(lr),
+                                               None), "train_steps")
 
     def loss_grad(self, in5, t4):
         loss = ctypes.c_double()

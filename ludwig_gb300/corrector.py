@@ -250,8 +250,10 @@ def rollout(model, nfine, seed, t0, ncoarse_steps, every, params=FINE_PARAMS,
 
 
 def time_network(model, x, t, reps=20):
-    """Wall time of one forward pass and of one training step (forward,
-    backward, Adam) on one pair, and the tensor-core work they carry."""
+    """Time per forward pass and per training step (forward, backward,
+    Adam) on one pair, issued back to back (`forward_n`, `train_steps`:
+    one error check per batch), the same with one call and one host check
+    per pass ("call"), and the tensor-core work they carry."""
     torch = _torch()
     out = torch.empty_like(t)
     model.forward(x.data_ptr(), out.data_ptr())
@@ -260,12 +262,20 @@ def time_network(model, x, t, reps=20):
     for _ in range(reps):
         model.forward(x.data_ptr(), out.data_ptr())
     sync()
+    fwd_call = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    model.forward_n([x.data_ptr()] * reps, [out.data_ptr()] * reps)
+    sync()
     fwd = (time.perf_counter() - t0) / reps
     lr = 1e-12
     model.train_step(x.data_ptr(), t.data_ptr(), lr)
     t0 = time.perf_counter()
     for _ in range(reps):
         model.train_step(x.data_ptr(), t.data_ptr(), lr)
+    sync()
+    step_call = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    model.train_steps([x.data_ptr()] * reps, [t.data_ptr()] * reps, lr)
     sync()
     step = (time.perf_counter() - t0) / reps
     n = model.nsites
@@ -276,9 +286,13 @@ def time_network(model, x, t, reps=20):
     flop_fwd = 3.5 * flop_conv
     flop_step = flop_fwd + 3 * flop_conv + 4 * flop_conv * 28.0 / 27.0
     return {"sites": n, "forward_ms": 1e3 * fwd, "train_step_ms": 1e3 * step,
+            "forward_call_ms": 1e3 * fwd_call,
+            "train_step_call_ms": 1e3 * step_call,
             "forward_tflops": flop_fwd / fwd / 1e12,
             "train_step_tflops": flop_step / step / 1e12,
-            "note": "wall time incl. the host round trip of each call"}
+            "note": "forward_ms, train_step_ms: wall time per pass of a "
+                    "batch issued back to back; *_call_ms: one call and "
+                    "one host check per pass"}
 
 
 def bench(n, reps=20):

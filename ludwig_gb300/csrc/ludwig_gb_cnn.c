@@ -473,6 +473,26 @@ int ludwig_gb_cnn_forward(ludwig_gb_cnn_t * m, const float * in5,
   return rc;
 }
 
+int ludwig_gb_cnn_forward_n(ludwig_gb_cnn_t * m, int n,
+			    const float * const * in5,
+			    float * const * out4) {
+  if (m == NULL || n < 0 || (n > 0 && (in5 == NULL || out4 == NULL))) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_forward_n");
+  }
+  const size_t N = (size_t) m->g.nsites;
+  for (int k = 0; k < n; k++) {
+    if (in5[k] == NULL || out4[k] == NULL) {
+      return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_forward_n: pointer");
+    }
+    int rc = forward(m, in5[k], in5[k] + N, in5[k] + 4*N, 0);
+    if (!rc) rc = ck(cudaMemcpyAsync(out4[k], m->out4, sizeof(float)*4*N,
+				     cudaMemcpyDeviceToDevice, lib_stream()),
+		     "out4");
+    if (rc) return rc;
+  }
+  return check_err(m);
+}
+
 int ludwig_gb_cnn_loss_grad(ludwig_gb_cnn_t * m, const float * in5,
 			    const float * t4, double * loss) {
   if (m == NULL || in5 == NULL || t4 == NULL) {

@@ -295,3 +295,18 @@ def test_rollout_pairs(trained, gb):
     gb.fields_restrict(fine, y.data_ptr(), nc)
     gb.sync()
     assert torch.equal(x, X2[1]) and torch.equal(y, Y2[1])
+
+
+def test_forward_n_matches_forward(trained):
+    """Forward passes issued back to back give what single calls give."""
+    cr, m, _, _ = trained
+    N = m.nsites
+    rng = np.random.default_rng(3)
+    xs = [dev(0.1 * rng.standard_normal((5, N))) for _ in range(3)]
+    outs = [torch.empty((4, N), dtype=torch.float32, device="cuda")
+            for _ in range(3)]
+    m.forward_n([x.data_ptr() for x in xs], [o.data_ptr() for o in outs])
+    for x, o in zip(xs, outs):
+        ref = torch.empty_like(o)
+        m.forward(x.data_ptr(), ref.data_ptr())
+        assert torch.equal(ref, o)

@@ -396,10 +396,11 @@ static int kin_of(int l) {
   return (l == 0 && LGBK_CNN_NIN <= 16) ? 16 : LGBK_CNN_C;
 }
 
-/* a_0 from [phi, u, rho] pointers, then the four layers -> out4; the
- * pre-activations z (for the backward pass) are stored only when train */
+/* a_0 from [phi, u, rho] pointers, then the four layers -> out (m->out4
+ * when NULL); the pre-activations z (for the backward pass) are stored
+ * only when train */
 static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
-		   const float * rho, int train) {
+		   const float * rho, int train, float * out) {
   cudaStream_t s = lib_stream();
   const lgbk_cnn_geom_t * g = &m->g;
   int rc = lgbk_cnn_features(g, phi, u, rho, m->in_off, m->in_scale,
@@ -417,7 +418,7 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
     else {
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l), &m->tm_act[l],
 			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL, NULL,
-			 NULL, m->out4, m->err_dev, s);
+			 NULL, out ? out : m->out4, m->err_dev, s);
     }
     if (rc) return ck(rc, "cnn conv");
   }
@@ -465,10 +466,7 @@ int ludwig_gb_cnn_forward(ludwig_gb_cnn_t * m, const float * in5,
     return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_forward");
   }
   const size_t N = (size_t) m->g.nsites;
-  int rc = forward(m, in5, in5 + N, in5 + 4*N, 0);
-  if (!rc) rc = ck(cudaMemcpyAsync(out4, m->out4, sizeof(float)*4*N,
-				   cudaMemcpyDeviceToDevice, lib_stream()),
-		   "out4");
+  int rc = forward(m, in5, in5 + N, in5 + 4*N, 0, out4);
   if (!rc) rc = check_err(m);
   return rc;
 }
@@ -484,10 +482,7 @@ int ludwig_gb_cnn_forward_n(ludwig_gb_cnn_t * m, int n,
     if (in5[k] == NULL || out4[k] == NULL) {
       return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_forward_n: pointer");
     }
-    int rc = forward(m, in5[k], in5[k] + N, in5[k] + 4*N, 0);
-    if (!rc) rc = ck(cudaMemcpyAsync(out4[k], m->out4, sizeof(float)*4*N,
-				     cudaMemcpyDeviceToDevice, lib_stream()),
-		     "out4");
+    int rc = forward(m, in5[k], in5[k] + N, in5[k] + 4*N, 0, out4[k]);
     if (rc) return rc;
   }
   return check_err(m);
@@ -499,7 +494,7 @@ int ludwig_gb_cnn_loss_grad(ludwig_gb_cnn_t * m, const float * in5,
     return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_loss_grad");
   }
   const size_t N = (size_t) m->g.nsites;
-  int rc = forward(m, in5, in5 + N, in5 + 4*N, 1);
+  int rc = forward(m, in5, in5 + N, in5 + 4*N, 1, NULL);
   if (!rc) rc = backward(m, t4);
   if (!rc) rc = read_loss(m, loss);
   return rc;
@@ -521,7 +516,7 @@ int ludwig_gb_cnn_train_step(ludwig_gb_cnn_t * m, const float * in5,
     return lgb_internal_err(LUDWIG_GB_EINVAL, "cnn_train_step");
   }
   const size_t N = (size_t) m->g.nsites;
-  int rc = forward(m, in5, in5 + N, in5 + 4*N, 1);
+  int rc = forward(m, in5, in5 + N, in5 + 4*N, 1, NULL);
   if (!rc) rc = backward(m, t4);
   if (!rc) rc = adam(m, lr);
   if (!rc) rc = read_loss(m, loss);
@@ -538,7 +533,7 @@ int ludwig_gb_cnn_train_steps(ludwig_gb_cnn_t * m, int nsteps,
   }
   const size_t N = (size_t) m->g.nsites;
   for (int k = 0; k < nsteps; k++) {
-    int rc = forward(m, in5[k], in5[k] + N, in5[k] + 4*N, 1);
+    int rc = forward(m, in5[k], in5[k] + N, in5[k] + 4*N, 1, NULL);
     if (!rc) rc = backward(m, t4[k]);
     if (!rc) rc = adam(m, lr);
     if (!rc && losses) rc = read_loss(m, losses + k);
@@ -562,7 +557,7 @@ int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * m, lb_t * lb, field_t * phi,
   }
   const size_t N = (size_t) m->g.nsites;
   rc = forward(m, (const float *) v.phi, (const float *) v.u,
-	       (const float *) v.rho, 0);
+	       (const float *) v.rho, 0, NULL);
   if (rc) return rc;
   rc = lgbk_cnn_apply(&m->g, m->out4, m->out_scale, (float *) v.phi,
 		      (float *) v.u, (float *) v.f, (const float *) v.rho,

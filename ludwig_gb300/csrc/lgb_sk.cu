@@ -4,9 +4,10 @@
  *
  *  Spherically averaged structure factor S(|k|) of a scalar field and the
  *  domain length L = 2 pi sum S dk / sum k S dk (util/length_from_sk.c:
- *  88-190).  The 3-d transform is three passes of direct 1-d DFTs (one
- *  line per CTA, twiddles from a table), accurate in FP64 accumulation;
- *  this is a diagnostic computed between steps, not part of the step.
+ *  88-190).  The 3-d transform is three passes of 1-d transforms (one
+ *  line per CTA, twiddles from a table; radix-2 FFT for power-of-two
+ *  lengths, the direct sum otherwise), in FP64; this is a diagnostic
+ *  computed between steps, not part of the step.
  *
  *  Binning follows the reference: half space k_z in [0, N/2], 128 bins of
  *  width sqrt(3) pi / 128.  With faithful = 1 the bin of each wavevector
@@ -27,7 +28,11 @@
 
 /* One 1-d DFT along axis `axis` for every line: out[k] = sum_n in[n] w^kn,
  * w = exp(-2 pi i / n).  in/out: complex double2 arrays in the canonical
- * site order.  One CTA per line; the line is staged in shared memory. */
+ * site order.  One CTA per line; the line is staged in shared memory.
+ * A power-of-two length is transformed by the radix-2 Cooley-Tukey FFT
+ * (the line loaded in bit-reversed order, log2 n stages of butterflies
+ * with the twiddles w^(j n/m) of the table); other lengths by the direct
+ * sum. */
 __global__ void k_dft_axis(lgbk_dims_t d, int axis,
 			   const double2 * __restrict__ in,
 			   double2 * __restrict__ out,
@@ -45,6 +50,35 @@ __global__ void k_dft_axis(lgbk_dims_t d, int axis,
     base = x*(long long) d.ny*d.nz + z;
   }
   else base = li;                        /* x-lines: li = y*nz + z */
+
+  if (n > 1 && (n & (n - 1)) == 0) {
+    int lg = 0;
+    while ((1 << lg) < n) lg++;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int r = (int) (__brev((unsigned int) i) >> (32 - lg));
+      line[r] = in[base + i*stride];
+    }
+    __syncthreads();
+    for (int half = 1; half < n; half *= 2) {
+      const int step = n/(2*half);       /* twiddle index stride */
+      for (int b = threadIdx.x; b < n/2; b += blockDim.x) {
+	const int j = b % half;
+	const int i0 = (b / half)*2*half + j;
+	const int i1 = i0 + half;
+	const double2 w = tw[j*step];
+	const double2 v = line[i1];
+	const double2 t = make_double2(v.x*w.x - v.y*w.y, v.x*w.y + v.y*w.x);
+	const double2 u = line[i0];
+	line[i0] = make_double2(u.x + t.x, u.y + t.y);
+	line[i1] = make_double2(u.x - t.x, u.y - t.y);
+      }
+      __syncthreads();
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      out[base + k*stride] = line[k];
+    }
+    return;
+  }
 
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     line[i] = in[base + i*stride];
@@ -115,22 +149,40 @@ __device__ int bin_corrected(const lgbk_dims_t & d, int ii, int j, int k) {
 			       __dmul_rn(__dsqrt_rn(3.0), pi)));
 }
 
+/* Bins of the half-space wavevectors: each CTA sums its sites into
+ * shared-memory bins, then adds those to the global bins (one atomic per
+ * bin and CTA instead of one per site) */
 __global__ void k_bin_sk(lgbk_dims_t d, int faithful,
 			 const double2 * __restrict__ c,
 			 double * __restrict__ sk, double * __restrict__ nk) {
-  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  __shared__ double ssk[LGBK_SK_NBIN], snk[LGBK_SK_NBIN];
+  for (int b = threadIdx.x; b < LGBK_SK_NBIN; b += blockDim.x) {
+    ssk[b] = 0.0;
+    snk[b] = 0.0;
+  }
+  __syncthreads();
   const int nzh = d.nz/2 + 1;
-  long long nh = (long long) d.nx*d.ny*nzh;
-  if (i >= nh) return;
-  int k = (int) (i % nzh);
-  long long r = i / nzh;
-  int j = (int) (r % d.ny);
-  int ii = (int) (r / d.ny);
-  int n = faithful ? bin_reference(d, ii, j, k) : bin_corrected(d, ii, j, k);
-  if (n >= LGBK_SK_NBIN) n = LGBK_SK_NBIN - 1;
-  const double2 v = c[((long long) ii*d.ny + j)*d.nz + k];
-  atomicAdd(sk + n, v.x*v.x + v.y*v.y);
-  atomicAdd(nk + n, 1.0);
+  const long long nh = (long long) d.nx*d.ny*nzh;
+  for (long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x; i < nh;
+       i += (long long) gridDim.x*blockDim.x) {
+    const int k = (int) (i % nzh);
+    const long long r = i / nzh;
+    const int j = (int) (r % d.ny);
+    const int ii = (int) (r / d.ny);
+    int n = faithful ? bin_reference(d, ii, j, k)
+      : bin_corrected(d, ii, j, k);
+    if (n >= LGBK_SK_NBIN) n = LGBK_SK_NBIN - 1;
+    const double2 v = c[((long long) ii*d.ny + j)*d.nz + k];
+    atomicAdd(ssk + n, v.x*v.x + v.y*v.y);
+    atomicAdd(snk + n, 1.0);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < LGBK_SK_NBIN; b += blockDim.x) {
+    if (snk[b] != 0.0) {
+      atomicAdd(sk + b, ssk[b]);
+      atomicAdd(nk + b, snk[b]);
+    }
+  }
 }
 
 extern "C" int lgbk_structure_factor(const lgbk_dims_t * d, int prec,
@@ -178,7 +230,9 @@ extern "C" int lgbk_structure_factor(const lgbk_dims_t * d, int prec,
   err = cudaMemsetAsync(bins, 0, 2*LGBK_SK_NBIN*sizeof(double), s);
   if (err != cudaSuccess) return (int) err;
   long long nh = (long long) d->nx*d->ny*(d->nz/2 + 1);
-  k_bin_sk<<<(unsigned int) ((nh + 255)/256), 256, 0, s>>>(
+  long long nb = (nh + 255)/256;
+  if (nb > 1024) nb = 1024;
+  k_bin_sk<<<(unsigned int) nb, 256, 0, s>>>(
     *d, faithful, b, bins, bins + LGBK_SK_NBIN);
   err = cudaGetLastError();
   if (err != cudaSuccess) return (int) err;

@@ -496,6 +496,30 @@ k_binary_fused(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
   }
 }
 
+/* Work items of the ensemble kernels are taken from a counter (sched[0])
+ * in list order, the host having sorted the list longest first, so that
+ * the short items of small boxes fill in behind the long ones.  After its
+ * last fetch each CTA counts itself out (sched[1]); the last one resets
+ * both counters for the next launch, which the stream orders after this
+ * one. */
+__device__ __forceinline__ int2 lgbk_sched_next(int * sched,
+						const int2 * items,
+						int nitems) {
+  const int k = atomicAdd(sched, 1);
+  return (k < nitems) ? items[k] : make_int2(-1, 0);
+}
+
+__device__ __forceinline__ void lgbk_sched_retire(int * sched) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    if (atomicAdd(sched + 1, 1) == (int) gridDim.x - 1) {
+      __threadfence();
+      atomicExch(sched, 0);
+      atomicExch(sched + 1, 0);
+    }
+  }
+}
+
 /* Ensemble of independent boxes: box descriptors and a flat list of
  * (box, local item) pairs; one launch covers every box.  Boxes marked
  * inactive (quarantined) are skipped. */
@@ -503,14 +527,20 @@ template <typename T, typename S, bool SEQ, bool SHIFT, bool GZERO,
 	  bool HAS_MAP, int TY, int MINB>
 __global__ void __launch_bounds__(32*TY, MINB)
 k_binary_ensemble(const lgbk_box_t * __restrict__ boxes,
-		  const int2 * __restrict__ items, int nitems, int xchunk) {
+		  const int2 * __restrict__ items, int nitems, int xchunk,
+		  int * __restrict__ sched) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ lgbk_box_t sb;
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-    const int2 it = items[item];
+  __shared__ int2 sit;
+  for (;;) {
+    __syncthreads();                 /* the last item is done with sb, sit */
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      sit = lgbk_sched_next(sched, items, nitems);
+      if (sit.x >= 0) sb = boxes[sit.x];
+    }
     __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) sb = boxes[it.x];
-    __syncthreads();
+    const int2 it = sit;
+    if (it.x < 0) break;
     if (!sb.active) continue;
     const int ntz = (sb.d.nz + 31)/32;
     const int nty = (sb.d.ny + TY - 1)/TY;
@@ -520,6 +550,7 @@ k_binary_ensemble(const lgbk_box_t * __restrict__ boxes,
     binary_item<T, S, SEQ, SHIFT, GZERO, HAS_MAP, TY>(
       sb.d, sb.a, itz, ity, x0, min(x0 + xchunk, sb.d.nx), smem_raw);
   }
+  lgbk_sched_retire(sched);
 }
 
 #endif

@@ -456,15 +456,21 @@ k_binary_fused2(lgbk_dims_t d, lgbk_binary_args_t a, int xchunk) {
 template <typename S, int TYT, int MINB>
 __global__ void __launch_bounds__(32*TYT, MINB)
 k_binary_ensemble2(const lgbk_box_t * __restrict__ boxes,
-		   const int2 * __restrict__ items, int nitems, int xchunk) {
+		   const int2 * __restrict__ items, int nitems, int xchunk,
+		   int * __restrict__ sched) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ lgbk_box_t sb;
+  __shared__ int2 sit;
   constexpr int TY = 2*TYT;
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-    const int2 it = items[item];
+  for (;;) {
+    __syncthreads();                 /* the last item is done with sb, sit */
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+      sit = lgbk_sched_next(sched, items, nitems);
+      if (sit.x >= 0) sb = boxes[sit.x];
+    }
     __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) sb = boxes[it.x];
-    __syncthreads();
+    const int2 it = sit;
+    if (it.x < 0) break;
     if (!sb.active) continue;
     const int ntz = (sb.d.nz + 31)/32;
     const int nty = (sb.d.ny + TY - 1)/TY;
@@ -474,6 +480,7 @@ k_binary_ensemble2(const lgbk_box_t * __restrict__ boxes,
     binary_item2<S, TYT>(sb.d, sb.a, itz, ity, x0,
 			 min(x0 + xchunk, sb.d.nx), smem_raw);
   }
+  lgbk_sched_retire(sched);
 }
 
 #endif

@@ -21,7 +21,8 @@ extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
 				    int ty, void * stream);
 extern "C" int lgbk_ensemble_step_f64(const lgbk_box_t * boxes,
 				      const void * items, int nitems,
-				      int xchunk, int has_map, void * stream);
+				      int xchunk, int has_map, int * sched,
+				      void * stream);
 
 template <typename S, bool HAS_MAP, int TY, int MINB>
 static int launch32(const lgbk_dims_t * d, const lgbk_binary_args_t * a,
@@ -140,7 +141,8 @@ extern "C" int lgbk_binary_step(const lgbk_dims_t * d, int prec,
 
 template <typename S, bool HAS_MAP, int TY, int MINB>
 static int launch_ens32(const lgbk_box_t * boxes, const void * items,
-			int nitems, int xchunk, cudaStream_t stream) {
+			int nitems, int xchunk, int * sched,
+			cudaStream_t stream) {
   auto kern = k_binary_ensemble<float, S, false, true, true, HAS_MAP, TY,
 				MINB>;
   size_t smem = FusedSmem<float, TY>::bytes();
@@ -156,13 +158,14 @@ static int launch_ens32(const lgbk_box_t * boxes, const void * items,
   if (grid > nitems) grid = nitems;
   if (grid < 1) return 0;
   kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(
-    boxes, (const int2 *) items, nitems, xchunk);
+    boxes, (const int2 *) items, nitems, xchunk, sched);
   return (int) cudaGetLastError();
 }
 
 template <typename S, int TYT, int MINB>
 static int launch_ens32_two(const lgbk_box_t * boxes, const void * items,
-			    int nitems, int xchunk, cudaStream_t stream) {
+			    int nitems, int xchunk, int * sched,
+			    cudaStream_t stream) {
   auto kern = k_binary_ensemble2<S, TYT, MINB>;
   size_t smem = FusedSmem<float, 2*TYT>::bytes();
   cudaError_t err = cudaFuncSetAttribute(kern,
@@ -177,7 +180,7 @@ static int launch_ens32_two(const lgbk_box_t * boxes, const void * items,
   if (grid > nitems) grid = nitems;
   if (grid < 1) return 0;
   kern<<<(unsigned int) grid, dim3(32, TYT), smem, stream>>>(
-    boxes, (const int2 *) items, nitems, xchunk);
+    boxes, (const int2 *) items, nitems, xchunk, sched);
   return (int) cudaGetLastError();
 }
 
@@ -186,46 +189,46 @@ static int launch_ens32_two(const lgbk_box_t * boxes, const void * items,
 template <typename S>
 static int dispatch_ens32(const lgbk_box_t * b, const void * it, int n,
 			  int xchunk, int ty, int minb, int m, int sites,
-			  cudaStream_t s) {
+			  int * q, cudaStream_t s) {
   if (sites == 2 && !m && ty == 16) {
-    return launch_ens32_two<S, 8, 2>(b, it, n, xchunk, s);
+    return launch_ens32_two<S, 8, 2>(b, it, n, xchunk, q, s);
   }
   if (sites == 2 && !m && ty == 8) {
-    if (minb == 4) return launch_ens32_two<S, 4, 4>(b, it, n, xchunk, s);
-    if (minb == 2) return launch_ens32_two<S, 4, 2>(b, it, n, xchunk, s);
-    return launch_ens32_two<S, 4, 3>(b, it, n, xchunk, s);
+    if (minb == 4) return launch_ens32_two<S, 4, 4>(b, it, n, xchunk, q, s);
+    if (minb == 2) return launch_ens32_two<S, 4, 2>(b, it, n, xchunk, q, s);
+    return launch_ens32_two<S, 4, 3>(b, it, n, xchunk, q, s);
   }
   if (ty == 4) {
-    return m ? launch_ens32<S, true, 4, 8>(b, it, n, xchunk, s)
-             : launch_ens32<S, false, 4, 8>(b, it, n, xchunk, s);
+    return m ? launch_ens32<S, true, 4, 8>(b, it, n, xchunk, q, s)
+             : launch_ens32<S, false, 4, 8>(b, it, n, xchunk, q, s);
   }
   if (ty == 16) {
-    return m ? launch_ens32<S, true, 16, 2>(b, it, n, xchunk, s)
-             : launch_ens32<S, false, 16, 2>(b, it, n, xchunk, s);
+    return m ? launch_ens32<S, true, 16, 2>(b, it, n, xchunk, q, s)
+             : launch_ens32<S, false, 16, 2>(b, it, n, xchunk, q, s);
   }
   if (minb == 3) {
-    return m ? launch_ens32<S, true, 8, 3>(b, it, n, xchunk, s)
-             : launch_ens32<S, false, 8, 3>(b, it, n, xchunk, s);
+    return m ? launch_ens32<S, true, 8, 3>(b, it, n, xchunk, q, s)
+             : launch_ens32<S, false, 8, 3>(b, it, n, xchunk, q, s);
   }
-  return m ? launch_ens32<S, true, 8, 4>(b, it, n, xchunk, s)
-           : launch_ens32<S, false, 8, 4>(b, it, n, xchunk, s);
+  return m ? launch_ens32<S, true, 8, 4>(b, it, n, xchunk, q, s)
+           : launch_ens32<S, false, 8, 4>(b, it, n, xchunk, q, s);
 }
 
 extern "C" int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes,
 				  const void * items, int nitems, int xchunk,
 				  int ty, int minb, int has_map, int sites,
-				  void * stream) {
+				  int * sched, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
   switch (prec) {
   case LGBK_PREC_FP64:
     return lgbk_ensemble_step_f64(boxes, items, nitems, xchunk, has_map,
-				  stream);
+				  sched, stream);
   case LGBK_PREC_FP32:
     return dispatch_ens32<float>(boxes, items, nitems, xchunk, ty, minb,
-				 has_map, (sites == 2) ? 2 : 1, s);
+				 has_map, (sites == 2) ? 2 : 1, sched, s);
   case LGBK_PREC_FP16:
     return dispatch_ens32<__half>(boxes, items, nitems, xchunk, ty, minb,
-				  has_map, (sites == 1) ? 1 : 2, s);
+				  has_map, (sites == 1) ? 1 : 2, sched, s);
   default:
     return (int) cudaErrorInvalidValue;
   }

@@ -52,7 +52,8 @@ extern "C" int lgbk_binary_step_f64(const lgbk_dims_t * d,
 /* Ensembles in FP64 (tile 8 x 32, 2 CTAs per SM) */
 template <bool HAS_MAP>
 static int launch_ens64(const lgbk_box_t * boxes, const void * items,
-			int nitems, int xchunk, cudaStream_t stream) {
+			int nitems, int xchunk, int * sched,
+			cudaStream_t stream) {
   constexpr int TY = 8;
   auto kern = k_binary_ensemble<double, double, true, false, true, HAS_MAP,
 				TY, 2>;
@@ -69,15 +70,17 @@ static int launch_ens64(const lgbk_box_t * boxes, const void * items,
   if (grid > nitems) grid = nitems;
   if (grid < 1) return 0;
   kern<<<(unsigned int) grid, dim3(32, TY), smem, stream>>>(
-    boxes, (const int2 *) items, nitems, xchunk);
+    boxes, (const int2 *) items, nitems, xchunk, sched);
   return (int) cudaGetLastError();
 }
 
 /* Requires every box to relax its ghost modes with rtau = 1 (M10). */
 extern "C" int lgbk_ensemble_step_f64(const lgbk_box_t * boxes,
 				      const void * items, int nitems,
-				      int xchunk, int has_map, void * stream) {
+				      int xchunk, int has_map, int * sched,
+				      void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
-  return has_map ? launch_ens64<true>(boxes, items, nitems, xchunk, s)
-                 : launch_ens64<false>(boxes, items, nitems, xchunk, s);
+  return has_map ? launch_ens64<true>(boxes, items, nitems, xchunk, sched, s)
+                 : launch_ens64<false>(boxes, items, nitems, xchunk, sched,
+				       s);
 }

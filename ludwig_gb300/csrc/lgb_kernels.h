@@ -151,10 +151,13 @@ typedef struct lgbk_box_s {
 } lgbk_box_t;
 
 /* One step of every active box: items[k] = (box, item within the box),
- * built for tile height ty and xchunk by lgbk_ensemble_items(). */
+ * built for tile height ty and xchunk by lgbk_ensemble_items(); CTAs take
+ * the items in list order from the counters sched_dev[0..1] (two ints,
+ * zero before the first step; each launch leaves them zero). */
 int lgbk_ensemble_step(int prec, const lgbk_box_t * boxes_dev,
 		       const void * items_dev, int nitems, int xchunk, int ty,
-		       int minb, int has_map, int sites, void * stream);
+		       int minb, int has_map, int sites, int * sched_dev,
+		       void * stream);
 /* Number of work items of one box (and fill items if non-NULL, host) */
 int lgbk_ensemble_items(const lgbk_dims_t * d, int box, int xchunk, int ty,
 			int * items);

@@ -3153,8 +3153,9 @@ struct ludwig_gb_ensemble_s {
   void * rho;                  /* ntot */
   lgbk_box_t * boxes_h[2];     /* arrangement k: reads buffer k */
   lgbk_box_t * boxes_d[2];
-  int * items_d;
+  int * items_d;               /* (box, item) pairs, longest items first */
   int nitems;
+  int * sched_d;               /* work counters of the ensemble kernels */
   int xchunk, ty, minb;
   int parity;                  /* buffers read by the next step */
   cudaGraphExec_t pair[2];
@@ -3168,6 +3169,23 @@ static void ens_graph_reset(ludwig_gb_ensemble_t * e) {
   }
 }
 
+/* Work of an item: its planes plus the two of the pipeline's start */
+static int ens_item_cost(const lgbk_dims_t * d, int xchunk, int ty, int k) {
+  const int ntz = (d->nz + 31)/32, nty = (d->ny + ty - 1)/ty;
+  const int x0 = (k/(ntz*nty))*xchunk;
+  const int xl = (d->nx - x0 < xchunk) ? d->nx - x0 : xchunk;
+  return xl + 2;
+}
+
+typedef struct { int cost, pos, box, item; } ens_item_t;
+
+static int ens_item_cmp(const void * a, const void * b) {
+  const ens_item_t * p = (const ens_item_t *) a;
+  const ens_item_t * q = (const ens_item_t *) b;
+  if (p->cost != q->cost) return (p->cost > q->cost) ? -1 : 1;
+  return (p->pos < q->pos) ? -1 : (p->pos > q->pos);
+}
+
 static int ens_items(ludwig_gb_ensemble_t * e) {
   int n = 0;
   for (int b = 0; b < e->nbox; b++) {
@@ -3175,12 +3193,32 @@ static int ens_items(ludwig_gb_ensemble_t * e) {
     n += lgbk_ensemble_items(&d, b, e->xchunk, e->ty, NULL);
   }
   int * h = (int *) malloc(2*(size_t) n*sizeof(int));
-  if (h == NULL) return err_set(LUDWIG_GB_ENOMEM, "ensemble items");
+  ens_item_t * t = (ens_item_t *) malloc((size_t) n*sizeof(ens_item_t));
+  if (h == NULL || t == NULL) {
+    free(h);
+    free(t);
+    return err_set(LUDWIG_GB_ENOMEM, "ensemble items");
+  }
   int k = 0;
   for (int b = 0; b < e->nbox; b++) {
     lgbk_dims_t d = e->boxes_h[0][b].d;
     k += lgbk_ensemble_items(&d, b, e->xchunk, e->ty, h + 2*k);
   }
+  /* longest items first (list order otherwise kept): the CTAs take them
+   * from a counter, so the short items fill in at the end */
+  for (int i = 0; i < n; i++) {
+    const lgbk_dims_t * d = &e->boxes_h[0][h[2*i]].d;
+    t[i].cost = ens_item_cost(d, e->xchunk, e->ty, h[2*i + 1]);
+    t[i].pos = i;
+    t[i].box = h[2*i];
+    t[i].item = h[2*i + 1];
+  }
+  qsort(t, (size_t) n, sizeof(ens_item_t), ens_item_cmp);
+  for (int i = 0; i < n; i++) {
+    h[2*i] = t[i].box;
+    h[2*i + 1] = t[i].item;
+  }
+  free(t);
   dev_free(e->items_d);
   e->items_d = NULL;
   int rc = dev_alloc((void **) &e->items_d, 2*(size_t) n*sizeof(int),
@@ -3215,6 +3253,7 @@ int ludwig_gb_ensemble_free(ludwig_gb_ensemble_t * e) {
   }
   dev_free(e->rho);
   dev_free(e->items_d);
+  dev_free(e->sched_d);
   free(e->param); free(e->off); free(e->active);
   free(e);
   return LUDWIG_GB_OK;
@@ -3366,6 +3405,10 @@ int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
   }
   if (rc == 0) rc = ens_items(e);
   if (rc == 0) rc = ens_upload_boxes(e);
+  if (rc == 0) rc = dev_alloc((void **) &e->sched_d, 2*sizeof(int), "sched");
+  if (rc == 0) {
+    rc = cuda_check(cudaMemset(e->sched_d, 0, 2*sizeof(int)), "sched");
+  }
   if (rc) { ludwig_gb_ensemble_free(e); return rc; }
   e->parity = 0;
   *pens = e;
@@ -3375,7 +3418,7 @@ int ludwig_gb_ensemble_create(int nbox, const ludwig_gb_box_param_t * p,
 static int ens_launch(ludwig_gb_ensemble_t * e, int k) {
   return lgbk_ensemble_step(e->prec, e->boxes_d[k], e->items_d, e->nitems,
 			    e->xchunk, e->ty, e->minb, 0, tune_sites_,
-			    stream_);
+			    e->sched_d, stream_);
 }
 
 static int ens_step_async(ludwig_gb_ensemble_t * e, int nsteps) {

@@ -1344,10 +1344,12 @@ struct FeatP {
   float scale[5];
 };
 
+/* full = 0: channels 0..15 only (channels 16..31 of the rows are zero
+ * already, and only the first layer, which reads 16, uses them) */
 __global__ void k_cnn_features(lgbk_cnn_geom_t g, const float * __restrict__ phi,
 			       const float * __restrict__ u,
 			       const float * __restrict__ rho, FeatP fp,
-			       uint8_t * __restrict__ p0) {
+			       uint8_t * __restrict__ p0, int full) {
   const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
   if (s >= g.nsites) return;
   const int z = (int) (s % g.nz);
@@ -1363,18 +1365,20 @@ __global__ void k_cnn_features(lgbk_cnn_geom_t g, const float * __restrict__ phi
   v[2] = __fmul_rn(__fsub_rn(u[N + s], fp.off[2]), fp.scale[2]);
   v[3] = __fmul_rn(__fsub_rn(u[2*N + s], fp.off[3]), fp.scale[3]);
   v[4] = __fmul_rn(__fsub_rn(rho[s], fp.off[4]), fp.scale[4]);
-  store_row_bf16(p0 + (long long) prow(g, x, y, z)*ROWB, v);
+  uint8_t * row = p0 + (long long) prow(g, x, y, z)*ROWB;
+  if (full) store_row_bf16(row, v);
+  else store_half_row_bf16(row, v);
 }
 
 extern "C" int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
 				 const float * u, const float * rho,
 				 const float off[5], const float scale[5],
-				 void * p0, void * stream) {
+				 void * p0, int full, void * stream) {
   FeatP fp;
   for (int c = 0; c < 5; c++) { fp.off[c] = off[c]; fp.scale[c] = scale[c]; }
   cudaStream_t s = (cudaStream_t) stream;
   k_cnn_features<<<(unsigned int) ((g->nsites + 255)/256), 256, 0, s>>>(
-    *g, phi, u, rho, fp, (uint8_t *) p0);
+    *g, phi, u, rho, fp, (uint8_t *) p0, full);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int) e;
   return lgbk_cnn_halo(g, p0, stream);

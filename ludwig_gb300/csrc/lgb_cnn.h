@@ -83,10 +83,12 @@ int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
 
 int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p, void * stream);
 
-/* channel c < 5: (src[c][s] - off[c]) * scale[c]; others 0; then halo */
+/* channel c < 5: (src[c][s] - off[c]) * scale[c]; others 0 (full = 0:
+ * channels 5..15 only, 16..31 left as they are); then halo */
 int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
 		      const float * u, const float * rho, const float off[5],
-		      const float scale[5], void * p0, void * stream);
+		      const float scale[5], void * p0, int full,
+		      void * stream);
 
 /* Loss (1/N) sum (out - t)^2 over 4 channels and dL/dz_4 (bf16, padded,
  * halo filled); part: LGBK_CNN_RED_BLOCKS doubles; loss: 1 double */

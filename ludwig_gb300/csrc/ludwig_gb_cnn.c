@@ -47,6 +47,7 @@ struct ludwig_gb_cnn_s {
   lgbk_cnn_geom_t g;
   int line_ok;                 /* nz a multiple of 128: line-reuse kernel */
   int line_on;
+  int act0_dirty;              /* act[0] channels 16..31 may be nonzero */
   float * params;              /* [NL][PL] */
   float * grads;
   float * adam_m;
@@ -403,8 +404,11 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
 		   const float * rho, int train, float * out) {
   cudaStream_t s = lib_stream();
   const lgbk_cnn_geom_t * g = &m->g;
+  /* the first layer reads channels 0..15; 16..31 stay zero unless a
+   * direct convolution call packed other data into act[0] */
   int rc = lgbk_cnn_features(g, phi, u, rho, m->in_off, m->in_scale,
-			     m->act[0], s);
+			     m->act[0], m->act0_dirty, s);
+  m->act0_dirty = 0;
   if (rc) return ck(rc, "cnn features");
   for (int l = 0; l < NL; l++) {
     const float * b = m->params + l*PL + WL;
@@ -643,6 +647,7 @@ int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * m, const float * a, const float * w,
   }
   cudaStream_t s = lib_stream();
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
+  m->act0_dirty = 1;
   if (!rc) rc = lgbk_cnn_wprep(w, m->wf[0], m->wt[0], s);
   if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, LGBK_CNN_C, &m->tm_act[0],
 			      lmap(m, 1, 0), m->line_on,
@@ -665,6 +670,7 @@ int ludwig_gb_cnn_wgrad3(ludwig_gb_cnn_t * m, const float * gr,
   }
   cudaStream_t s = lib_stream();
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
+  m->act0_dirty = 1;
   if (!rc) rc = lgbk_cnn_pack_rows(&m->g, gr, m->gpad[1], s);
   if (!rc) rc = lgbk_cnn_wgrad(&m->g, &m->tm_g[1],
 			       m->line_on ? &m->tm_gs[1] : NULL, &m->tm_act[0],

@@ -310,3 +310,31 @@ def test_forward_n_matches_forward(trained):
         ref = torch.empty_like(o)
         m.forward(x.data_ptr(), ref.data_ptr())
         assert torch.equal(ref, o)
+
+
+def test_forward_after_direct_convolution(gb, orc):
+    """A direct convolution call packs its own 32-channel data into the
+    first layer's input rows; the next forward pass must rewrite all 32
+    channels (the feature kernel otherwise writes 16): the result equals
+    that of a model that never made the call."""
+    n = (2, 4, 128)
+    N = n[0] * n[1] * n[2]
+    rng = np.random.default_rng(5)
+    m1, m2 = gb.Corrector(n, seed=3), gb.Corrector(n, seed=3)
+    a = dev(rng.standard_normal((N, 32)))
+    w = dev(0.2 * rng.standard_normal((27, 32, 32)))
+    b = dev(rng.standard_normal(32))
+    junk = torch.empty((N, 32), dtype=torch.float32, device="cuda")
+    m1.conv3(a.data_ptr(), w.data_ptr(), b.data_ptr(), 0, junk.data_ptr())
+    x = dev(0.1 * rng.standard_normal((5, N)))
+    t = dev(0.1 * rng.standard_normal((4, N)))
+    o1 = torch.empty((4, N), dtype=torch.float32, device="cuda")
+    o2 = torch.empty_like(o1)
+    m1.forward(x.data_ptr(), o1.data_ptr())
+    m2.forward(x.data_ptr(), o2.data_ptr())
+    assert torch.equal(o1, o2)
+    # the weight gradient of the first layer reads all 32 input channels
+    l1 = m1.loss_grad(x.data_ptr(), t.data_ptr())
+    l2 = m2.loss_grad(x.data_ptr(), t.data_ptr())
+    assert l1 == l2
+    assert np.array_equal(m1.grads(), m2.grads())

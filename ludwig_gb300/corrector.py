@@ -249,7 +249,7 @@ def rollout(model, nfine, seed, t0, ncoarse_steps, every, params=FINE_PARAMS,
     return out
 
 
-def time_network(model, x, t, reps=20):
+def time_network(model, x, t, reps=20, exec_layers=3.5):
     """Time per forward pass and per training step (forward, backward,
     Adam) on one pair, issued back to back (`forward_n`, `train_steps`:
     one error check per batch), the same with one call and one host check
@@ -279,11 +279,13 @@ def time_network(model, x, t, reps=20):
     sync()
     step = (time.perf_counter() - t0) / reps
     n = model.nsites
-    # executed MMA work: 4 convolutions forward (the first with K = 16 of
-    # its 32 input channels: the 5 features and zeros), 3 backward-data
-    # and 4 weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
+    # executed MMA work: 4 convolutions forward in units of a 32 -> 32
+    # layer (exec_layers: the first with K = 16 of its 32 input channels,
+    # the 5 features and zeros, counts 0.5; the last counts 0.5 where its
+    # 4 outputs are computed as 16 rows, 1 otherwise), 3 backward-data and
+    # 4 weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
     flop_conv = 2.0 * n * 27 * 32 * 32
-    flop_fwd = 3.5 * flop_conv
+    flop_fwd = exec_layers * flop_conv
     flop_step = flop_fwd + 3 * flop_conv + 4 * flop_conv * 28.0 / 27.0
     return {"sites": n, "forward_ms": 1e3 * fwd, "train_step_ms": 1e3 * step,
             "forward_call_ms": 1e3 * fwd_call,
@@ -306,11 +308,16 @@ def bench(n, reps=20):
     x[4] += 1.0
     t = 0.1 * torch.randn((4, N), device="cuda", generator=g)
     torch.cuda.synchronize()
-    res = {"default": time_network(model, x, t, reps)}
+    # the three-tap form (the default where nz = 128) computes the last
+    # layer's 4 outputs as 16 weight rows
+    three = (n == 128)
+    res = {"default": time_network(model, x, t, reps,
+                                   3.0 if three else 3.5)}
     for mode, name in ((0, "per_tap"), (1, "line_planes"),
                        (2, "line_swizzled"), (3, "line_three_taps")):
         model.line_reuse(mode)
-        res[name] = time_network(model, x, t, reps)
+        res[name] = time_network(model, x, t, reps,
+                                 3.0 if (mode == 3 and three) else 3.5)
     return res
 
 

@@ -213,6 +213,9 @@ struct ConvP {
   float * outf;
   int * err;
   int khn;                    /* K halves of 16 input channels: 1 or 2 */
+  int nb;                     /* weight rows per tap in shared memory: 32,
+				 or 16 for the last layer's 4 outputs in
+				 the three-tap line form */
 };
 
 /* Epilogue of channels c0 .. c0+15 of one output site (x, y, z) from 16
@@ -521,7 +524,10 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   const uint32_t bX = bW + 56;                 /* 4: [channel half][parity] */
   const uint32_t sXch = sBar + 256;            /* [half][parity][quarter] */
   /* accumulator columns per tile and TMEM columns allocated */
-  constexpr uint32_t NACC = CYC ? 3*CNN_C : CNN_C;
+  /* accumulator columns per tile (three taps of nb outputs each in the
+   * three-tap form) and TMEM columns allocated */
+  const int nbk = CYC ? p.nb : CNN_C;
+  const uint32_t NACC = CYC ? 3u*(uint32_t) nbk : (uint32_t) CNN_C;
   constexpr uint32_t TCOLS = CYC ? 256 : CONV_TMEM_COLS;
 
   const int warp = threadIdx.x/32;
@@ -553,9 +559,11 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   if (warp == 0 && lane == 0) {
     tc_prefetch_map(&tm_line);
     tc_prefetch_map(&tm_w);
-    tc_mbar_arrive_tx(bW, CNN_NTAP*WTAPB);
+    /* the first nb output rows of every tap's weights */
+    const uint32_t wtap = (uint32_t) (CYC ? p.nb : CNN_C)*ROWB;
+    tc_mbar_arrive_tx(bW, CNN_NTAP*wtap);
     for (int t = 0; t < CNN_NTAP; t++) {
-      tc_tma_load_2d(sW + t*WTAPB, &tm_w, bW, 0, t*CNN_C);
+      tc_tma_load_2d(sW + t*wtap, &tm_w, bW, 0, t*CNN_C);
     }
     /* y-lines are numbered in load order (sq); line sq fills ring slot
      * sq % LN_NY, after line sq - LN_NY has been released */
@@ -602,7 +610,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     }
   }
   else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = tc_idesc_bf16(128, (int) NACC, 0, 0);
+    const uint32_t idesc = tc_idesc_bf16(128, (int) NACC, 0, 0);
     /* descriptors of the first ring slot and of the first tap's weights */
     const uint64_t ad0 = SWZ
       ? tc_sdesc(sL, 16, 512, LGB_TC_SWIZZLE_64B)
@@ -652,9 +660,9 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	    #pragma unroll
 	    for (int kh = 0; kh < 2; kh++) {
 	      if (kh >= p.khn) break;
-	      tc_mma_bf16_w(d, a + kh*KHA, ahi, blo0 + (3*ln*WTAPB >> 4)
-			    + kh*KHB, bhi, idesc,
-			    (uint32_t) ((ln | kh) != 0));
+	      tc_mma_bf16_w(d, a + kh*KHA, ahi,
+			    blo0 + (uint32_t) (3*ln*nbk*ROWB >> 4) + kh*KHB,
+			    bhi, idesc, (uint32_t) ((ln | kh) != 0));
 	    }
 	  }
 	}
@@ -706,11 +714,17 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	uint32_t r[16];
 	const uint32_t ta = tmem + (uint32_t) acc*NACC + (uint32_t) c0
 	  + ((uint32_t) (q*32) << 16);
+	if (CYC && c0 >= nbk) {
+	  /* no accumulator columns for this channel half */
+	  tc_fence_before();
+	  tc_mbar_arrive(bTEmpty + 8*acc);
+	  continue;
+	}
 	if (CYC) {
 	  uint32_t rm[16], rp[16];
 	  tc_tmem_ld16_async(ta, rm);                /* D_-1, this row */
-	  tc_tmem_ld16_async(ta + CNN_C, r);         /* D_0 */
-	  tc_tmem_ld16_async(ta + 2*CNN_C, rp);      /* D_+1 */
+	  tc_tmem_ld16_async(ta + nbk, r);           /* D_0 */
+	  tc_tmem_ld16_async(ta + 2*nbk, rp);        /* D_+1 */
 	  tc_tmem_wait_ld16x3(rm, r, rp);
 	  tc_fence_before();
 	  tc_mbar_arrive(bTEmpty + 8*acc);
@@ -823,7 +837,7 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
   return cudaGetLastError();
 }
 
-extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
+extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int wrows,
 			     const void * tm_in, const void * tm_line,
 			     int line_kind, const void * tm_w, const float * bias,
 			     const void * zprev, void * zout, void * pout,
@@ -838,6 +852,7 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
   p.err = err;
   if (kin != 16 && kin != CNN_C) return (int) cudaErrorInvalidValue;
   p.khn = kin/16;
+  p.nb = wrows;
   const CUtensorMap mi = *(const CUtensorMap *) tm_in;
   const CUtensorMap mw = *(const CUtensorMap *) tm_w;
   const CUtensorMap * ml = NULL;
@@ -845,6 +860,12 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
   if (tm_line && g->bz == LGBK_CNN_TILE && g->lpt == 1) {
     mlv = *(const CUtensorMap *) tm_line;
     ml = &mlv;
+  }
+  /* 16 weight rows per tap (tm_w boxes of 16 rows): only where the
+   * three-tap line form runs */
+  if (wrows != CNN_C &&
+      !(wrows == 16 && ml && line_kind == 3 && g->nz == LGBK_CNN_TILE)) {
+    return (int) cudaErrorInvalidValue;
   }
   cudaStream_t s = (cudaStream_t) stream;
   cudaError_t e;

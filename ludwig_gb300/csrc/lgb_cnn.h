@@ -65,8 +65,11 @@ int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
  * 32 x 130, 64-byte swizzle (line-reuse kernel); line_kind 3 (nz = 128):
  * the kind-1 map, three z taps per MMA. */
 /* kin: input channels read, 32 or 16 (the first layer: channels 16..31 of
- * its input rows are zero, so their products are left out) */
-int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin,
+ * its input rows are zero, so their products are left out); wrows: weight
+ * rows (output channels) per tap in tm_w's boxes, 32, or 16 for the last
+ * layer's 4 outputs where the three-tap line form runs (line_kind 3,
+ * nz = 128) */
+int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int wrows,
 		  const void * tm_in,
 		  const void * tm_line, int line_kind, const void * tm_w,
 		  const float * bias,

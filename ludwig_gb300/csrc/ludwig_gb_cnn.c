@@ -39,6 +39,7 @@ struct ludwig_gb_cnn_s {
   CUtensorMap tm_act[NL];      /* padded activations a_0 .. a_3 */
   CUtensorMap tm_g[NL + 1];    /* padded dL/dz_1 .. dL/dz_4 (index 1..4) */
   CUtensorMap tm_wf[NL];       /* bf16 weights, forward order */
+  CUtensorMap tm_wf16;         /* the last layer's, 16 rows a tap */
   CUtensorMap tm_wt[NL];       /* bf16 weights, flipped and transposed */
   CUtensorMap tm_actl[NL];     /* the same buffers as 8 x 130 line boxes */
   CUtensorMap tm_gl[NL + 1];
@@ -250,6 +251,7 @@ int ludwig_gb_cnn_create(const int n[3], unsigned long long seed,
     if (!rc) rc = map_rows(&m->tm_wf[l], m->wf[l], LGBK_CNN_NTAP*32, 32);
     if (!rc) rc = map_rows(&m->tm_wt[l], m->wt[l], LGBK_CNN_NTAP*32, 32);
   }
+  if (!rc) rc = map_rows(&m->tm_wf16, m->wf[NL - 1], LGBK_CNN_NTAP*32, 16);
   for (int l = 1; l <= NL && !rc; l++) {
     rc = map_rows(&m->tm_g[l], m->gpad[l], g.rows, g.bz);
   }
@@ -413,15 +415,20 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
   for (int l = 0; l < NL; l++) {
     const float * b = m->params + l*PL + WL;
     if (l < NL - 1) {
-      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, kin_of(l), &m->tm_act[l],
+      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, kin_of(l), LGBK_CNN_C,
+			 &m->tm_act[l],
 			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL,
 			 train ? m->zpre[l + 1] : NULL, m->act[l + 1], NULL,
 			 m->err_dev, s);
       if (!rc) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
     }
     else {
-      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l), &m->tm_act[l],
-			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL, NULL,
+      /* the 4 outputs: 16 weight rows a tap where the three-tap form runs */
+      const int w16 = (m->line_on == 3);
+      rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l),
+			 w16 ? 16 : LGBK_CNN_C, &m->tm_act[l],
+			 lmap(m, 1, l), m->line_on,
+			 w16 ? &m->tm_wf16 : &m->tm_wf[l], b, NULL, NULL,
 			 NULL, out ? out : m->out4, m->err_dev, s);
     }
     if (rc) return ck(rc, "cnn conv");
@@ -445,7 +452,8 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
 				     m->grads + l*PL + WL, s);
     if (rc) return ck(rc, "cnn wgrad");
     if (l == 0) break;
-    rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, LGBK_CNN_C, &m->tm_g[l + 1],
+    rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, LGBK_CNN_C, LGBK_CNN_C,
+		       &m->tm_g[l + 1],
 		       lmap(m, 0, l + 1), m->line_on, &m->tm_wt[l], NULL, m->zpre[l],
 		       NULL, m->gpad[l], NULL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_halo(g, m->gpad[l], s);
@@ -649,7 +657,8 @@ int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * m, const float * a, const float * w,
   int rc = lgbk_cnn_pack_rows(&m->g, a, m->act[0], s);
   m->act0_dirty = 1;
   if (!rc) rc = lgbk_cnn_wprep(w, m->wf[0], m->wt[0], s);
-  if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, LGBK_CNN_C, &m->tm_act[0],
+  if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, LGBK_CNN_C, LGBK_CNN_C,
+			      &m->tm_act[0],
 			      lmap(m, 1, 0), m->line_on,
 			      flip ? &m->tm_wt[0] : &m->tm_wf[0],
 			      flip ? NULL : b, NULL, NULL, NULL, out,

@@ -338,3 +338,28 @@ def test_forward_after_direct_convolution(gb, orc):
     l2 = m2.loss_grad(x.data_ptr(), t.data_ptr())
     assert l1 == l2
     assert np.array_equal(m1.grads(), m2.grads())
+
+
+@pytest.mark.parametrize("n", [(4, 4, 128), (3, 17, 128)])
+def test_three_tap_forward_matches_one_tap(gb, n):
+    """The network's forward pass in the three-tap line form (the last
+    layer with 16 weight rows a tap) against the one-tap line form: the
+    same products summed in another order.  The activations between the
+    layers are rounded to BF16, where a last-bit difference of a sum can
+    move a value by one BF16 step (2^-8 relative), so the outputs agree to
+    the network oracle's tolerance, not to FP32 rounding."""
+    N = n[0] * n[1] * n[2]
+    rng = np.random.default_rng(21)
+    m = gb.Corrector(n, seed=11)
+    p = m.params()
+    p[3 * 27680:3 * 27680 + 27648] *= 10.0
+    m.set_params(p)
+    x = dev(0.3 * rng.standard_normal((5, N)))
+    outs = {}
+    for mode in (1, 3):
+        m.line_reuse(mode)
+        o = torch.empty((4, N), dtype=torch.float32, device="cuda")
+        m.forward(x.data_ptr(), o.data_ptr())
+        outs[mode] = o
+    d = (outs[3] - outs[1]).abs().max().item()
+    assert d <= 1e-2 * outs[1].abs().max().item(), d

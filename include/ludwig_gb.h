@@ -826,6 +826,11 @@ int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * cnn, lb_t * lb, field_t * phi,
  * with the three z taps of a line in one tensor-core MMA; mode 0: one TMA
  * box per tap (any supported extents).  Default: 3 where nz = 128, else 1 */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * cnn, int mode);
+/* Failure detection of the tensor-core kernels: runs one device wait that
+ * nothing satisfies; returns LUDWIG_GB_ETIMEOUT once the bounded wait has
+ * given up and the kernel has returned (the context stays usable), with
+ * the kernel's duration in *seconds */
+int ludwig_gb_selftest_bounded_wait(double * seconds);
 /* one convolution / weight gradient on given fp32 device arrays
  * (operands rounded to bf16), for checks of the kernels themselves:
  * flip = 0: out[s][n] = b[n] + sum_t sum_c a[s+e_t][c] w[t][n][c];

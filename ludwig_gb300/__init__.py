@@ -152,6 +152,7 @@ def _declare(L):
         "ludwig_gb_sync": ([], ctypes.c_int),
         "ludwig_gb_tune_set": ([ctypes.c_int] * 3, ctypes.c_int),
         "ludwig_gb_tune_sites": ([ctypes.c_int], ctypes.c_int),
+        "ludwig_gb_selftest_bounded_wait": ([_D], ctypes.c_int),
         "ludwig_gb_lb_fp16_rescale": ([_P, _D], ctypes.c_int),
         "pe_create": ([ctypes.c_int, pp], ctypes.c_int),
         "pe_free": ([_P], ctypes.c_int),

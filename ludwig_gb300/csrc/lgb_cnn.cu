@@ -1306,6 +1306,34 @@ extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
 }
 
 /*****************************************************************************
+ *  Self-test of the bounded waits: one thread waits on an mbarrier that
+ *  nothing arrives on.  The wait gives up after LGB_TC_WAIT_CYCLES, raises
+ *  the error word and returns, so the context stays usable (the failure
+ *  path every tensor-core kernel takes when a copy or an MMA never
+ *  completes).
+ *****************************************************************************/
+
+__global__ void k_wait_selftest(int * err) {
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int abort_word;
+  if (threadIdx.x == 0) {
+    tc_mbar_init(tc_smem_u32(&bar), 1);
+    abort_word = 0;
+    tc_fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    (void) tc_mbar_wait(tc_smem_u32(&bar), 0u, (volatile int *) &abort_word,
+			err);
+  }
+}
+
+extern "C" int lgbk_wait_selftest(int * err, void * stream) {
+  k_wait_selftest<<<1, 32, 0, (cudaStream_t) stream>>>(err);
+  return (int) cudaGetLastError();
+}
+
+/*****************************************************************************
  *  Elementwise kernels
  *****************************************************************************/
 

@@ -122,6 +122,9 @@ int lgbk_cnn_apply(const lgbk_cnn_geom_t * g, const float * out4,
 int lgbk_cnn_pack_rows(const lgbk_cnn_geom_t * g, const float * src,
 		       void * p, void * stream);
 
+/* One bounded wait that runs out (nothing arrives): raises *err */
+int lgbk_wait_selftest(int * err, void * stream);
+
 #ifdef __cplusplus
 }
 #endif

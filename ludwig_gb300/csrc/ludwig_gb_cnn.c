@@ -689,3 +689,44 @@ int ludwig_gb_cnn_wgrad3(ludwig_gb_cnn_t * m, const float * gr,
   if (!rc) rc = ck(cudaStreamSynchronize(s), "sync");
   return rc;
 }
+
+/* Runs one device wait that nothing satisfies and reports how the bounded
+ * wait ended: LUDWIG_GB_ETIMEOUT (the expected outcome) once the kernel
+ * has given up, raised its error word and returned; *seconds: the time
+ * the kernel took. */
+int ludwig_gb_selftest_bounded_wait(double * seconds) {
+  if (seconds == NULL) {
+    return lgb_internal_err(LUDWIG_GB_EINVAL, "selftest_bounded_wait");
+  }
+  cudaStream_t s = lib_stream();
+  int * err = NULL;
+  if (cudaMalloc((void **) &err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return lgb_internal_err(LUDWIG_GB_ENOMEM, "selftest_bounded_wait");
+  }
+  cudaEvent_t e0, e1;
+  int herr = 0;
+  int rc = ck(cudaEventCreate(&e0), "event");
+  if (!rc) rc = ck(cudaEventCreate(&e1), "event");
+  if (!rc) rc = ck(cudaMemsetAsync(err, 0, sizeof(int), s), "memset");
+  if (!rc) rc = ck(cudaEventRecord(e0, s), "record");
+  if (!rc) rc = ck(lgbk_wait_selftest(err, s), "selftest kernel");
+  if (!rc) rc = ck(cudaEventRecord(e1, s), "record");
+  if (!rc) rc = ck(cudaMemcpyAsync(&herr, err, sizeof(int),
+				   cudaMemcpyDeviceToHost, s), "err");
+  if (!rc) rc = ck(cudaStreamSynchronize(s), "sync");
+  if (!rc) {
+    float ms = 0.0f;
+    rc = ck(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+    *seconds = 1e-3*ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(err);
+  if (rc) return rc;
+  if (herr) {
+    return lgb_internal_err(LUDWIG_GB_ETIMEOUT, "selftest: the bounded "
+			    "wait ran out as intended");
+  }
+  return LUDWIG_GB_OK;
+}

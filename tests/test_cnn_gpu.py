@@ -363,3 +363,20 @@ def test_three_tap_forward_matches_one_tap(gb, n):
         outs[mode] = o
     d = (outs[3] - outs[1]).abs().max().item()
     assert d <= 1e-2 * outs[1].abs().max().item(), d
+
+
+def test_bounded_wait_times_out_and_context_survives(gb):
+    """Failure detection without a fault: a device wait that nothing
+    satisfies gives up after its clock budget (about a second), raises the
+    error word and returns; the host reads LUDWIG_GB_ETIMEOUT, and the
+    context still runs a step afterwards."""
+    import ctypes
+    secs = ctypes.c_double()
+    rc = gb.lib().ludwig_gb_selftest_bounded_wait(ctypes.byref(secs))
+    assert rc == 5                      # LUDWIG_GB_ETIMEOUT
+    assert b"bounded" in gb.lib().ludwig_gb_last_error()
+    assert 0.2 < secs.value < 10.0, secs.value
+    s = gb.BinaryFluid((16, 16, 32), precision=gb.FP32)
+    s.phi.init_spinodal(5, 0.0, 0.02)
+    s.step(4)
+    assert np.isfinite(s.phi.stats()[0])

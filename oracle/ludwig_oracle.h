@@ -10,7 +10,7 @@
  *
  *  Parity: pinned bit-for-bit against the reference's own serial build
  *  (oracle/ref.mk + oracle/ref_shim.c) on the same seeded inputs; see
- *  tests/test_oracle_pin.py and tests/golden/.
+ *  tests/test_oracle_golden.py and tests/golden/.
  *
  *  Layout of every array: interior sites only, periodic, component-major
  *  with z fastest:  a[((n*Lx + x)*Ly + y)*Lz + z].

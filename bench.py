@@ -80,9 +80,11 @@ NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4,
 # executed as 4 layers of 32 x 32 channels, 2*27*32*32 each; useful are
 # the real layer shapes 5 -> 32 -> 32 -> 32 -> 4: 2*27*(5*32 + 2*32*32 +
 # 32*4) = 126,144.
-# executed per site: first layer K = 16, last layer 16 output rows (the
-# three-tap form at 128^3)
-CNN_EXEC_FLOP = 2 * 27 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16)
+# executed per site: first layer K = 16; the last layer in the folded
+# form at 128^3, 3 MMAs (dx) of N = 48 and K = 32 per y-line, 18 y-lines
+# per run of 16 output lines
+CNN_EXEC_FLOP = 2 * 27 * (16 * 32 + 32 * 32 + 32 * 32) + \
+    2 * 3 * 48 * 32 * 18 // 16
 CNN_USEFUL_FLOP = 2 * 27 * (5 * 32 + 2 * 32 * 32 + 32 * 4)
 
 # What bounds each kernel (ncu): the FP64 form is FP64-pipe bound.
@@ -528,8 +530,9 @@ def gpu_arm(args):
                                           for k, v in r.items()},
                    "unit_note": "forward_tflops: executed BF16 MMA work "
                                 "(layers of 32x32 channels, the first "
-                                "with 16 input channels, the last with "
-                                "16 output rows) / wall time per "
+                                "with 16 input channels, the last as "
+                                "3 MMAs of N = 48 per y-line) / wall "
+                                "time per "
                                 "pass, passes issued back to back; "
                                 "forward_tflops_useful: the real layer "
                                 "shapes 5-32-32-32-4; *_call_ms: one call "

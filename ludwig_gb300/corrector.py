@@ -249,6 +249,14 @@ def rollout(model, nfine, seed, t0, ncoarse_steps, every, params=FINE_PARAMS,
     return out
 
 
+# Executed forward work of the default convolution forms, in units of a
+# 32 -> 32 layer: the first layer reads 16 input channels (0.5); where
+# nz = 128 the last layer runs folded, 3 MMAs of N = 48 per y-line and 18
+# y-lines per 16 outputs (0.1875 of a layer), else as a full layer.
+def default_exec_layers(nz):
+    return 2.5 + 0.1875 if nz == 128 else 3.5
+
+
 def time_network(model, x, t, reps=20, exec_layers=3.5):
     """Time per forward pass and per training step (forward, backward,
     Adam) on one pair, issued back to back (`forward_n`, `train_steps`:
@@ -280,10 +288,8 @@ def time_network(model, x, t, reps=20, exec_layers=3.5):
     step = (time.perf_counter() - t0) / reps
     n = model.nsites
     # executed MMA work: 4 convolutions forward in units of a 32 -> 32
-    # layer (exec_layers: the first with K = 16 of its 32 input channels,
-    # the 5 features and zeros, counts 0.5; the last counts 0.5 where its
-    # 4 outputs are computed as 16 rows, 1 otherwise), 3 backward-data and
-    # 4 weight gradients (28 of 27 taps), 2 * 128 * 32 * K per tile
+    # layer (exec_layers; default_exec_layers gives it for the default
+    # forms), 3 backward-data and 4 weight gradients (28 of 27 taps)
     flop_conv = 2.0 * n * 27 * 32 * 32
     flop_fwd = exec_layers * flop_conv
     flop_step = flop_fwd + 3 * flop_conv + 4 * flop_conv * 28.0 / 27.0
@@ -308,16 +314,23 @@ def bench(n, reps=20):
     x[4] += 1.0
     t = 0.1 * torch.randn((4, N), device="cuda", generator=g)
     torch.cuda.synchronize()
-    # the three-tap form (the default where nz = 128) computes the last
-    # layer's 4 outputs as 16 weight rows
+    # executed layers (in 32 x 32 layers): the three-tap last layer
+    # computes 16 weight rows a tap (0.5), the folded one (the default
+    # where nz = 128) 0.1875
     three = (n == 128)
+    folded = default_exec_layers(128)
     res = {"default": time_network(model, x, t, reps,
-                                   3.0 if three else 3.5)}
+                                   default_exec_layers(n))}
     for mode, name in ((0, "per_tap"), (1, "line_planes"),
-                       (2, "line_swizzled"), (3, "line_three_taps")):
+                       (2, "line_swizzled"), (3, "line_three_taps"),
+                       (4, "line_folded_last")):
         model.line_reuse(mode)
-        res[name] = time_network(model, x, t, reps,
-                                 3.0 if (mode == 3 and three) else 3.5)
+        ex = 3.5
+        if three and mode == 3:
+            ex = 3.0
+        if three and mode == 4:
+            ex = folded
+        res[name] = time_network(model, x, t, reps, ex)
     return res
 
 
@@ -388,7 +401,8 @@ def main(argv=None):
     sync()
     t_train = time.time() - t
     base1, corr1 = one_step_errors(model, X, T)
-    timing = time_network(model, X[0], T[0])
+    timing = time_network(model, X[0], T[0],
+                          exec_layers=default_exec_layers(model.n[2]))
     log("timing %s" % json.dumps(timing))
     del X, Y, T
     pf_hist = []

@@ -124,14 +124,27 @@ __device__ __forceinline__ bool tc_drain_wait(uint32_t bar, uint32_t parity,
   return tc_mbar_wait(bar, parity, &never, err);
 }
 
+/* GELU in the tanh form of Hendrycks and Gimpel (2016),
+ * 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3), evaluated as
+ * z sigma(2u) = z / (1 + exp(-2u)): one fast exponential and one fast
+ * division per value, and no cancellation where z < 0.  2u is held above
+ * -80 so that the divisor stays finite (the value there is below 1e-33
+ * in magnitude either way). */
+#define GELU_K0 1.5957691216057308f          /* 2 sqrt(2/pi) */
+#define GELU_K1 0.044715f
+
 __device__ __forceinline__ float gelu_f(float z) {
-  return 0.5f*z*(1.0f + erff(z*0.70710678118654752f));
+  const float v = fmaxf(GELU_K0*z*fmaf(GELU_K1*z, z, 1.0f), -80.0f);
+  return __fdividef(z, 1.0f + __expf(-v));
 }
 
+/* d/dz z sigma(2u) = s + z s (1 - s) d(2u)/dz, s = sigma(2u) */
 __device__ __forceinline__ float gelu_d_f(float z) {
-  const float cdf = 0.5f*(1.0f + erff(z*0.70710678118654752f));
-  const float pdf = expf(-0.5f*z*z)*0.39894228040143268f;
-  return cdf + z*pdf;
+  const float z2 = z*z;
+  const float v = fmaxf(GELU_K0*z*fmaf(GELU_K1, z2, 1.0f), -80.0f);
+  const float s = __fdividef(1.0f, 1.0f + __expf(-v));
+  const float dv = GELU_K0*fmaf(3.0f*GELU_K1, z2, 1.0f);
+  return fmaf(z*s*(1.0f - s), dv, s);
 }
 
 __device__ __forceinline__ void store_row_bf16(uint8_t * dst,
@@ -501,7 +514,18 @@ __device__ __forceinline__ void lds_ld4(uint32_t a, uint32_t v[4]) {
  * channel half through shared memory (an mbarrier per channel half and
  * tile parity, bounded waits).  Sums in another order than the one-box-per-tap kernel: equal to
  * FP32 rounding, not bit for bit. */
-template <int MODE, int SWZ, int CYC>
+/* FOLD = 1 (the last layer, 4 outputs, with CYC): the y taps go into N
+ * as well.  Each step takes one new y-line (x-1, x, x+1 at y') and issues
+ * one MMA per dx and K half with B = the 48 rows [dz][dy][4 outputs] (12
+ * of each 16 used; weights rearranged by k_cnn_wfold, nine 16-row blocks
+ * (dx, dz)), so that a tile costs 6 MMAs instead of 18.  The accumulator
+ * then holds, per dz, the contributions of line y' to the output lines
+ * y' + 1 (dy = -1), y' and y' - 1; the epilogue combines the dz taps as in
+ * the three-tap form and adds the three dy parts into three running output
+ * lines kept in registers, writing line y' - 1 once line y' has been
+ * added.  A run of output lines ya .. yb - 1 takes the lines ya - 1 .. yb:
+ * the same lines, in the same order, as the other forms load. */
+template <int MODE, int SWZ, int CYC, int FOLD>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
 k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	     const __grid_constant__ CUtensorMap tm_w, const ConvP p) {
@@ -559,10 +583,12 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   if (warp == 0 && lane == 0) {
     tc_prefetch_map(&tm_line);
     tc_prefetch_map(&tm_w);
-    /* the first nb output rows of every tap's weights */
+    /* the first nb output rows of every tap's weights (FOLD: of the
+     * nine (dx, dz) blocks) */
     const uint32_t wtap = (uint32_t) (CYC ? p.nb : CNN_C)*ROWB;
-    tc_mbar_arrive_tx(bW, CNN_NTAP*wtap);
-    for (int t = 0; t < CNN_NTAP; t++) {
+    constexpr int NTW = FOLD ? 9 : CNN_NTAP;
+    tc_mbar_arrive_tx(bW, NTW*wtap);
+    for (int t = 0; t < NTW; t++) {
       tc_tma_load_2d(sW + t*wtap, &tm_w, bW, 0, t*CNN_C);
     }
     /* y-lines are numbered in load order (sq); line sq fills ring slot
@@ -621,7 +647,45 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     bool ok = tc_mbar_wait(bW, 0, abort_flag, p.err);
     uint32_t sq = 0;                   /* y-lines consumed, as loaded */
     int i = 0;
-    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+    for (int it = blockIdx.x; ok && FOLD && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      /* one step per y-line ya - 1 .. yb, as loaded */
+      for (int y = ya - 1; y <= yb; y++, i++, sq++) {
+	const int acc = i & 1;
+	if (!tc_mbar_wait(bTEmpty + 8*acc, ((uint32_t) (i >> 1) & 1u) ^ 1u,
+			  abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	const uint32_t r = sq % LN_NY;
+	if (!tc_mbar_wait(bFull + 8*r, (sq/LN_NY) & 1u, abort_flag, p.err)) {
+	  ok = false;
+	  break;
+	}
+	tc_fence_after();
+	constexpr uint32_t DXS = LN_NY*LN_SLOT >> 4;
+	constexpr uint32_t DZS = 16 >> 4;
+	constexpr uint32_t KHA = 2*LN_CHUNK >> 4;
+	constexpr uint32_t KHB = 32 >> 4;
+	const uint32_t a0 = alo0 + r*(LN_SLOT >> 4) + DZS;
+	const uint32_t d = tmem + (uint32_t) acc*NACC;
+	#pragma unroll
+	for (int dxi = 0; dxi < 3; dxi++) {
+	  #pragma unroll
+	  for (int kh = 0; kh < 2; kh++) {
+	    if (kh >= p.khn) break;
+	    tc_mma_bf16_w(d, a0 + (uint32_t) dxi*DXS + kh*KHA, ahi,
+			  blo0 + (uint32_t) (3*dxi*nbk*ROWB >> 4) + kh*KHB,
+			  bhi, idesc, (uint32_t) ((dxi | kh) != 0));
+	  }
+	}
+	/* no later step reads this line */
+	tc_commit(bRel + 8*r);
+	tc_commit(bTFull + 8*acc);
+      }
+    }
+    for (int it = blockIdx.x; ok && !FOLD && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
       for (int y = ya; y < yb; y++, i++) {
@@ -705,7 +769,12 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
-      for (int y = ya; y < yb; y++, i++) {
+      /* FOLD: the output lines y - 1, y, y + 1 of this thread's site */
+      float o0[LGBK_CNN_NOUT], o1[LGBK_CNN_NOUT], o2[LGBK_CNN_NOUT];
+      #pragma unroll
+      for (int c = 0; c < LGBK_CNN_NOUT; c++) o0[c] = o1[c] = o2[c] = 0.0f;
+      /* FOLD: y runs over the lines ya - 1 .. yb, else the outputs */
+      for (int y = ya - FOLD; y < yb + FOLD; y++, i++) {
 	const int acc = i & 1;
 	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
 				abort_flag, p.err);
@@ -778,7 +847,31 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	  tc_fence_before();
 	  tc_mbar_arrive(bTEmpty + 8*acc);
 	}
-	conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
+	if (FOLD) {
+	  /* column 4 dyi + c: the part of output line y + 1 - dyi */
+	  #pragma unroll
+	  for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	    o2[c] += __uint_as_float(r[c]);
+	    o1[c] += __uint_as_float(r[4 + c]);
+	    o0[c] += __uint_as_float(r[8 + c]);
+	  }
+	  if (y - 1 >= ya) {
+	    const long long sy = ((long long) x*g.ny + (y - 1))*g.nz + z0 + m;
+	    #pragma unroll
+	    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	      p.outf[c*g.nsites + sy] = o0[c] + bias[c];
+	    }
+	  }
+	  #pragma unroll
+	  for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	    o0[c] = o1[c];
+	    o1[c] = o2[c];
+	    o2[c] = 0.0f;
+	  }
+	}
+	else {
+	  conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
+	}
       }
     }
   }
@@ -792,18 +885,18 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   }
 }
 
-template <int MODE, int SWZ, int CYC>
+template <int MODE, int SWZ, int CYC, int FOLD = 0>
 static cudaError_t launch_line(const lgbk_cnn_geom_t * g,
 			       const CUtensorMap & ml, const CUtensorMap & mw,
 			       const ConvP & p, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_conv3_line<MODE, SWZ, CYC>,
+  cudaError_t e = cudaFuncSetAttribute(k_conv3_line<MODE, SWZ, CYC, FOLD>,
     cudaFuncAttributeMaxDynamicSharedMemorySize, LN_SMEM);
   if (e != cudaSuccess) return e;
   int grid = line_items(*g);
   const int nsm = num_sms();
   if (grid > nsm) grid = nsm;
-  k_conv3_line<MODE, SWZ, CYC><<<grid, CONV_THREADS, LN_SMEM, s>>>(ml, mw,
-								    p);
+  k_conv3_line<MODE, SWZ, CYC, FOLD><<<grid, CONV_THREADS, LN_SMEM, s>>>(
+    ml, mw, p);
   return cudaSuccess;
 }
 
@@ -812,9 +905,19 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
 			       const CUtensorMap * ml, int line_kind,
 			       const CUtensorMap & mw, const ConvP & p,
 			       cudaStream_t s) {
-  cudaError_t e;
+  cudaError_t e = cudaSuccess;
   if (ml) {
-    if (line_kind == 3) {
+    if (line_kind == 4) {
+      /* y taps folded into N: the last layer only */
+      if (MODE != LGBK_CNN_FWD_OUT || g->nz != LGBK_CNN_TILE ||
+	  p.nb != 16) {
+	return cudaErrorInvalidValue;
+      }
+      if constexpr (MODE == LGBK_CNN_FWD_OUT) {
+	e = launch_line<MODE, 0, 1, 1>(g, *ml, mw, p, s);
+      }
+    }
+    else if (line_kind == 3) {
       if (g->nz != LGBK_CNN_TILE) return cudaErrorInvalidValue;
       e = launch_line<MODE, 0, 1>(g, *ml, mw, p, s);
     }
@@ -864,7 +967,11 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int w
   /* 16 weight rows per tap (tm_w boxes of 16 rows): only where the
    * three-tap line form runs */
   if (wrows != CNN_C &&
-      !(wrows == 16 && ml && line_kind == 3 && g->nz == LGBK_CNN_TILE)) {
+      !(wrows == 16 && ml && (line_kind == 3 || line_kind == 4) &&
+	g->nz == LGBK_CNN_TILE)) {
+    return (int) cudaErrorInvalidValue;
+  }
+  if (line_kind == 4 && (wrows != 16 || mode != LGBK_CNN_FWD_OUT)) {
     return (int) cudaErrorInvalidValue;
   }
   cudaStream_t s = (cudaStream_t) stream;
@@ -1637,6 +1744,32 @@ extern "C" int lgbk_cnn_wprep(const float * w, void * wf, void * wt,
 			      void * stream) {
   k_cnn_wprep<<<(LGBK_CNN_WL + 255)/256, 256, 0, (cudaStream_t) stream>>>(
     w, (__nv_bfloat16 *) wf, (__nv_bfloat16 *) wt);
+  return (int) cudaGetLastError();
+}
+
+/* The last layer's weights for the folded form: block b = 3 dxi + dzi
+ * (32-row stride, 16 rows loaded), row 4 dyi + c = tap (dxi, dyi, dzi),
+ * output c; rows 12..15 zero */
+__global__ void k_cnn_wfold(const __nv_bfloat16 * __restrict__ wf,
+			    __nv_bfloat16 * __restrict__ wfold) {
+  const int k = blockIdx.x*blockDim.x + threadIdx.x;
+  if (k >= 9*32*32) return;
+  const int ci = k % 32;
+  const int row = (k/32) % 32;
+  const int b = k/1024;
+  const int dxi = b/3, dzi = b % 3;
+  __nv_bfloat16 h = __float2bfloat16_rn(0.0f);
+  if (row < 3*LGBK_CNN_NOUT) {
+    const int dyi = row/LGBK_CNN_NOUT, c = row % LGBK_CNN_NOUT;
+    const int t = 9*dxi + 3*dyi + dzi;
+    h = wf[(t*32 + c)*32 + ci];
+  }
+  wfold[k] = h;
+}
+
+extern "C" int lgbk_cnn_wfold(const void * wf, void * wfold, void * stream) {
+  k_cnn_wfold<<<(9*32*32 + 255)/256, 256, 0, (cudaStream_t) stream>>>(
+    (const __nv_bfloat16 *) wf, (__nv_bfloat16 *) wfold);
   return (int) cudaGetLastError();
 }
 

@@ -111,6 +111,10 @@ int lgbk_cnn_adam(float * w, float * m, float * v, const float * grad,
 /* Master weights [27][32][32] fp32 -> bf16 forward copy (same order) and
  * the flipped, transposed copy wt[26 - t][c][n] = w[t][n][c] */
 int lgbk_cnn_wprep(const float * w, void * wf, void * wt, void * stream);
+/* The last layer's bf16 weights (wf, [27][32][32]) rearranged for the
+ * folded line form (line_kind 4): wfold [9][32][32], block 3 dxi + dzi,
+ * row 4 dyi + c */
+int lgbk_cnn_wfold(const void * wf, void * wfold, void * stream);
 
 /* phi += os0 out0; du = os out1..3; u += du; f_p += 3 w_p rho c_p.du
  * (FP32 deviation storage of f) */

@@ -40,6 +40,7 @@ struct ludwig_gb_cnn_s {
   CUtensorMap tm_g[NL + 1];    /* padded dL/dz_1 .. dL/dz_4 (index 1..4) */
   CUtensorMap tm_wf[NL];       /* bf16 weights, forward order */
   CUtensorMap tm_wf16;         /* the last layer's, 16 rows a tap */
+  CUtensorMap tm_wfold;        /* ... rearranged for the folded form */
   CUtensorMap tm_wt[NL];       /* bf16 weights, flipped and transposed */
   CUtensorMap tm_actl[NL];     /* the same buffers as 8 x 130 line boxes */
   CUtensorMap tm_gl[NL + 1];
@@ -55,6 +56,7 @@ struct ludwig_gb_cnn_s {
   float * adam_v;
   void * wf[NL];
   void * wt[NL];
+  void * wfold;                /* bf16 [9][32][32] */
   void * act[NL];
   void * zpre[NL];             /* bf16 [N][32], index 1..3 */
   void * gpad[NL + 1];         /* index 1..4 */
@@ -184,6 +186,7 @@ int ludwig_gb_cnn_free(ludwig_gb_cnn_t * m) {
     cudaFree(m->act[l]); cudaFree(m->zpre[l]);
   }
   for (int l = 0; l <= NL; l++) cudaFree(m->gpad[l]);
+  cudaFree(m->wfold);
   cudaFree(m->out4); cudaFree(m->part); cudaFree(m->red);
   cudaFree(m->loss_dev); cudaFree(m->err_dev);
   free(m);
@@ -196,6 +199,8 @@ static int wprep(ludwig_gb_cnn_t * m) {
     int rc = lgbk_cnn_wprep(m->params + l*PL, m->wf[l], m->wt[l], s);
     if (rc) return ck(rc, "cnn wprep");
   }
+  int rc = lgbk_cnn_wfold(m->wf[NL - 1], m->wfold, s);
+  if (rc) return ck(rc, "cnn wfold");
   m->wprep_valid = 1;
   return LUDWIG_GB_OK;
 }
@@ -238,6 +243,7 @@ int ludwig_gb_cnn_create(const int n[3], unsigned long long seed,
     if (!rc && l > 0) rc = dalloc(&m->zpre[l], N*64);
   }
   for (int l = 1; l <= NL && !rc; l++) rc = dalloc(&m->gpad[l], prow);
+  if (!rc) rc = dalloc(&m->wfold, 2*9*32*32);
   if (!rc) rc = dalloc((void **) &m->out4, sizeof(float)*4*N);
   if (!rc) rc = dalloc((void **) &m->part, sizeof(float)*nblk*WL);
   if (!rc) rc = dalloc((void **) &m->red,
@@ -252,13 +258,16 @@ int ludwig_gb_cnn_create(const int n[3], unsigned long long seed,
     if (!rc) rc = map_rows(&m->tm_wt[l], m->wt[l], LGBK_CNN_NTAP*32, 32);
   }
   if (!rc) rc = map_rows(&m->tm_wf16, m->wf[NL - 1], LGBK_CNN_NTAP*32, 16);
+  if (!rc) rc = map_rows(&m->tm_wfold, m->wfold, 9*32, 16);
   for (int l = 1; l <= NL && !rc; l++) {
     rc = map_rows(&m->tm_g[l], m->gpad[l], g.rows, g.bz);
   }
   m->line_ok = (g.bz == LGBK_CNN_TILE && g.lpt == 1);
-  /* default: three z taps per MMA where a line is the whole z extent
-   * (0.83 against 1.15 ms per forward pass at 128^3), planes otherwise */
-  m->line_on = m->line_ok ? ((g.nz == LGBK_CNN_TILE) ? 3 : 1) : 0;
+  /* default: three z taps per MMA where a line is the whole z extent,
+   * the last layer's y taps folded into its MMAs too (0.584 against 0.590
+   * ms per forward pass at 128^3, 0.916 with one tap per MMA), planes
+   * otherwise */
+  m->line_on = m->line_ok ? ((g.nz == LGBK_CNN_TILE) ? 4 : 1) : 0;
   for (int l = 0; l < NL && !rc && m->line_ok; l++) {
     rc = map_lines(&m->tm_actl[l], m->act[l], g.rows, 0);
     if (!rc) rc = map_lines(&m->tm_acts[l], m->act[l], g.rows, 1);
@@ -365,16 +374,22 @@ static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
 
 /* 1: the line-reuse convolution where the extents allow it; 2: the same
  * with swizzled line boxes; 3: the same with the three z taps of a line
- * in one MMA where nz = 128 (1 otherwise; the default is 3 where nz = 128,
- * else 1); 0: one box per tap */
+ * in one MMA where nz = 128; 4: as 3, and the last layer with the y taps
+ * folded into the MMA as well (3 and 4 fall back to 1 where nz != 128;
+ * the default is 4 where nz = 128, else 1); 0: one box per tap */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int mode) {
-  if (m == NULL || mode < 0 || mode > 3) {
+  if (m == NULL || mode < 0 || mode > 4) {
     return lgb_internal_err(LUDWIG_GB_EINVAL,
-			    "cnn_line_reuse: 0, 1, 2 or 3");
+			    "cnn_line_reuse: 0, 1, 2, 3 or 4");
   }
-  if (mode == 3 && m->g.nz != LGBK_CNN_TILE) mode = 1;
+  if (mode >= 3 && m->g.nz != LGBK_CNN_TILE) mode = 1;
   m->line_on = m->line_ok ? mode : 0;
   return LUDWIG_GB_OK;
+}
+
+/* the line form of the hidden layers and of every backward convolution */
+static int lkind(const ludwig_gb_cnn_t * m) {
+  return (m->line_on == 4) ? 3 : m->line_on;
 }
 
 static int check_err(ludwig_gb_cnn_t * m) {
@@ -417,18 +432,20 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
     if (l < NL - 1) {
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_GELU, kin_of(l), LGBK_CNN_C,
 			 &m->tm_act[l],
-			 lmap(m, 1, l), m->line_on, &m->tm_wf[l], b, NULL,
+			 lmap(m, 1, l), lkind(m), &m->tm_wf[l], b, NULL,
 			 train ? m->zpre[l + 1] : NULL, m->act[l + 1], NULL,
 			 m->err_dev, s);
       if (!rc) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
     }
     else {
-      /* the 4 outputs: 16 weight rows a tap where the three-tap form runs */
-      const int w16 = (m->line_on == 3);
+      /* the 4 outputs: 16 weight rows a tap where the three-tap form
+       * runs; the folded blocks in the folded form */
+      const int w16 = (m->line_on >= 3);
+      const CUtensorMap * tw = (m->line_on == 4) ? &m->tm_wfold
+	: (w16 ? &m->tm_wf16 : &m->tm_wf[l]);
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l),
 			 w16 ? 16 : LGBK_CNN_C, &m->tm_act[l],
-			 lmap(m, 1, l), m->line_on,
-			 w16 ? &m->tm_wf16 : &m->tm_wf[l], b, NULL, NULL,
+			 lmap(m, 1, l), m->line_on, tw, b, NULL, NULL,
 			 NULL, out ? out : m->out4, m->err_dev, s);
     }
     if (rc) return ck(rc, "cnn conv");
@@ -454,7 +471,7 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
     if (l == 0) break;
     rc = lgbk_cnn_conv(g, LGBK_CNN_BWD_GELU, LGBK_CNN_C, LGBK_CNN_C,
 		       &m->tm_g[l + 1],
-		       lmap(m, 0, l + 1), m->line_on, &m->tm_wt[l], NULL, m->zpre[l],
+		       lmap(m, 0, l + 1), lkind(m), &m->tm_wt[l], NULL, m->zpre[l],
 		       NULL, m->gpad[l], NULL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_halo(g, m->gpad[l], s);
     if (rc) return ck(rc, "cnn conv (backward)");
@@ -659,7 +676,7 @@ int ludwig_gb_cnn_conv3(ludwig_gb_cnn_t * m, const float * a, const float * w,
   if (!rc) rc = lgbk_cnn_wprep(w, m->wf[0], m->wt[0], s);
   if (!rc) rc = lgbk_cnn_conv(&m->g, LGBK_CNN_RAW, LGBK_CNN_C, LGBK_CNN_C,
 			      &m->tm_act[0],
-			      lmap(m, 1, 0), m->line_on,
+			      lmap(m, 1, 0), lkind(m),
 			      flip ? &m->tm_wt[0] : &m->tm_wf[0],
 			      flip ? NULL : b, NULL, NULL, NULL, out,
 			      m->err_dev, s);

@@ -11,7 +11,7 @@
  *  Network (the corrector of a 2x-coarsened binary fluid):
  *    a0 = features (5 real channels, zero-padded to 32)
  *    z_l = b_l + sum_t sum_c a_{l-1}(s + e_t)[c] W_l[t][n][c]   (3^3 taps)
- *    a_l = GELU(z_l), l = 1, 2, 3;   output = z_4 channels 0..3
+ *    a_l = GELU(z_l) (tanh form), l = 1, 2, 3;   output = z_4 channels 0..3
  *  Periodic neighbours; tap t = (dx+1)*9 + (dy+1)*3 + (dz+1).
  *  Loss = (1/N) sum_s sum_{c<4} (z_4[c](s) - target[c](s))^2.
  *
@@ -49,11 +49,19 @@ static double bf16r(double v) {
 
 static double rnd(int emulate, double v) { return emulate ? bf16r(v) : v; }
 
-static double gelu(double z) { return 0.5*z*(1.0 + erf(z/sqrt(2.0))); }
+/* GELU, tanh form (Hendrycks and Gimpel 2016):
+ * 0.5 z (1 + tanh(u)) = z sigma(2u), u = sqrt(2/pi) (z + 0.044715 z^3) */
+static double gelu_v(double z) {
+  const double k0 = 2.0*sqrt(2.0/3.14159265358979323846);
+  return k0*z*(1.0 + 0.044715*z*z);
+}
+
+static double gelu(double z) { return z/(1.0 + exp(-gelu_v(z))); }
 
 static double gelu_d(double z) {
-  const double pdf = exp(-0.5*z*z)/sqrt(2.0*3.14159265358979323846);
-  return 0.5*(1.0 + erf(z/sqrt(2.0))) + z*pdf;
+  const double k0 = 2.0*sqrt(2.0/3.14159265358979323846);
+  const double s = 1.0/(1.0 + exp(-gelu_v(z)));
+  return s + z*s*(1.0 - s)*k0*(1.0 + 3.0*0.044715*z*z);
 }
 
 static long long nbr(const int n[3], long long s, int t, int sign) {

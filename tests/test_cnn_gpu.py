@@ -134,11 +134,18 @@ def _data(rng, N):
     return in5, t4
 
 
-@pytest.mark.parametrize("n", [(8, 8, 32), (4, 4, 128)])
-def test_network_loss_and_gradient_vs_oracle(gb, orc, n):
+@pytest.mark.parametrize("n,mode", [((8, 8, 32), None), ((4, 4, 128), None),
+                                    ((4, 4, 128), 3), ((4, 4, 128), 4),
+                                    ((3, 17, 128), 4)])
+def test_network_loss_and_gradient_vs_oracle(gb, orc, n, mode):
+    """The whole network (default form, or the given line form: 3 three z
+    taps per MMA, 4 the same with the last layer's y taps folded into its
+    MMAs) against the oracle with the same BF16 rounding points."""
     N = n[0] * n[1] * n[2]
     rng = np.random.default_rng(13)
     m = gb.Corrector(n, seed=7)
+    if mode is not None:
+        m.line_reuse(mode)
     one = np.ones(5, np.float32)
     m.set_scales(np.zeros(5), one, np.ones(4))
     # a trained-looking last layer: scale it up so every layer matters
@@ -356,13 +363,17 @@ def test_three_tap_forward_matches_one_tap(gb, n):
     m.set_params(p)
     x = dev(0.3 * rng.standard_normal((5, N)))
     outs = {}
-    for mode in (1, 3):
+    for mode in (1, 3, 4):
         m.line_reuse(mode)
         o = torch.empty((4, N), dtype=torch.float32, device="cuda")
         m.forward(x.data_ptr(), o.data_ptr())
         outs[mode] = o
     d = (outs[3] - outs[1]).abs().max().item()
     assert d <= 1e-2 * outs[1].abs().max().item(), d
+    # 4 differs from 3 in the last layer only, whose inputs are the same
+    # BF16 activations: its sums in another order, FP32 rounding apart
+    d = (outs[4] - outs[3]).abs().max().item()
+    assert d <= 1e-5 * outs[3].abs().max().item(), d
 
 
 def test_bounded_wait_times_out_and_context_survives(gb):

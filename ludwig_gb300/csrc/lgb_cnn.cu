@@ -463,7 +463,7 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
 #define LN_NSLOT  (3*LN_NY)             /* 3 dx x LN_NY y-lines */
 #define LN_YRUN   16
 #define LN_TXLINE (4*LN_ROWS*16)        /* bytes of one line (4 planes) */
-#define LN_XCH   2048                  /* boundary-row exchange (CYC) */
+#define LN_XCH   4096                  /* boundary-row exchange (CYC) */
 #define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256 + LN_XCH)
 
 __device__ __forceinline__ void line_item(const lgbk_cnn_geom_t & g, int it,
@@ -551,6 +551,9 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   /* accumulator columns per tile (three taps of nb outputs each in the
    * three-tap form) and TMEM columns allocated */
   const int nbk = CYC ? p.nb : CNN_C;
+  /* the two groups of epilogue warps take alternate tiles (three-tap
+   * form, not folded) */
+  constexpr bool ALT = CYC && !FOLD;
   const uint32_t NACC = CYC ? 3u*(uint32_t) nbk : (uint32_t) CNN_C;
   constexpr uint32_t TCOLS = CYC ? 256 : CONV_TMEM_COLS;
 
@@ -568,8 +571,9 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     tc_mbar_init(bW, 1);
     tc_mbar_init(bTFull, 1);
     tc_mbar_init(bTFull + 8, 1);
-    tc_mbar_init(bTEmpty, CONV_EPI_THREADS);
-    tc_mbar_init(bTEmpty + 8, CONV_EPI_THREADS);
+    /* ALT: one group of four epilogue warps releases each accumulator */
+    tc_mbar_init(bTEmpty, ALT ? 128 : CONV_EPI_THREADS);
+    tc_mbar_init(bTEmpty + 8, ALT ? 128 : CONV_EPI_THREADS);
     tc_mbar_init(bFin, 1);
     *abort_flag = 0;
     tc_fence_barrier_init();
@@ -756,6 +760,119 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     tc_commit(bFin);
     tc_drain_wait(bFin, 0, p.err);
   }
+  else if (ALT && warp >= 2) {
+    /* Warps 2-5 take the even tiles (accumulator 0), warps 6-9 the odd
+     * ones, so that two tiles' epilogues overlap; warp w reads TMEM lanes
+     * 32 (w % 4) .. + 31 and both channel halves (one where the layer has
+     * 16 weight rows a tap).  The shifted terms of the interior rows are
+     * added before the edge rows' exchange completes. */
+    const int grp = (warp - 2) >> 2;
+    const int q = warp & 3;
+    const int m = q*32 + lane;
+    const bool two = (nbk > 16);
+    float bias[32];
+    #pragma unroll
+    for (int n = 0; n < 32; n++) bias[n] = p.bias ? p.bias[n] : 0.0f;
+    int i = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya; y < yb; y++, i++) {
+	if ((i & 1) != grp) continue;
+	const int acc = grp;
+	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
+				abort_flag, p.err);
+	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
+	tc_fence_after();
+	const uint32_t ta = tmem + (uint32_t) acc*NACC
+	  + ((uint32_t) (q*32) << 16);
+	uint32_t rm0[16], r0[16], rp0[16], rm1[16], r1[16], rp1[16];
+	tc_tmem_ld16_async(ta, rm0);                 /* D_-1 */
+	tc_tmem_ld16_async(ta + nbk, r0);            /* D_0 */
+	tc_tmem_ld16_async(ta + 2*nbk, rp0);         /* D_+1 */
+	if (two) {
+	  tc_tmem_ld16_async(ta + 16, rm1);
+	  tc_tmem_ld16_async(ta + nbk + 16, r1);
+	  tc_tmem_ld16_async(ta + 2*nbk + 16, rp1);
+	}
+	tc_tmem_wait_ld16x3(rm0, r0, rp0);
+	if (two) tc_tmem_wait_ld16x3(rm1, r1, rp1);
+	tc_fence_before();
+	tc_mbar_arrive(bTEmpty + 8*acc);
+	/* edge rows: slot [group][buffer][quarter] of 256 bytes, lane 31's
+	 * D_-1 (bytes 0-127, both halves) and lane 0's D_+1 (128-255); a
+	 * group's consecutive tiles alternate between two buffers */
+	const int xb = grp*2 + ((i >> 1) & 1);
+	const uint32_t sx = sXch + (uint32_t) (xb*4)*256u;
+	if (lane == 31) {
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) {
+	    lds_st4(sx + (uint32_t) q*256u + 16u*k, rm0 + 4*k);
+	    if (two) lds_st4(sx + (uint32_t) q*256u + 64u + 16u*k, rm1 + 4*k);
+	  }
+	  tc_mbar_arrive(bX + 8*xb);
+	}
+	if (lane == 0) {
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) {
+	    lds_st4(sx + (uint32_t) q*256u + 128u + 16u*k, rp0 + 4*k);
+	    if (two) lds_st4(sx + (uint32_t) q*256u + 192u + 16u*k, rp1 + 4*k);
+	  }
+	  tc_mbar_arrive(bX + 8*xb);
+	}
+	/* out(r) = D_-1[r - 1] + D_0[r] + D_+1[r + 1]: within the warp by
+	 * shuffles; lane 0's D_-1 and lane 31's D_+1 term come next */
+	#pragma unroll
+	for (int n = 0; n < 16; n++) {
+	  float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm0[n]), 1);
+	  float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp0[n]), 1);
+	  if (lane == 0) dm = 0.0f;
+	  if (lane == 31) dp = 0.0f;
+	  r0[n] = __float_as_uint((__uint_as_float(r0[n]) + dm) + dp);
+	}
+	if (two) {
+	  #pragma unroll
+	  for (int n = 0; n < 16; n++) {
+	    float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm1[n]), 1);
+	    float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp1[n]),
+					1);
+	    if (lane == 0) dm = 0.0f;
+	    if (lane == 31) dp = 0.0f;
+	    r1[n] = __float_as_uint((__uint_as_float(r1[n]) + dm) + dp);
+	  }
+	}
+	const bool okx = tc_mbar_wait(bX + 8*xb, (uint32_t) (i >> 2) & 1u,
+				      abort_flag, p.err);
+	if (!__all_sync(0xffffffffu, okx)) { ok = false; break; }
+	if (lane == 0 || lane == 31) {
+	  /* lane 0: row 32 q - 1's D_-1; lane 31: row 32 q + 32's D_+1 */
+	  const uint32_t src = (lane == 0)
+	    ? sx + (uint32_t) ((q + 3) & 3)*256u
+	    : sx + (uint32_t) ((q + 1) & 3)*256u + 128u;
+	  uint32_t ev[16];
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) lds_ld4(src + 16u*k, ev + 4*k);
+	  #pragma unroll
+	  for (int n = 0; n < 16; n++) {
+	    r0[n] = __float_as_uint(__uint_as_float(r0[n])
+				    + __uint_as_float(ev[n]));
+	  }
+	  if (two) {
+	    #pragma unroll
+	    for (int k = 0; k < 4; k++) lds_ld4(src + 64u + 16u*k, ev + 4*k);
+	    #pragma unroll
+	    for (int n = 0; n < 16; n++) {
+	      r1[n] = __float_as_uint(__uint_as_float(r1[n])
+				      + __uint_as_float(ev[n]));
+	    }
+	  }
+	}
+	conv_epilogue<MODE>(p, bias, x, y, z0 + m, 0, r0);
+	if (two) conv_epilogue<MODE>(p, bias + 16, x, y, z0 + m, 16, r1);
+      }
+    }
+  }
   else if (warp >= 2) {
     /* warp w reads TMEM lanes 32*(w % 4) .. +31, columns c0 .. c0+15 */
     const int q = warp & 3;
@@ -821,25 +938,31 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	    }
 	    tc_mbar_arrive(bX + 8*xb);
 	  }
+	  /* the interior rows' shifted terms while the exchange completes */
+	  #pragma unroll
+	  for (int n = 0; n < 16; n++) {
+	    float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[n]), 1);
+	    float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[n]), 1);
+	    if (lane == 0) dm = 0.0f;
+	    if (lane == 31) dp = 0.0f;
+	    r[n] = __float_as_uint((__uint_as_float(r[n]) + dm) + dp);
+	  }
 	  const bool okx = tc_mbar_wait(bX + 8*xb, (uint32_t) (i >> 1) & 1u,
 					abort_flag, p.err);
 	  if (!__all_sync(0xffffffffu, okx)) { ok = false; break; }
 	  /* lane 0: row 32 q - 1's D_-1; lane 31: row 32 q + 32's D_+1 */
-	  uint32_t ev[16];
 	  if (lane == 0 || lane == 31) {
+	    uint32_t ev[16];
 	    const uint32_t src = (lane == 0)
 	      ? sx + (uint32_t) ((q + 3) & 3)*128u
 	      : sx + (uint32_t) ((q + 1) & 3)*128u + 64u;
 	    #pragma unroll
 	    for (int k = 0; k < 4; k++) lds_ld4(src + 16u*k, ev + 4*k);
-	  }
-	  #pragma unroll
-	  for (int n = 0; n < 16; n++) {
-	    float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[n]), 1);
-	    float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[n]), 1);
-	    if (lane == 0) dm = __uint_as_float(ev[n]);
-	    if (lane == 31) dp = __uint_as_float(ev[n]);
-	    r[n] = __float_as_uint((__uint_as_float(r[n]) + dm) + dp);
+	    #pragma unroll
+	    for (int n = 0; n < 16; n++) {
+	      r[n] = __float_as_uint(__uint_as_float(r[n])
+				     + __uint_as_float(ev[n]));
+	    }
 	  }
 	}
 	else {
@@ -1449,38 +1572,45 @@ extern "C" int lgbk_wait_selftest(int * err, void * stream) {
  * x; the two z faces for interior x and y), 4 threads (16 bytes each) per
  * row; each image is copied from its interior source row. */
 __global__ void k_cnn_halo(lgbk_cnn_geom_t g, uint4 * __restrict__ p) {
-  const long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  const int Z = g.nz + 2, Y = g.ny + 2;
-  const long long nxf = 2LL*Y*Z, nyf = 2LL*g.nx*Z, nzf = 2LL*g.nx*g.ny;
-  const long long h = i >> 2;
-  const int q = (int) (i & 3);
+  /* 32-bit arithmetic: the padded rows number below 2^31, their halo
+   * rows far fewer */
+  const unsigned i = blockIdx.x*blockDim.x + threadIdx.x;
+  const unsigned Z = (unsigned) g.nz + 2u, Y = (unsigned) g.ny + 2u;
+  const unsigned nx = (unsigned) g.nx, ny = (unsigned) g.ny;
+  const unsigned nxf = 2u*Y*Z, nyf = 2u*nx*Z, nzf = 2u*nx*ny;
+  const unsigned h = i >> 2;
+  const int q = (int) (i & 3u);
   int xp, yp, zp;
   if (h < nxf) {
-    zp = (int) (h % Z);
-    const long long r = h / Z;
-    yp = (int) (r % Y);
-    xp = (r / Y) ? g.nx + 1 : 0;
+    const unsigned r = h / Z;
+    zp = (int) (h - r*Z);
+    const unsigned f = r / Y;
+    yp = (int) (r - f*Y);
+    xp = f ? g.nx + 1 : 0;
   }
   else if (h < nxf + nyf) {
-    const long long k = h - nxf;
-    zp = (int) (k % Z);
-    const long long r = k / Z;
-    xp = 1 + (int) (r % g.nx);
-    yp = (r / g.nx) ? g.ny + 1 : 0;
+    const unsigned k = h - nxf;
+    const unsigned r = k / Z;
+    zp = (int) (k - r*Z);
+    const unsigned f = r / nx;
+    xp = 1 + (int) (r - f*nx);
+    yp = f ? g.ny + 1 : 0;
   }
   else if (h < nxf + nyf + nzf) {
-    const long long k = h - nxf - nyf;
-    yp = 1 + (int) (k % g.ny);
-    const long long r = k / g.ny;
-    xp = 1 + (int) (r % g.nx);
-    zp = (r / g.nx) ? g.nz + 1 : 0;
+    const unsigned k = h - nxf - nyf;
+    const unsigned r = k / ny;
+    yp = 1 + (int) (k - r*ny);
+    const unsigned f = r / nx;
+    xp = 1 + (int) (r - f*nx);
+    zp = f ? g.nz + 1 : 0;
   }
   else {
     return;
   }
-  const int x = (xp - 1 + g.nx) % g.nx;
-  const int y = (yp - 1 + g.ny) % g.ny;
-  const int z = (zp - 1 + g.nz) % g.nz;
+  /* the interior source of each image: one period in from the face */
+  const int x = (xp == 0) ? g.nx - 1 : ((xp == g.nx + 1) ? 0 : xp - 1);
+  const int y = (yp == 0) ? g.ny - 1 : ((yp == g.ny + 1) ? 0 : yp - 1);
+  const int z = (zp == 0) ? g.nz - 1 : ((zp == g.nz + 1) ? 0 : zp - 1);
   const long long row = ((long long) xp*Y + yp)*Z + zp;
   const long long src = ((long long) (x + 1)*Y + (y + 1))*Z + (z + 1);
   p[row*4 + q] = p[src*4 + q];
@@ -1490,6 +1620,7 @@ extern "C" int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p,
 			     void * stream) {
   const long long Z = g->nz + 2, Y = g->ny + 2;
   const long long n = 4*(2*Y*Z + 2LL*g->nx*Z + 2LL*g->nx*g->ny);
+  if (n >= 0xffffffffLL) return (int) cudaErrorInvalidValue;
   k_cnn_halo<<<(unsigned int) ((n + 255)/256), 256, 0,
     (cudaStream_t) stream>>>(*g, (uint4 *) p);
   return (int) cudaGetLastError();
@@ -1506,13 +1637,15 @@ __global__ void k_cnn_features(lgbk_cnn_geom_t g, const float * __restrict__ phi
 			       const float * __restrict__ u,
 			       const float * __restrict__ rho, FeatP fp,
 			       uint8_t * __restrict__ p0, int full) {
-  const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  if (s >= g.nsites) return;
-  const int z = (int) (s % g.nz);
-  const long long r = s / g.nz;
-  const int y = (int) (r % g.ny);
-  const int x = (int) (r / g.ny);
-  const long long N = g.nsites;
+  /* 32-bit site index and decoding (the padded rows, and so the sites,
+   * number below 2^31) */
+  const unsigned s = blockIdx.x*blockDim.x + threadIdx.x;
+  if (s >= (unsigned) g.nsites) return;
+  const unsigned r = s / (unsigned) g.nz;
+  const int z = (int) (s - r*(unsigned) g.nz);
+  const int x = (int) (r / (unsigned) g.ny);
+  const int y = (int) (r - (unsigned) x*(unsigned) g.ny);
+  const size_t N = (size_t) g.nsites;
   float v[32];
   #pragma unroll
   for (int c = 0; c < 32; c++) v[c] = 0.0f;
@@ -1543,15 +1676,17 @@ extern "C" int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
 /* fp32 rows [s][32] -> padded bf16 rows (interior), then halo */
 __global__ void k_cnn_pack(lgbk_cnn_geom_t g, const float * __restrict__ src,
 			   uint8_t * __restrict__ p) {
-  const long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  if (s >= g.nsites) return;
-  const int z = (int) (s % g.nz);
-  const long long r = s / g.nz;
-  const int y = (int) (r % g.ny);
-  const int x = (int) (r / g.ny);
+  /* 32-bit site index and decoding (the padded rows, and so the sites,
+   * number below 2^31) */
+  const unsigned s = blockIdx.x*blockDim.x + threadIdx.x;
+  if (s >= (unsigned) g.nsites) return;
+  const unsigned r = s / (unsigned) g.nz;
+  const int z = (int) (s - r*(unsigned) g.nz);
+  const int x = (int) (r / (unsigned) g.ny);
+  const int y = (int) (r - (unsigned) x*(unsigned) g.ny);
   float v[32];
   #pragma unroll
-  for (int c = 0; c < 32; c++) v[c] = src[s*32 + c];
+  for (int c = 0; c < 32; c++) v[c] = src[(size_t) s*32 + c];
   store_row_bf16(p + (long long) prow(g, x, y, z)*ROWB, v);
 }
 
@@ -1577,10 +1712,11 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
   double acc = 0.0;
   for (long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x; s < N;
        s += (long long) gridDim.x*blockDim.x) {
-    const int z = (int) (s % g.nz);
-    const long long r = s / g.nz;
-    const int y = (int) (r % g.ny);
-    const int x = (int) (r / g.ny);
+    const unsigned su = (unsigned) s;             /* sites < 2^31 */
+    const unsigned r = su / (unsigned) g.nz;
+    const int z = (int) (su - r*(unsigned) g.nz);
+    const int x = (int) (r / (unsigned) g.ny);
+    const int y = (int) (r - (unsigned) x*(unsigned) g.ny);
     float v[32];
     #pragma unroll
     for (int c = 0; c < 32; c++) v[c] = 0.0f;

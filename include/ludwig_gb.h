@@ -825,8 +825,9 @@ int ludwig_gb_cnn_correct(ludwig_gb_cnn_t * cnn, lb_t * lb, field_t * phi,
  * 64-byte-swizzled rows, mode 3 (nz = 128; mode 1 otherwise) as mode 1
  * with the three z taps of a line in one tensor-core MMA, mode 4 (nz =
  * 128; mode 1 otherwise) as mode 3 with the last layer's three y taps in
- * its MMAs as well (one MMA per x neighbour line); mode 0: one TMA box per
- * tap (any supported extents).  Default: 4 where nz = 128, else 1 */
+ * its MMAs as well (one MMA per x neighbour line), mode 5 (nz = 128; mode
+ * 1 otherwise) as mode 4 on 64-byte-swizzled lines; mode 0: one TMA box
+ * per tap (any supported extents).  Default: 5 where nz = 128, else 1 */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * cnn, int mode);
 /* Failure detection of the tensor-core kernels: runs one device wait that
  * nothing satisfies; returns LUDWIG_GB_ETIMEOUT once the bounded wait has

@@ -1401,8 +1401,8 @@ class Corrector(_Obj):
         of 8 channels), 2 (swizzled rows), 3 (planes, the three z taps of
         a line in one MMA; nz = 128 only, 1 otherwise), 4 (as 3, and the
         last layer with its y taps folded into the MMAs as well; nz = 128
-        only), 0/False (one box per tap).  The default is 4 where
-        nz = 128, else 1."""
+        only), 5 (as 4 on swizzled lines; nz = 128 only), 0/False (one box
+        per tap).  The default is 5 where nz = 128, else 1."""
         _check(lib().ludwig_gb_cnn_line_reuse(self.ptr, int(mode)),
                "cnn_line_reuse")
 

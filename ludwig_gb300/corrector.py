@@ -323,12 +323,13 @@ def bench(n, reps=20):
                                    default_exec_layers(n))}
     for mode, name in ((0, "per_tap"), (1, "line_planes"),
                        (2, "line_swizzled"), (3, "line_three_taps"),
-                       (4, "line_folded_last")):
+                       (4, "line_folded_last"),
+                       (5, "line_three_taps_swizzled")):
         model.line_reuse(mode)
         ex = 3.5
         if three and mode == 3:
             ex = 3.0
-        if three and mode == 4:
+        if three and mode in (4, 5):
             ex = folded
         res[name] = time_network(model, x, t, reps, ex)
     return res

@@ -669,8 +669,8 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	}
 	tc_fence_after();
 	constexpr uint32_t DXS = LN_NY*LN_SLOT >> 4;
-	constexpr uint32_t DZS = 16 >> 4;
-	constexpr uint32_t KHA = 2*LN_CHUNK >> 4;
+	constexpr uint32_t DZS = (SWZ ? ROWB : 16) >> 4;
+	constexpr uint32_t KHA = (SWZ ? 32 : 2*LN_CHUNK) >> 4;
 	constexpr uint32_t KHB = 32 >> 4;
 	const uint32_t a0 = alo0 + r*(LN_SLOT >> 4) + DZS;
 	const uint32_t d = tmem + (uint32_t) acc*NACC;
@@ -1030,19 +1030,25 @@ static cudaError_t launch_conv(const lgbk_cnn_geom_t * g, const CUtensorMap & mi
 			       cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   if (ml) {
-    if (line_kind == 4) {
-      /* y taps folded into N: the last layer only */
+    if (line_kind == 4 || line_kind == 6) {
+      /* y taps folded into N: the last layer only; 6 on swizzled lines */
       if (MODE != LGBK_CNN_FWD_OUT || g->nz != LGBK_CNN_TILE ||
 	  p.nb != 16) {
 	return cudaErrorInvalidValue;
       }
       if constexpr (MODE == LGBK_CNN_FWD_OUT) {
-	e = launch_line<MODE, 0, 1, 1>(g, *ml, mw, p, s);
+	e = (line_kind == 6) ? launch_line<MODE, 1, 1, 1>(g, *ml, mw, p, s)
+	                     : launch_line<MODE, 0, 1, 1>(g, *ml, mw, p, s);
       }
     }
     else if (line_kind == 3) {
       if (g->nz != LGBK_CNN_TILE) return cudaErrorInvalidValue;
       e = launch_line<MODE, 0, 1>(g, *ml, mw, p, s);
+    }
+    else if (line_kind == 5) {
+      /* the three-tap form on 64-byte-swizzled lines (one box a line) */
+      if (g->nz != LGBK_CNN_TILE) return cudaErrorInvalidValue;
+      e = launch_line<MODE, 1, 1>(g, *ml, mw, p, s);
     }
     else if (line_kind == 2) {
       e = launch_line<MODE, 1, 0>(g, *ml, mw, p, s);
@@ -1090,11 +1096,12 @@ extern "C" int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int w
   /* 16 weight rows per tap (tm_w boxes of 16 rows): only where the
    * three-tap line form runs */
   if (wrows != CNN_C &&
-      !(wrows == 16 && ml && (line_kind == 3 || line_kind == 4) &&
+      !(wrows == 16 && ml && line_kind >= 3 && line_kind <= 6 &&
 	g->nz == LGBK_CNN_TILE)) {
     return (int) cudaErrorInvalidValue;
   }
-  if (line_kind == 4 && (wrows != 16 || mode != LGBK_CNN_FWD_OUT)) {
+  if ((line_kind == 4 || line_kind == 6) &&
+      (wrows != 16 || mode != LGBK_CNN_FWD_OUT)) {
     return (int) cudaErrorInvalidValue;
   }
   cudaStream_t s = (cudaStream_t) stream;
@@ -1284,13 +1291,29 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_g,
 }
 
 /* dw[k] = sum over blocks of part[b][k], fixed order */
+/* dw[k] = sum over the nblk per-CTA partials, in a fixed order: a block
+ * of 32 x 8 threads takes 32 consecutive k; thread (k, j) adds the
+ * partials b = j, j + 8, ... (eight chains of loads in flight per k), and
+ * thread (k, 0) then adds the eight chain sums in order j = 0 .. 7 */
 __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
 			       float * __restrict__ dw) {
-  const int k = blockIdx.x*blockDim.x + threadIdx.x;
-  if (k >= LGBK_CNN_WL) return;
+  __shared__ double red[8][32];
+  const int k = blockIdx.x*32 + threadIdx.x;
+  const int j = threadIdx.y;
   double s = 0.0;
-  for (int b = 0; b < nblk; b++) s += (double) part[(long long) b*LGBK_CNN_WL + k];
-  dw[k] = (float) s;
+  if (k < LGBK_CNN_WL) {
+    for (int b = j; b < nblk; b += 8) {
+      s += (double) part[(long long) b*LGBK_CNN_WL + k];
+    }
+  }
+  red[j][threadIdx.x] = s;
+  __syncthreads();
+  if (j == 0 && k < LGBK_CNN_WL) {
+    double t = 0.0;
+    #pragma unroll
+    for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
+    dw[k] = (float) t;
+  }
 }
 
 /*****************************************************************************
@@ -1531,7 +1554,8 @@ extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
     if (e != cudaSuccess) return (int) e;
     k_wgrad_tc<<<grid, WG_THREADS, WG_SMEM, s>>>(mg, mx, p);
   }
-  k_wgrad_reduce<<<(LGBK_CNN_WL + 255)/256, 256, 0, s>>>(part, grid, dw);
+  k_wgrad_reduce<<<(LGBK_CNN_WL + 31)/32, dim3(32, 8), 0, s>>>(part, grid,
+								 dw);
   return (int) cudaGetLastError();
 }
 
@@ -1717,16 +1741,20 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
     const int z = (int) (su - r*(unsigned) g.nz);
     const int x = (int) (r / (unsigned) g.ny);
     const int y = (int) (r - (unsigned) x*(unsigned) g.ny);
-    float v[32];
-    #pragma unroll
-    for (int c = 0; c < 32; c++) v[c] = 0.0f;
+    /* channels 0..3; 4..7 zero in the same 16 bytes; 8..31 of these
+     * rows are zero from the buffer's creation and nothing else writes
+     * this buffer */
+    float v[4];
     #pragma unroll
     for (int c = 0; c < LGBK_CNN_NOUT; c++) {
       const float d = out4[c*N + s] - t4[c*N + s];
       acc += (double) d*(double) d;
       v[c] = rn2*d;
     }
-    store_row_bf16(pg + (long long) prow(g, x, y, z)*ROWB, v);
+    const __nv_bfloat162 h0 = __floats2bfloat162_rn(v[0], v[1]);
+    const __nv_bfloat162 h1 = __floats2bfloat162_rn(v[2], v[3]);
+    *(uint4 *) (pg + (long long) prow(g, x, y, z)*ROWB) =
+      make_uint4(*(const uint32_t *) &h0, *(const uint32_t *) &h1, 0u, 0u);
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -1737,13 +1765,20 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
+/* 256 threads: thread j adds part[j], part[j + 256], ...; a fixed
+ * pairwise tree then adds the 256 sums */
 __global__ void k_cnn_loss_final(const double * __restrict__ part, int n,
 				 double rn, double * __restrict__ loss) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < n; i++) s += part[i];
-    *loss = s*rn;
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w /= 2) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) *loss = red[0]*rn;
 }
 
 extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
@@ -1752,49 +1787,53 @@ extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
   cudaStream_t s = (cudaStream_t) stream;
   k_cnn_loss_grad<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, out4, t4,
 						       (uint8_t *) pg, part);
-  k_cnn_loss_final<<<1, 32, 0, s>>>(part, LGBK_CNN_RED_BLOCKS,
+  k_cnn_loss_final<<<1, 256, 0, s>>>(part, LGBK_CNN_RED_BLOCKS,
 				    1.0/(double) g->nsites, loss);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int) e;
   return lgbk_cnn_halo(g, pg, stream);
 }
 
-/* Bias gradient: per-block channel sums of the interior rows.  Blocks
- * take whole z-lines (contiguous rows); thread t reads 16 bytes (8
- * channels, group t % 4) of every 64th row, so a warp reads 512
- * contiguous bytes. */
+/* Bias gradient: per-block channel sums of the interior rows.  Block b
+ * takes the z-lines b, b + G, ... (G blocks); a line's interior rows are
+ * contiguous, 4 x 16 bytes a row, and thread t reads the 16-byte pieces
+ * t, t + 256, ... of it, always channel group t % 4 (8 channels); two
+ * lines' loads are issued before either is summed. */
 __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ pg,
 				double * __restrict__ part) {
   __shared__ float red[256][9];
   const int cg = threadIdx.x & 3;
-  const int r0 = threadIdx.x >> 2;
   float acc[8];
   #pragma unroll
   for (int k = 0; k < 8; k++) acc[k] = 0.0f;
   const int nlines = g.nx*g.ny;
-  /* four lines at a time, their loads issued before any is summed */
-  for (int l0 = blockIdx.x; l0 < nlines; l0 += 4*gridDim.x) {
-    for (int z = r0; z < g.nz; z += 64) {
-      uint4 u[4];
-      #pragma unroll
-      for (int j = 0; j < 4; j++) {
-	const int ln = l0 + j*gridDim.x;
-	u[j] = make_uint4(0u, 0u, 0u, 0u);
-	if (ln < nlines) {
-	  const int x = ln / g.ny, y = ln % g.ny;
-	  u[j] = *(const uint4 *) (pg + ((long long) prow(g, x, y, z)*ROWB
-					 + 16*cg));
-	}
-      }
-      #pragma unroll
-      for (int j = 0; j < 4; j++) {
-	const uint32_t w[4] = {u[j].x, u[j].y, u[j].z, u[j].w};
-	#pragma unroll
-	for (int k = 0; k < 4; k++) {
-	  const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
-	  acc[2*k] += f.x;
-	  acc[2*k + 1] += f.y;
-	}
+  const int npiece = 4*g.nz;                    /* 16-byte pieces a line */
+  auto add = [&](const uint4 & u) {
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
+      acc[2*k] += f.x;
+      acc[2*k + 1] += f.y;
+    }
+  };
+  for (int l0 = blockIdx.x; l0 < nlines; l0 += 2*gridDim.x) {
+    const int l1 = l0 + gridDim.x;
+    const uint4 * a0 = (const uint4 *) (pg + (long long) prow(g, l0/g.ny,
+							       l0 % g.ny, 0)*ROWB);
+    const uint4 * a1 = (l1 < nlines)
+      ? (const uint4 *) (pg + (long long) prow(g, l1/g.ny, l1 % g.ny, 0)*ROWB)
+      : a0;
+    for (int j = threadIdx.x; j < npiece; j += 2*256) {
+      const bool two = (j + 256 < npiece);
+      uint4 u00 = a0[j], u10 = a1[j];
+      uint4 u01 = two ? a0[j + 256] : make_uint4(0u, 0u, 0u, 0u);
+      uint4 u11 = two ? a1[j + 256] : make_uint4(0u, 0u, 0u, 0u);
+      add(u00);
+      add(u01);
+      if (l1 < nlines) {
+	add(u10);
+	add(u11);
       }
     }
   }
@@ -1809,20 +1848,19 @@ __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ 
   }
 }
 
-/* 256 threads: thread (j, c) sums the partials b = j, j + 8, ... of
- * channel c, then thread c adds the eight in order j = 0 .. 7 */
+/* 32 x 32 threads: thread (c, j) sums the partials b = j, j + 32, ... of
+ * channel c, then thread (c, 0) adds the 32 sums in order j = 0 .. 31 */
 __global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
 				 float * __restrict__ db) {
-  __shared__ double red[8][32];
-  const int c = threadIdx.x & 31, j = threadIdx.x >> 5;
+  __shared__ double red[32][33];
+  const int c = threadIdx.x, j = threadIdx.y;
   double s = 0.0;
-  for (int b = j; b < nblk; b += 8) s += part[b*32 + c];
+  for (int b = j; b < nblk; b += 32) s += part[b*32 + c];
   red[j][c] = s;
   __syncthreads();
-  if (threadIdx.x < 32) {
+  if (j == 0) {
     double t = 0.0;
-    #pragma unroll
-    for (int k = 0; k < 8; k++) t += red[k][c];
+    for (int k = 0; k < 32; k++) t += red[k][c];
     db[c] = (float) t;
   }
 }
@@ -1832,7 +1870,7 @@ extern "C" int lgbk_cnn_bias_grad(const lgbk_cnn_geom_t * g, const void * pg,
   cudaStream_t s = (cudaStream_t) stream;
   k_cnn_bias_part<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, (const uint8_t *) pg,
 						       part);
-  k_cnn_bias_final<<<1, 256, 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
+  k_cnn_bias_final<<<1, dim3(32, 32), 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
   return (int) cudaGetLastError();
 }
 

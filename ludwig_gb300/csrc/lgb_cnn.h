@@ -33,7 +33,7 @@ extern "C" {
 #define LGBK_CNN_WL     (LGBK_CNN_NTAP*LGBK_CNN_C*LGBK_CNN_C)
 #define LGBK_CNN_PL     (LGBK_CNN_WL + LGBK_CNN_C)   /* params per layer */
 #define LGBK_CNN_TILE   128
-#define LGBK_CNN_RED_BLOCKS 256
+#define LGBK_CNN_RED_BLOCKS 1024
 
 typedef struct lgbk_cnn_geom_s {
   int nx, ny, nz;
@@ -63,11 +63,14 @@ int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
  * 32 x 32, 64-byte swizzle; tm_line (may be NULL; nz a multiple of 128):
  * line_kind 1: rows, box 8 x 130, no swizzle; line_kind 2: rows, box
  * 32 x 130, 64-byte swizzle (line-reuse kernel); line_kind 3 (nz = 128):
- * the kind-1 map, three z taps per MMA. */
+ * the kind-1 map, three z taps per MMA; line_kind 5: the same on the
+ * kind-2 map; line_kind 4 / 6 (nz = 128, mode LGBK_CNN_FWD_OUT, tm_w the
+ * folded weights of lgbk_cnn_wfold): the kind-1 / kind-2 map, the y taps
+ * folded into the MMAs as well. */
 /* kin: input channels read, 32 or 16 (the first layer: channels 16..31 of
  * its input rows are zero, so their products are left out); wrows: weight
  * rows (output channels) per tap in tm_w's boxes, 32, or 16 for the last
- * layer's 4 outputs where the three-tap line form runs (line_kind 3,
+ * layer's 4 outputs where a three-tap line form runs (line_kind 3 .. 6,
  * nz = 128) */
 int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int wrows,
 		  const void * tm_in,

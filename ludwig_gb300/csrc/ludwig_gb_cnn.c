@@ -264,10 +264,11 @@ int ludwig_gb_cnn_create(const int n[3], unsigned long long seed,
   }
   m->line_ok = (g.bz == LGBK_CNN_TILE && g.lpt == 1);
   /* default: three z taps per MMA where a line is the whole z extent,
-   * the last layer's y taps folded into its MMAs too (0.584 against 0.590
-   * ms per forward pass at 128^3, 0.916 with one tap per MMA), planes
-   * otherwise */
-  m->line_on = m->line_ok ? ((g.nz == LGBK_CNN_TILE) ? 4 : 1) : 0;
+   * the last layer's y taps folded into its MMAs too, on swizzled lines
+   * (one TMA box a line instead of four of 16-byte rows): 0.547 ms per
+   * forward pass at 128^3 against 0.562 on planes and 0.907 with one tap
+   * per MMA; planes otherwise */
+  m->line_on = m->line_ok ? ((g.nz == LGBK_CNN_TILE) ? 5 : 1) : 0;
   for (int l = 0; l < NL && !rc && m->line_ok; l++) {
     rc = map_lines(&m->tm_actl[l], m->act[l], g.rows, 0);
     if (!rc) rc = map_lines(&m->tm_acts[l], m->act[l], g.rows, 1);
@@ -365,22 +366,26 @@ int ludwig_gb_cnn_grads_get(ludwig_gb_cnn_t * m, float * h) {
   return rc;
 }
 
-/* line map for activation layer l (act = 1) or gradient l (act = 0) */
-static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
-  if (!m->line_on) return NULL;
-  if (m->line_on == 2) return act ? &m->tm_acts[l] : &m->tm_gs[l];
+/* line map for activation layer l (act = 1) or gradient l (act = 0) in
+ * the line form kind: swizzled rows for 2 and 5, planes otherwise */
+static const void * lmapk(ludwig_gb_cnn_t * m, int act, int l, int kind) {
+  if (!kind) return NULL;
+  if (kind == 2 || kind == 5 || kind == 6) {
+    return act ? &m->tm_acts[l] : &m->tm_gs[l];
+  }
   return act ? &m->tm_actl[l] : &m->tm_gl[l];
 }
 
 /* 1: the line-reuse convolution where the extents allow it; 2: the same
  * with swizzled line boxes; 3: the same with the three z taps of a line
  * in one MMA where nz = 128; 4: as 3, and the last layer with the y taps
- * folded into the MMA as well (3 and 4 fall back to 1 where nz != 128;
- * the default is 4 where nz = 128, else 1); 0: one box per tap */
+ * folded into the MMA as well; 5: as 4 on swizzled lines (3, 4 and 5 fall
+ * back to 1 where nz != 128; the default is 5 where nz = 128, else 1);
+ * 0: one box per tap */
 int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int mode) {
-  if (m == NULL || mode < 0 || mode > 4) {
+  if (m == NULL || mode < 0 || mode > 5) {
     return lgb_internal_err(LUDWIG_GB_EINVAL,
-			    "cnn_line_reuse: 0, 1, 2, 3 or 4");
+			    "cnn_line_reuse: 0 .. 5");
   }
   if (mode >= 3 && m->g.nz != LGBK_CNN_TILE) mode = 1;
   m->line_on = m->line_ok ? mode : 0;
@@ -390,6 +395,11 @@ int ludwig_gb_cnn_line_reuse(ludwig_gb_cnn_t * m, int mode) {
 /* the line form of the hidden layers and of every backward convolution */
 static int lkind(const ludwig_gb_cnn_t * m) {
   return (m->line_on == 4) ? 3 : m->line_on;
+}
+/* mode 5: mode 4 on swizzled lines (one TMA box a line) */
+
+static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
+  return lmapk(m, act, l, lkind(m));
 }
 
 static int check_err(ludwig_gb_cnn_t * m) {
@@ -441,11 +451,13 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
       /* the 4 outputs: 16 weight rows a tap where the three-tap form
        * runs; the folded blocks in the folded form */
       const int w16 = (m->line_on >= 3);
-      const CUtensorMap * tw = (m->line_on == 4) ? &m->tm_wfold
+      const int fold = (m->line_on == 4 || m->line_on == 5);
+      const int kl = fold ? ((m->line_on == 5) ? 6 : 4) : m->line_on;
+      const CUtensorMap * tw = fold ? &m->tm_wfold
 	: (w16 ? &m->tm_wf16 : &m->tm_wf[l]);
       rc = lgbk_cnn_conv(g, LGBK_CNN_FWD_OUT, kin_of(l),
 			 w16 ? 16 : LGBK_CNN_C, &m->tm_act[l],
-			 lmap(m, 1, l), m->line_on, tw, b, NULL, NULL,
+			 lmapk(m, 1, l, kl), kl, tw, b, NULL, NULL,
 			 NULL, out ? out : m->out4, m->err_dev, s);
     }
     if (rc) return ck(rc, "cnn conv");

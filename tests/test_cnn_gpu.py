@@ -50,7 +50,7 @@ def test_conv3_forward(gb, orc, n):
 @pytest.mark.parametrize("n", [(2, 2, 128), (8, 40, 128), (3, 5, 256),
                                (160, 17, 128)])
 @pytest.mark.parametrize("flip", [0, 1])
-@pytest.mark.parametrize("mode", [1, 2, 3])
+@pytest.mark.parametrize("mode", [1, 2, 3, 5])
 def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip, mode):
     """nz a multiple of 128: the line-reuse kernel (runs of tiles along y,
     including runs of one tile and several runs per CTA) against the
@@ -78,7 +78,7 @@ def test_conv3_line_reuse_matches_per_tap(gb, orc, n, flip, mode):
     else:
         ref = orc.conv3_fwd(n, a, w, b)
     assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
-    if mode == 3 and n[2] == 128:
+    if mode in (3, 5) and n[2] == 128:
         # the same products summed in another order
         d = (out_l - out_t).abs().max().item()
         assert d <= 1e-5 * out_t.abs().max().item(), d
@@ -136,7 +136,7 @@ def _data(rng, N):
 
 @pytest.mark.parametrize("n,mode", [((8, 8, 32), None), ((4, 4, 128), None),
                                     ((4, 4, 128), 3), ((4, 4, 128), 4),
-                                    ((3, 17, 128), 4)])
+                                    ((3, 17, 128), 4), ((3, 17, 128), 5)])
 def test_network_loss_and_gradient_vs_oracle(gb, orc, n, mode):
     """The whole network (default form, or the given line form: 3 three z
     taps per MMA, 4 the same with the last layer's y taps folded into its
@@ -363,7 +363,7 @@ def test_three_tap_forward_matches_one_tap(gb, n):
     m.set_params(p)
     x = dev(0.3 * rng.standard_normal((5, N)))
     outs = {}
-    for mode in (1, 3, 4):
+    for mode in (1, 3, 4, 5):
         m.line_reuse(mode)
         o = torch.empty((4, N), dtype=torch.float32, device="cuda")
         m.forward(x.data_ptr(), o.data_ptr())
@@ -374,6 +374,8 @@ def test_three_tap_forward_matches_one_tap(gb, n):
     # BF16 activations: its sums in another order, FP32 rounding apart
     d = (outs[4] - outs[3]).abs().max().item()
     assert d <= 1e-5 * outs[3].abs().max().item(), d
+    # 5: the hidden layers on swizzled lines, the same sums as 4
+    assert torch.equal(outs[5], outs[4])
 
 
 def test_bounded_wait_times_out_and_context_survives(gb):

@@ -233,6 +233,27 @@ struct ConvP {
 
 /* Epilogue of channels c0 .. c0+15 of one output site (x, y, z) from 16
  * accumulator columns */
+/* The backward-data epilogue of channels c0 .. c0+15 with the stored
+ * pre-activations already loaded (two 16-byte pieces of the row) */
+__device__ __forceinline__ void conv_epilogue_bwd(const ConvP & p, int x,
+						  int y, int z, int c0,
+						  const uint32_t r[16],
+						  const uint4 zq[2]) {
+  const lgbk_cnn_geom_t & g = p.g;
+  float v[16];
+  #pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const uint32_t w[4] = {zq[q].x, zq[q].y, zq[q].z, zq[q].w};
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
+      v[8*q + 2*k] = __uint_as_float(r[8*q + 2*k])*gelu_d_f(f.x);
+      v[8*q + 2*k + 1] = __uint_as_float(r[8*q + 2*k + 1])*gelu_d_f(f.y);
+    }
+  }
+  store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
+}
+
 template <int MODE>
 __device__ __forceinline__ void conv_epilogue(const ConvP & p,
 					      const float bias[16], int x,
@@ -781,6 +802,19 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
       for (int y = ya; y < yb; y++, i++) {
 	if ((i & 1) != grp) continue;
 	const int acc = grp;
+	/* backward: this site's stored pre-activations, loaded before the
+	 * accumulator is waited for */
+	uint4 zq[4];
+	if (MODE == LGBK_CNN_BWD_GELU) {
+	  const long long sq = ((long long) x*g.ny + y)*g.nz + z0 + m;
+	  const uint4 * zr = (const uint4 *) (p.zprev + sq*ROWB);
+	  zq[0] = zr[0];
+	  zq[1] = zr[1];
+	  if (two) {
+	    zq[2] = zr[2];
+	    zq[3] = zr[3];
+	  }
+	}
 	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
 				abort_flag, p.err);
 	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
@@ -868,8 +902,14 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	    }
 	  }
 	}
-	conv_epilogue<MODE>(p, bias, x, y, z0 + m, 0, r0);
-	if (two) conv_epilogue<MODE>(p, bias + 16, x, y, z0 + m, 16, r1);
+	if (MODE == LGBK_CNN_BWD_GELU) {
+	  conv_epilogue_bwd(p, x, y, z0 + m, 0, r0, zq);
+	  if (two) conv_epilogue_bwd(p, x, y, z0 + m, 16, r1, zq + 2);
+	}
+	else {
+	  conv_epilogue<MODE>(p, bias, x, y, z0 + m, 0, r0);
+	  if (two) conv_epilogue<MODE>(p, bias + 16, x, y, z0 + m, 16, r1);
+	}
       }
     }
   }
@@ -1302,8 +1342,16 @@ __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
   const int j = threadIdx.y;
   double s = 0.0;
   if (k < LGBK_CNN_WL) {
-    for (int b = j; b < nblk; b += 8) {
-      s += (double) part[(long long) b*LGBK_CNN_WL + k];
+    /* eight loads in flight, added in the order b = j, j + 8, ... */
+    for (int b0 = j; b0 < nblk; b0 += 64) {
+      float v[8];
+      #pragma unroll
+      for (int u = 0; u < 8; u++) {
+	const int b = b0 + 8*u;
+	v[u] = (b < nblk) ? part[(long long) b*LGBK_CNN_WL + k] : 0.0f;
+      }
+      #pragma unroll
+      for (int u = 0; u < 8; u++) s += (double) v[u];
     }
   }
   red[j][threadIdx.x] = s;
@@ -1733,7 +1781,9 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
   __shared__ double red[256];
   const long long N = g.nsites;
   const float rn2 = (float) (2.0/(double) N);
-  double acc = 0.0;
+  /* per-thread sums of a few sites' squares in FP32 (the FP64 pipe is a
+   * small fraction of the FP32 one here), block sums in FP64 */
+  float acc = 0.0f;
   for (long long s = (long long) blockIdx.x*blockDim.x + threadIdx.x; s < N;
        s += (long long) gridDim.x*blockDim.x) {
     const unsigned su = (unsigned) s;             /* sites < 2^31 */
@@ -1748,7 +1798,7 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
     #pragma unroll
     for (int c = 0; c < LGBK_CNN_NOUT; c++) {
       const float d = out4[c*N + s] - t4[c*N + s];
-      acc += (double) d*(double) d;
+      acc = fmaf(d, d, acc);
       v[c] = rn2*d;
     }
     const __nv_bfloat162 h0 = __floats2bfloat162_rn(v[0], v[1]);
@@ -1756,7 +1806,7 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
     *(uint4 *) (pg + (long long) prow(g, x, y, z)*ROWB) =
       make_uint4(*(const uint32_t *) &h0, *(const uint32_t *) &h1, 0u, 0u);
   }
-  red[threadIdx.x] = acc;
+  red[threadIdx.x] = (double) acc;
   __syncthreads();
   for (int w = blockDim.x/2; w > 0; w /= 2) {
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
@@ -1855,7 +1905,17 @@ __global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
   __shared__ double red[32][33];
   const int c = threadIdx.x, j = threadIdx.y;
   double s = 0.0;
-  for (int b = j; b < nblk; b += 32) s += part[b*32 + c];
+  /* eight loads in flight, added in the order b = j, j + 32, ... */
+  for (int b0 = j; b0 < nblk; b0 += 256) {
+    double v[8];
+    #pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int b = b0 + 32*u;
+      v[u] = (b < nblk) ? part[b*32 + c] : 0.0;
+    }
+    #pragma unroll
+    for (int u = 0; u < 8; u++) s += v[u];
+  }
   red[j][c] = s;
   __syncthreads();
   if (j == 0) {

@@ -1387,12 +1387,12 @@ __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
 #define WL_BANK    (WL_NY*LN_SLOT)      /* bytes per dx bank */
 #define WL_THREADS 192
 #define WL_TMEM_COLS 512
-#define WL_SMEM (1024 + 4*WL_BANK + WL_XST*TILEB + 256)
+#define WL_SMEM (1024 + 4*WL_BANK + WL_XST*LN_SLOT + 256)
 
 template <int DUMMY>
 __global__ void __launch_bounds__(WL_THREADS, 1)
 k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
-	     const __grid_constant__ CUtensorMap tm_x, const WgP p) {
+	     const __grid_constant__ CUtensorMap tm_xline, const WgP p) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = tc_smem_u32(smem_raw);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
@@ -1400,7 +1400,7 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 
   const uint32_t sL = sbase;                    /* 4 dx banks (the 4th empty) */
   const uint32_t sX = sL + 4*WL_BANK;
-  const uint32_t sBar = sX + WL_XST*TILEB;
+  const uint32_t sBar = sX + WL_XST*LN_SLOT;
   const uint32_t bFull = sBar;                  /* WL_NY */
   const uint32_t bRel = sBar + 8*WL_NY;         /* WL_NY */
   const uint32_t bXFull = sBar + 16*WL_NY;      /* WL_XST */
@@ -1435,14 +1435,14 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 
   if (warp == 0 && lane == 0) {
     tc_prefetch_map(&tm_gline);
-    tc_prefetch_map(&tm_x);
+    tc_prefetch_map(&tm_xline);
     uint32_t sq = 0, nx = 0;           /* gradient lines and x tiles loaded */
     bool ok = true;
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
       for (int y = ya; ok && y < yb; y++) {
-	/* x rows of the tile */
+	/* the x line of the tile: rows z0 - 1 .. z0 + 128 */
 	const uint32_t xs = nx % WL_XST;
 	if (nx >= WL_XST &&
 	    !tc_mbar_wait(bXEmpty + 8*xs, (nx/WL_XST - 1u) & 1u, abort_flag,
@@ -1450,9 +1450,9 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 	  ok = false;
 	  break;
 	}
-	tc_mbar_arrive_tx(bXFull + 8*xs, TILEB);
-	tc_tma_load_2d(sX + xs*TILEB, &tm_x, bXFull + 8*xs, 0,
-		       prow(g, x, y, z0));
+	tc_mbar_arrive_tx(bXFull + 8*xs, LN_ROWS*ROWB);
+	tc_tma_load_2d(sX + xs*LN_SLOT, &tm_xline, bXFull + 8*xs, 0,
+		       prow(g, x, y, z0 - 1));
 	nx++;
 	/* gradient lines y - 1 .. y + 1 (a new run) or y + 1 */
 	const bool first = (y == ya);
@@ -1483,9 +1483,12 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
     }
   }
   else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = tc_idesc_bf16(128, CNN_C, 1, 1);
+    /* N = 96: the x line's rows from z0 - 1 + dzi for dzi = 0, 1, 2, as
+     * three 32-channel atoms of the MN-major operand one row (64 bytes,
+     * the leading byte offset) apart */
+    constexpr uint32_t idesc = tc_idesc_bf16(128, 3*CNN_C, 1, 1);
     const uint64_t ad0 = tc_sdesc(sL, WL_BANK, 512, LGB_TC_SWIZZLE_64B);
-    const uint64_t bd0 = tc_sdesc(sX, TILEB, 512, LGB_TC_SWIZZLE_64B);
+    const uint64_t bd0 = tc_sdesc(sX, ROWB, 512, LGB_TC_SWIZZLE_64B);
     const uint32_t alo0 = (uint32_t) ad0, ahi = (uint32_t) (ad0 >> 32);
     const uint32_t blo0 = (uint32_t) bd0, bhi = (uint32_t) (bd0 >> 32);
     uint32_t sq = 0, nx = 0;
@@ -1506,20 +1509,16 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 	/* ring slots of the lines y - 1, y, y + 1 (dy = 1, 0, -1) */
 	const uint32_t rr[3] = {(sq - 3u) % WL_NY, (sq - 2u) % WL_NY,
 				(sq - 1u) % WL_NY};
-	const uint32_t bx = blo0 + xs*(TILEB >> 4);
+	const uint32_t bx = blo0 + xs*(LN_SLOT >> 4);
 	#pragma unroll
 	for (int j = 0; j < 3; j++) {
-	  const uint32_t aj = alo0 + rr[j]*(LN_SLOT >> 4);
+	  /* gradient rows z0 .. z0 + 127 (line row 1 on) */
+	  const uint32_t a = alo0 + rr[j]*(LN_SLOT >> 4) + (ROWB >> 4);
+	  const uint32_t d = tmem + (uint32_t) (j*3*CNN_C);
 	  #pragma unroll
-	  for (int dzi = 0; dzi < 3; dzi++) {
-	    /* z shift dz = dzi - 1: rows from 1 - dz = 2 - dzi */
-	    const uint32_t a = aj + (uint32_t) ((2 - dzi)*ROWB >> 4);
-	    const uint32_t d = tmem + (uint32_t) ((3*j + dzi)*CNN_C);
-	    #pragma unroll
-	    for (int k = 0; k < LGBK_CNN_TILE/16; k++) {
-	      tc_mma_bf16_w(d, a + k*(1024 >> 4), ahi, bx + k*(1024 >> 4), bhi,
-			    idesc, (uint32_t) ((nx | k) != 0));
-	    }
+	  for (int k = 0; k < LGBK_CNN_TILE/16; k++) {
+	    tc_mma_bf16_w(d, a + k*(1024 >> 4), ahi, bx + k*(1024 >> 4), bhi,
+			  idesc, (uint32_t) ((nx | k) != 0));
 	  }
 	}
 	tc_commit(bXEmpty + 8*xs);
@@ -1545,6 +1544,7 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 	  uint32_t r[32];
 	  tc_tmem_ld32(tmem + (uint32_t) ((3*j + dzi)*CNN_C)
 		       + ((uint32_t) (q*32) << 16), r);
+	  /* columns 96 j + 32 dzi: gradient rows z, x rows z - 1 + dzi */
 	  /* dx = 1 - q, dy = 1 - j, dz = dzi - 1 */
 	  const int t = (2 - q)*9 + (2 - j)*3 + dzi;
 	  float4 * o = (float4 *) (p.part + (((long long) blockIdx.x*CNN_NTAP
@@ -1576,8 +1576,8 @@ k_wgrad_line(const __grid_constant__ CUtensorMap tm_gline,
 
 extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
 			      const void * tm_gline, const void * tm_x,
-			      float * part, float * dw, int * err,
-			      void * stream) {
+			      const void * tm_xline, float * part, float * dw,
+			      int * err, void * stream) {
   WgP p;
   p.g = *g;
   p.part = part;
@@ -1586,14 +1586,15 @@ extern "C" int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
   cudaStream_t s = (cudaStream_t) stream;
   int grid = lgbk_cnn_wgrad_blocks(g);
   cudaError_t e;
-  if (tm_gline && g->bz == LGBK_CNN_TILE && g->lpt == 1) {
+  if (tm_gline && tm_xline && g->bz == LGBK_CNN_TILE && g->lpt == 1) {
     const CUtensorMap ml = *(const CUtensorMap *) tm_gline;
+    const CUtensorMap mxl = *(const CUtensorMap *) tm_xline;
     const int items = line_items(*g);
     if (grid > items) grid = items;
     e = cudaFuncSetAttribute(k_wgrad_line<0>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, WL_SMEM);
     if (e != cudaSuccess) return (int) e;
-    k_wgrad_line<0><<<grid, WL_THREADS, WL_SMEM, s>>>(ml, mx, p);
+    k_wgrad_line<0><<<grid, WL_THREADS, WL_SMEM, s>>>(ml, mxl, p);
   }
   else {
     const CUtensorMap mg = *(const CUtensorMap *) tm_g;

@@ -80,12 +80,14 @@ int lgbk_cnn_conv(const lgbk_cnn_geom_t * g, int mode, int kin, int wrows,
 		  int * err, void * stream);
 
 /* dW[t][n][c] = sum_s g[s - e_t][n] x[s][c]; part: wgrad_blocks*27*1024
- * floats of scratch; dw: 27*1024 floats.  tm_gline (may be NULL): the
- * gradient's line map (box 32 x 130, 64-byte swizzle); given and nz a
- * multiple of 128, the line-reuse kernel runs. */
+ * floats of scratch; dw: 27*1024 floats.  tm_gline, tm_xline (may be
+ * NULL): the gradient's and the input's line maps (box 32 x 130, 64-byte
+ * swizzle); both given and nz a multiple of 128, the line-reuse kernel
+ * runs. */
 int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
-		   const void * tm_gline, const void * tm_x, float * part,
-		   float * dw, int * err, void * stream);
+		   const void * tm_gline, const void * tm_x,
+		   const void * tm_xline, float * part, float * dw, int * err,
+		   void * stream);
 
 int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p, void * stream);
 

@@ -476,6 +476,7 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
     /* dL/dz_{l+1} is in gpad[l+1]; the layer input is act[l] */
     rc = lgbk_cnn_wgrad(g, &m->tm_g[l + 1],
 			m->line_on ? &m->tm_gs[l + 1] : NULL, &m->tm_act[l],
+			m->line_on ? &m->tm_acts[l] : NULL,
 			m->part, m->grads + l*PL, m->err_dev, s);
     if (!rc) rc = lgbk_cnn_bias_grad(g, m->gpad[l + 1], m->red,
 				     m->grads + l*PL + WL, s);
@@ -712,6 +713,7 @@ int ludwig_gb_cnn_wgrad3(ludwig_gb_cnn_t * m, const float * gr,
   if (!rc) rc = lgbk_cnn_pack_rows(&m->g, gr, m->gpad[1], s);
   if (!rc) rc = lgbk_cnn_wgrad(&m->g, &m->tm_g[1],
 			       m->line_on ? &m->tm_gs[1] : NULL, &m->tm_act[0],
+			       m->line_on ? &m->tm_acts[0] : NULL,
 			       m->part, dw, m->err_dev, s);
   if (rc) return ck(rc, "cnn_wgrad3");
   rc = check_err(m);

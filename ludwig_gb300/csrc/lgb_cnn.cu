@@ -1334,13 +1334,15 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap tm_g,
 /* dw[k] = sum over the nblk per-CTA partials, in a fixed order: a block
  * of 32 x 8 threads takes 32 consecutive k; thread (k, j) adds the
  * partials b = j, j + 8, ... (eight chains of loads in flight per k), and
- * thread (k, 0) then adds the eight chain sums in order j = 0 .. 7 */
+ * thread (k, 0) then adds the eight chain sums in order j = 0 .. 7.  FP32
+ * sums (chains of about 20 values, then 8): in FP64 this kernel was bound
+ * by the FP64 pipe, a small fraction of the FP32 one on this part. */
 __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
 			       float * __restrict__ dw) {
-  __shared__ double red[8][32];
+  __shared__ float red[8][32];
   const int k = blockIdx.x*32 + threadIdx.x;
   const int j = threadIdx.y;
-  double s = 0.0;
+  float s = 0.0f;
   if (k < LGBK_CNN_WL) {
     /* eight loads in flight, added in the order b = j, j + 8, ... */
     for (int b0 = j; b0 < nblk; b0 += 64) {
@@ -1351,16 +1353,16 @@ __global__ void k_wgrad_reduce(const float * __restrict__ part, int nblk,
 	v[u] = (b < nblk) ? part[(long long) b*LGBK_CNN_WL + k] : 0.0f;
       }
       #pragma unroll
-      for (int u = 0; u < 8; u++) s += (double) v[u];
+      for (int u = 0; u < 8; u++) s += v[u];
     }
   }
   red[j][threadIdx.x] = s;
   __syncthreads();
   if (j == 0 && k < LGBK_CNN_WL) {
-    double t = 0.0;
+    float t = 0.0f;
     #pragma unroll
     for (int q = 0; q < 8; q++) t += red[q][threadIdx.x];
-    dw[k] = (float) t;
+    dw[k] = t;
   }
 }
 
@@ -1851,7 +1853,7 @@ extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
  * t, t + 256, ... of it, always channel group t % 4 (8 channels); two
  * lines' loads are issued before either is summed. */
 __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ pg,
-				double * __restrict__ part) {
+				float * __restrict__ part) {
   __shared__ float red[256][9];
   const int cg = threadIdx.x & 3;
   float acc[8];
@@ -1893,26 +1895,27 @@ __global__ void k_cnn_bias_part(lgbk_cnn_geom_t g, const uint8_t * __restrict__ 
   __syncthreads();
   if (threadIdx.x < 32) {
     const int c = threadIdx.x;             /* channel: group c/8, entry c%8 */
-    double sum = 0.0;
-    for (int t = c/8; t < 256; t += 4) sum += (double) red[t][c % 8];
+    float sum = 0.0f;
+    for (int t = c/8; t < 256; t += 4) sum += red[t][c % 8];
     part[blockIdx.x*32 + c] = sum;
   }
 }
 
 /* 32 x 32 threads: thread (c, j) sums the partials b = j, j + 32, ... of
- * channel c, then thread (c, 0) adds the 32 sums in order j = 0 .. 31 */
-__global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
+ * channel c, then thread (c, 0) adds the 32 sums in order j = 0 .. 31
+ * (FP32 throughout: a single block of FP64 additions bounded this step) */
+__global__ void k_cnn_bias_final(const float * __restrict__ part, int nblk,
 				 float * __restrict__ db) {
-  __shared__ double red[32][33];
+  __shared__ float red[32][33];
   const int c = threadIdx.x, j = threadIdx.y;
-  double s = 0.0;
+  float s = 0.0f;
   /* eight loads in flight, added in the order b = j, j + 32, ... */
   for (int b0 = j; b0 < nblk; b0 += 256) {
-    double v[8];
+    float v[8];
     #pragma unroll
     for (int u = 0; u < 8; u++) {
       const int b = b0 + 32*u;
-      v[u] = (b < nblk) ? part[b*32 + c] : 0.0;
+      v[u] = (b < nblk) ? part[b*32 + c] : 0.0f;
     }
     #pragma unroll
     for (int u = 0; u < 8; u++) s += v[u];
@@ -1920,18 +1923,20 @@ __global__ void k_cnn_bias_final(const double * __restrict__ part, int nblk,
   red[j][c] = s;
   __syncthreads();
   if (j == 0) {
-    double t = 0.0;
+    float t = 0.0f;
     for (int k = 0; k < 32; k++) t += red[k][c];
-    db[c] = (float) t;
+    db[c] = t;
   }
 }
 
 extern "C" int lgbk_cnn_bias_grad(const lgbk_cnn_geom_t * g, const void * pg,
 				  double * part, float * db, void * stream) {
   cudaStream_t s = (cudaStream_t) stream;
+  /* float partials in the first half of the scratch */
+  float * pf = (float *) part;
   k_cnn_bias_part<<<LGBK_CNN_RED_BLOCKS, 256, 0, s>>>(*g, (const uint8_t *) pg,
-						       part);
-  k_cnn_bias_final<<<1, dim3(32, 32), 0, s>>>(part, LGBK_CNN_RED_BLOCKS, db);
+						       pf);
+  k_cnn_bias_final<<<1, dim3(32, 32), 0, s>>>(pf, LGBK_CNN_RED_BLOCKS, db);
   return (int) cudaGetLastError();
 }
 

@@ -196,6 +196,46 @@ __device__ __forceinline__ void store_half_row_bf16(uint8_t * dst,
   }
 }
 
+/* 16 values -> 16 BF16 (two 16-byte words) */
+__device__ __forceinline__ void pack_half_row_bf16(const float v[16],
+						   uint4 w[2]) {
+  #pragma unroll
+  for (int q = 0; q < 2; q++) {
+    uint32_t u[4];
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      __nv_bfloat162 h = __floats2bfloat162_rn(v[8*q + 2*k],
+					       v[8*q + 2*k + 1]);
+      u[k] = *(uint32_t *) &h;
+    }
+    w[q] = make_uint4(u[0], u[1], u[2], u[3]);
+  }
+}
+
+/* Bytes [off, off + nw*16) of site (x, y, z)'s padded row and of every
+ * periodic image of it in the halo (a site on a face of the lattice has
+ * up to seven), so that no separate halo pass is needed */
+template <int NW>
+__device__ __forceinline__ void store_row_images(const lgbk_cnn_geom_t & g,
+						 uint8_t * base, int x, int y,
+						 int z, int off,
+						 const uint4 * w) {
+  const int xb = (x == 0) ? g.nx + 1 : ((x == g.nx - 1) ? 0 : -1);
+  const int yb = (y == 0) ? g.ny + 1 : ((y == g.ny - 1) ? 0 : -1);
+  const int zb = (z == 0) ? g.nz + 1 : ((z == g.nz - 1) ? 0 : -1);
+  #pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int xp = (k & 1) ? xb : x + 1;
+    const int yp = (k & 2) ? yb : y + 1;
+    const int zp = (k & 4) ? zb : z + 1;
+    if (xp < 0 || yp < 0 || zp < 0) continue;
+    uint4 * d = (uint4 *) (base + (long long) ((xp*(g.ny + 2) + yp)
+					       *(g.nz + 2) + zp)*ROWB + off);
+    #pragma unroll
+    for (int j = 0; j < NW; j++) d[j] = w[j];
+  }
+}
+
 __device__ __forceinline__ void load_half_row_bf16(const uint8_t * src,
 						   float v[16]) {
   const uint4 * s4 = (const uint4 *) src;
@@ -251,10 +291,13 @@ __device__ __forceinline__ void conv_epilogue_bwd(const ConvP & p, int x,
       v[8*q + 2*k + 1] = __uint_as_float(r[8*q + 2*k + 1])*gelu_d_f(f.y);
     }
   }
-  store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
+  /* with the periodic images: the three-tap line form writes the halo */
+  uint4 w[2];
+  pack_half_row_bf16(v, w);
+  store_row_images<2>(g, p.pout, x, y, z, 2*c0, w);
 }
 
-template <int MODE>
+template <int MODE, bool IMG = false>
 __device__ __forceinline__ void conv_epilogue(const ConvP & p,
 					      const float bias[16], int x,
 					      int y, int z, int c0,
@@ -272,7 +315,15 @@ __device__ __forceinline__ void conv_epilogue(const ConvP & p,
     if (p.zout) store_half_row_bf16(p.zout + s*ROWB + 2*c0, v);
     #pragma unroll
     for (int n = 0; n < 16; n++) v[n] = gelu_f(v[n]);
-    store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
+    if (IMG) {
+      uint4 w[2];
+      pack_half_row_bf16(v, w);
+      store_row_images<2>(g, p.pout, x, y, z, 2*c0, w);
+    }
+    else {
+      store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0,
+			  v);
+    }
   }
   else if (MODE == LGBK_CNN_FWD_OUT) {
     if (c0 == 0) {
@@ -907,8 +958,11 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	  if (two) conv_epilogue_bwd(p, x, y, z0 + m, 16, r1, zq + 2);
 	}
 	else {
-	  conv_epilogue<MODE>(p, bias, x, y, z0 + m, 0, r0);
-	  if (two) conv_epilogue<MODE>(p, bias + 16, x, y, z0 + m, 16, r1);
+	  /* padded rows with their periodic images (no halo pass) */
+	  conv_epilogue<MODE, true>(p, bias, x, y, z0 + m, 0, r0);
+	  if (two) {
+	    conv_epilogue<MODE, true>(p, bias + 16, x, y, z0 + m, 16, r1);
+	  }
 	}
       }
     }
@@ -1729,9 +1783,16 @@ __global__ void k_cnn_features(lgbk_cnn_geom_t g, const float * __restrict__ phi
   v[2] = __fmul_rn(__fsub_rn(u[N + s], fp.off[2]), fp.scale[2]);
   v[3] = __fmul_rn(__fsub_rn(u[2*N + s], fp.off[3]), fp.scale[3]);
   v[4] = __fmul_rn(__fsub_rn(rho[s], fp.off[4]), fp.scale[4]);
-  uint8_t * row = p0 + (long long) prow(g, x, y, z)*ROWB;
-  if (full) store_row_bf16(row, v);
-  else store_half_row_bf16(row, v);
+  /* the row and its periodic images (no halo pass) */
+  uint4 w[4];
+  pack_half_row_bf16(v, w);
+  if (full) {
+    pack_half_row_bf16(v + 16, w + 2);
+    store_row_images<4>(g, p0, x, y, z, 0, w);
+  }
+  else {
+    store_row_images<2>(g, p0, x, y, z, 0, w);
+  }
 }
 
 extern "C" int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
@@ -1743,9 +1804,7 @@ extern "C" int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
   cudaStream_t s = (cudaStream_t) stream;
   k_cnn_features<<<(unsigned int) ((g->nsites + 255)/256), 256, 0, s>>>(
     *g, phi, u, rho, fp, (uint8_t *) p0, full);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return (int) e;
-  return lgbk_cnn_halo(g, p0, stream);
+  return (int) cudaGetLastError();
 }
 
 /* fp32 rows [s][32] -> padded bf16 rows (interior), then halo */
@@ -1806,8 +1865,9 @@ __global__ void k_cnn_loss_grad(lgbk_cnn_geom_t g, const float * __restrict__ ou
     }
     const __nv_bfloat162 h0 = __floats2bfloat162_rn(v[0], v[1]);
     const __nv_bfloat162 h1 = __floats2bfloat162_rn(v[2], v[3]);
-    *(uint4 *) (pg + (long long) prow(g, x, y, z)*ROWB) =
-      make_uint4(*(const uint32_t *) &h0, *(const uint32_t *) &h1, 0u, 0u);
+    const uint4 w = make_uint4(*(const uint32_t *) &h0,
+			       *(const uint32_t *) &h1, 0u, 0u);
+    store_row_images<1>(g, pg, x, y, z, 0, &w);   /* no halo pass */
   }
   red[threadIdx.x] = (double) acc;
   __syncthreads();
@@ -1842,9 +1902,7 @@ extern "C" int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
 						       (uint8_t *) pg, part);
   k_cnn_loss_final<<<1, 256, 0, s>>>(part, LGBK_CNN_RED_BLOCKS,
 				    1.0/(double) g->nsites, loss);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return (int) e;
-  return lgbk_cnn_halo(g, pg, stream);
+  return (int) cudaGetLastError();
 }
 
 /* Bias gradient: per-block channel sums of the interior rows.  Block b

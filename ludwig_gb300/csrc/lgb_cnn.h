@@ -66,7 +66,9 @@ int lgbk_cnn_wgrad_blocks(const lgbk_cnn_geom_t * g);
  * the kind-1 map, three z taps per MMA; line_kind 5: the same on the
  * kind-2 map; line_kind 4 / 6 (nz = 128, mode LGBK_CNN_FWD_OUT, tm_w the
  * folded weights of lgbk_cnn_wfold): the kind-1 / kind-2 map, the y taps
- * folded into the MMAs as well. */
+ * folded into the MMAs as well.  With line_kind 3 or 5 the modes
+ * LGBK_CNN_FWD_GELU and LGBK_CNN_BWD_GELU also write the periodic images
+ * of the rows they write (no lgbk_cnn_halo pass after them). */
 /* kin: input channels read, 32 or 16 (the first layer: channels 16..31 of
  * its input rows are zero, so their products are left out); wrows: weight
  * rows (output channels) per tap in tm_w's boxes, 32, or 16 for the last
@@ -92,14 +94,16 @@ int lgbk_cnn_wgrad(const lgbk_cnn_geom_t * g, const void * tm_g,
 int lgbk_cnn_halo(const lgbk_cnn_geom_t * g, void * p, void * stream);
 
 /* channel c < 5: (src[c][s] - off[c]) * scale[c]; others 0 (full = 0:
- * channels 5..15 only, 16..31 left as they are); then halo */
+ * channels 5..15 only, 16..31 left as they are); the periodic images in
+ * the halo written with the rows */
 int lgbk_cnn_features(const lgbk_cnn_geom_t * g, const float * phi,
 		      const float * u, const float * rho, const float off[5],
 		      const float scale[5], void * p0, int full,
 		      void * stream);
 
 /* Loss (1/N) sum (out - t)^2 over 4 channels and dL/dz_4 (bf16, padded,
- * halo filled); part: LGBK_CNN_RED_BLOCKS doubles; loss: 1 double */
+ * the periodic images written with the rows; channels 8..31 of pg must be
+ * zero and stay so); part: LGBK_CNN_RED_BLOCKS doubles; loss: 1 double */
 int lgbk_cnn_loss_grad(const lgbk_cnn_geom_t * g, const float * out4,
 		       const float * t4, void * pg, double * part,
 		       double * loss, void * stream);

@@ -402,6 +402,13 @@ static const void * lmap(ludwig_gb_cnn_t * m, int act, int l) {
   return lmapk(m, act, l, lkind(m));
 }
 
+/* the three-tap line forms write the periodic images of the padded rows
+ * themselves (no halo pass after their convolutions) */
+static int writes_images(const ludwig_gb_cnn_t * m) {
+  const int k = lkind(m);
+  return k == 3 || k == 5;
+}
+
 static int check_err(ludwig_gb_cnn_t * m) {
   cudaStream_t s = lib_stream();
   int herr = 0;
@@ -445,7 +452,7 @@ static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
 			 lmap(m, 1, l), lkind(m), &m->tm_wf[l], b, NULL,
 			 train ? m->zpre[l + 1] : NULL, m->act[l + 1], NULL,
 			 m->err_dev, s);
-      if (!rc) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
+      if (!rc && !writes_images(m)) rc = lgbk_cnn_halo(g, m->act[l + 1], s);
     }
     else {
       /* the 4 outputs: 16 weight rows a tap where the three-tap form
@@ -486,7 +493,7 @@ static int backward(ludwig_gb_cnn_t * m, const float * t4) {
 		       &m->tm_g[l + 1],
 		       lmap(m, 0, l + 1), lkind(m), &m->tm_wt[l], NULL, m->zpre[l],
 		       NULL, m->gpad[l], NULL, m->err_dev, s);
-    if (!rc) rc = lgbk_cnn_halo(g, m->gpad[l], s);
+    if (!rc && !writes_images(m)) rc = lgbk_cnn_halo(g, m->gpad[l], s);
     if (rc) return ck(rc, "cnn conv (backward)");
   }
   return LUDWIG_GB_OK;

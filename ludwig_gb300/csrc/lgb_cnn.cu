@@ -536,7 +536,9 @@ k_conv3_tc(const __grid_constant__ CUtensorMap tm_in,
 #define LN_YRUN   16
 #define LN_TXLINE (4*LN_ROWS*16)        /* bytes of one line (4 planes) */
 #define LN_XCH   4096                  /* boundary-row exchange (CYC) */
-#define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256 + LN_XCH)
+#define LN_OUTL  (3*LGBK_CNN_TILE*16)      /* FOLD: three output lines */
+#define LN_SMEM (1024 + CNN_NTAP*WTAPB + LN_NSLOT*LN_SLOT + 256 + LN_XCH \
+		 + LN_OUTL)
 
 __device__ __forceinline__ void line_item(const lgbk_cnn_geom_t & g, int it,
 					  int & x, int & z0, int & ya,
@@ -594,8 +596,10 @@ __device__ __forceinline__ void lds_ld4(uint32_t a, uint32_t v[4]) {
  * then holds, per dz, the contributions of line y' to the output lines
  * y' + 1 (dy = -1), y' and y' - 1; the epilogue combines the dz taps as in
  * the three-tap form and adds the three dy parts into three running output
- * lines kept in registers, writing line y' - 1 once line y' has been
- * added.  A run of output lines ya .. yb - 1 takes the lines ya - 1 .. yb:
+ * lines in shared memory, writing line y' - 1 once line y' has been
+ * added; the two groups of epilogue warps take alternate steps, and each
+ * step adds its parts after the previous one's (a token per step
+ * parity), so that every line is summed in step order.  A run of output lines ya .. yb - 1 takes the lines ya - 1 .. yb:
  * the same lines, in the same order, as the other forms load. */
 template <int MODE, int SWZ, int CYC, int FOLD>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
@@ -618,7 +622,9 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
   uint32_t * tslot = (uint32_t *) (sgen + (bW + 48 - sbase));
   volatile int * abort_flag = (volatile int *) (sgen + (bW + 52 - sbase));
   const uint32_t bX = bW + 56;                 /* 4: [channel half][parity] */
+  const uint32_t bTok = bW + 88;               /* FOLD: 2, [step parity] */
   const uint32_t sXch = sBar + 256;            /* [half][parity][quarter] */
+  const uint32_t sOut = sXch + LN_XCH;         /* FOLD: [3][128][4] floats */
   /* accumulator columns per tile and TMEM columns allocated */
   /* accumulator columns per tile (three taps of nb outputs each in the
    * three-tap form) and TMEM columns allocated */
@@ -640,12 +646,14 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
       tc_mbar_init(bRel + 8*k, 1);
     }
     for (int k = 0; k < 4; k++) tc_mbar_init(bX + 8*k, 8);
+    tc_mbar_init(bTok, 128);
+    tc_mbar_init(bTok + 8, 128);
     tc_mbar_init(bW, 1);
     tc_mbar_init(bTFull, 1);
     tc_mbar_init(bTFull + 8, 1);
     /* ALT: one group of four epilogue warps releases each accumulator */
-    tc_mbar_init(bTEmpty, ALT ? 128 : CONV_EPI_THREADS);
-    tc_mbar_init(bTEmpty + 8, ALT ? 128 : CONV_EPI_THREADS);
+    tc_mbar_init(bTEmpty, (ALT || FOLD) ? 128 : CONV_EPI_THREADS);
+    tc_mbar_init(bTEmpty + 8, (ALT || FOLD) ? 128 : CONV_EPI_THREADS);
     tc_mbar_init(bFin, 1);
     *abort_flag = 0;
     tc_fence_barrier_init();
@@ -967,7 +975,137 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
       }
     }
   }
-  else if (warp >= 2) {
+  else if (FOLD && warp >= 2) {
+    /* The two groups of four warps take alternate steps (y-lines).  A
+     * step's three y parts go into three running output lines in shared
+     * memory (this thread's row of each), after the previous step's parts
+     * (a token per step parity, 128 arrivals), so that every line is
+     * summed in step order; the line a step completes is written out and
+     * its slot cleared for the line three further on. */
+    const int grp = (warp - 2) >> 2;
+    const int q = warp & 3;
+    const int m = q*32 + lane;
+    float bias4[LGBK_CNN_NOUT];
+    #pragma unroll
+    for (int c = 0; c < LGBK_CNN_NOUT; c++) bias4[c] = p.bias ? p.bias[c] : 0.0f;
+    auto line_slot = [&](int ln) {
+      return sOut + (uint32_t) (((ln % 3) + 3) % 3)*(LGBK_CNN_TILE*16)
+	+ (uint32_t) m*16u;
+    };
+    if (grp == 0) {
+      /* the lines start cleared (by the group of step 0; the other group
+       * first touches them after step 0's token) */
+      const uint32_t zero[4] = {0u, 0u, 0u, 0u};
+      #pragma unroll
+      for (int k = 0; k < 3; k++) lds_st4(line_slot(k), zero);
+    }
+    int i = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
+      int x, z0, ya, yb;
+      line_item(g, it, x, z0, ya, yb);
+      for (int y = ya - 1; y <= yb; y++, i++) {
+	if ((i & 1) != grp) continue;
+	const int acc = grp;
+	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
+				abort_flag, p.err);
+	if (!__all_sync(0xffffffffu, okw)) { ok = false; break; }
+	tc_fence_after();
+	const uint32_t ta = tmem + (uint32_t) acc*NACC
+	  + ((uint32_t) (q*32) << 16);
+	uint32_t rm[16], r[16], rp[16];
+	tc_tmem_ld16_async(ta, rm);                  /* D_-1 */
+	tc_tmem_ld16_async(ta + nbk, r);             /* D_0 */
+	tc_tmem_ld16_async(ta + 2*nbk, rp);          /* D_+1 */
+	tc_tmem_wait_ld16x3(rm, r, rp);
+	tc_fence_before();
+	tc_mbar_arrive(bTEmpty + 8*acc);
+	/* edge rows: slot [group][buffer][quarter] of 128 bytes, lane 31's
+	 * D_-1 (0-63) and lane 0's D_+1 (64-127) */
+	const int xb = grp*2 + ((i >> 1) & 1);
+	const uint32_t sx = sXch + (uint32_t) (xb*4)*128u;
+	if (lane == 31) {
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) {
+	    lds_st4(sx + (uint32_t) q*128u + 16u*k, rm + 4*k);
+	  }
+	  tc_mbar_arrive(bX + 8*xb);
+	}
+	if (lane == 0) {
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) {
+	    lds_st4(sx + (uint32_t) q*128u + 64u + 16u*k, rp + 4*k);
+	  }
+	  tc_mbar_arrive(bX + 8*xb);
+	}
+	#pragma unroll
+	for (int n = 0; n < 12; n++) {
+	  float dm = __shfl_up_sync(0xffffffffu, __uint_as_float(rm[n]), 1);
+	  float dp = __shfl_down_sync(0xffffffffu, __uint_as_float(rp[n]), 1);
+	  if (lane == 0) dm = 0.0f;
+	  if (lane == 31) dp = 0.0f;
+	  r[n] = __float_as_uint((__uint_as_float(r[n]) + dm) + dp);
+	}
+	const bool okx = tc_mbar_wait(bX + 8*xb, (uint32_t) (i >> 2) & 1u,
+				      abort_flag, p.err);
+	if (!__all_sync(0xffffffffu, okx)) { ok = false; break; }
+	if (lane == 0 || lane == 31) {
+	  /* lane 0: row 32 q - 1's D_-1; lane 31: row 32 q + 32's D_+1 */
+	  const uint32_t src = (lane == 0)
+	    ? sx + (uint32_t) ((q + 3) & 3)*128u
+	    : sx + (uint32_t) ((q + 1) & 3)*128u + 64u;
+	  uint32_t ev[16];
+	  #pragma unroll
+	  for (int k = 0; k < 4; k++) lds_ld4(src + 16u*k, ev + 4*k);
+	  #pragma unroll
+	  for (int n = 0; n < 12; n++) {
+	    r[n] = __float_as_uint(__uint_as_float(r[n])
+				   + __uint_as_float(ev[n]));
+	  }
+	}
+	/* the previous step's parts are in */
+	if (i > 0) {
+	  const bool okt = tc_mbar_wait(bTok + 8*((i - 1) & 1),
+					(uint32_t) ((i - 1) >> 1) & 1u,
+					abort_flag, p.err);
+	  if (!__all_sync(0xffffffffu, okt)) { ok = false; break; }
+	}
+	/* column 4 dyi + c: the part of output line y + 1 - dyi */
+	#pragma unroll
+	for (int dyi = 0; dyi < 3; dyi++) {
+	  const uint32_t a = line_slot(y + 1 - dyi);
+	  uint32_t v[4];
+	  lds_ld4(a, v);
+	  #pragma unroll
+	  for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	    v[c] = __float_as_uint(__uint_as_float(v[c])
+				   + __uint_as_float(r[4*dyi + c]));
+	  }
+	  if (dyi < 2) lds_st4(a, v);
+	  else if (y - 1 >= ya) {
+	    /* line y - 1 is complete */
+	    const long long sy = ((long long) x*g.ny + (y - 1))*g.nz + z0 + m;
+	    #pragma unroll
+	    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
+	      p.outf[c*g.nsites + sy] = __uint_as_float(v[c]) + bias4[c];
+	    }
+	  }
+	}
+	{
+	  /* clear the completed line's slot; after the run's last step the
+	   * two lines past the run as well */
+	  const uint32_t zero[4] = {0u, 0u, 0u, 0u};
+	  lds_st4(line_slot(y - 1), zero);
+	  if (y == yb) {
+	    lds_st4(line_slot(y), zero);
+	    lds_st4(line_slot(y + 1), zero);
+	  }
+	}
+	tc_mbar_arrive(bTok + 8*(i & 1));
+      }
+    }
+  }
+  else if (!FOLD && warp >= 2) {
     /* warp w reads TMEM lanes 32*(w % 4) .. +31, columns c0 .. c0+15 */
     const int q = warp & 3;
     const int m = q*32 + lane;
@@ -980,12 +1118,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
     for (int it = blockIdx.x; ok && it < nitems; it += gridDim.x) {
       int x, z0, ya, yb;
       line_item(g, it, x, z0, ya, yb);
-      /* FOLD: the output lines y - 1, y, y + 1 of this thread's site */
-      float o0[LGBK_CNN_NOUT], o1[LGBK_CNN_NOUT], o2[LGBK_CNN_NOUT];
-      #pragma unroll
-      for (int c = 0; c < LGBK_CNN_NOUT; c++) o0[c] = o1[c] = o2[c] = 0.0f;
-      /* FOLD: y runs over the lines ya - 1 .. yb, else the outputs */
-      for (int y = ya - FOLD; y < yb + FOLD; y++, i++) {
+      for (int y = ya; y < yb; y++, i++) {
 	const int acc = i & 1;
 	bool okw = tc_mbar_wait(bTFull + 8*acc, (uint32_t) (i >> 1) & 1u,
 				abort_flag, p.err);
@@ -1064,31 +1197,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
 	  tc_fence_before();
 	  tc_mbar_arrive(bTEmpty + 8*acc);
 	}
-	if (FOLD) {
-	  /* column 4 dyi + c: the part of output line y + 1 - dyi */
-	  #pragma unroll
-	  for (int c = 0; c < LGBK_CNN_NOUT; c++) {
-	    o2[c] += __uint_as_float(r[c]);
-	    o1[c] += __uint_as_float(r[4 + c]);
-	    o0[c] += __uint_as_float(r[8 + c]);
-	  }
-	  if (y - 1 >= ya) {
-	    const long long sy = ((long long) x*g.ny + (y - 1))*g.nz + z0 + m;
-	    #pragma unroll
-	    for (int c = 0; c < LGBK_CNN_NOUT; c++) {
-	      p.outf[c*g.nsites + sy] = o0[c] + bias[c];
-	    }
-	  }
-	  #pragma unroll
-	  for (int c = 0; c < LGBK_CNN_NOUT; c++) {
-	    o0[c] = o1[c];
-	    o1[c] = o2[c];
-	    o2[c] = 0.0f;
-	  }
-	}
-	else {
-	  conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
-	}
+	conv_epilogue<MODE>(p, bias, x, y, z0 + m, c0, r);
       }
     }
   }

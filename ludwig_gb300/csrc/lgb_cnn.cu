@@ -585,9 +585,15 @@ __device__ __forceinline__ void lds_ld4(uint32_t a, uint32_t v[4]) {
  * .. + 31, and the output is out(r) = D_-1[r - 1] + D_0[r] + D_+1[r + 1]
  * with r - 1, r + 1 taken modulo 128: the epilogue moves the two shifted
  * terms one TMEM lane with warp shuffles, and across the four warps of a
- * channel half through shared memory (an mbarrier per channel half and
- * tile parity, bounded waits).  Sums in another order than the one-box-per-tap kernel: equal to
- * FP32 rounding, not bit for bit. */
+ * group through shared memory (16-byte accesses, an mbarrier per group
+ * and buffer, bounded waits).  The two groups of four epilogue warps take
+ * alternate tiles (the accumulator parity), each warp both channel
+ * halves, and write the periodic images of the rows they store (no halo
+ * pass).  Sums in another order than the one-box-per-tap kernel: equal to
+ * FP32 rounding, not bit for bit.
+ *
+ * The ring also runs on 64-byte-swizzled lines (SWZ = 1: one TMA box a
+ * line instead of four boxes of 16-byte rows), the default form. */
 /* FOLD = 1 (the last layer, 4 outputs, with CYC): the y taps go into N
  * as well.  Each step takes one new y-line (x-1, x, x+1 at y') and issues
  * one MMA per dx and K half with B = the 48 rows [dz][dy][4 outputs] (12

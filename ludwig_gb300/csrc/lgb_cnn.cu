@@ -138,13 +138,16 @@ __device__ __forceinline__ float gelu_f(float z) {
   return __fdividef(z, 1.0f + __expf(-v));
 }
 
-/* d/dz z sigma(2u) = s + z s (1 - s) d(2u)/dz, s = sigma(2u) */
-__device__ __forceinline__ float gelu_d_f(float z) {
-  const float z2 = z*z;
-  const float v = fmaxf(GELU_K0*z*fmaf(GELU_K1, z2, 1.0f), -80.0f);
-  const float s = __fdividef(1.0f, 1.0f + __expf(-v));
-  const float dv = GELU_K0*fmaf(3.0f*GELU_K1, z2, 1.0f);
-  return fmaf(z*s*(1.0f - s), dv, s);
+/* GELU(z) and its slope d/dz z sigma(2u) = s + z s (1 - s) d(2u)/dz,
+ * s = sigma(2u), from one exponential: the forward pass of training keeps
+ * the slope for the backward pass */
+__device__ __forceinline__ float gelu_and_slope(float z, float & d) {
+  const float v = fmaxf(GELU_K0*z*fmaf(GELU_K1*z, z, 1.0f), -80.0f);
+  const float e = 1.0f + __expf(-v);
+  const float s = __fdividef(1.0f, e);
+  const float dv = GELU_K0*fmaf(3.0f*GELU_K1*z, z, 1.0f);
+  d = fmaf(z*s*(1.0f - s), dv, s);
+  return __fdividef(z, e);                /* as gelu_f */
 }
 
 __device__ __forceinline__ void store_row_bf16(uint8_t * dst,
@@ -274,7 +277,7 @@ struct ConvP {
 /* Epilogue of channels c0 .. c0+15 of one output site (x, y, z) from 16
  * accumulator columns */
 /* The backward-data epilogue of channels c0 .. c0+15 with the stored
- * pre-activations already loaded (two 16-byte pieces of the row) */
+ * slopes GELU'(z) already loaded (two 16-byte pieces of the row) */
 __device__ __forceinline__ void conv_epilogue_bwd(const ConvP & p, int x,
 						  int y, int z, int c0,
 						  const uint32_t r[16],
@@ -287,8 +290,8 @@ __device__ __forceinline__ void conv_epilogue_bwd(const ConvP & p, int x,
     #pragma unroll
     for (int k = 0; k < 4; k++) {
       const float2 f = __bfloat1622float2(*(const __nv_bfloat162 *) &w[k]);
-      v[8*q + 2*k] = __uint_as_float(r[8*q + 2*k])*gelu_d_f(f.x);
-      v[8*q + 2*k + 1] = __uint_as_float(r[8*q + 2*k + 1])*gelu_d_f(f.y);
+      v[8*q + 2*k] = __uint_as_float(r[8*q + 2*k])*f.x;
+      v[8*q + 2*k + 1] = __uint_as_float(r[8*q + 2*k + 1])*f.y;
     }
   }
   /* with the periodic images: the three-tap line form writes the halo */
@@ -311,10 +314,17 @@ __device__ __forceinline__ void conv_epilogue(const ConvP & p,
   if (MODE == LGBK_CNN_FWD_GELU) {
     #pragma unroll
     for (int n = 0; n < 16; n++) v[n] += bias[n];
-    /* pre-activation, kept for a backward pass (training only) */
-    if (p.zout) store_half_row_bf16(p.zout + s*ROWB + 2*c0, v);
-    #pragma unroll
-    for (int n = 0; n < 16; n++) v[n] = gelu_f(v[n]);
+    if (p.zout) {
+      /* training: the slopes GELU'(z), kept for the backward pass */
+      float d[16];
+      #pragma unroll
+      for (int n = 0; n < 16; n++) v[n] = gelu_and_slope(v[n], d[n]);
+      store_half_row_bf16(p.zout + s*ROWB + 2*c0, d);
+    }
+    else {
+      #pragma unroll
+      for (int n = 0; n < 16; n++) v[n] = gelu_f(v[n]);
+    }
     if (IMG) {
       uint4 w[2];
       pack_half_row_bf16(v, w);
@@ -334,10 +344,11 @@ __device__ __forceinline__ void conv_epilogue(const ConvP & p,
     }
   }
   else if (MODE == LGBK_CNN_BWD_GELU) {
+    /* the slopes GELU'(z) the forward pass kept */
     float zp[16];
     load_half_row_bf16(p.zprev + s*ROWB + 2*c0, zp);
     #pragma unroll
-    for (int n = 0; n < 16; n++) v[n] *= gelu_d_f(zp[n]);
+    for (int n = 0; n < 16; n++) v[n] *= zp[n];
     store_half_row_bf16(p.pout + (long long) prow(g, x, y, z)*ROWB + 2*c0, v);
   }
   else {
@@ -867,7 +878,7 @@ k_conv3_line(const __grid_constant__ CUtensorMap tm_line,
       for (int y = ya; y < yb; y++, i++) {
 	if ((i & 1) != grp) continue;
 	const int acc = grp;
-	/* backward: this site's stored pre-activations, loaded before the
+	/* backward: this site's stored slopes GELU'(z), loaded before the
 	 * accumulator is waited for */
 	uint4 zq[4];
 	if (MODE == LGBK_CNN_BWD_GELU) {

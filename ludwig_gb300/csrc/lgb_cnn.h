@@ -45,9 +45,10 @@ typedef struct lgbk_cnn_geom_s {
 } lgbk_cnn_geom_t;
 
 enum lgbk_cnn_mode {
-  LGBK_CNN_FWD_GELU = 0,      /* z = acc + b -> zout (bf16), GELU(z) -> pout */
+  LGBK_CNN_FWD_GELU = 0,      /* z = acc + b: GELU(z) -> pout, GELU'(z) ->
+				 zout (bf16; when zout is not NULL) */
   LGBK_CNN_FWD_OUT  = 1,      /* acc + b, channels 0..3 -> outf[c][s] fp32 */
-  LGBK_CNN_BWD_GELU = 2,      /* acc * GELU'(zprev) -> pout */
+  LGBK_CNN_BWD_GELU = 2,      /* acc * zprev (the stored GELU'(z)) -> pout */
   LGBK_CNN_RAW      = 3       /* acc + b (b may be NULL) -> outf[s][32] fp32 */
 };
 

@@ -58,7 +58,7 @@ struct ludwig_gb_cnn_s {
   void * wt[NL];
   void * wfold;                /* bf16 [9][32][32] */
   void * act[NL];
-  void * zpre[NL];             /* bf16 [N][32], index 1..3 */
+  void * zpre[NL];             /* bf16 [N][32] GELU'(z), index 1..3 */
   void * gpad[NL + 1];         /* index 1..4 */
   float * out4;                /* [4][N] */
   float * part;                /* wgrad partial sums */
@@ -432,8 +432,8 @@ static int kin_of(int l) {
 }
 
 /* a_0 from [phi, u, rho] pointers, then the four layers -> out (m->out4
- * when NULL); the pre-activations z (for the backward pass) are stored
- * only when train */
+ * when NULL); the slopes GELU'(z) of the hidden layers (for the backward
+ * pass) are stored only when train */
 static int forward(ludwig_gb_cnn_t * m, const float * phi, const float * u,
 		   const float * rho, int train, float * out) {
   cudaStream_t s = lib_stream();

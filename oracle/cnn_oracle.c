@@ -17,9 +17,10 @@
  *
  *  With emulate = 1 every quantity the device stores in bf16 is rounded
  *  to bf16 (round to nearest even) at the same point: weights, features,
- *  activations a_l, pre-activations z_l (the backward pass evaluates
- *  GELU' at the rounded z_l), and the gradients dL/dz_l.  The output z_4
- *  and the loss stay unrounded (the device keeps them in fp32).
+ *  activations a_l, the slopes GELU'(z_l) that the forward pass keeps for
+ *  the backward pass (evaluated at the unrounded z_l), and the gradients
+ *  dL/dz_l.  The output z_4 and the loss stay unrounded (the device keeps
+ *  them in fp32).
  *
  *****************************************************************************/
 
@@ -152,7 +153,8 @@ static void features(const int n[3], int emulate, const float * in5,
   }
 }
 
-/* Runs the network; optionally keeps the activations and pre-activations.
+/* Runs the network; optionally keeps the activations and the slopes
+ * GELU'(z) of the hidden layers.
  * W: [4][27][32][32] float; b: [4][32] float; out4: [4][N] double. */
 static int cnn_forward_keep(const int n[3], int emulate, const float * in5,
 			    const float * scale, const float * W,
@@ -177,7 +179,7 @@ static int cnn_forward_keep(const int n[3], int emulate, const float * in5,
     }
     if (l < ORC_CNN_NLAYER - 1) {
       for (long long k = 0; k < NC; k++) {
-	pre[l + 1][k] = rnd(emulate, z[k]);
+	pre[l + 1][k] = rnd(emulate, gelu_d(z[k]));
 	act[l + 1][k] = rnd(emulate, gelu(z[k]));
       }
     }
@@ -266,7 +268,7 @@ int orc_cnn_loss_grad(const int n[3], int emulate, const float * in5,
     for (long long k = 0; k < NC; k++) {
       double v = ga[k];
       if (emulate) v = (double) (float) v;
-      g[k] = rnd(emulate, v*gelu_d(pre[l][k]));
+      g[k] = rnd(emulate, v*pre[l][k]);
     }
   }
 

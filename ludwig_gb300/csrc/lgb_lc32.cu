@@ -38,6 +38,22 @@ static int launch_collide(const lgbk_dims_t * d, const lgbk_lc_step_args_t * a,
   return (int) cudaGetLastError();
 }
 
+/* Force + collision without a plane ring (all-fluid lattices) */
+#define LC32_DTY 4
+#define LC32_DMINB 4
+
+template <typename S>
+static int launch_collide_direct(const lgbk_dims_t * d,
+				 const lgbk_lc_step_args_t * a,
+				 cudaStream_t s) {
+  const dim3 grid((unsigned int) (((d->nz + 31)/32)
+				  *((d->ny + LC32_DTY - 1)/LC32_DTY)),
+		  (unsigned int) d->nx);
+  k_lc32_collide_direct<S, LC32_DTY, LC32_DMINB><<<grid, dim3(32, LC32_DTY),
+    0, s>>>(*d, *a);
+  return (int) cudaGetLastError();
+}
+
 /* The same with two sites per thread (tiles of 2 TYT rows) */
 template <typename S, int TYT, int MINB>
 static int launch_collide2(const lgbk_dims_t * d,
@@ -113,7 +129,8 @@ static int lc_step32(const lgbk_dims_t * d, const lgbk_lc_t * p,
    * kernels are the faster (0.161 against 0.171 ms per LC step with the
    * two-site collision, FP32) */
   if (a->sites == 2) return launch_collide2<S, 4, 3>(d, a, s);
-  return launch_collide<S, false>(d, a, s);
+  if (a->sites == 1) return launch_collide<S, false>(d, a, s);
+  return launch_collide_direct<S>(d, a, s);
 }
 
 extern "C" int lgbk_lc_step(const lgbk_dims_t * d, int prec,

@@ -229,6 +229,85 @@ k_lc32_fields_be(lgbk_dims_t d, lgbk_lc_f_t p, lgbk_lc_step_args_t a) {
   for (int n = 0; n < 5; n++) (qo + n*N)[i] = qnew[n];
 }
 
+/* Force + collision without a plane ring (all-fluid lattices): one site
+ * per thread on a (z tiles x y tiles, nx) grid; the stress neighbours
+ * come through L1 like the fields kernel's Q neighbours, so that no
+ * barrier separates the planes. */
+template <typename S, int TY, int MINB>
+__global__ void __launch_bounds__(32*TY, MINB)
+k_lc32_collide_direct(lgbk_dims_t d, lgbk_lc_step_args_t a) {
+  const int ntz = (d.nz + 31)/32;
+  const int z = (blockIdx.x % ntz)*32 + threadIdx.x;
+  const int y = (blockIdx.x / ntz)*TY + threadIdx.y;
+  const int x = blockIdx.y;
+  if (z >= d.nz || y >= d.ny) return;
+  const long long N = d.nsites;
+  const int NP = d.ny*d.nz;
+  const unsigned s0 = (unsigned) x*NP + y*d.nz + z;
+  const unsigned xw = (unsigned) (d.nx - 1)*NP;
+  /* neighbours: x+1, x-1, y+1, y-1, z+1, z-1 */
+  const unsigned sxp = (x == d.nx - 1) ? s0 - xw : s0 + NP;
+  const unsigned sxm = (x == 0) ? s0 + xw : s0 - NP;
+  const unsigned syp = s0 + ((y == d.ny - 1) ? -(d.ny - 1)*d.nz : d.nz);
+  const unsigned sym = s0 + ((y == 0) ? (d.ny - 1)*d.nz : -d.nz);
+  const unsigned szp = s0 + ((z == d.nz - 1) ? -(d.nz - 1) : 1);
+  const unsigned szm = s0 + ((z == 0) ? d.nz - 1 : -1);
+  const float * __restrict__ pth = (const float *) a.pth;
+  const S * __restrict__ f_in = (const S *) a.f_in;
+  S * __restrict__ f_out = (S *) a.f_out;
+  float * __restrict__ u_out = (float *) a.u_out;
+  float * __restrict__ rho_out = (float *) a.rho_out;
+  const float rho0 = a.fp[LGBK_LCF_RHO0];
+  const float fscale = a.fp[LGBK_LCF_FSCALE];
+  const float rfscale = a.fp[LGBK_LCF_RFSCALE];
+
+  /* pulled populations f_p(x - c_p) */
+  const int oxp = (x == 0) ? (d.nx - 1)*NP : -NP;
+  const int oxm = (x == d.nx - 1) ? -(d.nx - 1)*NP : NP;
+  const int oyp = (y == 0) ? (d.ny - 1)*d.nz : -d.nz;
+  const int oym = (y == d.ny - 1) ? -(d.ny - 1)*d.nz : d.nz;
+  const int ozp = (z == 0) ? d.nz - 1 : -1;
+  const int ozm = (z == d.nz - 1) ? -(d.nz - 1) : 1;
+  float fs[LGB_NVEL];
+  const S * fb = f_in + s0;
+  Unroll<LGB_NVEL>::run([&](auto P) {
+    constexpr int pp = decltype(P)::value;
+    int off = 0;
+    if (Cv<pp>::X == +1) off += oxp;
+    if (Cv<pp>::X == -1) off += oxm;
+    if (Cv<pp>::Y == +1) off += oyp;
+    if (Cv<pp>::Y == -1) off += oym;
+    if (Cv<pp>::Z == +1) off += ozp;
+    if (Cv<pp>::Z == -1) off += ozm;
+    fs[pp] = FStore<S, float>::ld(fb + pp*N + off, rfscale);
+  });
+
+  /* minus the divergence of the face values 0.5 (P(s) + P(s + e)); the
+   * own-site halves cancel */
+  float ftot[3];
+  #pragma unroll
+  for (int ia = 0; ia < 3; ia++) {
+    const float * Px = pth + (3*ia + 0)*N;
+    const float * Py = pth + (3*ia + 1)*N;
+    const float * Pz = pth + (3*ia + 2)*N;
+    const float force = 0.5f*((Px[sxm] - Px[sxp]) + (Py[sym] - Py[syp])
+			      + (Pz[szm] - Pz[szp]));
+    ftot[ia] = a.fp[LGBK_LCF_FX + ia] + force;
+  }
+  float rho, uu[3];
+  lgb_collide_site<float, false, true, true>(
+    a.fp[LGBK_LCF_RTAU_SHEAR], a.fp[LGBK_LCF_RTAU_BULK],
+    a.cp.rtau_ghost, rho0, fs, ftot, rho, uu);
+  rho_out[s0] = rho;
+  S * ob = f_out + s0;
+  #pragma unroll
+  for (int pp = 0; pp < LGB_NVEL; pp++) {
+    FStore<S, float>::st(ob + pp*N, fs[pp], fscale);
+  }
+  #pragma unroll
+  for (int ia = 0; ia < 3; ia++) u_out[ia*N + s0] = uu[ia];
+}
+
 /* A plane of P in shared memory: 9 components x (TY + 2) rows of RZ
  * floats; the 32 interior z values of a row start at float 4 (16-byte
  * aligned, so that they arrive as 16-byte copies), the z halo sits at

@@ -158,7 +158,32 @@ def _one_step_close(gb, solid, precision):
         assert err < tol * scale, (k, err, scale)
 
 
-@pytest.mark.parametrize("sites", [0, 2])
+@pytest.mark.parametrize("precision", [1, 2])
+@pytest.mark.parametrize("L", [(16, 12, 40), (11, 9, 37), (8, 8, 64),
+                               (3, 5, 7)])
+def test_lc_collide_direct_matches_ring(gb, L, precision):
+    """The float LC force + collision kernel that reads the stress
+    neighbours through L1 (the default on all-fluid lattices) against the
+    one that streams stress planes through a shared-memory ring (asked for
+    by tune_sites(1)): the same arithmetic on the same values."""
+    out = {}
+    for sites in (1, 0):
+        gb.tune_sites(sites)
+        try:
+            s = gb.LiquidCrystal(L, eta=0.5, gamma_rot=0.5,
+                                 precision=precision)
+            s.init_o8m()
+            s.step(10)
+            out[sites] = s.state()
+        finally:
+            gb.tune_sites(0)
+    for k in ("q", "u", "f", "rho"):
+        scale = np.abs(out[1][k]).max()
+        err = np.abs(out[0][k] - out[1][k]).max()
+        assert err <= 1e-6 * scale, (k, err, scale)
+
+
+@pytest.mark.parametrize("sites", [0, 1, 2])
 def test_lc_fp32_ragged_lattice_close_to_fp64(gb, sites):
     """The float LC kernels on extents that are no multiple of the tile or
     of 4 (P planes copied element by element; with two sites a thread, an

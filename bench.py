@@ -70,11 +70,11 @@ DROPIN_BYTES = {"dropin_binary64": 872, "dropin_lc64": 1768,
 
 # DRAM bytes (read + write) per site of the fused kernels, from one ncu
 # capture each (binary fluid at 160^3, cholesteric at 128^3; the fused
-# float LC step is two kernels, 32.5 + 34.0 + 114.8 + 72.5); a streaming
+# float LC step is two kernels, 32.5 + 35.0 + 112.2 + 72.0); a streaming
 # kernel's traffic grows in proportion to the sites, so traffic =
 # bytes/site x sites.
 NCU_BYTES_PER_SITE = {"fp32": 179.8, "fp64": 370.5, "fp16": 103.4,
-                      "lc32": 253.8}
+                      "lc32": 251.7}
 
 # Corrector FLOPs per coarse site and forward pass (3x3x3 convolutions):
 # executed as 4 layers of 32 x 32 channels, 2*27*32*32 each; useful are
@@ -100,8 +100,9 @@ LIMITER = {"fp32": "hbm (traffic = compulsory bytes; issue 65% busy)",
            "lc64": "fp64 pipe",
            "lb2_64": "fp64 pipe (two collisions a site, --fmad=false)",
            "lc32": "two kernels: fields + Beris-Edwards (issue and load "
-                   "latency), force + collision (HBM, 2.5-D); the stress "
-                   "(9 values a site) crosses HBM between them"}
+                   "latency), force + collision (HBM: stress neighbours "
+                   "through L1, 91% of the measured copy bandwidth); the "
+                   "stress (9 values a site) crosses HBM between them"}
 
 
 def env_int(name, default):

@@ -618,8 +618,11 @@ int ludwig_gb_tune_set(int xchunk, int tile_y, int min_blocks);
  * the next plane loaded while the current one is computed; the tile then
  * has tile_y rows in tile_y/2 thread rows), 1, or 0 (the default: the
  * faster form of each on GB300: 2 for the binary fluid with FP16 storage,
- * 1 for it in FP32 and for the cholesteric's force + collision kernel).
- * A status map with solid sites always uses 1. */
+ * 1 for it in FP32; for the cholesteric, one site a thread with the
+ * force + collision kernel reading the stress neighbours through L1,
+ * where 1 asks for the one that streams stress planes through a
+ * shared-memory ring).  A status map with solid sites always uses the
+ * one-site ring forms. */
 int ludwig_gb_tune_sites(int sites_per_thread);
 
 /*---------------------------------------------------------------------------

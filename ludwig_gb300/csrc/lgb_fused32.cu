@@ -257,10 +257,11 @@ template <typename S>
 __global__ void k_to_store(long long nsites, int ncomp, double rho0,
 			   double scale, const double * __restrict__ src,
 			   S * __restrict__ dst) {
-  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  long long n = nsites*ncomp;
-  if (i >= n) return;
-  int p = (int) (i / nsites);
+  /* component p = blockIdx.y: no division to find it */
+  const long long k = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (k >= nsites) return;
+  const int p = (int) blockIdx.y;
+  const long long i = (long long) p*nsites + k;
   double v = src[i];
   if (ncomp == LGB_NVEL) v -= lgb_w(p)*rho0;
   FStore<S, double>::st(dst + i, v, scale);
@@ -270,10 +271,10 @@ template <typename S>
 __global__ void k_from_store(long long nsites, int ncomp, double rho0,
 			     double scale, const S * __restrict__ src,
 			     double * __restrict__ dst) {
-  long long i = (long long) blockIdx.x*blockDim.x + threadIdx.x;
-  long long n = nsites*ncomp;
-  if (i >= n) return;
-  int p = (int) (i / nsites);
+  const long long k = (long long) blockIdx.x*blockDim.x + threadIdx.x;
+  if (k >= nsites) return;
+  const int p = (int) blockIdx.y;
+  const long long i = (long long) p*nsites + k;
   double v = FStore<S, double>::ld(src + i, 1.0/scale);
   if (ncomp == LGB_NVEL) v += lgb_w(p)*rho0;
   dst[i] = v;
@@ -299,6 +300,10 @@ __global__ void k_propagate_store(lgbk_dims_t d, int dir,
 }
 
 static dim3 g256(long long n) { return dim3((unsigned int) ((n + 255)/256)); }
+/* blocks of 256 sites x one component each */
+static dim3 g256c(long long nsites, int ncomp) {
+  return dim3((unsigned int) ((nsites + 255)/256), (unsigned int) ncomp);
+}
 
 extern "C" int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,
 				 double shift_rho0, double scale,
@@ -310,11 +315,11 @@ extern "C" int lgbk_f64_to_store(const lgbk_dims_t * d, int prec, int ncomp,
 				 cudaMemcpyDeviceToDevice, s);
   }
   if (prec == LGBK_PREC_FP16 && ncomp == LGB_NVEL) {
-    k_to_store<__half><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+    k_to_store<__half><<<g256c(d->nsites, ncomp), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
 					       scale, src, (__half *) dst);
   }
   else {
-    k_to_store<float><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+    k_to_store<float><<<g256c(d->nsites, ncomp), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
 					      1.0, src, (float *) dst);
   }
   return (int) cudaGetLastError();
@@ -330,12 +335,12 @@ extern "C" int lgbk_store_to_f64(const lgbk_dims_t * d, int prec, int ncomp,
 				 cudaMemcpyDeviceToDevice, s);
   }
   if (prec == LGBK_PREC_FP16 && ncomp == LGB_NVEL) {
-    k_from_store<__half><<<g256(n), 256, 0, s>>>(d->nsites, ncomp,
+    k_from_store<__half><<<g256c(d->nsites, ncomp), 256, 0, s>>>(d->nsites, ncomp,
 						 shift_rho0, scale,
 						 (const __half *) src, dst);
   }
   else {
-    k_from_store<float><<<g256(n), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
+    k_from_store<float><<<g256c(d->nsites, ncomp), 256, 0, s>>>(d->nsites, ncomp, shift_rho0,
 						1.0, (const float *) src, dst);
   }
   return (int) cudaGetLastError();
